@@ -1,0 +1,313 @@
+/*
+ * mrt_cuda.h -- the C ABI of the GB300 (sm_103a) ray-tracing device layer.
+ *
+ * This replaces the Vulkan device layer of MinoteRT (src/sys/vulkan.ixx plus
+ * the vuk render graph) on the ray-tracing hot path.  The renderer keeps the
+ * pass structure of src/gfx/modules/pathtracer.ixx:
+ *
+ *   Pathtracer::primaryRays   (pathtracer.ixx:29-116)  -> mrt_cuda_primary_rays
+ *   Pathtracer::secondaryRays (pathtracer.ixx:118-195) -> mrt_cuda_secondary_rays
+ *
+ * and the device work those passes dispatched (src/gpu/primaryRay.comp,
+ * src/gpu/secondaryRays.comp) runs as hand-written CUDA kernels.
+ *
+ * Conventions
+ *   - Every entry point returns MRT_OK (0) or a negative MRT_E* code; nothing
+ *     throws across the ABI.  mrt_cuda_last_error() gives a message.
+ *   - Device pointers are plain pointers obtained from mrt_cuda_alloc (or any
+ *     other CUDA allocation on the context's device).  Streams are passed as
+ *     `void*` holding a cudaStream_t (NULL = the legacy default stream).
+ *   - All work is stream-ordered; only mrt_cuda_sync / mrt_cuda_status /
+ *     the *_host entry points synchronise.
+ *   - A context is used from one host thread at a time; many contexts may
+ *     coexist.
+ *   - Matrices are column-major float[16] (GLSL / minote.math layout,
+ *     src/stx/math.ixx): m[col*4 + row].
+ */
+#ifndef MRT_CUDA_H
+#define MRT_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MRT_ABI_VERSION 1
+
+/* ---- return codes ------------------------------------------------------ */
+enum {
+    MRT_OK       = 0,
+    MRT_EINVAL   = -1, /* bad argument (null pointer, size, enum)            */
+    MRT_ECUDA    = -2, /* a CUDA runtime call failed                          */
+    MRT_ENOMEM   = -3, /* device or host allocation failed                   */
+    MRT_ETIMEOUT = -4, /* mrt_cuda_sync wall-clock limit expired             */
+    MRT_EDEVICE  = -5, /* a kernel raised a device status flag (see below)   */
+    MRT_ESTATE   = -6, /* call made in the wrong state (e.g. no blue noise)  */
+    MRT_ERANGE   = -7  /* size beyond a documented maximum                   */
+};
+
+/* ---- device status flags (mrt_cuda_status) ----------------------------- */
+#define MRT_STATUS_ITER_CAP  0x01u /* a traversal hit its iteration cap      */
+#define MRT_STATUS_STACK_OVF 0x02u /* traversal stack overflow               */
+#define MRT_STATUS_BAD_NODE  0x04u /* child node index out of range          */
+#define MRT_STATUS_BAD_TRI   0x08u /* triangle index out of range            */
+#define MRT_STATUS_QUEUE_OVF 0x10u /* a wavefront queue overflowed           */
+#define MRT_STATUS_BAD_SCENE 0x20u /* batched launch: scene index invalid    */
+
+/* ---- scene data formats ------------------------------------------------ */
+
+/* One node of the compressed 8-wide BVH (quantised child boxes), 128 bytes,
+ * 128-byte aligned so a node is exactly one L2 line; the first 80 bytes are
+ * read by traversal.  Child slot i covers the box
+ *     lo = origin + q_lo[i] * 2^exp,  hi = origin + q_hi[i] * 2^exp
+ * per axis.  meta[i] == 0: empty slot.  imask bit i: slot i is an internal
+ * node; its index is child_base + popcount(imask & ((1<<i)-1)).  Otherwise
+ * slot i is a leaf: meta[i] >> 5 is a unary triangle count (1, 3 or 7 for
+ * 1..3 triangles) and meta[i] & 31 the first triangle's offset from
+ * tri_base.  Internal slots carry meta = 0x20 | (24 + i).
+ * The reference has no BVH (it loops over 5 spheres, primaryRay.comp:26-32);
+ * this format is new. */
+typedef struct mrt_bvh8_node {
+    float    origin[3];
+    int8_t   exp[3];
+    uint8_t  imask;
+    uint32_t child_base;
+    uint32_t tri_base;
+    uint8_t  meta[8];
+    uint8_t  q_lo_x[8], q_lo_y[8], q_lo_z[8];
+    uint8_t  q_hi_x[8], q_hi_y[8], q_hi_z[8];
+    uint32_t reserved[12];
+} mrt_bvh8_node;
+
+/* A triangle in BVH leaf order, 48 bytes: three vertices, each padded to
+ * 16 bytes; `id` is the triangle's index in the caller's original mesh. */
+typedef struct mrt_tri {
+    float v0[3]; uint32_t id;
+    float v1[3]; uint32_t pad1;
+    float v2[3]; uint32_t pad2;
+} mrt_tri;
+
+/* Per-original-triangle shading record, 16 bytes: unit geometric normal
+ * (winding v0,v1,v2) and albedo as RGBA8 UNORM (albedo = byte / 255). */
+typedef struct mrt_material {
+    float    normal[3];
+    uint32_t albedo_rgba8;
+} mrt_material;
+
+/* Analytic sphere, the primitive of the reference's scene
+ * (intersect.glsl:9-13, scene.glsl:4-11). */
+typedef struct mrt_sphere {
+    float center[3];
+    float radius;
+    float albedo[3];
+    float pad;
+} mrt_sphere;
+
+/* Generic ray, 32 bytes: a hit is accepted for tmin < t < tmax. */
+typedef struct mrt_ray {
+    float org[3]; float tmin;
+    float dir[3]; float tmax;
+} mrt_ray;
+
+/* Closest/any hit, 8 bytes.  prim = original triangle id (or sphere index),
+ * 0xFFFFFFFF on a miss.  Ties at equal t resolve to the lower prim id. */
+typedef struct mrt_hit {
+    uint32_t prim;
+    float    t;
+} mrt_hit;
+
+#define MRT_MISS 0xFFFFFFFFu
+
+/* Per-dispatch camera constants: the union of the two reference UBOs
+ * (primaryRay.comp:14-21 and secondaryRays.comp:25-32).  Host fill as in
+ * pathtracer.ixx:86-105 / 171-184. */
+typedef struct mrt_camera_consts {
+    float    view[16];
+    float    projection[16];
+    float    inv_view[16];
+    float    inv_projection[16];
+    float    prev_view[16];
+    float    camera_pos[3];
+    uint32_t frame_counter;
+} mrt_camera_consts;
+
+/* The g-buffer of Pathtracer::GBuffer (pathtracer.ixx:22-27).  Device
+ * pointers to width*height texels, row-major, row 0 = top of the image
+ * (the shader's gl_GlobalInvocationID.y = 0).  Formats follow the reference
+ * (pathtracer.ixx:42-69): visibility R32_UINT, depth R16F (NDC z of the
+ * inverted infinite projection), normal RGBA16F (w = 0), motion RG16F.
+ * hit_t (FP32 closest-hit distance) is new; the triangle path reads it
+ * instead of reconstructing the hit from FP16 depth.  Any pointer but
+ * visibility may be NULL to skip that output. */
+typedef struct mrt_gbuffer {
+    uint32_t* visibility;
+    float*    hit_t;
+    uint16_t* depth;
+    uint16_t* normal;
+    uint16_t* motion;
+    uint32_t  width;
+    uint32_t  height;
+} mrt_gbuffer;
+
+/* RNG modes */
+#define MRT_RNG_REFERENCE 0u /* seed=(frame<<1)|1 for every pixel, decorrelated
+                                only by the blue-noise Cranley-Patterson
+                                rotation (secondaryRays.comp:124-125)        */
+#define MRT_RNG_PER_PIXEL 1u /* seed also hashed with the pixel index        */
+
+/* Estimators */
+#define MRT_EST_ESCAPE 0u /* reference: light only from the sky on escape,
+                             zero if the path runs out of bounces
+                             (secondaryRays.comp:64-100)                     */
+#define MRT_EST_NEE    1u /* plus one shadow ray per vertex toward a
+                             directional light (new; no reference code)     */
+
+typedef struct mrt_trace_params {
+    uint32_t samples;      /* paths per pixel in this call (reference: 8)   */
+    uint32_t max_bounces;  /* diffuse bounces after the primary hit
+                              (reference: 8)                                 */
+    uint32_t rr_start;     /* Russian roulette for bounces > rr_start;
+                              0 = off                                        */
+    uint32_t rng_mode;     /* MRT_RNG_*                                      */
+    uint32_t estimator;    /* MRT_EST_*                                      */
+    uint32_t accumulate;   /* 0: write this call's mean; 1: fold it into the
+                              running mean with weight 1/(frame_index+1)     */
+    uint32_t frame_index;  /* frames already in the running mean             */
+    uint32_t sort_rays;    /* 1: sort extension rays between bounces         */
+    float    sun_dir[3];   /* unit vector toward the directional light       */
+    float    pad0;
+    float    sun_irradiance[3];
+    float    pad1;
+    float    sky_radiance[3]; /* constant radiance of escaping rays          */
+    float    pad2;
+} mrt_trace_params;
+
+/* Per-frame statistics of the last mrt_cuda_secondary_rays call, filled when
+ * timing is enabled (mrt_cuda_set_timing). */
+#define MRT_MAX_BOUNCES 16
+typedef struct mrt_frame_stats {
+    uint64_t primary_rays;
+    uint64_t extension_rays[MRT_MAX_BOUNCES]; /* rays traced at bounce b+1   */
+    uint64_t shadow_rays;
+    float    ms_primary;     /* primary closest-hit kernel                   */
+    float    ms_extend;      /* all extension (closest-hit) kernels          */
+    float    ms_extend_b[MRT_MAX_BOUNCES];
+    float    ms_shadow;      /* all shadow (any-hit) kernels                 */
+    float    ms_shade;       /* shade + ray generation kernels               */
+    float    ms_sort;        /* ray sort kernels                             */
+    float    ms_total;       /* whole secondary pass                         */
+    uint32_t launches;       /* kernels launched by the pass                 */
+    uint32_t pad;
+} mrt_frame_stats;
+
+typedef struct mrt_ctx   mrt_ctx;
+typedef struct mrt_scene mrt_scene;
+
+/* ---- context ----------------------------------------------------------- */
+/* Replaces the Vulkan service (src/sys/vulkan.ixx:426, Vulkan_impl ctor
+ * :106-115): selects `device` and creates the per-context device state. */
+int         mrt_cuda_create(mrt_ctx** out, int device);
+int         mrt_cuda_destroy(mrt_ctx* ctx);
+const char* mrt_cuda_last_error(const mrt_ctx* ctx);
+int         mrt_cuda_abi_version(void);
+/* Reads (and with clear != 0 resets) the device status word; synchronises
+ * the context.  Returns MRT_OK; *flags holds MRT_STATUS_* bits. */
+int mrt_cuda_status(mrt_ctx* ctx, uint32_t* flags, int clear);
+/* Waits for `stream` with a wall-clock limit (polling cudaStreamQuery);
+ * MRT_ETIMEOUT when it expires.  timeout_s <= 0: no limit. */
+int mrt_cuda_sync(mrt_ctx* ctx, void* stream, double timeout_s);
+/* Enables per-kernel CUDA-event timing into mrt_frame_stats. */
+int mrt_cuda_set_timing(mrt_ctx* ctx, int enable);
+int mrt_cuda_frame_stats(mrt_ctx* ctx, mrt_frame_stats* out);
+
+/* ---- memory and streams (the reference's vuk allocator role,
+ *      renderer.ixx:42-43) --------------------------------------------- */
+int mrt_cuda_alloc(mrt_ctx* ctx, size_t bytes, void** dptr);
+int mrt_cuda_free(mrt_ctx* ctx, void* dptr);
+int mrt_cuda_host_alloc(mrt_ctx* ctx, size_t bytes, void** hptr); /* pinned */
+int mrt_cuda_host_free(mrt_ctx* ctx, void* hptr);
+int mrt_cuda_copy_h2d(mrt_ctx* ctx, void* dst, const void* src, size_t bytes, void* stream);
+int mrt_cuda_copy_d2h(mrt_ctx* ctx, void* dst, const void* src, size_t bytes, void* stream);
+int mrt_cuda_copy_d2d(mrt_ctx* ctx, void* dst, const void* src, size_t bytes, void* stream);
+int mrt_cuda_memset(mrt_ctx* ctx, void* dst, int value, size_t bytes, void* stream);
+int mrt_cuda_stream_create(mrt_ctx* ctx, void** stream);
+int mrt_cuda_stream_destroy(mrt_ctx* ctx, void* stream);
+int mrt_cuda_event_create(mrt_ctx* ctx, void** event);
+int mrt_cuda_event_destroy(mrt_ctx* ctx, void* event);
+int mrt_cuda_event_record(mrt_ctx* ctx, void* event, void* stream);
+int mrt_cuda_event_elapsed(mrt_ctx* ctx, void* start, void* stop, float* ms);
+
+/* ---- scenes ------------------------------------------------------------ */
+/* Uploads a host-built BVH8 (see mrt_host.h, mrt_bvh8_build) with its
+ * leaf-ordered triangles and per-original-triangle materials; the library
+ * owns the device copy.  Replaces the reference's compile-time scene
+ * constant (scene.glsl:4-11). */
+int mrt_cuda_scene_upload_triangles(mrt_ctx* ctx,
+                                    const mrt_bvh8_node* nodes, uint32_t node_count,
+                                    const mrt_tri* tris, uint32_t tri_count,
+                                    const mrt_material* materials, uint32_t material_count,
+                                    mrt_scene** out);
+/* Uploads an analytic sphere list (the reference's own scene 0 form). */
+int mrt_cuda_scene_upload_spheres(mrt_ctx* ctx, const mrt_sphere* spheres,
+                                  uint32_t count, mrt_scene** out);
+int mrt_cuda_scene_destroy(mrt_ctx* ctx, mrt_scene* scene);
+
+/* Blue-noise texture upload (renderer.ixx:101-110 decodes an RGBA8 PNG and
+ * creates an R8G8B8A8_UNORM texture).  Channels R,G become the per-pixel
+ * Cranley-Patterson rotation, fetched at (x % w, y % h)
+ * (secondaryRays.comp:125).  w, h <= 1024. */
+int mrt_cuda_blue_noise_upload(mrt_ctx* ctx, const uint8_t* rgba, uint32_t w, uint32_t h);
+
+/* ---- passes ------------------------------------------------------------ */
+/* Primary rays: one pinhole ray per pixel from inv_view/inv_projection
+ * (primaryRay.comp:46-51), closest hit, g-buffer stores (primaryRay.comp:
+ * 60-75).  Replaces Pathtracer::primaryRays (pathtracer.ixx:29-116). */
+int mrt_cuda_primary_rays(mrt_ctx* ctx, const mrt_scene* scene,
+                          const mrt_camera_consts* consts,
+                          const mrt_gbuffer* gbuffer, void* stream);
+
+/* Secondary rays: per pixel, `samples` paths of up to `max_bounces`
+ * cosine-weighted diffuse bounces from the primary hit in the g-buffer,
+ * throughput times albedo, sky (and for MRT_EST_NEE the directional light)
+ * as light, mean written or accumulated to `color` (device, float RGB,
+ * width*height*3).  Replaces Pathtracer::secondaryRays
+ * (pathtracer.ixx:118-195) and secondaryRays.comp:102-135.  Triangle scenes
+ * run as a wavefront (extend / shade / shadow kernels with compaction
+ * between bounces); sphere scenes run the reference's per-pixel loop. */
+int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene,
+                            const mrt_gbuffer* gbuffer,
+                            const mrt_camera_consts* consts,
+                            const mrt_trace_params* params,
+                            float* color, void* stream);
+
+/* Generic closest-hit (flags = 0) or any-hit (MRT_TRACE_ANY_HIT) query for
+ * `count` rays in device memory; hits written to device memory. */
+#define MRT_TRACE_ANY_HIT 0x1u
+int mrt_cuda_trace_rays(mrt_ctx* ctx, const mrt_scene* scene,
+                        const mrt_ray* rays, uint32_t count, mrt_hit* hits,
+                        uint32_t flags, void* stream);
+
+/* Per-ray traversal counters for the roofline (nodes and triangles visited,
+ * closest-hit): device arrays of `count` uint32 each. */
+int mrt_cuda_trace_rays_counted(mrt_ctx* ctx, const mrt_scene* scene,
+                                const mrt_ray* rays, uint32_t count, mrt_hit* hits,
+                                uint32_t* nodes_visited, uint32_t* tris_visited,
+                                void* stream);
+
+/* One whole frame through HOST buffers: primary + secondary passes on
+ * library-owned device buffers, then copies of visibility, hit_t (may be
+ * NULL) and color (float RGB) back to the host.  Synchronises `stream`. */
+int mrt_cuda_render_frame_host(mrt_ctx* ctx, const mrt_scene* scene,
+                               const mrt_camera_consts* consts,
+                               const mrt_trace_params* params,
+                               uint32_t width, uint32_t height,
+                               uint32_t* visibility, float* hit_t, float* color,
+                               void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MRT_CUDA_H */

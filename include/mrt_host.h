@@ -1,0 +1,117 @@
+/*
+ * mrt_host.h -- host-side C++ modules of the renderer, exported as C.
+ *
+ * These are the CPU parts that stay on the host in MinoteRT and that the
+ * device layer (mrt_cuda.h) consumes:
+ *   - camera math: Camera::view / Camera::projection (src/gfx/camera.ixx:
+ *     26-44) over look / perspective / inverse (src/stx/math.ixx:739-861),
+ *     and the per-dispatch constant fill of pathtracer.ixx:86-105, 171-184;
+ *   - the acceleration structure: an SAH BVH2 collapsed to the quantised
+ *     BVH8 of mrt_cuda.h (new: the reference has no BVH);
+ *   - procedural scenes from a seed (new: the reference's scene is a
+ *     5-sphere constant, scene.glsl:4-11, returned by mrt_scene_reference);
+ *   - a blue-noise tile generator (void-and-cluster) standing in for the
+ *     reference's assets/blue_noise.png (renderer.ixx:101-110).
+ * All entry points return MRT_OK or a negative MRT_E* code.
+ */
+#ifndef MRT_HOST_H
+#define MRT_HOST_H
+
+#include "mrt_cuda.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* The reference's Camera (camera.ixx:10-26), without the movement speeds. */
+typedef struct mrt_camera {
+    uint32_t viewport[2];  /* width, height                                  */
+    float    vertical_fov; /* radians                                        */
+    float    near_plane;
+    float    position[3];
+    float    yaw;          /* radians; direction = (cp*cy, cp*sy, sp)        */
+    float    pitch;
+} mrt_camera;
+
+/* view = look(position, direction(), +Z)        (camera.ixx:32-35)
+ * projection = perspective(fov, h/w, near)      (camera.ixx:38-41) */
+void mrt_camera_view(const mrt_camera* cam, float out[16]);
+void mrt_camera_projection(const mrt_camera* cam, float out[16]);
+/* 4x4 inverse by cofactors (math.ixx:739-820). */
+void mrt_mat4_inverse(const float m[16], float out[16]);
+/* Fills mrt_camera_consts as pathtracer.ixx:86-105 and :171-184 do. */
+void mrt_camera_consts_make(const mrt_camera* cam, const mrt_camera* prev_cam,
+                            uint32_t frame_counter, mrt_camera_consts* out);
+
+/* ---- triangle meshes ------------------------------------------------- */
+typedef struct mrt_mesh {
+    float*        verts;     /* tri_count * 9 floats: v0 v1 v2 per triangle  */
+    mrt_material* materials; /* tri_count records                            */
+    uint32_t      tri_count;
+    uint32_t      pad;
+    float         bounds_lo[3];
+    float         bounds_hi[3];
+} mrt_mesh;
+
+void mrt_mesh_free(mrt_mesh* mesh);
+
+/* Heightfield + boxes: a grid x grid cell heightfield (z = sum of 4 sine
+ * octaves with seeded phases and frequencies; 2*grid^2 triangles) plus
+ * `boxes` axis-aligned boxes with edge lengths U[0.5, 3] (12 triangles
+ * each) resting on it; albedo U[0.2, 0.8] per object. */
+int mrt_scene_heightfield_boxes(uint64_t seed, uint32_t grid, uint32_t boxes,
+                                mrt_mesh* out);
+
+/* Icosphere field: `spheres` icospheres subdivided `levels` times
+ * (20*4^levels triangles each), radius log-uniform[rmin, rmax], vertices
+ * displaced along the normal by seeded Perlin noise of amplitude
+ * 0.05 * radius, over a ground plane of >= ground_tris triangles. */
+int mrt_scene_icospheres(uint64_t seed, uint32_t spheres, uint32_t levels,
+                         float rmin, float rmax, uint32_t ground_tris,
+                         mrt_mesh* out);
+
+/* Number of triangles of a heightfield whose triangle count is close to
+ * `target` (used by the batched scene mix). */
+uint32_t mrt_heightfield_grid_for(uint32_t target_tris);
+
+/* ---- BVH ------------------------------------------------------------- */
+typedef struct mrt_bvh_build_params {
+    uint32_t sah_bins;       /* binned SAH bins (default 32)                 */
+    uint32_t max_leaf_tris;  /* <= 3                                         */
+    uint32_t threads;        /* 0 = hardware concurrency                     */
+    uint32_t pad;
+} mrt_bvh_build_params;
+
+typedef struct mrt_bvh8 {
+    mrt_bvh8_node* nodes;
+    mrt_tri*       tris;
+    uint32_t       node_count;
+    uint32_t       tri_count;
+    uint32_t       depth;       /* BVH8 levels, root = 1                     */
+    uint32_t       leaf_count;
+    double         build_ms;
+    double         sah_cost;
+} mrt_bvh8;
+
+/* Binned SAH BVH2 over the triangles, collapsed into 8-wide nodes with
+ * octant-ordered child slots and conservative 8-bit quantised boxes. */
+int  mrt_bvh8_build(const float* verts, uint32_t tri_count,
+                    const mrt_bvh_build_params* params, mrt_bvh8* out);
+void mrt_bvh8_free(mrt_bvh8* bvh);
+
+/* ---- reference scene 0 ---------------------------------------------- */
+/* The 5 spheres of src/gpu/scene.glsl:4-11 (km units). */
+uint32_t mrt_scene_reference(mrt_sphere* out /* [5] */);
+/* The reference's default camera (app.ixx:20-32) at a given viewport. */
+void mrt_camera_reference(uint32_t width, uint32_t height, mrt_camera* out);
+
+/* ---- blue noise ------------------------------------------------------ */
+/* size x size RGBA8 blue-noise tile by void-and-cluster (Ulichney 1993),
+ * one independent rank map per channel, seeded. size <= 256. */
+int mrt_blue_noise_generate(uint32_t seed, uint32_t size, uint8_t* rgba_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MRT_HOST_H */

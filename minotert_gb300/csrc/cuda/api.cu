@@ -1,0 +1,612 @@
+// The mrt_cuda_* C ABI: context, memory, scene upload and the two renderer
+// passes.  Replaces the Vulkan device layer (src/sys/vulkan.ixx) and the vuk
+// dispatches of src/gfx/modules/pathtracer.ixx on the ray-tracing path.
+#include "internal.hpp"
+
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <thread>
+
+using namespace mrt;
+
+namespace {
+
+int fail(mrt_ctx* ctx, int code, const char* fmt, ...) {
+    if (ctx) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        std::vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        ctx->err = buf;
+    }
+    return code;
+}
+
+#define MRT_CK(call)                                                                                   \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess) return fail(ctx, MRT_ECUDA, "%s: %s", #call, cudaGetErrorString(e_));  \
+    } while (0)
+
+inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+// minote.math mat * mat (math.ixx:680-697): column c of the result is
+// ((L0*R[c][0] + L1*R[c][1]) + L2*R[c][2]) + L3*R[c][3], no contraction.
+void matmul4(const float* l, const float* r, float* out) {
+    for (int c = 0; c < 4; ++c)
+        for (int row = 0; row < 4; ++row) {
+            float acc = l[0 * 4 + row] * r[c * 4 + 0];
+            acc = acc + l[1 * 4 + row] * r[c * 4 + 1];
+            acc = acc + l[2 * 4 + row] * r[c * 4 + 2];
+            acc = acc + l[3 * 4 + row] * r[c * 4 + 3];
+            out[c * 4 + row] = acc;
+        }
+}
+
+FrameParams frame_params(const mrt_camera_consts* c, uint32_t w, uint32_t h) {
+    FrameParams fp;
+    std::memset(&fp, 0, sizeof(fp));
+    fp.c = *c;
+    matmul4(c->projection, c->view, fp.pv);
+    matmul4(c->projection, c->prev_view, fp.ppv);
+    fp.width = w;
+    fp.height = h;
+    fp.pitch_x = 1.0f / float(w); // OutPitch = vec2(1) / vec2(OutBounds)
+    fp.pitch_y = 1.0f / float(h);
+    return fp;
+}
+
+TraceParams trace_params(const mrt_trace_params* p) {
+    TraceParams t;
+    t.samples = p->samples;
+    t.max_bounces = p->max_bounces;
+    t.rr_start = p->rr_start;
+    t.rng_mode = p->rng_mode;
+    t.estimator = p->estimator;
+    for (int k = 0; k < 3; ++k) {
+        t.sun[k] = p->sun_dir[k];
+        t.sun_e[k] = p->sun_irradiance[k];
+        t.sky[k] = p->sky_radiance[k];
+    }
+    return t;
+}
+
+cudaEvent_t get_event(mrt_ctx* ctx) {
+    if (!ctx->ev_pool.empty()) {
+        cudaEvent_t e = ctx->ev_pool.back();
+        ctx->ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+struct Scope {
+    mrt_ctx* ctx;
+    cudaStream_t s;
+    int kind, bounce;
+    cudaEvent_t a = nullptr;
+    Scope(mrt_ctx* c, cudaStream_t st, int k, int b) : ctx(c), s(st), kind(k), bounce(b) {
+        if (ctx->timing) {
+            a = get_event(ctx);
+            cudaEventRecord(a, s);
+        }
+    }
+    ~Scope() {
+        if (ctx->timing && a) {
+            cudaEvent_t b = get_event(ctx);
+            cudaEventRecord(b, s);
+            ctx->recs.push_back(mrt_timing_rec{kind, bounce, a, b});
+        }
+    }
+};
+
+void free_wave(WaveBuffers& wb) {
+    cudaFree(wb.q[0]); cudaFree(wb.q[1]); cudaFree(wb.hits); cudaFree(wb.sq); cudaFree(wb.L);
+    cudaFree(wb.rng); cudaFree(wb.counters); cudaFree(wb.totals); cudaFree(wb.keys); cudaFree(wb.perm);
+    cudaFree(wb.qsort); cudaFree(wb.hist);
+    wb = WaveBuffers();
+}
+
+int ensure_wave(mrt_ctx* ctx, size_t npix) {
+    WaveBuffers& wb = ctx->wb;
+    if (wb.cap >= npix && wb.counters) {
+        wb.npix = npix;
+        return MRT_OK;
+    }
+    unsigned long long* totals = wb.totals;
+    wb.totals = nullptr;
+    free_wave(wb);
+    size_t cap = npix;
+    bool ok = cudaMalloc(&wb.q[0], cap * sizeof(PathRay)) == cudaSuccess &&
+              cudaMalloc(&wb.q[1], cap * sizeof(PathRay)) == cudaSuccess &&
+              cudaMalloc(&wb.hits, cap * sizeof(uint2)) == cudaSuccess &&
+              cudaMalloc(&wb.sq, cap * sizeof(ShadowRay)) == cudaSuccess &&
+              cudaMalloc(&wb.L, npix * sizeof(float4)) == cudaSuccess &&
+              cudaMalloc(&wb.rng, npix * sizeof(uint32_t)) == cudaSuccess &&
+              cudaMalloc(&wb.counters, kCntSlots * sizeof(uint32_t)) == cudaSuccess;
+    if (ok && !totals) ok = cudaMalloc(&totals, 64 * sizeof(unsigned long long)) == cudaSuccess &&
+                            cudaMemset(totals, 0, 64 * sizeof(unsigned long long)) == cudaSuccess;
+    wb.totals = totals;
+    if (!ok) {
+        free_wave(wb);
+        return fail(ctx, MRT_ENOMEM, "wavefront buffers for %zu rays: out of device memory", npix);
+    }
+    wb.cap = cap;
+    wb.npix = npix;
+    return MRT_OK;
+}
+
+int check_gbuffer(mrt_ctx* ctx, const mrt_gbuffer* g) {
+    if (!g || !g->visibility) return fail(ctx, MRT_EINVAL, "gbuffer.visibility is NULL");
+    if (g->width == 0 || g->height == 0) return fail(ctx, MRT_EINVAL, "gbuffer has zero size");
+    if (uint64_t(g->width) * g->height > (1ull << 28)) return fail(ctx, MRT_ERANGE, "gbuffer larger than 2^28 pixels");
+    return MRT_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int mrt_cuda_abi_version(void) { return MRT_ABI_VERSION; }
+
+const char* mrt_cuda_last_error(const mrt_ctx* ctx) {
+    if (!ctx) return "null context";
+    return ctx->err.c_str();
+}
+
+int mrt_cuda_create(mrt_ctx** out, int device) {
+    if (!out) return MRT_EINVAL;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return MRT_ECUDA;
+    if (device < 0 || device >= n) return MRT_EINVAL;
+    if (cudaSetDevice(device) != cudaSuccess) return MRT_ECUDA;
+    mrt_ctx* ctx = new (std::nothrow) mrt_ctx;
+    if (!ctx) return MRT_ENOMEM;
+    ctx->device = device;
+    cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (cudaMalloc(&ctx->d_status, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMemset(ctx->d_status, 0, sizeof(uint32_t)) != cudaSuccess) {
+        delete ctx;
+        return MRT_ENOMEM;
+    }
+    *out = ctx;
+    return MRT_OK;
+}
+
+int mrt_cuda_destroy(mrt_ctx* ctx) {
+    if (!ctx) return MRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    free_wave(ctx->wb);
+    cudaFree(ctx->d_status);
+    cudaFree(ctx->d_bn);
+    cudaFree(ctx->d_vis);
+    cudaFree(ctx->d_aux);
+    cudaFree(ctx->d_t);
+    cudaFree(ctx->d_color);
+    for (auto& r : ctx->recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+    for (auto e : ctx->ev_pool) cudaEventDestroy(e);
+    delete ctx;
+    return MRT_OK;
+}
+
+int mrt_cuda_status(mrt_ctx* ctx, uint32_t* flags, int clear) {
+    if (!ctx || !flags) return MRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    MRT_CK(cudaDeviceSynchronize());
+    MRT_CK(cudaMemcpy(flags, ctx->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (clear) MRT_CK(cudaMemset(ctx->d_status, 0, sizeof(uint32_t)));
+    return MRT_OK;
+}
+
+int mrt_cuda_sync(mrt_ctx* ctx, void* stream, double timeout_s) {
+    if (!ctx) return MRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    auto t0 = std::chrono::steady_clock::now();
+    while (true) {
+        cudaError_t e = cudaStreamQuery(as_stream(stream));
+        if (e == cudaSuccess) return MRT_OK;
+        if (e != cudaErrorNotReady) return fail(ctx, MRT_ECUDA, "stream query: %s", cudaGetErrorString(e));
+        double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (timeout_s > 0.0 && el > timeout_s)
+            return fail(ctx, MRT_ETIMEOUT, "stream not finished after %.3f s", timeout_s);
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+}
+
+int mrt_cuda_set_timing(mrt_ctx* ctx, int enable) {
+    if (!ctx) return MRT_EINVAL;
+    ctx->timing = enable != 0;
+    return MRT_OK;
+}
+
+int mrt_cuda_frame_stats(mrt_ctx* ctx, mrt_frame_stats* out) {
+    if (!ctx || !out) return MRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    MRT_CK(cudaDeviceSynchronize());
+    mrt_frame_stats st = ctx->acc;
+    for (auto& r : ctx->recs) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, r.a, r.b);
+        switch (r.kind) {
+        case 0: st.ms_primary += ms; break;
+        case 1:
+            st.ms_extend += ms;
+            if (r.bounce >= 1 && r.bounce <= MRT_MAX_BOUNCES) st.ms_extend_b[r.bounce - 1] += ms;
+            break;
+        case 2: st.ms_shadow += ms; break;
+        case 3: st.ms_shade += ms; break;
+        case 4: st.ms_sort += ms; break;
+        case 5: st.ms_total += ms; break;
+        default: break;
+        }
+        ctx->ev_pool.push_back(r.a);
+        ctx->ev_pool.push_back(r.b);
+    }
+    ctx->recs.clear();
+    if (ctx->wb.totals) {
+        unsigned long long tot[64];
+        MRT_CK(cudaMemcpy(tot, ctx->wb.totals, sizeof(tot), cudaMemcpyDeviceToHost));
+        MRT_CK(cudaMemset(ctx->wb.totals, 0, sizeof(tot)));
+        for (int b = 1; b <= MRT_MAX_BOUNCES; ++b) st.extension_rays[b - 1] += tot[kCntExt + b];
+        for (int v = 0; v <= MRT_MAX_BOUNCES; ++v) st.shadow_rays += tot[kCntShadow + v];
+    }
+    st.launches = ctx->launches;
+    *out = st;
+    ctx->acc = mrt_frame_stats{};
+    ctx->launches = 0;
+    return MRT_OK;
+}
+
+// ---- memory ---------------------------------------------------------------
+
+int mrt_cuda_alloc(mrt_ctx* ctx, size_t bytes, void** dptr) {
+    if (!ctx || !dptr) return MRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    *dptr = nullptr;
+    if (bytes == 0) return MRT_OK;
+    if (cudaMalloc(dptr, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, MRT_ENOMEM, "cudaMalloc(%zu) failed", bytes);
+    }
+    return MRT_OK;
+}
+
+int mrt_cuda_free(mrt_ctx* ctx, void* dptr) {
+    if (!ctx) return MRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    MRT_CK(cudaFree(dptr));
+    return MRT_OK;
+}
+
+int mrt_cuda_host_alloc(mrt_ctx* ctx, size_t bytes, void** hptr) {
+    if (!ctx || !hptr) return MRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    if (cudaMallocHost(hptr, bytes ? bytes : 1) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, MRT_ENOMEM, "cudaMallocHost(%zu) failed", bytes);
+    }
+    return MRT_OK;
+}
+
+int mrt_cuda_host_free(mrt_ctx* ctx, void* hptr) {
+    if (!ctx) return MRT_EINVAL;
+    MRT_CK(cudaFreeHost(hptr));
+    return MRT_OK;
+}
+
+int mrt_cuda_copy_h2d(mrt_ctx* ctx, void* dst, const void* src, size_t bytes, void* stream) {
+    if (!ctx || (bytes && (!dst || !src))) return MRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    MRT_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, as_stream(stream)));
+    return MRT_OK;
+}
+
+int mrt_cuda_copy_d2h(mrt_ctx* ctx, void* dst, const void* src, size_t bytes, void* stream) {
+    if (!ctx || (bytes && (!dst || !src))) return MRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    MRT_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, as_stream(stream)));
+    return MRT_OK;
+}
+
+int mrt_cuda_copy_d2d(mrt_ctx* ctx, void* dst, const void* src, size_t bytes, void* stream) {
+    if (!ctx || (bytes && (!dst || !src))) return MRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    MRT_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, as_stream(stream)));
+    return MRT_OK;
+}
+
+int mrt_cuda_memset(mrt_ctx* ctx, void* dst, int value, size_t bytes, void* stream) {
+    if (!ctx || (bytes && !dst)) return MRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    MRT_CK(cudaMemsetAsync(dst, value, bytes, as_stream(stream)));
+    return MRT_OK;
+}
+
+int mrt_cuda_stream_create(mrt_ctx* ctx, void** stream) {
+    if (!ctx || !stream) return MRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    cudaStream_t s;
+    MRT_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    *stream = s;
+    return MRT_OK;
+}
+
+int mrt_cuda_stream_destroy(mrt_ctx* ctx, void* stream) {
+    if (!ctx) return MRT_EINVAL;
+    MRT_CK(cudaStreamDestroy(as_stream(stream)));
+    return MRT_OK;
+}
+
+int mrt_cuda_event_create(mrt_ctx* ctx, void** event) {
+    if (!ctx || !event) return MRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    cudaEvent_t e;
+    MRT_CK(cudaEventCreate(&e));
+    *event = e;
+    return MRT_OK;
+}
+
+int mrt_cuda_event_destroy(mrt_ctx* ctx, void* event) {
+    if (!ctx) return MRT_EINVAL;
+    MRT_CK(cudaEventDestroy(static_cast<cudaEvent_t>(event)));
+    return MRT_OK;
+}
+
+int mrt_cuda_event_record(mrt_ctx* ctx, void* event, void* stream) {
+    if (!ctx || !event) return MRT_EINVAL;
+    MRT_CK(cudaEventRecord(static_cast<cudaEvent_t>(event), as_stream(stream)));
+    return MRT_OK;
+}
+
+int mrt_cuda_event_elapsed(mrt_ctx* ctx, void* start, void* stop, float* ms) {
+    if (!ctx || !start || !stop || !ms) return MRT_EINVAL;
+    MRT_CK(cudaEventSynchronize(static_cast<cudaEvent_t>(stop)));
+    MRT_CK(cudaEventElapsedTime(ms, static_cast<cudaEvent_t>(start), static_cast<cudaEvent_t>(stop)));
+    return MRT_OK;
+}
+
+// ---- scenes ---------------------------------------------------------------
+
+int mrt_cuda_scene_upload_triangles(mrt_ctx* ctx, const mrt_bvh8_node* nodes, uint32_t node_count,
+                                    const mrt_tri* tris, uint32_t tri_count, const mrt_material* materials,
+                                    uint32_t material_count, mrt_scene** out) {
+    if (!ctx || !out || !nodes || !tris || !materials || node_count == 0 || tri_count == 0 || material_count == 0)
+        return fail(ctx, MRT_EINVAL, "scene_upload_triangles: null pointer or empty scene");
+    cudaSetDevice(ctx->device);
+    *out = nullptr;
+    mrt_scene* sc = new (std::nothrow) mrt_scene;
+    if (!sc) return MRT_ENOMEM;
+    size_t nb = size_t(node_count) * sizeof(mrt_bvh8_node), tb = size_t(tri_count) * sizeof(mrt_tri),
+           mb = size_t(material_count) * sizeof(mrt_material);
+    if (cudaMalloc(&sc->d_nodes, nb) != cudaSuccess || cudaMalloc(&sc->d_tris, tb) != cudaSuccess ||
+        cudaMalloc(&sc->d_mats, mb) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(sc->d_nodes); cudaFree(sc->d_tris); cudaFree(sc->d_mats);
+        delete sc;
+        return fail(ctx, MRT_ENOMEM, "scene upload: out of device memory (%zu bytes)", nb + tb + mb);
+    }
+    if (cudaMemcpy(sc->d_nodes, nodes, nb, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(sc->d_tris, tris, tb, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(sc->d_mats, materials, mb, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(sc->d_nodes); cudaFree(sc->d_tris); cudaFree(sc->d_mats);
+        delete sc;
+        return fail(ctx, MRT_ECUDA, "scene upload: copy failed");
+    }
+    sc->kind = 0;
+    sc->dev.nodes = static_cast<const uint4*>(sc->d_nodes);
+    sc->dev.tris = static_cast<const float4*>(sc->d_tris);
+    sc->dev.mats = static_cast<const mrt_material*>(sc->d_mats);
+    sc->dev.spheres = nullptr;
+    sc->dev.node_count = node_count;
+    sc->dev.tri_count = tri_count;
+    sc->dev.mat_count = material_count;
+    sc->dev.sphere_count = 0;
+    *out = sc;
+    return MRT_OK;
+}
+
+int mrt_cuda_scene_upload_spheres(mrt_ctx* ctx, const mrt_sphere* spheres, uint32_t count, mrt_scene** out) {
+    if (!ctx || !out || !spheres || count == 0 || count > 4096)
+        return fail(ctx, MRT_EINVAL, "scene_upload_spheres: bad arguments");
+    cudaSetDevice(ctx->device);
+    mrt_scene* sc = new (std::nothrow) mrt_scene;
+    if (!sc) return MRT_ENOMEM;
+    if (cudaMalloc(&sc->d_spheres, count * sizeof(mrt_sphere)) != cudaSuccess) {
+        cudaGetLastError();
+        delete sc;
+        return fail(ctx, MRT_ENOMEM, "sphere upload failed");
+    }
+    if (cudaMemcpy(sc->d_spheres, spheres, count * sizeof(mrt_sphere), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(sc->d_spheres);
+        delete sc;
+        return fail(ctx, MRT_ECUDA, "sphere upload copy failed");
+    }
+    sc->kind = 1;
+    sc->dev.spheres = static_cast<const float4*>(sc->d_spheres);
+    sc->dev.sphere_count = count;
+    *out = sc;
+    return MRT_OK;
+}
+
+int mrt_cuda_scene_destroy(mrt_ctx* ctx, mrt_scene* scene) {
+    if (!ctx || !scene) return MRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    cudaFree(scene->d_nodes);
+    cudaFree(scene->d_tris);
+    cudaFree(scene->d_mats);
+    cudaFree(scene->d_spheres);
+    delete scene;
+    return MRT_OK;
+}
+
+int mrt_cuda_blue_noise_upload(mrt_ctx* ctx, const uint8_t* rgba, uint32_t w, uint32_t h) {
+    if (!ctx || !rgba || w == 0 || h == 0 || w > 1024 || h > 1024)
+        return fail(ctx, MRT_EINVAL, "blue_noise_upload: bad arguments");
+    cudaSetDevice(ctx->device);
+    std::vector<float2> rot(size_t(w) * h);
+    for (size_t i = 0; i < rot.size(); ++i) {
+        // R8G8B8A8_UNORM: channel byte / 255 (renderer.ixx:104-105)
+        rot[i].x = float(rgba[4 * i + 0]) / 255.0f;
+        rot[i].y = float(rgba[4 * i + 1]) / 255.0f;
+    }
+    cudaFree(ctx->d_bn);
+    ctx->d_bn = nullptr;
+    MRT_CK(cudaMalloc(&ctx->d_bn, rot.size() * sizeof(float2)));
+    MRT_CK(cudaMemcpy(ctx->d_bn, rot.data(), rot.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    ctx->bn_w = w;
+    ctx->bn_h = h;
+    return MRT_OK;
+}
+
+// ---- passes ---------------------------------------------------------------
+
+int mrt_cuda_primary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_camera_consts* consts,
+                          const mrt_gbuffer* gbuffer, void* stream) {
+    if (!ctx || !scene || !consts) return fail(ctx, MRT_EINVAL, "primary_rays: null argument");
+    int rc = check_gbuffer(ctx, gbuffer);
+    if (rc) return rc;
+    cudaSetDevice(ctx->device);
+    FrameParams fp = frame_params(consts, gbuffer->width, gbuffer->height);
+    cudaStream_t s = as_stream(stream);
+    {
+        Scope sc(ctx, s, 0, 0);
+        cudaError_t e = scene->kind == 0 ? launch_primary_tri(scene->dev, fp, *gbuffer, ctx->d_status, s)
+                                         : launch_primary_sphere(scene->dev, fp, *gbuffer, s);
+        if (e != cudaSuccess) return fail(ctx, MRT_ECUDA, "primary rays launch: %s", cudaGetErrorString(e));
+    }
+    ctx->launches++;
+    ctx->acc.primary_rays += uint64_t(gbuffer->width) * gbuffer->height;
+    return MRT_OK;
+}
+
+int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuffer* gbuffer,
+                            const mrt_camera_consts* consts, const mrt_trace_params* params, float* color,
+                            void* stream) {
+    if (!ctx || !scene || !consts || !params || !color) return fail(ctx, MRT_EINVAL, "secondary_rays: null argument");
+    int rc = check_gbuffer(ctx, gbuffer);
+    if (rc) return rc;
+    if (params->samples == 0 || params->samples > 65536) return fail(ctx, MRT_EINVAL, "samples must be 1..65536");
+    if (params->max_bounces > MRT_MAX_BOUNCES) return fail(ctx, MRT_ERANGE, "max_bounces > %d", MRT_MAX_BOUNCES);
+    if (params->rng_mode > MRT_RNG_PER_PIXEL || params->estimator > MRT_EST_NEE)
+        return fail(ctx, MRT_EINVAL, "bad rng_mode or estimator");
+    if (!ctx->d_bn) return fail(ctx, MRT_ESTATE, "no blue-noise texture uploaded");
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = as_stream(stream);
+    const uint32_t W = gbuffer->width, H = gbuffer->height;
+    FrameParams fp = frame_params(consts, W, H);
+    TraceParams tp = trace_params(params);
+    BlueNoise bn{ctx->d_bn, ctx->bn_w, ctx->bn_h};
+    Scope total(ctx, s, 5, 0);
+    if (scene->kind == 1) {
+        if (!gbuffer->depth || !gbuffer->normal)
+            return fail(ctx, MRT_EINVAL, "sphere scenes need gbuffer depth and normal");
+        Scope sc(ctx, s, 3, 0);
+        cudaError_t e = launch_secondary_sphere(scene->dev, fp, *gbuffer, tp, bn, color, params->accumulate,
+                                                params->frame_index, s);
+        if (e != cudaSuccess) return fail(ctx, MRT_ECUDA, "secondary launch: %s", cudaGetErrorString(e));
+        ctx->launches++;
+        return MRT_OK;
+    }
+    if (!gbuffer->hit_t) return fail(ctx, MRT_EINVAL, "triangle scenes need gbuffer hit_t");
+    rc = ensure_wave(ctx, size_t(W) * H);
+    if (rc) return rc;
+    WaveBuffers& wb = ctx->wb;
+    const int tblocks = trace_blocks_per_sm() * ctx->sm_count;
+    const bool nee = tp.estimator == MRT_EST_NEE;
+#define MRT_LAUNCH(kind, bounce, expr)                                                                   \
+    do {                                                                                                 \
+        Scope sc_(ctx, s, kind, bounce);                                                                 \
+        cudaError_t e_ = (expr);                                                                         \
+        if (e_ != cudaSuccess) return fail(ctx, MRT_ECUDA, "%s: %s", #expr, cudaGetErrorString(e_));    \
+        ctx->launches++;                                                                                 \
+    } while (0)
+    for (uint32_t smp = 0; smp < tp.samples; ++smp) {
+        MRT_CK(cudaMemsetAsync(wb.counters, 0, kCntSlots * sizeof(uint32_t), s));
+        MRT_LAUNCH(3, 0, launch_shade_primary(scene->dev, fp, *gbuffer, tp, bn, wb, smp, ctx->d_status, s));
+        for (uint32_t b = 1; b <= tp.max_bounces; ++b) {
+            if (nee) MRT_LAUNCH(2, int(b - 1), launch_trace_shadow(scene->dev, wb, tp, b - 1, tblocks, ctx->d_status, s));
+            if (params->sort_rays) MRT_LAUNCH(4, int(b), launch_sort_ext(scene->dev, wb, b, s));
+            MRT_LAUNCH(1, int(b), launch_trace_ext(scene->dev, wb, b, tblocks, ctx->d_status, s));
+            MRT_LAUNCH(3, int(b), launch_shade(scene->dev, tp, bn, wb, W, b, ctx->d_status, s));
+        }
+        if (nee) MRT_LAUNCH(2, int(tp.max_bounces), launch_trace_shadow(scene->dev, wb, tp, tp.max_bounces, tblocks, ctx->d_status, s));
+        MRT_LAUNCH(3, 0, launch_tally(wb, s));
+    }
+    MRT_LAUNCH(3, 0, launch_finalize(wb, color, tp.samples, params->accumulate, params->frame_index, s));
+#undef MRT_LAUNCH
+    return MRT_OK;
+}
+
+int mrt_cuda_trace_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_ray* rays, uint32_t count, mrt_hit* hits,
+                        uint32_t flags, void* stream) {
+    if (!ctx || !scene || (count && (!rays || !hits))) return fail(ctx, MRT_EINVAL, "trace_rays: bad arguments");
+    cudaSetDevice(ctx->device);
+    cudaError_t e = launch_trace_rays(scene->dev, rays, count, hits, (flags & MRT_TRACE_ANY_HIT) != 0, nullptr,
+                                      nullptr, ctx->d_status, as_stream(stream));
+    if (e != cudaSuccess) return fail(ctx, MRT_ECUDA, "trace_rays launch: %s", cudaGetErrorString(e));
+    ctx->launches++;
+    return MRT_OK;
+}
+
+int mrt_cuda_trace_rays_counted(mrt_ctx* ctx, const mrt_scene* scene, const mrt_ray* rays, uint32_t count,
+                                mrt_hit* hits, uint32_t* nodes_visited, uint32_t* tris_visited, void* stream) {
+    if (!ctx || !scene || (count && (!rays || !hits || !nodes_visited || !tris_visited)) || scene->kind != 0)
+        return fail(ctx, MRT_EINVAL, "trace_rays_counted: bad arguments");
+    cudaSetDevice(ctx->device);
+    cudaError_t e = launch_trace_rays(scene->dev, rays, count, hits, false, nodes_visited, tris_visited,
+                                      ctx->d_status, as_stream(stream));
+    if (e != cudaSuccess) return fail(ctx, MRT_ECUDA, "trace_rays_counted launch: %s", cudaGetErrorString(e));
+    ctx->launches++;
+    return MRT_OK;
+}
+
+int mrt_cuda_render_frame_host(mrt_ctx* ctx, const mrt_scene* scene, const mrt_camera_consts* consts,
+                               const mrt_trace_params* params, uint32_t width, uint32_t height, uint32_t* visibility,
+                               float* hit_t, float* color, void* stream) {
+    if (!ctx || !scene || !consts || !params || !color || width == 0 || height == 0)
+        return fail(ctx, MRT_EINVAL, "render_frame_host: bad arguments");
+    cudaSetDevice(ctx->device);
+    const size_t npix = size_t(width) * height;
+    if (ctx->frame_pixels != npix) {
+        cudaFree(ctx->d_vis); cudaFree(ctx->d_aux); cudaFree(ctx->d_t); cudaFree(ctx->d_color);
+        ctx->d_vis = nullptr; ctx->d_aux = nullptr; ctx->d_t = nullptr; ctx->d_color = nullptr;
+        ctx->frame_pixels = 0;
+        MRT_CK(cudaMalloc(&ctx->d_vis, npix * sizeof(uint32_t)));
+        MRT_CK(cudaMalloc(&ctx->d_aux, npix * (8 + 2)));
+        MRT_CK(cudaMalloc(&ctx->d_t, npix * sizeof(float)));
+        MRT_CK(cudaMalloc(&ctx->d_color, npix * 3 * sizeof(float)));
+        MRT_CK(cudaMemset(ctx->d_color, 0, npix * 3 * sizeof(float)));
+        ctx->frame_pixels = npix;
+    }
+    mrt_gbuffer g;
+    std::memset(&g, 0, sizeof(g));
+    g.visibility = ctx->d_vis;
+    g.hit_t = ctx->d_t;
+    if (scene->kind == 1) {
+        g.normal = static_cast<uint16_t*>(ctx->d_aux);
+        g.depth = reinterpret_cast<uint16_t*>(static_cast<char*>(ctx->d_aux) + npix * 8);
+    }
+    g.width = width;
+    g.height = height;
+    int rc = mrt_cuda_primary_rays(ctx, scene, consts, &g, stream);
+    if (rc) return rc;
+    rc = mrt_cuda_secondary_rays(ctx, scene, &g, consts, params, ctx->d_color, stream);
+    if (rc) return rc;
+    cudaStream_t s = as_stream(stream);
+    if (visibility) MRT_CK(cudaMemcpyAsync(visibility, ctx->d_vis, npix * 4, cudaMemcpyDeviceToHost, s));
+    if (hit_t) MRT_CK(cudaMemcpyAsync(hit_t, ctx->d_t, npix * 4, cudaMemcpyDeviceToHost, s));
+    MRT_CK(cudaMemcpyAsync(color, ctx->d_color, npix * 12, cudaMemcpyDeviceToHost, s));
+    MRT_CK(cudaStreamSynchronize(s));
+    return MRT_OK;
+}
+
+} // extern "C"

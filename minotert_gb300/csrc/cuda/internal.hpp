@@ -1,0 +1,139 @@
+// Private declarations shared by the C-ABI layer (api.cu) and the kernels.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "mrt_cuda.h"
+#include "traverse.cuh"
+
+namespace mrt {
+
+constexpr int kTraceBlock = 128;   // threads per traversal block
+constexpr int kStackDepth = 32;    // traversal stack entries per thread
+constexpr int kShadeBlock = 256;
+
+// Wavefront records
+struct PathRay {     // 48 bytes
+    float4 o_pix;    // origin xyz, pixel index (bits)
+    float4 d;        // direction xyz, unused
+    float4 beta;     // throughput rgb, unused
+};
+struct ShadowRay {   // 32 bytes
+    float4 o_pix;    // origin xyz, pixel index (bits)
+    float4 contrib;  // radiance added when unoccluded
+};
+
+// Device counters (uint32 slots)
+enum : uint32_t {
+    kCntExt = 0,                       // [b]: rays in the extension queue of bounce b
+    kCntShadow = kCntExt + 17,         // [b]: shadow rays emitted at vertex b
+    kCntFetchExt = kCntShadow + 17,    // [b]: work fetch of extension trace b
+    kCntFetchShadow = kCntFetchExt + 17,
+    kCntSlots = kCntFetchShadow + 17,
+};
+
+struct WaveBuffers {
+    size_t cap = 0;        // rays per queue
+    size_t npix = 0;
+    PathRay* q[2] = {nullptr, nullptr};
+    uint2* hits = nullptr;
+    ShadowRay* sq = nullptr;
+    float4* L = nullptr;
+    uint32_t* rng = nullptr;
+    uint32_t* counters = nullptr;
+    unsigned long long* totals = nullptr; // accumulated ray counts
+    uint32_t* keys = nullptr;             // sort scratch
+    uint32_t* perm = nullptr;
+    PathRay* qsort = nullptr;
+    uint32_t* hist = nullptr;
+};
+
+struct FrameParams {
+    mrt_camera_consts c;
+    float pv[16];       // projection * view
+    float ppv[16];      // projection * prev_view
+    uint32_t width, height;
+    float pitch_x, pitch_y;
+};
+
+struct TraceParams {
+    uint32_t samples, max_bounces, rr_start, rng_mode, estimator;
+    float sun[3], sun_e[3], sky[3];
+};
+
+struct BlueNoise {
+    const float2* rot;
+    uint32_t w, h;
+};
+
+// Launchers (kernels.cu).  All return cudaError_t of the launch.
+cudaError_t launch_primary_tri(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g,
+                               uint32_t* status, cudaStream_t s);
+cudaError_t launch_primary_sphere(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g,
+                                  cudaStream_t s);
+cudaError_t launch_secondary_sphere(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g,
+                                    const TraceParams& tp, BlueNoise bn, float* color,
+                                    uint32_t accumulate, uint32_t frame_index, cudaStream_t s);
+cudaError_t launch_trace_rays(const DevScene& sc, const mrt_ray* rays, uint32_t n, mrt_hit* hits,
+                              bool any_hit, uint32_t* nodes_v, uint32_t* tris_v, uint32_t* status,
+                              cudaStream_t s);
+
+// wavefront pieces
+cudaError_t launch_shade_primary(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g,
+                                 const TraceParams& tp, BlueNoise bn, const WaveBuffers& wb,
+                                 uint32_t sample, uint32_t* status, cudaStream_t s);
+cudaError_t launch_trace_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t bounce, int blocks,
+                             uint32_t* status, cudaStream_t s);
+cudaError_t launch_trace_shadow(const DevScene& sc, const WaveBuffers& wb, const TraceParams& tp,
+                                uint32_t vertex, int blocks, uint32_t* status, cudaStream_t s);
+cudaError_t launch_shade(const DevScene& sc, const TraceParams& tp, BlueNoise bn, const WaveBuffers& wb,
+                         uint32_t width, uint32_t bounce, uint32_t* status, cudaStream_t s);
+cudaError_t launch_tally(const WaveBuffers& wb, cudaStream_t s);
+cudaError_t launch_sort_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t bounce, cudaStream_t s);
+cudaError_t launch_finalize(const WaveBuffers& wb, float* color, uint32_t samples, uint32_t accumulate,
+                            uint32_t frame_index, cudaStream_t s);
+
+int trace_blocks_per_sm();  // occupancy of the traversal kernels
+
+} // namespace mrt
+
+struct mrt_scene {
+    int kind = 0; // 0 triangles, 1 spheres
+    mrt::DevScene dev{};
+    void* d_nodes = nullptr;
+    void* d_tris = nullptr;
+    void* d_mats = nullptr;
+    void* d_spheres = nullptr;
+};
+
+struct mrt_timing_rec {
+    int kind;      // 0 primary, 1 extend, 2 shadow, 3 shade, 4 sort, 5 total
+    int bounce;
+    cudaEvent_t a, b;
+};
+
+struct mrt_ctx {
+    int device = 0;
+    int sm_count = 0;
+    std::string err;
+    uint32_t* d_status = nullptr;
+    float2* d_bn = nullptr;
+    uint32_t bn_w = 0, bn_h = 0;
+    mrt::WaveBuffers wb;
+    // render_frame_host buffers
+    uint32_t* d_vis = nullptr;
+    void* d_aux = nullptr;   // normal (8 B/px) then depth (2 B/px)
+    float* d_t = nullptr;
+    float* d_color = nullptr;
+    size_t frame_pixels = 0;
+    // timing
+    bool timing = false;
+    std::vector<mrt_timing_rec> recs;
+    std::vector<cudaEvent_t> ev_pool;
+    mrt_frame_stats acc{};
+    uint32_t launches = 0;
+};

@@ -1,0 +1,608 @@
+// Ray-tracing kernels for sm_103a.
+//
+//   k_primary_tri / k_primary_sphere    primaryRay.comp:38-76 (pinhole ray,
+//                                       closest hit, g-buffer stores)
+//   k_secondary_sphere                  secondaryRays.comp:64-135 (the
+//                                       reference's per-pixel sample/bounce
+//                                       loop over analytic spheres)
+//   k_shade_primary / k_shade           wavefront shade: throughput x albedo,
+//   k_trace_ext / k_trace_shadow        cosine-weighted blue-noise-rotated
+//   k_finalize                          bounce (secondaryRays.comp:60-72,
+//                                       94-96), directional-light shadow
+//                                       rays, compaction, accumulation
+//   k_trace_rays                        generic closest/any-hit queries
+#include "internal.hpp"
+
+#include <cfloat>
+
+namespace mrt {
+
+constexpr float kInvPi = 0.318309886183790671538f;
+
+// Pinhole ray of pixel (x, y) (primaryRay.comp:46-51): uv at the pixel
+// centre with v flipped, origin = invView * (0,0,0,1),
+// dir = normalize(invView * vec4((invProj * vec4(2uv-1, 1, 1)).xyz, 0)).
+MRT_DEV void primary_ray(const FrameParams& fp, uint32_t x, uint32_t y, f3& o, f3& d) {
+    const float uvx = __fmul_rn(__fadd_rn(float(x), 0.5f), fp.pitch_x);
+    const float uvy = __fsub_rn(1.0f, __fmul_rn(__fadd_rn(float(y), 0.5f), fp.pitch_y));
+    float org[4], vd[4], wd[4];
+    matvec_rn(fp.c.inv_view, 0.0f, 0.0f, 0.0f, 1.0f, org);
+    matvec_rn(fp.c.inv_projection, __fsub_rn(__fmul_rn(uvx, 2.0f), 1.0f),
+              __fsub_rn(__fmul_rn(uvy, 2.0f), 1.0f), 1.0f, 1.0f, vd);
+    matvec_rn(fp.c.inv_view, vd[0], vd[1], vd[2], 0.0f, wd);
+    o = f3{org[0], org[1], org[2]};
+    d = normalize_rn(f3{wd[0], wd[1], wd[2]});
+}
+
+MRT_DEV f3 ray_at(f3 o, f3 d, float t) { return add_rn(o, scale_rn(d, t)); } // intersect.glsl:22-24
+
+// g-buffer extras: depth = (P V hit).z / w as R16F, normal RGBA16F (the ray
+// direction on a miss), motion = (proj - prev proj).xy / pitch as RG16F
+// (primaryRay.comp:62-75).  A miss (undefined in the reference) stores
+// depth 0 and motion 0.
+MRT_DEV void store_extras(const FrameParams& fp, const mrt_gbuffer& g, size_t pi, bool hit, f3 pos, f3 n) {
+    float depth = 0.0f, mx = 0.0f, my = 0.0f;
+    if (hit && (g.depth || g.motion)) {
+        float ph[4], pp[4];
+        matvec_rn(fp.pv, pos.x, pos.y, pos.z, 1.0f, ph);
+        const float px = __fdiv_rn(ph[0], ph[3]), py = __fdiv_rn(ph[1], ph[3]);
+        depth = __fdiv_rn(ph[2], ph[3]);
+        if (g.motion) {
+            matvec_rn(fp.ppv, pos.x, pos.y, pos.z, 1.0f, pp);
+            const float qx = __fdiv_rn(pp[0], pp[3]), qy = __fdiv_rn(pp[1], pp[3]);
+            mx = __fdiv_rn(__fsub_rn(px, qx), fp.pitch_x);
+            my = __fdiv_rn(__fsub_rn(py, qy), fp.pitch_y);
+        }
+    }
+    if (g.depth) g.depth[pi] = f2h(depth);
+    if (g.normal) {
+        ushort4 v = make_ushort4(f2h(n.x), f2h(n.y), f2h(n.z), f2h(0.0f));
+        reinterpret_cast<ushort4*>(g.normal)[pi] = v;
+    }
+    if (g.motion) reinterpret_cast<ushort2*>(g.motion)[pi] = make_ushort2(f2h(mx), f2h(my));
+}
+
+// Material of original triangle `prim`; an out-of-range id (corrupt scene
+// data) raises MRT_STATUS_BAD_TRI and shades as black.
+MRT_DEV mrt_material load_mat(const DevScene& sc, uint32_t prim, uint32_t* status) {
+    if (prim < sc.mat_count) return sc.mats[prim];
+    atomicOr(status, MRT_STATUS_BAD_TRI);
+    mrt_material m;
+    m.normal[0] = 0.0f; m.normal[1] = 0.0f; m.normal[2] = 1.0f;
+    m.albedo_rgba8 = 0u;
+    return m;
+}
+
+MRT_DEV f3 facing_normal(const mrt_material& m, f3 d) {
+    f3 n{m.normal[0], m.normal[1], m.normal[2]};
+    if (dot_rn(n, d) > 0.0f) n = f3{-n.x, -n.y, -n.z};
+    return n;
+}
+
+// Pixel of thread: blocks of 16x8 pixels, each warp an 8x4 tile.
+MRT_DEV bool tile_pixel(uint32_t w, uint32_t h, uint32_t& x, uint32_t& y) {
+    const uint32_t wi = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    x = blockIdx.x * 16u + (wi & 1u) * 8u + (lane & 7u);
+    y = blockIdx.y * 8u + (wi >> 1) * 4u + (lane >> 3);
+    return x < w && y < h;
+}
+
+__global__ void __launch_bounds__(kTraceBlock)
+k_primary_tri(DevScene sc, FrameParams fp, mrt_gbuffer g, uint32_t* status) {
+    __shared__ uint2 stk[kStackDepth * kTraceBlock];
+    uint32_t x, y;
+    if (!tile_pixel(fp.width, fp.height, x, y)) return;
+    f3 o, d;
+    primary_ray(fp, x, y, o, d);
+    uint32_t prim, st = 0u, cn = 0u, ct = 0u;
+    float t;
+    trace_bvh8<false, false, kStackDepth>(sc, o, d, 0.0f, INFINITY, prim, t, stk + threadIdx.x, kTraceBlock,
+                                          st, cn, ct);
+    if (st) atomicOr(status, st);
+    const size_t pi = size_t(y) * fp.width + x;
+    g.visibility[pi] = prim;
+    if (g.hit_t) g.hit_t[pi] = t;
+    if (g.depth || g.normal || g.motion) {
+        const bool hit = prim != kMiss;
+        f3 pos = o, n = d;
+        if (hit) {
+            pos = ray_at(o, d, t);
+            n = facing_normal(load_mat(sc, prim, status), d);
+        }
+        store_extras(fp, g, pi, hit, pos, n);
+    }
+}
+
+MRT_DEV void sphere_at(const DevScene& sc, uint32_t i, f3& c, float& r) {
+    const float4 s = sc.spheres[2 * i];
+    c = f3{s.x, s.y, s.z};
+    r = s.w;
+}
+
+__global__ void __launch_bounds__(128) k_primary_sphere(DevScene sc, FrameParams fp, mrt_gbuffer g) {
+    uint32_t x, y;
+    if (!tile_pixel(fp.width, fp.height, x, y)) return;
+    f3 o, d;
+    primary_ray(fp, x, y, o, d);
+    // tracePrimaryRay (primaryRay.comp:23-36): first nearest t >= 0
+    uint32_t prim = kMiss;
+    float tb = 0.0f;
+    for (uint32_t i = 0; i < sc.sphere_count; ++i) {
+        f3 c; float r;
+        sphere_at(sc, i, c, r);
+        const float t = ray_sphere(o, d, c, r);
+        if (t >= 0.0f && (prim == kMiss || t < tb)) { tb = t; prim = i; }
+    }
+    const size_t pi = size_t(y) * fp.width + x;
+    g.visibility[pi] = prim;
+    const bool hit = prim != kMiss;
+    if (g.hit_t) g.hit_t[pi] = hit ? tb : INFINITY;
+    f3 pos = o, n = d;
+    if (hit) {
+        f3 c; float r;
+        sphere_at(sc, prim, c, r);
+        pos = ray_at(o, d, tb);
+        n = normalize_rn(sub_rn(pos, c));
+    }
+    store_extras(fp, g, pi, hit, pos, n);
+}
+
+MRT_DEV uint32_t initial_seed(uint32_t mode, uint32_t frame, uint32_t pixel) {
+    uint32_t s = (frame << 1u) | 1u; // secondaryRays.comp:124
+    if (mode == MRT_RNG_PER_PIXEL) {
+        uint32_t h = pixel * 0x9E3779B1u + s;
+        s = pcg(h) | 1u;
+    }
+    return s;
+}
+
+MRT_DEV float2 bn_rot(const BlueNoise& bn, uint32_t x, uint32_t y) { return bn.rot[(y % bn.h) * bn.w + (x % bn.w)]; }
+
+// secondaryRays.comp:102-135 with the reference's sample/bounce loop.
+// skyColor() is a constant radiance here (the sky-view LUT is not built).
+__global__ void __launch_bounds__(128)
+k_secondary_sphere(DevScene sc, FrameParams fp, mrt_gbuffer g, TraceParams tp, BlueNoise bn, float* color,
+                   uint32_t accumulate, uint32_t frame_index) {
+    uint32_t x, y;
+    if (!tile_pixel(fp.width, fp.height, x, y)) return;
+    const size_t pi = size_t(y) * fp.width + x;
+    const float uvx = __fmul_rn(__fadd_rn(float(x), 0.5f), fp.pitch_x);
+    const float uvy = __fsub_rn(1.0f, __fmul_rn(__fadd_rn(float(y), 0.5f), fp.pitch_y));
+    // reconstruct the primary hit from the g-buffer (:114-123)
+    const uint32_t prim0 = g.visibility[pi];
+    const ushort4 nh = reinterpret_cast<const ushort4*>(g.normal)[pi];
+    const f3 n0{h2f(nh.x), h2f(nh.y), h2f(nh.z)};
+    const float depth = h2f(g.depth[pi]);
+    float vp[4], wp[4];
+    matvec_rn(fp.c.inv_projection, __fsub_rn(__fmul_rn(uvx, 2.0f), 1.0f), __fsub_rn(__fmul_rn(uvy, 2.0f), 1.0f),
+              depth, 1.0f, vp);
+    vp[0] = __fdiv_rn(vp[0], vp[3]);
+    vp[1] = __fdiv_rn(vp[1], vp[3]);
+    vp[2] = __fdiv_rn(vp[2], vp[3]);
+    matvec_rn(fp.c.inv_view, vp[0], vp[1], vp[2], 1.0f, wp);
+    const f3 p0{wp[0], wp[1], wp[2]};
+    uint32_t rng = initial_seed(tp.rng_mode, fp.c.frame_counter, uint32_t(pi));
+    const float2 rot = bn_rot(bn, x, y);
+    const f3 sky{tp.sky[0], tp.sky[1], tp.sky[2]};
+
+    f3 acc{0.0f, 0.0f, 0.0f};
+    for (uint32_t s = 0; s < tp.samples; ++s) {
+        // traceSecondaryRays (:64-100)
+        f3 col{1.0f, 1.0f, 1.0f}, hp = p0, hn = n0, res{0.0f, 0.0f, 0.0f};
+        uint32_t hprim = prim0;
+        for (uint32_t i = 0; i < tp.max_bounces + 1u; ++i) {
+            if (i > 0) {
+                const f3 ro = add_rn(hp, scale_rn(hn, 0.000001f));
+                const float u1 = rotated_random(rng, rot.x);
+                const float u2 = rotated_random(rng, rot.y);
+                const f3 sp = random_sphere_point(__fsub_rn(__fmul_rn(u1, 2.0f), 1.0f),
+                                                  __fsub_rn(__fmul_rn(u2, 2.0f), 1.0f));
+                const f3 rd = normalize_rn(add_rn(hn, sp));
+                hprim = kMiss;
+                float ht = -1.0f;
+                for (uint32_t k = 0; k < sc.sphere_count; ++k) {
+                    f3 c; float r;
+                    sphere_at(sc, k, c, r);
+                    const float t = ray_sphere(ro, rd, c, r);
+                    if (t >= 0.0f && (t < ht || ht < 0.0f)) { hprim = k; ht = t; }
+                }
+                if (hprim != kMiss) {
+                    f3 c; float r;
+                    sphere_at(sc, hprim, c, r);
+                    hp = ray_at(ro, rd, ht);
+                    hn = normalize_rn(sub_rn(hp, c));
+                } else {
+                    hn = rd;
+                }
+            }
+            if (hprim != kMiss) {
+                const float4 al = sc.spheres[2 * hprim + 1];
+                col = mul_rn(col, f3{al.x, al.y, al.z});
+            } else {
+                res = mul_rn(col, sky);
+                break;
+            }
+        }
+        acc = add_rn(acc, res);
+    }
+    const float ns = float(tp.samples);
+    f3 mean{__fdiv_rn(acc.x, ns), __fdiv_rn(acc.y, ns), __fdiv_rn(acc.z, ns)};
+    float* out = color + pi * 3;
+    if (accumulate) {
+        const float w = float(frame_index + 1u);
+        mean.x = __fadd_rn(out[0], __fdiv_rn(__fsub_rn(mean.x, out[0]), w));
+        mean.y = __fadd_rn(out[1], __fdiv_rn(__fsub_rn(mean.y, out[1]), w));
+        mean.z = __fadd_rn(out[2], __fdiv_rn(__fsub_rn(mean.z, out[2]), w));
+    }
+    out[0] = mean.x;
+    out[1] = mean.y;
+    out[2] = mean.z;
+}
+
+// ---------------------------------------------------------------- wavefront
+
+// Warp-aggregated slot reservation: one atomic per warp for all lanes that
+// `want` a slot.  Must be called by all 32 lanes.
+MRT_DEV uint32_t warp_reserve(uint32_t* counter, bool want) {
+    const uint32_t mask = __ballot_sync(0xFFFFFFFFu, want);
+    if (!mask) return 0u;
+    const uint32_t lane = lane_id();
+    const uint32_t leader = __ffs(mask) - 1u;
+    uint32_t base = 0u;
+    if (lane == leader) base = atomicAdd(counter, uint32_t(__popc(mask)));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+struct VertexOut {
+    bool shadow;
+    bool ext;
+    ShadowRay sr;
+    PathRay pr;
+};
+
+// Shade one path vertex: directional-light shadow ray (MRT_EST_NEE),
+// throughput *= albedo (secondaryRays.comp:94), next cosine-weighted
+// direction normalize(n + uniformSpherePoint) with blue-noise-rotated PCG
+// numbers (:70-72), Russian roulette on bounces > rr_start.
+MRT_DEV VertexOut shade_vertex(const DevScene& sc, const TraceParams& tp, const BlueNoise& bn, uint32_t width,
+                               uint32_t vertex, uint32_t pix, f3 p, f3 d, uint32_t prim, f3 beta, uint32_t& rng,
+                               uint32_t* status) {
+    VertexOut vo;
+    vo.shadow = false;
+    vo.ext = false;
+    const mrt_material m = load_mat(sc, prim, status);
+    const f3 n = facing_normal(m, d);
+    const f3 rho{__fdiv_rn(float(m.albedo_rgba8 & 0xFFu), 255.0f),
+                 __fdiv_rn(float((m.albedo_rgba8 >> 8) & 0xFFu), 255.0f),
+                 __fdiv_rn(float((m.albedo_rgba8 >> 16) & 0xFFu), 255.0f)};
+    if (tp.estimator == MRT_EST_NEE) {
+        const f3 sun{tp.sun[0], tp.sun[1], tp.sun[2]};
+        const float cosl = dot_rn(n, sun);
+        if (cosl > 0.0f) {
+            const f3 os = offset_ray(p, n);
+            const float k = __fmul_rn(cosl, kInvPi);
+            const f3 c = scale_rn(mul_rn(mul_rn(beta, rho), f3{tp.sun_e[0], tp.sun_e[1], tp.sun_e[2]}), k);
+            vo.shadow = true;
+            vo.sr.o_pix = make_float4(os.x, os.y, os.z, __uint_as_float(pix));
+            vo.sr.contrib = make_float4(c.x, c.y, c.z, 0.0f);
+        }
+    }
+    beta = mul_rn(beta, rho);
+    if (vertex >= tp.max_bounces) return vo;
+    const float2 rot = bn_rot(bn, pix % width, pix / width);
+    const float u1 = rotated_random(rng, rot.x);
+    const float u2 = rotated_random(rng, rot.y);
+    const f3 sp = random_sphere_point(__fsub_rn(__fmul_rn(u1, 2.0f), 1.0f), __fsub_rn(__fmul_rn(u2, 2.0f), 1.0f));
+    f3 nd = add_rn(n, sp);
+    if (dot_rn(nd, nd) == 0.0f) nd = n;
+    nd = normalize_rn(nd);
+    if (tp.rr_start != 0u && vertex + 1u > tp.rr_start) {
+        float q = fmaxf(fmaxf(beta.x, beta.y), beta.z);
+        q = fminf(fmaxf(q, 0.05f), 1.0f);
+        const float u3 = rotated_random(rng, rot.x);
+        if (u3 >= q) return vo;
+        beta = f3{__fdiv_rn(beta.x, q), __fdiv_rn(beta.y, q), __fdiv_rn(beta.z, q)};
+    }
+    const f3 oe = offset_ray(p, n);
+    vo.ext = true;
+    vo.pr.o_pix = make_float4(oe.x, oe.y, oe.z, __uint_as_float(pix));
+    vo.pr.d = make_float4(nd.x, nd.y, nd.z, 0.0f);
+    vo.pr.beta = make_float4(beta.x, beta.y, beta.z, 0.0f);
+    return vo;
+}
+
+MRT_DEV void add_L(float4* L, uint32_t pix, f3 v) {
+    float4 a = L[pix];
+    a.x = __fadd_rn(a.x, v.x);
+    a.y = __fadd_rn(a.y, v.y);
+    a.z = __fadd_rn(a.z, v.z);
+    L[pix] = a;
+}
+
+MRT_DEV void emit(const VertexOut& vo, const WaveBuffers& wb, uint32_t vertex) {
+    const uint32_t si = warp_reserve(wb.counters + kCntShadow + vertex, vo.shadow);
+    if (vo.shadow) wb.sq[si] = vo.sr;
+    const uint32_t ei = warp_reserve(wb.counters + kCntExt + vertex + 1u, vo.ext);
+    PathRay* q = ((vertex + 1u) & 1u) ? wb.q[1] : wb.q[0];
+    if (vo.ext) q[ei] = vo.pr;
+}
+
+// Vertex 0: the primary hit from the g-buffer (visibility + FP32 hit_t).
+__global__ void __launch_bounds__(kShadeBlock)
+k_shade_primary(DevScene sc, FrameParams fp, mrt_gbuffer g, TraceParams tp, BlueNoise bn, WaveBuffers wb,
+                uint32_t sample, uint32_t* status) {
+    const uint32_t npix = fp.width * fp.height;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounded = (npix + 31u) & ~31u;
+    const f3 sky{tp.sky[0], tp.sky[1], tp.sky[2]};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < rounded; i += stride) {
+        const bool valid = i < npix;
+        VertexOut vo;
+        vo.shadow = vo.ext = false;
+        if (valid) {
+            uint32_t rng = sample == 0u ? initial_seed(tp.rng_mode, fp.c.frame_counter, i) : wb.rng[i];
+            if (sample == 0u) wb.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            const uint32_t prim = g.visibility[i];
+            if (prim == kMiss) {
+                add_L(wb.L, i, sky);
+            } else {
+                const uint32_t x = i % fp.width, y = i / fp.width;
+                f3 o, d;
+                primary_ray(fp, x, y, o, d);
+                const f3 p = ray_at(o, d, g.hit_t[i]);
+                vo = shade_vertex(sc, tp, bn, fp.width, 0u, i, p, d, prim, f3{1.0f, 1.0f, 1.0f}, rng, status);
+            }
+            wb.rng[i] = rng;
+        }
+        emit(vo, wb, 0u);
+    }
+}
+
+// Vertex `vertex` >= 1: hits of the extension rays of bounce `vertex`.
+__global__ void __launch_bounds__(kShadeBlock)
+k_shade(DevScene sc, TraceParams tp, BlueNoise bn, WaveBuffers wb, uint32_t width, uint32_t vertex,
+        uint32_t* status) {
+    const uint32_t n = wb.counters[kCntExt + vertex];
+    const PathRay* q = (vertex & 1u) ? wb.q[1] : wb.q[0];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounded = (n + 31u) & ~31u;
+    const f3 sky{tp.sky[0], tp.sky[1], tp.sky[2]};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < rounded; i += stride) {
+        VertexOut vo;
+        vo.shadow = vo.ext = false;
+        if (i < n) {
+            const PathRay pr = q[i];
+            const uint2 h = wb.hits[i];
+            const uint32_t pix = __float_as_uint(pr.o_pix.w);
+            const f3 beta{pr.beta.x, pr.beta.y, pr.beta.z};
+            if (h.x == kMiss) {
+                add_L(wb.L, pix, mul_rn(beta, sky));
+            } else {
+                uint32_t rng = wb.rng[pix];
+                const f3 o{pr.o_pix.x, pr.o_pix.y, pr.o_pix.z}, d{pr.d.x, pr.d.y, pr.d.z};
+                const f3 p = ray_at(o, d, __uint_as_float(h.y));
+                vo = shade_vertex(sc, tp, bn, width, vertex, pix, p, d, h.x, beta, rng, status);
+                wb.rng[pix] = rng;
+            }
+        }
+        emit(vo, wb, vertex);
+    }
+}
+
+// Persistent closest-hit over the extension queue of bounce `bounce`;
+// each warp fetches 32 rays at a time.
+__global__ void __launch_bounds__(kTraceBlock)
+k_trace_ext(DevScene sc, WaveBuffers wb, uint32_t bounce, uint32_t* status) {
+    __shared__ uint2 stk[kStackDepth * kTraceBlock];
+    const uint32_t n = wb.counters[kCntExt + bounce];
+    const PathRay* q = (bounce & 1u) ? wb.q[1] : wb.q[0];
+    uint32_t* fetch = wb.counters + kCntFetchExt + bounce;
+    const uint32_t lane = lane_id();
+    uint32_t st = 0u;
+    while (true) {
+        uint32_t base = 0u;
+        if (lane == 0u) base = atomicAdd(fetch, 32u);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= n) break;
+        const uint32_t i = base + lane;
+        if (i < n) {
+            const float4 a = q[i].o_pix, b = q[i].d;
+            uint32_t prim, cn = 0u, ct = 0u;
+            float t;
+            trace_bvh8<false, false, kStackDepth>(sc, f3{a.x, a.y, a.z}, f3{b.x, b.y, b.z}, 0.0f, INFINITY, prim, t,
+                                                  stk + threadIdx.x, kTraceBlock, st, cn, ct);
+            wb.hits[i] = make_uint2(prim, __float_as_uint(t));
+        }
+    }
+    if (st) atomicOr(status, st);
+}
+
+// Persistent any-hit over the shadow queue of vertex `vertex`; unoccluded
+// rays add their contribution to the pixel's radiance.
+__global__ void __launch_bounds__(kTraceBlock)
+k_trace_shadow(DevScene sc, WaveBuffers wb, TraceParams tp, uint32_t vertex, uint32_t* status) {
+    __shared__ uint2 stk[kStackDepth * kTraceBlock];
+    const uint32_t n = wb.counters[kCntShadow + vertex];
+    uint32_t* fetch = wb.counters + kCntFetchShadow + vertex;
+    const uint32_t lane = lane_id();
+    const f3 sun{tp.sun[0], tp.sun[1], tp.sun[2]};
+    uint32_t st = 0u;
+    while (true) {
+        uint32_t base = 0u;
+        if (lane == 0u) base = atomicAdd(fetch, 32u);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= n) break;
+        const uint32_t i = base + lane;
+        if (i < n) {
+            const ShadowRay sr = wb.sq[i];
+            uint32_t prim, cn = 0u, ct = 0u;
+            float t;
+            trace_bvh8<true, false, kStackDepth>(sc, f3{sr.o_pix.x, sr.o_pix.y, sr.o_pix.z}, sun, 0.0f, INFINITY, prim,
+                                                 t, stk + threadIdx.x, kTraceBlock, st, cn, ct);
+            if (prim == kMiss)
+                add_L(wb.L, __float_as_uint(sr.o_pix.w), f3{sr.contrib.x, sr.contrib.y, sr.contrib.z});
+        }
+    }
+    if (st) atomicOr(status, st);
+}
+
+__global__ void k_tally(WaveBuffers wb) {
+    const uint32_t j = threadIdx.x;
+    if (j < kCntFetchExt) atomicAdd(wb.totals + j, (unsigned long long)wb.counters[j]);
+}
+
+__global__ void __launch_bounds__(kShadeBlock)
+k_finalize(WaveBuffers wb, float* color, uint32_t npix, uint32_t samples, uint32_t accumulate, uint32_t frame_index) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npix) return;
+    const float4 l = wb.L[i];
+    const float ns = float(samples);
+    float m[3] = {__fdiv_rn(l.x, ns), __fdiv_rn(l.y, ns), __fdiv_rn(l.z, ns)};
+    float* out = color + size_t(i) * 3;
+    if (accumulate) {
+        const float w = float(frame_index + 1u);
+        for (int k = 0; k < 3; ++k) m[k] = __fadd_rn(out[k], __fdiv_rn(__fsub_rn(m[k], out[k]), w));
+    }
+    out[0] = m[0];
+    out[1] = m[1];
+    out[2] = m[2];
+}
+
+template <bool kAnyHit, bool kCount>
+__global__ void __launch_bounds__(kTraceBlock)
+k_trace_rays(DevScene sc, const mrt_ray* rays, uint32_t n, mrt_hit* hits, uint32_t* nodes_v, uint32_t* tris_v,
+             uint32_t* status) {
+    __shared__ uint2 stk[kStackDepth * kTraceBlock];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4* rp = reinterpret_cast<const float4*>(rays + i);
+    const float4 a = rp[0], b = rp[1];
+    uint32_t prim, st = 0u, cn = 0u, ct = 0u;
+    float t;
+    trace_bvh8<kAnyHit, kCount, kStackDepth>(sc, f3{a.x, a.y, a.z}, f3{b.x, b.y, b.z}, a.w, b.w, prim, t,
+                                             stk + threadIdx.x, kTraceBlock, st, cn, ct);
+    hits[i].prim = prim;
+    hits[i].t = t;
+    if (kCount) {
+        nodes_v[i] = cn;
+        tris_v[i] = ct;
+    }
+    if (st) atomicOr(status, st);
+}
+
+template <bool kAnyHit>
+__global__ void __launch_bounds__(128)
+k_trace_rays_sphere(DevScene sc, const mrt_ray* rays, uint32_t n, mrt_hit* hits) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const mrt_ray r = rays[i];
+    const f3 o{r.org[0], r.org[1], r.org[2]}, d{r.dir[0], r.dir[1], r.dir[2]};
+    uint32_t prim = kMiss;
+    float tb = r.tmax;
+    for (uint32_t k = 0; k < sc.sphere_count; ++k) {
+        f3 c; float rad;
+        sphere_at(sc, k, c, rad);
+        const float t = ray_sphere(o, d, c, rad);
+        if (t > r.tmin && t < tb) {
+            tb = t;
+            prim = k;
+            if (kAnyHit) break;
+        }
+    }
+    hits[i].prim = prim;
+    hits[i].t = tb;
+}
+
+// ------------------------------------------------------------------ launchers
+
+cudaError_t launch_primary_tri(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g, uint32_t* status,
+                               cudaStream_t s) {
+    dim3 grid((fp.width + 15) / 16, (fp.height + 7) / 8);
+    k_primary_tri<<<grid, kTraceBlock, 0, s>>>(sc, fp, g, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_primary_sphere(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g, cudaStream_t s) {
+    dim3 grid((fp.width + 15) / 16, (fp.height + 7) / 8);
+    k_primary_sphere<<<grid, 128, 0, s>>>(sc, fp, g);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_secondary_sphere(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g,
+                                    const TraceParams& tp, BlueNoise bn, float* color, uint32_t accumulate,
+                                    uint32_t frame_index, cudaStream_t s) {
+    dim3 grid((fp.width + 15) / 16, (fp.height + 7) / 8);
+    k_secondary_sphere<<<grid, 128, 0, s>>>(sc, fp, g, tp, bn, color, accumulate, frame_index);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_rays(const DevScene& sc, const mrt_ray* rays, uint32_t n, mrt_hit* hits, bool any_hit,
+                              uint32_t* nodes_v, uint32_t* tris_v, uint32_t* status, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const uint32_t blocks = (n + kTraceBlock - 1) / kTraceBlock;
+    if (sc.sphere_count) {
+        if (any_hit) k_trace_rays_sphere<true><<<blocks, 128, 0, s>>>(sc, rays, n, hits);
+        else k_trace_rays_sphere<false><<<blocks, 128, 0, s>>>(sc, rays, n, hits);
+    } else if (nodes_v) {
+        k_trace_rays<false, true><<<blocks, kTraceBlock, 0, s>>>(sc, rays, n, hits, nodes_v, tris_v, status);
+    } else if (any_hit) {
+        k_trace_rays<true, false><<<blocks, kTraceBlock, 0, s>>>(sc, rays, n, hits, nullptr, nullptr, status);
+    } else {
+        k_trace_rays<false, false><<<blocks, kTraceBlock, 0, s>>>(sc, rays, n, hits, nullptr, nullptr, status);
+    }
+    return cudaGetLastError();
+}
+
+static int shade_blocks(uint32_t n) {
+    uint32_t b = (n + kShadeBlock - 1) / kShadeBlock;
+    return int(b < 1 ? 1 : (b > 4096 ? 4096 : b));
+}
+
+cudaError_t launch_shade_primary(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g, const TraceParams& tp,
+                                 BlueNoise bn, const WaveBuffers& wb, uint32_t sample, uint32_t* status,
+                                 cudaStream_t s) {
+    k_shade_primary<<<shade_blocks(fp.width * fp.height), kShadeBlock, 0, s>>>(sc, fp, g, tp, bn, wb, sample, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t bounce, int blocks, uint32_t* status,
+                             cudaStream_t s) {
+    k_trace_ext<<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_shadow(const DevScene& sc, const WaveBuffers& wb, const TraceParams& tp, uint32_t vertex,
+                                int blocks, uint32_t* status, cudaStream_t s) {
+    k_trace_shadow<<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shade(const DevScene& sc, const TraceParams& tp, BlueNoise bn, const WaveBuffers& wb,
+                         uint32_t width, uint32_t bounce, uint32_t* status, cudaStream_t s) {
+    k_shade<<<shade_blocks(uint32_t(wb.cap)), kShadeBlock, 0, s>>>(sc, tp, bn, wb, width, bounce, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sort_ext(const DevScene&, const WaveBuffers&, uint32_t, cudaStream_t) { return cudaSuccess; }
+
+cudaError_t launch_finalize(const WaveBuffers& wb, float* color, uint32_t samples, uint32_t accumulate,
+                            uint32_t frame_index, cudaStream_t s) {
+    const uint32_t npix = uint32_t(wb.npix);
+    k_finalize<<<(npix + kShadeBlock - 1) / kShadeBlock, kShadeBlock, 0, s>>>(wb, color, npix, samples, accumulate,
+                                                                             frame_index);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tally(const WaveBuffers& wb, cudaStream_t s) {
+    k_tally<<<1, 64, 0, s>>>(wb);
+    return cudaGetLastError();
+}
+
+int trace_blocks_per_sm() {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_ext, kTraceBlock, 0) != cudaSuccess || b < 1) b = 1;
+    return b;
+}
+
+} // namespace mrt

@@ -1,0 +1,234 @@
+// BVH8 traversal and watertight ray/triangle intersection.
+//
+// The reference finds closest hits by looping over 5 spheres
+// (primaryRay.comp:23-36, secondaryRays.comp:74-89); this is the triangle
+// replacement, built from published methods:
+//   - watertight ray/triangle test: Woop, Benthin & Wald, "Watertight
+//     Ray/Triangle Intersection", JCGT 2(1), 2013 -- per-ray shear to the
+//     dominant axis, 2D edge functions, double-precision recheck on zero;
+//   - compressed 8-wide BVH traversal with octant-ordered children and an
+//     (base, hit-mask) group stack: Ylitie, Karras & Laine, HPG 2017;
+//   - conservative slab test: Ize, "Robust BVH Ray Traversal", JCGT 2013
+//     (far distances scaled up by a relative epsilon).
+// Ties at equal t resolve to the lower original triangle id, so the result
+// is independent of the BVH and of traversal order.
+#pragma once
+
+#include "common.cuh"
+
+namespace mrt {
+
+struct DevScene {
+    const uint4* nodes;       // 8 x uint4 per node (128 bytes)
+    const float4* tris;       // 3 x float4 per triangle, leaf order
+    const mrt_material* mats; // per original triangle id
+    const float4* spheres;    // 2 x float4 per sphere: center+radius, albedo
+    uint32_t node_count;
+    uint32_t tri_count;
+    uint32_t mat_count;
+    uint32_t sphere_count;
+};
+
+constexpr float kRobustScale = 1.0f + 1.0f / 1048576.0f; // 1 + 2^-20
+
+struct RayPre {
+    f3 o;
+    float ix, iy, iz; // 1/d with |d| clamped away from 0
+    uint32_t oct;     // bit a set: inverse direction negative along axis a
+    int kx, ky, kz;   // watertight shear axes
+    float sx, sy, sz;
+    float okx, oky, okz;
+};
+
+MRT_DEV float sel3(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
+
+MRT_DEV float safe_inv(float d) {
+    const float kTiny = 8.271806125530277e-25f; // 2^-80
+    float dd = fabsf(d) < kTiny ? copysignf(kTiny, d) : d;
+    return __frcp_rn(dd);
+}
+
+MRT_DEV RayPre ray_pre(f3 o, f3 d) {
+    RayPre r;
+    r.o = o;
+    r.ix = safe_inv(d.x);
+    r.iy = safe_inv(d.y);
+    r.iz = safe_inv(d.z);
+    r.oct = (r.ix < 0.0f ? 1u : 0u) | (r.iy < 0.0f ? 2u : 0u) | (r.iz < 0.0f ? 4u : 0u);
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int kz = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+    int kx = kz == 2 ? 0 : kz + 1;
+    int ky = kx == 2 ? 0 : kx + 1;
+    float dkz = sel3(d.x, d.y, d.z, kz);
+    if (dkz < 0.0f) { int t = kx; kx = ky; ky = t; }
+    r.kx = kx; r.ky = ky; r.kz = kz;
+    r.sx = __fdiv_rn(sel3(d.x, d.y, d.z, kx), dkz);
+    r.sy = __fdiv_rn(sel3(d.x, d.y, d.z, ky), dkz);
+    r.sz = __frcp_rn(dkz);
+    r.okx = sel3(o.x, o.y, o.z, kx);
+    r.oky = sel3(o.x, o.y, o.z, ky);
+    r.okz = sel3(o.x, o.y, o.z, kz);
+    return r;
+}
+
+// Watertight test; returns true with t (> tmin) when the ray crosses the
+// triangle (either facing).
+MRT_DEV bool intersect_tri(const RayPre& r, float4 a, float4 b, float4 c, float tmin, float& t_out) {
+    const float akx = __fsub_rn(sel3(a.x, a.y, a.z, r.kx), r.okx);
+    const float aky = __fsub_rn(sel3(a.x, a.y, a.z, r.ky), r.oky);
+    const float akz = __fsub_rn(sel3(a.x, a.y, a.z, r.kz), r.okz);
+    const float bkx = __fsub_rn(sel3(b.x, b.y, b.z, r.kx), r.okx);
+    const float bky = __fsub_rn(sel3(b.x, b.y, b.z, r.ky), r.oky);
+    const float bkz = __fsub_rn(sel3(b.x, b.y, b.z, r.kz), r.okz);
+    const float ckx = __fsub_rn(sel3(c.x, c.y, c.z, r.kx), r.okx);
+    const float cky = __fsub_rn(sel3(c.x, c.y, c.z, r.ky), r.oky);
+    const float ckz = __fsub_rn(sel3(c.x, c.y, c.z, r.kz), r.okz);
+    const float Ax = fmaf(-r.sx, akz, akx), Ay = fmaf(-r.sy, akz, aky);
+    const float Bx = fmaf(-r.sx, bkz, bkx), By = fmaf(-r.sy, bkz, bky);
+    const float Cx = fmaf(-r.sx, ckz, ckx), Cy = fmaf(-r.sy, ckz, cky);
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = float(__dsub_rn(__dmul_rn(double(Cx), double(By)), __dmul_rn(double(Cy), double(Bx))));
+        V = float(__dsub_rn(__dmul_rn(double(Ax), double(Cy)), __dmul_rn(double(Ay), double(Cx))));
+        W = float(__dsub_rn(__dmul_rn(double(Bx), double(Ay)), __dmul_rn(double(By), double(Ax))));
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.0f) return false;
+    const float Az = __fmul_rn(r.sz, akz), Bz = __fmul_rn(r.sz, bkz), Cz = __fmul_rn(r.sz, ckz);
+    const float T = fmaf(U, Az, fmaf(V, Bz, __fmul_rn(W, Cz)));
+    if (T == 0.0f || ((T < 0.0f) != (det < 0.0f))) return false;
+    const float t = __fdiv_rn(T, det);
+    if (!(t > tmin)) return false;
+    t_out = t;
+    return true;
+}
+
+MRT_DEV float byte_to_float(uint32_t word, uint32_t k) {
+    // 2^23 + byte as float bits, minus 2^23: exact
+    return __fsub_rn(__int_as_float(__byte_perm(word, 0x4B000000u, k | 0x7440u)), 8388608.0f);
+}
+
+// Closest hit (kAnyHit = false) or first hit with t < tmax (kAnyHit = true).
+// `stk` points at this thread's first stack slot; slot i is stk[i * stride].
+// Returns the number of loop iterations (for the counters).
+template <bool kAnyHit, bool kCount, int kStack>
+MRT_DEV void trace_bvh8(const DevScene& sc, f3 o, f3 d, float tmin, float tmax, uint32_t& hit_prim,
+                        float& hit_t, uint2* stk, uint32_t stride, uint32_t& status,
+                        uint32_t& cnt_nodes, uint32_t& cnt_tris) {
+    const RayPre r = ray_pre(o, d);
+    float tbest = tmax;
+    uint32_t best = kMiss;
+    // current internal-node group: base index, hit keys (bit k: slot k^oct),
+    // imask of the node the group came from
+    uint32_t g_base = 0, g_hits = 1u << r.oct, g_imask = 1u;
+    int sp = 0;
+    const uint32_t cap = sc.node_count + 64u;
+    uint32_t iters = 0;
+    const bool negx = r.ix < 0.0f, negy = r.iy < 0.0f, negz = r.iz < 0.0f;
+
+    while (true) {
+        if (g_hits == 0u) {
+            if (sp == 0) break;
+            --sp;
+            const uint2 e = stk[sp * stride];
+            g_base = e.x;
+            g_hits = e.y >> 8;
+            g_imask = e.y & 0xFFu;
+        }
+        const uint32_t key = __ffs(g_hits) - 1u;
+        g_hits &= g_hits - 1u;
+        const uint32_t slot = key ^ r.oct;
+        const uint32_t node = g_base + __popc(g_imask & ((1u << slot) - 1u));
+        if (g_hits) {
+            if (sp >= kStack) { status |= MRT_STATUS_STACK_OVF; break; }
+            stk[sp * stride] = make_uint2(g_base, (g_hits << 8) | g_imask);
+            ++sp;
+        }
+        if (++iters > cap) { status |= MRT_STATUS_ITER_CAP; break; }
+        if (node >= sc.node_count) { status |= MRT_STATUS_BAD_NODE; break; }
+        if (kCount) ++cnt_nodes;
+
+        const uint4* np = sc.nodes + size_t(node) * 8u;
+        const uint4 L0 = __ldg(np + 0), L1 = __ldg(np + 1), L2 = __ldg(np + 2), L3 = __ldg(np + 3),
+                    L4 = __ldg(np + 4);
+        const int ex = int(int8_t(L0.w & 0xFFu)), ey = int(int8_t((L0.w >> 8) & 0xFFu)),
+                  ez = int(int8_t((L0.w >> 16) & 0xFFu));
+        const uint32_t imask = L0.w >> 24;
+        const float scx = __fmul_rn(__int_as_float((ex + 127) << 23), r.ix);
+        const float scy = __fmul_rn(__int_as_float((ey + 127) << 23), r.iy);
+        const float scz = __fmul_rn(__int_as_float((ez + 127) << 23), r.iz);
+        const float adx = __fmul_rn(__fsub_rn(__uint_as_float(L0.x), r.o.x), r.ix);
+        const float ady = __fmul_rn(__fsub_rn(__uint_as_float(L0.y), r.o.y), r.iy);
+        const float adz = __fmul_rn(__fsub_rn(__uint_as_float(L0.z), r.o.z), r.iz);
+        // near/far quantised planes per axis, chosen by the direction sign
+        const uint32_t nx0 = negx ? L3.z : L2.x, nx1 = negx ? L3.w : L2.y;
+        const uint32_t fx0 = negx ? L2.x : L3.z, fx1 = negx ? L2.y : L3.w;
+        const uint32_t ny0 = negy ? L4.x : L2.z, ny1 = negy ? L4.y : L2.w;
+        const uint32_t fy0 = negy ? L2.z : L4.x, fy1 = negy ? L2.w : L4.y;
+        const uint32_t nz0 = negz ? L4.z : L3.x, nz1 = negz ? L4.w : L3.y;
+        const uint32_t fz0 = negz ? L3.x : L4.z, fz1 = negz ? L3.y : L4.w;
+
+        uint32_t int_keys = 0u, tri_mask = 0u;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const uint32_t k = uint32_t(i & 3);
+            const float tnx = fmaf(byte_to_float(i < 4 ? nx0 : nx1, k), scx, adx);
+            const float tny = fmaf(byte_to_float(i < 4 ? ny0 : ny1, k), scy, ady);
+            const float tnz = fmaf(byte_to_float(i < 4 ? nz0 : nz1, k), scz, adz);
+            const float tfx = fmaf(byte_to_float(i < 4 ? fx0 : fx1, k), scx, adx);
+            const float tfy = fmaf(byte_to_float(i < 4 ? fy0 : fy1, k), scy, ady);
+            const float tfz = fmaf(byte_to_float(i < 4 ? fz0 : fz1, k), scz, adz);
+            const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+            const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tbest));
+            if (tn <= __fmul_rn(tf, kRobustScale)) {
+                const uint32_t meta = ((i < 4 ? L1.z : L1.w) >> (8 * k)) & 0xFFu;
+                if ((imask >> i) & 1u) int_keys |= 1u << (uint32_t(i) ^ r.oct);
+                else tri_mask |= (meta >> 5) << (meta & 31u);
+            }
+        }
+        g_base = L1.x;
+        g_hits = int_keys;
+        g_imask = imask;
+
+        const uint32_t tri_base = L1.y;
+        while (tri_mask) {
+            const uint32_t bit = __ffs(tri_mask) - 1u;
+            tri_mask &= tri_mask - 1u;
+            const uint32_t ti = tri_base + bit;
+            if (ti >= sc.tri_count) { status |= MRT_STATUS_BAD_TRI; tri_mask = 0u; g_hits = 0u; sp = 0; break; }
+            if (kCount) ++cnt_tris;
+            const float4* tp = sc.tris + size_t(ti) * 3u;
+            const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), c = __ldg(tp + 2);
+            float t;
+            if (intersect_tri(r, a, b, c, tmin, t)) {
+                const uint32_t id = __float_as_uint(a.w);
+                if (kAnyHit) {
+                    if (t < tmax) { best = id; tbest = t; tri_mask = 0u; g_hits = 0u; sp = 0; break; }
+                } else if (t < tbest || (t == tbest && id < best)) {
+                    tbest = t;
+                    best = id;
+                }
+            }
+        }
+    }
+    hit_prim = best;
+    hit_t = best == kMiss ? tmax : tbest;
+}
+
+// Reference ray/sphere test (intersect.glsl:26-37): the nearer root of
+// |o + t d - c|^2 = r^2, or -1 when the discriminant is negative.  It never
+// returns the far root, so an origin inside a sphere reads as t < 0.
+MRT_DEV float ray_sphere(f3 o, f3 d, f3 c, float radius) {
+    const f3 oc = sub_rn(o, c);
+    const float a = dot_rn(d, d);
+    const float half_b = dot_rn(oc, d);
+    const float cc = __fsub_rn(dot_rn(oc, oc), __fmul_rn(radius, radius));
+    const float disc = __fsub_rn(__fmul_rn(half_b, half_b), __fmul_rn(a, cc));
+    if (disc < 0.0f) return -1.0f;
+    return __fdiv_rn(__fsub_rn(-half_b, __fsqrt_rn(disc)), a);
+}
+
+} // namespace mrt

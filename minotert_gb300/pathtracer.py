@@ -1,0 +1,198 @@
+"""Host mirror of MinoteRT's path-tracer module over the mrt_cuda C ABI.
+
+Keeps the reference's interface (src/gfx/modules/pathtracer.ixx:18-200,
+src/gfx/camera.ixx:10-44) so a renderer written against it switches over
+by changing the device layer only:
+
+    Camera(viewport, verticalFov, nearPlane, position, yaw, pitch)
+        .view(), .projection(), .direction()
+    Pathtracer.primaryRays(size, camera, prevCamera) -> GBuffer
+    Pathtracer.secondaryRays(gbuffer, camera, sky, blueNoise) -> color
+
+Differences, by design: the scene is a Pathtracer member (the reference
+compiles its 5 spheres into the shaders, scene.glsl:4-11); `sky` is a Sky
+(constant radiance + optional directional light) in place of the
+atmosphere LUTs; errors raise MrtError (the reference throws
+runtime_error_fmt, src/stx/except.ixx:12-20); g-buffer images are device
+buffers owned by the returned GBuffer instead of vuk futures.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from ._lib import (MRT_EST_ESCAPE, MRT_EST_NEE, MRT_RNG_REFERENCE, Camera_C, CameraConsts, Context, DeviceBuffer,
+                   GBuffer as GBuffer_C, TraceParams, lib, ptr)
+from .scene import DeviceScene
+
+
+@dataclass
+class Camera:
+    """src/gfx/camera.ixx:10-26 (movement speeds omitted)."""
+    viewport: tuple
+    verticalFov: float
+    nearPlane: float
+    position: tuple
+    yaw: float
+    pitch: float
+
+    def direction(self) -> np.ndarray:
+        cp, sp = math.cos(self.pitch), math.sin(self.pitch)
+        return np.array([cp * math.cos(self.yaw), cp * math.sin(self.yaw), sp], np.float32)
+
+    def _c(self) -> Camera_C:
+        c = Camera_C()
+        c.viewport[0], c.viewport[1] = int(self.viewport[0]), int(self.viewport[1])
+        c.vertical_fov, c.near_plane = float(self.verticalFov), float(self.nearPlane)
+        for k in range(3):
+            c.position[k] = float(self.position[k])
+        c.yaw, c.pitch = float(self.yaw), float(self.pitch)
+        return c
+
+    def view(self) -> np.ndarray:
+        """4x4 column-major (m[col*4+row]) look(position, direction, +Z)."""
+        out = (C.c_float * 16)()
+        lib().mrt_camera_view(C.byref(self._c()), out)
+        return np.array(out[:], np.float32)
+
+    def projection(self) -> np.ndarray:
+        out = (C.c_float * 16)()
+        lib().mrt_camera_projection(C.byref(self._c()), out)
+        return np.array(out[:], np.float32)
+
+    @classmethod
+    def reference(cls, width: int, height: int) -> "Camera":
+        """The reference's start-up camera (src/app.ixx:20-32)."""
+        return cls((width, height), math.radians(60.0), 0.001, (0.0, -0.001, 0.1), math.radians(90.0), 0.0)
+
+
+def camera_consts(camera: Camera, prev: Camera | None = None, frame_counter: int = 0) -> CameraConsts:
+    """The per-dispatch constants of pathtracer.ixx:86-105 / 171-184."""
+    out = CameraConsts()
+    pc = (prev or camera)._c()
+    lib().mrt_camera_consts_make(C.byref(camera._c()), C.byref(pc), frame_counter, C.byref(out))
+    return out
+
+
+@dataclass
+class Sky:
+    """Light for the secondary pass: constant sky radiance on escape and an
+    optional directional light sampled with shadow rays."""
+    radiance: tuple = (0.25, 0.32, 0.45)
+    sun_dir: tuple | None = None
+    sun_irradiance: tuple = (2.5, 2.5, 2.5)
+
+
+@dataclass
+class TraceSettings:
+    samples: int = 8          # secondaryRays.comp:128
+    bounces: int = 8          # secondaryRays.comp:129
+    rr_start: int = 0
+    rng_mode: int = MRT_RNG_REFERENCE
+    accumulate: bool = False
+    frame_index: int = 0
+    sort_rays: bool = False
+
+    def params(self, sky: Sky) -> TraceParams:
+        p = TraceParams()
+        p.samples, p.max_bounces, p.rr_start = self.samples, self.bounces, self.rr_start
+        p.rng_mode = self.rng_mode
+        p.estimator = MRT_EST_NEE if sky.sun_dir is not None else MRT_EST_ESCAPE
+        p.accumulate, p.frame_index, p.sort_rays = int(self.accumulate), self.frame_index, int(self.sort_rays)
+        sd = np.asarray(sky.sun_dir if sky.sun_dir is not None else (0.0, 0.0, 1.0), np.float64)
+        sd = (sd / np.linalg.norm(sd)).astype(np.float32)
+        for k in range(3):
+            p.sun_dir[k] = float(sd[k])
+            p.sun_irradiance[k] = float(sky.sun_irradiance[k])
+            p.sky_radiance[k] = float(sky.radiance[k])
+        return p
+
+
+@dataclass
+class GBuffer:
+    """pathtracer.ixx:22-27: visibility R32_UINT, depth R16F, normal RGBA16F,
+    motion RG16F, plus the FP32 hit distance of the triangle path."""
+    width: int
+    height: int
+    visibility: DeviceBuffer
+    hit_t: DeviceBuffer
+    depth: DeviceBuffer
+    normal: DeviceBuffer
+    motion: DeviceBuffer
+    _c: GBuffer_C = field(default=None, repr=False)
+
+    def c(self) -> GBuffer_C:
+        if self._c is None:
+            g = GBuffer_C()
+            g.visibility, g.hit_t = self.visibility.ptr, self.hit_t.ptr
+            g.depth = self.depth.ptr if self.depth is not None else None
+            g.normal = self.normal.ptr if self.normal is not None else None
+            g.motion = self.motion.ptr if self.motion is not None else None
+            g.width, g.height = self.width, self.height
+            self._c = g
+        return self._c
+
+    def download(self) -> dict:
+        n = self.width * self.height
+        out = {"visibility": self.visibility.download(np.uint32, (self.height, self.width)),
+               "hit_t": self.hit_t.download(np.float32, (self.height, self.width))}
+        if self.depth is not None:
+            out["depth"] = self.depth.download(np.uint16, (self.height, self.width))
+        if self.normal is not None:
+            out["normal"] = self.normal.download(np.uint16, (self.height, self.width, 4))
+        if self.motion is not None:
+            out["motion"] = self.motion.download(np.uint16, (self.height, self.width, 2))
+        return out
+
+
+class Pathtracer:
+    """Pathtracer (pathtracer.ixx:18-200) over one scene on one context."""
+
+    def __init__(self, ctx: Context, scene: DeviceScene, full_gbuffer: bool = True):
+        self.ctx, self.scene = ctx, scene
+        self.full_gbuffer = full_gbuffer
+        self._gb = None
+        self._bn_id = None
+        self.frame_counter = 0
+
+    def _gbuffer(self, w: int, h: int) -> GBuffer:
+        if self._gb is None or (self._gb.width, self._gb.height) != (w, h):
+            n = w * h
+            full = self.full_gbuffer or self.scene.kind == "spheres"
+            a = self.ctx.alloc
+            self._gb = GBuffer(w, h, a(4 * n), a(4 * n), a(2 * n) if full else None, a(8 * n) if full else None,
+                               a(4 * n) if full else None)
+        return self._gb
+
+    def primaryRays(self, size, camera: Camera, prevCamera: Camera, stream=None) -> GBuffer:
+        w, h = int(size[0]), int(size[1])
+        g = self._gbuffer(w, h)
+        consts = camera_consts(camera, prevCamera, self.frame_counter)
+        self.ctx.check(lib().mrt_cuda_primary_rays(self.ctx.handle, self.scene.handle, C.byref(consts),
+                                                   C.byref(g.c()), ptr(stream)), "primaryRays")
+        return g
+
+    def secondaryRays(self, gbuffer: GBuffer, camera: Camera, sky: Sky, blueNoise: np.ndarray,
+                      settings: TraceSettings | None = None, color: DeviceBuffer | None = None,
+                      stream=None) -> DeviceBuffer:
+        settings = settings or TraceSettings()
+        if self._bn_id is not id(blueNoise):
+            self.ctx.blue_noise(blueNoise)
+            self._bn_id = id(blueNoise)
+        color = color or self.ctx.alloc(12 * gbuffer.width * gbuffer.height)
+        consts = camera_consts(camera, camera, self.frame_counter)
+        params = settings.params(sky)
+        self.ctx.check(lib().mrt_cuda_secondary_rays(self.ctx.handle, self.scene.handle, C.byref(gbuffer.c()),
+                                                     C.byref(consts), C.byref(params), C.c_void_p(color.ptr),
+                                                     ptr(stream)), "secondaryRays")
+        return color
+
+    # snake_case aliases
+    primary_rays = primaryRays
+    secondary_rays = secondaryRays
+
+    def next_frame(self):
+        self.frame_counter += 1

@@ -1,0 +1,142 @@
+"""Host-side scene modules: procedural meshes, the BVH8 builder and the
+device upload (mrt_host.h / mrt_cuda_scene_upload_*)."""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._lib import (MAT_DTYPE, NODE_DTYPE, SPHERE_DTYPE, TRI_DTYPE, Bvh8_C, BvhBuildParams, Context, Mesh_C, MrtError,
+                   lib, ptr)
+
+
+@dataclass
+class Mesh:
+    verts: np.ndarray   # (n, 9) float32: v0 v1 v2
+    mats: np.ndarray    # (n,) MAT_DTYPE: unit normal + RGBA8 albedo
+    lo: np.ndarray
+    hi: np.ndarray
+
+    @property
+    def tri_count(self) -> int:
+        return int(self.verts.shape[0])
+
+    def albedo(self) -> np.ndarray:
+        a = self.mats["albedo"]
+        return np.stack([(a >> s) & 0xFF for s in (0, 8, 16)], axis=1).astype(np.float32) / np.float32(255.0)
+
+
+def _take_mesh(m: Mesh_C) -> Mesh:
+    n = m.tri_count
+    verts = np.ctypeslib.as_array(m.verts, shape=(n * 9,)).reshape(n, 9).copy()
+    mats = np.frombuffer((C.c_char * (n * 16)).from_address(m.materials), dtype=MAT_DTYPE, count=n).copy()
+    mesh = Mesh(verts, mats, np.array(m.bounds_lo[:], np.float32), np.array(m.bounds_hi[:], np.float32))
+    lib().mrt_mesh_free(C.byref(m))
+    return mesh
+
+
+def heightfield_boxes(seed: int = 1, grid: int = 64, boxes: int = 32) -> Mesh:
+    """Heightfield (grid x grid cells, 4 sine octaves) + axis-aligned boxes."""
+    m = Mesh_C()
+    rc = lib().mrt_scene_heightfield_boxes(seed, grid, boxes, C.byref(m))
+    if rc:
+        raise MrtError(rc, "mrt_scene_heightfield_boxes")
+    return _take_mesh(m)
+
+
+def icospheres(seed: int = 1, spheres: int = 200, levels: int = 4, rmin: float = 0.2, rmax: float = 5.0,
+               ground_tris: int = 10240) -> Mesh:
+    """Perlin-displaced icospheres on a ground plane."""
+    m = Mesh_C()
+    rc = lib().mrt_scene_icospheres(seed, spheres, levels, rmin, rmax, ground_tris, C.byref(m))
+    if rc:
+        raise MrtError(rc, "mrt_scene_icospheres")
+    return _take_mesh(m)
+
+
+def concat(meshes) -> Mesh:
+    verts = np.concatenate([m.verts for m in meshes])
+    mats = np.concatenate([m.mats for m in meshes])
+    return Mesh(verts, mats, verts.reshape(-1, 3).min(0), verts.reshape(-1, 3).max(0))
+
+
+@dataclass
+class Bvh8:
+    nodes: np.ndarray   # NODE_DTYPE
+    tris: np.ndarray    # TRI_DTYPE (leaf order)
+    depth: int
+    leaf_count: int
+    build_ms: float
+
+
+def build_bvh8(mesh_or_verts, bins: int = 32, threads: int = 0) -> Bvh8:
+    verts = mesh_or_verts.verts if isinstance(mesh_or_verts, Mesh) else np.asarray(mesh_or_verts)
+    verts = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 9)
+    out = Bvh8_C()
+    params = BvhBuildParams(bins, 3, threads, 0)
+    rc = lib().mrt_bvh8_build(ptr(verts), verts.shape[0], C.byref(params), C.byref(out))
+    if rc:
+        raise MrtError(rc, "mrt_bvh8_build")
+    nodes = np.frombuffer((C.c_char * (out.node_count * 128)).from_address(out.nodes), dtype=NODE_DTYPE).copy()
+    tris = np.frombuffer((C.c_char * (out.tri_count * 48)).from_address(out.tris), dtype=TRI_DTYPE).copy()
+    res = Bvh8(nodes, tris, out.depth, out.leaf_count, out.build_ms)
+    lib().mrt_bvh8_free(C.byref(out))
+    return res
+
+
+def reference_spheres() -> np.ndarray:
+    """The reference's 5 spheres (src/gpu/scene.glsl:4-11)."""
+    s = np.zeros(5, dtype=SPHERE_DTYPE)
+    lib().mrt_scene_reference(ptr(s))
+    return s
+
+
+def blue_noise(seed: int = 1, size: int = 64) -> np.ndarray:
+    """size x size x 4 RGBA8 blue-noise tile (void-and-cluster)."""
+    out = np.zeros((size, size, 4), dtype=np.uint8)
+    rc = lib().mrt_blue_noise_generate(seed, size, ptr(out))
+    if rc:
+        raise MrtError(rc, "mrt_blue_noise_generate")
+    return out
+
+
+class DeviceScene:
+    """A scene uploaded to one context (mrt_scene)."""
+
+    def __init__(self, ctx: Context, handle: C.c_void_p, kind: str, mesh: Mesh | None = None,
+                 bvh: Bvh8 | None = None, spheres: np.ndarray | None = None):
+        self.ctx, self._h, self.kind = ctx, handle, kind
+        self.mesh, self.bvh, self.spheres = mesh, bvh, spheres
+
+    @property
+    def handle(self):
+        return self._h
+
+    @classmethod
+    def triangles(cls, ctx: Context, mesh: Mesh, bvh: Bvh8 | None = None) -> "DeviceScene":
+        bvh = bvh or build_bvh8(mesh)
+        h = C.c_void_p()
+        ctx.check(lib().mrt_cuda_scene_upload_triangles(ctx.handle, ptr(bvh.nodes), len(bvh.nodes), ptr(bvh.tris),
+                                                         len(bvh.tris), ptr(mesh.mats), len(mesh.mats), C.byref(h)),
+                  "scene_upload_triangles")
+        return cls(ctx, h, "triangles", mesh=mesh, bvh=bvh)
+
+    @classmethod
+    def from_spheres(cls, ctx: Context, spheres: np.ndarray) -> "DeviceScene":
+        spheres = np.ascontiguousarray(spheres, dtype=SPHERE_DTYPE)
+        h = C.c_void_p()
+        ctx.check(lib().mrt_cuda_scene_upload_spheres(ctx.handle, ptr(spheres), len(spheres), C.byref(h)),
+                  "scene_upload_spheres")
+        return cls(ctx, h, "spheres", spheres=spheres)
+
+    def close(self):
+        if self._h and self.ctx.handle:
+            lib().mrt_cuda_scene_destroy(self.ctx.handle, self._h)
+        self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,142 @@
+"""Host modules and the C-ABI library, CPU only (no kernel launches)."""
+import ctypes
+import hashlib
+import json
+import math
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import oracle_consts
+
+ROOT = Path(__file__).resolve().parent.parent
+GOLD = json.loads((Path(__file__).parent / "golden" / "known_answers.json").read_text())
+
+
+def _declared_symbols():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        txt = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(mrt_\w+)\s*\(", txt, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    lib = ctypes.CDLL(str(built_lib))
+    names = _declared_symbols()
+    assert len(names) > 40
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_abi_version(built_lib):
+    from minotert_gb300._lib import lib
+    assert lib().mrt_cuda_abi_version() == 1
+
+
+def test_struct_layouts(built_lib):
+    from minotert_gb300 import _lib as L
+    assert ctypes.sizeof(L.CameraConsts) == 336
+    assert ctypes.sizeof(L.TraceParams) == 80
+    assert ctypes.sizeof(L.GBuffer) == 48
+    assert L.NODE_DTYPE.itemsize == 128
+
+
+def test_scene_generators_are_deterministic(built_lib):
+    from minotert_gb300 import workloads
+    m = workloads.heightfield_boxes_256().mesh()
+    g = GOLD["heightfield_boxes_seed1"]
+    assert m.tri_count == g["tris"] == 64 * 64 * 2 + 32 * 12
+    assert hashlib.sha256(m.verts.tobytes()).hexdigest() == g["verts_sha256"]
+    assert hashlib.sha256(m.mats.tobytes()).hexdigest() == g["mats_sha256"]
+    a = m.albedo()
+    assert a.min() >= 0.19 and a.max() <= 0.81
+    assert np.allclose(np.linalg.norm(m.mats["normal"], axis=1), 1.0, atol=1e-5)
+
+
+def test_icosphere_scene_size(built_lib):
+    from minotert_gb300 import workloads
+    m = workloads.icospheres_1080p().mesh()
+    g = GOLD["icospheres_seed1"]
+    assert m.tri_count == g["tris"] == 200 * 5120 + 10240
+    assert hashlib.sha256(m.verts.tobytes()).hexdigest() == g["verts_sha256"]
+
+
+def test_blue_noise_tile(built_lib):
+    from minotert_gb300 import scene
+    bn = scene.blue_noise(1, 64)
+    assert bn.shape == (64, 64, 4)
+    assert hashlib.sha256(bn.tobytes()).hexdigest() == GOLD["blue_noise_seed1_64"]["sha256"]
+    for ch in range(4):
+        hist = np.bincount(bn[..., ch].ravel(), minlength=256)
+        assert hist.min() == hist.max() == 16  # every level equally often
+    # blue noise: low-frequency energy well below white noise
+    x = bn[..., 0].astype(np.float64) - 127.5
+    f = np.abs(np.fft.fft2(x)) ** 2
+    low = f[1:4, 1:4].mean()
+    assert low < 0.2 * f[1:, 1:].mean()
+
+
+def test_camera_consts_match_oracle(built_lib, hf_workload):
+    from minotert_gb300.pathtracer import Camera, camera_consts
+    wl, _, _ = hf_workload
+    prev = Camera(wl.camera.viewport, wl.camera.verticalFov, wl.camera.nearPlane, (1.0, -26.0, 13.5),
+                  wl.camera.yaw + 0.01, wl.camera.pitch)
+    for cam, pv in ((wl.camera, None), (Camera.reference(960, 540), None), (wl.camera, prev)):
+        ours = np.frombuffer(bytes(camera_consts(cam, pv or cam, 7)), np.uint32)
+        ref = oracle_consts(cam, 7, pv).view(np.uint32)
+        assert np.array_equal(ours, ref)
+
+
+def test_bvh_build_quality_and_validity(built_lib, ico_workload):
+    _, mesh, bvh = ico_workload
+    info = oracle.bvh8_validate(bvh.nodes, bvh.tris, mesh.verts)
+    assert info["error"] == 0
+    assert bvh.depth <= 32
+    assert len(bvh.tris) == mesh.tri_count
+    # roughly one node per 8 triangles for a full 8-wide tree
+    assert len(bvh.nodes) < mesh.tri_count / 6
+
+
+def test_bvh_degenerate_inputs(built_lib):
+    from minotert_gb300 import scene
+    # one triangle, coincident triangles, zero-area triangles
+    one = np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32)
+    b = scene.build_bvh8(one)
+    assert len(b.nodes) == 1 and len(b.tris) == 1
+    same = np.repeat(one, 100, axis=0)
+    b = scene.build_bvh8(same)
+    assert oracle.bvh8_validate(b.nodes, b.tris, same)["error"] == 0
+    flat = np.zeros((50, 9), np.float32)
+    flat[:, 0::3] = np.arange(50)[:, None]
+    b = scene.build_bvh8(flat)
+    assert oracle.bvh8_validate(b.nodes, b.tris, flat)["error"] == 0
+    with pytest.raises(Exception):
+        scene.build_bvh8(np.zeros((0, 9), np.float32))
+    bad = one.copy()
+    bad[0, 0] = np.nan
+    with pytest.raises(Exception):
+        scene.build_bvh8(bad)
+
+
+def test_reference_scene_and_camera(built_lib):
+    from minotert_gb300 import scene
+    from minotert_gb300.pathtracer import Camera
+    s = scene.reference_spheres()
+    assert len(s) == 5
+    assert s["radius"][4] == np.float32(0.1) and s["center"][0][1] == np.float32(0.0017)
+    c = Camera.reference(960, 540)
+    assert np.allclose(c.direction(), [0, 1, 0], atol=1e-7)
+
+
+def test_product_library_fails_loudly_without_gpu(built_lib):
+    from minotert_gb300._lib import Context, MrtError
+    from conftest import _has_gpu
+    if _has_gpu():
+        pytest.skip("GPU present")
+    with pytest.raises(MrtError):
+        Context(0)
