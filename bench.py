@@ -1,0 +1,385 @@
+#!/usr/bin/env python
+"""Mrays/s of the GB300 path tracer on the 1.03M-triangle icosphere field.
+
+A step is one frame of the hot path on 1920x1080: primary rays (BVH8
+closest hit) plus a 4-bounce Lambertian path trace with Russian roulette
+after bounce 2 and a directional-light shadow ray per vertex, accumulated
+into RGB32F.  `value` counts primary + diffuse extension rays per second
+with the scene resident in HBM and the L2 flushed between timed steps;
+`e2e` is the same metric through mrt_cuda_render_frame_host with host
+buffers (results copied back every step).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mine|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mrays/s (primary, diffuse) at 1 GB300; GPU ms to target RMSE: learned vs plain"
+UNIT = "Mrays/s"
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # host-side barrier / max only; the path has no collective
+        dist.init_process_group("gloo")
+    return world, rank, local, dist
+
+
+def _allmax(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _allsum(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu, self.rows, self.proc, self.th = gpu, [], None, None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.th = threading.Thread(target=self._read, daemon=True)
+        self.th.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self) -> dict:
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.th is not None:
+            self.th.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def _workload():
+    from minotert_gb300 import scene, workloads
+    wl = workloads.icospheres_1080p()
+    t0 = time.perf_counter()
+    mesh = wl.mesh()
+    t1 = time.perf_counter()
+    bvh = scene.build_bvh8(mesh)
+    return wl, mesh, bvh, {"scene_gen_ms": (t1 - t0) * 1e3, "bvh_build_ms": bvh.build_ms}
+
+
+def _config(wl, mesh, bvh, extra=None):
+    c = {"workload": wl.name, "triangles": mesh.tri_count, "bvh8_nodes": int(len(bvh.nodes)),
+         "width": wl.width, "height": wl.height, "spp": wl.settings.samples, "bounces": wl.settings.bounces,
+         "rr_after_bounce": wl.settings.rr_start, "light": "directional (shadow ray per vertex) + constant sky",
+         "l2": "256 MiB memset between timed steps (scene 69 MB < L2 129 MB)", "parallelism": "replicas"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def cpu_baseline(wl, mesh, bvh, bn, budget_s: float = 12.0, threads: int | None = None) -> dict:
+    """The FP32 oracle (scalar C++, one std::thread per core) on a bounded
+    band of rows of the same frame: primary + path trace, rays per second."""
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    c = wl.camera
+    consts = oracle.camera_consts(c.position, c.yaw, c.pitch, c.verticalFov, c.nearPlane, wl.width, wl.height)
+    sd = np.asarray(wl.sky.sun_dir, np.float64)
+    sd = (sd / np.linalg.norm(sd)).astype(np.float32)
+    s = wl.settings
+    prm = oracle.params_array(s.samples, s.bounces, s.rr_start, s.rng_mode, 1, sun=sd, sun_e=wl.sky.sun_irradiance,
+                              sky=wl.sky.radiance)
+    rows, y0, rays, secs = 16, 0, 0, 0.0
+    color = np.zeros((wl.height, wl.width, 3), np.float32)
+    done_rows = 0
+    # bands of rows (wrapping to the next frame) until the budget is spent
+    while secs < budget_s:
+        y1 = min(wl.height, y0 + rows)
+        frame = done_rows // wl.height
+        consts = oracle.camera_consts(c.position, c.yaw, c.pitch, c.verticalFov, c.nearPlane, wl.width, wl.height,
+                                      frame=frame)
+        t0 = time.perf_counter()
+        p = oracle.primary(consts, wl.width, wl.height, bvh.nodes, bvh.tris, mesh.mats, threads=threads, y0=y0, y1=y1)
+        _, counts, _ = oracle.pathtrace(bvh.nodes, bvh.tris, mesh.mats, consts, wl.width, wl.height, p["visibility"],
+                                        p["hit_t"], bn, prm, y0=y0, y1=y1, color=color, threads=threads)
+        dt = time.perf_counter() - t0
+        secs += dt
+        rays += int(counts[0]) + int(counts[1])
+        done_rows += y1 - y0
+        y0 = y1 if y1 < wl.height else 0
+        rows = max(16, min(wl.height - y0 if y0 else wl.height, int(rows * 1.5)))
+    return {"value": rays / secs / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{done_rows / wl.height:.2f} frames of 1920x1080 in row bands (primary + 4-bounce path trace, "
+                      f"FP32 oracle, all host threads), {secs:.1f} s", "rays": rays, "seconds": secs}
+
+
+def run_mine(args, world, rank, local, dist):
+    from minotert_gb300 import build as _build
+    _build.build()
+    from minotert_gb300 import scene
+    from minotert_gb300._lib import Context, lib, ptr
+    from minotert_gb300.pathtracer import Pathtracer, TraceSettings, camera_consts
+    import ctypes as C
+
+    wl, mesh, bvh, build_info = _workload()
+    bn = scene.blue_noise(1, 64)
+    ctx = Context(local)
+    ds = scene.DeviceScene.triangles(ctx, mesh, bvh)
+    ctx.blue_noise(bn)
+    pt = Pathtracer(ctx, ds, full_gbuffer=False)
+    W, H = wl.width, wl.height
+    color = ctx.alloc(12 * W * H)
+    flush = ctx.alloc(256 << 20)
+    stream = ctx.stream()
+    s = wl.settings
+
+    def frame(f):
+        pt.frame_counter = f
+        gb = pt.primaryRays((W, H), wl.camera, wl.camera, stream)
+        pt.secondaryRays(gb, wl.camera, wl.sky, bn, TraceSettings(s.samples, s.bounces, s.rr_start, s.rng_mode),
+                         color=color, stream=stream)
+
+    for f in range(args.warmup):
+        frame(f)
+    ctx.sync(stream)
+    ctx.frame_stats()
+    assert ctx.status() == 0
+
+    ev = [(ctx.event(), ctx.event()) for _ in range(args.steps)]
+    ctx.set_timing(True)
+    if dist is not None:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    for k in range(args.steps):
+        flush.zero(stream)
+        ctx.record(ev[k][0], stream)
+        frame(args.warmup + k)
+        ctx.record(ev[k][1], stream)
+    ctx.sync(stream)
+    clk = clocks.stop()
+    ms = [ctx.elapsed_ms(a, b) for a, b in ev]
+    st = ctx.frame_stats()
+    ctx.set_timing(False)
+    if dist is not None:
+        dist.barrier()
+    status = ctx.status()
+    total_ms = sum(ms)
+    prim = int(st.primary_rays)
+    ext = [int(x) for x in st.extension_rays]
+    rays = prim + sum(ext)
+    max_s = _allmax(dist, total_ms / 1e3)
+    all_rays = _allsum(dist, float(rays))
+    value = all_rays / max_s / 1e6
+
+    # traversal work per ray (counting form of the same kernels, one frame)
+    ctx.set_counters(True)
+    frame(args.warmup + args.steps)
+    ctx.sync(stream)
+    cs = ctx.frame_stats()
+    ctx.set_counters(False)
+    ext_rays = sum(int(x) for x in cs.extension_rays)
+    n_node_ext = sum(int(x) for x in cs.nodes_extension) / max(ext_rays, 1)
+    n_tri_ext = sum(int(x) for x in cs.tris_extension) / max(ext_rays, 1)
+    n_node_prim = cs.nodes_primary / max(cs.primary_rays, 1)
+    n_tri_prim = cs.tris_primary / max(cs.primary_rays, 1)
+    n_node_sh = cs.nodes_shadow / max(cs.shadow_rays, 1)
+    n_tri_sh = cs.tris_shadow / max(cs.shadow_rays, 1)
+
+    def bytes_per_ray(nn, nt):  # algorithmic bytes per ray: ray + hit + nodes + triangles
+        return 32 + 16 + 128 * nn + 48 * nt
+
+    kernels = {
+        "extend": (st.ms_extend, ext_rays and sum(ext) * bytes_per_ray(n_node_ext, n_tri_ext)),
+        "primary": (st.ms_primary, prim * bytes_per_ray(n_node_prim, n_tri_prim)),
+        "shadow": (st.ms_shadow, int(st.shadow_rays) * bytes_per_ray(n_node_sh, n_tri_sh)),
+        "shade": (st.ms_shade, None),
+    }
+    dom = max(kernels, key=lambda k: kernels[k][0])
+    peaks = _peaks()
+    dk_ms, dk_bytes = kernels["extend"] if kernels[dom][1] is None else kernels[dom]
+    dname = "extend" if kernels[dom][1] is None else dom
+    achieved = dk_bytes / (dk_ms / 1e3) / 1e9 if dk_ms > 0 else 0.0
+    launches_per_frame = {"extend": s.bounces, "primary": 1, "shadow": s.bounces + 1}[dname]
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if tfile.exists():
+        tj = json.loads(tfile.read_text()).get(wl.name, {}).get(dname)
+        if tj:
+            traffic = tj["bytes_per_ray"] * (dk_bytes / bytes_per_ray(
+                *{"extend": (n_node_ext, n_tri_ext), "primary": (n_node_prim, n_tri_prim),
+                  "shadow": (n_node_sh, n_tri_sh)}[dname])) / (args.steps * launches_per_frame)
+    roofline = {"bound": "hbm", "kernel": f"k_trace_{'ext' if dname == 'extend' else dname}",
+                "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                "traffic": traffic, "bytes_per_ray": bytes_per_ray(
+                    *{"extend": (n_node_ext, n_tri_ext), "primary": (n_node_prim, n_tri_prim),
+                      "shadow": (n_node_sh, n_tri_sh)}[dname]),
+                "nodes_per_ray": {"primary": n_node_prim, "extension": n_node_ext, "shadow": n_node_sh},
+                "tris_per_ray": {"primary": n_tri_prim, "extension": n_tri_ext, "shadow": n_tri_sh},
+                "note": "bytes/ray = 32 + 16 + 128 N_node + 48 N_tri with N from the counting kernels "
+                        "(equal to the oracle's counts); the scene (69 MB) is L2-resident, so a fraction "
+                        "above 1 of the HBM copy peak means the traversal runs out of L2"}
+
+    b2 = sum(ext[1:])
+    b2_ms = sum(st.ms_extend_b[1:s.bounces])
+    breakdown = {
+        "primary_mrays_s": prim / (st.ms_primary / 1e3) / 1e6 if st.ms_primary else None,
+        "bounce1_mrays_s": ext[0] / (st.ms_extend_b[0] / 1e3) / 1e6 if st.ms_extend_b[0] else None,
+        "bounce2plus_mrays_s": b2 / (b2_ms / 1e3) / 1e6 if b2_ms else None,
+        "shadow_mrays_s": st.shadow_rays / (st.ms_shadow / 1e3) / 1e6 if st.ms_shadow else None,
+        "all_rays_incl_shadow_mrays_s": (rays + int(st.shadow_rays)) / (total_ms / 1e3) / 1e6,
+        "rays_per_frame": {"primary": prim / args.steps, "extension": [e / args.steps for e in ext[:s.bounces]],
+                           "shadow": st.shadow_rays / args.steps},
+        "ms_per_frame": {"primary": st.ms_primary / args.steps, "extend": st.ms_extend / args.steps,
+                         "shadow": st.ms_shadow / args.steps, "shade": st.ms_shade / args.steps},
+    }
+
+    # end to end through the C ABI with host buffers
+    vis_h = ctx.host_alloc((H, W), np.uint32)
+    t_h = ctx.host_alloc((H, W), np.float32)
+    col_h = ctx.host_alloc((H, W, 3), np.float32)
+    params = TraceSettings(s.samples, s.bounces, s.rr_start, s.rng_mode).params(wl.sky)
+    e2e_ms = []
+    ctx.frame_stats()
+    for k in range(args.warmup + args.steps):
+        consts = camera_consts(wl.camera, wl.camera, k)
+        if k == args.warmup:
+            ctx.frame_stats()
+        t0 = time.perf_counter()
+        ctx.check(lib().mrt_cuda_render_frame_host(ctx.handle, ds.handle, C.byref(consts), C.byref(params), W, H,
+                                                   ptr(vis_h), ptr(t_h), ptr(col_h), C.c_void_p(stream)), "frame")
+        if k >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    est = ctx.frame_stats()
+    e2e_rays = int(est.primary_rays) + sum(int(x) for x in est.extension_rays)
+    e2e_val = _allsum(dist, float(e2e_rays)) / _allmax(dist, sum(e2e_ms) / 1e3) / 1e6
+    e2e = {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 336 + 80,
+           "d2h_bytes_per_step": W * H * (4 + 4 + 12), "ms_per_step": statistics.mean(e2e_ms),
+           "api": "mrt_cuda_render_frame_host"}
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": _allmax(dist, total_ms / args.steps), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+           "config": _config(wl, mesh, bvh, build_info), "breakdown": breakdown, "roofline": roofline,
+           "e2e": e2e, "gpu_launches": int(st.launches), "clocks": clk, "device_status": status}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(wl, mesh, bvh, bn)
+    if rank == 0:
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_reference(args, world, rank, local, dist):
+    """The reference path on the host cores: MinoteRT's own implementation
+    is Vulkan + MSVC only and cannot run here, so its CPU restatement (the
+    oracle) runs the same frame, a bounded band of rows per step."""
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    wl, mesh, bvh, build_info = _workload()
+    from minotert_gb300 import scene
+    bn = scene.blue_noise(1, 64)
+    per_step = max(1.0, min(6.0, 150.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        cpu_baseline(wl, mesh, bvh, bn, budget_s=min(per_step, 2.0))
+    vals, rays, secs = [], 0, 0.0
+    for _ in range(args.steps):
+        r = cpu_baseline(wl, mesh, bvh, bn, budget_s=per_step)
+        vals.append(r["value"])
+        rays += r["rays"]
+        secs += r["seconds"]
+    value = rays / secs / 1e6
+    cores = os.cpu_count() or 1
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+           "config": _config(wl, mesh, bvh, build_info), "impl": "reference",
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": f"per step ~{per_step:.1f} s of rows of the 1920x1080 frame; the reference's "
+                                      "Vulkan/MSVC build cannot run on this box, its FP32 CPU restatement runs"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args(argv)
+    args.warmup = max(args.warmup, 3)
+    world, rank, local, dist = _dist()
+    if args.impl == "reference":
+        run_reference(args, world, rank, local, dist)
+    else:
+        run_mine(args, world, rank, local, dist)
+
+
+if __name__ == "__main__":
+    main()

@@ -191,6 +191,11 @@ typedef struct mrt_frame_stats {
     uint64_t primary_rays;
     uint64_t extension_rays[MRT_MAX_BOUNCES]; /* rays traced at bounce b+1   */
     uint64_t shadow_rays;
+    /* traversal work, filled when counters are enabled
+     * (mrt_cuda_set_counters): BVH8 nodes and triangles visited */
+    uint64_t nodes_primary, tris_primary;
+    uint64_t nodes_extension[MRT_MAX_BOUNCES], tris_extension[MRT_MAX_BOUNCES];
+    uint64_t nodes_shadow, tris_shadow;
     float    ms_primary;     /* primary closest-hit kernel                   */
     float    ms_extend;      /* all extension (closest-hit) kernels          */
     float    ms_extend_b[MRT_MAX_BOUNCES];
@@ -220,6 +225,11 @@ int mrt_cuda_status(mrt_ctx* ctx, uint32_t* flags, int clear);
 int mrt_cuda_sync(mrt_ctx* ctx, void* stream, double timeout_s);
 /* Enables per-kernel CUDA-event timing into mrt_frame_stats. */
 int mrt_cuda_set_timing(mrt_ctx* ctx, int enable);
+/* Runs the traversal kernels in their counting form (nodes / triangles
+ * visited per ray, summed into mrt_frame_stats).  Slower; for profiling. */
+int mrt_cuda_set_counters(mrt_ctx* ctx, int enable);
+/* Returns the statistics accumulated since the previous call and resets
+ * them; synchronises the context. */
 int mrt_cuda_frame_stats(mrt_ctx* ctx, mrt_frame_stats* out);
 
 /* ---- memory and streams (the reference's vuk allocator role,

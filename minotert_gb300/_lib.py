@@ -60,7 +60,9 @@ class TraceParams(C.Structure):
 
 class FrameStats(C.Structure):
     _fields_ = [("primary_rays", C.c_uint64), ("extension_rays", C.c_uint64 * MRT_MAX_BOUNCES),
-                ("shadow_rays", C.c_uint64), ("ms_primary", C.c_float), ("ms_extend", C.c_float),
+                ("shadow_rays", C.c_uint64), ("nodes_primary", C.c_uint64), ("tris_primary", C.c_uint64),
+                ("nodes_extension", C.c_uint64 * MRT_MAX_BOUNCES), ("tris_extension", C.c_uint64 * MRT_MAX_BOUNCES),
+                ("nodes_shadow", C.c_uint64), ("tris_shadow", C.c_uint64), ("ms_primary", C.c_float), ("ms_extend", C.c_float),
                 ("ms_extend_b", C.c_float * MRT_MAX_BOUNCES), ("ms_shadow", C.c_float), ("ms_shade", C.c_float),
                 ("ms_sort", C.c_float), ("ms_total", C.c_float), ("launches", C.c_uint32), ("pad", C.c_uint32)]
 
@@ -115,6 +117,7 @@ def lib() -> C.CDLL:
             "mrt_cuda_status": ([vp, C.POINTER(u32), i32], i32),
             "mrt_cuda_sync": ([vp, vp, C.c_double], i32),
             "mrt_cuda_set_timing": ([vp, i32], i32),
+            "mrt_cuda_set_counters": ([vp, i32], i32),
             "mrt_cuda_frame_stats": ([vp, C.POINTER(FrameStats)], i32),
             "mrt_cuda_alloc": ([vp, sz, pp], i32),
             "mrt_cuda_free": ([vp, vp], i32),
@@ -234,6 +237,9 @@ class Context:
 
     def set_timing(self, on: bool):
         self.check(lib().mrt_cuda_set_timing(self._h, 1 if on else 0), "set_timing")
+
+    def set_counters(self, on: bool):
+        self.check(lib().mrt_cuda_set_counters(self._h, 1 if on else 0), "set_counters")
 
     def frame_stats(self) -> FrameStats:
         st = FrameStats()

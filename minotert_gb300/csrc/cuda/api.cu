@@ -108,7 +108,7 @@ struct Scope {
 
 void free_wave(WaveBuffers& wb) {
     cudaFree(wb.q[0]); cudaFree(wb.q[1]); cudaFree(wb.hits); cudaFree(wb.sq); cudaFree(wb.L);
-    cudaFree(wb.rng); cudaFree(wb.counters); cudaFree(wb.totals); cudaFree(wb.keys); cudaFree(wb.perm);
+    cudaFree(wb.rng); cudaFree(wb.counters); cudaFree(wb.keys); cudaFree(wb.perm);
     cudaFree(wb.qsort); cudaFree(wb.hist);
     wb = WaveBuffers();
 }
@@ -119,8 +119,6 @@ int ensure_wave(mrt_ctx* ctx, size_t npix) {
         wb.npix = npix;
         return MRT_OK;
     }
-    unsigned long long* totals = wb.totals;
-    wb.totals = nullptr;
     free_wave(wb);
     size_t cap = npix;
     bool ok = cudaMalloc(&wb.q[0], cap * sizeof(PathRay)) == cudaSuccess &&
@@ -130,9 +128,7 @@ int ensure_wave(mrt_ctx* ctx, size_t npix) {
               cudaMalloc(&wb.L, npix * sizeof(float4)) == cudaSuccess &&
               cudaMalloc(&wb.rng, npix * sizeof(uint32_t)) == cudaSuccess &&
               cudaMalloc(&wb.counters, kCntSlots * sizeof(uint32_t)) == cudaSuccess;
-    if (ok && !totals) ok = cudaMalloc(&totals, 64 * sizeof(unsigned long long)) == cudaSuccess &&
-                            cudaMemset(totals, 0, 64 * sizeof(unsigned long long)) == cudaSuccess;
-    wb.totals = totals;
+    wb.totals = ctx->d_totals;
     if (!ok) {
         free_wave(wb);
         return fail(ctx, MRT_ENOMEM, "wavefront buffers for %zu rays: out of device memory", npix);
@@ -172,7 +168,11 @@ int mrt_cuda_create(mrt_ctx** out, int device) {
     ctx->device = device;
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (cudaMalloc(&ctx->d_status, sizeof(uint32_t)) != cudaSuccess ||
-        cudaMemset(ctx->d_status, 0, sizeof(uint32_t)) != cudaSuccess) {
+        cudaMemset(ctx->d_status, 0, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_totals, kTotSlots * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMemset(ctx->d_totals, 0, kTotSlots * sizeof(unsigned long long)) != cudaSuccess) {
+        cudaFree(ctx->d_status);
+        cudaFree(ctx->d_totals);
         delete ctx;
         return MRT_ENOMEM;
     }
@@ -186,6 +186,7 @@ int mrt_cuda_destroy(mrt_ctx* ctx) {
     cudaDeviceSynchronize();
     free_wave(ctx->wb);
     cudaFree(ctx->d_status);
+    cudaFree(ctx->d_totals);
     cudaFree(ctx->d_bn);
     cudaFree(ctx->d_vis);
     cudaFree(ctx->d_aux);
@@ -227,6 +228,12 @@ int mrt_cuda_set_timing(mrt_ctx* ctx, int enable) {
     return MRT_OK;
 }
 
+int mrt_cuda_set_counters(mrt_ctx* ctx, int enable) {
+    if (!ctx) return MRT_EINVAL;
+    ctx->counters = enable != 0;
+    return MRT_OK;
+}
+
 int mrt_cuda_frame_stats(mrt_ctx* ctx, mrt_frame_stats* out) {
     if (!ctx || !out) return MRT_EINVAL;
     cudaSetDevice(ctx->device);
@@ -251,12 +258,20 @@ int mrt_cuda_frame_stats(mrt_ctx* ctx, mrt_frame_stats* out) {
         ctx->ev_pool.push_back(r.b);
     }
     ctx->recs.clear();
-    if (ctx->wb.totals) {
-        unsigned long long tot[64];
-        MRT_CK(cudaMemcpy(tot, ctx->wb.totals, sizeof(tot), cudaMemcpyDeviceToHost));
-        MRT_CK(cudaMemset(ctx->wb.totals, 0, sizeof(tot)));
-        for (int b = 1; b <= MRT_MAX_BOUNCES; ++b) st.extension_rays[b - 1] += tot[kCntExt + b];
+    {
+        unsigned long long tot[kTotSlots];
+        MRT_CK(cudaMemcpy(tot, ctx->d_totals, sizeof(tot), cudaMemcpyDeviceToHost));
+        MRT_CK(cudaMemset(ctx->d_totals, 0, sizeof(tot)));
+        for (int b = 1; b <= MRT_MAX_BOUNCES; ++b) {
+            st.extension_rays[b - 1] += tot[kCntExt + b];
+            st.nodes_extension[b - 1] += tot[kTotNodesExt + b];
+            st.tris_extension[b - 1] += tot[kTotTrisExt + b];
+        }
         for (int v = 0; v <= MRT_MAX_BOUNCES; ++v) st.shadow_rays += tot[kCntShadow + v];
+        st.nodes_shadow += tot[kTotNodesShadow];
+        st.tris_shadow += tot[kTotTrisShadow];
+        st.nodes_primary += tot[kTotNodesPrim];
+        st.tris_primary += tot[kTotTrisPrim];
     }
     st.launches = ctx->launches;
     *out = st;
@@ -479,7 +494,8 @@ int mrt_cuda_primary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_camera
     cudaStream_t s = as_stream(stream);
     {
         Scope sc(ctx, s, 0, 0);
-        cudaError_t e = scene->kind == 0 ? launch_primary_tri(scene->dev, fp, *gbuffer, ctx->d_status, s)
+        cudaError_t e = scene->kind == 0 ? launch_primary_tri(scene->dev, fp, *gbuffer, ctx->d_status,
+                                                              ctx->counters ? ctx->d_totals : nullptr, s)
                                          : launch_primary_sphere(scene->dev, fp, *gbuffer, s);
         if (e != cudaSuccess) return fail(ctx, MRT_ECUDA, "primary rays launch: %s", cudaGetErrorString(e));
     }
@@ -533,12 +549,12 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
         MRT_CK(cudaMemsetAsync(wb.counters, 0, kCntSlots * sizeof(uint32_t), s));
         MRT_LAUNCH(3, 0, launch_shade_primary(scene->dev, fp, *gbuffer, tp, bn, wb, smp, ctx->d_status, s));
         for (uint32_t b = 1; b <= tp.max_bounces; ++b) {
-            if (nee) MRT_LAUNCH(2, int(b - 1), launch_trace_shadow(scene->dev, wb, tp, b - 1, tblocks, ctx->d_status, s));
+            if (nee) MRT_LAUNCH(2, int(b - 1), launch_trace_shadow(scene->dev, wb, tp, b - 1, tblocks, ctx->d_status, ctx->counters, s));
             if (params->sort_rays) MRT_LAUNCH(4, int(b), launch_sort_ext(scene->dev, wb, b, s));
-            MRT_LAUNCH(1, int(b), launch_trace_ext(scene->dev, wb, b, tblocks, ctx->d_status, s));
+            MRT_LAUNCH(1, int(b), launch_trace_ext(scene->dev, wb, b, tblocks, ctx->d_status, ctx->counters, s));
             MRT_LAUNCH(3, int(b), launch_shade(scene->dev, tp, bn, wb, W, b, ctx->d_status, s));
         }
-        if (nee) MRT_LAUNCH(2, int(tp.max_bounces), launch_trace_shadow(scene->dev, wb, tp, tp.max_bounces, tblocks, ctx->d_status, s));
+        if (nee) MRT_LAUNCH(2, int(tp.max_bounces), launch_trace_shadow(scene->dev, wb, tp, tp.max_bounces, tblocks, ctx->d_status, ctx->counters, s));
         MRT_LAUNCH(3, 0, launch_tally(wb, s));
     }
     MRT_LAUNCH(3, 0, launch_finalize(wb, color, tp.samples, params->accumulate, params->frame_index, s));

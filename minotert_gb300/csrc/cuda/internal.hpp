@@ -36,6 +36,18 @@ enum : uint32_t {
     kCntSlots = kCntFetchShadow + 17,
 };
 
+// Accumulated totals (uint64 slots): ray counts copied from the counters
+// above (slots 0..33), then traversal work in counting mode.
+enum : uint32_t {
+    kTotNodesExt = 64,     // [b]
+    kTotTrisExt = 82,      // [b]
+    kTotNodesShadow = 100,
+    kTotTrisShadow = 101,
+    kTotNodesPrim = 102,
+    kTotTrisPrim = 103,
+    kTotSlots = 128,
+};
+
 struct WaveBuffers {
     size_t cap = 0;        // rays per queue
     size_t npix = 0;
@@ -72,7 +84,7 @@ struct BlueNoise {
 
 // Launchers (kernels.cu).  All return cudaError_t of the launch.
 cudaError_t launch_primary_tri(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g,
-                               uint32_t* status, cudaStream_t s);
+                               uint32_t* status, unsigned long long* totals, cudaStream_t s);
 cudaError_t launch_primary_sphere(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g,
                                   cudaStream_t s);
 cudaError_t launch_secondary_sphere(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g,
@@ -87,9 +99,9 @@ cudaError_t launch_shade_primary(const DevScene& sc, const FrameParams& fp, cons
                                  const TraceParams& tp, BlueNoise bn, const WaveBuffers& wb,
                                  uint32_t sample, uint32_t* status, cudaStream_t s);
 cudaError_t launch_trace_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t bounce, int blocks,
-                             uint32_t* status, cudaStream_t s);
+                             uint32_t* status, bool count, cudaStream_t s);
 cudaError_t launch_trace_shadow(const DevScene& sc, const WaveBuffers& wb, const TraceParams& tp,
-                                uint32_t vertex, int blocks, uint32_t* status, cudaStream_t s);
+                                uint32_t vertex, int blocks, uint32_t* status, bool count, cudaStream_t s);
 cudaError_t launch_shade(const DevScene& sc, const TraceParams& tp, BlueNoise bn, const WaveBuffers& wb,
                          uint32_t width, uint32_t bounce, uint32_t* status, cudaStream_t s);
 cudaError_t launch_tally(const WaveBuffers& wb, cudaStream_t s);
@@ -132,6 +144,8 @@ struct mrt_ctx {
     size_t frame_pixels = 0;
     // timing
     bool timing = false;
+    bool counters = false;
+    unsigned long long* d_totals = nullptr;  // kTotSlots accumulated totals
     std::vector<mrt_timing_rec> recs;
     std::vector<cudaEvent_t> ev_pool;
     mrt_frame_stats acc{};

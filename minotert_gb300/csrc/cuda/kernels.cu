@@ -87,8 +87,9 @@ MRT_DEV bool tile_pixel(uint32_t w, uint32_t h, uint32_t& x, uint32_t& y) {
     return x < w && y < h;
 }
 
+template <bool kCount>
 __global__ void __launch_bounds__(kTraceBlock)
-k_primary_tri(DevScene sc, FrameParams fp, mrt_gbuffer g, uint32_t* status) {
+k_primary_tri(DevScene sc, FrameParams fp, mrt_gbuffer g, uint32_t* status, unsigned long long* totals) {
     __shared__ uint2 stk[kStackDepth * kTraceBlock];
     uint32_t x, y;
     if (!tile_pixel(fp.width, fp.height, x, y)) return;
@@ -96,9 +97,13 @@ k_primary_tri(DevScene sc, FrameParams fp, mrt_gbuffer g, uint32_t* status) {
     primary_ray(fp, x, y, o, d);
     uint32_t prim, st = 0u, cn = 0u, ct = 0u;
     float t;
-    trace_bvh8<false, false, kStackDepth>(sc, o, d, 0.0f, INFINITY, prim, t, stk + threadIdx.x, kTraceBlock,
-                                          st, cn, ct);
+    trace_bvh8<false, kCount, kStackDepth>(sc, o, d, 0.0f, INFINITY, prim, t, stk + threadIdx.x, kTraceBlock,
+                                           st, cn, ct);
     if (st) atomicOr(status, st);
+    if (kCount) {
+        atomicAdd(totals + kTotNodesPrim, (unsigned long long)cn);
+        atomicAdd(totals + kTotTrisPrim, (unsigned long long)ct);
+    }
     const size_t pi = size_t(y) * fp.width + x;
     g.visibility[pi] = prim;
     if (g.hit_t) g.hit_t[pi] = t;
@@ -392,6 +397,7 @@ k_shade(DevScene sc, TraceParams tp, BlueNoise bn, WaveBuffers wb, uint32_t widt
 
 // Persistent closest-hit over the extension queue of bounce `bounce`;
 // each warp fetches 32 rays at a time.
+template <bool kCount>
 __global__ void __launch_bounds__(kTraceBlock)
 k_trace_ext(DevScene sc, WaveBuffers wb, uint32_t bounce, uint32_t* status) {
     __shared__ uint2 stk[kStackDepth * kTraceBlock];
@@ -399,7 +405,7 @@ k_trace_ext(DevScene sc, WaveBuffers wb, uint32_t bounce, uint32_t* status) {
     const PathRay* q = (bounce & 1u) ? wb.q[1] : wb.q[0];
     uint32_t* fetch = wb.counters + kCntFetchExt + bounce;
     const uint32_t lane = lane_id();
-    uint32_t st = 0u;
+    uint32_t st = 0u, cn = 0u, ct = 0u;
     while (true) {
         uint32_t base = 0u;
         if (lane == 0u) base = atomicAdd(fetch, 32u);
@@ -408,18 +414,23 @@ k_trace_ext(DevScene sc, WaveBuffers wb, uint32_t bounce, uint32_t* status) {
         const uint32_t i = base + lane;
         if (i < n) {
             const float4 a = q[i].o_pix, b = q[i].d;
-            uint32_t prim, cn = 0u, ct = 0u;
+            uint32_t prim;
             float t;
-            trace_bvh8<false, false, kStackDepth>(sc, f3{a.x, a.y, a.z}, f3{b.x, b.y, b.z}, 0.0f, INFINITY, prim, t,
-                                                  stk + threadIdx.x, kTraceBlock, st, cn, ct);
+            trace_bvh8<false, kCount, kStackDepth>(sc, f3{a.x, a.y, a.z}, f3{b.x, b.y, b.z}, 0.0f, INFINITY, prim, t,
+                                                   stk + threadIdx.x, kTraceBlock, st, cn, ct);
             wb.hits[i] = make_uint2(prim, __float_as_uint(t));
         }
     }
     if (st) atomicOr(status, st);
+    if (kCount) {
+        atomicAdd(wb.totals + kTotNodesExt + bounce, (unsigned long long)cn);
+        atomicAdd(wb.totals + kTotTrisExt + bounce, (unsigned long long)ct);
+    }
 }
 
 // Persistent any-hit over the shadow queue of vertex `vertex`; unoccluded
 // rays add their contribution to the pixel's radiance.
+template <bool kCount>
 __global__ void __launch_bounds__(kTraceBlock)
 k_trace_shadow(DevScene sc, WaveBuffers wb, TraceParams tp, uint32_t vertex, uint32_t* status) {
     __shared__ uint2 stk[kStackDepth * kTraceBlock];
@@ -427,7 +438,7 @@ k_trace_shadow(DevScene sc, WaveBuffers wb, TraceParams tp, uint32_t vertex, uin
     uint32_t* fetch = wb.counters + kCntFetchShadow + vertex;
     const uint32_t lane = lane_id();
     const f3 sun{tp.sun[0], tp.sun[1], tp.sun[2]};
-    uint32_t st = 0u;
+    uint32_t st = 0u, cn = 0u, ct = 0u;
     while (true) {
         uint32_t base = 0u;
         if (lane == 0u) base = atomicAdd(fetch, 32u);
@@ -436,15 +447,19 @@ k_trace_shadow(DevScene sc, WaveBuffers wb, TraceParams tp, uint32_t vertex, uin
         const uint32_t i = base + lane;
         if (i < n) {
             const ShadowRay sr = wb.sq[i];
-            uint32_t prim, cn = 0u, ct = 0u;
+            uint32_t prim;
             float t;
-            trace_bvh8<true, false, kStackDepth>(sc, f3{sr.o_pix.x, sr.o_pix.y, sr.o_pix.z}, sun, 0.0f, INFINITY, prim,
-                                                 t, stk + threadIdx.x, kTraceBlock, st, cn, ct);
+            trace_bvh8<true, kCount, kStackDepth>(sc, f3{sr.o_pix.x, sr.o_pix.y, sr.o_pix.z}, sun, 0.0f, INFINITY,
+                                                  prim, t, stk + threadIdx.x, kTraceBlock, st, cn, ct);
             if (prim == kMiss)
                 add_L(wb.L, __float_as_uint(sr.o_pix.w), f3{sr.contrib.x, sr.contrib.y, sr.contrib.z});
         }
     }
     if (st) atomicOr(status, st);
+    if (kCount) {
+        atomicAdd(wb.totals + kTotNodesShadow, (unsigned long long)cn);
+        atomicAdd(wb.totals + kTotTrisShadow, (unsigned long long)ct);
+    }
 }
 
 __global__ void k_tally(WaveBuffers wb) {
@@ -517,9 +532,10 @@ k_trace_rays_sphere(DevScene sc, const mrt_ray* rays, uint32_t n, mrt_hit* hits)
 // ------------------------------------------------------------------ launchers
 
 cudaError_t launch_primary_tri(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g, uint32_t* status,
-                               cudaStream_t s) {
+                               unsigned long long* totals, cudaStream_t s) {
     dim3 grid((fp.width + 15) / 16, (fp.height + 7) / 8);
-    k_primary_tri<<<grid, kTraceBlock, 0, s>>>(sc, fp, g, status);
+    if (totals) k_primary_tri<true><<<grid, kTraceBlock, 0, s>>>(sc, fp, g, status, totals);
+    else k_primary_tri<false><<<grid, kTraceBlock, 0, s>>>(sc, fp, g, status, nullptr);
     return cudaGetLastError();
 }
 
@@ -567,14 +583,16 @@ cudaError_t launch_shade_primary(const DevScene& sc, const FrameParams& fp, cons
 }
 
 cudaError_t launch_trace_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t bounce, int blocks, uint32_t* status,
-                             cudaStream_t s) {
-    k_trace_ext<<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
+                             bool count, cudaStream_t s) {
+    if (count) k_trace_ext<true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
+    else k_trace_ext<false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
     return cudaGetLastError();
 }
 
 cudaError_t launch_trace_shadow(const DevScene& sc, const WaveBuffers& wb, const TraceParams& tp, uint32_t vertex,
-                                int blocks, uint32_t* status, cudaStream_t s) {
-    k_trace_shadow<<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
+                                int blocks, uint32_t* status, bool count, cudaStream_t s) {
+    if (count) k_trace_shadow<true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
+    else k_trace_shadow<false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
     return cudaGetLastError();
 }
 
@@ -601,7 +619,8 @@ cudaError_t launch_tally(const WaveBuffers& wb, cudaStream_t s) {
 
 int trace_blocks_per_sm() {
     int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_ext, kTraceBlock, 0) != cudaSuccess || b < 1) b = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_ext<false>, kTraceBlock, 0) != cudaSuccess || b < 1)
+        b = 1;
     return b;
 }
 

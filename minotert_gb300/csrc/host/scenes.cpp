@@ -261,7 +261,8 @@ int mrt_scene_icospheres(uint64_t seed, uint32_t spheres, uint32_t levels, float
     icosphere(levels, uv, uf);
 
     // field of spheres over a square whose side grows with the count
-    const double half = 6.0 * std::sqrt(double(std::max<uint32_t>(spheres, 1)));
+    // (200 spheres: 90 x 90 units, about a fifth of the ground covered)
+    const double half = 3.2 * std::sqrt(double(std::max<uint32_t>(spheres, 1)));
     MeshBuilder mb;
     mb.verts.reserve((size_t(spheres) * (uf.size() / 3) + ground_tris + 64) * 9);
 
@@ -269,7 +270,7 @@ int mrt_scene_icospheres(uint64_t seed, uint32_t spheres, uint32_t levels, float
         // gx * gy * 2 >= ground_tris with gy/gx = 5/4 (64 x 80 cells = 10,240)
         uint32_t gx = uint32_t(std::ceil(std::sqrt(ground_tris / 2.5)));
         uint32_t gy = uint32_t(std::ceil(double(ground_tris) / (2.0 * gx)));
-        double ext = 2.6 * half;
+        double ext = 6.0 * half;
         uint32_t albedo = pack_albedo(rng);
         for (uint32_t j = 0; j < gy; ++j)
             for (uint32_t i = 0; i < gx; ++i) {

@@ -44,8 +44,8 @@ def heightfield_boxes_256(seed: int = 1, size: int = 256) -> Workload:
 
 
 def icospheres_1080p(seed: int = 1, width: int = 1920, height: int = 1080) -> Workload:
-    cam = Camera((width, height), math.radians(60.0), 0.05, (0.0, -125.0, 42.0), math.radians(90.0),
-                 math.radians(-17.0))
+    cam = Camera((width, height), math.radians(60.0), 0.05, (0.0, -62.0, 40.0), math.radians(90.0),
+                 math.radians(-36.0))
     return Workload("icospheres_1080p", width, height, cam, Sky((0.25, 0.32, 0.45), SUN, (2.5, 2.5, 2.5)),
                     TraceSettings(samples=1, bounces=4, rr_start=2),
                     lambda s: _scene.icospheres(s, 200, 4, 0.2, 5.0, 10240), seed)

@@ -38,7 +38,7 @@ def lib() -> C.CDLL:
             "orc_trace_brute": ([vp, u32, vp, u32, vp, i32, i32], None),
             "orc_trace_bvh8": ([vp, u32, vp, u32, vp, u32, vp, i32, vp, vp, i32], u32),
             "orc_bvh8_validate": ([vp, u32, vp, u32, vp, u32, vp], None),
-            "orc_primary": ([vp, u32, vp, u32, vp, vp, u32, vp, u32, u32, vp, vp, vp, vp, vp, i32], u32),
+            "orc_primary": ([vp, u32, vp, u32, vp, vp, u32, vp, u32, u32, u32, u32, vp, vp, vp, vp, vp, i32], u32),
             "orc_secondary_spheres": ([vp, u32, vp, u32, u32, vp, vp, vp, vp, u32, u32, vp, vp, i32], None),
             "orc_pathtrace": ([vp, u32, vp, u32, vp, u32, vp, u32, u32, vp, vp, vp, u32, u32, vp, i32, u32, u32, vp,
                                vp, i32], u32),
@@ -140,8 +140,10 @@ def bvh8_validate(nodes, tris, verts) -> dict:
     return {"depth": int(info[0]), "max_tris_per_node": int(info[1]), "error": int(info[2])}
 
 
-def primary(consts: np.ndarray, w: int, h: int, nodes=None, tris=None, mats=None, spheres=None, threads=0):
-    """Returns dict of visibility, hit_t, depth(u16), normal(u16x4), motion(u16x2), status."""
+def primary(consts: np.ndarray, w: int, h: int, nodes=None, tris=None, mats=None, spheres=None, threads=0,
+            y0=0, y1=None):
+    """Returns dict of visibility, hit_t, depth(u16), normal(u16x4), motion(u16x2), status; rows [y0, y1)
+    are computed (the rest stay zero)."""
     vis = np.zeros((h, w), np.uint32)
     ht = np.zeros((h, w), np.float32)
     dep = np.zeros((h, w), np.uint16)
@@ -149,8 +151,8 @@ def primary(consts: np.ndarray, w: int, h: int, nodes=None, tris=None, mats=None
     mot = np.zeros((h, w, 2), np.uint16)
     ns = 0 if spheres is None else len(spheres)
     st = lib().orc_primary(_p(nodes), 0 if nodes is None else len(nodes), _p(tris), 0 if tris is None else len(tris),
-                           _p(mats), _p(spheres), ns, _p(consts), w, h, _p(vis), _p(ht), _p(dep), _p(nrm), _p(mot),
-                           threads)
+                           _p(mats), _p(spheres), ns, _p(consts), w, h, y0, h if y1 is None else y1, _p(vis), _p(ht),
+                           _p(dep), _p(nrm), _p(mot), threads)
     return {"visibility": vis, "hit_t": ht, "depth": dep, "normal": nrm, "motion": mot, "status": st}
 
 

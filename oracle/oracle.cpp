@@ -885,11 +885,15 @@ void orc_bvh8_validate(const Node* nodes, uint32_t nn, const Tri* tris, uint32_t
 // FP32 t, and the reference g-buffer formats (depth R16F, normal RGBA16F,
 // motion RG16F; any output may be NULL).
 uint32_t orc_primary(const Node* nodes, uint32_t nn, const Tri* tris, uint32_t nt, const Mat* mats,
-                     const float* spheres, uint32_t ns, const Consts* c, uint32_t w, uint32_t h, uint32_t* vis,
-                     float* hit_t, uint16_t* depth, uint16_t* normal, uint16_t* motion, int threads) {
+                     const float* spheres, uint32_t ns, const Consts* c, uint32_t w, uint32_t h, uint32_t y0,
+                     uint32_t y1, uint32_t* vis, float* hit_t, uint16_t* depth, uint16_t* normal, uint16_t* motion,
+                     int threads) {
     FrameInfo fi = frame_info(c, w, h);
     std::atomic<uint32_t> status{0};
-    parallel_rows(h, threads, [&](uint32_t y, int) {
+    y1 = std::min(y1, h);
+    if (y0 >= y1) return 0;
+    parallel_rows(y1 - y0, threads, [&](uint32_t r, int) {
+        const uint32_t y = y0 + r;
         uint32_t st = 0;
         for (uint32_t x = 0; x < w; ++x) {
             V3<float> o, d;
