@@ -232,6 +232,32 @@ int mrt_cuda_set_counters(mrt_ctx* ctx, int enable);
  * them; synchronises the context. */
 int mrt_cuda_frame_stats(mrt_ctx* ctx, mrt_frame_stats* out);
 
+/* Launch-schedule knobs of the traversal kernels (new; the reference
+ * dispatches fixed 8x8 groups, pathtracer.ixx:106,190).  Picked by the
+ * autotuner; defaults are the tuned values for GB300. */
+typedef struct mrt_tuning {
+    uint32_t trace_blocks_per_sm; /* persistent blocks per SM; 0 = occupancy max */
+    uint32_t dynamic_fetch;       /* 1: idle lanes refill after every node step
+                                     (0: each warp fetches 32 rays)          */
+    uint32_t primary_persistent;  /* 1: primary rays through the persistent
+                                     dynamic-fetch kernel (0: one thread per
+                                     pixel, 8x4-pixel warps)                 */
+    uint32_t sort_min_rays;       /* sort extension queues with at least this
+                                     many rays when sort_rays is set          */
+} mrt_tuning;
+int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning);
+int mrt_cuda_get_tuning(mrt_ctx* ctx, mrt_tuning* tuning);
+
+typedef struct mrt_device_info {
+    char     name[96];
+    int32_t  sm_count;
+    int32_t  cc_major, cc_minor;
+    uint32_t trace_blocks_per_sm_max; /* occupancy limit of the traversal kernels */
+    uint64_t total_mem;
+    uint64_t l2_bytes;
+} mrt_device_info;
+int mrt_cuda_device_info(mrt_ctx* ctx, mrt_device_info* out);
+
 /* ---- memory and streams (the reference's vuk allocator role,
  *      renderer.ixx:42-43) --------------------------------------------- */
 int mrt_cuda_alloc(mrt_ctx* ctx, size_t bytes, void** dptr);

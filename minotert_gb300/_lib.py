@@ -67,6 +67,16 @@ class FrameStats(C.Structure):
                 ("ms_sort", C.c_float), ("ms_total", C.c_float), ("launches", C.c_uint32), ("pad", C.c_uint32)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("trace_blocks_per_sm", C.c_uint32), ("dynamic_fetch", C.c_uint32),
+                ("primary_persistent", C.c_uint32), ("sort_min_rays", C.c_uint32)]
+
+
+class DeviceInfo(C.Structure):
+    _fields_ = [("name", C.c_char * 96), ("sm_count", C.c_int32), ("cc_major", C.c_int32), ("cc_minor", C.c_int32),
+                ("trace_blocks_per_sm_max", C.c_uint32), ("total_mem", C.c_uint64), ("l2_bytes", C.c_uint64)]
+
+
 class Camera_C(C.Structure):
     _fields_ = [("viewport", C.c_uint32 * 2), ("vertical_fov", C.c_float), ("near_plane", C.c_float),
                 ("position", C.c_float * 3), ("yaw", C.c_float), ("pitch", C.c_float)]
@@ -118,6 +128,9 @@ def lib() -> C.CDLL:
             "mrt_cuda_sync": ([vp, vp, C.c_double], i32),
             "mrt_cuda_set_timing": ([vp, i32], i32),
             "mrt_cuda_set_counters": ([vp, i32], i32),
+            "mrt_cuda_set_tuning": ([vp, C.POINTER(Tuning)], i32),
+            "mrt_cuda_get_tuning": ([vp, C.POINTER(Tuning)], i32),
+            "mrt_cuda_device_info": ([vp, C.POINTER(DeviceInfo)], i32),
             "mrt_cuda_frame_stats": ([vp, C.POINTER(FrameStats)], i32),
             "mrt_cuda_alloc": ([vp, sz, pp], i32),
             "mrt_cuda_free": ([vp, vp], i32),
@@ -237,6 +250,22 @@ class Context:
 
     def set_timing(self, on: bool):
         self.check(lib().mrt_cuda_set_timing(self._h, 1 if on else 0), "set_timing")
+
+    def device_info(self) -> DeviceInfo:
+        d = DeviceInfo()
+        self.check(lib().mrt_cuda_device_info(self._h, C.byref(d)), "device_info")
+        return d
+
+    def tuning(self) -> Tuning:
+        t = Tuning()
+        self.check(lib().mrt_cuda_get_tuning(self._h, C.byref(t)), "get_tuning")
+        return t
+
+    def set_tuning(self, **kw):
+        t = self.tuning()
+        for k, v in kw.items():
+            setattr(t, k, int(v))
+        self.check(lib().mrt_cuda_set_tuning(self._h, C.byref(t)), "set_tuning")
 
     def set_counters(self, on: bool):
         self.check(lib().mrt_cuda_set_counters(self._h, 1 if on else 0), "set_counters")

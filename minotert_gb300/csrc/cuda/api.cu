@@ -138,6 +138,41 @@ int ensure_wave(mrt_ctx* ctx, size_t npix) {
     return MRT_OK;
 }
 
+// Persistent traversal grid: blocks per SM from the tuning (0 = the
+// occupancy maximum, computed once per context) times the SM count.
+int trace_blocks(mrt_ctx* ctx) {
+    if (ctx->occ_blocks == 0) ctx->occ_blocks = trace_blocks_per_sm();
+    int per_sm = ctx->tuning.trace_blocks_per_sm ? int(ctx->tuning.trace_blocks_per_sm) : ctx->occ_blocks;
+    if (per_sm > ctx->occ_blocks) per_sm = ctx->occ_blocks;
+    return per_sm * ctx->sm_count;
+}
+
+// Depth of a BVH8 along in-range child links, each node counted once (a
+// corrupt blob with cycles still terminates; traversal bounds-checks the
+// rest at run time).  The traversal stack holds at most depth - 1 entries.
+uint32_t bvh8_depth(const mrt_bvh8_node* nodes, uint32_t n) {
+    std::vector<uint8_t> seen(n, 0);
+    std::vector<std::pair<uint32_t, uint32_t>> st{{0u, 1u}};
+    uint32_t depth = 0;
+    seen[0] = 1;
+    while (!st.empty()) {
+        auto [ni, d] = st.back();
+        st.pop_back();
+        depth = d > depth ? d : depth;
+        const mrt_bvh8_node& nd = nodes[ni];
+        uint32_t k = 0;
+        for (int s = 0; s < 8; ++s) {
+            if (!((nd.imask >> s) & 1u)) continue;
+            uint64_t c = uint64_t(nd.child_base) + k++;
+            if (c < n && !seen[c]) {
+                seen[c] = 1;
+                st.push_back({uint32_t(c), d + 1});
+            }
+        }
+    }
+    return depth;
+}
+
 int check_gbuffer(mrt_ctx* ctx, const mrt_gbuffer* g) {
     if (!g || !g->visibility) return fail(ctx, MRT_EINVAL, "gbuffer.visibility is NULL");
     if (g->width == 0 || g->height == 0) return fail(ctx, MRT_EINVAL, "gbuffer has zero size");
@@ -170,9 +205,11 @@ int mrt_cuda_create(mrt_ctx** out, int device) {
     if (cudaMalloc(&ctx->d_status, sizeof(uint32_t)) != cudaSuccess ||
         cudaMemset(ctx->d_status, 0, sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&ctx->d_totals, kTotSlots * sizeof(unsigned long long)) != cudaSuccess ||
-        cudaMemset(ctx->d_totals, 0, kTotSlots * sizeof(unsigned long long)) != cudaSuccess) {
+        cudaMemset(ctx->d_totals, 0, kTotSlots * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_prim_fetch, sizeof(uint32_t)) != cudaSuccess) {
         cudaFree(ctx->d_status);
         cudaFree(ctx->d_totals);
+        cudaFree(ctx->d_prim_fetch);
         delete ctx;
         return MRT_ENOMEM;
     }
@@ -187,6 +224,7 @@ int mrt_cuda_destroy(mrt_ctx* ctx) {
     free_wave(ctx->wb);
     cudaFree(ctx->d_status);
     cudaFree(ctx->d_totals);
+    cudaFree(ctx->d_prim_fetch);
     cudaFree(ctx->d_bn);
     cudaFree(ctx->d_vis);
     cudaFree(ctx->d_aux);
@@ -225,6 +263,37 @@ int mrt_cuda_sync(mrt_ctx* ctx, void* stream, double timeout_s) {
 int mrt_cuda_set_timing(mrt_ctx* ctx, int enable) {
     if (!ctx) return MRT_EINVAL;
     ctx->timing = enable != 0;
+    return MRT_OK;
+}
+
+int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning) {
+    if (!ctx || !tuning) return fail(ctx, MRT_EINVAL, "set_tuning: null argument");
+    if (tuning->trace_blocks_per_sm > 64 || tuning->dynamic_fetch > 1 || tuning->primary_persistent > 1)
+        return fail(ctx, MRT_EINVAL, "set_tuning: value out of range");
+    ctx->tuning = *tuning;
+    return MRT_OK;
+}
+
+int mrt_cuda_get_tuning(mrt_ctx* ctx, mrt_tuning* tuning) {
+    if (!ctx || !tuning) return fail(ctx, MRT_EINVAL, "get_tuning: null argument");
+    *tuning = ctx->tuning;
+    return MRT_OK;
+}
+
+int mrt_cuda_device_info(mrt_ctx* ctx, mrt_device_info* out) {
+    if (!ctx || !out) return fail(ctx, MRT_EINVAL, "device_info: null argument");
+    cudaSetDevice(ctx->device);
+    cudaDeviceProp p;
+    MRT_CK(cudaGetDeviceProperties(&p, ctx->device));
+    std::memset(out, 0, sizeof(*out));
+    std::snprintf(out->name, sizeof(out->name), "%s", p.name);
+    out->sm_count = p.multiProcessorCount;
+    out->cc_major = p.major;
+    out->cc_minor = p.minor;
+    if (ctx->occ_blocks == 0) ctx->occ_blocks = trace_blocks_per_sm();
+    out->trace_blocks_per_sm_max = uint32_t(ctx->occ_blocks);
+    out->total_mem = p.totalGlobalMem;
+    out->l2_bytes = uint64_t(p.l2CacheSize);
     return MRT_OK;
 }
 
@@ -397,6 +466,9 @@ int mrt_cuda_scene_upload_triangles(mrt_ctx* ctx, const mrt_bvh8_node* nodes, ui
         return fail(ctx, MRT_EINVAL, "scene_upload_triangles: null pointer or empty scene");
     cudaSetDevice(ctx->device);
     *out = nullptr;
+    const uint32_t depth = bvh8_depth(nodes, node_count);
+    if (depth > uint32_t(kStackDepth))
+        return fail(ctx, MRT_ERANGE, "BVH8 depth %u exceeds the traversal stack (%d levels)", depth, kStackDepth);
     mrt_scene* sc = new (std::nothrow) mrt_scene;
     if (!sc) return MRT_ENOMEM;
     size_t nb = size_t(node_count) * sizeof(mrt_bvh8_node), tb = size_t(tri_count) * sizeof(mrt_tri),
@@ -494,9 +566,12 @@ int mrt_cuda_primary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_camera
     cudaStream_t s = as_stream(stream);
     {
         Scope sc(ctx, s, 0, 0);
-        cudaError_t e = scene->kind == 0 ? launch_primary_tri(scene->dev, fp, *gbuffer, ctx->d_status,
-                                                              ctx->counters ? ctx->d_totals : nullptr, s)
-                                         : launch_primary_sphere(scene->dev, fp, *gbuffer, s);
+        cudaError_t e = scene->kind == 0
+                            ? launch_primary_tri(scene->dev, fp, *gbuffer, ctx->d_status,
+                                                 ctx->counters ? ctx->d_totals : nullptr,
+                                                 ctx->tuning.primary_persistent ? ctx->d_prim_fetch : nullptr,
+                                                 trace_blocks(ctx), s)
+                            : launch_primary_sphere(scene->dev, fp, *gbuffer, s);
         if (e != cudaSuccess) return fail(ctx, MRT_ECUDA, "primary rays launch: %s", cudaGetErrorString(e));
     }
     ctx->launches++;
@@ -536,8 +611,8 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
     rc = ensure_wave(ctx, size_t(W) * H);
     if (rc) return rc;
     WaveBuffers& wb = ctx->wb;
-    const int tblocks = trace_blocks_per_sm() * ctx->sm_count;
-    const bool nee = tp.estimator == MRT_EST_NEE;
+    const int tblocks = trace_blocks(ctx);
+    const bool nee = tp.estimator == MRT_EST_NEE, dyn = ctx->tuning.dynamic_fetch != 0u;
 #define MRT_LAUNCH(kind, bounce, expr)                                                                   \
     do {                                                                                                 \
         Scope sc_(ctx, s, kind, bounce);                                                                 \
@@ -549,12 +624,16 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
         MRT_CK(cudaMemsetAsync(wb.counters, 0, kCntSlots * sizeof(uint32_t), s));
         MRT_LAUNCH(3, 0, launch_shade_primary(scene->dev, fp, *gbuffer, tp, bn, wb, smp, ctx->d_status, s));
         for (uint32_t b = 1; b <= tp.max_bounces; ++b) {
-            if (nee) MRT_LAUNCH(2, int(b - 1), launch_trace_shadow(scene->dev, wb, tp, b - 1, tblocks, ctx->d_status, ctx->counters, s));
+            if (nee)
+                MRT_LAUNCH(2, int(b - 1), launch_trace_shadow(scene->dev, wb, tp, b - 1, tblocks, ctx->d_status,
+                                                              ctx->counters, dyn, s));
             if (params->sort_rays) MRT_LAUNCH(4, int(b), launch_sort_ext(scene->dev, wb, b, s));
-            MRT_LAUNCH(1, int(b), launch_trace_ext(scene->dev, wb, b, tblocks, ctx->d_status, ctx->counters, s));
+            MRT_LAUNCH(1, int(b), launch_trace_ext(scene->dev, wb, b, tblocks, ctx->d_status, ctx->counters, dyn, s));
             MRT_LAUNCH(3, int(b), launch_shade(scene->dev, tp, bn, wb, W, b, ctx->d_status, s));
         }
-        if (nee) MRT_LAUNCH(2, int(tp.max_bounces), launch_trace_shadow(scene->dev, wb, tp, tp.max_bounces, tblocks, ctx->d_status, ctx->counters, s));
+        if (nee)
+            MRT_LAUNCH(2, int(tp.max_bounces), launch_trace_shadow(scene->dev, wb, tp, tp.max_bounces, tblocks,
+                                                                   ctx->d_status, ctx->counters, dyn, s));
         MRT_LAUNCH(3, 0, launch_tally(wb, s));
     }
     MRT_LAUNCH(3, 0, launch_finalize(wb, color, tp.samples, params->accumulate, params->frame_index, s));

@@ -12,8 +12,19 @@
 
 namespace mrt {
 
+// Traversal stack entries per thread (shared memory) and the residency
+// target of the traversal kernels: 24 entries x 8 B x 128 threads = 24 KB
+// and <= 64 registers give 8 blocks (32 warps) per SM on GB300, the
+// fastest schedule measured (6 blocks: +10% frame time, 5: +20%).
+#ifndef MRT_TRACE_STACK
+#define MRT_TRACE_STACK 24
+#endif
+#ifndef MRT_TRACE_MIN_BLOCKS
+#define MRT_TRACE_MIN_BLOCKS 8
+#endif
 constexpr int kTraceBlock = 128;   // threads per traversal block
-constexpr int kStackDepth = 32;    // traversal stack entries per thread
+constexpr int kStackDepth = MRT_TRACE_STACK;
+constexpr int kTraceMinBlocks = MRT_TRACE_MIN_BLOCKS;
 constexpr int kShadeBlock = 256;
 
 // Wavefront records
@@ -83,8 +94,11 @@ struct BlueNoise {
 };
 
 // Launchers (kernels.cu).  All return cudaError_t of the launch.
+// fetch != nullptr selects the persistent dynamic-fetch kernel (`blocks`
+// blocks); otherwise one thread per pixel.
 cudaError_t launch_primary_tri(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g,
-                               uint32_t* status, unsigned long long* totals, cudaStream_t s);
+                               uint32_t* status, unsigned long long* totals, uint32_t* fetch, int blocks,
+                               cudaStream_t s);
 cudaError_t launch_primary_sphere(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g,
                                   cudaStream_t s);
 cudaError_t launch_secondary_sphere(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g,
@@ -99,9 +113,10 @@ cudaError_t launch_shade_primary(const DevScene& sc, const FrameParams& fp, cons
                                  const TraceParams& tp, BlueNoise bn, const WaveBuffers& wb,
                                  uint32_t sample, uint32_t* status, cudaStream_t s);
 cudaError_t launch_trace_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t bounce, int blocks,
-                             uint32_t* status, bool count, cudaStream_t s);
+                             uint32_t* status, bool count, bool dyn, cudaStream_t s);
 cudaError_t launch_trace_shadow(const DevScene& sc, const WaveBuffers& wb, const TraceParams& tp,
-                                uint32_t vertex, int blocks, uint32_t* status, bool count, cudaStream_t s);
+                                uint32_t vertex, int blocks, uint32_t* status, bool count, bool dyn,
+                                cudaStream_t s);
 cudaError_t launch_shade(const DevScene& sc, const TraceParams& tp, BlueNoise bn, const WaveBuffers& wb,
                          uint32_t width, uint32_t bounce, uint32_t* status, cudaStream_t s);
 cudaError_t launch_tally(const WaveBuffers& wb, cudaStream_t s);
@@ -145,6 +160,9 @@ struct mrt_ctx {
     // timing
     bool timing = false;
     bool counters = false;
+    mrt_tuning tuning{0u, 1u, 0u, 1u << 20};  // autotuned on GB300 (icosphere field, 1080p)
+    uint32_t* d_prim_fetch = nullptr;  // work counter of the persistent primary kernel
+    int occ_blocks = 0;                // traversal blocks per SM at full occupancy
     unsigned long long* d_totals = nullptr;  // kTotSlots accumulated totals
     std::vector<mrt_timing_rec> recs;
     std::vector<cudaEvent_t> ev_pool;

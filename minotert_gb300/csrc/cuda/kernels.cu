@@ -88,7 +88,7 @@ MRT_DEV bool tile_pixel(uint32_t w, uint32_t h, uint32_t& x, uint32_t& y) {
 }
 
 template <bool kCount>
-__global__ void __launch_bounds__(kTraceBlock)
+__global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
 k_primary_tri(DevScene sc, FrameParams fp, mrt_gbuffer g, uint32_t* status, unsigned long long* totals) {
     __shared__ uint2 stk[kStackDepth * kTraceBlock];
     uint32_t x, y;
@@ -115,6 +115,65 @@ k_primary_tri(DevScene sc, FrameParams fp, mrt_gbuffer g, uint32_t* status, unsi
             n = facing_normal(load_mat(sc, prim, status), d);
         }
         store_extras(fp, g, pi, hit, pos, n);
+    }
+}
+
+MRT_DEV uint32_t warp_refill(uint32_t* fetch, uint32_t n, bool need, bool& exhausted);
+
+// Persistent primary rays with per-lane refill.  Ray index i maps to pixel
+// tile i/32 (8x4 pixels, row-major tiles) and lane i%32 inside it, so the
+// rays a warp fetches together are neighbours.
+template <bool kCount>
+__global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
+k_primary_tri_dyn(DevScene sc, FrameParams fp, mrt_gbuffer g, uint32_t* status, unsigned long long* totals,
+                  uint32_t* fetch) {
+    __shared__ uint2 stk[kStackDepth * kTraceBlock];
+    const uint32_t tiles_x = (fp.width + 7u) / 8u, tiles_y = (fp.height + 3u) / 4u;
+    const uint32_t n = tiles_x * tiles_y * 32u;
+    uint2* my = stk + threadIdx.x;
+    uint32_t st = 0u, cn = 0u, ct = 0u, px = 0u, py = 0u;
+    Trav s;
+    bool have = false, exhausted = false;
+    while (true) {
+        const uint32_t idx = warp_refill(fetch, n, !have, exhausted);
+        if (idx != kMiss) {
+            const uint32_t tile = idx >> 5, l = idx & 31u;
+            const uint32_t x = (tile % tiles_x) * 8u + (l & 7u), y = (tile / tiles_x) * 4u + (l >> 3);
+            if (x < fp.width && y < fp.height) {
+                f3 o, d;
+                primary_ray(fp, x, y, o, d);
+                trav_init(s, o, d, 0.0f, INFINITY);
+                px = x;
+                py = y;
+                have = true;
+            }
+        }
+        const bool any = __any_sync(0xFFFFFFFFu, have);
+        if (!any && exhausted) break;
+        if (have && trav_step<false, kCount, kStackDepth>(sc, s, my, kTraceBlock, st, cn, ct)) {
+            have = false;
+            const uint32_t prim = s.best;
+            const float t = prim == kMiss ? s.tmax : s.tbest;
+            const size_t pi = size_t(py) * fp.width + px;
+            g.visibility[pi] = prim;
+            if (g.hit_t) g.hit_t[pi] = t;
+            if (g.depth || g.normal || g.motion) {
+                f3 o, d;
+                primary_ray(fp, px, py, o, d);
+                const bool hit = prim != kMiss;
+                f3 pos = o, nrm = d;
+                if (hit) {
+                    pos = ray_at(o, d, t);
+                    nrm = facing_normal(load_mat(sc, prim, status), d);
+                }
+                store_extras(fp, g, pi, hit, pos, nrm);
+            }
+        }
+    }
+    if (st) atomicOr(status, st);
+    if (kCount) {
+        atomicAdd(totals + kTotNodesPrim, (unsigned long long)cn);
+        atomicAdd(totals + kTotTrisPrim, (unsigned long long)ct);
     }
 }
 
@@ -395,30 +454,72 @@ k_shade(DevScene sc, TraceParams tp, BlueNoise bn, WaveBuffers wb, uint32_t widt
     }
 }
 
-// Persistent closest-hit over the extension queue of bounce `bounce`;
-// each warp fetches 32 rays at a time.
-template <bool kCount>
-__global__ void __launch_bounds__(kTraceBlock)
+// Per-lane work refill for persistent traversal (Aila & Laine, "Understanding
+// the efficiency of ray traversal on GPUs", HPG 2009, dynamic fetch): the
+// lanes that `need` a ray share one atomic on the work counter.  Returns the
+// lane's new ray index or kMiss.  `exhausted` is warp-uniform and stops all
+// further fetches once the counter has passed n, so the counter grows by at
+// most n + 32 per warp.  Must be called by all 32 lanes.
+MRT_DEV uint32_t warp_refill(uint32_t* fetch, uint32_t n, bool need, bool& exhausted) {
+    if (exhausted) return kMiss;
+    const uint32_t mask = __ballot_sync(0xFFFFFFFFu, need);
+    if (!mask) return kMiss;
+    const uint32_t lane = lane_id(), leader = __ffs(mask) - 1u, cnt = __popc(mask);
+    uint32_t base = 0u;
+    if (lane == leader) base = atomicAdd(fetch, cnt);
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    if (base + cnt >= n) exhausted = true;
+    if (!need) return kMiss;
+    const uint32_t i = base + __popc(mask & ((1u << lane) - 1u));
+    return i < n ? i : kMiss;
+}
+
+// Persistent closest-hit over the extension queue of bounce `bounce`.
+// kDyn: idle lanes refill after every traversal step; otherwise each warp
+// fetches 32 rays and runs them all to completion.
+template <bool kCount, bool kDyn>
+__global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
 k_trace_ext(DevScene sc, WaveBuffers wb, uint32_t bounce, uint32_t* status) {
     __shared__ uint2 stk[kStackDepth * kTraceBlock];
     const uint32_t n = wb.counters[kCntExt + bounce];
     const PathRay* q = (bounce & 1u) ? wb.q[1] : wb.q[0];
     uint32_t* fetch = wb.counters + kCntFetchExt + bounce;
-    const uint32_t lane = lane_id();
+    uint2* my = stk + threadIdx.x;
     uint32_t st = 0u, cn = 0u, ct = 0u;
-    while (true) {
-        uint32_t base = 0u;
-        if (lane == 0u) base = atomicAdd(fetch, 32u);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (base >= n) break;
-        const uint32_t i = base + lane;
-        if (i < n) {
-            const float4 a = q[i].o_pix, b = q[i].d;
-            uint32_t prim;
-            float t;
-            trace_bvh8<false, kCount, kStackDepth>(sc, f3{a.x, a.y, a.z}, f3{b.x, b.y, b.z}, 0.0f, INFINITY, prim, t,
-                                                   stk + threadIdx.x, kTraceBlock, st, cn, ct);
-            wb.hits[i] = make_uint2(prim, __float_as_uint(t));
+    if (kDyn) {
+        Trav s;
+        bool have = false, exhausted = false;
+        uint32_t ri = 0u;
+        while (true) {
+            const uint32_t idx = warp_refill(fetch, n, !have, exhausted);
+            if (idx != kMiss) {
+                const float4 a = q[idx].o_pix, b = q[idx].d;
+                trav_init(s, f3{a.x, a.y, a.z}, f3{b.x, b.y, b.z}, 0.0f, INFINITY);
+                ri = idx;
+                have = true;
+            }
+            if (!__any_sync(0xFFFFFFFFu, have)) break;
+            if (have && trav_step<false, kCount, kStackDepth>(sc, s, my, kTraceBlock, st, cn, ct)) {
+                wb.hits[ri] = make_uint2(s.best, __float_as_uint(s.best == kMiss ? s.tmax : s.tbest));
+                have = false;
+            }
+        }
+    } else {
+        const uint32_t lane = lane_id();
+        while (true) {
+            uint32_t base = 0u;
+            if (lane == 0u) base = atomicAdd(fetch, 32u);
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base >= n) break;
+            const uint32_t i = base + lane;
+            if (i < n) {
+                const float4 a = q[i].o_pix, b = q[i].d;
+                uint32_t prim;
+                float t;
+                trace_bvh8<false, kCount, kStackDepth>(sc, f3{a.x, a.y, a.z}, f3{b.x, b.y, b.z}, 0.0f, INFINITY,
+                                                       prim, t, my, kTraceBlock, st, cn, ct);
+                wb.hits[i] = make_uint2(prim, __float_as_uint(t));
+            }
         }
     }
     if (st) atomicOr(status, st);
@@ -430,29 +531,53 @@ k_trace_ext(DevScene sc, WaveBuffers wb, uint32_t bounce, uint32_t* status) {
 
 // Persistent any-hit over the shadow queue of vertex `vertex`; unoccluded
 // rays add their contribution to the pixel's radiance.
-template <bool kCount>
-__global__ void __launch_bounds__(kTraceBlock)
+template <bool kCount, bool kDyn>
+__global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
 k_trace_shadow(DevScene sc, WaveBuffers wb, TraceParams tp, uint32_t vertex, uint32_t* status) {
     __shared__ uint2 stk[kStackDepth * kTraceBlock];
     const uint32_t n = wb.counters[kCntShadow + vertex];
     uint32_t* fetch = wb.counters + kCntFetchShadow + vertex;
-    const uint32_t lane = lane_id();
     const f3 sun{tp.sun[0], tp.sun[1], tp.sun[2]};
+    uint2* my = stk + threadIdx.x;
     uint32_t st = 0u, cn = 0u, ct = 0u;
-    while (true) {
-        uint32_t base = 0u;
-        if (lane == 0u) base = atomicAdd(fetch, 32u);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (base >= n) break;
-        const uint32_t i = base + lane;
-        if (i < n) {
-            const ShadowRay sr = wb.sq[i];
-            uint32_t prim;
-            float t;
-            trace_bvh8<true, kCount, kStackDepth>(sc, f3{sr.o_pix.x, sr.o_pix.y, sr.o_pix.z}, sun, 0.0f, INFINITY,
-                                                  prim, t, stk + threadIdx.x, kTraceBlock, st, cn, ct);
-            if (prim == kMiss)
-                add_L(wb.L, __float_as_uint(sr.o_pix.w), f3{sr.contrib.x, sr.contrib.y, sr.contrib.z});
+    if (kDyn) {
+        Trav s;
+        bool have = false, exhausted = false;
+        uint32_t ri = 0u;
+        while (true) {
+            const uint32_t idx = warp_refill(fetch, n, !have, exhausted);
+            if (idx != kMiss) {
+                const float4 a = wb.sq[idx].o_pix;
+                trav_init(s, f3{a.x, a.y, a.z}, sun, 0.0f, INFINITY);
+                ri = idx;
+                have = true;
+            }
+            if (!__any_sync(0xFFFFFFFFu, have)) break;
+            if (have && trav_step<true, kCount, kStackDepth>(sc, s, my, kTraceBlock, st, cn, ct)) {
+                if (s.best == kMiss) {
+                    const ShadowRay sr = wb.sq[ri];
+                    add_L(wb.L, __float_as_uint(sr.o_pix.w), f3{sr.contrib.x, sr.contrib.y, sr.contrib.z});
+                }
+                have = false;
+            }
+        }
+    } else {
+        const uint32_t lane = lane_id();
+        while (true) {
+            uint32_t base = 0u;
+            if (lane == 0u) base = atomicAdd(fetch, 32u);
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base >= n) break;
+            const uint32_t i = base + lane;
+            if (i < n) {
+                const ShadowRay sr = wb.sq[i];
+                uint32_t prim;
+                float t;
+                trace_bvh8<true, kCount, kStackDepth>(sc, f3{sr.o_pix.x, sr.o_pix.y, sr.o_pix.z}, sun, 0.0f,
+                                                      INFINITY, prim, t, my, kTraceBlock, st, cn, ct);
+                if (prim == kMiss)
+                    add_L(wb.L, __float_as_uint(sr.o_pix.w), f3{sr.contrib.x, sr.contrib.y, sr.contrib.z});
+            }
         }
     }
     if (st) atomicOr(status, st);
@@ -485,7 +610,7 @@ k_finalize(WaveBuffers wb, float* color, uint32_t npix, uint32_t samples, uint32
 }
 
 template <bool kAnyHit, bool kCount>
-__global__ void __launch_bounds__(kTraceBlock)
+__global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
 k_trace_rays(DevScene sc, const mrt_ray* rays, uint32_t n, mrt_hit* hits, uint32_t* nodes_v, uint32_t* tris_v,
              uint32_t* status) {
     __shared__ uint2 stk[kStackDepth * kTraceBlock];
@@ -532,7 +657,14 @@ k_trace_rays_sphere(DevScene sc, const mrt_ray* rays, uint32_t n, mrt_hit* hits)
 // ------------------------------------------------------------------ launchers
 
 cudaError_t launch_primary_tri(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g, uint32_t* status,
-                               unsigned long long* totals, cudaStream_t s) {
+                               unsigned long long* totals, uint32_t* fetch, int blocks, cudaStream_t s) {
+    if (fetch) {
+        cudaError_t e = cudaMemsetAsync(fetch, 0, sizeof(uint32_t), s);
+        if (e != cudaSuccess) return e;
+        if (totals) k_primary_tri_dyn<true><<<blocks, kTraceBlock, 0, s>>>(sc, fp, g, status, totals, fetch);
+        else k_primary_tri_dyn<false><<<blocks, kTraceBlock, 0, s>>>(sc, fp, g, status, nullptr, fetch);
+        return cudaGetLastError();
+    }
     dim3 grid((fp.width + 15) / 16, (fp.height + 7) / 8);
     if (totals) k_primary_tri<true><<<grid, kTraceBlock, 0, s>>>(sc, fp, g, status, totals);
     else k_primary_tri<false><<<grid, kTraceBlock, 0, s>>>(sc, fp, g, status, nullptr);
@@ -583,16 +715,26 @@ cudaError_t launch_shade_primary(const DevScene& sc, const FrameParams& fp, cons
 }
 
 cudaError_t launch_trace_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t bounce, int blocks, uint32_t* status,
-                             bool count, cudaStream_t s) {
-    if (count) k_trace_ext<true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
-    else k_trace_ext<false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
+                             bool count, bool dyn, cudaStream_t s) {
+    if (count) {
+        if (dyn) k_trace_ext<true, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
+        else k_trace_ext<true, false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
+    } else {
+        if (dyn) k_trace_ext<false, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
+        else k_trace_ext<false, false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_trace_shadow(const DevScene& sc, const WaveBuffers& wb, const TraceParams& tp, uint32_t vertex,
-                                int blocks, uint32_t* status, bool count, cudaStream_t s) {
-    if (count) k_trace_shadow<true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
-    else k_trace_shadow<false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
+                                int blocks, uint32_t* status, bool count, bool dyn, cudaStream_t s) {
+    if (count) {
+        if (dyn) k_trace_shadow<true, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
+        else k_trace_shadow<true, false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
+    } else {
+        if (dyn) k_trace_shadow<false, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
+        else k_trace_shadow<false, false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
+    }
     return cudaGetLastError();
 }
 
@@ -619,7 +761,8 @@ cudaError_t launch_tally(const WaveBuffers& wb, cudaStream_t s) {
 
 int trace_blocks_per_sm() {
     int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_ext<false>, kTraceBlock, 0) != cudaSuccess || b < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_ext<false, true>, kTraceBlock, 0) != cudaSuccess ||
+        b < 1)
         b = 1;
     return b;
 }

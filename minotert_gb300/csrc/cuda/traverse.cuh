@@ -111,45 +111,64 @@ MRT_DEV float byte_to_float(uint32_t word, uint32_t k) {
     return __fsub_rn(__int_as_float(__byte_perm(word, 0x4B000000u, k | 0x7440u)), 8388608.0f);
 }
 
-// Closest hit (kAnyHit = false) or first hit with t < tmax (kAnyHit = true).
-// `stk` points at this thread's first stack slot; slot i is stk[i * stride].
-// Returns the number of loop iterations (for the counters).
-template <bool kAnyHit, bool kCount, int kStack>
-MRT_DEV void trace_bvh8(const DevScene& sc, f3 o, f3 d, float tmin, float tmax, uint32_t& hit_prim,
-                        float& hit_t, uint2* stk, uint32_t stride, uint32_t& status,
-                        uint32_t& cnt_nodes, uint32_t& cnt_tris) {
-    const RayPre r = ray_pre(o, d);
-    float tbest = tmax;
-    uint32_t best = kMiss;
-    // current internal-node group: base index, hit keys (bit k: slot k^oct),
-    // imask of the node the group came from
-    uint32_t g_base = 0, g_hits = 1u << r.oct, g_imask = 1u;
-    int sp = 0;
-    const uint32_t cap = sc.node_count + 64u;
-    uint32_t iters = 0;
-    const bool negx = r.ix < 0.0f, negy = r.iy < 0.0f, negz = r.iz < 0.0f;
+// Resumable traversal state of one ray.  The group (g_base, g_hits,
+// g_imask) is the current internal-node group: base index of the children,
+// hit keys (bit k: child slot k ^ oct), imask of the node the group came
+// from.  Stack slot i of a thread lives at stk[i * stride].
+struct Trav {
+    RayPre r;
+    float tmin, tmax, tbest;
+    uint32_t best;
+    uint32_t g_base, g_hits, g_imask;
+    int sp;
+    uint32_t iters;
+};
 
-    while (true) {
-        if (g_hits == 0u) {
-            if (sp == 0) break;
-            --sp;
-            const uint2 e = stk[sp * stride];
-            g_base = e.x;
-            g_hits = e.y >> 8;
-            g_imask = e.y & 0xFFu;
-        }
-        const uint32_t key = __ffs(g_hits) - 1u;
-        g_hits &= g_hits - 1u;
-        const uint32_t slot = key ^ r.oct;
-        const uint32_t node = g_base + __popc(g_imask & ((1u << slot) - 1u));
-        if (g_hits) {
-            if (sp >= kStack) { status |= MRT_STATUS_STACK_OVF; break; }
-            stk[sp * stride] = make_uint2(g_base, (g_hits << 8) | g_imask);
-            ++sp;
-        }
-        if (++iters > cap) { status |= MRT_STATUS_ITER_CAP; break; }
-        if (node >= sc.node_count) { status |= MRT_STATUS_BAD_NODE; break; }
-        if (kCount) ++cnt_nodes;
+MRT_DEV void trav_init(Trav& s, f3 o, f3 d, float tmin, float tmax) {
+    s.r = ray_pre(o, d);
+    s.tmin = tmin;
+    s.tmax = tmax;
+    s.tbest = tmax;
+    s.best = kMiss;
+    s.g_base = 0u;
+    s.g_hits = 1u << s.r.oct; // the root is child slot 0 of a virtual group
+    s.g_imask = 1u;
+    s.sp = 0;
+    s.iters = 0u;
+}
+
+// One traversal step: visit the next node (box tests of its 8 children)
+// and test the triangles of its hit leaves.  Returns true when the ray is
+// finished (s.best / s.tbest hold the result).  Every path through the
+// step is bounded: at most 24 triangle tests, and the iteration cap
+// (node_count + 64 node visits) ends a ray whose BVH links cycle.
+template <bool kAnyHit, bool kCount, int kStack>
+MRT_DEV bool trav_step(const DevScene& sc, Trav& s, uint2* stk, uint32_t stride, uint32_t& status,
+                       uint32_t& cnt_nodes, uint32_t& cnt_tris) {
+    const RayPre& r = s.r;
+    if (s.g_hits == 0u) {
+        if (s.sp == 0) return true;
+        --s.sp;
+        const uint2 e = stk[s.sp * stride];
+        s.g_base = e.x;
+        s.g_hits = e.y >> 8;
+        s.g_imask = e.y & 0xFFu;
+    }
+    const uint32_t key = __ffs(s.g_hits) - 1u;
+    s.g_hits &= s.g_hits - 1u;
+    const uint32_t slot = key ^ r.oct;
+    const uint32_t node = s.g_base + __popc(s.g_imask & ((1u << slot) - 1u));
+    if (s.g_hits) {
+        if (s.sp >= kStack) { status |= MRT_STATUS_STACK_OVF; return true; }
+        stk[s.sp * stride] = make_uint2(s.g_base, (s.g_hits << 8) | s.g_imask);
+        ++s.sp;
+    }
+    if (++s.iters > sc.node_count + 64u) { status |= MRT_STATUS_ITER_CAP; return true; }
+    if (node >= sc.node_count) { status |= MRT_STATUS_BAD_NODE; return true; }
+    if (kCount) ++cnt_nodes;
+    {
+        const float tmin = s.tmin, tbest = s.tbest;
+        const bool negx = r.ix < 0.0f, negy = r.iy < 0.0f, negz = r.iz < 0.0f;
 
         const uint4* np = sc.nodes + size_t(node) * 8u;
         const uint4 L0 = __ldg(np + 0), L1 = __ldg(np + 1), L2 = __ldg(np + 2), L3 = __ldg(np + 3),
@@ -189,16 +208,16 @@ MRT_DEV void trace_bvh8(const DevScene& sc, f3 o, f3 d, float tmin, float tmax, 
                 else tri_mask |= (meta >> 5) << (meta & 31u);
             }
         }
-        g_base = L1.x;
-        g_hits = int_keys;
-        g_imask = imask;
+        s.g_base = L1.x;
+        s.g_hits = int_keys;
+        s.g_imask = imask;
 
         const uint32_t tri_base = L1.y;
         while (tri_mask) {
             const uint32_t bit = __ffs(tri_mask) - 1u;
             tri_mask &= tri_mask - 1u;
             const uint32_t ti = tri_base + bit;
-            if (ti >= sc.tri_count) { status |= MRT_STATUS_BAD_TRI; tri_mask = 0u; g_hits = 0u; sp = 0; break; }
+            if (ti >= sc.tri_count) { status |= MRT_STATUS_BAD_TRI; return true; }
             if (kCount) ++cnt_tris;
             const float4* tp = sc.tris + size_t(ti) * 3u;
             const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), c = __ldg(tp + 2);
@@ -206,16 +225,29 @@ MRT_DEV void trace_bvh8(const DevScene& sc, f3 o, f3 d, float tmin, float tmax, 
             if (intersect_tri(r, a, b, c, tmin, t)) {
                 const uint32_t id = __float_as_uint(a.w);
                 if (kAnyHit) {
-                    if (t < tmax) { best = id; tbest = t; tri_mask = 0u; g_hits = 0u; sp = 0; break; }
-                } else if (t < tbest || (t == tbest && id < best)) {
-                    tbest = t;
-                    best = id;
+                    if (t < s.tmax) { s.best = id; s.tbest = t; return true; }
+                } else if (t < s.tbest || (t == s.tbest && id < s.best)) {
+                    s.tbest = t;
+                    s.best = id;
                 }
             }
         }
     }
-    hit_prim = best;
-    hit_t = best == kMiss ? tmax : tbest;
+    return s.g_hits == 0u && s.sp == 0;
+}
+
+// Closest hit (kAnyHit = false) or first hit with t < tmax (kAnyHit = true)
+// of one ray, run to completion.
+template <bool kAnyHit, bool kCount, int kStack>
+MRT_DEV void trace_bvh8(const DevScene& sc, f3 o, f3 d, float tmin, float tmax, uint32_t& hit_prim,
+                        float& hit_t, uint2* stk, uint32_t stride, uint32_t& status,
+                        uint32_t& cnt_nodes, uint32_t& cnt_tris) {
+    Trav s;
+    trav_init(s, o, d, tmin, tmax);
+    while (!trav_step<kAnyHit, kCount, kStack>(sc, s, stk, stride, status, cnt_nodes, cnt_tris)) {
+    }
+    hit_prim = s.best;
+    hit_t = s.best == kMiss ? s.tmax : s.tbest;
 }
 
 // Reference ray/sphere test (intersect.glsl:26-37): the nearer root of

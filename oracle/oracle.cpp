@@ -412,7 +412,7 @@ void trace_bvh32(const Node* nodes, uint32_t nn, const Tri* tris, uint32_t nt, c
         uint32_t slot = key ^ r.oct;
         uint32_t node = g_base + uint32_t(__builtin_popcount(g_imask & ((1u << slot) - 1u)));
         if (g_hits) {
-            if (sp >= 32) { if (status) *status |= 2u; break; }
+            if (sp >= 24) { if (status) *status |= 2u; break; }  // the kernels' 24-entry stack
             stk[sp++] = E{g_base, g_hits, g_imask};
         }
         if (++iters > nn + 64u) { if (status) *status |= 1u; break; }
