@@ -15,11 +15,14 @@
 //   quantised BVH8 decode + stack traversal    Ylitie, Karras & Laine, HPG 2017
 //   directional-light path estimator           (new; specified in the design notes)
 //
-// Parity status: the reference publishes no golden vectors or tests and its
-// Vulkan/MSVC build cannot run here, so the oracle is pinned by (a) known-
-// answer values computed from the published formulas (PCG, the camera
-// matrices, analytic ray/sphere and ray/triangle cases) committed under
-// tests/golden, and (b) brute-force cross-checks of its own BVH traversal.
+// Parity status: PARITY UNPINNED.  The reference ships no tests, golden
+// vectors or fixtures, and its own implementation (GLSL through Vulkan,
+// MSVC-only host code) cannot run here, so nothing of the reference itself
+// pins this restatement.  It is checked instead against (a) known-answer
+// values computed independently from the formulas in the reference source
+// (PCG, 24-bit floats, sphere points, the camera matrices; analytic
+// ray/sphere and ray/triangle cases) committed under tests/golden, and
+// (b) brute-force cross-checks of its own BVH traversal.
 //
 // FP32 mode reproduces the kernels' arithmetic order (explicit fma where the
 // kernels use one, no contraction elsewhere; built with -ffp-contract=off),
