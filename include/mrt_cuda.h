@@ -332,6 +332,44 @@ int mrt_cuda_trace_rays_counted(mrt_ctx* ctx, const mrt_scene* scene,
                                 uint32_t* nodes_visited, uint32_t* tris_visited,
                                 void* stream);
 
+/* Primary rays for callers that cannot allocate device memory.
+ *
+ * No counterpart in the reference.  Some callers of this library may not
+ * call cudaMalloc: a renderer whose host engine owns every device byte
+ * through its own pool or budget, code running while a stream is being
+ * captured into a CUDA graph (where a cudaMalloc is not recorded), or a
+ * plug-in whose host forbids allocations on its render thread.  They pass
+ * their own device buffers for the scene (BVH8 nodes, leaf-ordered
+ * triangles, materials, as built by mrt_bvh8_build) and for the g-buffer,
+ * and this entry point allocates nothing: no context, no cudaMalloc or
+ * cudaFree, no allocating library call.
+ *
+ * It runs the persistent dynamic-fetch primary-ray kernel, whose work
+ * counter (and, when `status` is NULL, its status word) live in a
+ * file-scope device array of 256 bytes that every GPU loading the library
+ * holds until the process exits.  The results equal mrt_cuda_primary_rays.
+ *
+ *   - Works on the calling thread's current CUDA device.  The first call on
+ *     a device looks up that device's copy of the array and its launch
+ *     size; make that first call before any stream capture.
+ *   - width * height must be at most MRT_NOALLOC_MAX_PIXELS; larger images
+ *     return MRT_ERANGE and launch nothing.
+ *   - All calls on a device share the one array, which keeps the previous
+ *     call's contents; each call clears what must start at zero on
+ *     `stream`.  Calls whose work overlaps on the GPU (other streams, other
+ *     threads) race on the array: serialise them.
+ *   - `status` (device, may be NULL) receives MRT_STATUS_* bits ORed in;
+ *     the caller clears it.  BVH depth is not checked on the host here (the
+ *     device stack check reports MRT_STATUS_STACK_OVF instead).
+ * Returns MRT_OK, MRT_EINVAL (null pointer, zero size), MRT_ERANGE (too
+ * large) or MRT_ECUDA. */
+#define MRT_NOALLOC_MAX_PIXELS (1u << 26)
+int mrt_cuda_primary_rays_noalloc(const mrt_bvh8_node* nodes, uint32_t node_count,
+                                  const mrt_tri* tris, uint32_t tri_count,
+                                  const mrt_material* materials, uint32_t material_count,
+                                  const mrt_camera_consts* consts, const mrt_gbuffer* gbuffer,
+                                  uint32_t* status, void* stream);
+
 /* One whole frame through HOST buffers: primary + secondary passes on
  * library-owned device buffers, then copies of visibility, hit_t (may be
  * NULL) and color (float RGB) back to the host.  Synchronises `stream`. */

@@ -157,6 +157,8 @@ def lib() -> C.CDLL:
             "mrt_cuda_trace_rays_counted": ([vp, vp, vp, u32, vp, vp, vp, vp], i32),
             "mrt_cuda_render_frame_host": ([vp, vp, C.POINTER(CameraConsts), C.POINTER(TraceParams), u32, u32,
                                             vp, vp, vp, vp], i32),
+            "mrt_cuda_primary_rays_noalloc": ([vp, u32, vp, u32, vp, u32, C.POINTER(CameraConsts),
+                                               C.POINTER(GBuffer), vp, vp], i32),
             # host modules
             "mrt_camera_view": ([C.POINTER(Camera_C), C.POINTER(C.c_float)], None),
             "mrt_camera_projection": ([C.POINTER(Camera_C), C.POINTER(C.c_float)], None),

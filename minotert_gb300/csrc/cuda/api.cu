@@ -182,6 +182,11 @@ int check_gbuffer(mrt_ctx* ctx, const mrt_gbuffer* g) {
 
 } // namespace
 
+namespace mrt {
+// Frame constants for entry points outside this file (noalloc.cu).
+FrameParams make_frame_params(const mrt_camera_consts* c, uint32_t w, uint32_t h) { return frame_params(c, w, h); }
+} // namespace mrt
+
 extern "C" {
 
 int mrt_cuda_abi_version(void) { return MRT_ABI_VERSION; }
