@@ -237,13 +237,18 @@ int mrt_cuda_frame_stats(mrt_ctx* ctx, mrt_frame_stats* out);
  * autotuner; defaults are the tuned values for GB300. */
 typedef struct mrt_tuning {
     uint32_t trace_blocks_per_sm; /* persistent blocks per SM; 0 = occupancy max */
-    uint32_t dynamic_fetch;       /* 1: idle lanes refill after every node step
-                                     (0: each warp fetches 32 rays)          */
+    uint32_t dynamic_fetch;       /* bit 0: extension rays, bit 1: shadow rays
+                                     refill idle lanes after every node step
+                                     (clear: each warp fetches 32 rays and
+                                     runs them to completion)                */
     uint32_t primary_persistent;  /* 1: primary rays through the persistent
                                      dynamic-fetch kernel (0: one thread per
                                      pixel, 8x4-pixel warps)                 */
-    uint32_t sort_min_rays;       /* sort extension queues with at least this
-                                     many rays when sort_rays is set          */
+    uint32_t sort_min_rays;       /* sort extension queues holding at least
+                                     this many rays (direction octant + origin
+                                     Morton key); 0xFFFFFFFF = never.  A call
+                                     with mrt_trace_params.sort_rays = 1 sorts
+                                     every queue                             */
 } mrt_tuning;
 int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning);
 int mrt_cuda_get_tuning(mrt_ctx* ctx, mrt_tuning* tuning);
@@ -331,6 +336,36 @@ int mrt_cuda_trace_rays_counted(mrt_ctx* ctx, const mrt_scene* scene,
                                 const mrt_ray* rays, uint32_t count, mrt_hit* hits,
                                 uint32_t* nodes_visited, uint32_t* tris_visited,
                                 void* stream);
+
+/* ---- batched scenes (new: the reference renders one scene) ----------- */
+/* Concatenates `count` BVH8 scenes into one device BVH: child and triangle
+ * indices are rebased and triangle ids are offset by the triangle counts of
+ * the preceding scenes, so hits report batch-wide ids (scene s's local id =
+ * prim - sum of tri_counts[0..s-1]).  Rays of any scene then trace in one
+ * persistent launch, each starting at its own scene's root node. */
+typedef struct mrt_batch mrt_batch;
+int mrt_cuda_batch_create(mrt_ctx* ctx, uint32_t scene_count,
+                          const mrt_bvh8_node* const* nodes, const uint32_t* node_counts,
+                          const mrt_tri* const* tris, const uint32_t* tri_counts,
+                          const mrt_material* const* materials, mrt_batch** out);
+int mrt_cuda_batch_destroy(mrt_ctx* ctx, mrt_batch* batch);
+/* Closest hit (flags = 0) or any hit of `rays` (device), grouped by scene:
+ * scene s owns rays [ray_offsets[s], ray_offsets[s+1]) (host array of
+ * scene_count + 1 entries). */
+int mrt_cuda_batch_trace(mrt_ctx* ctx, mrt_batch* batch, const mrt_ray* rays,
+                         const uint32_t* ray_offsets, mrt_hit* hits, uint32_t flags,
+                         void* stream);
+/* Closest-hit Lambertian path trace of the given primary rays over
+ * params->max_bounces diffuse bounces: throughput x albedo, sky radiance on
+ * escape, a per-ray PCG stream seeded by (ray index, frame), compaction of
+ * live paths after every bounce.  radiance: device float RGB per ray.
+ * use_graph != 0: the first call captures the whole bounce loop into a
+ * CUDA graph (kept in the batch for these buffers and sizes) and later
+ * calls replay it with one launch; make that first call outside any
+ * caller's stream capture. */
+int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* batch, const mrt_ray* rays,
+                             const uint32_t* ray_offsets, const mrt_trace_params* params,
+                             uint32_t frame, float* radiance, int use_graph, void* stream);
 
 /* Primary rays for callers that cannot allocate device memory.
  *

@@ -159,6 +159,10 @@ def lib() -> C.CDLL:
                                             vp, vp, vp, vp], i32),
             "mrt_cuda_primary_rays_noalloc": ([vp, u32, vp, u32, vp, u32, C.POINTER(CameraConsts),
                                                C.POINTER(GBuffer), vp, vp], i32),
+            "mrt_cuda_batch_create": ([vp, u32, vp, vp, vp, vp, vp, pp], i32),
+            "mrt_cuda_batch_destroy": ([vp, vp], i32),
+            "mrt_cuda_batch_trace": ([vp, vp, vp, vp, vp, u32, vp], i32),
+            "mrt_cuda_batch_pathtrace": ([vp, vp, vp, vp, C.POINTER(TraceParams), u32, vp, i32, vp], i32),
             # host modules
             "mrt_camera_view": ([C.POINTER(Camera_C), C.POINTER(C.c_float)], None),
             "mrt_camera_projection": ([C.POINTER(Camera_C), C.POINTER(C.c_float)], None),

@@ -22,10 +22,14 @@ from ._lib import Context
 DEFAULT_CACHE = Path(__file__).resolve().parent / "_build" / "autotune.json"
 
 
+SORT_NEVER = 0xFFFFFFFF
+
+
 def candidates(max_blocks_per_sm: int, sort: bool = False):
     blocks = sorted({b for b in (1, 2, 3, 4, 5, 6, 8) if b <= max_blocks_per_sm} | {max_blocks_per_sm})
-    sort_thr = [1 << 30, 1 << 18] if sort else [1 << 30]
-    for b, dyn, prim, thr in itertools.product(blocks, (1, 0), (1, 0), sort_thr):
+    sort_thr = [SORT_NEVER, 1 << 18, 1 << 14] if sort else [SORT_NEVER]
+    # dynamic_fetch bit 0: extension rays, bit 1: shadow rays
+    for b, dyn, prim, thr in itertools.product(blocks, (1, 3, 0, 2), (0, 1), sort_thr):
         yield {"trace_blocks_per_sm": b, "dynamic_fetch": dyn, "primary_persistent": prim, "sort_min_rays": thr}
 
 

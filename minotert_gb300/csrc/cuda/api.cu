@@ -4,6 +4,7 @@
 #include "internal.hpp"
 
 #include <chrono>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -127,7 +128,10 @@ int ensure_wave(mrt_ctx* ctx, size_t npix) {
               cudaMalloc(&wb.sq, cap * sizeof(ShadowRay)) == cudaSuccess &&
               cudaMalloc(&wb.L, npix * sizeof(float4)) == cudaSuccess &&
               cudaMalloc(&wb.rng, npix * sizeof(uint32_t)) == cudaSuccess &&
-              cudaMalloc(&wb.counters, kCntSlots * sizeof(uint32_t)) == cudaSuccess;
+              cudaMalloc(&wb.counters, kCntSlots * sizeof(uint32_t)) == cudaSuccess &&
+              cudaMalloc(&wb.keys, cap * sizeof(uint32_t)) == cudaSuccess &&
+              cudaMalloc(&wb.qsort, cap * sizeof(PathRay)) == cudaSuccess &&
+              cudaMalloc(&wb.hist, 4096 * sizeof(uint32_t)) == cudaSuccess;
     wb.totals = ctx->d_totals;
     if (!ok) {
         free_wave(wb);
@@ -185,6 +189,11 @@ int check_gbuffer(mrt_ctx* ctx, const mrt_gbuffer* g) {
 namespace mrt {
 // Frame constants for entry points outside this file (noalloc.cu).
 FrameParams make_frame_params(const mrt_camera_consts* c, uint32_t w, uint32_t h) { return frame_params(c, w, h); }
+// Error reporting, persistent grid size and trace-parameter conversion for
+// the other C-ABI files (batch.cu).
+int set_error(mrt_ctx* ctx, int code, const char* msg) { return fail(ctx, code, "%s", msg); }
+int persistent_blocks(mrt_ctx* ctx) { return trace_blocks(ctx); }
+TraceParams make_trace_params(const mrt_trace_params* p) { return trace_params(p); }
 } // namespace mrt
 
 extern "C" {
@@ -273,7 +282,7 @@ int mrt_cuda_set_timing(mrt_ctx* ctx, int enable) {
 
 int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning) {
     if (!ctx || !tuning) return fail(ctx, MRT_EINVAL, "set_tuning: null argument");
-    if (tuning->trace_blocks_per_sm > 64 || tuning->dynamic_fetch > 1 || tuning->primary_persistent > 1)
+    if (tuning->trace_blocks_per_sm > 64 || tuning->dynamic_fetch > 3 || tuning->primary_persistent > 1)
         return fail(ctx, MRT_EINVAL, "set_tuning: value out of range");
     ctx->tuning = *tuning;
     return MRT_OK;
@@ -501,6 +510,21 @@ int mrt_cuda_scene_upload_triangles(mrt_ctx* ctx, const mrt_bvh8_node* nodes, ui
     sc->dev.tri_count = tri_count;
     sc->dev.mat_count = material_count;
     sc->dev.sphere_count = 0;
+    // scene bounds from the root's quantised child boxes (conservative)
+    {
+        const mrt_bvh8_node& r = nodes[0];
+        const uint8_t* ql[3] = {r.q_lo_x, r.q_lo_y, r.q_lo_z};
+        const uint8_t* qh[3] = {r.q_hi_x, r.q_hi_y, r.q_hi_z};
+        for (int a = 0; a < 3; ++a) {
+            int lo = 255, hi = 0;
+            for (int s = 0; s < 8; ++s)
+                if (r.meta[s]) { lo = ql[a][s] < lo ? ql[a][s] : lo; hi = qh[a][s] > hi ? qh[a][s] : hi; }
+            const float sc_e = std::ldexp(1.0f, r.exp[a]);
+            const float l = r.origin[a] + float(lo) * sc_e, h = r.origin[a] + float(hi) * sc_e;
+            sc->dev.lo[a] = l;
+            sc->dev.inv_ext[a] = h > l ? 1.0f / (h - l) : 0.0f;
+        }
+    }
     *out = sc;
     return MRT_OK;
 }
@@ -617,7 +641,8 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
     if (rc) return rc;
     WaveBuffers& wb = ctx->wb;
     const int tblocks = trace_blocks(ctx);
-    const bool nee = tp.estimator == MRT_EST_NEE, dyn = ctx->tuning.dynamic_fetch != 0u;
+    const bool nee = tp.estimator == MRT_EST_NEE;
+    const bool dyn = (ctx->tuning.dynamic_fetch & 1u) != 0u, dyn_sh = (ctx->tuning.dynamic_fetch & 2u) != 0u;
 #define MRT_LAUNCH(kind, bounce, expr)                                                                   \
     do {                                                                                                 \
         Scope sc_(ctx, s, kind, bounce);                                                                 \
@@ -631,14 +656,18 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
         for (uint32_t b = 1; b <= tp.max_bounces; ++b) {
             if (nee)
                 MRT_LAUNCH(2, int(b - 1), launch_trace_shadow(scene->dev, wb, tp, b - 1, tblocks, ctx->d_status,
-                                                              ctx->counters, dyn, s));
-            if (params->sort_rays) MRT_LAUNCH(4, int(b), launch_sort_ext(scene->dev, wb, b, s));
+                                                              ctx->counters, dyn_sh, s));
+            if (params->sort_rays || ctx->tuning.sort_min_rays != kSortNever) {
+                MRT_LAUNCH(4, int(b), launch_sort_ext(scene->dev, wb, b,
+                                                      params->sort_rays ? 0u : ctx->tuning.sort_min_rays, s));
+                ctx->launches += 2;  // histogram, scan, scatter
+            }
             MRT_LAUNCH(1, int(b), launch_trace_ext(scene->dev, wb, b, tblocks, ctx->d_status, ctx->counters, dyn, s));
             MRT_LAUNCH(3, int(b), launch_shade(scene->dev, tp, bn, wb, W, b, ctx->d_status, s));
         }
         if (nee)
             MRT_LAUNCH(2, int(tp.max_bounces), launch_trace_shadow(scene->dev, wb, tp, tp.max_bounces, tblocks,
-                                                                   ctx->d_status, ctx->counters, dyn, s));
+                                                                   ctx->d_status, ctx->counters, dyn_sh, s));
         MRT_LAUNCH(3, 0, launch_tally(wb, s));
     }
     MRT_LAUNCH(3, 0, launch_finalize(wb, color, tp.samples, params->accumulate, params->frame_index, s));

@@ -1,0 +1,486 @@
+// Batched multi-scene tracing: many scenes of uneven triangle and ray
+// counts in one persistent launch, and a closest-hit Lambertian bounce loop
+// over all of them captured once into a CUDA graph.  The reference renders
+// a single compiled-in scene; this is new.
+//
+// Layout: the scenes' BVH8 nodes, leaf-ordered triangles and materials are
+// concatenated; child_base / tri_base of every node and every triangle id
+// are rebased on the host, so traversal is unchanged except that each ray
+// starts at its scene's root node (trav_init's `root`).
+#include "internal.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+namespace mrt {
+int set_error(mrt_ctx* ctx, int code, const char* msg);
+int persistent_blocks(mrt_ctx* ctx);
+TraceParams make_trace_params(const mrt_trace_params* p);
+}
+
+using namespace mrt;
+
+constexpr uint32_t kMaxBatchScenes = 4096;
+
+struct mrt_batch {
+    uint32_t scenes = 0;
+    DevScene dev{};
+    void* d_nodes = nullptr;
+    void* d_tris = nullptr;
+    void* d_mats = nullptr;
+    uint32_t* d_roots = nullptr;     // first node of each scene
+    uint32_t* d_ray_off = nullptr;   // scenes + 1 ray offsets of the current call
+    std::vector<uint32_t> h_ray_off;
+    // path-trace state (sized for the largest call so far)
+    size_t cap = 0;
+    PathRay* q[2] = {nullptr, nullptr};
+    uint2* hits = nullptr;
+    uint32_t* rng = nullptr;
+    uint32_t* counters = nullptr;
+    TraceParams* d_tp = nullptr;     // parameters read by the graph's kernels
+    uint32_t* d_frame = nullptr;
+    TraceParams* h_tp = nullptr;     // pinned staging for the per-call copy
+    uint32_t* h_frame = nullptr;
+    // captured bounce loop and what it was captured for
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cap_stream = nullptr;
+    const void* g_rays = nullptr;
+    float* g_radiance = nullptr;
+    uint32_t g_n = 0, g_bounces = 0, g_blocks = 0, g_dyn = 0;
+};
+
+namespace {
+
+// scene of ray i: the last s with off[s] <= i (off in shared memory)
+MRT_DEV uint32_t scene_of(const uint32_t* off, uint32_t scenes, uint32_t i) {
+    uint32_t lo = 0, hi = scenes;  // invariant: off[lo] <= i < off[hi]
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (off[mid] <= i) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ uint32_t refill(uint32_t* fetch, uint32_t n, bool need, bool& exhausted) {
+    if (exhausted) return kMiss;
+    const uint32_t mask = __ballot_sync(0xFFFFFFFFu, need);
+    if (!mask) return kMiss;
+    const uint32_t lane = lane_id(), leader = __ffs(mask) - 1u, cnt = __popc(mask);
+    uint32_t base = 0u;
+    if (lane == leader) base = atomicAdd(fetch, cnt);
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    if (base + cnt >= n) exhausted = true;
+    if (!need) return kMiss;
+    const uint32_t i = base + __popc(mask & ((1u << lane) - 1u));
+    return i < n ? i : kMiss;
+}
+
+// One persistent launch over the rays of all scenes (per-lane refill).
+template <bool kAnyHit>
+__global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
+k_batch_trace(DevScene sc, const uint32_t* roots, const uint32_t* ray_off, uint32_t scenes, const mrt_ray* rays,
+              uint32_t n, mrt_hit* hits, uint32_t* fetch, uint32_t* status) {
+    __shared__ uint2 stk[kStackDepth * kTraceBlock];
+    extern __shared__ uint32_t off[];  // scenes + 1 ray offsets
+    for (uint32_t i = threadIdx.x; i <= scenes; i += blockDim.x) off[i] = ray_off[i];
+    __syncthreads();
+    uint2* my = stk + threadIdx.x;
+    uint32_t st = 0u, cn = 0u, ct = 0u, ri = 0u;
+    Trav s;
+    bool have = false, exhausted = false;
+    while (true) {
+        const uint32_t idx = refill(fetch, n, !have, exhausted);
+        if (idx != kMiss) {
+            const float4* rp = reinterpret_cast<const float4*>(rays + idx);
+            const float4 a = rp[0], b = rp[1];
+            const uint32_t scn = scene_of(off, scenes, idx);
+            trav_init(s, f3{a.x, a.y, a.z}, f3{b.x, b.y, b.z}, a.w, b.w, roots[scn]);
+            ri = idx;
+            have = true;
+        }
+        if (!__any_sync(0xFFFFFFFFu, have)) break;
+        if (have && trav_step<kAnyHit, false, kStackDepth>(sc, s, my, kTraceBlock, st, cn, ct)) {
+            hits[ri].prim = s.best;
+            hits[ri].t = s.best == kMiss ? s.tmax : s.tbest;
+            have = false;
+        }
+    }
+    if (st) atomicOr(status, st);
+}
+
+// Bounce loop state: queue entry = origin | ray index, direction | scene,
+// throughput | tmax.
+__global__ void __launch_bounds__(kShadeBlock)
+k_batch_init(const mrt_ray* rays, const uint32_t* ray_off, uint32_t scenes, uint32_t n, PathRay* q0, uint32_t* rng,
+             float* radiance, uint32_t* counters, const uint32_t* frame) {
+    extern __shared__ uint32_t off[];  // scenes + 1 ray offsets
+    for (uint32_t i = threadIdx.x; i <= scenes; i += blockDim.x) off[i] = ray_off[i];
+    __syncthreads();
+    const uint32_t f = *frame;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4* rp = reinterpret_cast<const float4*>(rays + i);
+        const float4 a = rp[0], b = rp[1];
+        PathRay pr;
+        pr.o_pix = make_float4(a.x, a.y, a.z, __uint_as_float(i));
+        pr.d = make_float4(b.x, b.y, b.z, __uint_as_float(scene_of(off, scenes, i)));
+        pr.beta = make_float4(1.0f, 1.0f, 1.0f, b.w);
+        q0[i] = pr;
+        uint32_t h = i * 0x9E3779B1u + ((f << 1u) | 1u);
+        rng[i] = pcg(h) | 1u;
+        radiance[3 * size_t(i) + 0] = 0.0f;
+        radiance[3 * size_t(i) + 1] = 0.0f;
+        radiance[3 * size_t(i) + 2] = 0.0f;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) counters[kCntExt] = n;
+}
+
+__global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
+k_batch_trace_queue(DevScene sc, const uint32_t* roots, const PathRay* q, uint2* hits, uint32_t* counters,
+                    uint32_t bounce, uint32_t* status) {
+    __shared__ uint2 stk[kStackDepth * kTraceBlock];
+    const uint32_t n = counters[kCntExt + bounce];
+    uint32_t* fetch = counters + kCntFetchExt + bounce;
+    uint2* my = stk + threadIdx.x;
+    uint32_t st = 0u, cn = 0u, ct = 0u, ri = 0u;
+    Trav s;
+    bool have = false, exhausted = false;
+    while (true) {
+        const uint32_t idx = refill(fetch, n, !have, exhausted);
+        if (idx != kMiss) {
+            const PathRay pr = q[idx];
+            const float tmax = bounce == 0u ? pr.beta.w : INFINITY;
+            trav_init(s, f3{pr.o_pix.x, pr.o_pix.y, pr.o_pix.z}, f3{pr.d.x, pr.d.y, pr.d.z}, 0.0f, tmax,
+                      roots[__float_as_uint(pr.d.w)]);
+            ri = idx;
+            have = true;
+        }
+        if (!__any_sync(0xFFFFFFFFu, have)) break;
+        if (have && trav_step<false, false, kStackDepth>(sc, s, my, kTraceBlock, st, cn, ct)) {
+            hits[ri] = make_uint2(s.best, __float_as_uint(s.best == kMiss ? s.tmax : s.tbest));
+            have = false;
+        }
+    }
+    if (st) atomicOr(status, st);
+}
+
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want) {
+    const uint32_t mask = __ballot_sync(0xFFFFFFFFu, want);
+    if (!mask) return 0u;
+    const uint32_t lane = lane_id(), leader = __ffs(mask) - 1u;
+    uint32_t base = 0u;
+    if (lane == leader) base = atomicAdd(counter, uint32_t(__popc(mask)));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+// Shade vertex `bounce`: escape adds throughput x sky; a hit multiplies the
+// albedo and, below the bounce limit, appends a cosine-weighted bounce ray
+// (normalize(n + uniform sphere point), random.glsl:10-19 with per-ray PCG
+// numbers) with Russian roulette past rr_start.
+__global__ void __launch_bounds__(kShadeBlock)
+k_batch_shade(DevScene sc, const TraceParams* tpp, const PathRay* qin, PathRay* qout, const uint2* hits,
+              uint32_t* rng, float* radiance, uint32_t* counters, uint32_t bounce, uint32_t* status) {
+    const TraceParams tp = *tpp;
+    const uint32_t n = counters[kCntExt + bounce];
+    const uint32_t rounded = (n + 31u) & ~31u;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < rounded; i += gridDim.x * blockDim.x) {
+        bool want = false;
+        PathRay out;
+        if (i < n) {
+            const PathRay pr = qin[i];
+            const uint2 h = hits[i];
+            const uint32_t idx = __float_as_uint(pr.o_pix.w);
+            f3 beta{pr.beta.x, pr.beta.y, pr.beta.z};
+            if (h.x == kMiss) {
+                float* r = radiance + 3 * size_t(idx);
+                r[0] = __fmul_rn(beta.x, tp.sky[0]);
+                r[1] = __fmul_rn(beta.y, tp.sky[1]);
+                r[2] = __fmul_rn(beta.z, tp.sky[2]);
+            } else if (h.x < sc.mat_count) {
+                const mrt_material m = sc.mats[h.x];
+                const f3 d{pr.d.x, pr.d.y, pr.d.z};
+                f3 nrm{m.normal[0], m.normal[1], m.normal[2]};
+                if (dot_rn(nrm, d) > 0.0f) nrm = f3{-nrm.x, -nrm.y, -nrm.z};
+                const f3 rho{__fdiv_rn(float(m.albedo_rgba8 & 0xFFu), 255.0f),
+                             __fdiv_rn(float((m.albedo_rgba8 >> 8) & 0xFFu), 255.0f),
+                             __fdiv_rn(float((m.albedo_rgba8 >> 16) & 0xFFu), 255.0f)};
+                beta = mul_rn(beta, rho);
+                if (bounce < tp.max_bounces) {
+                    uint32_t s = rng[idx];
+                    const float u1 = random_float(s), u2 = random_float(s);
+                    const f3 sp = random_sphere_point(__fsub_rn(__fmul_rn(u1, 2.0f), 1.0f),
+                                                      __fsub_rn(__fmul_rn(u2, 2.0f), 1.0f));
+                    f3 nd = add_rn(nrm, sp);
+                    if (dot_rn(nd, nd) == 0.0f) nd = nrm;
+                    nd = normalize_rn(nd);
+                    bool live = true;
+                    if (tp.rr_start != 0u && bounce + 1u > tp.rr_start) {
+                        float qv = fminf(fmaxf(fmaxf(fmaxf(beta.x, beta.y), beta.z), 0.05f), 1.0f);
+                        if (random_float(s) >= qv) live = false;
+                        else beta = f3{__fdiv_rn(beta.x, qv), __fdiv_rn(beta.y, qv), __fdiv_rn(beta.z, qv)};
+                    }
+                    rng[idx] = s;
+                    if (live) {
+                        const f3 p = add_rn(f3{pr.o_pix.x, pr.o_pix.y, pr.o_pix.z}, scale_rn(d, __uint_as_float(h.y)));
+                        const f3 o = offset_ray(p, nrm);
+                        want = true;
+                        out.o_pix = make_float4(o.x, o.y, o.z, pr.o_pix.w);
+                        out.d = make_float4(nd.x, nd.y, nd.z, pr.d.w);
+                        out.beta = make_float4(beta.x, beta.y, beta.z, INFINITY);
+                    }
+                }
+            } else {
+                atomicOr(status, MRT_STATUS_BAD_TRI);
+            }
+        }
+        const uint32_t slot = warp_append(counters + kCntExt + bounce + 1u, want);
+        if (want) qout[slot] = out;
+    }
+}
+
+// ray counts of the bounce loop into the context's totals (frame stats)
+__global__ void k_batch_tally(const uint32_t* counters, unsigned long long* totals, uint32_t bounces) {
+    const uint32_t v = threadIdx.x;
+    if (v >= 1u && v <= bounces) atomicAdd(totals + kCntExt + v, (unsigned long long)counters[kCntExt + v]);
+}
+
+int free_batch_state(mrt_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+    cudaFree(b->q[0]); cudaFree(b->q[1]); cudaFree(b->hits); cudaFree(b->rng); cudaFree(b->counters);
+    b->exec = nullptr;
+    b->cap_stream = nullptr;
+    b->q[0] = b->q[1] = nullptr;
+    b->hits = nullptr;
+    b->rng = nullptr;
+    b->counters = nullptr;
+    b->cap = 0;
+    return MRT_OK;
+}
+
+int upload_offsets(mrt_ctx* ctx, mrt_batch* b, const uint32_t* ray_offsets, uint32_t& n, cudaStream_t s) {
+    for (uint32_t i = 0; i < b->scenes; ++i)
+        if (ray_offsets[i + 1] < ray_offsets[i]) return set_error(ctx, MRT_EINVAL, "ray_offsets must not decrease");
+    if (ray_offsets[0] != 0) return set_error(ctx, MRT_EINVAL, "ray_offsets[0] must be 0");
+    n = ray_offsets[b->scenes];
+    bool same = b->h_ray_off.size() == b->scenes + 1u &&
+                std::memcmp(b->h_ray_off.data(), ray_offsets, (b->scenes + 1u) * sizeof(uint32_t)) == 0;
+    if (!same) {
+        b->h_ray_off.assign(ray_offsets, ray_offsets + b->scenes + 1u);
+        // a pageable H2D copy returns once the source is consumed
+        if (cudaMemcpyAsync(b->d_ray_off, b->h_ray_off.data(), (b->scenes + 1u) * sizeof(uint32_t),
+                            cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return set_error(ctx, MRT_ECUDA, "ray offset upload failed");
+    }
+    return MRT_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int mrt_cuda_batch_create(mrt_ctx* ctx, uint32_t count, const mrt_bvh8_node* const* nodes,
+                          const uint32_t* node_counts, const mrt_tri* const* tris, const uint32_t* tri_counts,
+                          const mrt_material* const* materials, mrt_batch** out) {
+    if (!ctx || !out || !nodes || !node_counts || !tris || !tri_counts || !materials || count == 0)
+        return set_error(ctx, MRT_EINVAL, "batch_create: null argument or no scenes");
+    if (count > kMaxBatchScenes) return set_error(ctx, MRT_ERANGE, "batch_create: more than 4096 scenes");
+    *out = nullptr;
+    uint64_t nn = 0, nt = 0;
+    for (uint32_t s = 0; s < count; ++s) {
+        if (!nodes[s] || !tris[s] || !materials[s] || node_counts[s] == 0 || tri_counts[s] == 0)
+            return set_error(ctx, MRT_EINVAL, "batch_create: empty scene");
+        nn += node_counts[s];
+        nt += tri_counts[s];
+    }
+    if (nn >= 0xFFFFFFFFull || nt >= 0xFFFFFFFFull) return set_error(ctx, MRT_ERANGE, "batch_create: too large");
+    std::vector<mrt_bvh8_node> an;
+    std::vector<mrt_tri> at;
+    std::vector<mrt_material> am;
+    std::vector<uint32_t> roots(count);
+    an.reserve(nn);
+    at.reserve(nt);
+    am.reserve(nt);
+    for (uint32_t s = 0; s < count; ++s) {
+        const uint32_t nb = uint32_t(an.size()), tb = uint32_t(at.size());
+        roots[s] = nb;
+        for (uint32_t i = 0; i < node_counts[s]; ++i) {
+            mrt_bvh8_node n = nodes[s][i];
+            n.child_base += nb;
+            n.tri_base += tb;
+            an.push_back(n);
+        }
+        for (uint32_t i = 0; i < tri_counts[s]; ++i) {
+            mrt_tri t = tris[s][i];
+            t.id += tb;
+            at.push_back(t);
+        }
+        // materials are indexed by the scene's original triangle id
+        am.insert(am.end(), materials[s], materials[s] + tri_counts[s]);
+    }
+    mrt_batch* b = new (std::nothrow) mrt_batch;
+    if (!b) return MRT_ENOMEM;
+    b->scenes = count;
+    bool ok = cudaMalloc(&b->d_nodes, an.size() * sizeof(mrt_bvh8_node)) == cudaSuccess &&
+              cudaMalloc(&b->d_tris, at.size() * sizeof(mrt_tri)) == cudaSuccess &&
+              cudaMalloc(&b->d_mats, am.size() * sizeof(mrt_material)) == cudaSuccess &&
+              cudaMalloc(&b->d_roots, count * sizeof(uint32_t)) == cudaSuccess &&
+              cudaMalloc(&b->d_ray_off, (count + 1) * sizeof(uint32_t)) == cudaSuccess &&
+              cudaMalloc(&b->d_tp, sizeof(TraceParams)) == cudaSuccess &&
+              cudaMalloc(&b->d_frame, sizeof(uint32_t)) == cudaSuccess &&
+              cudaMallocHost(&b->h_tp, sizeof(TraceParams)) == cudaSuccess &&
+              cudaMallocHost(&b->h_frame, sizeof(uint32_t)) == cudaSuccess;
+    ok = ok && cudaMemcpy(b->d_nodes, an.data(), an.size() * sizeof(mrt_bvh8_node), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(b->d_tris, at.data(), at.size() * sizeof(mrt_tri), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(b->d_mats, am.data(), am.size() * sizeof(mrt_material), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(b->d_roots, roots.data(), count * sizeof(uint32_t), cudaMemcpyHostToDevice) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        mrt_cuda_batch_destroy(ctx, b);
+        return set_error(ctx, MRT_ENOMEM, "batch_create: device allocation or copy failed");
+    }
+    b->dev.nodes = static_cast<const uint4*>(b->d_nodes);
+    b->dev.tris = static_cast<const float4*>(b->d_tris);
+    b->dev.mats = static_cast<const mrt_material*>(b->d_mats);
+    b->dev.node_count = uint32_t(an.size());
+    b->dev.tri_count = uint32_t(at.size());
+    b->dev.mat_count = uint32_t(am.size());
+    *out = b;
+    return MRT_OK;
+}
+
+int mrt_cuda_batch_destroy(mrt_ctx* ctx, mrt_batch* b) {
+    if (!ctx || !b) return MRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    free_batch_state(b);
+    cudaFree(b->d_nodes); cudaFree(b->d_tris); cudaFree(b->d_mats); cudaFree(b->d_roots); cudaFree(b->d_ray_off);
+    cudaFree(b->d_tp); cudaFree(b->d_frame);
+    if (b->h_tp) cudaFreeHost(b->h_tp);
+    if (b->h_frame) cudaFreeHost(b->h_frame);
+    delete b;
+    return MRT_OK;
+}
+
+int mrt_cuda_batch_trace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, const uint32_t* ray_offsets, mrt_hit* hits,
+                         uint32_t flags, void* stream) {
+    if (!ctx || !b || !ray_offsets) return set_error(ctx, MRT_EINVAL, "batch_trace: null argument");
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    uint32_t n = 0;
+    int rc = upload_offsets(ctx, b, ray_offsets, n, s);
+    if (rc) return rc;
+    if (n == 0) return MRT_OK;
+    if (!rays || !hits) return set_error(ctx, MRT_EINVAL, "batch_trace: null rays or hits");
+    // the context's primary-ray work counter doubles as this launch's counter
+    if (cudaMemsetAsync(ctx->d_prim_fetch, 0, sizeof(uint32_t), s) != cudaSuccess)
+        return set_error(ctx, MRT_ECUDA, "batch_trace: memset failed");
+    const int blocks = persistent_blocks(ctx);
+    const size_t dsm = (b->scenes + 1u) * sizeof(uint32_t);
+    if (flags & MRT_TRACE_ANY_HIT)
+        k_batch_trace<true><<<blocks, kTraceBlock, dsm, s>>>(b->dev, b->d_roots, b->d_ray_off, b->scenes, rays, n,
+                                                             hits, ctx->d_prim_fetch, ctx->d_status);
+    else
+        k_batch_trace<false><<<blocks, kTraceBlock, dsm, s>>>(b->dev, b->d_roots, b->d_ray_off, b->scenes, rays, n,
+                                                              hits, ctx->d_prim_fetch, ctx->d_status);
+    if (cudaGetLastError() != cudaSuccess) return set_error(ctx, MRT_ECUDA, "batch_trace: launch failed");
+    ctx->launches++;
+    return MRT_OK;
+}
+
+int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, const uint32_t* ray_offsets,
+                             const mrt_trace_params* params, uint32_t frame, float* radiance, int use_graph,
+                             void* stream) {
+    if (!ctx || !b || !ray_offsets || !params) return set_error(ctx, MRT_EINVAL, "batch_pathtrace: null argument");
+    if (params->max_bounces > MRT_MAX_BOUNCES) return set_error(ctx, MRT_ERANGE, "batch_pathtrace: max_bounces > 16");
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    uint32_t n = 0;
+    int rc = upload_offsets(ctx, b, ray_offsets, n, s);
+    if (rc) return rc;
+    if (n == 0) return MRT_OK;
+    if (!rays || !radiance) return set_error(ctx, MRT_EINVAL, "batch_pathtrace: null rays or radiance");
+    if (b->cap < n) {
+        free_batch_state(b);
+        bool ok = cudaMalloc(&b->q[0], n * sizeof(PathRay)) == cudaSuccess &&
+                  cudaMalloc(&b->q[1], n * sizeof(PathRay)) == cudaSuccess &&
+                  cudaMalloc(&b->hits, n * sizeof(uint2)) == cudaSuccess &&
+                  cudaMalloc(&b->rng, n * sizeof(uint32_t)) == cudaSuccess &&
+                  cudaMalloc(&b->counters, kCntSlots * sizeof(uint32_t)) == cudaSuccess;
+        if (!ok) {
+            cudaGetLastError();
+            free_batch_state(b);
+            return set_error(ctx, MRT_ENOMEM, "batch_pathtrace: out of device memory for the path queues");
+        }
+        b->cap = n;
+    }
+    // per-call parameters go through device memory so a captured graph
+    // replays with new values
+    *b->h_tp = make_trace_params(params);
+    *b->h_frame = frame;
+    if (cudaMemcpyAsync(b->d_tp, b->h_tp, sizeof(TraceParams), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(b->d_frame, b->h_frame, sizeof(uint32_t), cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return set_error(ctx, MRT_ECUDA, "batch_pathtrace: parameter upload failed");
+
+    const int blocks = persistent_blocks(ctx);
+    const uint32_t bounces = params->max_bounces;
+    const int sblocks = int(std::min<size_t>((n + kShadeBlock - 1) / kShadeBlock, 8192));
+    auto enqueue = [&](cudaStream_t st) -> bool {
+        if (cudaMemsetAsync(b->counters, 0, kCntSlots * sizeof(uint32_t), st) != cudaSuccess) return false;
+        k_batch_init<<<sblocks, kShadeBlock, (b->scenes + 1u) * sizeof(uint32_t), st>>>(
+            rays, b->d_ray_off, b->scenes, n, b->q[0], b->rng, radiance, b->counters, b->d_frame);
+        for (uint32_t v = 0; v <= bounces; ++v) {
+            k_batch_trace_queue<<<blocks, kTraceBlock, 0, st>>>(b->dev, b->d_roots, b->q[v & 1u], b->hits,
+                                                                b->counters, v, ctx->d_status);
+            k_batch_shade<<<sblocks, kShadeBlock, 0, st>>>(b->dev, b->d_tp, b->q[v & 1u], b->q[(v + 1u) & 1u],
+                                                           b->hits, b->rng, radiance, b->counters, v,
+                                                           ctx->d_status);
+        }
+        k_batch_tally<<<1, 32, 0, st>>>(b->counters, ctx->d_totals, bounces);
+        return cudaGetLastError() == cudaSuccess;
+    };
+    ctx->acc.primary_rays += n;
+    if (!use_graph) {
+        if (!enqueue(s)) return set_error(ctx, MRT_ECUDA, "batch_pathtrace: launch failed");
+        ctx->launches += 2 + 2 * (bounces + 1);
+        return MRT_OK;
+    }
+    const bool same = b->exec && b->g_rays == rays && b->g_radiance == radiance && b->g_n == n &&
+                      b->g_bounces == bounces && b->g_blocks == uint32_t(blocks);
+    if (!same) {
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+        if (!b->cap_stream && cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) != cudaSuccess)
+            return set_error(ctx, MRT_ECUDA, "batch_pathtrace: capture stream");
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+            return set_error(ctx, MRT_ECUDA, "batch_pathtrace: begin capture failed");
+        const bool ok = enqueue(b->cap_stream);
+        cudaError_t e = cudaStreamEndCapture(b->cap_stream, &g);
+        if (!ok || e != cudaSuccess || !g) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            return set_error(ctx, MRT_ECUDA, "batch_pathtrace: graph capture failed");
+        }
+        e = cudaGraphInstantiate(&b->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            b->exec = nullptr;
+            return set_error(ctx, MRT_ECUDA, "batch_pathtrace: graph instantiation failed");
+        }
+        b->g_rays = rays;
+        b->g_radiance = radiance;
+        b->g_n = n;
+        b->g_bounces = bounces;
+        b->g_blocks = uint32_t(blocks);
+    }
+    if (cudaGraphLaunch(b->exec, s) != cudaSuccess) return set_error(ctx, MRT_ECUDA, "batch_pathtrace: graph launch");
+    ctx->launches += 2 + 2 * (bounces + 1);
+    return MRT_OK;
+}
+
+} // extern "C"

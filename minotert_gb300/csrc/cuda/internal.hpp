@@ -26,6 +26,7 @@ constexpr int kTraceBlock = 128;   // threads per traversal block
 constexpr int kStackDepth = MRT_TRACE_STACK;
 constexpr int kTraceMinBlocks = MRT_TRACE_MIN_BLOCKS;
 constexpr int kShadeBlock = 256;
+constexpr uint32_t kSortNever = 0xFFFFFFFFu;  // mrt_tuning.sort_min_rays: never sort
 
 // Wavefront records
 struct PathRay {     // 48 bytes
@@ -44,7 +45,8 @@ enum : uint32_t {
     kCntShadow = kCntExt + 17,         // [b]: shadow rays emitted at vertex b
     kCntFetchExt = kCntShadow + 17,    // [b]: work fetch of extension trace b
     kCntFetchShadow = kCntFetchExt + 17,
-    kCntSlots = kCntFetchShadow + 17,
+    kCntSorted = kCntFetchShadow + 17,  // [b]: 1 when the queue of bounce b was sorted into qsort
+    kCntSlots = kCntSorted + 17,
 };
 
 // Accumulated totals (uint64 slots): ray counts copied from the counters
@@ -74,6 +76,12 @@ struct WaveBuffers {
     PathRay* qsort = nullptr;
     uint32_t* hist = nullptr;
 };
+
+// The extension queue of bounce b as the trace and shade kernels read it.
+__device__ __forceinline__ const PathRay* ext_queue(const WaveBuffers& wb, uint32_t bounce) {
+    if (wb.counters[kCntSorted + bounce]) return wb.qsort;
+    return (bounce & 1u) ? wb.q[1] : wb.q[0];
+}
 
 struct FrameParams {
     mrt_camera_consts c;
@@ -120,7 +128,8 @@ cudaError_t launch_trace_shadow(const DevScene& sc, const WaveBuffers& wb, const
 cudaError_t launch_shade(const DevScene& sc, const TraceParams& tp, BlueNoise bn, const WaveBuffers& wb,
                          uint32_t width, uint32_t bounce, uint32_t* status, cudaStream_t s);
 cudaError_t launch_tally(const WaveBuffers& wb, cudaStream_t s);
-cudaError_t launch_sort_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t bounce, cudaStream_t s);
+cudaError_t launch_sort_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t bounce, uint32_t min_rays,
+                            cudaStream_t s);
 cudaError_t launch_finalize(const WaveBuffers& wb, float* color, uint32_t samples, uint32_t accumulate,
                             uint32_t frame_index, cudaStream_t s);
 
@@ -160,7 +169,7 @@ struct mrt_ctx {
     // timing
     bool timing = false;
     bool counters = false;
-    mrt_tuning tuning{0u, 1u, 0u, 1u << 20};  // autotuned on GB300 (icosphere field, 1080p)
+    mrt_tuning tuning{0u, 1u, 0u, mrt::kSortNever};  // autotuned on GB300 (icosphere field, 1080p)
     uint32_t* d_prim_fetch = nullptr;  // work counter of the persistent primary kernel
     int occ_blocks = 0;                // traversal blocks per SM at full occupancy
     unsigned long long* d_totals = nullptr;  // kTotSlots accumulated totals

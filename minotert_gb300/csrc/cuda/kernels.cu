@@ -428,7 +428,7 @@ __global__ void __launch_bounds__(kShadeBlock)
 k_shade(DevScene sc, TraceParams tp, BlueNoise bn, WaveBuffers wb, uint32_t width, uint32_t vertex,
         uint32_t* status) {
     const uint32_t n = wb.counters[kCntExt + vertex];
-    const PathRay* q = (vertex & 1u) ? wb.q[1] : wb.q[0];
+    const PathRay* q = ext_queue(wb, vertex);
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t rounded = (n + 31u) & ~31u;
     const f3 sky{tp.sky[0], tp.sky[1], tp.sky[2]};
@@ -482,7 +482,7 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
 k_trace_ext(DevScene sc, WaveBuffers wb, uint32_t bounce, uint32_t* status) {
     __shared__ uint2 stk[kStackDepth * kTraceBlock];
     const uint32_t n = wb.counters[kCntExt + bounce];
-    const PathRay* q = (bounce & 1u) ? wb.q[1] : wb.q[0];
+    const PathRay* q = ext_queue(wb, bounce);
     uint32_t* fetch = wb.counters + kCntFetchExt + bounce;
     uint2* my = stk + threadIdx.x;
     uint32_t st = 0u, cn = 0u, ct = 0u;
@@ -744,7 +744,90 @@ cudaError_t launch_shade(const DevScene& sc, const TraceParams& tp, BlueNoise bn
     return cudaGetLastError();
 }
 
-cudaError_t launch_sort_ext(const DevScene&, const WaveBuffers&, uint32_t, cudaStream_t) { return cudaSuccess; }
+// ---- ray sorting between bounces: one counting-sort pass on a 12-bit key,
+// direction octant (3 bits) above a 9-bit Morton code of the origin in the
+// scene box (3 bits per axis), so rays sharing a direction octant and a
+// region of space trace side by side.  Order inside a bin is arbitrary;
+// results do not depend on it (each pixel owns one path).
+constexpr uint32_t kSortBins = 4096;
+
+MRT_DEV uint32_t sort_key(const DevScene& sc, const PathRay& r) {
+    uint32_t key = (r.d.x < 0.0f ? 1u : 0u) | (r.d.y < 0.0f ? 2u : 0u) | (r.d.z < 0.0f ? 4u : 0u);
+    const float o[3] = {r.o_pix.x, r.o_pix.y, r.o_pix.z};
+    uint32_t q[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float u = (o[a] - sc.lo[a]) * sc.inv_ext[a];
+        q[a] = uint32_t(fminf(fmaxf(u * 8.0f, 0.0f), 7.0f));
+    }
+    uint32_t m = 0u;
+#pragma unroll
+    for (int b = 2; b >= 0; --b) m = (m << 3) | (((q[0] >> b) & 1u) << 2) | (((q[1] >> b) & 1u) << 1) | ((q[2] >> b) & 1u);
+    return (key << 9) | m;
+}
+
+__global__ void __launch_bounds__(kShadeBlock) k_sort_hist(DevScene sc, WaveBuffers wb, uint32_t bounce,
+                                                           uint32_t min_rays) {
+    __shared__ uint32_t h[kSortBins];
+    const uint32_t n = wb.counters[kCntExt + bounce];
+    if (n < min_rays) return;  // short queues are traced unsorted
+    for (uint32_t i = threadIdx.x; i < kSortBins; i += blockDim.x) h[i] = 0u;
+    __syncthreads();
+    const PathRay* q = (bounce & 1u) ? wb.q[1] : wb.q[0];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = sort_key(sc, q[i]);
+        wb.keys[i] = k;
+        atomicAdd(&h[k], 1u);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < kSortBins; i += blockDim.x)
+        if (h[i]) atomicAdd(&wb.hist[i], h[i]);
+}
+
+// exclusive scan of the 4096 bin counts, one block of 1024 threads
+__global__ void __launch_bounds__(1024) k_sort_scan(WaveBuffers wb) {
+    __shared__ uint32_t part[1024];
+    const uint32_t t = threadIdx.x;
+    uint32_t v[4], s = 0u;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { v[k] = wb.hist[4 * t + k]; s += v[k]; }
+    part[t] = s;
+    __syncthreads();
+    for (uint32_t off = 1; off < 1024; off <<= 1) {
+        const uint32_t add = t >= off ? part[t - off] : 0u;
+        __syncthreads();
+        part[t] += add;
+        __syncthreads();
+    }
+    uint32_t run = part[t] - s;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { wb.hist[4 * t + k] = run; run += v[k]; }
+}
+
+__global__ void __launch_bounds__(kShadeBlock) k_sort_scatter(WaveBuffers wb, uint32_t bounce, uint32_t min_rays) {
+    const uint32_t n = wb.counters[kCntExt + bounce];
+    if (n < min_rays) return;
+    const PathRay* q = (bounce & 1u) ? wb.q[1] : wb.q[0];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t pos = atomicAdd(&wb.hist[wb.keys[i]], 1u);
+        wb.qsort[pos] = q[i];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) wb.counters[kCntSorted + bounce] = 1u;
+}
+
+// Sorts the extension queue of `bounce` into wb.qsort when it holds at
+// least `min_rays` rays and flags it, so the trace and shade kernels of
+// that bounce read the sorted copy (ext_queue).  No host synchronisation.
+cudaError_t launch_sort_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t bounce, uint32_t min_rays,
+                            cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(wb.hist, 0, kSortBins * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    const int blocks = shade_blocks(uint32_t(wb.cap));
+    k_sort_hist<<<blocks, kShadeBlock, 0, s>>>(sc, wb, bounce, min_rays);
+    k_sort_scan<<<1, 1024, 0, s>>>(wb);
+    k_sort_scatter<<<blocks, kShadeBlock, 0, s>>>(wb, bounce, min_rays);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_finalize(const WaveBuffers& wb, float* color, uint32_t samples, uint32_t accumulate,
                             uint32_t frame_index, cudaStream_t s) {

@@ -27,6 +27,8 @@ struct DevScene {
     uint32_t tri_count;
     uint32_t mat_count;
     uint32_t sphere_count;
+    float lo[3];        // scene bounds (ray-sort keys)
+    float inv_ext[3];   // 1 / extent per axis
 };
 
 constexpr float kRobustScale = 1.0f + 1.0f / 1048576.0f; // 1 + 2^-20
@@ -124,13 +126,15 @@ struct Trav {
     uint32_t iters;
 };
 
-MRT_DEV void trav_init(Trav& s, f3 o, f3 d, float tmin, float tmax) {
+// `root` is the index of the BVH8 root node: 0 for a single scene, the
+// scene's first node in a concatenated multi-scene BVH.
+MRT_DEV void trav_init(Trav& s, f3 o, f3 d, float tmin, float tmax, uint32_t root = 0u) {
     s.r = ray_pre(o, d);
     s.tmin = tmin;
     s.tmax = tmax;
     s.tbest = tmax;
     s.best = kMiss;
-    s.g_base = 0u;
+    s.g_base = root;
     s.g_hits = 1u << s.r.oct; // the root is child slot 0 of a virtual group
     s.g_imask = 1u;
     s.sp = 0;

@@ -101,6 +101,88 @@ def blue_noise(seed: int = 1, size: int = 64) -> np.ndarray:
     return out
 
 
+class DeviceBatch:
+    """Many scenes concatenated into one device BVH (mrt_batch): rays of all
+    scenes trace in one persistent launch.  Hit ids are batch-wide:
+    scene s's local id = prim - tri_offsets[s]."""
+
+    def __init__(self, ctx: Context, scenes):
+        """scenes: list of (Mesh, Bvh8)."""
+        self.ctx = ctx
+        self.meshes = [m for m, _ in scenes]
+        self.bvhs = [b for _, b in scenes]
+        n = len(scenes)
+        self._keep = [np.ascontiguousarray(b.nodes) for b in self.bvhs] + [np.ascontiguousarray(b.tris)
+                                                                           for b in self.bvhs]
+        self._keep += [np.ascontiguousarray(m.mats) for m in self.meshes]
+        node_ptrs = (C.c_void_p * n)(*[b.nodes.ctypes.data for b in self.bvhs])
+        tri_ptrs = (C.c_void_p * n)(*[b.tris.ctypes.data for b in self.bvhs])
+        mat_ptrs = (C.c_void_p * n)(*[m.mats.ctypes.data for m in self.meshes])
+        node_counts = np.array([len(b.nodes) for b in self.bvhs], np.uint32)
+        tri_counts = np.array([len(b.tris) for b in self.bvhs], np.uint32)
+        self.tri_offsets = np.concatenate([[0], np.cumsum(tri_counts)]).astype(np.uint64)
+        h = C.c_void_p()
+        ctx.check(lib().mrt_cuda_batch_create(ctx.handle, n, node_ptrs, ptr(node_counts), tri_ptrs, ptr(tri_counts),
+                                              mat_ptrs, C.byref(h)), "batch_create")
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def trace(self, rays, ray_offsets: np.ndarray, hits, any_hit: bool = False, stream=None):
+        off = np.ascontiguousarray(ray_offsets, np.uint32)
+        self.ctx.check(lib().mrt_cuda_batch_trace(self.ctx.handle, self._h, ptr(rays), ptr(off), ptr(hits),
+                                                  int(any_hit), ptr(stream)), "batch_trace")
+
+    def pathtrace(self, rays, ray_offsets: np.ndarray, params, frame: int, radiance, use_graph: bool = True,
+                  stream=None):
+        off = np.ascontiguousarray(ray_offsets, np.uint32)
+        self.ctx.check(lib().mrt_cuda_batch_pathtrace(self.ctx.handle, self._h, ptr(rays), ptr(off),
+                                                      C.byref(params), frame, ptr(radiance), int(use_graph),
+                                                      ptr(stream)), "batch_pathtrace")
+
+    def close(self):
+        if self._h and self.ctx.handle:
+            lib().mrt_cuda_batch_destroy(self.ctx.handle, self._h)
+        self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def pinhole_rays(lo, hi, width: int, height: int, seed: int = 0, fov_deg: float = 50.0) -> np.ndarray:
+    """width x height camera rays looking at the centre of the box [lo, hi]
+    from a seeded direction above it (RAY_DTYPE, tmin 0, tmax inf)."""
+    from ._lib import RAY_DTYPE
+    lo, hi = np.asarray(lo, np.float64), np.asarray(hi, np.float64)
+    c = 0.5 * (lo + hi)
+    r = 0.5 * np.linalg.norm(hi - lo) + 1e-3
+    rng = np.random.default_rng(seed)
+    az, el = rng.uniform(0, 2 * np.pi), np.radians(rng.uniform(20, 60))
+    eye = c + 1.6 * r / np.tan(np.radians(fov_deg) / 2) * 0.6 * np.array(
+        [np.cos(el) * np.cos(az), np.cos(el) * np.sin(az), np.sin(el)])
+    fwd = c - eye
+    fwd /= np.linalg.norm(fwd)
+    right = np.cross(fwd, [0.0, 0.0, 1.0])
+    right /= np.linalg.norm(right)
+    up = np.cross(right, fwd)
+    th = np.tan(np.radians(fov_deg) / 2)
+    xs = ((np.arange(width) + 0.5) / width * 2 - 1) * th * width / height
+    ys = (1 - (np.arange(height) + 0.5) / height * 2) * th
+    d = fwd[None, None, :] + xs[None, :, None] * right[None, None, :] + ys[:, None, None] * up[None, None, :]
+    d /= np.linalg.norm(d, axis=2, keepdims=True)
+    rays = np.zeros(width * height, RAY_DTYPE)
+    rays["org"] = eye.astype(np.float32)
+    rays["dir"] = d.reshape(-1, 3).astype(np.float32)
+    rays["tmin"] = 0.0
+    rays["tmax"] = np.inf
+    return rays
+
+
 class DeviceScene:
     """A scene uploaded to one context (mrt_scene)."""
 

@@ -51,4 +51,53 @@ def icospheres_1080p(seed: int = 1, width: int = 1920, height: int = 1080) -> Wo
                     lambda s: _scene.icospheres(s, 200, 4, 0.2, 5.0, 10240), seed)
 
 
-WORKLOADS = {"heightfield_boxes_256": heightfield_boxes_256, "icospheres_1080p": icospheres_1080p}
+@dataclass
+class BatchScene:
+    kind: str         # "heightfield" or "icospheres"
+    target_tris: int
+    rays: int         # width * height of the scene's camera
+    width: int
+    height: int
+    seed: int
+
+    def mesh(self):
+        from ._lib import lib
+        if self.kind == "heightfield":
+            return _scene.heightfield_boxes(self.seed, lib().mrt_heightfield_grid_for(self.target_tris), 0)
+        if self.target_tris >= 5120:
+            return _scene.icospheres(self.seed, max(1, round(self.target_tris / 5120)), 4, 0.2, 5.0, 0)
+        level = max(0, int(math.floor(math.log(max(self.target_tris, 20) / 20.0, 4))))
+        return _scene.icospheres(self.seed, max(1, round(self.target_tris / (20 * 4 ** level))), level, 0.2, 5.0, 0)
+
+    def rays_for(self, mesh):
+        return _scene.pinhole_rays(mesh.lo, mesh.hi, self.width, self.height, seed=self.seed)
+
+
+@dataclass
+class BatchWorkload:
+    name: str
+    scenes: list
+    settings: TraceSettings
+    sky: Sky
+
+
+def batched64(seed: int = 1, count: int = 64, tri_range=(1_000, 500_000), ray_range=(16_000, 2_000_000),
+              bounces: int = 3) -> BatchWorkload:
+    """`count` independent scenes alternating heightfields and icosphere
+    clusters, triangle counts log-uniform in tri_range, ray counts uniform
+    in ray_range (square pinhole images), closest-hit bounce loop of
+    `bounces` diffuse bounces."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    scenes = []
+    for s in range(count):
+        t = int(round(math.exp(rng.uniform(math.log(tri_range[0]), math.log(tri_range[1])))))
+        r = int(rng.uniform(*ray_range))
+        w = max(1, int(round(math.sqrt(r))))
+        scenes.append(BatchScene("heightfield" if s % 2 == 0 else "icospheres", t, w * w, w, w, seed * 1000 + s))
+    return BatchWorkload(f"batched{count}", scenes, TraceSettings(samples=1, bounces=bounces, rr_start=0),
+                         Sky((0.6, 0.7, 0.9), None))
+
+
+WORKLOADS = {"heightfield_boxes_256": heightfield_boxes_256, "icospheres_1080p": icospheres_1080p,
+             "batched64": batched64}

@@ -42,6 +42,7 @@ def lib() -> C.CDLL:
             "orc_secondary_spheres": ([vp, u32, vp, u32, u32, vp, vp, vp, vp, u32, u32, vp, vp, i32], None),
             "orc_pathtrace": ([vp, u32, vp, u32, vp, u32, vp, u32, u32, vp, vp, vp, u32, u32, vp, i32, u32, u32, vp,
                                vp, i32], u32),
+            "orc_pathtrace_rays": ([vp, u32, vp, u32, vp, vp, u32, u32, vp, u32, vp, i32], u32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -187,3 +188,12 @@ def pathtrace(nodes, tris, mats, consts, w, h, vis, hit_t, bn_rgba, params, prec
                              bn.shape[0], _p(params), precision, y0, h if y1 is None else y1, _p(color), _p(counts),
                              threads)
     return color, counts, st
+
+
+def pathtrace_rays(nodes, tris, mats, rays, params, frame=0, index_base=0, threads=0):
+    """Batched bounce loop for the rays of one scene; returns (radiance (n,3), status)."""
+    rays = np.ascontiguousarray(rays)
+    rad = np.zeros((len(rays), 3), np.float32)
+    st = lib().orc_pathtrace_rays(_p(nodes), len(nodes), _p(tris), len(tris), _p(mats), _p(rays), len(rays),
+                                  index_base, _p(params), frame, _p(rad), threads)
+    return rad, st

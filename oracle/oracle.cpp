@@ -1020,6 +1020,58 @@ void orc_secondary_spheres(const float* spheres, uint32_t ns, const Consts* c, u
     });
 }
 
+// Batched bounce loop restated per ray for one scene: closest hits only,
+// throughput x albedo, sky on escape, a PCG stream per ray seeded by its
+// batch-wide index (index_base + i) and the frame, Russian roulette past
+// rr_start.  radiance: 3 floats per ray.
+uint32_t orc_pathtrace_rays(const Node* nodes, uint32_t nn, const Tri* tris, uint32_t nt, const Mat* mats,
+                            const Ray* rays, uint32_t n, uint32_t index_base, const Params* p, uint32_t frame,
+                            float* radiance, int threads) {
+    std::atomic<uint32_t> status{0};
+    const V3<float> sky{p->sky[0], p->sky[1], p->sky[2]};
+    parallel_rows(n, threads, [&](uint32_t i, int) {
+        uint32_t st = 0;
+        const Ray& ry = rays[i];
+        uint32_t h = (index_base + i) * 0x9E3779B1u + ((frame << 1u) | 1u);
+        uint32_t rng = pcg(h) | 1u;
+        V3<float> o{ry.o[0], ry.o[1], ry.o[2]}, d{ry.d[0], ry.d[1], ry.d[2]}, beta{1, 1, 1}, L{0, 0, 0};
+        float tmax = ry.tmax;
+        for (uint32_t v = 0;; ++v) {
+            uint32_t prim;
+            float t;
+            Pre32 r = pre32(o, d);
+            trace_bvh32(nodes, nn, tris, nt, r, 0.0f, tmax, false, prim, t, nullptr, &st);
+            tmax = INFINITY;
+            if (prim == kMiss) { L = cmul(beta, sky); break; }
+            const Mat& m = mats[prim];
+            V3<float> nrm{m.n[0], m.n[1], m.n[2]};
+            if (dot(nrm, d) > 0.0f) nrm = V3<float>{-nrm.x, -nrm.y, -nrm.z};
+            V3<float> rho{float(m.albedo & 0xFFu) / 255.0f, float((m.albedo >> 8) & 0xFFu) / 255.0f,
+                          float((m.albedo >> 16) & 0xFFu) / 255.0f};
+            beta = cmul(beta, rho);
+            if (v >= p->max_bounces) break;
+            float u1 = random_float(rng), u2 = random_float(rng);
+            V3<float> sp = sphere_point<float>(u1 * 2.0f - 1.0f, u2 * 2.0f - 1.0f);
+            V3<float> nd = nrm + sp;
+            if (dot(nd, nd) == 0.0f) nd = nrm;
+            nd = normalize(nd);
+            if (p->rr_start != 0u && v + 1u > p->rr_start) {
+                float q = std::fmin(std::fmax(std::fmax(std::fmax(beta.x, beta.y), beta.z), 0.05f), 1.0f);
+                if (random_float(rng) >= q) break;
+                beta = V3<float>{beta.x / q, beta.y / q, beta.z / q};
+            }
+            V3<float> hp = o + d * t;
+            o = offset_ray(hp, nrm);
+            d = nd;
+        }
+        radiance[3 * size_t(i)] = L.x;
+        radiance[3 * size_t(i) + 1] = L.y;
+        radiance[3 * size_t(i) + 2] = L.z;
+        if (st) status.fetch_or(st);
+    });
+    return status.load();
+}
+
 // Triangle path tracer (the wavefront estimator, evaluated per pixel) from
 // a primary visibility/t buffer; precision 32 or 64; rows [y0, y1) only
 // (the rest of `color` is left untouched).  counts[0..2] += primary,

@@ -336,3 +336,19 @@ def test_schedule_variants_are_bit_identical(ctx, hf_workload, hf_scene, blue_no
     lib().mrt_cuda_set_tuning(ctx.handle, saved)
     assert np.array_equal(g["visibility"], ref_g["visibility"])
     assert np.array_equal(img.view(np.uint32), ref_img.view(np.uint32))
+
+
+def test_ray_sorting_gives_identical_images(ctx, ico_workload, ico_scene, blue_noise):
+    # sorting reorders the extension queues between bounces; every pixel
+    # owns its path, so the image is bit-identical
+    wl, mesh, bvh = ico_workload
+    saved = ctx.tuning()
+    try:
+        ctx.set_tuning(sort_min_rays=0xFFFFFFFF)
+        ref, _ = _pathtrace_gpu(ctx, wl, ico_scene, blue_noise, frame=1)
+        ctx.set_tuning(sort_min_rays=0)
+        img, _ = _pathtrace_gpu(ctx, wl, ico_scene, blue_noise, frame=1)
+        assert ctx.status() == 0
+    finally:
+        lib().mrt_cuda_set_tuning(ctx.handle, saved)
+    assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
