@@ -367,6 +367,59 @@ int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* batch, const mrt_ray* rays
                              const uint32_t* ray_offsets, const mrt_trace_params* params,
                              uint32_t frame, float* radiance, int use_graph, void* stream);
 
+/* ---- learned radiance cache (new: the reference has no learned part) -- */
+/* A multiresolution hash grid over position (16 levels x 2 FP16 features,
+ * 2^log2_table entries per level, resolutions base_res .. max_res per unit
+ * of the scene box) plus normal and direction, into an MLP of 4 hidden
+ * layers of width 64 (ReLU, no biases, FP16 weights, FP32 accumulation on
+ * the tensor cores) predicting outgoing RGB radiance.  Trained online with
+ * Adam on the relative L2 loss against path-traced suffix radiance. */
+typedef struct mrt_cache_config {
+    uint32_t log2_table;    /* 19                                          */
+    float    base_res;      /* 16                                          */
+    float    max_res;       /* 2048                                        */
+    float    lr_grid;       /* Adam learning rate of the grid features     */
+    float    lr_mlp;        /* Adam learning rate of the MLP weights       */
+    uint32_t seed;
+    uint32_t train_paths;   /* training paths per frame (65536)            */
+    uint32_t train_steps;   /* optimiser steps per frame (4)               */
+    uint32_t train_bounces; /* bounce limit of the training paths (8)      */
+    uint32_t pad;
+} mrt_cache_config;
+typedef struct mrt_cache mrt_cache;
+int mrt_cuda_cache_create(mrt_ctx* ctx, const mrt_cache_config* cfg, mrt_cache** out);
+int mrt_cuda_cache_destroy(mrt_ctx* ctx, mrt_cache* cache);
+/* Scene box the positions are normalised by (queries use [0,1]^3). */
+int mrt_cuda_cache_set_bounds(mrt_ctx* ctx, mrt_cache* cache, const float lo[3], const float hi[3]);
+/* Queries: device rows of 9 floats (position in [0,1]^3, unit normal,
+ * unit outgoing direction); out: device rows of 3 floats. */
+int mrt_cuda_cache_infer(mrt_ctx* ctx, mrt_cache* cache, const float* queries, uint32_t n,
+                         float* out, void* stream);
+/* One training step on n device samples (queries + 3-float targets; n is
+ * rounded down to a multiple of 16): forward, loss, backward; with
+ * apply_update an Adam step (gradients are cleared), otherwise gradients
+ * accumulate.  loss_out (host, may be NULL) receives the mean loss and
+ * synchronises the stream. */
+int mrt_cuda_cache_train_step(mrt_ctx* ctx, mrt_cache* cache, const float* queries,
+                              const float* targets, uint32_t n, int apply_update,
+                              float* loss_out, void* stream);
+/* Host copies of parameters and gradients: which = 0 MLP weights (17408
+ * FP32: 4 layers of 64x64 [out][in], then 16x64 output rows), 1 their
+ * gradients, 2 grid features (16 * 2^log2_table * 2 FP32), 3 their
+ * gradients.  set != 0 writes host -> device (and refreshes FP16 copies). */
+int mrt_cuda_cache_params(mrt_ctx* ctx, mrt_cache* cache, int which, float* host,
+                          size_t count, int set);
+/* One frame of cache-terminated path tracing (replaces the secondary pass):
+ * trains the cache on cfg.train_paths fresh paths from this frame's camera
+ * (cfg.train_steps Adam steps), then per pixel traces the primary hit's
+ * shadow ray and one diffuse bounce and ends the path in the cache at the
+ * bounce's hit: color += throughput x cache(x1, n1, -d1).  Same g-buffer,
+ * parameters and output as mrt_cuda_secondary_rays (max_bounces is
+ * ignored: paths end at the first bounce). */
+int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
+                         const mrt_gbuffer* gbuffer, const mrt_camera_consts* consts,
+                         const mrt_trace_params* params, float* color, int train, void* stream);
+
 /* Primary rays for callers that cannot allocate device memory.
  *
  * No counterpart in the reference.  Some callers of this library may not

@@ -72,6 +72,12 @@ class Tuning(C.Structure):
                 ("primary_persistent", C.c_uint32), ("sort_min_rays", C.c_uint32)]
 
 
+class CacheConfig(C.Structure):
+    _fields_ = [("log2_table", C.c_uint32), ("base_res", C.c_float), ("max_res", C.c_float), ("lr_grid", C.c_float),
+                ("lr_mlp", C.c_float), ("seed", C.c_uint32), ("train_paths", C.c_uint32), ("train_steps", C.c_uint32),
+                ("train_bounces", C.c_uint32), ("pad", C.c_uint32)]
+
+
 class DeviceInfo(C.Structure):
     _fields_ = [("name", C.c_char * 96), ("sm_count", C.c_int32), ("cc_major", C.c_int32), ("cc_minor", C.c_int32),
                 ("trace_blocks_per_sm_max", C.c_uint32), ("total_mem", C.c_uint64), ("l2_bytes", C.c_uint64)]
@@ -159,6 +165,14 @@ def lib() -> C.CDLL:
                                             vp, vp, vp, vp], i32),
             "mrt_cuda_primary_rays_noalloc": ([vp, u32, vp, u32, vp, u32, C.POINTER(CameraConsts),
                                                C.POINTER(GBuffer), vp, vp], i32),
+            "mrt_cuda_cache_create": ([vp, C.POINTER(CacheConfig), pp], i32),
+            "mrt_cuda_cache_destroy": ([vp, vp], i32),
+            "mrt_cuda_cache_set_bounds": ([vp, vp, C.POINTER(C.c_float), C.POINTER(C.c_float)], i32),
+            "mrt_cuda_cache_infer": ([vp, vp, vp, u32, vp, vp], i32),
+            "mrt_cuda_cache_train_step": ([vp, vp, vp, vp, u32, i32, C.POINTER(C.c_float), vp], i32),
+            "mrt_cuda_cache_params": ([vp, vp, i32, vp, sz, i32], i32),
+            "mrt_cuda_cache_frame": ([vp, vp, vp, C.POINTER(GBuffer), C.POINTER(CameraConsts), C.POINTER(TraceParams),
+                                      vp, i32, vp], i32),
             "mrt_cuda_batch_create": ([vp, u32, vp, vp, vp, vp, vp, pp], i32),
             "mrt_cuda_batch_destroy": ([vp, vp], i32),
             "mrt_cuda_batch_trace": ([vp, vp, vp, vp, vp, u32, vp], i32),

@@ -187,6 +187,12 @@ int check_gbuffer(mrt_ctx* ctx, const mrt_gbuffer* g) {
 } // namespace
 
 namespace mrt {
+// learned radiance cache (nrc.cu)
+cudaError_t cache_infer(const mrt_cache* c, const float* q, uint32_t n, const uint32_t* n_dev, float* out,
+                        cudaStream_t s);
+int cache_frame_buffers(mrt_ctx* ctx, mrt_cache* c, size_t n, float** q, float4** pb, float** pred);
+int cache_train_frame(mrt_ctx* ctx, mrt_cache* c, const DevScene& sc, const FrameParams& fp, const TraceParams& tp,
+                      uint32_t* status, cudaStream_t s);
 // Frame constants for entry points outside this file (noalloc.cu).
 FrameParams make_frame_params(const mrt_camera_consts* c, uint32_t w, uint32_t h) { return frame_params(c, w, h); }
 // Error reporting, persistent grid size and trace-parameter conversion for
@@ -671,6 +677,62 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
         MRT_LAUNCH(3, 0, launch_tally(wb, s));
     }
     MRT_LAUNCH(3, 0, launch_finalize(wb, color, tp.samples, params->accumulate, params->frame_index, s));
+#undef MRT_LAUNCH
+    return MRT_OK;
+}
+
+int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene, const mrt_gbuffer* gbuffer,
+                         const mrt_camera_consts* consts, const mrt_trace_params* params, float* color, int train,
+                         void* stream) {
+    if (!ctx || !cache || !scene || !consts || !params || !color)
+        return fail(ctx, MRT_EINVAL, "cache_frame: null argument");
+    if (scene->kind != 0) return fail(ctx, MRT_EINVAL, "cache_frame: triangle scenes only");
+    int rc = check_gbuffer(ctx, gbuffer);
+    if (rc) return rc;
+    if (!gbuffer->hit_t) return fail(ctx, MRT_EINVAL, "cache_frame: gbuffer hit_t required");
+    if (!ctx->d_bn) return fail(ctx, MRT_ESTATE, "no blue-noise texture uploaded");
+    if (params->rng_mode > MRT_RNG_PER_PIXEL || params->estimator > MRT_EST_NEE)
+        return fail(ctx, MRT_EINVAL, "bad rng_mode or estimator");
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = as_stream(stream);
+    const uint32_t W = gbuffer->width, H = gbuffer->height;
+    const FrameParams fp = frame_params(consts, W, H);
+    TraceParams tp = trace_params(params);
+    const BlueNoise bn{ctx->d_bn, ctx->bn_w, ctx->bn_h};
+    Scope total(ctx, s, 5, 0);
+    if (train) {
+        Scope sc(ctx, s, 6, 0);
+        rc = cache_train_frame(ctx, cache, scene->dev, fp, tp, ctx->d_status, s);
+        if (rc) return rc;
+    }
+    rc = ensure_wave(ctx, size_t(W) * H);
+    if (rc) return rc;
+    WaveBuffers& wb = ctx->wb;
+    float *q = nullptr, *pred = nullptr;
+    float4* pb = nullptr;
+    rc = cache_frame_buffers(ctx, cache, wb.cap, &q, &pb, &pred);
+    if (rc) return rc;
+    tp.samples = 1;
+    tp.max_bounces = 1;  // the path ends in the cache at the first bounce's hit
+    const int tblocks = trace_blocks(ctx);
+    const bool nee = tp.estimator == MRT_EST_NEE;
+    const bool dyn = (ctx->tuning.dynamic_fetch & 1u) != 0u, dyn_sh = (ctx->tuning.dynamic_fetch & 2u) != 0u;
+#define MRT_LAUNCH(kind, bounce, expr)                                                                   \
+    do {                                                                                                 \
+        Scope sc_(ctx, s, kind, bounce);                                                                 \
+        cudaError_t e_ = (expr);                                                                         \
+        if (e_ != cudaSuccess) return fail(ctx, MRT_ECUDA, "%s: %s", #expr, cudaGetErrorString(e_));    \
+        ctx->launches++;                                                                                 \
+    } while (0)
+    MRT_CK(cudaMemsetAsync(wb.counters, 0, kCntSlots * sizeof(uint32_t), s));
+    MRT_LAUNCH(3, 0, launch_shade_primary(scene->dev, fp, *gbuffer, tp, bn, wb, 0, ctx->d_status, s));
+    if (nee) MRT_LAUNCH(2, 0, launch_trace_shadow(scene->dev, wb, tp, 0, tblocks, ctx->d_status, ctx->counters, dyn_sh, s));
+    MRT_LAUNCH(1, 1, launch_trace_ext(scene->dev, wb, 1, tblocks, ctx->d_status, ctx->counters, dyn, s));
+    MRT_LAUNCH(3, 1, launch_cache_query(scene->dev, tp, wb, q, pb, ctx->d_status, s));
+    MRT_LAUNCH(6, 1, cache_infer(cache, q, uint32_t(wb.cap), wb.counters + kCntExt + 1, pred, s));
+    MRT_LAUNCH(3, 1, launch_cache_apply(wb, pred, pb, s));
+    MRT_LAUNCH(3, 0, launch_tally(wb, s));
+    MRT_LAUNCH(3, 0, launch_finalize(wb, color, 1, params->accumulate, params->frame_index, s));
 #undef MRT_LAUNCH
     return MRT_OK;
 }

@@ -133,6 +133,14 @@ cudaError_t launch_sort_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t 
 cudaError_t launch_finalize(const WaveBuffers& wb, float* color, uint32_t samples, uint32_t accumulate,
                             uint32_t frame_index, cudaStream_t s);
 
+// learned radiance cache (kernels.cu)
+cudaError_t launch_cache_train_paths(const DevScene& sc, const FrameParams& fp, const TraceParams& tp,
+                                     uint32_t bounces, uint32_t n_paths, uint32_t frame, float* q, float* t,
+                                     uint32_t* count, uint32_t cap, uint32_t* status, cudaStream_t s);
+cudaError_t launch_cache_query(const DevScene& sc, const TraceParams& tp, const WaveBuffers& wb, float* q,
+                               float4* pb, uint32_t* status, cudaStream_t s);
+cudaError_t launch_cache_apply(const WaveBuffers& wb, const float* pred, const float4* pb, cudaStream_t s);
+
 int trace_blocks_per_sm();  // occupancy of the traversal kernels
 
 } // namespace mrt

@@ -744,6 +744,166 @@ cudaError_t launch_shade(const DevScene& sc, const TraceParams& tp, BlueNoise bn
     return cudaGetLastError();
 }
 
+// ---- learned radiance cache: training samples and cache-terminated shading
+
+constexpr int kTrainMaxVerts = 9;
+
+MRT_DEV void cache_query_row(const DevScene& sc, f3 p, f3 n, f3 wo, float* q) {
+    q[0] = __fmul_rn(__fsub_rn(p.x, sc.lo[0]), sc.inv_ext[0]);
+    q[1] = __fmul_rn(__fsub_rn(p.y, sc.lo[1]), sc.inv_ext[1]);
+    q[2] = __fmul_rn(__fsub_rn(p.z, sc.lo[2]), sc.inv_ext[2]);
+    q[3] = n.x; q[4] = n.y; q[5] = n.z;
+    q[6] = wo.x; q[7] = wo.y; q[8] = wo.z;
+}
+
+// One thread per training path from a hashed pixel of this frame's camera:
+// the plain estimator (shadow ray per vertex, cosine-weighted bounces,
+// Russian roulette past rr_start) up to `bounces` bounces; afterwards the
+// suffix radiance L_o(x_v, -d_v) of every vertex is a training target for
+// the cache query (x_v, n_v, -d_v).
+__global__ void __launch_bounds__(kTraceBlock)
+k_cache_train_paths(DevScene sc, FrameParams fp, TraceParams tp, uint32_t bounces, uint32_t n_paths,
+                    uint32_t frame, float* out_q, float* out_t, uint32_t* count, uint32_t cap, uint32_t* status) {
+    __shared__ uint2 stk[kStackDepth * kTraceBlock];
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_paths) return;
+    uint32_t st = 0u, cn = 0u, ct = 0u;
+    uint32_t h = p * 0x9E3779B1u + frame * 0x85EBCA6Bu + 0x632BE5ABu;
+    const uint32_t pix = pcg(h) % (fp.width * fp.height);
+    uint32_t rng = pcg(h) | 1u;
+    f3 o, d;
+    primary_ray(fp, pix % fp.width, pix / fp.width, o, d);
+    const f3 sun{tp.sun[0], tp.sun[1], tp.sun[2]};
+    const f3 sky{tp.sky[0], tp.sky[1], tp.sky[2]};
+    float qv[kTrainMaxVerts][9];
+    f3 nee[kTrainMaxVerts], rho[kTrainMaxVerts];
+    float wcont[kTrainMaxVerts];
+    int nv = 0;
+    bool escaped = false;
+    const uint32_t maxb = bounces < uint32_t(kTrainMaxVerts - 1) ? bounces : uint32_t(kTrainMaxVerts - 1);
+    for (uint32_t v = 0;; ++v) {
+        uint32_t prim;
+        float t;
+        trace_bvh8<false, false, kStackDepth>(sc, o, d, 0.0f, INFINITY, prim, t, stk + threadIdx.x, kTraceBlock, st,
+                                              cn, ct);
+        if (prim == kMiss) { escaped = v > 0; break; }
+        const mrt_material m = load_mat(sc, prim, status);
+        const f3 n = facing_normal(m, d);
+        const f3 x = ray_at(o, d, t);
+        cache_query_row(sc, x, n, f3{-d.x, -d.y, -d.z}, qv[nv]);
+        rho[nv] = f3{__fdiv_rn(float(m.albedo_rgba8 & 0xFFu), 255.0f),
+                     __fdiv_rn(float((m.albedo_rgba8 >> 8) & 0xFFu), 255.0f),
+                     __fdiv_rn(float((m.albedo_rgba8 >> 16) & 0xFFu), 255.0f)};
+        nee[nv] = f3{0.0f, 0.0f, 0.0f};
+        wcont[nv] = 0.0f;
+        if (tp.estimator == MRT_EST_NEE) {
+            const float cosl = dot_rn(n, sun);
+            if (cosl > 0.0f) {
+                uint32_t sp;
+                float stt;
+                trace_bvh8<true, false, kStackDepth>(sc, offset_ray(x, n), sun, 0.0f, INFINITY, sp, stt,
+                                                     stk + threadIdx.x, kTraceBlock, st, cn, ct);
+                if (sp == kMiss)
+                    nee[nv] = scale_rn(mul_rn(rho[nv], f3{tp.sun_e[0], tp.sun_e[1], tp.sun_e[2]}),
+                                       __fmul_rn(cosl, kInvPi));
+            }
+        }
+        ++nv;
+        if (v >= maxb) break;
+        const float u1 = random_float(rng), u2 = random_float(rng);
+        f3 nd = add_rn(n, random_sphere_point(__fsub_rn(__fmul_rn(u1, 2.0f), 1.0f),
+                                              __fsub_rn(__fmul_rn(u2, 2.0f), 1.0f)));
+        if (dot_rn(nd, nd) == 0.0f) nd = n;
+        nd = normalize_rn(nd);
+        float w = 1.0f;
+        if (tp.rr_start != 0u && v + 1u > tp.rr_start) {
+            const f3 b = rho[nv - 1];
+            const float q = fminf(fmaxf(fmaxf(fmaxf(b.x, b.y), b.z), 0.05f), 1.0f);
+            if (random_float(rng) >= q) break;
+            w = 1.0f / q;
+        }
+        wcont[nv - 1] = w;
+        o = offset_ray(x, n);
+        d = nd;
+    }
+    if (st) atomicOr(status, st);
+    // suffix radiance, last vertex first
+    f3 next = escaped ? sky : f3{0.0f, 0.0f, 0.0f};
+    for (int v = nv - 1; v >= 0; --v) {
+        const float w = wcont[v];
+        const f3 L{nee[v].x + rho[v].x * w * next.x, nee[v].y + rho[v].y * w * next.y,
+                   nee[v].z + rho[v].z * w * next.z};
+        const uint32_t slot = atomicAdd(count, 1u);
+        if (slot < cap) {
+            for (int k = 0; k < 9; ++k) out_q[size_t(slot) * 9 + k] = qv[v][k];
+            out_t[size_t(slot) * 3 + 0] = L.x;
+            out_t[size_t(slot) * 3 + 1] = L.y;
+            out_t[size_t(slot) * 3 + 2] = L.z;
+        }
+        next = L;
+    }
+}
+
+// For each bounce-1 extension ray: escaped -> sky into the pixel; hit ->
+// the cache query row at the hit and (throughput, pixel) for the apply.
+__global__ void __launch_bounds__(kShadeBlock)
+k_cache_query(DevScene sc, TraceParams tp, WaveBuffers wb, float* q, float4* pb, uint32_t* status) {
+    const uint32_t n = wb.counters[kCntExt + 1];
+    const PathRay* qin = ext_queue(wb, 1);
+    const f3 sky{tp.sky[0], tp.sky[1], tp.sky[2]};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const PathRay pr = qin[i];
+        const uint2 h = wb.hits[i];
+        const uint32_t pix = __float_as_uint(pr.o_pix.w);
+        const f3 beta{pr.beta.x, pr.beta.y, pr.beta.z};
+        float* row = q + size_t(i) * 9;
+        if (h.x == kMiss) {
+            add_L(wb.L, pix, mul_rn(beta, sky));
+            for (int k = 0; k < 9; ++k) row[k] = 0.0f;
+            pb[i] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(pix));
+        } else {
+            const f3 o{pr.o_pix.x, pr.o_pix.y, pr.o_pix.z}, d{pr.d.x, pr.d.y, pr.d.z};
+            const mrt_material m = load_mat(sc, h.x, status);
+            const f3 nrm = facing_normal(m, d);
+            cache_query_row(sc, ray_at(o, d, __uint_as_float(h.y)), nrm, f3{-d.x, -d.y, -d.z}, row);
+            pb[i] = make_float4(beta.x, beta.y, beta.z, __uint_as_float(pix));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kShadeBlock)
+k_cache_apply(WaveBuffers wb, const float* pred, const float4* pb) {
+    const uint32_t n = wb.counters[kCntExt + 1];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 b = pb[i];
+        if (b.x == 0.0f && b.y == 0.0f && b.z == 0.0f) continue;
+        const f3 y{fmaxf(pred[3 * size_t(i)], 0.0f), fmaxf(pred[3 * size_t(i) + 1], 0.0f),
+                   fmaxf(pred[3 * size_t(i) + 2], 0.0f)};
+        add_L(wb.L, __float_as_uint(b.w), mul_rn(f3{b.x, b.y, b.z}, y));
+    }
+}
+
+cudaError_t launch_cache_train_paths(const DevScene& sc, const FrameParams& fp, const TraceParams& tp,
+                                     uint32_t bounces, uint32_t n_paths, uint32_t frame, float* q, float* t,
+                                     uint32_t* count, uint32_t cap, uint32_t* status, cudaStream_t s) {
+    k_cache_train_paths<<<(n_paths + kTraceBlock - 1) / kTraceBlock, kTraceBlock, 0, s>>>(
+        sc, fp, tp, bounces, n_paths, frame, q, t, count, cap, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cache_query(const DevScene& sc, const TraceParams& tp, const WaveBuffers& wb, float* q, float4* pb,
+                               uint32_t* status, cudaStream_t s) {
+    const uint32_t b = uint32_t((wb.cap + kShadeBlock - 1) / kShadeBlock);
+    k_cache_query<<<b < 4096 ? b : 4096, kShadeBlock, 0, s>>>(sc, tp, wb, q, pb, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cache_apply(const WaveBuffers& wb, const float* pred, const float4* pb, cudaStream_t s) {
+    const uint32_t b = uint32_t((wb.cap + kShadeBlock - 1) / kShadeBlock);
+    k_cache_apply<<<b < 4096 ? b : 4096, kShadeBlock, 0, s>>>(wb, pred, pb);
+    return cudaGetLastError();
+}
+
 // ---- ray sorting between bounces: one counting-sort pass on a 12-bit key,
 // direction octant (3 bits) above a 9-bit Morton code of the origin in the
 // scene box (3 bits per axis), so rays sharing a direction octant and a

@@ -1,0 +1,134 @@
+"""Learned radiance cache on the GPU: forward and gradients of the CUDA
+kernels against the FP64 oracle (oracle/nrc.py, itself checked against
+finite differences), training convergence, and what the trained cache gains
+over the plain path tracer at equal frame count."""
+import numpy as np
+import pytest
+
+from oracle import nrc
+from minotert_gb300.cache import RadianceCache, default_config
+
+pytestmark = pytest.mark.gpu
+
+LOG2_T = 14
+
+
+def _queries(n, seed):
+    rng = np.random.default_rng(seed)
+    q = np.zeros((n, 9), np.float32)
+    q[:, :3] = rng.uniform(0.02, 0.98, (n, 3))
+    nn = rng.normal(size=(n, 3))
+    q[:, 3:6] = nn / np.linalg.norm(nn, axis=1, keepdims=True)
+    dd = rng.normal(size=(n, 3))
+    q[:, 6:9] = dd / np.linalg.norm(dd, axis=1, keepdims=True)
+    return q
+
+
+def _cache(ctx, seed=1):
+    c = RadianceCache(ctx, default_config(log2_table=LOG2_T, base_res=16.0, max_res=512.0, seed=seed))
+    rng = np.random.default_rng(seed)
+    W = c.params(0)
+    W[nrc.HIDDEN * 4096:nrc.HIDDEN * 4096 + 3 * 64] = rng.uniform(-0.3, 0.3, 192)  # non-trivial outputs
+    c.set_params(0, W)
+    G = rng.uniform(-0.5, 0.5, c.grid_floats).astype(np.float32)
+    c.set_params(2, G)
+    return c, W, G
+
+
+def test_cache_forward_matches_oracle(ctx):
+    c, W, G = _cache(ctx)
+    q = _queries(1000, 2)
+    d_q, d_o = ctx.to_device(q), ctx.alloc(12 * len(q))
+    c.infer(d_q, len(q), d_o)
+    y = d_o.download(np.float32, (len(q), 3))
+    ref = nrc.predict(G.astype(np.float64), W.astype(np.float64), q.astype(np.float64), LOG2_T, 16.0, 512.0)
+    assert np.all(np.isfinite(y))
+    err = np.abs(y - ref)
+    assert np.max(err) < 2e-2 * max(1.0, np.max(np.abs(ref)))
+    assert np.mean(err) < 2e-3 * max(1.0, np.mean(np.abs(ref)))
+
+
+def test_cache_gradients_match_oracle(ctx):
+    c, W, G = _cache(ctx, seed=3)
+    q = _queries(512, 4)
+    t = np.random.default_rng(5).uniform(0.1, 1.0, (len(q), 3)).astype(np.float32)
+    d_q, d_t = ctx.to_device(q), ctx.to_device(t)
+    loss = c.train_step(d_q, d_t, len(q), update=False, want_loss=True)
+    gW, gG = c.params(1).astype(np.float64), c.params(3).astype(np.float64)
+    rloss, rgW, rgG, _ = nrc.loss_and_grads(G.astype(np.float64), W.astype(np.float64), q.astype(np.float64),
+                                            t.astype(np.float64), LOG2_T, 16.0, 512.0, fp16=True)
+    assert abs(loss - rloss) < 2e-2 * rloss
+    for a, b in ((gW, rgW), (gG, rgG)):
+        cos = a @ b / (np.linalg.norm(a) * np.linalg.norm(b))
+        assert cos > 0.999, cos
+        assert abs(np.linalg.norm(a) / np.linalg.norm(b) - 1.0) < 0.03
+
+
+def test_cache_learns_a_smooth_function(ctx):
+    c = RadianceCache(ctx, default_config(log2_table=16, seed=7, lr_grid=1e-2, lr_mlp=1e-3))
+    q = _queries(8192, 8)
+    p = q[:, :3]
+    t = np.stack([0.5 + 0.4 * np.sin(6 * p[:, 0]) * np.cos(4 * p[:, 1]), 0.3 + 0.2 * p[:, 2],
+                  0.2 + 0.5 * p[:, 0] * p[:, 1]], axis=1).astype(np.float32)
+    d_q, d_t = ctx.to_device(q), ctx.to_device(t)
+    first = c.train_step(d_q, d_t, len(q), want_loss=True)
+    for _ in range(300):
+        c.train_step(d_q, d_t, len(q))
+    last = c.train_step(d_q, d_t, len(q), want_loss=True)
+    assert last < first / 20, (first, last)
+    d_o = ctx.alloc(12 * len(q))
+    c.infer(d_q, len(q), d_o)
+    y = d_o.download(np.float32, (len(q), 3))
+    assert np.sqrt(np.mean((y - t) ** 2)) < 0.05
+
+
+def _rmse(a, b):
+    return float(np.sqrt(np.mean((a - b) ** 2)))
+
+
+def test_trained_cache_beats_plain_path_tracing_at_equal_frames(ctx, hf_workload, blue_noise):
+    # 128x128 heightfield scene; reference: plain path tracer, 1024 frames of
+    # 1 spp.  After 48 training frames, 8 frames of cache-terminated paths
+    # must be closer to the reference than 8 frames of the plain tracer.
+    from minotert_gb300 import workloads
+    from minotert_gb300.pathtracer import Pathtracer, TraceSettings, camera_consts
+    from minotert_gb300.scene import DeviceScene
+    wl = workloads.heightfield_boxes_256(size=128)
+    mesh = hf_workload[1]
+    ds = DeviceScene.triangles(ctx, mesh, hf_workload[2])
+    pt = Pathtracer(ctx, ds, full_gbuffer=False)
+    W, H = wl.width, wl.height
+    ctx.blue_noise(blue_noise)
+    plain_settings = TraceSettings(samples=1, bounces=6, rr_start=2, rng_mode=1)
+
+    def accumulate(frames, fn, start=0):
+        col = ctx.alloc(12 * W * H)
+        for f in range(frames):
+            pt.frame_counter = start + f
+            gb = pt.primaryRays((W, H), wl.camera, wl.camera)
+            fn(gb, col, f)
+        return col.download(np.float32, (H, W, 3))
+
+    def plain(gb, col, f):
+        s = TraceSettings(1, 6, 2, 1, True, f)
+        pt.secondaryRays(gb, wl.camera, wl.sky, blue_noise, s, color=col)
+
+    ref = accumulate(1024, plain, start=10000)
+    plain8 = accumulate(8, plain, start=0)
+    cache = RadianceCache(ctx, default_config(train_paths=16384, train_steps=4, train_bounces=6),
+                          bounds=(mesh.lo, mesh.hi))
+
+    def learned(train):
+        def fn(gb, col, f):
+            consts = camera_consts(wl.camera, wl.camera, pt.frame_counter)
+            params = TraceSettings(1, 1, 2, 1, True, f).params(wl.sky)
+            cache.frame(ds, gb, consts, params, col, train=train)
+        return fn
+
+    accumulate(48, learned(True), start=20000)  # online training
+    learned8 = accumulate(8, learned(True), start=0)
+    assert ctx.status() == 0
+    r_plain, r_learned = _rmse(plain8, ref), _rmse(learned8, ref)
+    print(f"RMSE after 8 frames: plain {r_plain:.4f}, learned {r_learned:.4f}")
+    assert np.isfinite(learned8).all()
+    assert r_learned < r_plain
