@@ -432,6 +432,116 @@ def run_batched(args, world, rank, local, dist):
         dist.destroy_process_group()
 
 
+def run_cache_experiment(args, world, rank, local, dist):
+    """GPU milliseconds to a target RMSE against a 4096-spp plain reference:
+    plain 1-spp accumulation vs cache-terminated paths with online training
+    (training time included), heightfield + boxes scene at 1920x1080.  The
+    reference is checked on a crop against the FP64 oracle."""
+    from minotert_gb300 import build as _build
+    _build.build()
+    import oracle
+    from minotert_gb300 import scene, workloads
+    from minotert_gb300._lib import Context
+    from minotert_gb300.cache import RadianceCache, default_config
+    from minotert_gb300.pathtracer import Camera, Pathtracer, TraceSettings, camera_consts
+
+    base = workloads.heightfield_boxes_256()
+    W, H = 1920, 1080
+    c0 = base.camera
+    cam = Camera((W, H), c0.verticalFov, c0.nearPlane, c0.position, c0.yaw, c0.pitch)
+    mesh = base.mesh()
+    bvh = scene.build_bvh8(mesh)
+    bn = scene.blue_noise(1, 64)
+    ctx = Context(local)
+    ds = scene.DeviceScene.triangles(ctx, mesh, bvh)
+    ctx.blue_noise(bn)
+    pt = Pathtracer(ctx, ds, full_gbuffer=False)
+    stream = ctx.stream()
+    sky = base.sky
+    PLAIN = dict(bounces=8, rr_start=2, rng_mode=1)
+
+    def run(frames, start, fn, checkpoints=()):
+        col = ctx.alloc(12 * W * H)
+        evs, snaps = [], {}
+        for f in range(frames):
+            pt.frame_counter = start + f
+            a, b = ctx.event(), ctx.event()
+            ctx.record(a, stream)
+            gb = pt.primaryRays((W, H), cam, cam, stream)
+            fn(gb, col, f)
+            ctx.record(b, stream)
+            evs.append((a, b))
+            if f + 1 in checkpoints:
+                snaps[f + 1] = col.download(np.float32, (H, W, 3), stream)
+        ctx.sync(stream)
+        ms = np.cumsum([ctx.elapsed_ms(a, b) for a, b in evs])
+        return col.download(np.float32, (H, W, 3), stream), ms, snaps
+
+    def plain_fn(gb, col, f):
+        pt.secondaryRays(gb, cam, sky, bn, TraceSettings(1, PLAIN["bounces"], PLAIN["rr_start"], PLAIN["rng_mode"],
+                                                        True, f), color=col, stream=stream)
+
+    t0 = time.perf_counter()
+    ref_frames = 4096
+    ref, ref_ms, _ = run(ref_frames, 1 << 20, plain_fn)
+    ref_s = time.perf_counter() - t0
+    # FP64 check of the reference on a crop (4096 samples per pixel)
+    y0, y1, x0, x1 = 600, 616, 900, 932
+    consts = oracle.camera_consts(cam.position, cam.yaw, cam.pitch, cam.verticalFov, cam.nearPlane, W, H)
+    p = oracle.primary(consts, W, H, bvh.nodes, bvh.tris, mesh.mats, y0=y0, y1=y1)
+    sd = np.asarray(sky.sun_dir, np.float64)
+    sd = (sd / np.linalg.norm(sd)).astype(np.float32)
+    prm = oracle.params_array(4096, PLAIN["bounces"], PLAIN["rr_start"], PLAIN["rng_mode"], 1, sun=sd,
+                              sun_e=sky.sun_irradiance, sky=sky.radiance)
+    crop64, _, _ = oracle.pathtrace(bvh.nodes, bvh.tris, mesh.mats, consts, W, H, p["visibility"], p["hit_t"], bn, prm,
+                                    precision=64, y0=y0, y1=y1)
+    a, b = ref[y0:y1, x0:x1], crop64[y0:y1, x0:x1]
+    ref_check = {"crop": [y0, y1, x0, x1], "rmse_vs_fp64": float(np.sqrt(np.mean((a - b) ** 2))),
+                 "mean": float(b.mean()), "relative": float(np.sqrt(np.mean((a - b) ** 2)) / max(b.mean(), 1e-9))}
+
+    cps = (1, 2, 4, 8, 16, 32, 64, 128, 256, 512)
+    nmax = max(cps)
+    _, plain_ms, plain_snaps = run(nmax, 0, plain_fn, cps)
+    cache = RadianceCache(ctx, default_config(), bounds=(mesh.lo, mesh.hi))
+
+    def learned_fn(gb, col, f):
+        consts_c = camera_consts(cam, cam, pt.frame_counter)
+        params = TraceSettings(1, 1, 2, 1, True, f).params(sky)
+        cache.frame(ds, gb, consts_c, params, col, train=True, stream=stream)
+
+    _, learned_ms, learned_snaps = run(nmax, 0, learned_fn, cps)
+    rmse = lambda im: float(np.sqrt(np.mean((im - ref) ** 2)))
+    curve_p = [(k, float(plain_ms[k - 1]), rmse(plain_snaps[k])) for k in cps]
+    curve_l = [(k, float(learned_ms[k - 1]), rmse(learned_snaps[k])) for k in cps]
+
+    def time_to(curve, target):
+        # first checkpoint at or below target, log-log interpolation between checkpoints
+        for i, (k, ms, r) in enumerate(curve):
+            if r <= target:
+                if i == 0:
+                    return ms
+                k0, ms0, r0 = curve[i - 1]
+                u = (np.log(r0) - np.log(target)) / (np.log(r0) - np.log(r))
+                return float(np.exp(np.log(ms0) + u * (np.log(ms) - np.log(ms0))))
+        # beyond the last checkpoint: extrapolate plain Monte Carlo, RMSE ~ t^-1/2
+        k, ms, r = curve[-1]
+        return float(ms * (r / target) ** 2)
+
+    best_l = min(r for _, _, r in curve_l)
+    target = float(max(best_l * 1.02, 0.004))
+    tp, tl = time_to(curve_p, target), time_to(curve_l, target)
+    out = {"metric": "GPU ms to target RMSE: learned radiance cache vs plain path tracing", "unit": "ms",
+           "value": tl, "higher_is_better": False, "target_rmse": target,
+           "plain_ms": tp, "learned_ms": tl, "speedup": tp / tl if tl > 0 else None,
+           "config": {"workload": "heightfield_boxes_1080p_radiance_cache", "width": W, "height": H,
+                      "triangles": mesh.tri_count, "plain": PLAIN, "cache": "16 levels x 2 features, 2^19 entries, "
+                      "4x64 ReLU MLP, 65536 training paths x 4 Adam steps per frame, paths end at the first bounce",
+                      "reference": f"{ref_frames} frames of 1-spp plain path tracing ({ref_s:.1f} s)"},
+           "reference_check": ref_check, "curve_plain": curve_p, "curve_learned": curve_l,
+           "device_status": ctx.status()}
+    print(json.dumps(out))
+
+
 def run_reference(args, world, rank, local, dist):
     """The reference path on the host cores: MinoteRT's own implementation
     is Vulkan + MSVC only and cannot run here, so its CPU restatement (the
@@ -474,7 +584,8 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["icospheres_1080p", "batched64"], default="icospheres_1080p")
+    ap.add_argument("--workload", choices=["icospheres_1080p", "batched64", "radiance_cache"],
+                    default="icospheres_1080p")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
     world, rank, local, dist = _dist()
@@ -482,6 +593,8 @@ def main(argv=None):
         run_reference(args, world, rank, local, dist)
     elif args.workload == "batched64":
         run_batched(args, world, rank, local, dist)
+    elif args.workload == "radiance_cache":
+        run_cache_experiment(args, world, rank, local, dist)
     else:
         run_mine(args, world, rank, local, dist)
 

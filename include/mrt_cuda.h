@@ -420,6 +420,38 @@ int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
                          const mrt_gbuffer* gbuffer, const mrt_camera_consts* consts,
                          const mrt_trace_params* params, float* color, int train, void* stream);
 
+/* ---- learned denoiser (new; the reference's denoiser is the joint
+ *      bilateral filter of src/gpu/denoise/bilateral.comp) --------------
+ * A 3-level U-Net (3x3 convolutions, 32/64/128 channels, skip
+ * connections) over 16-channel BF16 NHWC features: log(1 + radiance),
+ * albedo, normal, depth, zero padding.  Forward on the tensor cores (BF16,
+ * FP32 accumulate); training backward in FP32; Adam.  The network predicts
+ * log(1 + radiance) with an L1 loss.  Width and height must be multiples
+ * of 4. */
+typedef struct mrt_denoiser mrt_denoiser;
+int mrt_cuda_denoiser_create(mrt_ctx* ctx, uint32_t seed, mrt_denoiser** out);
+int mrt_cuda_denoiser_destroy(mrt_ctx* ctx, mrt_denoiser* den);
+int mrt_cuda_denoiser_param_count(mrt_denoiser* den, size_t* weights, size_t* biases);
+/* Features of one frame from its g-buffer (visibility + hit_t) and colour
+ * (float RGB); scene_diagonal normalises depth.  features: device,
+ * width*height*16 BF16. */
+int mrt_cuda_denoiser_features(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuffer* gbuffer,
+                               const float* color, float scene_diagonal, uint16_t* features,
+                               void* stream);
+/* Denoised colour (float RGB) of `batch` feature images. */
+int mrt_cuda_denoiser_infer(mrt_ctx* ctx, mrt_denoiser* den, const uint16_t* features, uint32_t batch,
+                            uint32_t width, uint32_t height, float* out, void* stream);
+/* One step on a batch of feature images and float RGB targets; lr is the
+ * Adam learning rate; apply_update = 0 only accumulates gradients.
+ * loss_out (host, may be NULL) receives the mean L1 loss and synchronises. */
+int mrt_cuda_denoiser_train_step(mrt_ctx* ctx, mrt_denoiser* den, const uint16_t* features,
+                                 const float* targets, uint32_t batch, uint32_t width, uint32_t height,
+                                 float lr, int apply_update, float* loss_out, void* stream);
+/* which = 0 weights then biases (FP32 masters; layer l's weights are
+ * [cout][3x3 tap][cin]), 1 their gradients; set != 0 writes host -> device. */
+int mrt_cuda_denoiser_params(mrt_ctx* ctx, mrt_denoiser* den, int which, float* host, size_t count,
+                             int set);
+
 /* Primary rays for callers that cannot allocate device memory.
  *
  * No counterpart in the reference.  Some callers of this library may not

@@ -173,6 +173,14 @@ def lib() -> C.CDLL:
             "mrt_cuda_cache_params": ([vp, vp, i32, vp, sz, i32], i32),
             "mrt_cuda_cache_frame": ([vp, vp, vp, C.POINTER(GBuffer), C.POINTER(CameraConsts), C.POINTER(TraceParams),
                                       vp, i32, vp], i32),
+            "mrt_cuda_denoiser_create": ([vp, u32, pp], i32),
+            "mrt_cuda_denoiser_destroy": ([vp, vp], i32),
+            "mrt_cuda_denoiser_param_count": ([vp, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)], i32),
+            "mrt_cuda_denoiser_features": ([vp, vp, C.POINTER(GBuffer), vp, C.c_float, vp, vp], i32),
+            "mrt_cuda_denoiser_infer": ([vp, vp, vp, u32, u32, u32, vp, vp], i32),
+            "mrt_cuda_denoiser_train_step": ([vp, vp, vp, vp, u32, u32, u32, C.c_float, i32, C.POINTER(C.c_float),
+                                              vp], i32),
+            "mrt_cuda_denoiser_params": ([vp, vp, i32, vp, sz, i32], i32),
             "mrt_cuda_batch_create": ([vp, u32, vp, vp, vp, vp, vp, pp], i32),
             "mrt_cuda_batch_destroy": ([vp, vp], i32),
             "mrt_cuda_batch_trace": ([vp, vp, vp, vp, vp, u32, vp], i32),

@@ -1,0 +1,613 @@
+// Learned denoiser: a 3-level encoder-decoder CNN (U-Net) over the 1-spp
+// radiance and its feature buffers (albedo, normal, depth), trained on
+// pairs the path tracer renders itself.  The reference's denoiser is a
+// hand-set joint bilateral filter (src/gpu/denoise/bilateral.comp); this
+// learned one is new.
+//
+// Tensors are NHWC BF16 with channel counts padded to multiples of 16.
+// Topology (C = channels, s = 1/scale):
+//   in(16) -> e0a(32) -> e0b(32)=S0 -> pool -> e1a(64) -> e1b(64)=S1 -> pool
+//   -> e2a(128) -> e2b(128) -> [up ++ S1](192) -> d1a(64) -> d1b(64)
+//   -> [up ++ S0](96) -> d0a(32) -> d0b(32) -> out(16, 3 used)
+// 3x3 convolutions with bias, ReLU except the output layer.  The network
+// predicts log(1 + radiance); the loss is L1 in that space.
+//
+// Forward: implicit-GEMM convolution on the tensor cores (mma.sync
+// m16n8k16, BF16 in, FP32 accumulate): a warp computes 16 consecutive
+// pixels of a row x all output channels; the 2x upsampling and the skip
+// concatenation of the decoder are folded into the operand loads.
+// Backward: FP32 kernels on the CUDA cores for the data, weight and bias
+// gradients, reading the stored BF16 activations.
+#include "internal.hpp"
+
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+namespace mrt {
+int set_error(mrt_ctx* ctx, int code, const char* msg);
+}
+using namespace mrt;
+
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+struct ConvDesc {
+    int ca, cb, cout;   // input channels from source A, from source B (skip), outputs
+    int ups;            // source A is half resolution, nearest-upsampled
+    int relu;
+    int scale;          // resolution level of the output (0 full, 1 half, 2 quarter)
+    size_t w_off, b_off;
+};
+
+constexpr int kLayers = 11;
+// ca, cb, cout, ups, relu, scale
+const int kTopo[kLayers][6] = {
+    {16, 0, 32, 0, 1, 0},   // e0a
+    {32, 0, 32, 0, 1, 0},   // e0b -> S0
+    {32, 0, 64, 0, 1, 1},   // e1a (input pooled S0)
+    {64, 0, 64, 0, 1, 1},   // e1b -> S1
+    {64, 0, 128, 0, 1, 2},  // e2a (input pooled S1)
+    {128, 0, 128, 0, 1, 2}, // e2b
+    {128, 64, 64, 1, 1, 1}, // d1a: up(e2b) ++ S1
+    {64, 0, 64, 0, 1, 1},   // d1b
+    {64, 32, 32, 1, 1, 0},  // d0a: up(d1b) ++ S0
+    {32, 0, 32, 0, 1, 0},   // d0b
+    {32, 0, 16, 0, 0, 0},   // out (3 channels used)
+};
+
+__device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+struct ConvArgs {
+    const bf16* a;   // source A: N x Ha x Wa x ca
+    const bf16* b;   // source B: N x H x W x cb (or null)
+    const bf16* w;   // cout x 9 x (ca + cb)
+    const float* bias;
+    bf16* y;         // N x H x W x cout
+    int n, h, w_, ca, cb, cout, ups, relu;
+};
+
+// channel pair (c, c+1) of the virtual concatenated input at (n, y, x)
+__device__ __forceinline__ uint32_t in_pair(const ConvArgs& a, int n, int y, int x, int c) {
+    if (y < 0 || y >= a.h || x < 0 || x >= a.w_) return 0u;
+    if (c < a.ca) {
+        const int ha = a.ups ? a.h >> 1 : a.h, wa = a.ups ? a.w_ >> 1 : a.w_;
+        const int ya = a.ups ? y >> 1 : y, xa = a.ups ? x >> 1 : x;
+        return *reinterpret_cast<const uint32_t*>(a.a + ((size_t(n) * ha + ya) * wa + xa) * a.ca + c);
+    }
+    return *reinterpret_cast<const uint32_t*>(a.b + ((size_t(n) * a.h + y) * a.w_ + x) * a.cb + (c - a.ca));
+}
+
+// One warp: 16 pixels (x0 .. x0+15) of row y of image n, all 8*NT outputs.
+template <int NT>
+__global__ void __launch_bounds__(128) k_conv_fwd(ConvArgs a) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
+    const int tiles_x = (a.w_ + 63) / 64;
+    int bid = blockIdx.x;
+    const int tx = bid % tiles_x;
+    bid /= tiles_x;
+    const int y = bid % a.h, n = bid / a.h;
+    const int x0 = tx * 64 + warp * 16;
+    if (x0 >= a.w_) return;
+    const int cin = a.ca + a.cb;
+    float acc[NT][4];
+#pragma unroll
+    for (int j = 0; j < NT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+    for (int tap = 0; tap < 9; ++tap) {
+        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+        for (int kc = 0; kc < cin; kc += 16) {
+            uint32_t af[4];
+            af[0] = in_pair(a, n, y + dy, x0 + g + dx, kc + 2 * t);
+            af[1] = in_pair(a, n, y + dy, x0 + g + 8 + dx, kc + 2 * t);
+            af[2] = in_pair(a, n, y + dy, x0 + g + dx, kc + 8 + 2 * t);
+            af[3] = in_pair(a, n, y + dy, x0 + g + 8 + dx, kc + 8 + 2 * t);
+#pragma unroll
+            for (int j = 0; j < NT; ++j) {
+                const bf16* wr = a.w + (size_t(8 * j + g) * 9 + tap) * cin + kc + 2 * t;
+                mma_bf16(acc[j], af, __ldg(reinterpret_cast<const unsigned int*>(wr)),
+                         __ldg(reinterpret_cast<const unsigned int*>(wr + 8)));
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NT; ++j) {
+        const int c = 8 * j + 2 * t;
+        const float b0 = a.bias[c], b1 = a.bias[c + 1];
+        float v[4] = {acc[j][0] + b0, acc[j][1] + b1, acc[j][2] + b0, acc[j][3] + b1};
+        if (a.relu)
+            for (int k = 0; k < 4; ++k) v[k] = fmaxf(v[k], 0.0f);
+        const int xr0 = x0 + g, xr1 = x0 + g + 8;
+        if (xr0 < a.w_)
+            *reinterpret_cast<__nv_bfloat162*>(a.y + ((size_t(n) * a.h + y) * a.w_ + xr0) * a.cout + c) =
+                __floats2bfloat162_rn(v[0], v[1]);
+        if (xr1 < a.w_)
+            *reinterpret_cast<__nv_bfloat162*>(a.y + ((size_t(n) * a.h + y) * a.w_ + xr1) * a.cout + c) =
+                __floats2bfloat162_rn(v[2], v[3]);
+    }
+}
+
+// 2x2 average pool, NHWC
+__global__ void k_pool(const bf16* x, bf16* y, int n, int h, int w, int c) {
+    const size_t total = size_t(n) * (h / 2) * (w / 2) * c;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+        const int ch = int(i % c);
+        size_t p = i / c;
+        const int xo = int(p % (w / 2));
+        p /= (w / 2);
+        const int yo = int(p % (h / 2));
+        const int nn = int(p / (h / 2));
+        float s = 0.0f;
+        for (int k = 0; k < 4; ++k)
+            s += __bfloat162float(x[((size_t(nn) * h + 2 * yo + (k >> 1)) * w + 2 * xo + (k & 1)) * c + ch]);
+        y[i] = __float2bfloat16_rn(0.25f * s);
+    }
+}
+
+// ---- backward (FP32) ----------------------------------------------------
+
+// dz = dy * relu'(y) in place (y: stored bf16 output)
+__global__ void k_relu_bwd(float* dy, const bf16* y, size_t count) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < count; i += size_t(gridDim.x) * blockDim.x)
+        if (!(__bfloat162float(y[i]) > 0.0f)) dy[i] = 0.0f;
+}
+
+// data gradient: for each input element of the virtual concatenated input
+// at output resolution, sum over taps and outputs; written (accumulated) to
+// the source gradient buffers (upsampled source: atomics into its parent)
+__global__ void k_conv_bwd_data(const float* dz, const bf16* w, int n, int h, int wd, int ca, int cb, int cout, int ups,
+                                float* ga, float* gb) {
+    const int cin = ca + cb;
+    const size_t total = size_t(n) * h * wd * cin;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+        const int ci = int(i % cin);
+        size_t p = i / cin;
+        const int x = int(p % wd);
+        p /= wd;
+        const int y = int(p % h);
+        const int nn = int(p / h);
+        float s = 0.0f;
+        for (int tap = 0; tap < 9; ++tap) {
+            const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+            const int yo = y - dy, xo = x - dx;  // output pixel that read (y, x) through this tap
+            if (yo < 0 || yo >= h || xo < 0 || xo >= wd) continue;
+            const float* dzr = dz + ((size_t(nn) * h + yo) * wd + xo) * cout;
+            const bf16* wr = w + size_t(tap) * cin + ci;
+            for (int co = 0; co < cout; ++co) s = fmaf(dzr[co], __bfloat162float(wr[size_t(co) * 9 * cin]), s);
+        }
+        if (ci < ca) {
+            if (ups) atomicAdd(&ga[((size_t(nn) * (h / 2) + y / 2) * (wd / 2) + x / 2) * ca + ci], s);
+            else ga[((size_t(nn) * h + y) * wd + x) * ca + ci] += s;
+        } else {
+            gb[((size_t(nn) * h + y) * wd + x) * cb + (ci - ca)] += s;
+        }
+    }
+}
+
+// weight + bias gradients: block (co-tile of 16, ci-tile of 16, tap) over a
+// slice of pixels, partial sums atomically added
+__global__ void __launch_bounds__(256)
+k_conv_bwd_weight(const float* dz, const bf16* xa, const bf16* xb, int n, int h, int wd, int ca, int cb, int cout,
+                  int ups, int pix_per_block, float* gw, float* gbias) {
+    const int cin = ca + cb;
+    const int co_tiles = (cout + 15) / 16, ci_tiles = cin / 16;
+    int bid = blockIdx.x;
+    const int tap = bid % 9;
+    bid /= 9;
+    const int cit = bid % ci_tiles;
+    bid /= ci_tiles;
+    const int cot = bid % co_tiles;
+    const int slice = bid / co_tiles;
+    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+    const int co = cot * 16 + (threadIdx.x >> 4), ci = cit * 16 + (threadIdx.x & 15);
+    const size_t total = size_t(n) * h * wd;
+    const size_t p0 = size_t(slice) * pix_per_block, p1 = std::min(total, p0 + size_t(pix_per_block));
+    float s = 0.0f, sb = 0.0f;
+    const int ha = ups ? h / 2 : h, wa = ups ? wd / 2 : wd;
+    for (size_t p = p0; p < p1; ++p) {
+        const int x = int(p % wd);
+        const int y = int((p / wd) % h);
+        const int nn = int(p / (size_t(wd) * h));
+        const float d = co < cout ? dz[p * cout + co] : 0.0f;
+        sb += d;
+        const int yi = y + dy, xi = x + dx;
+        if (yi < 0 || yi >= h || xi < 0 || xi >= wd) continue;
+        float xv;
+        if (ci < ca) {
+            const int yy = ups ? yi >> 1 : yi, xx = ups ? xi >> 1 : xi;
+            xv = __bfloat162float(xa[((size_t(nn) * ha + yy) * wa + xx) * ca + ci]);
+        } else {
+            xv = __bfloat162float(xb[((size_t(nn) * h + yi) * wd + xi) * cb + (ci - ca)]);
+        }
+        s = fmaf(d, xv, s);
+    }
+    if (co < cout) {
+        atomicAdd(&gw[(size_t(co) * 9 + tap) * cin + ci], s);
+        if (tap == 4 && cit == 0 && (threadIdx.x & 15) == 0) atomicAdd(&gbias[co], sb);
+    }
+}
+
+// pool backward: g_in[2y+i][2x+j] += g_out[y][x] / 4
+__global__ void k_pool_bwd(const float* gout, float* gin, int n, int h, int w, int c) {
+    const size_t total = size_t(n) * h * w * c;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+        const int ch = int(i % c);
+        size_t p = i / c;
+        const int x = int(p % w);
+        p /= w;
+        const int y = int(p % h);
+        const int nn = int(p / h);
+        gin[i] += 0.25f * gout[((size_t(nn) * (h / 2) + y / 2) * (w / 2) + x / 2) * c + ch];
+    }
+}
+
+// L1 loss in log(1 + radiance) space on channels 0..2 of the output
+__global__ void k_l1_loss(const bf16* y, const float* target, size_t pixels, float* dy, float* loss) {
+    float l = 0.0f;
+    const float inv = 1.0f / float(pixels * 3);
+    for (size_t p = blockIdx.x * size_t(blockDim.x) + threadIdx.x; p < pixels; p += size_t(gridDim.x) * blockDim.x) {
+        for (int k = 0; k < 16; ++k) dy[p * 16 + k] = 0.0f;
+        for (int k = 0; k < 3; ++k) {
+            const float d = __bfloat162float(y[p * 16 + k]) - log1pf(fmaxf(target[p * 3 + k], 0.0f));
+            l += fabsf(d);
+            dy[p * 16 + k] = (d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f)) * inv;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xFFFFFFFFu, l, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, l * inv);
+}
+
+__global__ void k_adam_bf16(float* p, float* m, float* v, float* g, bf16* p16, size_t n, float lr, float b1, float b2,
+                            float eps, float bc1, float bc2) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+        const float gr = g[i];
+        g[i] = 0.0f;
+        const float mi = b1 * m[i] + (1.0f - b1) * gr, vi = b2 * v[i] + (1.0f - b2) * gr * gr;
+        m[i] = mi;
+        v[i] = vi;
+        const float pi = p[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+        p[i] = pi;
+        if (p16) p16[i] = __float2bfloat16_rn(pi);
+    }
+}
+
+// Input features of one frame: log(1 + radiance) (3), albedo (3), facing
+// normal (3), hit distance / scene diagonal (1), zeros to 16 channels.
+__global__ void k_features(DevScene sc, const float* color, const uint32_t* vis, const float* hit_t, int w, int h,
+                           float inv_diag, bf16* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w * h) return;
+    float f[16];
+    for (int k = 0; k < 16; ++k) f[k] = 0.0f;
+    for (int k = 0; k < 3; ++k) f[k] = log1pf(fmaxf(color[size_t(i) * 3 + k], 0.0f));
+    const uint32_t prim = vis[i];
+    if (prim != kMiss && prim < sc.mat_count) {
+        const mrt_material m = sc.mats[prim];
+        f[3] = float(m.albedo_rgba8 & 0xFFu) / 255.0f;
+        f[4] = float((m.albedo_rgba8 >> 8) & 0xFFu) / 255.0f;
+        f[5] = float((m.albedo_rgba8 >> 16) & 0xFFu) / 255.0f;
+        f[6] = m.normal[0]; f[7] = m.normal[1]; f[8] = m.normal[2];
+        f[9] = fminf(hit_t[i] * inv_diag, 4.0f);
+    } else {
+        f[9] = 4.0f;
+    }
+    for (int k = 0; k < 16; k += 2)
+        *reinterpret_cast<__nv_bfloat162*>(out + size_t(i) * 16 + k) = __floats2bfloat162_rn(f[k], f[k + 1]);
+}
+
+__global__ void k_decode(const bf16* y, size_t pixels, float* out) {
+    for (size_t p = blockIdx.x * size_t(blockDim.x) + threadIdx.x; p < pixels; p += size_t(gridDim.x) * blockDim.x)
+        for (int k = 0; k < 3; ++k) out[p * 3 + k] = expm1f(fmaxf(__bfloat162float(y[p * 16 + k]), 0.0f));
+}
+
+int grid_for(size_t n) { return int(std::min<size_t>((n + 255) / 256, 65535)); }
+
+} // namespace
+
+struct mrt_denoiser {
+    ConvDesc layers[kLayers];
+    size_t n_w = 0, n_b = 0;
+    float *w = nullptr, *wm = nullptr, *wv = nullptr, *wg = nullptr;  // weights + biases, FP32
+    bf16* w16 = nullptr;
+    // activation tensors (bf16) and their gradients (fp32), sized for n*h*w
+    size_t cap_pix = 0, grad_pix = 0;
+    bf16* act[kLayers] = {};
+    bf16 *pool0 = nullptr, *pool1 = nullptr;
+    float* grad[kLayers] = {};
+    float *gpool0 = nullptr, *gpool1 = nullptr, *gin = nullptr;
+    float* loss = nullptr;
+    float* h_loss = nullptr;
+    uint32_t step = 0;
+};
+
+namespace {
+
+size_t layer_pixels(size_t full, int scale) { return full >> (2 * scale); }
+
+// activations for n*h*w pixels; gradient buffers only when training
+int ensure_acts(mrt_ctx* ctx, mrt_denoiser* d, size_t pix, bool grads) {
+    if (d->cap_pix < pix) {
+        for (int l = 0; l < kLayers; ++l) { cudaFree(d->act[l]); d->act[l] = nullptr; }
+        cudaFree(d->pool0); cudaFree(d->pool1);
+        d->pool0 = d->pool1 = nullptr;
+        d->cap_pix = 0;
+        bool ok = true;
+        for (int l = 0; l < kLayers && ok; ++l)
+            ok = cudaMalloc(&d->act[l], layer_pixels(pix, d->layers[l].scale) * d->layers[l].cout * 2) == cudaSuccess;
+        ok = ok && cudaMalloc(&d->pool0, layer_pixels(pix, 1) * 32 * 2) == cudaSuccess &&
+             cudaMalloc(&d->pool1, layer_pixels(pix, 2) * 64 * 2) == cudaSuccess;
+        if (!ok) {
+            cudaGetLastError();
+            return set_error(ctx, MRT_ENOMEM, "denoiser: activation buffers");
+        }
+        d->cap_pix = pix;
+    }
+    if (grads && d->grad_pix < pix) {
+        for (int l = 0; l < kLayers; ++l) { cudaFree(d->grad[l]); d->grad[l] = nullptr; }
+        cudaFree(d->gpool0); cudaFree(d->gpool1); cudaFree(d->gin);
+        d->gpool0 = d->gpool1 = d->gin = nullptr;
+        d->grad_pix = 0;
+        bool ok = true;
+        for (int l = 0; l < kLayers && ok; ++l)
+            ok = cudaMalloc(&d->grad[l], layer_pixels(pix, d->layers[l].scale) * d->layers[l].cout * 4) == cudaSuccess;
+        ok = ok && cudaMalloc(&d->gpool0, layer_pixels(pix, 1) * 32 * 4) == cudaSuccess &&
+             cudaMalloc(&d->gpool1, layer_pixels(pix, 2) * 64 * 4) == cudaSuccess &&
+             cudaMalloc(&d->gin, pix * 16 * 4) == cudaSuccess;
+        if (!ok) {
+            cudaGetLastError();
+            return set_error(ctx, MRT_ENOMEM, "denoiser: gradient buffers");
+        }
+        d->grad_pix = pix;
+    }
+    return MRT_OK;
+}
+
+cudaError_t conv(const mrt_denoiser* d, int l, const bf16* a, const bf16* b, int n, int h, int w, cudaStream_t s) {
+    const ConvDesc& L = d->layers[l];
+    ConvArgs ca{a, b, d->w16 + L.w_off, d->w + L.b_off, d->act[l], n, h, w, L.ca, L.cb, L.cout, L.ups, L.relu};
+    const int blocks = ((w + 63) / 64) * h * n;
+    switch (L.cout) {
+    case 16: k_conv_fwd<2><<<blocks, 128, 0, s>>>(ca); break;
+    case 32: k_conv_fwd<4><<<blocks, 128, 0, s>>>(ca); break;
+    case 64: k_conv_fwd<8><<<blocks, 128, 0, s>>>(ca); break;
+    default: k_conv_fwd<16><<<blocks, 128, 0, s>>>(ca); break;
+    }
+    return cudaGetLastError();
+}
+
+// forward of the whole network over n images of h x w (h, w multiples of 4)
+cudaError_t forward(const mrt_denoiser* d, const bf16* in, int n, int h, int w, cudaStream_t s) {
+    cudaError_t e;
+    if ((e = conv(d, 0, in, nullptr, n, h, w, s))) return e;
+    if ((e = conv(d, 1, d->act[0], nullptr, n, h, w, s))) return e;
+    k_pool<<<grid_for(size_t(n) * h * w * 32 / 4), 256, 0, s>>>(d->act[1], d->pool0, n, h, w, 32);
+    if ((e = conv(d, 2, d->pool0, nullptr, n, h / 2, w / 2, s))) return e;
+    if ((e = conv(d, 3, d->act[2], nullptr, n, h / 2, w / 2, s))) return e;
+    k_pool<<<grid_for(size_t(n) * h * w * 64 / 16), 256, 0, s>>>(d->act[3], d->pool1, n, h / 2, w / 2, 64);
+    if ((e = conv(d, 4, d->pool1, nullptr, n, h / 4, w / 4, s))) return e;
+    if ((e = conv(d, 5, d->act[4], nullptr, n, h / 4, w / 4, s))) return e;
+    if ((e = conv(d, 6, d->act[5], d->act[3], n, h / 2, w / 2, s))) return e;
+    if ((e = conv(d, 7, d->act[6], nullptr, n, h / 2, w / 2, s))) return e;
+    if ((e = conv(d, 8, d->act[7], d->act[1], n, h, w, s))) return e;
+    if ((e = conv(d, 9, d->act[8], nullptr, n, h, w, s))) return e;
+    return conv(d, 10, d->act[9], nullptr, n, h, w, s);
+}
+
+// backward of layer l: grad[l] holds dL/d(output); accumulates into the
+// gradient buffers of its sources and into the weight/bias gradients
+void bwd_layer(mrt_denoiser* d, int l, const bf16* xa, const bf16* xb, float* ga, float* gb, int n, int h, int w,
+               cudaStream_t s) {
+    const ConvDesc& L = d->layers[l];
+    const size_t pix = size_t(n) * h * w;
+    if (L.relu) k_relu_bwd<<<grid_for(pix * L.cout), 256, 0, s>>>(d->grad[l], d->act[l], pix * L.cout);
+    const int ppb = 1024;
+    const int slices = int((pix + ppb - 1) / ppb);
+    const int blocks = slices * ((L.cout + 15) / 16) * ((L.ca + L.cb) / 16) * 9;
+    k_conv_bwd_weight<<<blocks, 256, 0, s>>>(d->grad[l], xa, xb, n, h, w, L.ca, L.cb, L.cout, L.ups, ppb,
+                                             d->wg + L.w_off, d->wg + L.b_off);
+    if (ga)
+        k_conv_bwd_data<<<grid_for(pix * (L.ca + L.cb)), 256, 0, s>>>(d->grad[l], d->w16 + L.w_off, n, h, w, L.ca,
+                                                                      L.cb, L.cout, L.ups, ga, gb);
+}
+
+} // namespace
+
+extern "C" {
+
+int mrt_cuda_denoiser_create(mrt_ctx* ctx, uint32_t seed, mrt_denoiser** out) {
+    if (!ctx || !out) return set_error(ctx, MRT_EINVAL, "denoiser_create: null argument");
+    cudaSetDevice(ctx->device);
+    mrt_denoiser* d = new (std::nothrow) mrt_denoiser;
+    if (!d) return MRT_ENOMEM;
+    size_t wo = 0;
+    for (int l = 0; l < kLayers; ++l) {
+        ConvDesc& L = d->layers[l];
+        L.ca = kTopo[l][0]; L.cb = kTopo[l][1]; L.cout = kTopo[l][2];
+        L.ups = kTopo[l][3]; L.relu = kTopo[l][4]; L.scale = kTopo[l][5];
+        L.w_off = wo;
+        wo += size_t(L.cout) * 9 * (L.ca + L.cb);
+    }
+    d->n_w = wo;
+    for (int l = 0; l < kLayers; ++l) {
+        d->layers[l].b_off = wo;
+        wo += d->layers[l].cout;
+    }
+    d->n_b = wo - d->n_w;
+    const size_t total = wo;
+    bool ok = cudaMalloc(&d->w, total * 4) == cudaSuccess && cudaMalloc(&d->wm, total * 4) == cudaSuccess &&
+              cudaMalloc(&d->wv, total * 4) == cudaSuccess && cudaMalloc(&d->wg, total * 4) == cudaSuccess &&
+              cudaMalloc(&d->w16, d->n_w * 2) == cudaSuccess && cudaMalloc(&d->loss, 4) == cudaSuccess &&
+              cudaMallocHost(&d->h_loss, 4) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        delete d;
+        return set_error(ctx, MRT_ENOMEM, "denoiser_create: out of memory");
+    }
+    // He-uniform initialisation over the fan-in (9 x inputs), zero biases;
+    // the output layer's unused channels stay zero
+    std::vector<float> w(total, 0.0f);
+    uint64_t st = 0xD3A0ull + seed;
+    auto next = [&]() {
+        uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return double((z ^ (z >> 31)) >> 11) * (1.0 / 9007199254740992.0);
+    };
+    for (int l = 0; l < kLayers; ++l) {
+        const ConvDesc& L = d->layers[l];
+        const int cin = L.ca + L.cb;
+        const int real_in = l == 0 ? 10 : cin;
+        const float a = std::sqrt(6.0f / float(9 * real_in)) * (l == kLayers - 1 ? 0.5f : 1.0f);
+        for (int co = 0; co < L.cout; ++co)
+            for (int tap = 0; tap < 9; ++tap)
+                for (int ci = 0; ci < cin; ++ci) {
+                    const bool used = (l != kLayers - 1 || co < 3) && (l != 0 || ci < 10);
+                    w[L.w_off + (size_t(co) * 9 + tap) * cin + ci] = used ? float((2.0 * next() - 1.0) * a) : 0.0f;
+                }
+    }
+    std::vector<bf16> w16(d->n_w);
+    for (size_t i = 0; i < d->n_w; ++i) w16[i] = __float2bfloat16_rn(w[i]);
+    ok = cudaMemcpy(d->w, w.data(), total * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(d->w16, w16.data(), d->n_w * 2, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemset(d->wm, 0, total * 4) == cudaSuccess && cudaMemset(d->wv, 0, total * 4) == cudaSuccess &&
+         cudaMemset(d->wg, 0, total * 4) == cudaSuccess;
+    if (!ok) {
+        mrt_cuda_denoiser_destroy(ctx, d);
+        return set_error(ctx, MRT_ECUDA, "denoiser_create: upload failed");
+    }
+    *out = d;
+    return MRT_OK;
+}
+
+int mrt_cuda_denoiser_destroy(mrt_ctx* ctx, mrt_denoiser* d) {
+    if (!ctx || !d) return MRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    for (int l = 0; l < kLayers; ++l) { cudaFree(d->act[l]); cudaFree(d->grad[l]); }
+    void* ps[] = {d->w, d->wm, d->wv, d->wg, d->w16, d->pool0, d->pool1, d->gpool0, d->gpool1, d->gin, d->loss};
+    for (void* p : ps) cudaFree(p);
+    if (d->h_loss) cudaFreeHost(d->h_loss);
+    delete d;
+    return MRT_OK;
+}
+
+int mrt_cuda_denoiser_param_count(mrt_denoiser* d, size_t* weights, size_t* biases) {
+    if (!d || !weights || !biases) return MRT_EINVAL;
+    *weights = d->n_w;
+    *biases = d->n_b;
+    return MRT_OK;
+}
+
+int mrt_cuda_denoiser_features(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuffer* gbuffer, const float* color,
+                               float scene_diagonal, uint16_t* features, void* stream) {
+    if (!ctx || !scene || !gbuffer || !color || !features || !gbuffer->hit_t || scene->kind != 0)
+        return set_error(ctx, MRT_EINVAL, "denoiser_features: bad arguments");
+    cudaSetDevice(ctx->device);
+    const int n = int(gbuffer->width * gbuffer->height);
+    k_features<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        scene->dev, color, gbuffer->visibility, gbuffer->hit_t, int(gbuffer->width), int(gbuffer->height),
+        scene_diagonal > 0.0f ? 1.0f / scene_diagonal : 1.0f, reinterpret_cast<bf16*>(features));
+    if (cudaGetLastError() != cudaSuccess) return set_error(ctx, MRT_ECUDA, "denoiser_features: launch");
+    ctx->launches++;
+    return MRT_OK;
+}
+
+int mrt_cuda_denoiser_infer(mrt_ctx* ctx, mrt_denoiser* d, const uint16_t* features, uint32_t batch, uint32_t width,
+                            uint32_t height, float* out, void* stream) {
+    if (!ctx || !d || !features || !out || batch == 0) return set_error(ctx, MRT_EINVAL, "denoiser_infer: bad arguments");
+    if (width % 4 || height % 4) return set_error(ctx, MRT_EINVAL, "denoiser_infer: width and height must be multiples of 4");
+    cudaSetDevice(ctx->device);
+    const size_t pix = size_t(batch) * width * height;
+    int rc = ensure_acts(ctx, d, pix, false);
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (forward(d, reinterpret_cast<const bf16*>(features), int(batch), int(height), int(width), s) != cudaSuccess)
+        return set_error(ctx, MRT_ECUDA, "denoiser_infer: launch");
+    k_decode<<<grid_for(pix), 256, 0, s>>>(d->act[kLayers - 1], pix, out);
+    ctx->launches += 14;
+    return MRT_OK;
+}
+
+int mrt_cuda_denoiser_train_step(mrt_ctx* ctx, mrt_denoiser* d, const uint16_t* features, const float* targets,
+                                 uint32_t batch, uint32_t width, uint32_t height, float lr, int apply_update,
+                                 float* loss_out, void* stream) {
+    if (!ctx || !d || !features || !targets || batch == 0) return set_error(ctx, MRT_EINVAL, "denoiser_train: bad arguments");
+    if (width % 4 || height % 4) return set_error(ctx, MRT_EINVAL, "denoiser_train: width and height must be multiples of 4");
+    cudaSetDevice(ctx->device);
+    const int n = int(batch), h = int(height), w = int(width);
+    const size_t pix = size_t(n) * h * w;
+    int rc = ensure_acts(ctx, d, pix, true);
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const bf16* in = reinterpret_cast<const bf16*>(features);
+    if (forward(d, in, n, h, w, s) != cudaSuccess) return set_error(ctx, MRT_ECUDA, "denoiser_train: forward");
+    cudaMemsetAsync(d->loss, 0, 4, s);
+    k_l1_loss<<<grid_for(pix), 256, 0, s>>>(d->act[kLayers - 1], targets, pix, d->grad[kLayers - 1], d->loss);
+    // zero the gradient buffers that accumulate from several consumers
+    for (int l = 0; l < kLayers - 1; ++l)
+        cudaMemsetAsync(d->grad[l], 0, layer_pixels(pix, d->layers[l].scale) * d->layers[l].cout * 4, s);
+    cudaMemsetAsync(d->gpool0, 0, layer_pixels(pix, 1) * 32 * 4, s);
+    cudaMemsetAsync(d->gpool1, 0, layer_pixels(pix, 2) * 64 * 4, s);
+    cudaMemsetAsync(d->gin, 0, pix * 16 * 4, s);
+    bwd_layer(d, 10, d->act[9], nullptr, d->grad[9], nullptr, n, h, w, s);
+    bwd_layer(d, 9, d->act[8], nullptr, d->grad[8], nullptr, n, h, w, s);
+    bwd_layer(d, 8, d->act[7], d->act[1], d->grad[7], d->grad[1], n, h, w, s);
+    bwd_layer(d, 7, d->act[6], nullptr, d->grad[6], nullptr, n, h / 2, w / 2, s);
+    bwd_layer(d, 6, d->act[5], d->act[3], d->grad[5], d->grad[3], n, h / 2, w / 2, s);
+    bwd_layer(d, 5, d->act[4], nullptr, d->grad[4], nullptr, n, h / 4, w / 4, s);
+    bwd_layer(d, 4, d->pool1, nullptr, d->gpool1, nullptr, n, h / 4, w / 4, s);
+    k_pool_bwd<<<grid_for(pix / 4 * 64), 256, 0, s>>>(d->gpool1, d->grad[3], n, h / 2, w / 2, 64);
+    bwd_layer(d, 3, d->act[2], nullptr, d->grad[2], nullptr, n, h / 2, w / 2, s);
+    bwd_layer(d, 2, d->pool0, nullptr, d->gpool0, nullptr, n, h / 2, w / 2, s);
+    k_pool_bwd<<<grid_for(pix * 32), 256, 0, s>>>(d->gpool0, d->grad[1], n, h, w, 32);
+    bwd_layer(d, 1, d->act[0], nullptr, d->grad[0], nullptr, n, h, w, s);
+    bwd_layer(d, 0, in, nullptr, nullptr, nullptr, n, h, w, s);
+    ctx->launches += 40;
+    if (apply_update) {
+        d->step++;
+        const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+        const float bc1 = 1.0f - std::pow(b1, float(d->step)), bc2 = 1.0f - std::pow(b2, float(d->step));
+        k_adam_bf16<<<grid_for(d->n_w), 256, 0, s>>>(d->w, d->wm, d->wv, d->wg, d->w16, d->n_w, lr, b1, b2, eps, bc1,
+                                                     bc2);
+        k_adam_bf16<<<grid_for(d->n_b), 256, 0, s>>>(d->w + d->n_w, d->wm + d->n_w, d->wv + d->n_w, d->wg + d->n_w,
+                                                     nullptr, d->n_b, lr, b1, b2, eps, bc1, bc2);
+    }
+    if (cudaGetLastError() != cudaSuccess) return set_error(ctx, MRT_ECUDA, "denoiser_train: launch");
+    if (loss_out) {
+        if (cudaMemcpyAsync(d->h_loss, d->loss, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return set_error(ctx, MRT_ECUDA, "denoiser_train: loss read-back");
+        *loss_out = *d->h_loss;
+    }
+    return MRT_OK;
+}
+
+// which = 0: weights then biases (FP32 masters), 1: their gradients;
+// set != 0 copies host -> device (and refreshes the BF16 weights)
+int mrt_cuda_denoiser_params(mrt_ctx* ctx, mrt_denoiser* d, int which, float* host, size_t count, int set) {
+    if (!ctx || !d || !host || which < 0 || which > 1 || count != d->n_w + d->n_b)
+        return set_error(ctx, MRT_EINVAL, "denoiser_params: bad arguments");
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    float* p = which == 0 ? d->w : d->wg;
+    if (!set) return cudaMemcpy(host, p, count * 4, cudaMemcpyDeviceToHost) == cudaSuccess ? MRT_OK : MRT_ECUDA;
+    if (cudaMemcpy(p, host, count * 4, cudaMemcpyHostToDevice) != cudaSuccess) return MRT_ECUDA;
+    if (which == 0) {
+        std::vector<bf16> w16(d->n_w);
+        for (size_t i = 0; i < d->n_w; ++i) w16[i] = __float2bfloat16_rn(host[i]);
+        cudaMemcpy(d->w16, w16.data(), d->n_w * 2, cudaMemcpyHostToDevice);
+    }
+    return MRT_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,96 @@
+"""The CNN denoiser on the GPU: forward (BF16 tensor-core convolutions) and
+gradients against the FP64 oracle (oracle/cnn.py, checked against finite
+differences), training convergence, and features from a rendered frame."""
+import numpy as np
+import pytest
+
+from oracle import cnn
+from minotert_gb300.denoiser import Denoiser, from_bf16_bits, to_bf16_bits
+
+pytestmark = pytest.mark.gpu
+
+
+def _inputs(n, h, w, seed):
+    rng = np.random.default_rng(seed)
+    x = np.zeros((n, h, w, 16), np.float32)
+    x[..., :10] = rng.uniform(0, 1, (n, h, w, 10))
+    t = rng.uniform(0, 2, (n, h, w, 3)).astype(np.float32)
+    return x, t
+
+
+def test_denoiser_forward_matches_oracle(ctx):
+    d = Denoiser(ctx, seed=2)
+    x, _ = _inputs(2, 16, 24, 1)
+    xb = to_bf16_bits(x)
+    d_x = ctx.to_device(xb)
+    d_o = ctx.alloc(2 * 16 * 24 * 3 * 4)
+    d.infer(d_x, 2, 24, 16, d_o)
+    y = d_o.download(np.float32, (2, 16, 24, 3))
+    params = d.params(0).astype(np.float64)
+    _, _, out = cnn.forward(params, from_bf16_bits(xb).astype(np.float64).reshape(2, 16, 24, 16))
+    ref = np.expm1(np.maximum(out[..., :3], 0.0))
+    assert np.all(np.isfinite(y))
+    err = np.abs(y - ref)
+    assert np.max(err) < 3e-2 * max(1.0, np.abs(ref).max()), np.max(err)
+    assert np.mean(err) < 3e-3 * max(1.0, np.abs(ref).mean())
+
+
+def test_denoiser_gradients_match_oracle(ctx):
+    d = Denoiser(ctx, seed=3)
+    x, t = _inputs(2, 16, 16, 4)
+    xb = to_bf16_bits(x)
+    d_x, d_t = ctx.to_device(xb), ctx.to_device(t)
+    loss = d.train_step(d_x, d_t, 2, 16, 16, update=False, want_loss=True)
+    g = d.params(1).astype(np.float64)
+    params = d.params(0).astype(np.float64)
+    rloss, rg, _ = cnn.loss_and_grads(params, from_bf16_bits(xb).astype(np.float64).reshape(2, 16, 16, 16),
+                                      t.astype(np.float64))
+    assert abs(loss - rloss) < 2e-2 * rloss
+    cos = g @ rg / (np.linalg.norm(g) * np.linalg.norm(rg))
+    assert cos > 0.995, cos
+    assert abs(np.linalg.norm(g) / np.linalg.norm(rg) - 1) < 0.05
+
+
+def test_denoiser_training_reduces_loss(ctx):
+    # learn to remove additive noise from a smooth colour field guided by
+    # clean albedo features
+    rng = np.random.default_rng(5)
+    n, h, w = 4, 32, 32
+    yy, xx = np.mgrid[0:h, 0:w] / 32.0
+    clean = np.stack([0.5 + 0.3 * np.sin(4 * xx), 0.4 + 0.3 * yy, 0.3 + 0.2 * np.cos(3 * yy)], -1)
+    t = np.repeat(clean[None], n, 0).astype(np.float32)
+    x = np.zeros((n, h, w, 16), np.float32)
+    noisy = np.clip(t * rng.gamma(2.0, 0.5, t.shape), 0, None)
+    x[..., :3] = np.log1p(noisy)
+    x[..., 3:6] = clean
+    d = Denoiser(ctx, seed=6)
+    d_x, d_t = ctx.to_device(to_bf16_bits(x)), ctx.to_device(t)
+    first = d.train_step(d_x, d_t, n, w, h, lr=2e-3, want_loss=True)
+    for _ in range(300):
+        d.train_step(d_x, d_t, n, w, h, lr=2e-3)
+    last = d.train_step(d_x, d_t, n, w, h, lr=2e-3, want_loss=True)
+    assert last < first / 4, (first, last)
+
+
+def test_denoiser_features_from_a_frame(ctx, hf_workload, blue_noise):
+    from minotert_gb300.pathtracer import Pathtracer, TraceSettings
+    from minotert_gb300.scene import DeviceScene
+    wl, mesh, bvh = hf_workload
+    ds = DeviceScene.triangles(ctx, mesh, bvh)
+    pt = Pathtracer(ctx, ds, full_gbuffer=False)
+    gb = pt.primaryRays((wl.width, wl.height), wl.camera, wl.camera)
+    col = pt.secondaryRays(gb, wl.camera, wl.sky, blue_noise, wl.settings)
+    d = Denoiser(ctx)
+    feats = ctx.alloc(wl.width * wl.height * 16 * 2)
+    d.features(ds, gb, col, float(np.linalg.norm(mesh.hi - mesh.lo)), feats)
+    f = from_bf16_bits(feats.download(np.uint16, (wl.height, wl.width, 16)))
+    img = col.download(np.float32, (wl.height, wl.width, 3))
+    g = gb.download()
+    hit = g["visibility"] != 0xFFFFFFFF
+    assert np.allclose(f[..., :3], np.log1p(img), atol=2e-2 * np.log1p(img).max())
+    alb = mesh.albedo()[g["visibility"][hit]]
+    assert np.allclose(f[hit][:, 3:6], alb, atol=1e-2)
+    assert np.all(f[..., 10:] == 0)
+    out = ctx.alloc(wl.width * wl.height * 12)
+    d.infer(feats, 1, wl.width, wl.height, out)
+    assert np.isfinite(out.download(np.float32, (wl.height, wl.width, 3))).all()
