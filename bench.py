@@ -542,6 +542,144 @@ def run_cache_experiment(args, world, rank, local, dist):
     print(json.dumps(out))
 
 
+def run_denoise_experiment(args, world, rank, local, dist):
+    """GPU milliseconds to RMSE 0.01 on a held-out 1920x1080 frame: plain
+    accumulation vs the CNN denoiser applied to the accumulated image.  The
+    denoiser is trained first on pairs the path tracer renders itself:
+    seeded heightfield + boxes scenes at random cameras, 128x128 crops,
+    1-spp inputs and 256-spp targets."""
+    from minotert_gb300 import build as _build
+    _build.build()
+    from minotert_gb300 import scene
+    from minotert_gb300._lib import Context
+    from minotert_gb300.denoiser import Denoiser
+    from minotert_gb300.pathtracer import Camera, Pathtracer, Sky, TraceSettings
+
+    ctx = Context(local)
+    stream = ctx.stream()
+    bn = scene.blue_noise(1, 64)
+    ctx.blue_noise(bn)
+    sky = Sky((0.25, 0.32, 0.45), (0.45, -0.35, 0.82), (2.5, 2.5, 2.5))
+    SET = dict(bounces=8, rr_start=2, rng_mode=1)
+    den = Denoiser(ctx, seed=11)
+
+    def camera(rng, w, h):
+        a = rng.uniform(0, 2 * np.pi)
+        r, z = rng.uniform(14, 26), rng.uniform(6, 16)
+        pos = (r * np.cos(a), r * np.sin(a), z)
+        yaw = np.arctan2(-pos[1], -pos[0]) + rng.uniform(-0.3, 0.3)
+        pitch = -np.arctan2(z, r) + rng.uniform(-0.15, 0.15)
+        return Camera((w, h), np.radians(60.0), 0.01, pos, float(yaw), float(pitch))
+
+    def render(pt, cam, w, h, frames, start):
+        col = ctx.alloc(12 * w * h)
+        for f in range(frames):
+            pt.frame_counter = start + f
+            gb = pt.primaryRays((w, h), cam, cam, stream)
+            pt.secondaryRays(gb, cam, sky, bn, TraceSettings(1, SET["bounces"], SET["rr_start"], SET["rng_mode"],
+                                                             True, f), color=col, stream=stream)
+        return col, gb
+
+    # ---- training data
+    t0 = time.perf_counter()
+    S, CW, TSPP = int(os.environ.get("MRT_DENOISE_SCENES", "160")), 128, 256
+    feats = ctx.alloc(S * CW * CW * 16 * 2)
+    targets = ctx.alloc(S * CW * CW * 3 * 4)
+    from minotert_gb300._lib import lib, ptr
+    import ctypes as C
+    for s in range(S):
+        rng = np.random.default_rng(1000 + s)
+        mesh = scene.heightfield_boxes(2000 + s, 64, 32)
+        ds = scene.DeviceScene.triangles(ctx, mesh)
+        pt = Pathtracer(ctx, ds, full_gbuffer=False)
+        cam = camera(rng, CW, CW)
+        noisy, gb = render(pt, cam, CW, CW, 1, 50_000 + s)
+        den.features(ds, gb, noisy, float(np.linalg.norm(mesh.hi - mesh.lo)),
+                     feats.ptr + s * CW * CW * 16 * 2, stream)
+        ref, _ = render(pt, cam, CW, CW, TSPP, 90_000 + s * TSPP)
+        ctx.check(lib().mrt_cuda_copy_d2d(ctx.handle, C.c_void_p(targets.ptr + s * CW * CW * 12),
+                                          C.c_void_p(ref.ptr), CW * CW * 12, C.c_void_p(stream)), "d2d")
+        ctx.sync(stream)
+    data_s = time.perf_counter() - t0
+
+    # ---- training
+    t1 = time.perf_counter()
+    steps, B = int(os.environ.get("MRT_DENOISE_STEPS", "3000")), 8
+    losses = []
+    order = np.random.default_rng(7).permutation(S)
+    ev0, ev1 = ctx.event(), ctx.event()
+    ctx.record(ev0, stream)
+    for k in range(steps):
+        i0 = int(order[(k * B) % (S - B + 1)])
+        lr = 2e-3 if k < steps * 0.7 else 5e-4
+        want = (k % 250 == 0) or k == steps - 1
+        loss = den.train_step(feats.ptr + i0 * CW * CW * 16 * 2, targets.ptr + i0 * CW * CW * 12, B, CW, CW, lr=lr,
+                              want_loss=want, stream=stream)
+        if want:
+            losses.append((k, loss))
+    ctx.record(ev1, stream)
+    ctx.sync(stream)
+    train_ms = ctx.elapsed_ms(ev0, ev1)
+    train_s = time.perf_counter() - t1
+
+    # ---- evaluation on a held-out scene at 1080p
+    W, H = 1920, 1080
+    mesh = scene.heightfield_boxes(99991, 64, 32)
+    ds = scene.DeviceScene.triangles(ctx, mesh)
+    pt = Pathtracer(ctx, ds, full_gbuffer=False)
+    cam = camera(np.random.default_rng(424242), W, H)
+    diag = float(np.linalg.norm(mesh.hi - mesh.lo))
+    ref_col, _ = render(pt, cam, W, H, 4096, 1 << 22)
+    ref = ref_col.download(np.float32, (H, W, 3), stream)
+    col = ctx.alloc(12 * W * H)
+    f_buf = ctx.alloc(W * H * 16 * 2)
+    out = ctx.alloc(12 * W * H)
+    curve_plain, curve_den = [], []
+    cum_ms = 0.0
+    for f in range(64):
+        a, b, c = ctx.event(), ctx.event(), ctx.event()
+        ctx.record(a, stream)
+        pt.frame_counter = f
+        gb = pt.primaryRays((W, H), cam, cam, stream)
+        pt.secondaryRays(gb, cam, sky, bn, TraceSettings(1, SET["bounces"], SET["rr_start"], SET["rng_mode"], True, f),
+                         color=col, stream=stream)
+        ctx.record(b, stream)
+        den.features(ds, gb, col, diag, f_buf, stream)
+        den.infer(f_buf, 1, W, H, out, stream)
+        ctx.record(c, stream)
+        ctx.sync(stream)
+        frame_ms, den_ms = ctx.elapsed_ms(a, b), ctx.elapsed_ms(b, c)
+        cum_ms += frame_ms
+        if f + 1 in (1, 2, 4, 8, 16, 32, 64):
+            acc = col.download(np.float32, (H, W, 3), stream)
+            dn = out.download(np.float32, (H, W, 3), stream)
+            curve_plain.append((f + 1, cum_ms, float(np.sqrt(np.mean((acc - ref) ** 2)))))
+            curve_den.append((f + 1, cum_ms + den_ms, float(np.sqrt(np.mean((dn - ref) ** 2)))))
+    target = 0.01
+
+    def time_to(curve):
+        for i, (k, ms, r) in enumerate(curve):
+            if r <= target:
+                if i == 0:
+                    return ms
+                k0, ms0, r0 = curve[i - 1]
+                u = (np.log(r0) - np.log(target)) / (np.log(r0) - np.log(r))
+                return float(np.exp(np.log(ms0) + u * (np.log(ms) - np.log(ms0))))
+        k, ms, r = curve[-1]
+        return float(ms * (r / target) ** 2)
+
+    tp, td = time_to(curve_plain), time_to(curve_den)
+    res = {"metric": "GPU ms to RMSE 0.01: CNN denoiser vs plain accumulation", "unit": "ms", "value": td,
+           "higher_is_better": False, "target_rmse": target, "plain_ms": tp, "denoiser_ms": td,
+           "speedup": tp / td if td > 0 else None, "curve_plain": curve_plain, "curve_denoised": curve_den,
+           "training": {"scenes": S, "crop": CW, "target_spp": TSPP, "steps": steps, "batch": B,
+                        "gpu_train_ms": train_ms, "wall_train_s": train_s, "data_gen_s": data_s, "loss": losses},
+           "config": {"workload": "heightfield_boxes_1080p_denoiser", "width": W, "height": H,
+                      "reference": "4096 frames of 1-spp plain path tracing", "plain": SET},
+           "device_status": ctx.status()}
+    print(json.dumps(res))
+
+
 def run_reference(args, world, rank, local, dist):
     """The reference path on the host cores: MinoteRT's own implementation
     is Vulkan + MSVC only and cannot run here, so its CPU restatement (the
@@ -584,7 +722,7 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["icospheres_1080p", "batched64", "radiance_cache"],
+    ap.add_argument("--workload", choices=["icospheres_1080p", "batched64", "radiance_cache", "denoiser"],
                     default="icospheres_1080p")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
@@ -595,6 +733,8 @@ def main(argv=None):
         run_batched(args, world, rank, local, dist)
     elif args.workload == "radiance_cache":
         run_cache_experiment(args, world, rank, local, dist)
+    elif args.workload == "denoiser":
+        run_denoise_experiment(args, world, rank, local, dist)
     else:
         run_mine(args, world, rank, local, dist)
 

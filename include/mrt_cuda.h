@@ -203,6 +203,8 @@ typedef struct mrt_frame_stats {
     float    ms_shade;       /* shade + ray generation kernels               */
     float    ms_sort;        /* ray sort kernels                             */
     float    ms_total;       /* whole secondary pass                         */
+    float    ms_cache_train; /* radiance cache: training paths + steps       */
+    float    ms_cache_infer; /* radiance cache: queries                      */
     uint32_t launches;       /* kernels launched by the pass                 */
     uint32_t pad;
 } mrt_frame_stats;

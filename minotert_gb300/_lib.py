@@ -64,7 +64,8 @@ class FrameStats(C.Structure):
                 ("nodes_extension", C.c_uint64 * MRT_MAX_BOUNCES), ("tris_extension", C.c_uint64 * MRT_MAX_BOUNCES),
                 ("nodes_shadow", C.c_uint64), ("tris_shadow", C.c_uint64), ("ms_primary", C.c_float), ("ms_extend", C.c_float),
                 ("ms_extend_b", C.c_float * MRT_MAX_BOUNCES), ("ms_shadow", C.c_float), ("ms_shade", C.c_float),
-                ("ms_sort", C.c_float), ("ms_total", C.c_float), ("launches", C.c_uint32), ("pad", C.c_uint32)]
+                ("ms_sort", C.c_float), ("ms_total", C.c_float), ("ms_cache_train", C.c_float),
+                ("ms_cache_infer", C.c_float), ("launches", C.c_uint32), ("pad", C.c_uint32)]
 
 
 class Tuning(C.Structure):

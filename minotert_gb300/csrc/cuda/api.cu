@@ -341,6 +341,8 @@ int mrt_cuda_frame_stats(mrt_ctx* ctx, mrt_frame_stats* out) {
         case 3: st.ms_shade += ms; break;
         case 4: st.ms_sort += ms; break;
         case 5: st.ms_total += ms; break;
+        case 6: st.ms_cache_train += ms; break;
+        case 7: st.ms_cache_infer += ms; break;
         default: break;
         }
         ctx->ev_pool.push_back(r.a);
@@ -729,7 +731,7 @@ int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
     if (nee) MRT_LAUNCH(2, 0, launch_trace_shadow(scene->dev, wb, tp, 0, tblocks, ctx->d_status, ctx->counters, dyn_sh, s));
     MRT_LAUNCH(1, 1, launch_trace_ext(scene->dev, wb, 1, tblocks, ctx->d_status, ctx->counters, dyn, s));
     MRT_LAUNCH(3, 1, launch_cache_query(scene->dev, tp, wb, q, pb, ctx->d_status, s));
-    MRT_LAUNCH(6, 1, cache_infer(cache, q, uint32_t(wb.cap), wb.counters + kCntExt + 1, pred, s));
+    MRT_LAUNCH(7, 1, cache_infer(cache, q, uint32_t(wb.cap), wb.counters + kCntExt + 1, pred, s));
     MRT_LAUNCH(3, 1, launch_cache_apply(wb, pred, pb, s));
     MRT_LAUNCH(3, 0, launch_tally(wb, s));
     MRT_LAUNCH(3, 0, launch_finalize(wb, color, 1, params->accumulate, params->frame_index, s));

@@ -74,44 +74,42 @@ __device__ __forceinline__ uint32_t grid_index(uint32_t x, uint32_t y, uint32_t 
     return ((x * 1u) ^ (y * 2654435761u) ^ (z * 805459861u)) & mask;
 }
 
-// Corner indices and trilinear weights of position p in [0,1]^3 on every
-// level.  Level l has scale s_l = base_res * growth^l cells per unit; dense
-// indexing while (ceil(s_l) + 2)^3 fits the table, hashed otherwise.
-__device__ void grid_corners(const GridSpec& g, float px, float py, float pz, uint32_t* idx, float* w) {
+// Corner indices (table-wide) and trilinear weights of position p in [0,1]^3
+// on level l.  Level l has scale s_l = base_res * growth^l cells per unit;
+// dense indexing while (ceil(s_l) + 2)^3 fits the table, hashed otherwise.
+__device__ __forceinline__ void level_corners(const GridSpec& g, int l, float px, float py, float pz,
+                                              uint32_t idx[8], float w[8]) {
     const uint32_t T = 1u << g.log2_t, mask = T - 1u;
-#pragma unroll 1
-    for (int l = 0; l < kLevels; ++l) {
-        const float s = g.base_res * exp2f(float(l) * log2f(g.growth));
-        const uint32_t res = uint32_t(ceilf(s)) + 2u;
-        const bool dense = uint64_t(res) * res * res <= T;
-        const float fx = px * s, fy = py * s, fz = pz * s;
-        const float x0 = floorf(fx), y0 = floorf(fy), z0 = floorf(fz);
-        const float tx = fx - x0, ty = fy - y0, tz = fz - z0;
-        const uint32_t ix = uint32_t(x0), iy = uint32_t(y0), iz = uint32_t(z0);
+    const float s = g.base_res * exp2f(float(l) * log2f(g.growth));
+    const uint32_t res = uint32_t(ceilf(s)) + 2u;
+    const bool dense = uint64_t(res) * res * res <= T;
+    const float fx = px * s, fy = py * s, fz = pz * s;
+    const float x0 = floorf(fx), y0 = floorf(fy), z0 = floorf(fz);
+    const float tx = fx - x0, ty = fy - y0, tz = fz - z0;
+    const uint32_t ix = uint32_t(x0), iy = uint32_t(y0), iz = uint32_t(z0);
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            const uint32_t cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
-            idx[l * 8 + c] = uint32_t(l) * T + grid_index(ix + cx, iy + cy, iz + cz, res, dense, mask);
-            w[l * 8 + c] = (cx ? tx : 1.0f - tx) * (cy ? ty : 1.0f - ty) * (cz ? tz : 1.0f - tz);
-        }
+    for (int c = 0; c < 8; ++c) {
+        const uint32_t cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
+        idx[c] = uint32_t(l) * T + grid_index(ix + cx, iy + cy, iz + cz, res, dense, mask);
+        w[c] = (cx ? tx : 1.0f - tx) * (cy ? ty : 1.0f - ty) * (cz ? tz : 1.0f - tz);
     }
 }
 
 // 64 input halves of one query: 32 features, normal, direction, zeros
 __device__ void encode_row(const GridSpec& g, const __half2* grid, const float* q, __half* row) {
-    uint32_t idx[kLevels * 8];
-    float w[kLevels * 8];
     const float px = fminf(fmaxf(q[0], 0.0f), 1.0f), py = fminf(fmaxf(q[1], 0.0f), 1.0f),
                 pz = fminf(fmaxf(q[2], 0.0f), 1.0f);
-    grid_corners(g, px, py, pz, idx, w);
 #pragma unroll 1
     for (int l = 0; l < kLevels; ++l) {
+        uint32_t idx[8];
+        float w[8];
+        level_corners(g, l, px, py, pz, idx, w);
         float f0 = 0.0f, f1 = 0.0f;
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
-            const float2 v = __half22float2(grid[idx[l * 8 + c]]);
-            f0 = fmaf(w[l * 8 + c], v.x, f0);
-            f1 = fmaf(w[l * 8 + c], v.y, f1);
+            const float2 v = __half22float2(grid[idx[c]]);
+            f0 = fmaf(w[c], v.x, f0);
+            f1 = fmaf(w[c], v.y, f1);
         }
         row[2 * l] = __float2half_rn(f0);
         row[2 * l + 1] = __float2half_rn(f1);
@@ -408,18 +406,18 @@ k_cache_train_bwd(CacheDev c, uint32_t n, const __half* inputs, const __half* ac
 __global__ void k_grid_bwd(CacheDev c, const float* q, const float* d_in, uint32_t n, float* g_grid) {
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
-    uint32_t idx[kLevels * 8];
-    float w[kLevels * 8];
     const float px = fminf(fmaxf(q[size_t(r) * 9 + 0], 0.0f), 1.0f);
     const float py = fminf(fmaxf(q[size_t(r) * 9 + 1], 0.0f), 1.0f);
     const float pz = fminf(fmaxf(q[size_t(r) * 9 + 2], 0.0f), 1.0f);
-    grid_corners(c.spec, px, py, pz, idx, w);
     for (int l = 0; l < kLevels; ++l) {
         const float d0 = d_in[size_t(r) * kEnc + 2 * l], d1 = d_in[size_t(r) * kEnc + 2 * l + 1];
         if (d0 == 0.0f && d1 == 0.0f) continue;
+        uint32_t idx[8];
+        float w[8];
+        level_corners(c.spec, l, px, py, pz, idx, w);
         for (int k = 0; k < 8; ++k) {
-            atomicAdd(&g_grid[2 * size_t(idx[l * 8 + k])], w[l * 8 + k] * d0);
-            atomicAdd(&g_grid[2 * size_t(idx[l * 8 + k]) + 1], w[l * 8 + k] * d1);
+            atomicAdd(&g_grid[2 * size_t(idx[k])], w[k] * d0);
+            atomicAdd(&g_grid[2 * size_t(idx[k]) + 1], w[k] * d1);
         }
     }
 }
