@@ -454,6 +454,131 @@ int mrt_cuda_denoiser_train_step(mrt_ctx* ctx, mrt_denoiser* den, const uint16_t
 int mrt_cuda_denoiser_params(mrt_ctx* ctx, mrt_denoiser* den, int which, float* host, size_t count,
                              int set);
 
+/* ---- sky / atmosphere ---------------------------------------------------
+ * Replaces Atmosphere and Sky (src/gfx/modules/sky.ixx:18-262) and their
+ * shaders (src/gpu/sky/genTransmittance.comp, genMultiScattering.comp,
+ * genView.comp).  Distances in kilometres; the planet centre is at
+ * (0, 0, -bottom_radius) in world space (+Z up).  LUTs are float RGBA:
+ * transmittance 256x64, multiple scattering 32x32, sky view 192x108. */
+typedef struct mrt_atmosphere_params {  /* sky.ixx Atmosphere::Params :29-56 */
+    float bottom_radius;               /* planet radius                      */
+    float top_radius;                  /* radius of the atmosphere's top     */
+    float rayleigh_density_exp_scale;  /* density = exp(scale * height)      */
+    float rayleigh_scattering[3];
+    float mie_density_exp_scale;
+    float mie_scattering[3];
+    float mie_extinction[3];
+    float mie_absorption[3];
+    float mie_phase_g;                 /* Cornette-Shanks asymmetry          */
+    float absorption_density0_layer_width;   /* ozone tent: below the width */
+    float absorption_density0_constant_term; /* linear*h + constant, above  */
+    float absorption_density0_linear_term;   /* the second line, clamped to */
+    float absorption_density1_constant_term; /* [0, 1]                      */
+    float absorption_density1_linear_term;
+    float absorption_extinction[3];
+    float ground_albedo[3];
+} mrt_atmosphere_params;
+/* Earth's atmosphere (Atmosphere::Params::earth, sky.ixx:59-83). */
+void mrt_atmosphere_earth(mrt_atmosphere_params* out);
+
+typedef struct mrt_sky mrt_sky;
+int mrt_cuda_sky_create(mrt_ctx* ctx, mrt_sky** out);
+int mrt_cuda_sky_destroy(mrt_ctx* ctx, mrt_sky* sky);
+/* Transmittance and multiple-scattering LUTs (Atmosphere ctor,
+ * sky.ixx:84-174); the reference rebuilds them every frame. */
+int mrt_cuda_sky_atmosphere(mrt_ctx* ctx, mrt_sky* sky, const mrt_atmosphere_params* params,
+                            void* stream);
+/* Sky-view LUT around probe_pos (Sky::createView, sky.ixx:199-262).  The
+ * sun direction and illuminance also drive the sun disc of the miss
+ * shader (the reference hard-codes the same defaults in
+ * secondaryRays.comp:43-44 and sky.ixx:187-188). */
+int mrt_cuda_sky_view(mrt_ctx* ctx, mrt_sky* sky, const float probe_pos[3], const float sun_dir[3],
+                      const float sun_illuminance[3], void* stream);
+/* Copies LUT `which` (0 transmittance, 1 multiple scattering, 2 sky view)
+ * to host RGBA floats; count = floats available.  Synchronises. */
+int mrt_cuda_sky_lut(mrt_ctx* ctx, const mrt_sky* sky, int which, float* host_rgba, size_t count);
+/* skyColor(dir) (secondaryRays.comp:36-58) for n device directions ->
+ * n device RGB floats, seen from camera_pos. */
+int mrt_cuda_sky_eval(mrt_ctx* ctx, const mrt_sky* sky, const float camera_pos[3], const float* dirs,
+                      uint32_t n, float* out_rgb, void* stream);
+/* Binds `sky` (NULL: unbind) as the radiance of escaping paths in
+ * mrt_cuda_secondary_rays and mrt_cuda_cache_frame, seen from the
+ * camera's position; unbound, they use mrt_trace_params.sky_radiance.
+ * The sky must outlive the binding and its view must be built. */
+int mrt_cuda_set_sky(mrt_ctx* ctx, const mrt_sky* sky);
+
+/* ---- joint bilateral filter ------------------------------------------------
+ * Replaces Denoiser::bilateral (src/gfx/modules/denoiser.ixx:34-97) and
+ * src/gpu/denoise/bilateral.comp: a circular Gaussian of radius
+ * round(k_sigma * sigma) over the colour, each tap weighted by how well its
+ * normal and linear depth agree with the centre's, plus the reference's
+ * 0.005 x random dither.  Taps sit on whole columns and fractional rows
+ * (the reference's d.y loop), read bilinearly with clamp-to-edge.  The
+ * output stays float RGB (the reference writes RGBA8 UNORM, clamping HDR). */
+#define MRT_BILATERAL_MAX_RADIUS 24
+typedef struct mrt_bilateral_params {  /* BilateralParams, denoiser.ixx:20-31 */
+    float    sigma;          /* 5.0                                          */
+    float    k_sigma;        /* 2.0                                          */
+    float    threshold;      /* 0.12                                         */
+    float    near_plane;     /* camera near plane: linear depth = near / z  */
+    uint32_t frame_counter;  /* dither seed (bilateral.comp:68)              */
+    uint32_t dither;         /* 1: add the dither                            */
+} mrt_bilateral_params;
+void mrt_bilateral_defaults(mrt_bilateral_params* out);
+/* color, out: device float RGB, width*height*3; gbuffer supplies depth
+ * (R16F) and normal (RGBA16F).  out must not alias color. */
+int mrt_cuda_bilateral(mrt_ctx* ctx, const mrt_gbuffer* gbuffer, const float* color,
+                       const mrt_bilateral_params* params, float* out, void* stream);
+
+/* ---- tonemappers ----------------------------------------------------------
+ * Replaces Tonemapper (src/gfx/modules/tonemapper.ixx) and
+ * src/gpu/tonemap/*.comp: exposure, one of six curves, sRGB encode, RGBA8
+ * UNORM (round to nearest even, alpha 255). */
+#define MRT_TONEMAP_LINEAR   0u
+#define MRT_TONEMAP_REINHARD 1u
+#define MRT_TONEMAP_HABLE    2u
+#define MRT_TONEMAP_ACES     3u
+#define MRT_TONEMAP_UCHIMURA 4u
+#define MRT_TONEMAP_AMD      5u
+typedef struct mrt_tonemap_params {
+    uint32_t mode;             /* MRT_TONEMAP_*; the renderer's default: AMD  */
+    float    exposure;         /* 1.0                                         */
+    float    reinhard_max;     /* 8.0 (renderer.ixx)                          */
+    float    uchimura[6];      /* max brightness 1, contrast 1, linear start
+                                  0.22, linear length 0.4, black tightness
+                                  1.33, pedestal 0 (tonemapper.ixx:20-40)     */
+    float    amd[5];           /* hdr max 16, contrast 2, shoulder 1, mid in
+                                  0.18, mid out 0.18 (tonemapper.ixx:42-57)   */
+} mrt_tonemap_params;
+void mrt_tonemap_defaults(mrt_tonemap_params* out);
+/* color: device float RGB (width*height*3); out: device RGBA8. */
+int mrt_cuda_tonemap(mrt_ctx* ctx, const float* color, uint32_t width, uint32_t height,
+                     const mrt_tonemap_params* params, uint8_t* out, void* stream);
+
+/* ---- temporal reprojection (new; the reference writes motion vectors in
+ *      primaryRay.comp:73-75 and never reads them) --------------------------
+ * Folds this frame's estimate into a history reprojected with the motion
+ * vectors: the history is read bilinearly at the previous-frame position,
+ * each of the four taps kept only when the previous frame saw a surface
+ * there whose normal and linear depth agree with this pixel's reprojected
+ * surface; the result is history + (sample - history) / n with the history
+ * length n = min(previous n + 1, max_history), and n = 1 where no tap
+ * survives (disocclusion) or the pixel sees the sky.  Both g-buffers need
+ * visibility, hit_t, depth, normal and motion; `consts` are this frame's
+ * (prev_view = the previous camera). */
+typedef struct mrt_reproject_params {
+    float max_history;  /* cap of n (frames)                                */
+    float normal_cos;   /* minimum cosine between the normals (0.9)         */
+    float depth_rel;    /* maximum |linear depth difference| / depth (0.05) */
+    float pad;
+} mrt_reproject_params;
+/* sample, hist, out: device float RGB; hist_len, out_len: device float.
+ * out / out_len must not alias hist / hist_len. */
+int mrt_cuda_reproject(mrt_ctx* ctx, const mrt_gbuffer* cur, const mrt_gbuffer* prev,
+                       const mrt_camera_consts* consts, const float* sample, const float* hist,
+                       const float* hist_len, const mrt_reproject_params* params, float* out,
+                       float* out_len, void* stream);
+
 /* Primary rays for callers that cannot allocate device memory.
  *
  * No counterpart in the reference.  Some callers of this library may not

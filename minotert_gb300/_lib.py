@@ -104,7 +104,23 @@ class Bvh8_C(C.Structure):
                 ("depth", C.c_uint32), ("leaf_count", C.c_uint32), ("build_ms", C.c_double), ("sah_cost", C.c_double)]
 
 
+class BilateralParams(C.Structure):
+    _fields_ = [("sigma", C.c_float), ("k_sigma", C.c_float), ("threshold", C.c_float), ("near_plane", C.c_float),
+                ("frame_counter", C.c_uint32), ("dither", C.c_uint32)]
+
+
+class TonemapParams(C.Structure):
+    _fields_ = [("mode", C.c_uint32), ("exposure", C.c_float), ("reinhard_max", C.c_float),
+                ("uchimura", C.c_float * 6), ("amd", C.c_float * 5)]
+
+
+class ReprojectParams(C.Structure):
+    _fields_ = [("max_history", C.c_float), ("normal_cos", C.c_float), ("depth_rel", C.c_float),
+                ("pad", C.c_float)]
+
+
 assert C.sizeof(CameraConsts) == 84 * 4 and C.sizeof(TraceParams) == 80
+assert C.sizeof(BilateralParams) == 24 and C.sizeof(TonemapParams) == 56 and C.sizeof(ReprojectParams) == 16
 
 
 class MrtError(RuntimeError):
@@ -182,6 +198,20 @@ def lib() -> C.CDLL:
             "mrt_cuda_denoiser_train_step": ([vp, vp, vp, vp, u32, u32, u32, C.c_float, i32, C.POINTER(C.c_float),
                                               vp], i32),
             "mrt_cuda_denoiser_params": ([vp, vp, i32, vp, sz, i32], i32),
+            "mrt_atmosphere_earth": ([vp], None),
+            "mrt_cuda_sky_create": ([vp, pp], i32),
+            "mrt_cuda_sky_destroy": ([vp, vp], i32),
+            "mrt_cuda_sky_atmosphere": ([vp, vp, vp, vp], i32),
+            "mrt_cuda_sky_view": ([vp, vp, vp, vp, vp, vp], i32),
+            "mrt_cuda_sky_lut": ([vp, vp, i32, vp, sz], i32),
+            "mrt_cuda_sky_eval": ([vp, vp, vp, vp, u32, vp, vp], i32),
+            "mrt_cuda_set_sky": ([vp, vp], i32),
+            "mrt_bilateral_defaults": ([C.POINTER(BilateralParams)], None),
+            "mrt_cuda_bilateral": ([vp, C.POINTER(GBuffer), vp, C.POINTER(BilateralParams), vp, vp], i32),
+            "mrt_tonemap_defaults": ([C.POINTER(TonemapParams)], None),
+            "mrt_cuda_tonemap": ([vp, vp, u32, u32, C.POINTER(TonemapParams), vp, vp], i32),
+            "mrt_cuda_reproject": ([vp, C.POINTER(GBuffer), C.POINTER(GBuffer), C.POINTER(CameraConsts), vp, vp, vp,
+                                    C.POINTER(ReprojectParams), vp, vp, vp], i32),
             "mrt_cuda_batch_create": ([vp, u32, vp, vp, vp, vp, vp, pp], i32),
             "mrt_cuda_batch_destroy": ([vp, vp], i32),
             "mrt_cuda_batch_trace": ([vp, vp, vp, vp, vp, u32, vp], i32),
@@ -298,6 +328,12 @@ class Context:
 
     def set_counters(self, on: bool):
         self.check(lib().mrt_cuda_set_counters(self._h, 1 if on else 0), "set_counters")
+
+    def set_sky(self, view):
+        """Escaping paths see `view` (a sky.SkyView); None: the constant
+        sky_radiance of the trace parameters."""
+        self.check(lib().mrt_cuda_set_sky(self._h, None if view is None else view.handle), "set_sky")
+        self._sky = view  # keeps the LUTs alive while bound
 
     def frame_stats(self) -> FrameStats:
         st = FrameStats()

@@ -62,7 +62,7 @@ FrameParams frame_params(const mrt_camera_consts* c, uint32_t w, uint32_t h) {
 }
 
 TraceParams trace_params(const mrt_trace_params* p) {
-    TraceParams t;
+    TraceParams t{};
     t.samples = p->samples;
     t.max_bounces = p->max_bounces;
     t.rr_start = p->rr_start;
@@ -632,6 +632,7 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
     const uint32_t W = gbuffer->width, H = gbuffer->height;
     FrameParams fp = frame_params(consts, W, H);
     TraceParams tp = trace_params(params);
+    tp.atmo = sky_dev(ctx->sky, consts->camera_pos);
     BlueNoise bn{ctx->d_bn, ctx->bn_w, ctx->bn_h};
     Scope total(ctx, s, 5, 0);
     if (scene->kind == 1) {
@@ -700,6 +701,7 @@ int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
     const uint32_t W = gbuffer->width, H = gbuffer->height;
     const FrameParams fp = frame_params(consts, W, H);
     TraceParams tp = trace_params(params);
+    tp.atmo = sky_dev(ctx->sky, consts->camera_pos);
     const BlueNoise bn{ctx->d_bn, ctx->bn_w, ctx->bn_h};
     Scope total(ctx, s, 5, 0);
     if (train) {

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include "mrt_cuda.h"
+#include "sky.cuh"
 #include "traverse.cuh"
 
 namespace mrt {
@@ -91,10 +92,38 @@ struct FrameParams {
     float pitch_x, pitch_y;
 };
 
+// Pinhole ray of pixel (x, y) (primaryRay.comp:46-51): uv at the pixel
+// centre with v flipped, origin = invView * (0,0,0,1),
+// dir = normalize(invView * vec4((invProj * vec4(2uv-1, 1, 1)).xyz, 0)).
+MRT_DEV void primary_ray(const FrameParams& fp, uint32_t x, uint32_t y, f3& o, f3& d) {
+    const float uvx = __fmul_rn(__fadd_rn(float(x), 0.5f), fp.pitch_x);
+    const float uvy = __fsub_rn(1.0f, __fmul_rn(__fadd_rn(float(y), 0.5f), fp.pitch_y));
+    float org[4], vd[4], wd[4];
+    matvec_rn(fp.c.inv_view, 0.0f, 0.0f, 0.0f, 1.0f, org);
+    matvec_rn(fp.c.inv_projection, __fsub_rn(__fmul_rn(uvx, 2.0f), 1.0f),
+              __fsub_rn(__fmul_rn(uvy, 2.0f), 1.0f), 1.0f, 1.0f, vd);
+    matvec_rn(fp.c.inv_view, vd[0], vd[1], vd[2], 0.0f, wd);
+    o = f3{org[0], org[1], org[2]};
+    d = normalize_rn(f3{wd[0], wd[1], wd[2]});
+}
+
+MRT_DEV f3 ray_at(f3 o, f3 d, float t) { return add_rn(o, scale_rn(d, t)); } // intersect.glsl:22-24
+
 struct TraceParams {
     uint32_t samples, max_bounces, rr_start, rng_mode, estimator;
     float sun[3], sun_e[3], sky[3];
+    SkyDev atmo;  // atmosphere miss shader; atmo.view == nullptr: constant sky
 };
+
+// Radiance of a path escaping in direction d: the bound sky, else the
+// constant sky radiance.
+MRT_DEV f3 escape_radiance(const TraceParams& tp, f3 d) {
+    if (tp.atmo.view) return sky_color(tp.atmo, d);
+    return f3{tp.sky[0], tp.sky[1], tp.sky[2]};
+}
+
+// Miss-shader state of a bound sky (sky.cu)
+SkyDev sky_dev(const mrt_sky* s, const float cam[3]);
 
 struct BlueNoise {
     const float2* rot;
@@ -185,4 +214,5 @@ struct mrt_ctx {
     std::vector<cudaEvent_t> ev_pool;
     mrt_frame_stats acc{};
     uint32_t launches = 0;
+    const mrt_sky* sky = nullptr;  // miss shader bound by mrt_cuda_set_sky
 };

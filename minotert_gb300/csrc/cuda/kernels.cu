@@ -19,22 +19,6 @@ namespace mrt {
 
 constexpr float kInvPi = 0.318309886183790671538f;
 
-// Pinhole ray of pixel (x, y) (primaryRay.comp:46-51): uv at the pixel
-// centre with v flipped, origin = invView * (0,0,0,1),
-// dir = normalize(invView * vec4((invProj * vec4(2uv-1, 1, 1)).xyz, 0)).
-MRT_DEV void primary_ray(const FrameParams& fp, uint32_t x, uint32_t y, f3& o, f3& d) {
-    const float uvx = __fmul_rn(__fadd_rn(float(x), 0.5f), fp.pitch_x);
-    const float uvy = __fsub_rn(1.0f, __fmul_rn(__fadd_rn(float(y), 0.5f), fp.pitch_y));
-    float org[4], vd[4], wd[4];
-    matvec_rn(fp.c.inv_view, 0.0f, 0.0f, 0.0f, 1.0f, org);
-    matvec_rn(fp.c.inv_projection, __fsub_rn(__fmul_rn(uvx, 2.0f), 1.0f),
-              __fsub_rn(__fmul_rn(uvy, 2.0f), 1.0f), 1.0f, 1.0f, vd);
-    matvec_rn(fp.c.inv_view, vd[0], vd[1], vd[2], 0.0f, wd);
-    o = f3{org[0], org[1], org[2]};
-    d = normalize_rn(f3{wd[0], wd[1], wd[2]});
-}
-
-MRT_DEV f3 ray_at(f3 o, f3 d, float t) { return add_rn(o, scale_rn(d, t)); } // intersect.glsl:22-24
 
 // g-buffer extras: depth = (P V hit).z / w as R16F, normal RGBA16F (the ray
 // direction on a miss), motion = (proj - prev proj).xy / pitch as RG16F
@@ -223,7 +207,7 @@ MRT_DEV uint32_t initial_seed(uint32_t mode, uint32_t frame, uint32_t pixel) {
 MRT_DEV float2 bn_rot(const BlueNoise& bn, uint32_t x, uint32_t y) { return bn.rot[(y % bn.h) * bn.w + (x % bn.w)]; }
 
 // secondaryRays.comp:102-135 with the reference's sample/bounce loop.
-// skyColor() is a constant radiance here (the sky-view LUT is not built).
+// skyColor() is the bound atmosphere (sky.cuh) or a constant radiance.
 __global__ void __launch_bounds__(128)
 k_secondary_sphere(DevScene sc, FrameParams fp, mrt_gbuffer g, TraceParams tp, BlueNoise bn, float* color,
                    uint32_t accumulate, uint32_t frame_index) {
@@ -247,7 +231,6 @@ k_secondary_sphere(DevScene sc, FrameParams fp, mrt_gbuffer g, TraceParams tp, B
     const f3 p0{wp[0], wp[1], wp[2]};
     uint32_t rng = initial_seed(tp.rng_mode, fp.c.frame_counter, uint32_t(pi));
     const float2 rot = bn_rot(bn, x, y);
-    const f3 sky{tp.sky[0], tp.sky[1], tp.sky[2]};
 
     f3 acc{0.0f, 0.0f, 0.0f};
     for (uint32_t s = 0; s < tp.samples; ++s) {
@@ -283,7 +266,7 @@ k_secondary_sphere(DevScene sc, FrameParams fp, mrt_gbuffer g, TraceParams tp, B
                 const float4 al = sc.spheres[2 * hprim + 1];
                 col = mul_rn(col, f3{al.x, al.y, al.z});
             } else {
-                res = mul_rn(col, sky);
+                res = mul_rn(col, escape_radiance(tp, hn));
                 break;
             }
         }
@@ -399,7 +382,6 @@ k_shade_primary(DevScene sc, FrameParams fp, mrt_gbuffer g, TraceParams tp, Blue
     const uint32_t npix = fp.width * fp.height;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t rounded = (npix + 31u) & ~31u;
-    const f3 sky{tp.sky[0], tp.sky[1], tp.sky[2]};
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < rounded; i += stride) {
         const bool valid = i < npix;
         VertexOut vo;
@@ -408,12 +390,12 @@ k_shade_primary(DevScene sc, FrameParams fp, mrt_gbuffer g, TraceParams tp, Blue
             uint32_t rng = sample == 0u ? initial_seed(tp.rng_mode, fp.c.frame_counter, i) : wb.rng[i];
             if (sample == 0u) wb.L[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             const uint32_t prim = g.visibility[i];
+            const uint32_t x = i % fp.width, y = i / fp.width;
+            f3 o, d;
+            primary_ray(fp, x, y, o, d);
             if (prim == kMiss) {
-                add_L(wb.L, i, sky);
+                add_L(wb.L, i, escape_radiance(tp, d));
             } else {
-                const uint32_t x = i % fp.width, y = i / fp.width;
-                f3 o, d;
-                primary_ray(fp, x, y, o, d);
                 const f3 p = ray_at(o, d, g.hit_t[i]);
                 vo = shade_vertex(sc, tp, bn, fp.width, 0u, i, p, d, prim, f3{1.0f, 1.0f, 1.0f}, rng, status);
             }
@@ -431,7 +413,6 @@ k_shade(DevScene sc, TraceParams tp, BlueNoise bn, WaveBuffers wb, uint32_t widt
     const PathRay* q = ext_queue(wb, vertex);
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t rounded = (n + 31u) & ~31u;
-    const f3 sky{tp.sky[0], tp.sky[1], tp.sky[2]};
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < rounded; i += stride) {
         VertexOut vo;
         vo.shadow = vo.ext = false;
@@ -441,7 +422,7 @@ k_shade(DevScene sc, TraceParams tp, BlueNoise bn, WaveBuffers wb, uint32_t widt
             const uint32_t pix = __float_as_uint(pr.o_pix.w);
             const f3 beta{pr.beta.x, pr.beta.y, pr.beta.z};
             if (h.x == kMiss) {
-                add_L(wb.L, pix, mul_rn(beta, sky));
+                add_L(wb.L, pix, mul_rn(beta, escape_radiance(tp, f3{pr.d.x, pr.d.y, pr.d.z})));
             } else {
                 uint32_t rng = wb.rng[pix];
                 const f3 o{pr.o_pix.x, pr.o_pix.y, pr.o_pix.z}, d{pr.d.x, pr.d.y, pr.d.z};
@@ -774,7 +755,6 @@ k_cache_train_paths(DevScene sc, FrameParams fp, TraceParams tp, uint32_t bounce
     f3 o, d;
     primary_ray(fp, pix % fp.width, pix / fp.width, o, d);
     const f3 sun{tp.sun[0], tp.sun[1], tp.sun[2]};
-    const f3 sky{tp.sky[0], tp.sky[1], tp.sky[2]};
     float qv[kTrainMaxVerts][9];
     f3 nee[kTrainMaxVerts], rho[kTrainMaxVerts];
     float wcont[kTrainMaxVerts];
@@ -828,7 +808,7 @@ k_cache_train_paths(DevScene sc, FrameParams fp, TraceParams tp, uint32_t bounce
     }
     if (st) atomicOr(status, st);
     // suffix radiance, last vertex first
-    f3 next = escaped ? sky : f3{0.0f, 0.0f, 0.0f};
+    f3 next = escaped ? escape_radiance(tp, d) : f3{0.0f, 0.0f, 0.0f};
     for (int v = nv - 1; v >= 0; --v) {
         const float w = wcont[v];
         const f3 L{nee[v].x + rho[v].x * w * next.x, nee[v].y + rho[v].y * w * next.y,
@@ -850,7 +830,6 @@ __global__ void __launch_bounds__(kShadeBlock)
 k_cache_query(DevScene sc, TraceParams tp, WaveBuffers wb, float* q, float4* pb, uint32_t* status) {
     const uint32_t n = wb.counters[kCntExt + 1];
     const PathRay* qin = ext_queue(wb, 1);
-    const f3 sky{tp.sky[0], tp.sky[1], tp.sky[2]};
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const PathRay pr = qin[i];
         const uint2 h = wb.hits[i];
@@ -858,7 +837,7 @@ k_cache_query(DevScene sc, TraceParams tp, WaveBuffers wb, float* q, float4* pb,
         const f3 beta{pr.beta.x, pr.beta.y, pr.beta.z};
         float* row = q + size_t(i) * 9;
         if (h.x == kMiss) {
-            add_L(wb.L, pix, mul_rn(beta, sky));
+            add_L(wb.L, pix, mul_rn(beta, escape_radiance(tp, f3{pr.d.x, pr.d.y, pr.d.z})));
             for (int k = 0; k < 9; ++k) row[k] = 0.0f;
             pb[i] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(pix));
         } else {

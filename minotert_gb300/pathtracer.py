@@ -177,7 +177,11 @@ class Pathtracer:
 
     def secondaryRays(self, gbuffer: GBuffer, camera: Camera, sky: Sky, blueNoise: np.ndarray,
                       settings: TraceSettings | None = None, color: DeviceBuffer | None = None,
-                      stream=None) -> DeviceBuffer:
+                      stream=None, skyView=None) -> DeviceBuffer:
+        """secondaryRays (pathtracer.ixx:118-195).  `sky` holds the constant
+        sky radiance and the NEE light; `skyView` (a sky.SkyView, as
+        secondaryRays' atmo + skyView arguments) makes escaping paths see
+        the atmosphere instead of the constant radiance."""
         settings = settings or TraceSettings()
         if self._bn_id is not id(blueNoise):
             self.ctx.blue_noise(blueNoise)
@@ -185,9 +189,15 @@ class Pathtracer:
         color = color or self.ctx.alloc(12 * gbuffer.width * gbuffer.height)
         consts = camera_consts(camera, camera, self.frame_counter)
         params = settings.params(sky)
-        self.ctx.check(lib().mrt_cuda_secondary_rays(self.ctx.handle, self.scene.handle, C.byref(gbuffer.c()),
-                                                     C.byref(consts), C.byref(params), C.c_void_p(color.ptr),
-                                                     ptr(stream)), "secondaryRays")
+        if skyView is not None:
+            self.ctx.set_sky(skyView)
+        try:
+            self.ctx.check(lib().mrt_cuda_secondary_rays(self.ctx.handle, self.scene.handle, C.byref(gbuffer.c()),
+                                                         C.byref(consts), C.byref(params), C.c_void_p(color.ptr),
+                                                         ptr(stream)), "secondaryRays")
+        finally:
+            if skyView is not None:
+                self.ctx.set_sky(None)
         return color
 
     # snake_case aliases

@@ -25,14 +25,14 @@ def _has_fma() -> bool:
 
 
 def build(force: bool = False) -> Path:
-    src = HERE / "oracle.cpp"
+    srcs = [HERE / "oracle.cpp", HERE / "post.cpp"]
     OUT.parent.mkdir(exist_ok=True)
-    if not force and OUT.exists() and OUT.stat().st_mtime > src.stat().st_mtime:
+    if not force and OUT.exists() and all(OUT.stat().st_mtime > s.stat().st_mtime for s in srcs):
         return OUT
     cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-math-errno", "-pthread"]
     if _has_fma():
         cmd.append("-mfma")
-    cmd += [str(src), "-o", str(OUT)]
+    cmd += [str(x) for x in srcs] + ["-o", str(OUT)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stderr}")

@@ -568,6 +568,16 @@ struct RayCounts { uint64_t primary = 0, ext = 0, shadow = 0; };
 
 // One path (all samples) for pixel (x, y); F = float reproduces the
 // kernels' order of operations, F = double is the FP64 judge.
+extern "C" int orc_sky_escape(const float* dir, float* out);  // post.cpp
+
+// Radiance of a path escaping along d: the bound atmosphere sky (post.cpp),
+// else the constant sky.
+inline V3<float> escape32(const V3<float>& sky, const V3<float>& d) {
+    float dd[3] = {d.x, d.y, d.z}, o[3];
+    if (orc_sky_escape(dd, o)) return V3<float>{o[0], o[1], o[2]};
+    return sky;
+}
+
 template <typename F>
 V3<F> shade_pixel(const Scene& sc, const FrameInfo& fi, const Params& p, const float* bn_rot, uint32_t bnw,
                   uint32_t bnh, uint32_t x, uint32_t y, uint32_t prim0, F t0, RayCounts& rc, uint32_t* status);
@@ -585,7 +595,7 @@ V3<float> shade_pixel<float>(const Scene& sc, const FrameInfo& fi, const Params&
     V3<float> o0, d0;
     primary_ray(fi, x, y, o0, d0);
     for (uint32_t s = 0; s < p.samples; ++s) {
-        if (prim0 == kMiss) { L = L + sky; continue; }
+        if (prim0 == kMiss) { L = L + escape32(sky, d0); continue; }
         V3<float> beta{1, 1, 1};
         V3<float> o = o0, d = d0;
         uint32_t prim = prim0;
@@ -632,7 +642,7 @@ V3<float> shade_pixel<float>(const Scene& sc, const FrameInfo& fi, const Params&
             Pre32 er = pre32(o, d);
             trace_bvh32(sc.nodes, sc.nn, sc.tris, sc.nt, er, 0.0f, INFINITY, false, prim, t, nullptr, status);
             rc.ext++;
-            if (prim == kMiss) { L = L + cmul(beta, sky); break; }
+            if (prim == kMiss) { L = L + cmul(beta, escape32(sky, d)); break; }
         }
     }
     return L;
@@ -953,7 +963,8 @@ uint32_t orc_primary(const Node* nodes, uint32_t nn, const Tri* tris, uint32_t n
 }
 
 // secondaryRays.comp:102-135 over a sphere list, from the g-buffer
-// (visibility, R16F depth, RGBA16F normal); sky = constant radiance.
+// (visibility, R16F depth, RGBA16F normal); sky = the bound atmosphere
+// (orc_sky_bind) or the constant radiance.
 void orc_secondary_spheres(const float* spheres, uint32_t ns, const Consts* c, uint32_t w, uint32_t h,
                            const uint32_t* vis, const uint16_t* depth, const uint16_t* normal, const uint8_t* bn_rgba,
                            uint32_t bnw, uint32_t bnh, const Params* p, float* color, int threads) {
@@ -1003,7 +1014,7 @@ void orc_secondary_spheres(const float* spheres, uint32_t ns, const Consts* c, u
                         const float* sk = spheres + 8 * hprim;
                         col = cmul(col, V3<float>{sk[4], sk[5], sk[6]});
                     } else {
-                        res = cmul(col, sky);
+                        res = cmul(col, escape32(sky, hn));
                         break;
                     }
                 }
@@ -1131,3 +1142,67 @@ uint32_t orc_pathtrace(const Node* nodes, uint32_t nn, const Tri* tris, uint32_t
 }
 
 } // extern "C"
+
+// ---- temporal reprojection (new; mirrors the CUDA kernel's definition) ----
+// History read bilinearly at this pixel's previous-frame position (its
+// motion vector), taps kept when the previous frame saw a surface with an
+// agreeing normal and linear depth; n = min(n_prev + 1, max_history); the
+// result is history + (sample - history) / n; n = 1 when nothing survives.
+extern "C" void orc_reproject(const Consts* c, uint32_t w, uint32_t h, const uint32_t* vis, const float* hit_t,
+                              const uint16_t* normal, const uint16_t* motion, const uint32_t* pvis,
+                              const uint16_t* pdepth, const uint16_t* pnormal, const float* sample,
+                              const float* hist, const float* hist_len, float max_history, float normal_cos,
+                              float depth_rel, float* out, float* out_len) {
+    const FrameInfo fi = frame_info(c, w, h);
+    const float near_plane = c->proj[3 * 4 + 2];
+    for (uint32_t y = 0; y < h; ++y)
+        for (uint32_t x = 0; x < w; ++x) {
+            const size_t i = size_t(y) * w + x;
+            V3<float> res{sample[3 * i], sample[3 * i + 1], sample[3 * i + 2]};
+            const V3<float> s = res;
+            float len = 1.0f;
+            if (vis[i] != kMiss) {
+                const float px = (float(x) + 0.5f) - h2f(motion[2 * i]) * 0.5f;
+                const float py = (float(y) + 0.5f) + h2f(motion[2 * i + 1]) * 0.5f;
+                V3<float> o, d;
+                primary_ray(fi, x, y, o, d);
+                const V3<float> p = o + d * hit_t[i];
+                float q[4];
+                matvec(fi.ppv, p.x, p.y, p.z, 1.0f, q);
+                const float exp_lin = q[3];
+                const V3<float> cn{h2f(normal[4 * i]), h2f(normal[4 * i + 1]), h2f(normal[4 * i + 2])};
+                const float fx = px - 0.5f, fy = py - 0.5f;
+                const float x0 = std::floor(fx), y0 = std::floor(fy);
+                if (exp_lin > 0.0f && x0 >= -1.0f && x0 <= float(w) - 1.0f && y0 >= -1.0f && y0 <= float(h) - 1.0f) {
+                    const float wx = fx - x0, wy = fy - y0, gx = 1.0f - wx, gy = 1.0f - wy;
+                    const float ws[4] = {gx * gy, wx * gy, gx * wy, wx * wy};
+                    const float tol = depth_rel * exp_lin;
+                    float sw = 0.0f, hl = 0.0f;
+                    V3<float> hh{0.0f, 0.0f, 0.0f};
+                    for (int t = 0; t < 4; ++t) {
+                        const int tx = int(x0) + (t & 1), ty = int(y0) + (t >> 1);
+                        if (tx < 0 || ty < 0 || tx >= int(w) || ty >= int(h) || !(ws[t] > 0.0f)) continue;
+                        const size_t j = size_t(ty) * w + tx;
+                        if (pvis[j] == kMiss) continue;
+                        const V3<float> pn{h2f(pnormal[4 * j]), h2f(pnormal[4 * j + 1]), h2f(pnormal[4 * j + 2])};
+                        if (!(dot(pn, cn) >= normal_cos)) continue;
+                        const float tl = near_plane / h2f(pdepth[j]);
+                        if (!(std::fabs(tl - exp_lin) <= tol)) continue;
+                        sw = sw + ws[t];
+                        hh = hh + V3<float>{hist[3 * j], hist[3 * j + 1], hist[3 * j + 2]} * ws[t];
+                        hl = hl + hist_len[j] * ws[t];
+                    }
+                    if (sw > 0.0f) {
+                        hh = V3<float>{hh.x / sw, hh.y / sw, hh.z / sw};
+                        len = std::fmin(hl / sw + 1.0f, max_history);
+                        const float a = 1.0f / len;
+                        res = hh + (s - hh) * a;
+                    }
+                }
+            }
+            out[3 * i] = res.x;
+            out[3 * i + 1] = res.y;
+            out[3 * i + 2] = res.z;
+            out_len[i] = len;
+        }
+}
