@@ -85,6 +85,32 @@ MRT_DEV float offset_axis(float p, float n) {
 }
 MRT_DEV f3 offset_ray(f3 p, f3 n) { return f3{offset_axis(p.x, n.x), offset_axis(p.y, n.y), offset_axis(p.z, n.z)}; }
 
+// e^x reproducible bit for bit on the CPU: Cody-Waite reduction
+// x = n ln2 + r (n = rint(x log2 e), ln2 split into a 16-bit head and a
+// tail so n * head is exact), the degree-7 Taylor polynomial of e^r on
+// |r| <= ln2/2 in Horner form with correctly rounded FMAs (truncation
+// r^8/8! < 6e-9 relative), then an exact scale by 2^n.  Results below
+// 2^-126 flush to 0.  Used where an expression cancels and would turn
+// a last-bit difference between two exp implementations into a visible one.
+MRT_DEV float exp_cw(float x) {
+    if (!(x > -87.0f)) return x != x ? x : 0.0f;
+    if (x > 88.0f) return __int_as_float(0x7F800000);
+    const float n = rintf(__fmul_rn(x, 1.44269502f));
+    float r = fmaf(-n, 0.693145752f, x);
+    r = fmaf(-n, 1.42860677e-6f, r);
+    float p = 1.98412701e-4f;           // 1/7!
+    p = fmaf(p, r, 1.38888892e-3f);     // 1/6!
+    p = fmaf(p, r, 8.33333377e-3f);     // 1/5!
+    p = fmaf(p, r, 4.16666679e-2f);     // 1/4!
+    p = fmaf(p, r, 1.66666672e-1f);     // 1/3!
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = fmaf(p, r, 1.0f);
+    const int e = int(n);
+    if (e < -126) return 0.0f;
+    return __fmul_rn(p, __int_as_float((e + 127) << 23));
+}
+
 MRT_DEV uint16_t f2h(float x) { return __half_as_ushort(__float2half_rn(x)); }
 MRT_DEV float h2f(uint16_t x) { return __half2float(__ushort_as_half(x)); }
 

@@ -7,10 +7,10 @@
 //                src/gpu/util.glsl:13-18 (sRGB), tonemapper.ixx:20-57
 //   reprojection new: uses the motion vectors of primaryRay.comp:73-75
 //
-// Arithmetic is explicitly rounded (fm/fa/fs/fd) in the GLSL's order so the
-// CPU oracle reproduces it; what is left between the two are the
-// transcendental functions (expf, powf).  Reprojection has none and is
-// bit-identical to its oracle.
+// Arithmetic is explicitly rounded (fm/fa/fs/fd) in the GLSL's order and the
+// bilateral weights use exp_cw (common.cuh), so the CPU oracle reproduces
+// the filter and reprojection bit for bit; the tonemap curves keep CUDA's
+// powf / expf and agree with the oracle to within one 8-bit step.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -130,7 +130,7 @@ k_bilateral(BilateralTable T, const float* __restrict__ color, const uint16_t* _
                 dz = fm(dz, 100.0f);
                 const float dn = dot_rn(wn, cn);
                 const float arg = fm(fclamp(fs(dn, fm(dz, dz)), 0.0f, 1.0f), T.inv_thr_sq2);
-                const float df = fm(fm(expf(arg), T.inv_thr_sqrt2pi), T.blur[t0 + k]);
+                const float df = fm(fm(exp_cw(arg), T.inv_thr_sqrt2pi), T.blur[t0 + k]);
                 zb = fa(zb, df);
                 ar = fa(ar, fm(df, fa(fm(cr[ia], gr), fm(cr[ib], fr))));
                 ag = fa(ag, fm(df, fa(fm(cg[ia], gr), fm(cg[ib], fr))));

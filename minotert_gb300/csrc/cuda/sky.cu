@@ -46,8 +46,8 @@ struct Medium {
 
 MRT_DEV Medium sample_medium(const Atmo& a, f3 p) {
     const float h = fs(len3(p), a.bottom_radius);
-    const float dm = expf(fm(a.mie_density_exp_scale, h));
-    const float dr = expf(fm(a.rayleigh_density_exp_scale, h));
+    const float dm = exp_cw(fm(a.mie_density_exp_scale, h));
+    const float dr = exp_cw(fm(a.rayleigh_density_exp_scale, h));
     const float dz = fclamp(h < a.absorption_density0_layer_width
                                 ? fa(fm(a.absorption_density0_linear_term, h), a.absorption_density0_constant_term)
                                 : fa(fm(a.absorption_density1_linear_term, h), a.absorption_density1_constant_term),
@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(256) k_sky_transmittance(Atmo a, float4* out) 
     const f3 pos{0.0f, 0.0f, h};
     const f3 dir{0.0f, __fsqrt_rn(fs(1.0f, fm(mu, mu))), mu};
     const March m = integrate<false, false, false>(a, pos, dir, f3s(1.0f), 40.0f, f3s(1.0f), nullptr, nullptr);
-    out[i] = make_float4(expf(-m.od.x), expf(-m.od.y), expf(-m.od.z), 1.0f);
+    out[i] = make_float4(exp_cw(-m.od.x), exp_cw(-m.od.y), exp_cw(-m.od.z), 1.0f);
 }
 
 // genMultiScattering.comp:26-146: per (sun zenith, height) texel, second-

@@ -10,7 +10,10 @@
 // CPU oracle evaluates the same expressions in the same order.  LUTs are
 // float4 texel arrays (RGB + 1), sampled bilinearly in software with
 // clamp-to-edge and full FP32 weights (a sampler's fixed-point weights and
-// the reference's FP16 / B10G11R11 storage are not emulated).
+// the reference's FP16 / B10G11R11 storage are not emulated).  The
+// exponentials are exp_cw (common.cuh), which the oracle reproduces bit for
+// bit: the march's segment integral (S - S e^-x) / sigma cancels for
+// optically thin segments and would magnify any exp difference.
 #pragma once
 
 #include "common.cuh"
@@ -42,7 +45,7 @@ MRT_DEV float fclamp(float x, float lo, float hi) { return fminf(fmaxf(x, lo), h
 MRT_DEV f3 f3s(float s) { return f3{s, s, s}; }
 MRT_DEV f3 div3(f3 a, f3 b) { return f3{fd(a.x, b.x), fd(a.y, b.y), fd(a.z, b.z)}; }
 MRT_DEV f3 div3s(f3 a, float s) { return f3{fd(a.x, s), fd(a.y, s), fd(a.z, s)}; }
-MRT_DEV f3 exp3(f3 a) { return f3{expf(a.x), expf(a.y), expf(a.z)}; }
+MRT_DEV f3 exp3(f3 a) { return f3{exp_cw(a.x), exp_cw(a.y), exp_cw(a.z)}; }
 MRT_DEV float len3(f3 a) { return __fsqrt_rn(dot_rn(a, a)); }
 MRT_DEV f3 cross_rn(f3 a, f3 b) {
     return f3{fs(fm(a.y, b.z), fm(a.z, b.y)), fs(fm(a.z, b.x), fm(a.x, b.z)), fs(fm(a.x, b.y), fm(a.y, b.x))};

@@ -41,7 +41,31 @@ inline float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 inline float length(V3 a) { return std::sqrt(dot(a, a)); }
 inline V3 normalize(V3 a) { return a / length(a); }
 inline V3 cross(V3 a, V3 b) { return V3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
-inline V3 vexp(V3 a) { return V3{std::exp(a.x), std::exp(a.y), std::exp(a.z)}; }
+// e^x as the CUDA kernels compute it (exp_cw in common.cuh): Cody-Waite
+// reduction x = n ln2 + r with a 16-bit head of ln2, the degree-7 Taylor
+// polynomial of e^r in Horner form with fma, an exact scale by 2^n.
+float exp_cw(float x) {
+    if (!(x > -87.0f)) return std::isnan(x) ? x : 0.0f;
+    if (x > 88.0f) return INFINITY;
+    const float n = std::nearbyint(x * 1.44269502f);
+    float r = std::fma(-n, 0.693145752f, x);
+    r = std::fma(-n, 1.42860677e-6f, r);
+    float p = 1.98412701e-4f;
+    p = std::fma(p, r, 1.38888892e-3f);
+    p = std::fma(p, r, 8.33333377e-3f);
+    p = std::fma(p, r, 4.16666679e-2f);
+    p = std::fma(p, r, 1.66666672e-1f);
+    p = std::fma(p, r, 0.5f);
+    p = std::fma(p, r, 1.0f);
+    p = std::fma(p, r, 1.0f);
+    const int e = int(n);
+    if (e < -126) return 0.0f;
+    const uint32_t bits = uint32_t(e + 127) << 23;
+    float s;
+    std::memcpy(&s, &bits, 4);
+    return p * s;
+}
+inline V3 vexp(V3 a) { return V3{exp_cw(a.x), exp_cw(a.y), exp_cw(a.z)}; }
 inline float clampf(float x, float lo, float hi) { return std::fmin(std::fmax(x, lo), hi); }
 
 struct Atmo {  // mrt_atmosphere_params
@@ -173,8 +197,8 @@ struct Medium {
 // sky.glsl sampleMediumRGB
 Medium medium(const Atmo& a, V3 p) {
     const float h = length(p) - a.bottom;
-    const float dm = std::exp(a.mie_exp * h);
-    const float dr = std::exp(a.ray_exp * h);
+    const float dm = exp_cw(a.mie_exp * h);
+    const float dr = exp_cw(a.ray_exp * h);
     const float dz = clampf(h < a.oz_width ? a.oz_l0 * h + a.oz_c0 : a.oz_l1 * h + a.oz_c1, 0.0f, 1.0f);
     Medium m;
     m.scat_mie = ld(a.mie_scat) * dm;
@@ -308,9 +332,9 @@ void orc_sky_transmittance(const Atmo* a, float* out) {
             const March m = integrate(*a, V3{0.0f, 0.0f, h}, dir, v3(1.0f), false, 40.0f, false, false, v3(1.0f),
                                       nullptr, nullptr);
             float* o = out + 4 * (y * kTW + x);
-            o[0] = std::exp(-m.od.x);
-            o[1] = std::exp(-m.od.y);
-            o[2] = std::exp(-m.od.z);
+            o[0] = exp_cw(-m.od.x);
+            o[1] = exp_cw(-m.od.y);
+            o[2] = exp_cw(-m.od.z);
             o[3] = 1.0f;
         }
 }
@@ -461,6 +485,8 @@ int orc_sky_escape(const float* dir, float* out) {
 // reference's taps texture(tex, uv + d/size) land on whole columns and at
 // row y + d.y; here row y + d.y is read as the rows y + floor(d.y) and
 // y + floor(d.y) + 1 at weight frac(d.y), clamped to the image.
+extern "C" float orc_exp_cw(float x) { return exp_cw(x); }
+
 extern "C" int orc_bilateral(const float* color, const float* depth, const float* normal, uint32_t w, uint32_t h,
                              float sigma, float k_sigma, float threshold, float near_plane, uint32_t frame,
                              int dither, float* out) {
@@ -503,7 +529,7 @@ extern "C" int orc_bilateral(const float* color, const float* depth, const float
                         dz = dz * 100.0f;
                         const float dn = wn[0] * cn[0] + wn[1] * cn[1] + wn[2] * cn[2];
                         const float arg = clampf(dn - dz * dz, 0.0f, 1.0f) * inv_thr_sq2;
-                        const float df = std::exp(arg) * inv_thr_sqrt2pi * blur;
+                        const float df = exp_cw(arg) * inv_thr_sqrt2pi * blur;
                         zb = zb + df;
                         for (int k = 0; k < 3; ++k) acc[k] = acc[k] + df * (color[3 * a + k] * gr + color[3 * b + k] * fr);
                     }

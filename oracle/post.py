@@ -183,3 +183,14 @@ def reproject(consts, w, h, vis, hit_t, normal, motion, pvis, pdepth, pnormal, s
     lib().orc_reproject(_p(arrs[0]), w, h, *[_p(a) for a in arrs[1:]], max_history, normal_cos, depth_rel,
                         _p(out), _p(out_len))
     return out, out_len
+
+
+def exp_cw(x) -> np.ndarray:
+    """The deterministic e^x shared with the CUDA kernels, elementwise."""
+    L = lib()
+    if not hasattr(L.orc_exp_cw, "_set"):
+        L.orc_exp_cw.argtypes = [C.c_float]
+        L.orc_exp_cw.restype = C.c_float
+        L.orc_exp_cw._set = True
+    xs = np.asarray(x, np.float32).ravel()
+    return np.array([L.orc_exp_cw(float(v)) for v in xs], np.float32).reshape(np.shape(x))

@@ -1,10 +1,10 @@
 """GPU parity of the post-processing kernels (mrt_cuda_bilateral,
 mrt_cuda_tonemap, mrt_cuda_reproject) against the CPU oracle.
 
-Bars: reprojection bit-identical (only + - * / and comparisons, explicitly
-rounded on both sides); bilateral within 2e-5 relative (expf per tap and
-the ratio of sums); tonemap within one 8-bit step with at least 99.9% of
-channels identical (powf / expf in the curves and the sRGB encode).
+Bars: reprojection and the bilateral filter bit-identical (explicitly
+rounded + - * / on both sides, and the filter's weights through the shared
+exp_cw); tonemap within one 8-bit step with at least 99.9% of channels
+identical (CUDA's powf / expf in the curves and the sRGB encode).
 """
 import ctypes as C
 
@@ -47,7 +47,7 @@ def test_bilateral_vs_oracle(ctx, hf_frame, sigma, k_sigma, dither):
     src = col.download(np.float32, (H, W, 3))
     ref = post.bilateral(src, g["depth"], g["normal"], sigma, k_sigma, 0.12, cam.nearPlane, 7, dither)
     assert np.isfinite(got).all()
-    assert np.allclose(got, ref, rtol=2e-5, atol=1e-7)
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
 
 
 def test_bilateral_smooths_a_flat_surface(ctx):
@@ -66,7 +66,7 @@ def test_bilateral_smooths_a_flat_surface(ctx):
     out = Denoiser(ctx).bilateral(ctx.to_device(noisy), gb, cam, dither=False)
     got = out.download(np.float32, (H, W, 3))
     ref = post.bilateral(noisy, depth, nrm.view(np.uint16), near_plane=0.1, dither=False)
-    assert np.allclose(got, ref, rtol=2e-5, atol=1e-7)
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
     inner = got[12:-12, 12:-12]
     assert inner.std() < 0.15 * noisy.std()
 

@@ -135,3 +135,18 @@ def test_reprojection_follows_camera_motion(hf_workload):
                                   np.full((h, w), 5.0, np.float32))
     assert (out_len[hit] == 6.0).mean() > 0.9
     assert np.allclose(out, 0.25, rtol=1e-6)
+
+
+def test_exp_cw_accuracy():
+    # the shared exponential is within 2 ulp of e^x over the float range it
+    # serves, flushes below 2^-126 and saturates above 88
+    rng = np.random.default_rng(9)
+    x = np.concatenate([rng.uniform(-87.0, 88.0, 3000), rng.uniform(-1.0, 1.0, 3000),
+                        [0.0, -0.0, 1.0, -1.0, 1e-8, -1e-8, 88.0, -86.9]]).astype(np.float32)
+    got = post.exp_cw(x).astype(np.float64)
+    ref = np.exp(x.astype(np.float64))
+    ulp = np.spacing(ref.astype(np.float32)).astype(np.float64)
+    normal = ref >= 2.0 ** -126
+    assert (np.abs(got - ref)[normal] <= 2.0 * ulp[normal]).all()
+    assert post.exp_cw(np.float32(0.0)) == 1.0
+    assert post.exp_cw(np.float32(-100.0)) == 0.0 and np.isinf(post.exp_cw(np.float32(89.0)))
