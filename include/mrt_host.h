@@ -105,6 +105,59 @@ uint32_t mrt_scene_reference(mrt_sphere* out /* [5] */);
 /* The reference's default camera (app.ixx:20-32) at a given viewport. */
 void mrt_camera_reference(uint32_t width, uint32_t height, mrt_camera* out);
 
+/* ---- headless renderer ------------------------------------------------
+ * Replaces Renderer_impl::draw (src/gfx/renderer.ixx:39-68) without the
+ * window, ImGui and swapchain: per frame it (re)builds the atmosphere and
+ * the sky view at the camera (:55-57), runs primaryRays with the previous
+ * camera (:58), secondaryRays (:59), optionally folds the frame into a
+ * reprojected history (new), denoises (:60, renderer.ixx:128-160) and
+ * tonemaps (:61, :162-230) into RGBA8, all on device buffers owned by the
+ * renderer; the previous camera is kept for the motion vectors (:66). */
+#define MRT_ACCUM_NONE      0u /* each frame stands alone (the reference)    */
+#define MRT_ACCUM_REPROJECT 1u /* mrt_cuda_reproject into a history          */
+#define MRT_DENOISE_NONE      0u
+#define MRT_DENOISE_BILATERAL 1u /* the reference's default                  */
+#define MRT_SKY_CONSTANT   0u /* trace.sky_radiance                          */
+#define MRT_SKY_ATMOSPHERE 1u /* the reference: LUTs rebuilt every frame     */
+typedef struct mrt_render_settings {
+    mrt_trace_params      trace;      /* samples, bounces, estimator, light   */
+    uint32_t              sky_mode;   /* MRT_SKY_*                            */
+    uint32_t              accumulation; /* MRT_ACCUM_*                        */
+    uint32_t              denoise;    /* MRT_DENOISE_*                        */
+    uint32_t              pad;
+    mrt_atmosphere_params atmosphere; /* MRT_SKY_ATMOSPHERE                   */
+    float                 sun_dir[3]; /* sky view sun (Sky, sky.ixx:186-187)  */
+    float                 sun_illuminance[3];
+    mrt_bilateral_params  bilateral;  /* near_plane / frame_counter are
+                                         taken from the camera and frame     */
+    mrt_reproject_params  reproject;
+    mrt_tonemap_params    tonemap;
+} mrt_render_settings;
+/* The reference's defaults: 8 samples x 8 bounces, escape-only estimator,
+ * reference RNG, Earth atmosphere, no accumulation, bilateral denoiser
+ * (sigma 5, kSigma 2, threshold 0.12), AMD tonemapper at exposure 1. */
+void mrt_render_settings_defaults(mrt_render_settings* out);
+
+typedef struct mrt_renderer mrt_renderer;
+int mrt_renderer_create(mrt_ctx* ctx, const mrt_scene* scene, uint32_t width, uint32_t height,
+                        mrt_renderer** out);
+int mrt_renderer_destroy(mrt_renderer* r);
+/* Draws one frame on `stream` (stream-ordered; returns before the GPU
+ * finishes).  The first frame's previous camera is the camera itself. */
+int mrt_renderer_draw(mrt_renderer* r, const mrt_camera* camera, const mrt_render_settings* settings,
+                      void* stream);
+/* Device pointers of the last frame's planes: 0 RGBA8 output, 1 float RGB
+ * before tonemapping, 2 float RGB path-traced estimate, 3 the g-buffer
+ * (mrt_gbuffer*).  Valid until the next draw. */
+const void* mrt_renderer_plane(const mrt_renderer* r, int which);
+/* Copies the last frame to host memory (either pointer may be NULL):
+ * rgba8 = width*height*4 bytes, hdr = width*height*3 floats.  Syncs. */
+int mrt_renderer_read(mrt_renderer* r, uint8_t* rgba8, float* hdr, void* stream);
+/* Binary PPM (P6, RGB from RGBA8) and PFM (PF, float RGB, bottom-up rows
+ * as the format stores them).  Return 0 or MRT_EINVAL on an I/O error. */
+int mrt_write_ppm(const char* path, const uint8_t* rgba8, uint32_t width, uint32_t height);
+int mrt_write_pfm(const char* path, const float* rgb, uint32_t width, uint32_t height);
+
 /* ---- blue noise ------------------------------------------------------ */
 /* size x size RGBA8 blue-noise tile by void-and-cluster (Ulichney 1993),
  * one independent rank map per channel, seeded. size <= 256. */

