@@ -611,7 +611,7 @@ def run_denoise_experiment(args, world, rank, local, dist):
     ctx.record(ev0, stream)
     for k in range(steps):
         i0 = int(order[(k * B) % (S - B + 1)])
-        lr = 2e-3 if k < steps * 0.7 else 5e-4
+        lr = 1e-3 if k < steps * 0.7 else 2.5e-4
         want = (k % 250 == 0) or k == steps - 1
         loss = den.train_step(feats.ptr + i0 * CW * CW * 16 * 2, targets.ptr + i0 * CW * CW * 12, B, CW, CW, lr=lr,
                               want_loss=want, stream=stream)

@@ -428,7 +428,7 @@ int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
  * connections) over 16-channel BF16 NHWC features: log(1 + radiance),
  * albedo, normal, depth, zero padding.  Forward on the tensor cores (BF16,
  * FP32 accumulate); training backward in FP32; Adam.  The network predicts
- * log(1 + radiance) with an L1 loss.  Width and height must be multiples
+ * a correction to the input's log(1 + radiance), with an L1 loss.  Width and height must be multiples
  * of 4. */
 typedef struct mrt_denoiser mrt_denoiser;
 int mrt_cuda_denoiser_create(mrt_ctx* ctx, uint32_t seed, mrt_denoiser** out);

@@ -10,7 +10,9 @@
 //   -> e2a(128) -> e2b(128) -> [up ++ S1](192) -> d1a(64) -> d1b(64)
 //   -> [up ++ S0](96) -> d0a(32) -> d0b(32) -> out(16, 3 used)
 // 3x3 convolutions with bias, ReLU except the output layer.  The network
-// predicts log(1 + radiance); the loss is L1 in that space.
+// predicts a correction to the input's log(1 + radiance) (a residual: an
+// untrained network passes the noisy image through); the loss is L1 in
+// that space.  The output layer starts at a tenth of the He scale.
 //
 // Forward: implicit-GEMM convolution on the tensor cores (mma.sync
 // m16n8k16, BF16 in, FP32 accumulate): a warp computes 16 consecutive
@@ -251,14 +253,17 @@ __global__ void k_pool_bwd(const float* gout, float* gin, int n, int h, int w, i
     }
 }
 
-// L1 loss in log(1 + radiance) space on channels 0..2 of the output
-__global__ void k_l1_loss(const bf16* y, const float* target, size_t pixels, float* dy, float* loss) {
+// L1 loss in log(1 + radiance) space on channels 0..2: the network predicts
+// a correction added to the input's own log(1 + radiance) (features 0..2)
+__global__ void k_l1_loss(const bf16* y, const bf16* feat, const float* target, size_t pixels, float* dy,
+                          float* loss) {
     float l = 0.0f;
     const float inv = 1.0f / float(pixels * 3);
     for (size_t p = blockIdx.x * size_t(blockDim.x) + threadIdx.x; p < pixels; p += size_t(gridDim.x) * blockDim.x) {
         for (int k = 0; k < 16; ++k) dy[p * 16 + k] = 0.0f;
         for (int k = 0; k < 3; ++k) {
-            const float d = __bfloat162float(y[p * 16 + k]) - log1pf(fmaxf(target[p * 3 + k], 0.0f));
+            const float pred = __bfloat162float(y[p * 16 + k]) + __bfloat162float(feat[p * 16 + k]);
+            const float d = pred - log1pf(fmaxf(target[p * 3 + k], 0.0f));
             l += fabsf(d);
             dy[p * 16 + k] = (d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f)) * inv;
         }
@@ -305,9 +310,13 @@ __global__ void k_features(DevScene sc, const float* color, const uint32_t* vis,
         *reinterpret_cast<__nv_bfloat162*>(out + size_t(i) * 16 + k) = __floats2bfloat162_rn(f[k], f[k + 1]);
 }
 
-__global__ void k_decode(const bf16* y, size_t pixels, float* out) {
+// radiance = exp(input log(1 + radiance) + predicted correction) - 1
+__global__ void k_decode(const bf16* y, const bf16* feat, size_t pixels, float* out) {
     for (size_t p = blockIdx.x * size_t(blockDim.x) + threadIdx.x; p < pixels; p += size_t(gridDim.x) * blockDim.x)
-        for (int k = 0; k < 3; ++k) out[p * 3 + k] = expm1f(fmaxf(__bfloat162float(y[p * 16 + k]), 0.0f));
+        for (int k = 0; k < 3; ++k) {
+            const float v = __bfloat162float(y[p * 16 + k]) + __bfloat162float(feat[p * 16 + k]);
+            out[p * 3 + k] = expm1f(fmaxf(v, 0.0f));
+        }
 }
 
 int grid_for(size_t n) { return int(std::min<size_t>((n + 255) / 256, 65535)); }
@@ -467,7 +476,7 @@ int mrt_cuda_denoiser_create(mrt_ctx* ctx, uint32_t seed, mrt_denoiser** out) {
         const ConvDesc& L = d->layers[l];
         const int cin = L.ca + L.cb;
         const int real_in = l == 0 ? 10 : cin;
-        const float a = std::sqrt(6.0f / float(9 * real_in)) * (l == kLayers - 1 ? 0.5f : 1.0f);
+        const float a = std::sqrt(6.0f / float(9 * real_in)) * (l == kLayers - 1 ? 0.1f : 1.0f);
         for (int co = 0; co < L.cout; ++co)
             for (int tap = 0; tap < 9; ++tap)
                 for (int ci = 0; ci < cin; ++ci) {
@@ -533,7 +542,7 @@ int mrt_cuda_denoiser_infer(mrt_ctx* ctx, mrt_denoiser* d, const uint16_t* featu
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (forward(d, reinterpret_cast<const bf16*>(features), int(batch), int(height), int(width), s) != cudaSuccess)
         return set_error(ctx, MRT_ECUDA, "denoiser_infer: launch");
-    k_decode<<<grid_for(pix), 256, 0, s>>>(d->act[kLayers - 1], pix, out);
+    k_decode<<<grid_for(pix), 256, 0, s>>>(d->act[kLayers - 1], reinterpret_cast<const bf16*>(features), pix, out);
     ctx->launches += 14;
     return MRT_OK;
 }
@@ -552,7 +561,7 @@ int mrt_cuda_denoiser_train_step(mrt_ctx* ctx, mrt_denoiser* d, const uint16_t* 
     const bf16* in = reinterpret_cast<const bf16*>(features);
     if (forward(d, in, n, h, w, s) != cudaSuccess) return set_error(ctx, MRT_ECUDA, "denoiser_train: forward");
     cudaMemsetAsync(d->loss, 0, 4, s);
-    k_l1_loss<<<grid_for(pix), 256, 0, s>>>(d->act[kLayers - 1], targets, pix, d->grad[kLayers - 1], d->loss);
+    k_l1_loss<<<grid_for(pix), 256, 0, s>>>(d->act[kLayers - 1], in, targets, pix, d->grad[kLayers - 1], d->loss);
     // zero the gradient buffers that accumulate from several consumers
     for (int l = 0; l < kLayers - 1; ++l)
         cudaMemsetAsync(d->grad[l], 0, layer_pixels(pix, d->layers[l].scale) * d->layers[l].cout * 4, s);

@@ -28,7 +28,8 @@ def test_denoiser_forward_matches_oracle(ctx):
     y = d_o.download(np.float32, (2, 16, 24, 3))
     params = d.params(0).astype(np.float64)
     _, _, out = cnn.forward(params, from_bf16_bits(xb).astype(np.float64).reshape(2, 16, 24, 16))
-    ref = np.expm1(np.maximum(out[..., :3], 0.0))
+    xin = from_bf16_bits(xb).astype(np.float64).reshape(2, 16, 24, 16)
+    ref = np.expm1(np.maximum(out[..., :3] + xin[..., :3], 0.0))
     assert np.all(np.isfinite(y))
     err = np.abs(y - ref)
     assert np.max(err) < 3e-2 * max(1.0, np.abs(ref).max()), np.max(err)

@@ -66,10 +66,11 @@ def test_sky_view_lut_vs_oracle(ctx, atmo, probe):
     t, m = atmo.lut(0), atmo.lut(1)
     ref = post.sky_view(atmo.params, t, m, probe, sky.sunDirection, sky.sunIlluminance)
     assert np.isfinite(gpu).all()
-    # the view march's sample count floor(mix(4, 14, tMax / 100 km)) is a
-    # step function of the ray length, so a last-bit cosf difference in a
-    # texel's direction can move it by one sample (~1e-3 of that texel)
-    _close(gpu, ref, typical=2e-5, worst=2e-3, quantile=0.99)
+    # near the horizon the ray length tMax -- and with it the view march's
+    # step count floor(mix(4, 14, tMax / 100 km)), a step function -- moves
+    # fast with the zenith angle, so a last-bit cosf difference in a texel's
+    # direction shows up at the 1e-4..1e-3 level there
+    _close(gpu, ref, typical=5e-4, worst=2e-3, quantile=0.99)
 
 
 def test_sky_color_vs_oracle(ctx, atmo):
