@@ -502,17 +502,34 @@ def run_cache_experiment(args, world, rank, local, dist):
     cps = (1, 2, 4, 8, 16, 32, 64, 128, 256, 512)
     nmax = max(cps)
     _, plain_ms, plain_snaps = run(nmax, 0, plain_fn, cps)
-    cache = RadianceCache(ctx, default_config(), bounds=(mesh.lo, mesh.hi))
-
-    def learned_fn(gb, col, f):
-        consts_c = camera_consts(cam, cam, pt.frame_counter)
-        params = TraceSettings(1, 1, 2, 1, True, f).params(sky)
-        cache.frame(ds, gb, consts_c, params, col, train=True, stream=stream)
-
-    _, learned_ms, learned_snaps = run(nmax, 0, learned_fn, cps)
     rmse = lambda im: float(np.sqrt(np.mean((im - ref) ** 2)))
     curve_p = [(k, float(plain_ms[k - 1]), rmse(plain_snaps[k])) for k in cps]
-    curve_l = [(k, float(learned_ms[k - 1]), rmse(learned_snaps[k])) for k in cps]
+
+    def learned_curve(query_vertex):
+        cache = RadianceCache(ctx, default_config(query_vertex=query_vertex), bounds=(mesh.lo, mesh.hi))
+
+        def learned_fn(gb, col, f):
+            consts_c = camera_consts(cam, cam, pt.frame_counter)
+            params = TraceSettings(1, 1, 2, 1, True, f).params(sky)
+            cache.frame(ds, gb, consts_c, params, col, train=True, stream=stream)
+
+        _, ms, snaps = run(nmax, 0, learned_fn, cps)
+        curve = [(k, float(ms[k - 1]), rmse(snaps[k])) for k in cps]
+        # per-pass breakdown over 16 more frames (events around every launch)
+        ctx.set_timing(True)
+        ctx.frame_stats()
+        col = ctx.alloc(12 * W * H)
+        for f in range(16):
+            pt.frame_counter = 5000 + f
+            gb = pt.primaryRays((W, H), cam, cam, stream)
+            learned_fn(gb, col, f)
+        ctx.sync(stream)
+        st = ctx.frame_stats()
+        ctx.set_timing(False)
+        passes = {k: round(getattr(st, k) / 16, 4) for k in ("ms_cache_train", "ms_cache_infer", "ms_primary",
+                                                              "ms_extend", "ms_shadow", "ms_shade", "ms_total")}
+        cache.close()
+        return curve, passes
 
     def time_to(curve, target):
         # first checkpoint at or below target, log-log interpolation between checkpoints
@@ -523,21 +540,37 @@ def run_cache_experiment(args, world, rank, local, dist):
                 k0, ms0, r0 = curve[i - 1]
                 u = (np.log(r0) - np.log(target)) / (np.log(r0) - np.log(r))
                 return float(np.exp(np.log(ms0) + u * (np.log(ms) - np.log(ms0))))
-        # beyond the last checkpoint: extrapolate plain Monte Carlo, RMSE ~ t^-1/2
-        k, ms, r = curve[-1]
-        return float(ms * (r / target) ** 2)
+        return None  # not reached within the run
 
-    best_l = min(r for _, _, r in curve_l)
-    target = float(max(best_l * 1.02, 0.004))
-    tp, tl = time_to(curve_p, target), time_to(curve_l, target)
-    out = {"metric": "GPU ms to target RMSE: learned radiance cache vs plain path tracing", "unit": "ms",
+    curves = {}
+    for qv in (1, 0):
+        curves[qv] = learned_curve(qv)
+    targets = (0.02, 0.01, 0.007, 0.005)
+    table = {}
+    for t in targets:
+        row = {"plain_ms": time_to(curve_p, t)}
+        for qv in (1, 0):
+            tl = time_to(curves[qv][0], t)
+            row[f"learned_q{qv}_ms"] = tl
+            row[f"speedup_q{qv}"] = (row["plain_ms"] / tl) if (tl and row["plain_ms"]) else None
+        table[str(t)] = row
+    target = 0.01
+    best = max((1, 0), key=lambda qv: table[str(target)][f"speedup_q{qv}"] or 0.0)
+    tl = table[str(target)][f"learned_q{best}_ms"]
+    tp = table[str(target)]["plain_ms"]
+    out = {"metric": "GPU ms to RMSE 0.01: learned radiance cache vs plain path tracing", "unit": "ms",
            "value": tl, "higher_is_better": False, "target_rmse": target,
-           "plain_ms": tp, "learned_ms": tl, "speedup": tp / tl if tl > 0 else None,
+           "plain_ms": tp, "learned_ms": tl, "speedup": (tp / tl) if (tl and tp) else None,
+           "learned_query_vertex": best, "targets": table,
            "config": {"workload": "heightfield_boxes_1080p_radiance_cache", "width": W, "height": H,
                       "triangles": mesh.tri_count, "plain": PLAIN, "cache": "16 levels x 2 features, 2^19 entries, "
-                      "4x64 ReLU MLP, 65536 training paths x 4 Adam steps per frame, paths end at the first bounce",
+                      "4x64 ReLU MLP, 65536 training paths x 4 Adam steps per frame; the cache learns indirect "
+                      "radiance, shadow rays give direct light; query_vertex 1 = paths end at the first bounce's "
+                      "hit, 0 = at the primary hit",
                       "reference": f"{ref_frames} frames of 1-spp plain path tracing ({ref_s:.1f} s)"},
-           "reference_check": ref_check, "curve_plain": curve_p, "curve_learned": curve_l,
+           "reference_check": ref_check, "curve_plain": curve_p,
+           "curve_learned_q1": curves[1][0], "passes_q1": curves[1][1],
+           "curve_learned_q0": curves[0][0], "passes_q0": curves[0][1],
            "device_status": ctx.status()}
     print(json.dumps(out))
 

@@ -386,7 +386,11 @@ typedef struct mrt_cache_config {
     uint32_t train_paths;   /* training paths per frame (65536)            */
     uint32_t train_steps;   /* optimiser steps per frame (4)               */
     uint32_t train_bounces; /* bounce limit of the training paths (8)      */
-    uint32_t pad;
+    uint32_t query_vertex;  /* where paths end in the cache: 1 = at the hit
+                               of the first diffuse bounce (default), 0 = at
+                               the primary hit.  The cache learns indirect
+                               outgoing radiance; every vertex's direct
+                               light comes from its shadow ray            */
 } mrt_cache_config;
 typedef struct mrt_cache mrt_cache;
 int mrt_cuda_cache_create(mrt_ctx* ctx, const mrt_cache_config* cfg, mrt_cache** out);
@@ -414,10 +418,13 @@ int mrt_cuda_cache_params(mrt_ctx* ctx, mrt_cache* cache, int which, float* host
 /* One frame of cache-terminated path tracing (replaces the secondary pass):
  * trains the cache on cfg.train_paths fresh paths from this frame's camera
  * (cfg.train_steps Adam steps), then per pixel traces the primary hit's
- * shadow ray and one diffuse bounce and ends the path in the cache at the
- * bounce's hit: color += throughput x cache(x1, n1, -d1).  Same g-buffer,
+ * shadow ray and, with query_vertex = 1, one diffuse bounce and that hit's
+ * shadow ray, and ends the path in the cache:
+ *   query_vertex 1: color = direct(x0) + throughput x (direct(x1) + cache(x1, n1, -d1))
+ *   query_vertex 0: color = direct(x0) + cache(x0, n0, -d0)
+ * where cache() is the learned indirect outgoing radiance.  Same g-buffer,
  * parameters and output as mrt_cuda_secondary_rays (max_bounces is
- * ignored: paths end at the first bounce). */
+ * ignored). */
 int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
                          const mrt_gbuffer* gbuffer, const mrt_camera_consts* consts,
                          const mrt_trace_params* params, float* color, int train, void* stream);

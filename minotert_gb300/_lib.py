@@ -76,7 +76,7 @@ class Tuning(C.Structure):
 class CacheConfig(C.Structure):
     _fields_ = [("log2_table", C.c_uint32), ("base_res", C.c_float), ("max_res", C.c_float), ("lr_grid", C.c_float),
                 ("lr_mlp", C.c_float), ("seed", C.c_uint32), ("train_paths", C.c_uint32), ("train_steps", C.c_uint32),
-                ("train_bounces", C.c_uint32), ("pad", C.c_uint32)]
+                ("train_bounces", C.c_uint32), ("query_vertex", C.c_uint32)]
 
 
 class DeviceInfo(C.Structure):

@@ -16,6 +16,7 @@ def default_config(**kw) -> CacheConfig:
     c.log2_table, c.base_res, c.max_res = 19, 16.0, 2048.0
     c.lr_grid, c.lr_mlp = 1e-2, 1e-3
     c.seed, c.train_paths, c.train_steps, c.train_bounces = 1, 65536, 4, 8
+    c.query_vertex = 1
     for k, v in kw.items():
         setattr(c, k, v)
     return c

@@ -729,12 +729,30 @@ int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
         ctx->launches++;                                                                                 \
     } while (0)
     MRT_CK(cudaMemsetAsync(wb.counters, 0, kCntSlots * sizeof(uint32_t), s));
-    MRT_LAUNCH(3, 0, launch_shade_primary(scene->dev, fp, *gbuffer, tp, bn, wb, 0, ctx->d_status, s));
-    if (nee) MRT_LAUNCH(2, 0, launch_trace_shadow(scene->dev, wb, tp, 0, tblocks, ctx->d_status, ctx->counters, dyn_sh, s));
-    MRT_LAUNCH(1, 1, launch_trace_ext(scene->dev, wb, 1, tblocks, ctx->d_status, ctx->counters, dyn, s));
-    MRT_LAUNCH(3, 1, launch_cache_query(scene->dev, tp, wb, q, pb, ctx->d_status, s));
-    MRT_LAUNCH(7, 1, cache_infer(cache, q, uint32_t(wb.cap), wb.counters + kCntExt + 1, pred, s));
-    MRT_LAUNCH(3, 1, launch_cache_apply(wb, pred, pb, s));
+    if (cache_query_vertex(cache) == 0u) {
+        // the cache supplies the indirect light at the primary hit
+        tp.max_bounces = 0;
+        MRT_LAUNCH(3, 0, launch_shade_primary(scene->dev, fp, *gbuffer, tp, bn, wb, 0, ctx->d_status, s));
+        if (nee)
+            MRT_LAUNCH(2, 0, launch_trace_shadow(scene->dev, wb, tp, 0, tblocks, ctx->d_status, ctx->counters, dyn_sh, s));
+        const uint32_t npix = W * H;
+        MRT_LAUNCH(3, 0, launch_cache_query_primary(scene->dev, fp, *gbuffer, q, pb, ctx->d_status, s));
+        MRT_LAUNCH(7, 0, cache_infer(cache, q, npix, nullptr, pred, s));
+        MRT_LAUNCH(3, 0, launch_cache_apply(wb, nullptr, npix, pred, pb, s));
+    } else {
+        // one diffuse bounce, then the cache supplies the indirect light at
+        // that hit; both hits' direct light comes from shadow rays
+        MRT_LAUNCH(3, 0, launch_shade_primary(scene->dev, fp, *gbuffer, tp, bn, wb, 0, ctx->d_status, s));
+        if (nee)
+            MRT_LAUNCH(2, 0, launch_trace_shadow(scene->dev, wb, tp, 0, tblocks, ctx->d_status, ctx->counters, dyn_sh, s));
+        MRT_LAUNCH(1, 1, launch_trace_ext(scene->dev, wb, 1, tblocks, ctx->d_status, ctx->counters, dyn, s));
+        MRT_LAUNCH(3, 1, launch_shade(scene->dev, tp, bn, wb, W, 1, ctx->d_status, s));
+        if (nee)
+            MRT_LAUNCH(2, 1, launch_trace_shadow(scene->dev, wb, tp, 1, tblocks, ctx->d_status, ctx->counters, dyn_sh, s));
+        MRT_LAUNCH(3, 1, launch_cache_query(scene->dev, tp, wb, q, pb, ctx->d_status, s));
+        MRT_LAUNCH(7, 1, cache_infer(cache, q, uint32_t(wb.cap), wb.counters + kCntExt + 1, pred, s));
+        MRT_LAUNCH(3, 1, launch_cache_apply(wb, wb.counters + kCntExt + 1, uint32_t(wb.cap), pred, pb, s));
+    }
     MRT_LAUNCH(3, 0, launch_tally(wb, s));
     MRT_LAUNCH(3, 0, launch_finalize(wb, color, 1, params->accumulate, params->frame_index, s));
 #undef MRT_LAUNCH

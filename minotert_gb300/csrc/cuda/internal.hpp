@@ -168,7 +168,11 @@ cudaError_t launch_cache_train_paths(const DevScene& sc, const FrameParams& fp, 
                                      uint32_t* count, uint32_t cap, uint32_t* status, cudaStream_t s);
 cudaError_t launch_cache_query(const DevScene& sc, const TraceParams& tp, const WaveBuffers& wb, float* q,
                                float4* pb, uint32_t* status, cudaStream_t s);
-cudaError_t launch_cache_apply(const WaveBuffers& wb, const float* pred, const float4* pb, cudaStream_t s);
+cudaError_t launch_cache_query_primary(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g, float* q,
+                                       float4* pb, uint32_t* status, cudaStream_t s);
+cudaError_t launch_cache_apply(const WaveBuffers& wb, const uint32_t* n_dev, uint32_t n_max, const float* pred,
+                               const float4* pb, cudaStream_t s);
+uint32_t cache_query_vertex(const mrt_cache* c);  // nrc.cu
 
 int trace_blocks_per_sm();  // occupancy of the traversal kernels
 

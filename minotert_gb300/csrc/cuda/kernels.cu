@@ -807,25 +807,27 @@ k_cache_train_paths(DevScene sc, FrameParams fp, TraceParams tp, uint32_t bounce
         d = nd;
     }
     if (st) atomicOr(status, st);
-    // suffix radiance, last vertex first
+    // suffix radiance, last vertex first; each vertex's sample is its
+    // indirect outgoing radiance (the suffix without its own direct light,
+    // which the frame adds exactly with a shadow ray)
     f3 next = escaped ? escape_radiance(tp, d) : f3{0.0f, 0.0f, 0.0f};
     for (int v = nv - 1; v >= 0; --v) {
         const float w = wcont[v];
-        const f3 L{nee[v].x + rho[v].x * w * next.x, nee[v].y + rho[v].y * w * next.y,
-                   nee[v].z + rho[v].z * w * next.z};
+        const f3 Li{rho[v].x * w * next.x, rho[v].y * w * next.y, rho[v].z * w * next.z};
         const uint32_t slot = atomicAdd(count, 1u);
         if (slot < cap) {
             for (int k = 0; k < 9; ++k) out_q[size_t(slot) * 9 + k] = qv[v][k];
-            out_t[size_t(slot) * 3 + 0] = L.x;
-            out_t[size_t(slot) * 3 + 1] = L.y;
-            out_t[size_t(slot) * 3 + 2] = L.z;
+            out_t[size_t(slot) * 3 + 0] = Li.x;
+            out_t[size_t(slot) * 3 + 1] = Li.y;
+            out_t[size_t(slot) * 3 + 2] = Li.z;
         }
-        next = L;
+        next = f3{nee[v].x + Li.x, nee[v].y + Li.y, nee[v].z + Li.z};
     }
 }
 
-// For each bounce-1 extension ray: escaped -> sky into the pixel; hit ->
-// the cache query row at the hit and (throughput, pixel) for the apply.
+// For each bounce-1 extension ray that hit: the cache query row at the hit
+// and (throughput, pixel) for the apply.  Escaped rays were shaded (sky) by
+// k_shade, which also sent the hit's direct-light shadow ray.
 __global__ void __launch_bounds__(kShadeBlock)
 k_cache_query(DevScene sc, TraceParams tp, WaveBuffers wb, float* q, float4* pb, uint32_t* status) {
     const uint32_t n = wb.counters[kCntExt + 1];
@@ -837,7 +839,6 @@ k_cache_query(DevScene sc, TraceParams tp, WaveBuffers wb, float* q, float4* pb,
         const f3 beta{pr.beta.x, pr.beta.y, pr.beta.z};
         float* row = q + size_t(i) * 9;
         if (h.x == kMiss) {
-            add_L(wb.L, pix, mul_rn(beta, escape_radiance(tp, f3{pr.d.x, pr.d.y, pr.d.z})));
             for (int k = 0; k < 9; ++k) row[k] = 0.0f;
             pb[i] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(pix));
         } else {
@@ -850,9 +851,32 @@ k_cache_query(DevScene sc, TraceParams tp, WaveBuffers wb, float* q, float4* pb,
     }
 }
 
+// For each primary hit: the cache query row at the hit (outgoing direction
+// toward the camera) with unit throughput; misses and the hit's direct light
+// were shaded by k_shade_primary.
 __global__ void __launch_bounds__(kShadeBlock)
-k_cache_apply(WaveBuffers wb, const float* pred, const float4* pb) {
-    const uint32_t n = wb.counters[kCntExt + 1];
+k_cache_query_primary(DevScene sc, FrameParams fp, mrt_gbuffer g, float* q, float4* pb, uint32_t* status) {
+    const uint32_t npix = fp.width * fp.height;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += gridDim.x * blockDim.x) {
+        float* row = q + size_t(i) * 9;
+        const uint32_t prim = g.visibility[i];
+        if (prim == kMiss) {
+            for (int k = 0; k < 9; ++k) row[k] = 0.0f;
+            pb[i] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(i));
+            continue;
+        }
+        f3 o, d;
+        primary_ray(fp, i % fp.width, i / fp.width, o, d);
+        const mrt_material m = load_mat(sc, prim, status);
+        cache_query_row(sc, ray_at(o, d, g.hit_t[i]), facing_normal(m, d), f3{-d.x, -d.y, -d.z}, row);
+        pb[i] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(i));
+    }
+}
+
+// L[pixel] += throughput x prediction for the first n_dev[0] (or n) rows.
+__global__ void __launch_bounds__(kShadeBlock)
+k_cache_apply(WaveBuffers wb, const uint32_t* n_dev, uint32_t n_max, const float* pred, const float4* pb) {
+    const uint32_t n = n_dev ? min(*n_dev, n_max) : n_max;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 b = pb[i];
         if (b.x == 0.0f && b.y == 0.0f && b.z == 0.0f) continue;
@@ -877,9 +901,17 @@ cudaError_t launch_cache_query(const DevScene& sc, const TraceParams& tp, const 
     return cudaGetLastError();
 }
 
-cudaError_t launch_cache_apply(const WaveBuffers& wb, const float* pred, const float4* pb, cudaStream_t s) {
-    const uint32_t b = uint32_t((wb.cap + kShadeBlock - 1) / kShadeBlock);
-    k_cache_apply<<<b < 4096 ? b : 4096, kShadeBlock, 0, s>>>(wb, pred, pb);
+cudaError_t launch_cache_query_primary(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g, float* q,
+                                       float4* pb, uint32_t* status, cudaStream_t s) {
+    const uint32_t b = (fp.width * fp.height + kShadeBlock - 1) / kShadeBlock;
+    k_cache_query_primary<<<b < 4096 ? b : 4096, kShadeBlock, 0, s>>>(sc, fp, g, q, pb, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cache_apply(const WaveBuffers& wb, const uint32_t* n_dev, uint32_t n_max, const float* pred,
+                               const float4* pb, cudaStream_t s) {
+    const uint32_t b = (n_max + kShadeBlock - 1) / kShadeBlock;
+    k_cache_apply<<<b < 4096 ? (b ? b : 1) : 4096, kShadeBlock, 0, s>>>(wb, n_dev, n_max, pred, pb);
     return cudaGetLastError();
 }
 

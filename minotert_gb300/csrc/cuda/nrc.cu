@@ -515,6 +515,8 @@ uint64_t splitmix(uint64_t& s) {
 } // namespace
 
 namespace mrt {
+uint32_t cache_query_vertex(const mrt_cache* c) { return c->cfg.query_vertex; }
+
 // Inference over device rows of 9 floats; with n_dev the row count is read
 // on the device (at most n).
 cudaError_t cache_infer(const mrt_cache* c, const float* q, uint32_t n, const uint32_t* n_dev, float* out,
@@ -594,6 +596,7 @@ int mrt_cuda_cache_create(mrt_ctx* ctx, const mrt_cache_config* cfg, mrt_cache**
     if (!ctx || !cfg || !out) return set_error(ctx, MRT_EINVAL, "cache_create: null argument");
     if (cfg->log2_table < 10 || cfg->log2_table > 24 || !(cfg->base_res >= 2.0f) || !(cfg->max_res >= cfg->base_res))
         return set_error(ctx, MRT_EINVAL, "cache_create: bad grid configuration");
+    if (cfg->query_vertex > 1u) return set_error(ctx, MRT_EINVAL, "cache_create: query_vertex must be 0 or 1");
     cudaSetDevice(ctx->device);
     mrt_cache* c = new (std::nothrow) mrt_cache;
     if (!c) return MRT_ENOMEM;

@@ -86,7 +86,8 @@ def _rmse(a, b):
     return float(np.sqrt(np.mean((a - b) ** 2)))
 
 
-def test_trained_cache_beats_plain_path_tracing_at_equal_frames(ctx, hf_workload, blue_noise):
+@pytest.mark.parametrize("query_vertex", [1, 0])
+def test_trained_cache_beats_plain_path_tracing_at_equal_frames(ctx, hf_workload, blue_noise, query_vertex):
     # 128x128 heightfield scene; reference: plain path tracer, 1024 frames of
     # 1 spp.  After 48 training frames, 8 frames of cache-terminated paths
     # must be closer to the reference than 8 frames of the plain tracer.
@@ -115,7 +116,8 @@ def test_trained_cache_beats_plain_path_tracing_at_equal_frames(ctx, hf_workload
 
     ref = accumulate(1024, plain, start=10000)
     plain8 = accumulate(8, plain, start=0)
-    cache = RadianceCache(ctx, default_config(train_paths=16384, train_steps=4, train_bounces=6),
+    cache = RadianceCache(ctx, default_config(train_paths=16384, train_steps=4, train_bounces=6,
+                                              query_vertex=query_vertex),
                           bounds=(mesh.lo, mesh.hi))
 
     def learned(train):
@@ -129,6 +131,6 @@ def test_trained_cache_beats_plain_path_tracing_at_equal_frames(ctx, hf_workload
     learned8 = accumulate(8, learned(True), start=0)
     assert ctx.status() == 0
     r_plain, r_learned = _rmse(plain8, ref), _rmse(learned8, ref)
-    print(f"RMSE after 8 frames: plain {r_plain:.4f}, learned {r_learned:.4f}")
+    print(f"RMSE after 8 frames: plain {r_plain:.4f}, learned (query vertex {query_vertex}) {r_learned:.4f}")
     assert np.isfinite(learned8).all()
     assert r_learned < r_plain
