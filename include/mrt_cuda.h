@@ -173,7 +173,9 @@ typedef struct mrt_trace_params {
     uint32_t rng_mode;     /* MRT_RNG_*                                      */
     uint32_t estimator;    /* MRT_EST_*                                      */
     uint32_t accumulate;   /* 0: write this call's mean; 1: fold it into the
-                              running mean with weight 1/(frame_index+1)     */
+                              running mean with weight 1/(frame_index+1)
+                              (frame_index 0 overwrites: the buffer's old
+                              contents are never read)                       */
     uint32_t frame_index;  /* frames already in the running mean             */
     uint32_t sort_rays;    /* 1: sort extension rays between bounces         */
     float    sun_dir[3];   /* unit vector toward the directional light       */

@@ -275,7 +275,7 @@ k_secondary_sphere(DevScene sc, FrameParams fp, mrt_gbuffer g, TraceParams tp, B
     const float ns = float(tp.samples);
     f3 mean{__fdiv_rn(acc.x, ns), __fdiv_rn(acc.y, ns), __fdiv_rn(acc.z, ns)};
     float* out = color + pi * 3;
-    if (accumulate) {
+    if (accumulate && frame_index > 0u) {  // frame 0 starts the mean: old contents are ignored
         const float w = float(frame_index + 1u);
         mean.x = __fadd_rn(out[0], __fdiv_rn(__fsub_rn(mean.x, out[0]), w));
         mean.y = __fadd_rn(out[1], __fdiv_rn(__fsub_rn(mean.y, out[1]), w));
@@ -581,7 +581,7 @@ k_finalize(WaveBuffers wb, float* color, uint32_t npix, uint32_t samples, uint32
     const float ns = float(samples);
     float m[3] = {__fdiv_rn(l.x, ns), __fdiv_rn(l.y, ns), __fdiv_rn(l.z, ns)};
     float* out = color + size_t(i) * 3;
-    if (accumulate) {
+    if (accumulate && frame_index > 0u) {  // frame 0 starts the mean: old contents are ignored
         const float w = float(frame_index + 1u);
         for (int k = 0; k < 3; ++k) m[k] = __fadd_rn(out[k], __fdiv_rn(__fsub_rn(m[k], out[k]), w));
     }

@@ -1024,7 +1024,7 @@ void orc_secondary_spheres(const float* spheres, uint32_t ns, const Consts* c, u
             float* out = color + 3 * pi;
             float m[3] = {acc.x / nsf, acc.y / nsf, acc.z / nsf};
             for (int k = 0; k < 3; ++k) {
-                if (p->accumulate) m[k] = out[k] + (m[k] - out[k]) / float(p->frame_index + 1u);
+                if (p->accumulate && p->frame_index > 0u) m[k] = out[k] + (m[k] - out[k]) / float(p->frame_index + 1u);
                 out[k] = m[k];
             }
         }
@@ -1129,7 +1129,7 @@ uint32_t orc_pathtrace(const Node* nodes, uint32_t nn, const Tri* tris, uint32_t
             }
             float* out = color + 3 * pi;
             for (int k = 0; k < 3; ++k) {
-                if (p->accumulate) m[k] = out[k] + (m[k] - out[k]) / float(p->frame_index + 1u);
+                if (p->accumulate && p->frame_index > 0u) m[k] = out[k] + (m[k] - out[k]) / float(p->frame_index + 1u);
                 out[k] = m[k];
             }
             rc.primary++;
