@@ -579,8 +579,9 @@ def run_denoise_experiment(args, world, rank, local, dist):
     """GPU milliseconds to RMSE 0.01 on a held-out 1920x1080 frame: plain
     accumulation vs the CNN denoiser applied to the accumulated image.  The
     denoiser is trained first on pairs the path tracer renders itself:
-    seeded heightfield + boxes scenes at random cameras, 128x128 crops,
-    1-spp inputs and 256-spp targets."""
+    seeded heightfield + boxes scenes at random cameras rendered at
+    1920x1080, 1-spp inputs and 256-spp targets, 16 random 128x128 crops
+    per scene."""
     from minotert_gb300 import build as _build
     _build.build()
     from minotert_gb300 import scene
@@ -613,25 +614,39 @@ def run_denoise_experiment(args, world, rank, local, dist):
                                                              True, f), color=col, stream=stream)
         return col, gb
 
-    # ---- training data
+    # ---- training data: 1-spp frames and TSPP-spp targets rendered at the
+    # evaluation resolution (so a pixel covers the same scene area), cut into
+    # K random 128x128 crops per scene, stored in shuffled order
     t0 = time.perf_counter()
-    S, CW, TSPP = int(os.environ.get("MRT_DENOISE_SCENES", "160")), 128, 256
-    feats = ctx.alloc(S * CW * CW * 16 * 2)
-    targets = ctx.alloc(S * CW * CW * 3 * 4)
-    from minotert_gb300._lib import lib, ptr
+    S, K, CW, TSPP = int(os.environ.get("MRT_DENOISE_SCENES", "48")), 16, 128, 256
+    FW, FH = 1920, 1080
+    N = S * K
+    feats = ctx.alloc(N * CW * CW * 16 * 2)
+    targets = ctx.alloc(N * CW * CW * 3 * 4)
+    f_full = ctx.alloc(FW * FH * 16 * 2)
+    from minotert_gb300._lib import lib
     import ctypes as C
-    for s in range(S):
-        rng = np.random.default_rng(1000 + s)
-        mesh = scene.heightfield_boxes(2000 + s, 64, 32)
+    slot = np.random.default_rng(3).permutation(N)
+    d2d = lib().mrt_cuda_copy_d2d
+    for s_ in range(S):
+        rng = np.random.default_rng(1000 + s_)
+        mesh = scene.heightfield_boxes(2000 + s_, 64, 32)
         ds = scene.DeviceScene.triangles(ctx, mesh)
         pt = Pathtracer(ctx, ds, full_gbuffer=False)
-        cam = camera(rng, CW, CW)
-        noisy, gb = render(pt, cam, CW, CW, 1, 50_000 + s)
-        den.features(ds, gb, noisy, float(np.linalg.norm(mesh.hi - mesh.lo)),
-                     feats.ptr + s * CW * CW * 16 * 2, stream)
-        ref, _ = render(pt, cam, CW, CW, TSPP, 90_000 + s * TSPP)
-        ctx.check(lib().mrt_cuda_copy_d2d(ctx.handle, C.c_void_p(targets.ptr + s * CW * CW * 12),
-                                          C.c_void_p(ref.ptr), CW * CW * 12, C.c_void_p(stream)), "d2d")
+        cam = camera(rng, FW, FH)
+        noisy, gb = render(pt, cam, FW, FH, 1, 50_000 + s_)
+        den.features(ds, gb, noisy, float(np.linalg.norm(mesh.hi - mesh.lo)), f_full, stream)
+        ref, _ = render(pt, cam, FW, FH, TSPP, 90_000 + s_ * TSPP)
+        for k in range(K):
+            y0 = 4 * int(rng.integers(0, (FH - CW) // 4 + 1))
+            x0 = 4 * int(rng.integers(0, (FW - CW) // 4 + 1))
+            i = int(slot[s_ * K + k])
+            for r in range(CW):
+                src = (y0 + r) * FW + x0
+                d2d(ctx.handle, C.c_void_p(feats.ptr + (i * CW * CW + r * CW) * 32), C.c_void_p(f_full.ptr + src * 32),
+                    CW * 32, C.c_void_p(stream))
+                d2d(ctx.handle, C.c_void_p(targets.ptr + (i * CW * CW + r * CW) * 12), C.c_void_p(ref.ptr + src * 12),
+                    CW * 12, C.c_void_p(stream))
         ctx.sync(stream)
     data_s = time.perf_counter() - t0
 
@@ -639,12 +654,11 @@ def run_denoise_experiment(args, world, rank, local, dist):
     t1 = time.perf_counter()
     steps, B = int(os.environ.get("MRT_DENOISE_STEPS", "3000")), 8
     losses = []
-    order = np.random.default_rng(7).permutation(S)
     ev0, ev1 = ctx.event(), ctx.event()
     ctx.record(ev0, stream)
     for k in range(steps):
-        i0 = int(order[(k * B) % (S - B + 1)])
-        lr = 1e-3 if k < steps * 0.7 else 2.5e-4
+        i0 = (k * B) % (N - B + 1)
+        lr = 5e-4 if k < steps * 0.7 else 1e-4
         want = (k % 250 == 0) or k == steps - 1
         loss = den.train_step(feats.ptr + i0 * CW * CW * 16 * 2, targets.ptr + i0 * CW * CW * 12, B, CW, CW, lr=lr,
                               want_loss=want, stream=stream)
@@ -705,7 +719,8 @@ def run_denoise_experiment(args, world, rank, local, dist):
     res = {"metric": "GPU ms to RMSE 0.01: CNN denoiser vs plain accumulation", "unit": "ms", "value": td,
            "higher_is_better": False, "target_rmse": target, "plain_ms": tp, "denoiser_ms": td,
            "speedup": tp / td if td > 0 else None, "curve_plain": curve_plain, "curve_denoised": curve_den,
-           "training": {"scenes": S, "crop": CW, "target_spp": TSPP, "steps": steps, "batch": B,
+           "training": {"scenes": S, "crops_per_scene": K, "render": [FW, FH], "crop": CW, "target_spp": TSPP,
+                        "steps": steps, "batch": B,
                         "gpu_train_ms": train_ms, "wall_train_s": train_s, "data_gen_s": data_s, "loss": losses},
            "config": {"workload": "heightfield_boxes_1080p_denoiser", "width": W, "height": H,
                       "reference": "4096 frames of 1-spp plain path tracing", "plain": SET},

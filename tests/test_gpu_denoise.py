@@ -95,3 +95,35 @@ def test_denoiser_features_from_a_frame(ctx, hf_workload, blue_noise):
     out = ctx.alloc(wl.width * wl.height * 12)
     d.infer(feats, 1, wl.width, wl.height, out)
     assert np.isfinite(out.download(np.float32, (wl.height, wl.width, 3))).all()
+
+
+def test_denoiser_inference_is_size_and_batch_consistent(ctx):
+    # a pixel's output depends only on the inputs within the network's
+    # receptive field (about 20 pixels), so the interior of a 128x128 crop
+    # taken at an offset that is a multiple of 4 (the pooling alignment) must
+    # equal the same pixels of the full 1920x1080 image, and an image must
+    # give the same output alone and inside a batch
+    d = Denoiser(ctx, seed=5)
+    rng = np.random.default_rng(12)
+    W, H = 1920, 1080
+    x = np.zeros((H, W, 16), np.float32)
+    x[..., :10] = rng.uniform(0, 1, (H, W, 10))
+    xb = to_bf16_bits(x)
+    d_x = ctx.to_device(xb)
+    d_o = ctx.alloc(W * H * 12)
+    d.infer(d_x, 1, W, H, d_o)
+    full = d_o.download(np.float32, (H, W, 3))
+    for (y0, x0) in [(0, 0), (476, 900), (952, 1792)]:
+        crop = np.ascontiguousarray(xb[y0:y0 + 128, x0:x0 + 128])
+        c_x, c_o = ctx.to_device(crop), ctx.alloc(128 * 128 * 12)
+        d.infer(c_x, 1, 128, 128, c_o)
+        part = c_o.download(np.float32, (128, 128, 3))
+        inner = (slice(32, 96), slice(32, 96))
+        assert np.array_equal(part[inner], full[y0 + 32:y0 + 96, x0 + 32:x0 + 96]), (y0, x0)
+    two = np.ascontiguousarray(np.stack([xb[:128, :128], xb[128:256, :128]]))
+    t_x, t_o = ctx.to_device(two), ctx.alloc(2 * 128 * 128 * 12)
+    d.infer(t_x, 2, 128, 128, t_o)
+    pair = t_o.download(np.float32, (2, 128, 128, 3))
+    one_x, one_o = ctx.to_device(np.ascontiguousarray(xb[128:256, :128])), ctx.alloc(128 * 128 * 12)
+    d.infer(one_x, 1, 128, 128, one_o)
+    assert np.array_equal(pair[1], one_o.download(np.float32, (128, 128, 3)))
