@@ -451,6 +451,35 @@ __global__ void k_adam(float* p, float* m, float* v, float* grad, __half* p16, _
     }
 }
 
+// Adam on the grid features, four at a time, lazily: a group whose four
+// gradients are all zero (no training sample touched those corners this
+// step) keeps its parameters and moments, so a step reads the whole
+// gradient array but only the touched part of the rest.
+__global__ void k_adam_grid4(float4* p, float4* m, float4* v, float4* grad, __half2* p16, uint32_t n4, float lr,
+                             float b1, float b2, float eps, float bc1, float bc2) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n4) return;
+    const float4 g = grad[i];
+    if (g.x == 0.0f && g.y == 0.0f && g.z == 0.0f && g.w == 0.0f) return;
+    grad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float4 mi = m[i], vi = v[i], pi = p[i];
+    const float gs[4] = {g.x, g.y, g.z, g.w};
+    float* ms = &mi.x;
+    float* vs = &vi.x;
+    float* ps = &pi.x;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        ms[k] = b1 * ms[k] + (1.0f - b1) * gs[k];
+        vs[k] = b2 * vs[k] + (1.0f - b2) * gs[k] * gs[k];
+        ps[k] = ps[k] - lr * (ms[k] / bc1) / (sqrtf(vs[k] / bc2) + eps);
+    }
+    m[i] = mi;
+    v[i] = vi;
+    p[i] = pi;
+    p16[2 * i] = __floats2half2_rn(pi.x, pi.y);
+    p16[2 * i + 1] = __floats2half2_rn(pi.z, pi.w);
+}
+
 } // namespace
 
 // ============================================================ host object
@@ -724,9 +753,10 @@ int mrt_cuda_cache_train_step(mrt_ctx* ctx, mrt_cache* c, const float* queries, 
         const float bc1 = 1.0f - std::pow(b1, float(c->step)), bc2 = 1.0f - std::pow(b2, float(c->step));
         k_adam<<<(kWeights + 255) / 256, 256, 0, s>>>(c->w, c->wm, c->wv, c->wg, c->w16, c->wt16, kWeights,
                                                       c->cfg.lr_mlp, b1, b2, eps, bc1, bc2);
-        const uint32_t gn = c->grid_entries * 2u;
-        k_adam<<<(gn + 255) / 256, 256, 0, s>>>(c->gp, c->gm, c->gv, c->gg, reinterpret_cast<__half*>(c->g16),
-                                                nullptr, gn, c->cfg.lr_grid, b1, b2, eps, bc1, bc2);
+        const uint32_t gn4 = c->grid_entries / 2u;  // 2 features per entry, 4 floats per group
+        k_adam_grid4<<<(gn4 + 255) / 256, 256, 0, s>>>(
+            reinterpret_cast<float4*>(c->gp), reinterpret_cast<float4*>(c->gm), reinterpret_cast<float4*>(c->gv),
+            reinterpret_cast<float4*>(c->gg), c->g16, gn4, c->cfg.lr_grid, b1, b2, eps, bc1, bc2);
         ctx->launches += 2;
     }
     if (cudaGetLastError() != cudaSuccess) return set_error(ctx, MRT_ECUDA, "train: launch failed");
