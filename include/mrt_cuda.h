@@ -434,8 +434,8 @@ int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
 /* ---- learned denoiser (new; the reference's denoiser is the joint
  *      bilateral filter of src/gpu/denoise/bilateral.comp) --------------
  * A 3-level U-Net (3x3 convolutions, 32/64/128 channels, skip
- * connections) over 16-channel BF16 NHWC features: log(1 + radiance),
- * albedo, normal, depth, zero padding.  Forward on the tensor cores (BF16,
+ * connections) over 16-channel BF16 NHWC features: log(1 + radiance /
+ * albedo), albedo, normal, depth, zero padding.  Forward on the tensor cores (BF16,
  * FP32 accumulate); training backward in FP32; Adam.  The network predicts
  * a correction to the input's log(1 + radiance), with an L1 loss.  Width and height must be multiples
  * of 4. */

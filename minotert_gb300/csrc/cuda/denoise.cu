@@ -9,10 +9,12 @@
 //   in(16) -> e0a(32) -> e0b(32)=S0 -> pool -> e1a(64) -> e1b(64)=S1 -> pool
 //   -> e2a(128) -> e2b(128) -> [up ++ S1](192) -> d1a(64) -> d1b(64)
 //   -> [up ++ S0](96) -> d0a(32) -> d0b(32) -> out(16, 3 used)
-// 3x3 convolutions with bias, ReLU except the output layer.  The network
-// predicts a correction to the input's log(1 + radiance) (a residual: an
-// untrained network passes the noisy image through); the loss is L1 in
-// that space.  The output layer starts at a tenth of the He scale.
+// 3x3 convolutions with bias, ReLU except the output layer.  Radiance is
+// demodulated by the surface albedo (the noise-free texture need not be
+// learned) and the network predicts a correction to the input's
+// log(1 + radiance / albedo) (a residual: an untrained network passes the
+// noisy image through); the loss is L1 in that space.  The output layer
+// starts at a tenth of the He scale.
 //
 // Forward: implicit-GEMM convolution on the tensor cores (mma.sync
 // m16n8k16, BF16 in, FP32 accumulate): a warp computes 16 consecutive
@@ -253,8 +255,16 @@ __global__ void k_pool_bwd(const float* gout, float* gin, int n, int h, int w, i
     }
 }
 
-// L1 loss in log(1 + radiance) space on channels 0..2: the network predicts
-// a correction added to the input's own log(1 + radiance) (features 0..2)
+// Albedo a pixel's radiance is divided by before denoising (features 3..5
+// as stored, BF16); sky pixels and black surfaces (albedo 0) use 1.
+__device__ __forceinline__ float demod_albedo(const bf16* feat, size_t p, int k) {
+    const float a = __bfloat162float(feat[p * 16 + 3 + k]);
+    return a > 0.0f ? a : 1.0f;
+}
+
+// L1 loss in log(1 + irradiance) space on channels 0..2 (irradiance =
+// radiance / albedo): the network predicts a correction added to the
+// input's own log(1 + irradiance) (features 0..2)
 __global__ void k_l1_loss(const bf16* y, const bf16* feat, const float* target, size_t pixels, float* dy,
                           float* loss) {
     float l = 0.0f;
@@ -263,7 +273,7 @@ __global__ void k_l1_loss(const bf16* y, const bf16* feat, const float* target, 
         for (int k = 0; k < 16; ++k) dy[p * 16 + k] = 0.0f;
         for (int k = 0; k < 3; ++k) {
             const float pred = __bfloat162float(y[p * 16 + k]) + __bfloat162float(feat[p * 16 + k]);
-            const float d = pred - log1pf(fmaxf(target[p * 3 + k], 0.0f));
+            const float d = pred - log1pf(fmaxf(target[p * 3 + k], 0.0f) / demod_albedo(feat, p, k));
             l += fabsf(d);
             dy[p * 16 + k] = (d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f)) * inv;
         }
@@ -286,36 +296,40 @@ __global__ void k_adam_bf16(float* p, float* m, float* v, float* g, bf16* p16, s
     }
 }
 
-// Input features of one frame: log(1 + radiance) (3), albedo (3), facing
-// normal (3), hit distance / scene diagonal (1), zeros to 16 channels.
+// Input features of one frame: log(1 + radiance / albedo) (3), albedo (3),
+// normal (3), hit distance / scene diagonal (1), zeros to 16 channels.  The
+// albedo divides out as stored in BF16, so decoding multiplies by exactly
+// the same value.
 __global__ void k_features(DevScene sc, const float* color, const uint32_t* vis, const float* hit_t, int w, int h,
                            float inv_diag, bf16* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w * h) return;
     float f[16];
     for (int k = 0; k < 16; ++k) f[k] = 0.0f;
-    for (int k = 0; k < 3; ++k) f[k] = log1pf(fmaxf(color[size_t(i) * 3 + k], 0.0f));
+    float a[3] = {1.0f, 1.0f, 1.0f};
     const uint32_t prim = vis[i];
     if (prim != kMiss && prim < sc.mat_count) {
         const mrt_material m = sc.mats[prim];
-        f[3] = float(m.albedo_rgba8 & 0xFFu) / 255.0f;
-        f[4] = float((m.albedo_rgba8 >> 8) & 0xFFu) / 255.0f;
-        f[5] = float((m.albedo_rgba8 >> 16) & 0xFFu) / 255.0f;
+        for (int k = 0; k < 3; ++k) {
+            f[3 + k] = __bfloat162float(__float2bfloat16_rn(float((m.albedo_rgba8 >> (8 * k)) & 0xFFu) / 255.0f));
+            if (f[3 + k] > 0.0f) a[k] = f[3 + k];
+        }
         f[6] = m.normal[0]; f[7] = m.normal[1]; f[8] = m.normal[2];
         f[9] = fminf(hit_t[i] * inv_diag, 4.0f);
     } else {
         f[9] = 4.0f;
     }
+    for (int k = 0; k < 3; ++k) f[k] = log1pf(fmaxf(color[size_t(i) * 3 + k], 0.0f) / a[k]);
     for (int k = 0; k < 16; k += 2)
         *reinterpret_cast<__nv_bfloat162*>(out + size_t(i) * 16 + k) = __floats2bfloat162_rn(f[k], f[k + 1]);
 }
 
-// radiance = exp(input log(1 + radiance) + predicted correction) - 1
+// radiance = albedo x (exp(input log(1 + irradiance) + correction) - 1)
 __global__ void k_decode(const bf16* y, const bf16* feat, size_t pixels, float* out) {
     for (size_t p = blockIdx.x * size_t(blockDim.x) + threadIdx.x; p < pixels; p += size_t(gridDim.x) * blockDim.x)
         for (int k = 0; k < 3; ++k) {
             const float v = __bfloat162float(y[p * 16 + k]) + __bfloat162float(feat[p * 16 + k]);
-            out[p * 3 + k] = expm1f(fmaxf(v, 0.0f));
+            out[p * 3 + k] = expm1f(fmaxf(v, 0.0f)) * demod_albedo(feat, p, k);
         }
 }
 

@@ -101,8 +101,10 @@ def loss_and_grads(params, x, target, round_bf16=True):
     wsq = [bf16(w) for w in ws] if round_bf16 else ws
     acts, ins, out = forward(params, x, round_bf16)
     n = out.shape[0] * out.shape[1] * out.shape[2] * 3
-    # residual: the prediction is the input's log(1 + radiance) plus the output
-    d = out[..., :3] + x[..., :3] - np.log1p(np.maximum(target, 0.0))
+    # residual on demodulated radiance: the prediction is the input's
+    # log(1 + radiance / albedo) plus the output (albedo 0 counts as 1)
+    a = np.where(x[..., 3:6] > 0, x[..., 3:6], 1.0)
+    d = out[..., :3] + x[..., :3] - np.log1p(np.maximum(target, 0.0) / a)
     loss = np.abs(d).sum() / n
     g = [None] * 11
     g[10] = np.zeros_like(out)

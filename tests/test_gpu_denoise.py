@@ -29,7 +29,8 @@ def test_denoiser_forward_matches_oracle(ctx):
     params = d.params(0).astype(np.float64)
     _, _, out = cnn.forward(params, from_bf16_bits(xb).astype(np.float64).reshape(2, 16, 24, 16))
     xin = from_bf16_bits(xb).astype(np.float64).reshape(2, 16, 24, 16)
-    ref = np.expm1(np.maximum(out[..., :3] + xin[..., :3], 0.0))
+    alb = np.where(xin[..., 3:6] > 0, xin[..., 3:6], 1.0)
+    ref = np.expm1(np.maximum(out[..., :3] + xin[..., :3], 0.0)) * alb
     assert np.all(np.isfinite(y))
     err = np.abs(y - ref)
     assert np.max(err) < 3e-2 * max(1.0, np.abs(ref).max()), np.max(err)
@@ -88,9 +89,12 @@ def test_denoiser_features_from_a_frame(ctx, hf_workload, blue_noise):
     img = col.download(np.float32, (wl.height, wl.width, 3))
     g = gb.download()
     hit = g["visibility"] != 0xFFFFFFFF
-    assert np.allclose(f[..., :3], np.log1p(img), atol=2e-2 * np.log1p(img).max())
     alb = mesh.albedo()[g["visibility"][hit]]
     assert np.allclose(f[hit][:, 3:6], alb, atol=1e-2)
+    a = np.ones_like(img)
+    a[hit] = f[hit][:, 3:6]
+    ir = np.log1p(img / a)
+    assert np.allclose(f[..., :3], ir, atol=2e-2 * ir.max())
     assert np.all(f[..., 10:] == 0)
     out = ctx.alloc(wl.width * wl.height * 12)
     d.infer(feats, 1, wl.width, wl.height, out)
