@@ -763,6 +763,56 @@ def run_reference(args, world, rank, local, dist):
         dist.destroy_process_group()
 
 
+def run_network_kernels(args, world, rank, local, dist):
+    """Inference time of the two networks at 1920x1080 with random weights
+    and inputs: the CNN denoiser on one frame of features and the radiance
+    cache on 2,073,600 queries (CUDA events, --steps timed runs after
+    --warmup).  The driver for the network-kernel ncu captures."""
+    from minotert_gb300 import build as _build
+    _build.build()
+    from minotert_gb300._lib import Context
+    from minotert_gb300.cache import RadianceCache, default_config
+    from minotert_gb300.denoiser import Denoiser, to_bf16_bits
+
+    ctx = Context(local)
+    W, H = 1920, 1080
+    rng = np.random.default_rng(1)
+    x = np.zeros((H, W, 16), np.float32)
+    x[..., :10] = rng.uniform(0, 1, (H, W, 10))
+    den = Denoiser(ctx, seed=3)
+    dx, do = ctx.to_device(to_bf16_bits(x)), ctx.alloc(W * H * 12)
+    n = W * H
+    q = np.zeros((n, 9), np.float32)
+    q[:, :3] = rng.uniform(0, 1, (n, 3))
+    for a in (3, 6):
+        v = rng.normal(size=(n, 3))
+        q[:, a:a + 3] = v / np.linalg.norm(v, axis=1, keepdims=True)
+    cache = RadianceCache(ctx, default_config(), bounds=(np.zeros(3, np.float32), np.ones(3, np.float32)))
+    dq, dout = ctx.to_device(q), ctx.alloc(n * 12)
+    a, b = ctx.event(), ctx.event()
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        ts = []
+        for _ in range(args.steps):
+            ctx.record(a)
+            fn()
+            ctx.record(b)
+            ctx.sync()
+            ts.append(ctx.elapsed_ms(a, b))
+        return float(np.median(ts))
+
+    den_ms = timed(lambda: den.infer(dx, 1, W, H, do))
+    cache_ms = timed(lambda: cache.infer(dq, n, dout))
+    flop = 2 * 9 * sum((ca + cb) * co * (W * H) // (4 ** sc) for ca, cb, co, ups, relu, sc in
+                       __import__("minotert_gb300.denoiser", fromlist=["TOPOLOGY"]).TOPOLOGY)
+    print(json.dumps({"metric": "network inference ms at 1920x1080", "unit": "ms", "denoiser_ms": den_ms,
+                      "denoiser_tflops": flop / den_ms / 1e9, "denoiser_gflop": flop / 1e9,
+                      "cache_ms_2073600_queries": cache_ms, "cache_mqueries_s": n / cache_ms / 1e3,
+                      "steps": args.steps, "warmup": args.warmup, "data": "random weights and inputs"}))
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -770,7 +820,8 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["icospheres_1080p", "batched64", "radiance_cache", "denoiser"],
+    ap.add_argument("--workload", choices=["icospheres_1080p", "batched64", "radiance_cache", "denoiser",
+                                           "network_kernels"],
                     default="icospheres_1080p")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
@@ -783,6 +834,8 @@ def main(argv=None):
         run_cache_experiment(args, world, rank, local, dist)
     elif args.workload == "denoiser":
         run_denoise_experiment(args, world, rank, local, dist)
+    elif args.workload == "network_kernels":
+        run_network_kernels(args, world, rank, local, dist)
     else:
         run_mine(args, world, rank, local, dist)
 
