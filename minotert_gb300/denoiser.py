@@ -29,6 +29,10 @@ class Denoiser:
     def handle(self):
         return self._h
 
+    def set_tcgen05(self, enable: bool):
+        """Forward convolutions on tcgen05 (default) or on mma.sync."""
+        self.ctx.check(lib().mrt_cuda_denoiser_set_tcgen05(self._h, int(enable)), "denoiser_set_tcgen05")
+
     def features(self, scene, gbuffer, d_color, diagonal: float, d_features, stream=None):
         self.ctx.check(lib().mrt_cuda_denoiser_features(self.ctx.handle, scene.handle, C.byref(gbuffer.c()),
                                                         ptr(d_color), float(diagonal), ptr(d_features),

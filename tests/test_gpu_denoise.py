@@ -131,3 +131,30 @@ def test_denoiser_inference_is_size_and_batch_consistent(ctx):
     one_x, one_o = ctx.to_device(np.ascontiguousarray(xb[128:256, :128])), ctx.alloc(128 * 128 * 12)
     d.infer(one_x, 1, 128, 128, one_o)
     assert np.array_equal(pair[1], one_o.download(np.float32, (128, 128, 3)))
+
+
+@pytest.mark.parametrize("shape", [(2, 16, 24), (1, 64, 200), (1, 540, 960)])
+def test_denoiser_tcgen05_matches_mma_sync(ctx, shape):
+    # the same network on the two tensor-core paths: tcgen05 (accumulators
+    # in tensor memory, operands staged in shared memory) and mma.sync;
+    # only the FP32 summation order differs, so layer outputs agree to BF16
+    # rounding and the decoded radiance to ~1 %
+    n, h, w = shape
+    d = Denoiser(ctx, seed=7)
+    rng = np.random.default_rng(3)
+    x = np.zeros((n, h, w, 16), np.float32)
+    x[..., :10] = rng.uniform(0, 1, (n, h, w, 10))
+    xb = to_bf16_bits(x)
+    d_x = ctx.to_device(xb)
+    outs = []
+    for tc in (True, False):
+        d.set_tcgen05(tc)
+        d_o = ctx.alloc(n * h * w * 12)
+        d.infer(d_x, n, w, h, d_o)
+        outs.append(d_o.download(np.float32, (n, h, w, 3)))
+    assert ctx.status() == 0
+    a, b = outs
+    assert np.isfinite(a).all()
+    err = np.abs(a - b)
+    assert err.max() < 3e-2 * max(1.0, np.abs(b).max()), err.max()
+    assert err.mean() < 2e-3 * max(1.0, np.abs(b).mean())
