@@ -1,0 +1,232 @@
+// tcgen05 implicit-GEMM 3x3 convolution for the denoiser (included inside
+// denoise.cu's anonymous namespace, after ConvArgs).
+//
+// One CTA (4 warps) computes two output rows x 128 consecutive pixels x all
+// COUT channels as two GEMMs on the 5th-generation tensor cores: M = 128
+// pixels per row, N = COUT, K = 9 taps x Cin, FP32 accumulators in tensor
+// memory (row r in columns [r * COUT, (r + 1) * COUT)).  The input is walked
+// in 16-channel slices of the virtual, concatenated, possibly upsampled
+// input; for each slice the CTA stages, with 16-byte loads, the 4-row x
+// 130-pixel halo and the slice's 9 x COUT weights in shared memory, in the
+// canonical no-swizzle K-major layout: each 8-channel half is a plane of
+// 16-byte rows, so a core matrix is 8 consecutive rows (SBO = 128 B) and the
+// second K half sits one plane further (LBO = the plane size).  A tap's A
+// operand is the halo plane of its input row shifted by its column, i.e. a
+// start address 16 * dx bytes later: the im2col never exists, and the two
+// output rows share the weight slice.  Two stages: while the tensor cores
+// run the 18 MMAs of slice k (issued by one thread and committed to that
+// stage's mbarrier), all threads load slice k + 1 into the other stage.
+// The epilogue reads the accumulators with tcgen05.ld (warp w owns TMEM
+// lanes 32w..32w+31 = pixels 32w..32w+31), adds the bias, applies ReLU and
+// stores BF16 with 16-byte stores.
+#pragma once
+
+constexpr int kTcPix = 128;             // output pixels per row of a CTA (MMA M)
+constexpr int kTcRows = 2;              // output rows per CTA
+constexpr int kTcHalo = kTcPix + 2;     // input pixels per halo row
+constexpr int kTcPlane = kTcHalo * 16;  // bytes of one 8-channel halo plane
+constexpr int kTcAbytes = (kTcRows + 2) * 2 * kTcPlane;
+constexpr uint32_t kTcSpin = 1u << 26;  // mbarrier wait cap (polls)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+// shared-memory matrix descriptor: start, leading (K) and stride (M/N) byte
+// offsets, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return uint64_t((saddr >> 4) & 0x3FFFu) | (uint64_t((lbo >> 4) & 0x3FFFu) << 16) |
+           (uint64_t((sbo >> 4) & 0x3FFFu) << 32) | (uint64_t(1) << 46);
+}
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N and M
+__host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(m >> 4) << 24);
+}
+constexpr size_t tc_stage_bytes(int cout) { return size_t(kTcAbytes) + size_t(9) * 2 * cout * 16; }
+constexpr size_t tc_smem_bytes(int cout) { return 2 * tc_stage_bytes(cout) + 32; }
+
+// Bounded wait for phase `parity` of an mbarrier; false when the cap ran out.
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
+    uint32_t done = 0;
+    for (uint32_t spins = 0; !done && spins < kTcSpin; ++spins)
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+    return done != 0;
+}
+
+template <int COUT>
+__device__ __forceinline__ void tc_load_slice(const ConvArgs& a, unsigned char* As, unsigned char* Bs, int n, int y0,
+                                              int x0, int c0, int cin, int ha, int wa) {
+    const int tid = threadIdx.x;
+    // halo: input rows y0-1..y0+2, pixels x0-1..x0+128, channels c0..c0+15
+    for (int i = tid; i < (kTcRows + 2) * 2 * kTcHalo; i += 128) {
+        const int hf = i & 1, p = (i >> 1) % kTcHalo, r = (i >> 1) / kTcHalo;
+        const int yy = y0 - 1 + r, xx = x0 - 1 + p, c = c0 + 8 * hf;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (yy >= 0 && yy < a.h && xx >= 0 && xx < a.w_) {
+            const bf16* src;
+            if (c < a.ca) {
+                const int ya = a.ups ? yy >> 1 : yy, xa = a.ups ? xx >> 1 : xx;
+                src = a.a + ((size_t(n) * ha + ya) * wa + xa) * a.ca + c;
+            } else {
+                src = a.b + ((size_t(n) * a.h + yy) * a.w_ + xx) * a.cb + (c - a.ca);
+            }
+            v = __ldg(reinterpret_cast<const uint4*>(src));
+        }
+        *reinterpret_cast<uint4*>(As + (r * 2 + hf) * kTcPlane + p * 16) = v;
+    }
+    // weights: 9 taps x 2 halves x COUT rows of 16 B
+    for (int i = tid; i < 9 * 2 * COUT; i += 128) {
+        const int co = i % COUT, hf = (i / COUT) & 1, t = i / (2 * COUT);
+        const uint4 v = __ldg(reinterpret_cast<const uint4*>(a.w + (size_t(co) * 9 + t) * cin + c0 + 8 * hf));
+        *reinterpret_cast<uint4*>(Bs + ((t * 2 + hf) * COUT + co) * 16) = v;
+    }
+}
+
+template <int COUT>
+__global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
+    constexpr int kAcc = kTcRows * COUT;
+    constexpr int kCols = kAcc < 32 ? 32 : kAcc;  // TMEM columns (power of 2, >= 32)
+    constexpr size_t kStage = tc_stage_bytes(COUT);
+    extern __shared__ __align__(128) unsigned char tsm[];
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(tsm + 2 * kStage);  // one per stage
+    uint32_t* slot = reinterpret_cast<uint32_t*>(mbar + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tiles_x = (a.w_ + kTcPix - 1) / kTcPix, rows_per_img = (a.h + kTcRows - 1) / kTcRows;
+    const int tx = blockIdx.x % tiles_x, rb = blockIdx.x / tiles_x;
+    const int y0 = (rb % rows_per_img) * kTcRows, n = rb / rows_per_img;
+    const int x0 = tx * kTcPix;
+    const int cin = a.ca + a.cb, nk = cin / 16;
+    const int ha = a.ups ? a.h >> 1 : a.h, wa = a.ups ? a.w_ >> 1 : a.w_;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                     "r"(uint32_t(kCols))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar + 1)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc_load_slice<COUT>(a, tsm, tsm + kTcAbytes, n, y0, x0, 0, cin, ha, wa);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = *slot;
+    const uint32_t smem0 = smem_u32(tsm);
+    constexpr uint32_t idesc = tc_idesc(kTcPix, COUT);
+    bool timed_out = false;
+    int issued = 0;  // slices whose MMAs were committed
+
+    for (int k = 0; k < nk; ++k) {
+        const int s = k & 1;
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t abase = smem0 + uint32_t(s * kStage), bbase = abase + kTcAbytes;
+#pragma unroll
+            for (int r = 0; r < kTcRows; ++r)
+#pragma unroll
+                for (int t = 0; t < 9; ++t) {
+                    const int ky = t / 3, kx = t % 3;
+                    const uint64_t ad = tc_sdesc(abase + ((r + ky) * 2) * kTcPlane + kx * 16, kTcPlane, 128);
+                    const uint64_t bd = tc_sdesc(bbase + (t * 2) * COUT * 16, COUT * 16, 128);
+                    const uint32_t acc = (k > 0 || t > 0) ? 1u : 0u;
+                    asm volatile(
+                        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr + uint32_t(r * COUT)),
+                        "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                        : "memory");
+                }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_u32(mbar + s))
+                         : "memory");
+        }
+        issued = k + 1;
+        if (k + 1 < nk) {
+            const int s2 = s ^ 1;
+            // slice k-1 used stage s2: its MMAs must be done before reloading
+            if (k >= 1 && !tc_wait(smem_u32(mbar + s2), uint32_t((k - 1) >> 1) & 1u)) {
+                timed_out = true;
+                atomicOr(status, MRT_STATUS_ITER_CAP);
+            }
+            timed_out = __syncthreads_or(timed_out) != 0;
+            if (timed_out) break;
+            unsigned char* st = tsm + s2 * kStage;
+            tc_load_slice<COUT>(a, st, st + kTcAbytes, n, y0, x0, 16 * (k + 1), cin, ha, wa);
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncthreads();
+        }
+    }
+    // the last two commits cover every MMA issued (bounded even after a
+    // timeout, so the tensor memory is only freed once they are done)
+    for (int j = issued - 1; j >= 0 && j >= issued - 2; --j)
+        if (!tc_wait(smem_u32(mbar + (j & 1)), uint32_t(j >> 1) & 1u)) {
+            timed_out = true;
+            atomicOr(status, MRT_STATUS_ITER_CAP);
+        }
+    timed_out = __syncthreads_or(timed_out) != 0;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!timed_out) {
+        const int m = 32 * warp + lane, x = x0 + m;
+#pragma unroll
+        for (int r = 0; r < kTcRows; ++r) {
+            const int y = y0 + r;
+            bf16* dst = a.y + ((size_t(n) * a.h + y) * a.w_ + x) * COUT;
+#pragma unroll
+            for (int j = 0; j < COUT / 16; ++j) {
+                uint32_t v[16];
+                const uint32_t ta = taddr + (uint32_t(32 * warp) << 16) + uint32_t(r * COUT + 16 * j);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                    "[%16];\n"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15])
+                    : "r"(ta));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (x < a.w_ && y < a.h) {
+                    uint32_t packed[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        float f0 = __uint_as_float(v[2 * q]) + a.bias[16 * j + 2 * q];
+                        float f1 = __uint_as_float(v[2 * q + 1]) + a.bias[16 * j + 2 * q + 1];
+                        if (a.relu) {
+                            f0 = fmaxf(f0, 0.0f);
+                            f1 = fmaxf(f1, 0.0f);
+                        }
+                        const __nv_bfloat162 hv = __floats2bfloat162_rn(f0, f1);
+                        packed[q] = *reinterpret_cast<const uint32_t*>(&hv);
+                    }
+                    uint4* o = reinterpret_cast<uint4*>(dst + 16 * j);
+                    o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                    o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(uint32_t(kCols))
+                     : "memory");
+}
+
+template <int COUT>
+cudaError_t launch_conv_tc(const ConvArgs& ca, uint32_t* status, cudaStream_t s) {
+    static bool configured = false;  // per process; all devices are sm_103
+    const size_t smem = tc_smem_bytes(COUT);
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_conv_tc<COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    const int blocks = ((ca.w_ + kTcPix - 1) / kTcPix) * ((ca.h + kTcRows - 1) / kTcRows) * ca.n;
+    k_conv_tc<COUT><<<blocks, 128, smem, s>>>(ca, status);
+    return cudaGetLastError();
+}

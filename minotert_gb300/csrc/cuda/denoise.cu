@@ -16,10 +16,11 @@
 // noisy image through); the loss is L1 in that space.  The output layer
 // starts at a tenth of the He scale.
 //
-// Forward: implicit-GEMM convolution on the tensor cores (mma.sync
-// m16n8k16, BF16 in, FP32 accumulate): a warp computes 16 consecutive
-// pixels of a row x all output channels; the 2x upsampling and the skip
-// concatenation of the decoder are folded into the operand loads.
+// Forward: implicit-GEMM convolution on the tcgen05 tensor cores with the
+// accumulators in tensor memory (conv_tc.cuh, the default), or on mma.sync
+// m16n8k16 (k_conv_fwd: a warp computes 16 consecutive pixels of a row x
+// all output channels); both fold the decoder's 2x upsampling and skip
+// concatenation into their operand loads.
 // Backward: FP32 kernels on the CUDA cores for the data, weight and bias
 // gradients, reading the stored BF16 activations.
 #include "internal.hpp"
@@ -141,184 +142,7 @@ __global__ void __launch_bounds__(128) k_conv_fwd(ConvArgs a) {
     }
 }
 
-// ---- tcgen05 implicit-GEMM convolution ------------------------------------
-//
-// One CTA (4 warps) computes 128 consecutive output pixels of one row x all
-// COUT channels as a GEMM on the 5th-generation tensor cores: M = 128
-// pixels, N = COUT, K = 9 taps x Cin, accumulated in FP32 in tensor memory.
-// Per 16-channel slice of the (virtual, concatenated, possibly upsampled)
-// input the CTA stages, with 16-byte loads, the 3-row x 130-pixel halo of
-// the slice and the slice's 9 x COUT weights in shared memory, in the
-// canonical no-swizzle K-major layout: each 8-channel half is a plane of
-// rows of 16 bytes, so a core matrix is 8 consecutive rows (SBO = 128 B) and
-// the second K half sits one plane further (LBO = plane size).  A tap's A
-// operand is then the halo plane of its row shifted by its column: a start
-// address 16 * dx bytes later -- the im2col never exists.  One thread issues
-// the 9 MMAs (K = 16 each) and commits them to an mbarrier; the epilogue
-// reads the accumulators with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31
-// = pixels 32w..32w+31), adds the bias, applies ReLU and stores BF16.
-constexpr int kTcPix = 128;            // output pixels per CTA (MMA M)
-constexpr int kTcHalo = kTcPix + 2;    // input pixels per halo row
-constexpr int kTcPlane = kTcHalo * 16; // bytes of one 8-channel halo plane
-constexpr int kTcAbytes = 3 * 2 * kTcPlane;
-constexpr uint32_t kTcSpin = 1u << 26; // mbarrier wait cap (polls)
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-// shared-memory matrix descriptor: start, leading (K) and stride (M/N) byte
-// offsets, descriptor version 1, no swizzle
-__device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-    return uint64_t((saddr >> 4) & 0x3FFFu) | (uint64_t((lbo >> 4) & 0x3FFFu) << 16) |
-           (uint64_t((sbo >> 4) & 0x3FFFu) << 32) | (uint64_t(1) << 46);
-}
-// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
-// K-major, N and M
-__host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(m >> 4) << 24);
-}
-
-template <int COUT>
-__global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
-    constexpr int kCols = COUT < 32 ? 32 : COUT;  // TMEM columns (power of 2, >= 32)
-    extern __shared__ __align__(128) unsigned char tsm[];
-    unsigned char* As = tsm;                          // 3 rows x 2 planes x 130 x 16 B
-    unsigned char* Bs = tsm + kTcAbytes;              // 9 taps x 2 planes x COUT x 16 B
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(Bs + 9 * 2 * COUT * 16);
-    uint32_t* slot = reinterpret_cast<uint32_t*>(mbar + 1);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int tiles_x = (a.w_ + kTcPix - 1) / kTcPix;
-    const int tx = blockIdx.x % tiles_x, row = blockIdx.x / tiles_x;
-    const int y = row % a.h, n = row / a.h;
-    const int x0 = tx * kTcPix;
-    const int cin = a.ca + a.cb;
-    const int ha = a.ups ? a.h >> 1 : a.h, wa = a.ups ? a.w_ >> 1 : a.w_;
-
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
-                     "r"(uint32_t(kCols))
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const uint32_t taddr = *slot;
-    const uint32_t a_base = smem_u32(As), b_base = smem_u32(Bs), mb = smem_u32(mbar);
-    constexpr uint32_t idesc = tc_idesc(kTcPix, COUT);
-    uint32_t phase = 0;
-    bool timed_out = false;
-
-    for (int c0 = 0; c0 < cin && !timed_out; c0 += 16) {
-        // halo slice: rows y-1..y+1, pixels x0-1..x0+128, channels c0..c0+15
-        for (int i = tid; i < 3 * 2 * kTcHalo; i += 128) {
-            const int hf = i & 1, p = (i >> 1) % kTcHalo, r = (i >> 1) / kTcHalo;
-            const int yy = y - 1 + r, xx = x0 - 1 + p, c = c0 + 8 * hf;
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (yy >= 0 && yy < a.h && xx >= 0 && xx < a.w_) {
-                const bf16* src;
-                if (c < a.ca) {
-                    const int ya = a.ups ? yy >> 1 : yy, xa = a.ups ? xx >> 1 : xx;
-                    src = a.a + ((size_t(n) * ha + ya) * wa + xa) * a.ca + c;
-                } else {
-                    src = a.b + ((size_t(n) * a.h + yy) * a.w_ + xx) * a.cb + (c - a.ca);
-                }
-                v = __ldg(reinterpret_cast<const uint4*>(src));
-            }
-            *reinterpret_cast<uint4*>(As + (r * 2 + hf) * kTcPlane + p * 16) = v;
-        }
-        // weight slice: 9 taps x 2 halves x COUT rows of 16 B
-        for (int i = tid; i < 9 * 2 * COUT; i += 128) {
-            const int co = i % COUT, hf = (i / COUT) & 1, t = i / (2 * COUT);
-            const uint4 v = __ldg(reinterpret_cast<const uint4*>(a.w + (size_t(co) * 9 + t) * cin + c0 + 8 * hf));
-            *reinterpret_cast<uint4*>(Bs + ((t * 2 + hf) * COUT + co) * 16) = v;
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-            for (int t = 0; t < 9; ++t) {
-                const int ky = t / 3, kx = t % 3;
-                const uint64_t ad = tc_sdesc(a_base + (ky * 2) * kTcPlane + kx * 16, kTcPlane, 128);
-                const uint64_t bd = tc_sdesc(b_base + (t * 2) * COUT * 16, COUT * 16, 128);
-                const uint32_t acc = (c0 > 0 || t > 0) ? 1u : 0u;
-                asm volatile(
-                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr),
-                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-                    : "memory");
-            }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)
-                         : "memory");
-        }
-        // the MMAs have read this slice (and accumulated) once the mbarrier
-        // phase flips.  Bounded wait: past the cap the status flag is set,
-        // the tile is abandoned, and a second bounded wait lets the MMAs in
-        // flight finish before the tensor memory is freed
-        uint32_t done = 0, spins = 0;
-        while (!done && spins < 2u * kTcSpin) {
-            asm volatile(
-                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-                : "=r"(done)
-                : "r"(mb), "r"(phase)
-                : "memory");
-            if (++spins == kTcSpin && !done) {
-                timed_out = true;
-                atomicOr(status, MRT_STATUS_ITER_CAP);
-            }
-        }
-        phase ^= 1u;
-        timed_out = __syncthreads_or(timed_out) != 0;  // one decision for the whole CTA
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (!timed_out) {
-        // epilogue: pixel m = 32 * warp + lane, channels in groups of 16
-        const int m = 32 * warp + lane, x = x0 + m;
-        bf16* dst = a.y + ((size_t(n) * a.h + y) * a.w_ + x) * COUT;
-#pragma unroll
-        for (int j = 0; j < COUT / 16; ++j) {
-            uint32_t r[16];
-            const uint32_t ta = taddr + (uint32_t(32 * warp) << 16) + uint32_t(16 * j);
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                "[%16];\n"
-                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                  "=r"(r[15])
-                : "r"(ta));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (x < a.w_) {
-                uint32_t packed[8];
-#pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    float v0 = __uint_as_float(r[2 * k]) + a.bias[16 * j + 2 * k];
-                    float v1 = __uint_as_float(r[2 * k + 1]) + a.bias[16 * j + 2 * k + 1];
-                    if (a.relu) {
-                        v0 = fmaxf(v0, 0.0f);
-                        v1 = fmaxf(v1, 0.0f);
-                    }
-                    const __nv_bfloat162 hv = __floats2bfloat162_rn(v0, v1);
-                    packed[k] = *reinterpret_cast<const uint32_t*>(&hv);
-                }
-                uint4* o = reinterpret_cast<uint4*>(dst + 16 * j);
-                o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-                o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
-            }
-        }
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(uint32_t(kCols))
-                     : "memory");
-}
-
-constexpr size_t tc_smem_bytes(int cout) { return size_t(kTcAbytes) + size_t(9) * 2 * cout * 16 + 16; }
+#include "conv_tc.cuh"
 
 // 2x2 average pool, NHWC
 __global__ void k_pool(const bf16* x, bf16* y, int n, int h, int w, int c) {
@@ -574,20 +398,6 @@ int ensure_acts(mrt_ctx* ctx, mrt_denoiser* d, size_t pix, bool grads) {
         d->grad_pix = pix;
     }
     return MRT_OK;
-}
-
-template <int COUT>
-cudaError_t launch_conv_tc(const ConvArgs& ca, uint32_t* status, cudaStream_t s) {
-    static bool configured = false;  // per process; all devices are sm_103
-    const size_t smem = tc_smem_bytes(COUT);
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_conv_tc<COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
-    const int blocks = ((ca.w_ + kTcPix - 1) / kTcPix) * ca.h * ca.n;
-    k_conv_tc<COUT><<<blocks, 128, smem, s>>>(ca, status);
-    return cudaGetLastError();
 }
 
 cudaError_t conv(const mrt_denoiser* d, int l, const bf16* a, const bf16* b, int n, int h, int w, cudaStream_t s) {
