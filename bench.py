@@ -813,6 +813,94 @@ def run_network_kernels(args, world, rank, local, dist):
                       "steps": args.steps, "warmup": args.warmup, "data": "random weights and inputs"}))
 
 
+def run_post_kernels(args, world, rank, local, dist):
+    """Per-frame cost at 1920x1080 of the passes around the path tracer:
+    atmosphere + sky-view LUTs, the sky miss shader on 2,073,600
+    directions, the joint bilateral filter (default parameters), the AMD
+    tonemapper, temporal reprojection, and the headless renderer's whole
+    reference frame (scene 0, 8 samples x 8 bounces, atmosphere, bilateral,
+    AMD).  CUDA events, median of --steps after --warmup."""
+    from minotert_gb300 import build as _build
+    _build.build()
+    from minotert_gb300 import scene
+    from minotert_gb300._lib import Context
+    from minotert_gb300.pathtracer import Camera, Pathtracer, Sky as ConstSky, TraceSettings, camera_consts
+    from minotert_gb300.post import BilateralParams, Denoiser, ReprojectParams, Tonemapper, reproject
+    from minotert_gb300.renderer import Renderer, RenderSettings
+    from minotert_gb300.sky import Atmosphere, Sky
+
+    ctx = Context(local)
+    W, H = 1920, 1080
+    n = W * H
+    a, b = ctx.event(), ctx.event()
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        ts = []
+        for _ in range(args.steps):
+            ctx.record(a)
+            fn()
+            ctx.record(b)
+            ctx.sync()
+            ts.append(ctx.elapsed_ms(a, b))
+        return float(np.median(ts))
+
+    out = {"metric": "post-processing ms per 1920x1080 frame", "unit": "ms", "steps": args.steps,
+           "warmup": args.warmup, "data": "synthetic (seeded scenes)"}
+    atmo = Atmosphere(ctx)
+    sky = Sky()
+    cam_pos = np.array([0.0, 0.0, 0.5], np.float32)
+    out["sky_view_ms"] = timed(lambda: sky.createView(atmo, cam_pos))
+    from minotert_gb300._lib import lib, ptr
+    out["sky_atmosphere_ms"] = timed(lambda: ctx.check(lib().mrt_cuda_sky_atmosphere(ctx.handle, atmo.handle,
+                                                                                     ptr(atmo.params), None), "atmo"))
+    view = sky.createView(atmo, cam_pos)
+    rng = np.random.default_rng(2)
+    dirs = rng.normal(size=(n, 3)).astype(np.float32)
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    d_dirs, d_out = ctx.to_device(dirs), ctx.alloc(n * 12)
+    out["sky_eval_ms_2073600_dirs"] = timed(lambda: view.eval(d_dirs, n, d_out))
+
+    # a real 1080p frame of the heightfield scene for the image passes
+    from minotert_gb300 import workloads
+    base = workloads.heightfield_boxes_256()
+    c0 = base.camera
+    cam = Camera((W, H), c0.verticalFov, c0.nearPlane, c0.position, c0.yaw, c0.pitch)
+    mesh = base.mesh()
+    ds = scene.DeviceScene.triangles(ctx, mesh, scene.build_bvh8(mesh))
+    bn = scene.blue_noise(1, 64)
+    pt = Pathtracer(ctx, ds, full_gbuffer=True)
+    gb = pt.primaryRays((W, H), cam, cam)
+    col = pt.secondaryRays(gb, cam, base.sky, bn, TraceSettings(1, 4, 2, 1))
+    den = Denoiser(ctx)
+    filt = ctx.alloc(n * 12)
+    out["bilateral_ms"] = timed(lambda: den.bilateral(col, gb, cam, BilateralParams(), out=filt))
+    tm = Tonemapper(ctx)
+    rgba = ctx.alloc(n * 4)
+    out["tonemap_amd_ms"] = timed(lambda: tm.amd(filt, W, H, 1.0, out=rgba))
+    out["tonemap_amd_gbs"] = n * 16 / out["tonemap_amd_ms"] / 1e6
+    pt2 = Pathtracer(ctx, ds, full_gbuffer=True)
+    cam1 = Camera((W, H), c0.verticalFov, c0.nearPlane, c0.position, c0.yaw + 0.01, c0.pitch)
+    gb1 = pt2.primaryRays((W, H), cam1, cam)
+    hist, hl = ctx.alloc(n * 12), ctx.to_device(np.full(n, 4.0, np.float32))
+    o, ol = ctx.alloc(n * 12), ctx.alloc(n * 4)
+    consts = camera_consts(cam1, cam, 1)
+    out["reproject_ms"] = timed(lambda: reproject(ctx, gb1, gb, consts, col, filt, hl, o, ol, ReprojectParams()))
+
+    # the headless renderer's reference frame on scene 0
+    spheres = scene.reference_spheres()
+    s0 = scene.DeviceScene.from_spheres(ctx, spheres)
+    r = Renderer(ctx, s0, W, H)
+    rc = Camera.reference(W, H)
+    out["renderer_reference_frame_ms"] = timed(lambda: r.draw(rc))
+    settings = RenderSettings.defaults()
+    settings.trace.samples, settings.trace.max_bounces = 1, 8
+    out["renderer_1spp_frame_ms"] = timed(lambda: r.draw(rc, settings))
+    out["device_status"] = ctx.status()
+    print(json.dumps(out))
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -821,7 +909,7 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", choices=["icospheres_1080p", "batched64", "radiance_cache", "denoiser",
-                                           "network_kernels"],
+                                           "network_kernels", "post_kernels"],
                     default="icospheres_1080p")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
@@ -836,6 +924,8 @@ def main(argv=None):
         run_denoise_experiment(args, world, rank, local, dist)
     elif args.workload == "network_kernels":
         run_network_kernels(args, world, rank, local, dist)
+    elif args.workload == "post_kernels":
+        run_post_kernels(args, world, rank, local, dist)
     else:
         run_mine(args, world, rank, local, dist)
 
