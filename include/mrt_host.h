@@ -76,10 +76,13 @@ uint32_t mrt_heightfield_grid_for(uint32_t target_tris);
 
 /* ---- BVH ------------------------------------------------------------- */
 typedef struct mrt_bvh_build_params {
-    uint32_t sah_bins;       /* binned SAH bins (default 32)                 */
+    uint32_t sah_bins;       /* binned SAH bins (0 = 64)                     */
     uint32_t max_leaf_tris;  /* <= 3                                         */
     uint32_t threads;        /* 0 = hardware concurrency                     */
-    uint32_t pad;
+    uint32_t trav_cost_pct;  /* SAH cost of a BVH2 node step relative to a
+                                triangle test, percent (0 = 50: splitting
+                                small leaves is cheap, the collapse packs
+                                the pieces into the same 8-wide node)        */
 } mrt_bvh_build_params;
 
 typedef struct mrt_bvh8 {

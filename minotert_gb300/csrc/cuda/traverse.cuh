@@ -108,6 +108,19 @@ MRT_DEV bool intersect_tri(const RayPre& r, float4 a, float4 b, float4 c, float 
     return true;
 }
 
+// Three-input min / max (one instruction on sm_100+; NaN inputs are
+// ignored like fminf / fmaxf)
+MRT_DEV float min3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+MRT_DEV float max3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 MRT_DEV float byte_to_float(uint32_t word, uint32_t k) {
     // 2^23 + byte as float bits, minus 2^23: exact
     return __fsub_rn(__int_as_float(__byte_perm(word, 0x4B000000u, k | 0x7440u)), 8388608.0f);
@@ -204,8 +217,8 @@ MRT_DEV bool trav_step(const DevScene& sc, Trav& s, uint2* stk, uint32_t stride,
             const float tfx = fmaf(byte_to_float(i < 4 ? fx0 : fx1, k), scx, adx);
             const float tfy = fmaf(byte_to_float(i < 4 ? fy0 : fy1, k), scy, ady);
             const float tfz = fmaf(byte_to_float(i < 4 ? fz0 : fz1, k), scz, adz);
-            const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
-            const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tbest));
+            const float tn = max3f(tnx, tny, fmaxf(tnz, tmin));
+            const float tf = min3f(tfx, tfy, fminf(tfz, tbest));
             if (tn <= __fmul_rn(tf, kRobustScale)) {
                 const uint32_t meta = ((i < 4 ? L1.z : L1.w) >> (8 * k)) & 0xFFu;
                 if ((imask >> i) & 1u) int_keys |= 1u << (uint32_t(i) ^ r.oct);

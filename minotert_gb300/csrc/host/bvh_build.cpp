@@ -3,7 +3,7 @@
 // shaders loop over 5 spheres, primaryRay.comp:26-32, secondaryRays.comp:
 // 77-83); this module is new and follows published methods:
 //   - binned SAH construction (Wald, "On fast construction of SAH-based
-//     bounding volume hierarchies", RT 2007), 32 bins per axis;
+//     bounding volume hierarchies", RT 2007), 64 bins per axis;
 //   - top-down collapse to 8-wide nodes by repeatedly opening the child of
 //     largest surface area, leaves of <= 3 triangles, <= 24 per node, and
 //     octant-ordered child slots with 8-bit quantised boxes (Ylitie, Karras
@@ -56,6 +56,7 @@ struct Builder2 {
     uint32_t n;
     uint32_t bins;
     uint32_t max_leaf;
+    double trav_cost = 0.5;  // SAH cost of a node step / cost of a triangle test
     std::vector<Box> pbox;
     std::vector<float> cent; // 3 per prim
     std::vector<uint32_t> ids;
@@ -119,9 +120,9 @@ struct Builder2 {
         }
         double parea = box.area();
         if (cnt <= max_leaf) {
-            // SAH: traversal cost 1, intersection cost 1 (relative to parent area)
+            // SAH: traversal cost trav_cost, intersection cost 1 (relative to parent area)
             double leaf_cost = double(cnt);
-            double split_cost = parea > 0.0 ? 1.0 + best_cost / parea : INFINITY;
+            double split_cost = parea > 0.0 ? trav_cost + best_cost / parea : INFINITY;
             if (best_axis < 0 || leaf_cost <= split_cost) { node.first = begin; node.count = cnt; return; }
         }
         uint32_t mid;
@@ -334,7 +335,8 @@ int mrt_bvh8_build(const float* verts, uint32_t tri_count, const mrt_bvh_build_p
     Builder2 b;
     b.verts = verts;
     b.n = tri_count;
-    b.bins = params && params->sah_bins ? params->sah_bins : 32;
+    b.bins = params && params->sah_bins ? params->sah_bins : 64;
+    b.trav_cost = params && params->trav_cost_pct ? double(params->trav_cost_pct) / 100.0 : 0.5;
     b.max_leaf = params && params->max_leaf_tris ? std::min<uint32_t>(params->max_leaf_tris, 3) : 3;
     b.bins = std::max<uint32_t>(4, std::min<uint32_t>(b.bins, 256));
     unsigned threads = params && params->threads ? params->threads : std::thread::hardware_concurrency();
