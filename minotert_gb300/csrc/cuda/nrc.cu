@@ -42,6 +42,7 @@ constexpr int kOutRows = 16;                                   // output weight 
 constexpr int kLayerW = kWidth * kWidth;                       // 4096 weights per hidden layer
 constexpr int kWeights = kHidden * kLayerW + kOutRows * kWidth; // 17408
 constexpr int kMlpWarps = 4;                                   // warps per MLP block (16 rows each)
+constexpr float kGradScale = 1024.0f;  // loss scale of the FP16 backward (undone on the gradients)
 
 struct GridSpec {
     uint32_t log2_t;           // entries per level = 2^log2_t
@@ -295,7 +296,9 @@ k_cache_train_fwd(CacheDev c, const float* q, const float* target, uint32_t n, _
                 const float y = O[lane * 3 + k], t = target[size_t(r) * 3 + k];
                 const float den = y * y + 0.01f;
                 loss += (y - t) * (y - t) / den;
-                dout[size_t(r) * 3 + k] = 2.0f * (y - t) / den / float(n);
+                // scaled by kGradScale so the FP16 MMA operands of the
+                // backward stay out of the subnormal range
+                dout[size_t(r) * 3 + k] = 2.0f * (y - t) / den / float(n) * kGradScale;
             }
         }
         __syncwarp();
@@ -341,14 +344,31 @@ k_cache_train_bwd(CacheDev c, uint32_t n, const __half* inputs, const __half* ac
             for (int i = lane; i < 16 * kWidth / 2; i += 32)
                 reinterpret_cast<uint32_t*>(H)[i] = reinterpret_cast<const uint32_t*>(hsrc)[i];
             __syncwarp();
-            // weight gradient: gW_L[o][i] += sum_r D[r][o] * H[r][i]
+            // weight gradient gW_L[o][i] += sum_r D[r][o] * H[r][i] on the
+            // tensor cores: A = D^T (out_w x 16 rows), B = H (16 rows x 64)
             float* G = sG + L * kLayerW;
-            for (int e = lane; e < out_w * kWidth; e += 32) {
-                const int o = e / kWidth, i = e % kWidth;
-                float s = 0.0f;
-#pragma unroll 4
-                for (int r = 0; r < 16; ++r) s = fmaf(D[r * kWidth + o], __half2float(H[r * kWidth + i]), s);
-                atomicAdd(&G[e], s);
+            for (int mt = 0; mt < out_w / 16; ++mt) {
+                const int o0 = 16 * mt + g, o1 = o0 + 8;
+                uint32_t a[4];
+                a[0] = pack_half2(D[(2 * t) * kWidth + o0], D[(2 * t + 1) * kWidth + o0]);
+                a[1] = pack_half2(D[(2 * t) * kWidth + o1], D[(2 * t + 1) * kWidth + o1]);
+                a[2] = pack_half2(D[(2 * t + 8) * kWidth + o0], D[(2 * t + 9) * kWidth + o0]);
+                a[3] = pack_half2(D[(2 * t + 8) * kWidth + o1], D[(2 * t + 9) * kWidth + o1]);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const int nn = 8 * j + g;
+                    const uint32_t b0 = uint32_t(__half_as_ushort(H[(2 * t) * kWidth + nn])) |
+                                        (uint32_t(__half_as_ushort(H[(2 * t + 1) * kWidth + nn])) << 16);
+                    const uint32_t b1 = uint32_t(__half_as_ushort(H[(2 * t + 8) * kWidth + nn])) |
+                                        (uint32_t(__half_as_ushort(H[(2 * t + 9) * kWidth + nn])) << 16);
+                    float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                    mma16816(c, a, b0, b1);
+                    const int i0 = 8 * j + 2 * t;
+                    atomicAdd(&G[o0 * kWidth + i0], c[0]);
+                    atomicAdd(&G[o0 * kWidth + i0 + 1], c[1]);
+                    atomicAdd(&G[o1 * kWidth + i0], c[2]);
+                    atomicAdd(&G[o1 * kWidth + i0 + 1], c[3]);
+                }
             }
             // dh_{L-1} = D * W_L: A = D (16 x out_w as half), B from W_L^T [in][out]
             float acc[8][4];
@@ -390,16 +410,16 @@ k_cache_train_bwd(CacheDev c, uint32_t n, const __half* inputs, const __half* ac
             }
             __syncwarp();
         }
-        // D holds dL/d(input row); keep the 32 encoded features
+        // D holds dL/d(input row) x kGradScale; keep the 32 encoded features
         for (int i = lane; i < 16 * kEnc; i += 32) {
             const int r = i / kEnc, k = i % kEnc;
-            d_in[size_t(base + r) * kEnc + k] = D[r * kWidth + k];
+            d_in[size_t(base + r) * kEnc + k] = D[r * kWidth + k] * (1.0f / kGradScale);
         }
         __syncwarp();
     }
     __syncthreads();
     for (int i = threadIdx.x; i < kWeights; i += blockDim.x)
-        if (sG[i] != 0.0f) atomicAdd(&gW[i], sG[i]);
+        if (sG[i] != 0.0f) atomicAdd(&gW[i], sG[i] * (1.0f / kGradScale));
 }
 
 // Hash-grid gradient: scatter dL/d(features) to the 8 corners per level.
