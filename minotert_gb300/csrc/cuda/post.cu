@@ -121,20 +121,28 @@ k_bilateral(BilateralTable T, const float* __restrict__ color, const uint16_t* _
             const float fr = T.fr[c], gr = fs(1.0f, fr);
             const int t0 = T.first[c], cnt = T.count[c];
             int ia = (ly + T.r0[c]) * tw + col;
+            // consecutive taps of a column share a row: the lower row of
+            // tap k is the upper row of tap k + 1, so it is loaded once
+            float a_z = zz[ia], a_nx = nx[ia], a_ny = ny[ia], a_nz = nz[ia];
+            float a_r = cr[ia], a_g = cg[ia], a_b = cb[ia];
             for (int k = 0; k < cnt; ++k, ia += tw) {
                 const int ib = ia + tw;
-                const float wz = fa(fm(zz[ia], gr), fm(zz[ib], fr));
-                const f3 wn{fa(fm(nx[ia], gr), fm(nx[ib], fr)), fa(fm(ny[ia], gr), fm(ny[ib], fr)),
-                            fa(fm(nz[ia], gr), fm(nz[ib], fr))};
+                const float b_z = zz[ib], b_nx = nx[ib], b_ny = ny[ib], b_nz = nz[ib];
+                const float b_r = cr[ib], b_g = cg[ib], b_b = cb[ib];
+                const float wz = fa(fm(a_z, gr), fm(b_z, fr));
+                const f3 wn{fa(fm(a_nx, gr), fm(b_nx, fr)), fa(fm(a_ny, gr), fm(b_ny, fr)),
+                            fa(fm(a_nz, gr), fm(b_nz, fr))};
                 float dz = fs(fd(T.near_plane, wz), ncz);
                 dz = fm(dz, 100.0f);
                 const float dn = dot_rn(wn, cn);
                 const float arg = fm(fclamp(fs(dn, fm(dz, dz)), 0.0f, 1.0f), T.inv_thr_sq2);
                 const float df = fm(fm(exp_cw(arg), T.inv_thr_sqrt2pi), T.blur[t0 + k]);
                 zb = fa(zb, df);
-                ar = fa(ar, fm(df, fa(fm(cr[ia], gr), fm(cr[ib], fr))));
-                ag = fa(ag, fm(df, fa(fm(cg[ia], gr), fm(cg[ib], fr))));
-                ab = fa(ab, fm(df, fa(fm(cb[ia], gr), fm(cb[ib], fr))));
+                ar = fa(ar, fm(df, fa(fm(a_r, gr), fm(b_r, fr))));
+                ag = fa(ag, fm(df, fa(fm(a_g, gr), fm(b_g, fr))));
+                ab = fa(ab, fm(df, fa(fm(a_b, gr), fm(b_b, fr))));
+                a_z = b_z; a_nx = b_nx; a_ny = b_ny; a_nz = b_nz;
+                a_r = b_r; a_g = b_g; a_b = b_b;
             }
         }
         res = f3{fd(ar, zb), fd(ag, zb), fd(ab, zb)};
