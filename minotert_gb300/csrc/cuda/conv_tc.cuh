@@ -6,16 +6,17 @@
 // pixels per row, N = COUT, K = 9 taps x Cin, FP32 accumulators in tensor
 // memory (row r in columns [r * COUT, (r + 1) * COUT)).  The input is walked
 // in 16-channel slices of the virtual, concatenated, possibly upsampled
-// input; for each slice the CTA stages, with 16-byte loads, the 4-row x
-// 130-pixel halo and the slice's 9 x COUT weights in shared memory, in the
-// canonical no-swizzle K-major layout: each 8-channel half is a plane of
-// 16-byte rows, so a core matrix is 8 consecutive rows (SBO = 128 B) and the
-// second K half sits one plane further (LBO = the plane size).  A tap's A
-// operand is the halo plane of its input row shifted by its column, i.e. a
-// start address 16 * dx bytes later: the im2col never exists, and the two
-// output rows share the weight slice.  Two stages: while the tensor cores
+// input; for each slice the CTA stages the 4-row x 130-pixel halo and the
+// slice's 9 x COUT weights in shared memory, in the canonical no-swizzle
+// K-major layout: each 8-channel half is a plane of 16-byte rows, so a core
+// matrix is 8 consecutive rows (SBO = 128 B) and the second K half sits one
+// plane further (LBO = the plane size).  A tap's A operand is the halo plane
+// of its input row shifted by its column, i.e. a start address 16 * dx bytes
+// later: the im2col never exists, and the two output rows share the weight
+// slice.  Slices stream through kStages shared-memory stages with cp.async
+// (16-byte copies, zero-filled outside the image): while the tensor cores
 // run the 18 MMAs of slice k (issued by one thread and committed to that
-// stage's mbarrier), all threads load slice k + 1 into the other stage.
+// stage's mbarrier) the copies of the next kStages - 1 slices are in flight.
 // The epilogue reads the accumulators with tcgen05.ld (warp w owns TMEM
 // lanes 32w..32w+31 = pixels 32w..32w+31), adds the bias, applies ReLU and
 // stores BF16 with 16-byte stores.
@@ -42,8 +43,11 @@ __device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint3
 __host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(m >> 4) << 24);
 }
+// pipeline depth: three stages where two CTAs still fit an SM, two for
+// COUT = 128 (its weight slices are large)
+__host__ __device__ constexpr int tc_stages(int cout) { return cout >= 128 ? 2 : 3; }
 constexpr size_t tc_stage_bytes(int cout) { return size_t(kTcAbytes) + size_t(9) * 2 * cout * 16; }
-constexpr size_t tc_smem_bytes(int cout) { return 2 * tc_stage_bytes(cout) + 32; }
+constexpr size_t tc_smem_bytes(int cout) { return tc_stages(cout) * tc_stage_bytes(cout) + 64; }
 
 // Bounded wait for phase `parity` of an mbarrier; false when the cap ran out.
 __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
@@ -57,32 +61,37 @@ __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
     return done != 0;
 }
 
+// 16-byte asynchronous copy global -> shared; zero-filled when !valid (the
+// source is then not read)
+__device__ __forceinline__ void cp16(uint32_t saddr, const void* g, bool valid) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(saddr), "l"(g), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+
 template <int COUT>
-__device__ __forceinline__ void tc_load_slice(const ConvArgs& a, unsigned char* As, unsigned char* Bs, int n, int y0,
-                                              int x0, int c0, int cin, int ha, int wa) {
+__device__ __forceinline__ void tc_load_slice(const ConvArgs& a, uint32_t As, uint32_t Bs, int n, int y0, int x0,
+                                              int c0, int cin, int ha, int wa) {
     const int tid = threadIdx.x;
     // halo: input rows y0-1..y0+2, pixels x0-1..x0+128, channels c0..c0+15
     for (int i = tid; i < (kTcRows + 2) * 2 * kTcHalo; i += 128) {
         const int hf = i & 1, p = (i >> 1) % kTcHalo, r = (i >> 1) / kTcHalo;
         const int yy = y0 - 1 + r, xx = x0 - 1 + p, c = c0 + 8 * hf;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (yy >= 0 && yy < a.h && xx >= 0 && xx < a.w_) {
-            const bf16* src;
+        const bool in = yy >= 0 && yy < a.h && xx >= 0 && xx < a.w_;
+        const bf16* src = a.w;  // any valid address when zero-filling
+        if (in) {
             if (c < a.ca) {
                 const int ya = a.ups ? yy >> 1 : yy, xa = a.ups ? xx >> 1 : xx;
                 src = a.a + ((size_t(n) * ha + ya) * wa + xa) * a.ca + c;
             } else {
                 src = a.b + ((size_t(n) * a.h + yy) * a.w_ + xx) * a.cb + (c - a.ca);
             }
-            v = __ldg(reinterpret_cast<const uint4*>(src));
         }
-        *reinterpret_cast<uint4*>(As + (r * 2 + hf) * kTcPlane + p * 16) = v;
+        cp16(As + uint32_t((r * 2 + hf) * kTcPlane + p * 16), src, in);
     }
     // weights: 9 taps x 2 halves x COUT rows of 16 B
     for (int i = tid; i < 9 * 2 * COUT; i += 128) {
         const int co = i % COUT, hf = (i / COUT) & 1, t = i / (2 * COUT);
-        const uint4 v = __ldg(reinterpret_cast<const uint4*>(a.w + (size_t(co) * 9 + t) * cin + c0 + 8 * hf));
-        *reinterpret_cast<uint4*>(Bs + ((t * 2 + hf) * COUT + co) * 16) = v;
+        cp16(Bs + uint32_t(((t * 2 + hf) * COUT + co) * 16), a.w + (size_t(co) * 9 + t) * cin + c0 + 8 * hf, true);
     }
 }
 
@@ -90,10 +99,11 @@ template <int COUT>
 __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
     constexpr int kAcc = kTcRows * COUT;
     constexpr int kCols = kAcc < 32 ? 32 : kAcc;  // TMEM columns (power of 2, >= 32)
-    constexpr size_t kStage = tc_stage_bytes(COUT);
+    constexpr int kStages = tc_stages(COUT);
+    constexpr uint32_t kStage = uint32_t(tc_stage_bytes(COUT));
     extern __shared__ __align__(128) unsigned char tsm[];
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(tsm + 2 * kStage);  // one per stage
-    uint32_t* slot = reinterpret_cast<uint32_t*>(mbar + 2);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(tsm + kStages * kStage);  // one per stage
+    uint32_t* slot = reinterpret_cast<uint32_t*>(mbar + kStages);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tiles_x = (a.w_ + kTcPix - 1) / kTcPix, rows_per_img = (a.h + kTcRows - 1) / kTcRows;
     const int tx = blockIdx.x % tiles_x, rb = blockIdx.x / tiles_x;
@@ -101,6 +111,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
     const int x0 = tx * kTcPix;
     const int cin = a.ca + a.cb, nk = cin / 16;
     const int ha = a.ups ? a.h >> 1 : a.h, wa = a.ups ? a.w_ >> 1 : a.w_;
+    const uint32_t smem0 = smem_u32(tsm);
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
@@ -109,26 +120,34 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar + 1)) : "memory");
+        for (int s = 0; s < kStages; ++s)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar + s)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    tc_load_slice<COUT>(a, tsm, tsm + kTcAbytes, n, y0, x0, 0, cin, ha, wa);
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    // prologue: slices 0 .. kStages-2 in flight
+    for (int s = 0; s < kStages - 1; ++s) {
+        if (s < nk) tc_load_slice<COUT>(a, smem0 + s * kStage, smem0 + s * kStage + kTcAbytes, n, y0, x0, 16 * s, cin,
+                                        ha, wa);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t taddr = *slot;
-    const uint32_t smem0 = smem_u32(tsm);
     constexpr uint32_t idesc = tc_idesc(kTcPix, COUT);
     bool timed_out = false;
     int issued = 0;  // slices whose MMAs were committed
 
     for (int k = 0; k < nk; ++k) {
-        const int s = k & 1;
+        const int s = k % kStages;
+        // slice k has landed (groups complete in order; kStages - 2 newer
+        // groups may still be in flight)
+        asm volatile("cp.async.wait_group %0;\n" ::"n"(kStages - 2) : "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t abase = smem0 + uint32_t(s * kStage), bbase = abase + kTcAbytes;
+            const uint32_t abase = smem0 + uint32_t(s) * kStage, bbase = abase + kTcAbytes;
 #pragma unroll
             for (int r = 0; r < kTcRows; ++r)
 #pragma unroll
@@ -148,25 +167,25 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
                          : "memory");
         }
         issued = k + 1;
-        if (k + 1 < nk) {
-            const int s2 = s ^ 1;
-            // slice k-1 used stage s2: its MMAs must be done before reloading
-            if (k >= 1 && !tc_wait(smem_u32(mbar + s2), uint32_t((k - 1) >> 1) & 1u)) {
+        // refill: slice k + kStages - 1 goes into the stage slice k - 1 used
+        const int j = k + kStages - 1;
+        if (j < nk) {
+            if (k >= 1 && !tc_wait(smem_u32(mbar + (k - 1) % kStages), uint32_t((k - 1) / kStages) & 1u)) {
                 timed_out = true;
                 atomicOr(status, MRT_STATUS_ITER_CAP);
             }
             timed_out = __syncthreads_or(timed_out) != 0;
             if (timed_out) break;
-            unsigned char* st = tsm + s2 * kStage;
-            tc_load_slice<COUT>(a, st, st + kTcAbytes, n, y0, x0, 16 * (k + 1), cin, ha, wa);
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            __syncthreads();
+            const uint32_t st = smem0 + uint32_t(j % kStages) * kStage;
+            tc_load_slice<COUT>(a, st, st + kTcAbytes, n, y0, x0, 16 * j, cin, ha, wa);
         }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
     }
-    // the last two commits cover every MMA issued (bounded even after a
-    // timeout, so the tensor memory is only freed once they are done)
-    for (int j = issued - 1; j >= 0 && j >= issued - 2; --j)
-        if (!tc_wait(smem_u32(mbar + (j & 1)), uint32_t(j >> 1) & 1u)) {
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    // the slices not yet waited for: the last kStages committed (bounded even
+    // after a timeout, so the tensor memory is only freed once they are done)
+    for (int c = issued - kStages < 0 ? 0 : issued - kStages; c < issued; ++c)
+        if (!tc_wait(smem_u32(mbar + c % kStages), uint32_t(c / kStages) & 1u)) {
             timed_out = true;
             atomicOr(status, MRT_STATUS_ITER_CAP);
         }
@@ -179,9 +198,9 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
             const int y = y0 + r;
             bf16* dst = a.y + ((size_t(n) * a.h + y) * a.w_ + x) * COUT;
 #pragma unroll
-            for (int j = 0; j < COUT / 16; ++j) {
+            for (int jj = 0; jj < COUT / 16; ++jj) {
                 uint32_t v[16];
-                const uint32_t ta = taddr + (uint32_t(32 * warp) << 16) + uint32_t(r * COUT + 16 * j);
+                const uint32_t ta = taddr + (uint32_t(32 * warp) << 16) + uint32_t(r * COUT + 16 * jj);
                 asm volatile(
                     "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
                     "[%16];\n"
@@ -194,8 +213,8 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
                     uint32_t packed[8];
 #pragma unroll
                     for (int q = 0; q < 8; ++q) {
-                        float f0 = __uint_as_float(v[2 * q]) + a.bias[16 * j + 2 * q];
-                        float f1 = __uint_as_float(v[2 * q + 1]) + a.bias[16 * j + 2 * q + 1];
+                        float f0 = __uint_as_float(v[2 * q]) + a.bias[16 * jj + 2 * q];
+                        float f1 = __uint_as_float(v[2 * q + 1]) + a.bias[16 * jj + 2 * q + 1];
                         if (a.relu) {
                             f0 = fmaxf(f0, 0.0f);
                             f1 = fmaxf(f1, 0.0f);
@@ -203,7 +222,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
                         const __nv_bfloat162 hv = __floats2bfloat162_rn(f0, f1);
                         packed[q] = *reinterpret_cast<const uint32_t*>(&hv);
                     }
-                    uint4* o = reinterpret_cast<uint4*>(dst + 16 * j);
+                    uint4* o = reinterpret_cast<uint4*>(dst + 16 * jj);
                     o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
                     o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
                 }
