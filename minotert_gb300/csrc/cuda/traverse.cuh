@@ -154,17 +154,14 @@ MRT_DEV void trav_init(Trav& s, f3 o, f3 d, float tmin, float tmax, uint32_t roo
     s.iters = 0u;
 }
 
-// One traversal step: visit the next node (box tests of its 8 children)
-// and test the triangles of its hit leaves.  Returns true when the ray is
-// finished (s.best / s.tbest hold the result).  Every path through the
-// step is bounded: at most 24 triangle tests, and the iteration cap
-// (node_count + 64 node visits) ends a ray whose BVH links cycle.
-template <bool kAnyHit, bool kCount, int kStack>
-MRT_DEV bool trav_step(const DevScene& sc, Trav& s, uint2* stk, uint32_t stride, uint32_t& status,
-                       uint32_t& cnt_nodes, uint32_t& cnt_tris) {
-    const RayPre& r = s.r;
+// Pops the next node of the ray's traversal into `node`.  Returns false
+// when the traversal is finished (empty stack) or stopped with a status bit:
+// stack overflow, or the iteration cap (node_count + 64 node visits) that
+// ends a ray whose BVH links cycle, or a node index out of range.
+template <int kStack>
+MRT_DEV bool next_node(const DevScene& sc, Trav& s, uint2* stk, uint32_t stride, uint32_t& status, uint32_t& node) {
     if (s.g_hits == 0u) {
-        if (s.sp == 0) return true;
+        if (s.sp == 0) return false;
         --s.sp;
         const uint2 e = stk[s.sp * stride];
         s.g_base = e.x;
@@ -173,82 +170,110 @@ MRT_DEV bool trav_step(const DevScene& sc, Trav& s, uint2* stk, uint32_t stride,
     }
     const uint32_t key = __ffs(s.g_hits) - 1u;
     s.g_hits &= s.g_hits - 1u;
-    const uint32_t slot = key ^ r.oct;
-    const uint32_t node = s.g_base + __popc(s.g_imask & ((1u << slot) - 1u));
+    const uint32_t slot = key ^ s.r.oct;
+    node = s.g_base + __popc(s.g_imask & ((1u << slot) - 1u));
     if (s.g_hits) {
-        if (s.sp >= kStack) { status |= MRT_STATUS_STACK_OVF; return true; }
+        if (s.sp >= kStack) { status |= MRT_STATUS_STACK_OVF; return false; }
         stk[s.sp * stride] = make_uint2(s.g_base, (s.g_hits << 8) | s.g_imask);
         ++s.sp;
     }
-    if (++s.iters > sc.node_count + 64u) { status |= MRT_STATUS_ITER_CAP; return true; }
-    if (node >= sc.node_count) { status |= MRT_STATUS_BAD_NODE; return true; }
-    if (kCount) ++cnt_nodes;
-    {
-        const float tmin = s.tmin, tbest = s.tbest;
-        const bool negx = r.ix < 0.0f, negy = r.iy < 0.0f, negz = r.iz < 0.0f;
+    if (++s.iters > sc.node_count + 64u) { status |= MRT_STATUS_ITER_CAP; return false; }
+    if (node >= sc.node_count) { status |= MRT_STATUS_BAD_NODE; return false; }
+    return true;
+}
 
-        const uint4* np = sc.nodes + size_t(node) * 8u;
-        const uint4 L0 = __ldg(np + 0), L1 = __ldg(np + 1), L2 = __ldg(np + 2), L3 = __ldg(np + 3),
-                    L4 = __ldg(np + 4);
-        const int ex = int(int8_t(L0.w & 0xFFu)), ey = int(int8_t((L0.w >> 8) & 0xFFu)),
-                  ez = int(int8_t((L0.w >> 16) & 0xFFu));
-        const uint32_t imask = L0.w >> 24;
-        const float scx = __fmul_rn(__int_as_float((ex + 127) << 23), r.ix);
-        const float scy = __fmul_rn(__int_as_float((ey + 127) << 23), r.iy);
-        const float scz = __fmul_rn(__int_as_float((ez + 127) << 23), r.iz);
-        const float adx = __fmul_rn(__fsub_rn(__uint_as_float(L0.x), r.o.x), r.ix);
-        const float ady = __fmul_rn(__fsub_rn(__uint_as_float(L0.y), r.o.y), r.iy);
-        const float adz = __fmul_rn(__fsub_rn(__uint_as_float(L0.z), r.o.z), r.iz);
-        // near/far quantised planes per axis, chosen by the direction sign
-        const uint32_t nx0 = negx ? L3.z : L2.x, nx1 = negx ? L3.w : L2.y;
-        const uint32_t fx0 = negx ? L2.x : L3.z, fx1 = negx ? L2.y : L3.w;
-        const uint32_t ny0 = negy ? L4.x : L2.z, ny1 = negy ? L4.y : L2.w;
-        const uint32_t fy0 = negy ? L2.z : L4.x, fy1 = negy ? L2.w : L4.y;
-        const uint32_t nz0 = negz ? L4.z : L3.x, nz1 = negz ? L4.w : L3.y;
-        const uint32_t fz0 = negz ? L3.x : L4.z, fz1 = negz ? L3.y : L4.w;
+// Box tests of the 8 children of one node: the hit interior children become
+// the ray's current group (s.g_*); the triangles of the hit leaves are
+// returned as a bit mask relative to tri_base.
+MRT_DEV uint32_t visit_node(const DevScene& sc, Trav& s, uint32_t node, uint32_t& tri_base) {
+    const RayPre& r = s.r;
+    const float tmin = s.tmin, tbest = s.tbest;
+    const bool negx = r.ix < 0.0f, negy = r.iy < 0.0f, negz = r.iz < 0.0f;
 
-        uint32_t int_keys = 0u, tri_mask = 0u;
+    const uint4* np = sc.nodes + size_t(node) * 8u;
+    const uint4 L0 = __ldg(np + 0), L1 = __ldg(np + 1), L2 = __ldg(np + 2), L3 = __ldg(np + 3),
+                L4 = __ldg(np + 4);
+    const int ex = int(int8_t(L0.w & 0xFFu)), ey = int(int8_t((L0.w >> 8) & 0xFFu)),
+              ez = int(int8_t((L0.w >> 16) & 0xFFu));
+    const uint32_t imask = L0.w >> 24;
+    const float scx = __fmul_rn(__int_as_float((ex + 127) << 23), r.ix);
+    const float scy = __fmul_rn(__int_as_float((ey + 127) << 23), r.iy);
+    const float scz = __fmul_rn(__int_as_float((ez + 127) << 23), r.iz);
+    const float adx = __fmul_rn(__fsub_rn(__uint_as_float(L0.x), r.o.x), r.ix);
+    const float ady = __fmul_rn(__fsub_rn(__uint_as_float(L0.y), r.o.y), r.iy);
+    const float adz = __fmul_rn(__fsub_rn(__uint_as_float(L0.z), r.o.z), r.iz);
+    // near/far quantised planes per axis, chosen by the direction sign
+    const uint32_t nx0 = negx ? L3.z : L2.x, nx1 = negx ? L3.w : L2.y;
+    const uint32_t fx0 = negx ? L2.x : L3.z, fx1 = negx ? L2.y : L3.w;
+    const uint32_t ny0 = negy ? L4.x : L2.z, ny1 = negy ? L4.y : L2.w;
+    const uint32_t fy0 = negy ? L2.z : L4.x, fy1 = negy ? L2.w : L4.y;
+    const uint32_t nz0 = negz ? L4.z : L3.x, nz1 = negz ? L4.w : L3.y;
+    const uint32_t fz0 = negz ? L3.x : L4.z, fz1 = negz ? L3.y : L4.w;
+
+    uint32_t int_keys = 0u, tri_mask = 0u;
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const uint32_t k = uint32_t(i & 3);
-            const float tnx = fmaf(byte_to_float(i < 4 ? nx0 : nx1, k), scx, adx);
-            const float tny = fmaf(byte_to_float(i < 4 ? ny0 : ny1, k), scy, ady);
-            const float tnz = fmaf(byte_to_float(i < 4 ? nz0 : nz1, k), scz, adz);
-            const float tfx = fmaf(byte_to_float(i < 4 ? fx0 : fx1, k), scx, adx);
-            const float tfy = fmaf(byte_to_float(i < 4 ? fy0 : fy1, k), scy, ady);
-            const float tfz = fmaf(byte_to_float(i < 4 ? fz0 : fz1, k), scz, adz);
-            const float tn = max3f(tnx, tny, fmaxf(tnz, tmin));
-            const float tf = min3f(tfx, tfy, fminf(tfz, tbest));
-            if (tn <= __fmul_rn(tf, kRobustScale)) {
-                const uint32_t meta = ((i < 4 ? L1.z : L1.w) >> (8 * k)) & 0xFFu;
-                if ((imask >> i) & 1u) int_keys |= 1u << (uint32_t(i) ^ r.oct);
-                else tri_mask |= (meta >> 5) << (meta & 31u);
-            }
+    for (int i = 0; i < 8; ++i) {
+        const uint32_t k = uint32_t(i & 3);
+        const float tnx = fmaf(byte_to_float(i < 4 ? nx0 : nx1, k), scx, adx);
+        const float tny = fmaf(byte_to_float(i < 4 ? ny0 : ny1, k), scy, ady);
+        const float tnz = fmaf(byte_to_float(i < 4 ? nz0 : nz1, k), scz, adz);
+        const float tfx = fmaf(byte_to_float(i < 4 ? fx0 : fx1, k), scx, adx);
+        const float tfy = fmaf(byte_to_float(i < 4 ? fy0 : fy1, k), scy, ady);
+        const float tfz = fmaf(byte_to_float(i < 4 ? fz0 : fz1, k), scz, adz);
+        const float tn = max3f(tnx, tny, fmaxf(tnz, tmin));
+        const float tf = min3f(tfx, tfy, fminf(tfz, tbest));
+        if (tn <= __fmul_rn(tf, kRobustScale)) {
+            const uint32_t meta = ((i < 4 ? L1.z : L1.w) >> (8 * k)) & 0xFFu;
+            if ((imask >> i) & 1u) int_keys |= 1u << (uint32_t(i) ^ r.oct);
+            else tri_mask |= (meta >> 5) << (meta & 31u);
         }
-        s.g_base = L1.x;
-        s.g_hits = int_keys;
-        s.g_imask = imask;
+    }
+    s.g_base = L1.x;
+    s.g_hits = int_keys;
+    s.g_imask = imask;
+    tri_base = L1.y;
+    return tri_mask;
+}
 
-        const uint32_t tri_base = L1.y;
-        while (tri_mask) {
-            const uint32_t bit = __ffs(tri_mask) - 1u;
-            tri_mask &= tri_mask - 1u;
-            const uint32_t ti = tri_base + bit;
-            if (ti >= sc.tri_count) { status |= MRT_STATUS_BAD_TRI; return true; }
-            if (kCount) ++cnt_tris;
-            const float4* tp = sc.tris + size_t(ti) * 3u;
-            const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), c = __ldg(tp + 2);
-            float t;
-            if (intersect_tri(r, a, b, c, tmin, t)) {
-                const uint32_t id = __float_as_uint(a.w);
-                if (kAnyHit) {
-                    if (t < s.tmax) { s.best = id; s.tbest = t; return true; }
-                } else if (t < s.tbest || (t == s.tbest && id < s.best)) {
-                    s.tbest = t;
-                    s.best = id;
-                }
-            }
+// Watertight test of triangle ti against the ray.  Closest hit: keeps the
+// nearest t, ties to the lower primitive id (the result does not depend on
+// the order of the tests).  Any hit: returns true at the first t < tmax.
+// A triangle index out of range sets a status bit and returns true.
+template <bool kAnyHit>
+MRT_DEV bool test_tri(const DevScene& sc, Trav& s, uint32_t ti, uint32_t& status) {
+    if (ti >= sc.tri_count) { status |= MRT_STATUS_BAD_TRI; return true; }
+    const float4* tp = sc.tris + size_t(ti) * 3u;
+    const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), c = __ldg(tp + 2);
+    float t;
+    if (intersect_tri(s.r, a, b, c, s.tmin, t)) {
+        const uint32_t id = __float_as_uint(a.w);
+        if (kAnyHit) {
+            if (t < s.tmax) { s.best = id; s.tbest = t; return true; }
+        } else if (t < s.tbest || (t == s.tbest && id < s.best)) {
+            s.tbest = t;
+            s.best = id;
         }
+    }
+    return false;
+}
+
+// One traversal step: visit the next node and test the triangles of its hit
+// leaves.  Returns true when the ray is finished (s.best / s.tbest hold the
+// result).  Every path through the step is bounded: one node and at most 24
+// triangle tests.
+template <bool kAnyHit, bool kCount, int kStack>
+MRT_DEV bool trav_step(const DevScene& sc, Trav& s, uint2* stk, uint32_t stride, uint32_t& status,
+                       uint32_t& cnt_nodes, uint32_t& cnt_tris) {
+    uint32_t node;
+    if (!next_node<kStack>(sc, s, stk, stride, status, node)) return true;
+    if (kCount) ++cnt_nodes;
+    uint32_t tri_base;
+    uint32_t tri_mask = visit_node(sc, s, node, tri_base);
+    while (tri_mask) {
+        const uint32_t bit = __ffs(tri_mask) - 1u;
+        tri_mask &= tri_mask - 1u;
+        if (kCount) ++cnt_tris;
+        if (test_tri<kAnyHit>(sc, s, tri_base + bit, status)) return true;
     }
     return s.g_hits == 0u && s.sp == 0;
 }
