@@ -1,32 +1,31 @@
 // tcgen05 implicit-GEMM 3x3 convolution for the denoiser (included inside
 // denoise.cu's anonymous namespace, after ConvArgs).
 //
-// One CTA (4 warps) computes two output rows x 128 consecutive pixels x all
-// COUT channels as two GEMMs on the 5th-generation tensor cores: M = 128
+// One CTA (4 warps) computes ROWS output rows x 128 consecutive pixels x all
+// COUT channels as ROWS GEMMs on the 5th-generation tensor cores: M = 128
 // pixels per row, N = COUT, K = 9 taps x Cin, FP32 accumulators in tensor
 // memory (row r in columns [r * COUT, (r + 1) * COUT)).  The input is walked
 // in 16-channel slices of the virtual, concatenated, possibly upsampled
-// input; for each slice the CTA stages the 4-row x 130-pixel halo and the
-// slice's 9 x COUT weights in shared memory, in the canonical no-swizzle
+// input; for each slice the CTA stages the (ROWS + 2)-row x 130-pixel halo and
+// the slice's 9 x COUT weights in shared memory, in the canonical no-swizzle
 // K-major layout: each 8-channel half is a plane of 16-byte rows, so a core
 // matrix is 8 consecutive rows (SBO = 128 B) and the second K half sits one
 // plane further (LBO = the plane size).  A tap's A operand is the halo plane
 // of its input row shifted by its column, i.e. a start address 16 * dx bytes
-// later: the im2col never exists, and the two output rows share the weight
-// slice.  Slices stream through kStages shared-memory stages with cp.async
+// later: the im2col never exists, and the output rows share the weight
+// slice.  Slices stream through STAGES shared-memory stages with cp.async
 // (16-byte copies, zero-filled outside the image): while the tensor cores
-// run the 18 MMAs of slice k (issued by one thread and committed to that
-// stage's mbarrier) the copies of the next kStages - 1 slices are in flight.
+// run the 9 x ROWS MMAs of slice k (issued by one thread and committed to that
+// stage's mbarrier) the copies of the next STAGES - 1 slices are in flight.
 // The epilogue reads the accumulators with tcgen05.ld (warp w owns TMEM
 // lanes 32w..32w+31 = pixels 32w..32w+31), adds the bias, applies ReLU and
 // stores BF16 with 16-byte stores.
 #pragma once
 
 constexpr int kTcPix = 128;             // output pixels per row of a CTA (MMA M)
-constexpr int kTcRows = 2;              // output rows per CTA
 constexpr int kTcHalo = kTcPix + 2;     // input pixels per halo row
 constexpr int kTcPlane = kTcHalo * 16;  // bytes of one 8-channel halo plane
-constexpr int kTcAbytes = (kTcRows + 2) * 2 * kTcPlane;
+__host__ __device__ constexpr int tc_abytes(int rows) { return (rows + 2) * 2 * kTcPlane; }
 constexpr uint32_t kTcSpin = 1u << 26;  // mbarrier wait cap (polls)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -43,11 +42,20 @@ __device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint3
 __host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(m >> 4) << 24);
 }
-// pipeline depth: three stages where two CTAs still fit an SM, two for
-// COUT = 128 (its weight slices are large)
-__host__ __device__ constexpr int tc_stages(int cout) { return cout >= 128 ? 2 : 3; }
-constexpr size_t tc_stage_bytes(int cout) { return size_t(kTcAbytes) + size_t(9) * 2 * cout * 16; }
-constexpr size_t tc_smem_bytes(int cout) { return tc_stages(cout) * tc_stage_bytes(cout) + 64; }
+// Output rows per CTA and pipeline depth per COUT, from a sweep on the 1080p
+// denoiser (ms per frame: 2 rows everywhere 2.19, 4 rows up to COUT 64 1.77,
+// 8 rows below COUT 64 and 4 above with two stages 1.70).  More rows share
+// each weight slice and amortise the 2-row halo; COUT <= 64 keeps two CTAs
+// per SM (<= 113 KB of shared memory, <= 256 tensor-memory columns each),
+// COUT 128 runs one (512 columns).
+__host__ __device__ constexpr int tc_rows(int cout) { return cout >= 64 ? 4 : 8; }
+__host__ __device__ constexpr int tc_stages(int) { return 2; }
+__host__ __device__ constexpr size_t tc_stage_bytes(int cout, int rows) {
+    return size_t(tc_abytes(rows)) + size_t(9) * 2 * cout * 16;
+}
+__host__ __device__ constexpr size_t tc_smem_bytes(int cout, int rows, int stages) {
+    return stages * tc_stage_bytes(cout, rows) + 64;
+}
 
 // Bounded wait for phase `parity` of an mbarrier; false when the cap ran out.
 __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
@@ -68,12 +76,12 @@ __device__ __forceinline__ void cp16(uint32_t saddr, const void* g, bool valid) 
                  : "memory");
 }
 
-template <int COUT>
+template <int COUT, int ROWS>
 __device__ __forceinline__ void tc_load_slice(const ConvArgs& a, uint32_t As, uint32_t Bs, int n, int y0, int x0,
                                               int c0, int cin, int ha, int wa) {
     const int tid = threadIdx.x;
-    // halo: input rows y0-1..y0+2, pixels x0-1..x0+128, channels c0..c0+15
-    for (int i = tid; i < (kTcRows + 2) * 2 * kTcHalo; i += 128) {
+    // halo: input rows y0-1..y0+ROWS, pixels x0-1..x0+128, channels c0..c0+15
+    for (int i = tid; i < (ROWS + 2) * 2 * kTcHalo; i += 128) {
         const int hf = i & 1, p = (i >> 1) % kTcHalo, r = (i >> 1) / kTcHalo;
         const int yy = y0 - 1 + r, xx = x0 - 1 + p, c = c0 + 8 * hf;
         const bool in = yy >= 0 && yy < a.h && xx >= 0 && xx < a.w_;
@@ -95,19 +103,21 @@ __device__ __forceinline__ void tc_load_slice(const ConvArgs& a, uint32_t As, ui
     }
 }
 
-template <int COUT>
+template <int COUT, int ROWS, int STAGES>
 __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
-    constexpr int kAcc = kTcRows * COUT;
+    constexpr int kAcc = ROWS * COUT;
     constexpr int kCols = kAcc < 32 ? 32 : kAcc;  // TMEM columns (power of 2, >= 32)
-    constexpr int kStages = tc_stages(COUT);
-    constexpr uint32_t kStage = uint32_t(tc_stage_bytes(COUT));
+    static_assert(kCols <= 512 && (kCols & (kCols - 1)) == 0, "tensor memory columns");
+    constexpr int kStages = STAGES;
+    constexpr int kTcAbytes = tc_abytes(ROWS);
+    constexpr uint32_t kStage = uint32_t(tc_stage_bytes(COUT, ROWS));
     extern __shared__ __align__(128) unsigned char tsm[];
     uint64_t* mbar = reinterpret_cast<uint64_t*>(tsm + kStages * kStage);  // one per stage
     uint32_t* slot = reinterpret_cast<uint32_t*>(mbar + kStages);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int tiles_x = (a.w_ + kTcPix - 1) / kTcPix, rows_per_img = (a.h + kTcRows - 1) / kTcRows;
+    const int tiles_x = (a.w_ + kTcPix - 1) / kTcPix, rows_per_img = (a.h + ROWS - 1) / ROWS;
     const int tx = blockIdx.x % tiles_x, rb = blockIdx.x / tiles_x;
-    const int y0 = (rb % rows_per_img) * kTcRows, n = rb / rows_per_img;
+    const int y0 = (rb % rows_per_img) * ROWS, n = rb / rows_per_img;
     const int x0 = tx * kTcPix;
     const int cin = a.ca + a.cb, nk = cin / 16;
     const int ha = a.ups ? a.h >> 1 : a.h, wa = a.ups ? a.w_ >> 1 : a.w_;
@@ -126,7 +136,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
     }
     // prologue: slices 0 .. kStages-2 in flight
     for (int s = 0; s < kStages - 1; ++s) {
-        if (s < nk) tc_load_slice<COUT>(a, smem0 + s * kStage, smem0 + s * kStage + kTcAbytes, n, y0, x0, 16 * s, cin,
+        if (s < nk) tc_load_slice<COUT, ROWS>(a, smem0 + s * kStage, smem0 + s * kStage + kTcAbytes, n, y0, x0, 16 * s, cin,
                                         ha, wa);
         asm volatile("cp.async.commit_group;\n" ::: "memory");
     }
@@ -149,7 +159,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t abase = smem0 + uint32_t(s) * kStage, bbase = abase + kTcAbytes;
 #pragma unroll
-            for (int r = 0; r < kTcRows; ++r)
+            for (int r = 0; r < ROWS; ++r)
 #pragma unroll
                 for (int t = 0; t < 9; ++t) {
                     const int ky = t / 3, kx = t % 3;
@@ -177,7 +187,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
             timed_out = __syncthreads_or(timed_out) != 0;
             if (timed_out) break;
             const uint32_t st = smem0 + uint32_t(j % kStages) * kStage;
-            tc_load_slice<COUT>(a, st, st + kTcAbytes, n, y0, x0, 16 * j, cin, ha, wa);
+            tc_load_slice<COUT, ROWS>(a, st, st + kTcAbytes, n, y0, x0, 16 * j, cin, ha, wa);
         }
         asm volatile("cp.async.commit_group;\n" ::: "memory");
     }
@@ -194,7 +204,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
     if (!timed_out) {
         const int m = 32 * warp + lane, x = x0 + m;
 #pragma unroll
-        for (int r = 0; r < kTcRows; ++r) {
+        for (int r = 0; r < ROWS; ++r) {
             const int y = y0 + r;
             bf16* dst = a.y + ((size_t(n) * a.h + y) * a.w_ + x) * COUT;
 #pragma unroll
@@ -238,14 +248,16 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
 
 template <int COUT>
 cudaError_t launch_conv_tc(const ConvArgs& ca, uint32_t* status, cudaStream_t s) {
+    constexpr int kRows = tc_rows(COUT), kStages = tc_stages(COUT);
     static bool configured = false;  // per process; all devices are sm_103
-    const size_t smem = tc_smem_bytes(COUT);
+    const size_t smem = tc_smem_bytes(COUT, kRows, kStages);
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_conv_tc<COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        cudaError_t e = cudaFuncSetAttribute(k_conv_tc<COUT, kRows, kStages>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    const int blocks = ((ca.w_ + kTcPix - 1) / kTcPix) * ((ca.h + kTcRows - 1) / kTcRows) * ca.n;
-    k_conv_tc<COUT><<<blocks, 128, smem, s>>>(ca, status);
+    const int blocks = ((ca.w_ + kTcPix - 1) / kTcPix) * ((ca.h + kRows - 1) / kRows) * ca.n;
+    k_conv_tc<COUT, kRows, kStages><<<blocks, 128, smem, s>>>(ca, status);
     return cudaGetLastError();
 }
