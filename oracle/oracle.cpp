@@ -15,14 +15,17 @@
 //   quantised BVH8 decode + stack traversal    Ylitie, Karras & Laine, HPG 2017
 //   directional-light path estimator           (new; specified in the design notes)
 //
-// Parity status: PARITY UNPINNED.  The reference ships no tests, golden
-// vectors or fixtures, and its own implementation (GLSL through Vulkan,
-// MSVC-only host code) cannot run here, so nothing of the reference itself
-// pins this restatement.  It is checked instead against (a) known-answer
-// values computed independently from the formulas in the reference source
-// (PCG, 24-bit floats, sphere points, the camera matrices; analytic
-// ray/sphere and ray/triangle cases) committed under tests/golden, and
-// (b) brute-force cross-checks of its own BVH traversal.
+// Parity status: pinned to the reference's own shaders.  The reference ships
+// no tests or golden vectors and its GPU path (GLSL through Vulkan) cannot
+// run here, so its compute shaders are compiled for the host instead
+// (oracle/glsl: a mechanical GLSL -> C++ rewrite of the sources where they
+// lie, against a small model of GLSL's types and built-ins) and the tests
+// compare this file with them: random.glsl, raySphereIntersect, the primary
+// pass's g-buffer and the secondary pass's colour under the sky agree bit for
+// bit (tests/test_oracle_glsl_pins.py, with vectors committed under
+// tests/golden for machines without the reference tree).  The triangle /
+// BVH8 / NEE parts have no counterpart in the reference; they are checked by
+// analytic cases and brute-force cross-checks of the BVH traversal.
 //
 // FP32 mode reproduces the kernels' arithmetic order (explicit fma where the
 // kernels use one, no contraction elsewhere; built with -ffp-contract=off),

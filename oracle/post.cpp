@@ -1,8 +1,9 @@
 // CPU oracle, part 2 (TEST INFRASTRUCTURE ONLY): sky / atmosphere LUTs and
 // miss shader, joint bilateral filter, tonemappers, temporal reprojection.
 //
-// PARITY UNPINNED: the reference's shaders need a Vulkan device and glslc,
-// neither of which exists here, and the reference ships no golden images.
+// Pinned to the reference's own shaders compiled for the host (oracle/glsl,
+// tests/test_oracle_glsl_pins.py): the sky LUTs and the tonemappers agree
+// bit for bit, the bilateral filter to 1e-5 (its sample positions).
 // This file restates the reference's shader arithmetic in plain FP32 C++
 // (compiled with -ffp-contract=off, so every + - * / rounds separately),
 // expression by expression and in the same evaluation order as the GLSL:
