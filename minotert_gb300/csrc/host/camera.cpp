@@ -35,6 +35,12 @@ inline V3 normalize3(V3 v) {
 }
 
 // column-major element access: m[col*4 + row]
+// sin / cos / tan of a binary32 angle, evaluated in binary64 and rounded
+// once, so the matrices have the same bits on every host
+inline float sin_(float x) { return float(std::sin(double(x))); }
+inline float cos_(float x) { return float(std::cos(double(x))); }
+inline float tan_(float x) { return float(std::tan(double(x))); }
+
 inline float& el(float* m, int col, int row) { return m[col * 4 + row]; }
 inline float el(const float* m, int col, int row) { return m[col * 4 + row]; }
 
@@ -51,7 +57,7 @@ void look(V3 pos, V3 dir, V3 up, float* out) {
 }
 
 void perspective(float vfov, float aspect, float znear, float* out) {
-    float h = 1.0f / std::tan(0.5f * vfov);
+    float h = 1.0f / tan_(0.5f * vfov);
     float w = h * aspect;
     for (int i = 0; i < 16; ++i) out[i] = 0.0f;
     el(out, 0, 0) = w;
@@ -65,8 +71,8 @@ void perspective(float vfov, float aspect, float znear, float* out) {
 extern "C" {
 
 void mrt_camera_view(const mrt_camera* cam, float out[16]) {
-    float cp = std::cos(cam->pitch), sp = std::sin(cam->pitch);
-    float cy = std::cos(cam->yaw), sy = std::sin(cam->yaw);
+    float cp = cos_(cam->pitch), sp = sin_(cam->pitch);
+    float cy = cos_(cam->yaw), sy = sin_(cam->yaw);
     V3 dir{cp * cy, cp * sy, sp};
     look(V3{cam->position[0], cam->position[1], cam->position[2]}, dir, V3{0.0f, 0.0f, 1.0f}, out);
 }

@@ -14,8 +14,9 @@
 //    normalize(x) = x / length(x); length(x) = sqrt(dot(x, x));
 //  * min / max / clamp return the non-NaN operand (IEEE minNum / maxNum,
 //    what GPUs execute);
-//  * transcendental functions are the C library's binary32 ones, except exp
-//    under GLSL_EXP_CW (the sky and filter shaders), which is the oracle's;
+//  * transcendental functions are evaluated in binary64 and rounded once to
+//    binary32 (the same bits on every host), except exp under GLSL_EXP_CW
+//    (the sky and filter shaders), which is the oracle's Cody-Waite form;
 //  * texture()/textureLod() filter bilinearly with clamp-to-edge addressing
 //    and FP32 weights (x first, then y); texelFetch() reads the texel.
 #pragma once
@@ -194,7 +195,7 @@ inline float smoothstep(float e0, float e1, float x) {
 }
 inline float sqrt(float x) { return std::sqrt(x); }
 inline float inversesqrt(float x) { return 1.0f / std::sqrt(x); }
-inline float pow(float x, float y) { return std::pow(x, y); }
+inline float pow(float x, float y) { return float(std::pow(double(x), double(y))); }
 #ifdef GLSL_EXP_CW
 // e^x by Cody-Waite reduction x = n ln2 + r (ln2 split into a 16-bit head
 // and a tail), the degree-7 Taylor polynomial of e^r in Horner form with
@@ -219,18 +220,18 @@ inline float exp(float x) {
     return q * std::ldexp(1.0f, e);
 }
 #else
-inline float exp(float x) { return std::exp(x); }
+inline float exp(float x) { return float(std::exp(double(x))); }
 #endif
-inline float exp2(float x) { return std::exp2(x); }
-inline float log(float x) { return std::log(x); }
-inline float log2(float x) { return std::log2(x); }
-inline float sin(float x) { return std::sin(x); }
-inline float cos(float x) { return std::cos(x); }
-inline float tan(float x) { return std::tan(x); }
-inline float asin(float x) { return std::asin(x); }
-inline float acos(float x) { return std::acos(x); }
-inline float atan(float y, float x) { return std::atan2(y, x); }
-inline float atan(float x) { return std::atan(x); }
+inline float exp2(float x) { return float(std::exp2(double(x))); }
+inline float log(float x) { return float(std::log(double(x))); }
+inline float log2(float x) { return float(std::log2(double(x))); }
+inline float sin(float x) { return float(std::sin(double(x))); }
+inline float cos(float x) { return float(std::cos(double(x))); }
+inline float tan(float x) { return float(std::tan(double(x))); }
+inline float asin(float x) { return float(std::asin(double(x))); }
+inline float acos(float x) { return float(std::acos(double(x))); }
+inline float atan(float y, float x) { return float(std::atan2(double(y), double(x))); }
+inline float atan(float x) { return float(std::atan(double(x))); }
 
 #define GLSL_UNARY(F)                                                                                         \
     inline vec2 F(const vec2& v) { return {F(v.x), F(v.y)}; }                                                 \

@@ -99,12 +99,19 @@ template <typename F> V3<F> normalize(V3<F> v) {
 }
 template <typename F> F comp(V3<F> v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
 
+// sin / cos / tan of a binary32 argument, evaluated in binary64 and rounded
+// once: the same bits on every host (the C library's binary32 versions
+// differ between x86-64 and AArch64 in the last place)
+template <typename F> F sin_(F x) { return F(std::sin(double(x))); }
+template <typename F> F cos_(F x) { return F(std::cos(double(x))); }
+template <typename F> F tan_(F x) { return F(std::tan(double(x))); }
+
 template <typename F> V3<F> sphere_point(F rx, F ry) {
     const F Pi = F(3.14159265359f);
     F ang1 = (rx + F(1)) * Pi;
     F u = ry;
     F s = std::sqrt(F(1) - u * u);
-    return {s * std::cos(ang1), s * std::sin(ang1), u};
+    return {s * cos_(ang1), s * sin_(ang1), u};
 }
 
 // column-major mat4 * vec4: sequential non-FMA dot per row (math.ixx:699)
@@ -173,7 +180,7 @@ struct Cam { float pos[3], yaw, pitch, fov, znear; uint32_t w, h; };
 
 void cam_view(const Cam& c, float* out) {
     // camera.ixx:19-35: direction from yaw/pitch, look(pos, dir, +Z)
-    V3<float> dir{std::cos(c.pitch) * std::cos(c.yaw), std::cos(c.pitch) * std::sin(c.yaw), std::sin(c.pitch)};
+    V3<float> dir{cos_(c.pitch) * cos_(c.yaw), cos_(c.pitch) * sin_(c.yaw), sin_(c.pitch)};
     V3<float> up{0.0f, 0.0f, 1.0f};
     auto cross = [](V3<float> l, V3<float> r) {
         return V3<float>{l.y * r.z - r.y * l.z, l.z * r.x - r.z * l.x, l.x * r.y - r.x * l.y};
@@ -197,7 +204,7 @@ void cam_view(const Cam& c, float* out) {
 void cam_proj(const Cam& c, float* out) {
     // math.ixx:848-861 with aspect = h / w (camera.ixx:38-41)
     float aspect = float(c.h) / float(c.w);
-    float hh = 1.0f / std::tan(0.5f * c.fov);
+    float hh = 1.0f / tan_(0.5f * c.fov);
     float ww = hh * aspect;
     for (int i = 0; i < 16; ++i) out[i] = 0.0f;
     out[0] = ww;

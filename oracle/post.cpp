@@ -66,6 +66,14 @@ float exp_cw(float x) {
     std::memcpy(&s, &bits, 4);
     return p * s;
 }
+// binary32 transcendental functions evaluated in binary64 and rounded once:
+// the same bits on every host (the C library's binary32 versions differ
+// between x86-64 and AArch64 in the last place)
+inline float acos_(float x) { return float(std::acos(double(x))); }
+inline float cos_(float x) { return float(std::cos(double(x))); }
+inline float sin_(float x) { return float(std::sin(double(x))); }
+inline float pow_(float x, float y) { return float(std::pow(double(x), double(y))); }
+inline float exp_(float x) { return float(std::exp(double(x))); }
 inline V3 vexp(V3 a) { return V3{exp_cw(a.x), exp_cw(a.y), exp_cw(a.z)}; }
 inline float clampf(float x, float lo, float hi) { return std::fmin(std::fmax(x, lo), hi); }
 
@@ -150,16 +158,16 @@ void trans_params(float u, float v, float bottom, float top, float& h, float& mu
 // skyAccess.glsl skyViewLutParamsToUv (non-linear)
 void view_uv(bool ground, float mu, float lv, float h, float bottom, float& u, float& v) {
     const float vh = std::sqrt(h * h - bottom * bottom);
-    const float beta = std::acos(vh / h);
+    const float beta = acos_(vh / h);
     const float zha = kPi - beta;
     if (!ground) {
-        float c = std::acos(mu) / zha;
+        float c = acos_(mu) / zha;
         c = 1.0f - c;
         c = std::sqrt(c);
         c = 1.0f - c;
         v = c * 0.5f;
     } else {
-        float c = (std::acos(mu) - zha) / beta;
+        float c = (acos_(mu) - zha) / beta;
         c = std::sqrt(c);
         v = c * 0.5f + 0.5f;
     }
@@ -173,18 +181,18 @@ void view_params(float u, float v, float h, float bottom, float& mu, float& lv) 
     u = from_sub(u, float(kVW));
     v = from_sub(v, float(kVH));
     const float vh = std::sqrt(h * h - bottom * bottom);
-    const float beta = std::acos(vh / h);
+    const float beta = acos_(vh / h);
     const float zha = kPi - beta;
     if (v < 0.5f) {
         float c = 2.0f * v;
         c = 1.0f - c;
         c *= c;
         c = 1.0f - c;
-        mu = std::cos(zha * c);
+        mu = cos_(zha * c);
     } else {
         float c = v * 2.0f - 1.0f;
         c *= c;
-        mu = std::cos(zha + beta * c);
+        mu = cos_(zha + beta * c);
     }
     float c = u;
     c *= c;
@@ -240,7 +248,7 @@ March integrate(const Atmo& a, V3 pos, V3 dir, V3 sun, bool ground, float count,
     const float g = a.mie_g;
     const float mc = -ct;  // cornetteShanksMiePhaseFunction(g, -cosTheta)
     const float k = 3.0f / (8.0f * kPi) * (1.0f - g * g) / (2.0f + g * g);
-    const float mie_phase = k * (1.0f + mc * mc) / std::pow(1.0f + g * g - 2.0f * g * -mc, 1.5f);
+    const float mie_phase = k * (1.0f + mc * mc) / pow_(1.0f + g * g - 2.0f * g * -mc, 1.5f);
     const float ray_phase = 3.0f / (16.0f * kPi) * (1.0f + ct * ct);
     const float uni = 1.0f / (4.0f * kPi);
     V3 thr = v3(1.0f);
@@ -304,14 +312,14 @@ March integrate(const Atmo& a, V3 pos, V3 dir, V3 sun, bool ground, float count,
 
 V3 sun_luminance(const Atmo& a, const float* trans, V3 pos, V3 dir, V3 sun, V3 sun_e) {
     const float radius = 0.5f * 0.505f * 3.14159f / 180.0f;
-    if (!(dot(dir, sun) > std::cos(radius))) return v3(0.0f);
+    if (!(dot(dir, sun) > cos_(radius))) return v3(0.0f);
     if (sphere_nearest(pos, dir, v3(0.0f), a.bottom) >= 0.0f) return v3(0.0f);
     float uu, vu, us, vs;
     trans_uv(a.bottom, 1.0f, a.bottom, a.top, uu, vu);
     const float ph = length(pos);
     const V3 up = pos / ph;
     trans_uv(ph, dot(sun, up), a.bottom, a.top, us, vs);
-    const float ang = std::acos(clampf(dot(dir, sun), -1.0f, 1.0f));
+    const float ang = acos_(clampf(dot(dir, sun), -1.0f, 1.0f));
     const float rr = ang / radius;
     const float limb = std::sqrt(clampf(1.0f - rr * rr, 0.0001f, 1.0f));
     const V3 space = sun_e / sample(trans, kTW, kTH, uu, vu);
@@ -355,7 +363,7 @@ void orc_sky_multiscatter(const Atmo* a, const float* trans, float* out) {
             for (int z = 0; z < 64; ++z) {
                 const float iv = 0.5f + float(z / 8), jv = 0.5f + float(z % 8);
                 const float theta = 2.0f * kPi * (iv / 8.0f), phi = kPi * (jv / 8.0f);
-                const V3 dir{std::cos(theta) * std::sin(phi), std::sin(theta) * std::sin(phi), std::cos(phi)};
+                const V3 dir{cos_(theta) * sin_(phi), sin_(theta) * sin_(phi), cos_(phi)};
                 const March m = integrate(*a, V3{0.0f, 0.0f, h}, dir, sun, true, 20.0f, false, false, v3(1.0f),
                                           trans, nullptr);
                 sms[z] = m.ms_as1 * sphere / 64.0f;
@@ -520,7 +528,7 @@ extern "C" int orc_bilateral(const float* color, const float* depth, const float
                     const float fr = -pt - f0, gr = 1.0f - fr;
                     int row = int(y) + int(f0);
                     for (float dy = -pt; dy <= pt; dy += 1.0f, ++row) {
-                        const float blur = std::exp(-(dx * dx + dy * dy) * inv_sq2) * inv_sq2pi;
+                        const float blur = exp_(-(dx * dx + dy * dy) * inv_sq2) * inv_sq2pi;
                         const size_t a = at(int(x) + c - r, row), b = at(int(x) + c - r, row + 1);
                         const float wz = depth[a] * gr + depth[b] * fr;
                         const float wn[3] = {normal[3 * a] * gr + normal[3 * b] * fr,
@@ -554,7 +562,7 @@ extern "C" int orc_bilateral(const float* color, const float* depth, const float
 // ---- tonemappers (src/gpu/tonemap/*.comp, util.glsl:13-18) ----------------
 namespace {
 
-float srgb1(float c) { return c < 0.0031308f ? 12.92f * c : 1.055f * std::pow(c, 1.0f / 2.4f) - 0.055f; }
+float srgb1(float c) { return c < 0.0031308f ? 12.92f * c : 1.055f * pow_(c, 1.0f / 2.4f) - 0.055f; }
 
 float hable_op(float x) {
     const float A = 0.15f, B = 0.50f, C = 0.10f, D = 0.20f, E = 0.02f, F = 0.30f;
@@ -578,8 +586,8 @@ float uchimura1(float x, const float* u) {
     const float w0 = 1.0f - t * t * (3.0f - 2.0f * t);
     const float w2 = x < m + l0 ? 0.0f : 1.0f;                       // step(m + l0, x)
     const float w1 = 1.0f - w0 - w2;
-    const float T = m * std::pow(x / m, c) + b;
-    const float S = P - (P - S1) * std::exp(CP * (x - S0));
+    const float T = m * pow_(x / m, c) + b;
+    const float S = P - (P - S1) * exp_(CP * (x - S0));
     const float L = m + a * (x - m);
     return T * w0 + L * w1 + S * w2;
 }
@@ -595,8 +603,8 @@ extern "C" void orc_tonemap(const float* color, uint32_t n, uint32_t mode, const
     const float* amd = params + 8;
     // amd.comp ColToneB / ColToneC
     const float hdr = amd[0], contrast = amd[1], shoulder = amd[2], mid_in = amd[3], mid_out = amd[4];
-    const float pa = std::pow(mid_in, contrast), hs = std::pow(hdr, contrast * shoulder);
-    const float ms = std::pow(mid_in, contrast * shoulder), hc = std::pow(hdr, contrast);
+    const float pa = pow_(mid_in, contrast), hs = pow_(hdr, contrast * shoulder);
+    const float ms = pow_(mid_in, contrast * shoulder), hc = pow_(hdr, contrast);
     const float bb = -((-pa + (mid_out * (hs * pa - hc * ms * mid_out)) / (hs * mid_out - ms * mid_out)) /
                        (ms * mid_out));
     const float cc = (hs * pa - hc * ms * mid_out) / (hs * mid_out - ms * mid_out);
@@ -621,14 +629,14 @@ extern "C" void orc_tonemap(const float* color, uint32_t n, uint32_t mode, const
             float peak = std::fmax(c[0], std::fmax(c[1], c[2]));
             peak = std::fmax(1e-6f, peak);
             float ratio[3] = {c[0] / peak, c[1] / peak, c[2] / peak};
-            const float z = std::pow(peak, contrast);
-            peak = z / (std::pow(z, shoulder) * bb + cc);
+            const float z = pow_(peak, contrast);
+            peak = z / (pow_(z, shoulder) * bb + cc);
             const float cross = contrast * 16.0f, e = contrast / cross;
-            const float mx = std::pow(peak, 4.0f);
+            const float mx = pow_(peak, 4.0f);
             for (int k = 0; k < 3; ++k) {
-                float q = std::pow(std::fabs(ratio[k]), e);
+                float q = pow_(std::fabs(ratio[k]), e);
                 q = q * (1.0f - mx) + 1.0f * mx;  // mix(ratio, white, pow(peak, crosstalk))
-                q = std::pow(std::fabs(q), cross);
+                q = pow_(std::fabs(q), cross);
                 c[k] = q * peak;
             }
         }
