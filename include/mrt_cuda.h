@@ -253,6 +253,11 @@ typedef struct mrt_tuning {
                                      Morton key); 0xFFFFFFFF = never.  A call
                                      with mrt_trace_params.sort_rays = 1 sorts
                                      every queue                             */
+    uint32_t tail_bounce;         /* 0: every bounce as separate wavefront
+                                     passes; b >= 1: the paths still alive
+                                     at bounce b finish in one persistent
+                                     launch (trace, shade, shadow ray and
+                                     the later bounces per lane; same image) */
 } mrt_tuning;
 int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning);
 int mrt_cuda_get_tuning(mrt_ctx* ctx, mrt_tuning* tuning);

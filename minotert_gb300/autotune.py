@@ -29,8 +29,11 @@ def candidates(max_blocks_per_sm: int, sort: bool = False):
     blocks = sorted({b for b in (1, 2, 3, 4, 5, 6, 8) if b <= max_blocks_per_sm} | {max_blocks_per_sm})
     sort_thr = [SORT_NEVER, 1 << 18, 1 << 14] if sort else [SORT_NEVER]
     # dynamic_fetch bit 0: extension rays, bit 1: shadow rays
-    for b, dyn, prim, thr in itertools.product(blocks, (1, 3, 0, 2), (0, 1), sort_thr):
-        yield {"trace_blocks_per_sm": b, "dynamic_fetch": dyn, "primary_persistent": prim, "sort_min_rays": thr}
+    # tail_bounce: 0 = wavefront passes for every bounce, 3 = one persistent
+    # launch finishes the paths alive at bounce 3
+    for b, dyn, prim, thr, tail in itertools.product(blocks, (1, 3, 0, 2), (0, 1), sort_thr, (3, 0)):
+        yield {"trace_blocks_per_sm": b, "dynamic_fetch": dyn, "primary_persistent": prim, "sort_min_rays": thr,
+               "tail_bounce": tail}
 
 
 def time_frames(ctx: Context, run_frame, stream, frames: int, warmup: int) -> float:

@@ -288,7 +288,8 @@ int mrt_cuda_set_timing(mrt_ctx* ctx, int enable) {
 
 int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning) {
     if (!ctx || !tuning) return fail(ctx, MRT_EINVAL, "set_tuning: null argument");
-    if (tuning->trace_blocks_per_sm > 64 || tuning->dynamic_fetch > 3 || tuning->primary_persistent > 1)
+    if (tuning->trace_blocks_per_sm > 64 || tuning->dynamic_fetch > 3 || tuning->primary_persistent > 1 ||
+        tuning->tail_bounce > MRT_MAX_BOUNCES)
         return fail(ctx, MRT_EINVAL, "set_tuning: value out of range");
     ctx->tuning = *tuning;
     return MRT_OK;
@@ -662,10 +663,19 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
     for (uint32_t smp = 0; smp < tp.samples; ++smp) {
         MRT_CK(cudaMemsetAsync(wb.counters, 0, kCntSlots * sizeof(uint32_t), s));
         MRT_LAUNCH(3, 0, launch_shade_primary(scene->dev, fp, *gbuffer, tp, bn, wb, smp, ctx->d_status, s));
+        // bounces from tail_bounce on go through one persistent launch (not
+        // while counting nodes: the counting kernels are the wavefront's)
+        const uint32_t tail = ctx->counters ? 0u : ctx->tuning.tail_bounce;
+        bool tail_done = false;
         for (uint32_t b = 1; b <= tp.max_bounces; ++b) {
             if (nee)
                 MRT_LAUNCH(2, int(b - 1), launch_trace_shadow(scene->dev, wb, tp, b - 1, tblocks, ctx->d_status,
                                                               ctx->counters, dyn_sh, s));
+            if (tail != 0u && b >= tail) {
+                MRT_LAUNCH(1, int(b), launch_tail(scene->dev, tp, bn, wb, W, b, tblocks, ctx->d_status, s));
+                tail_done = true;
+                break;
+            }
             if (params->sort_rays || ctx->tuning.sort_min_rays != kSortNever) {
                 MRT_LAUNCH(4, int(b), launch_sort_ext(scene->dev, wb, b,
                                                       params->sort_rays ? 0u : ctx->tuning.sort_min_rays, s));
@@ -674,7 +684,7 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
             MRT_LAUNCH(1, int(b), launch_trace_ext(scene->dev, wb, b, tblocks, ctx->d_status, ctx->counters, dyn, s));
             MRT_LAUNCH(3, int(b), launch_shade(scene->dev, tp, bn, wb, W, b, ctx->d_status, s));
         }
-        if (nee)
+        if (nee && !tail_done)
             MRT_LAUNCH(2, int(tp.max_bounces), launch_trace_shadow(scene->dev, wb, tp, tp.max_bounces, tblocks,
                                                                    ctx->d_status, ctx->counters, dyn_sh, s));
         MRT_LAUNCH(3, 0, launch_tally(wb, s));

@@ -568,6 +568,64 @@ k_trace_shadow(DevScene sc, WaveBuffers wb, TraceParams tp, uint32_t vertex, uin
     }
 }
 
+// The path tail: one persistent launch finishes every path of the
+// extension queue of bounce `first` — closest hit, shading, shadow ray and
+// the following bounces — instead of 3 launches per remaining bounce whose
+// small queues leave the GPU waiting on its longest ray each time.  Each
+// warp takes 32 paths, each lane runs its path to the end.  A pixel's
+// radiance receives the same additions in the same order as in the wavefront
+// passes (escape, then shadow, vertex by vertex) and the RNG state advances
+// identically, so the image is bit-identical; the ray counters of the
+// bounces and vertices it covers are incremented as the wavefront's queues
+// would have been, so ray statistics are unchanged.  Up to 128 registers (4
+// resident blocks per SM): the tail is latency bound, and the traversal and
+// shading code together spill at 64.
+__global__ void __launch_bounds__(kTraceBlock, 4)
+k_tail(DevScene sc, TraceParams tp, BlueNoise bn, WaveBuffers wb, uint32_t width, uint32_t first, uint32_t* status) {
+    __shared__ uint2 stk[kStackDepth * kTraceBlock];
+    const uint32_t n = wb.counters[kCntExt + first];
+    const PathRay* q = ext_queue(wb, first);
+    uint32_t* fetch = wb.counters + kCntFetchExt + first;
+    uint2* my = stk + threadIdx.x;
+    const f3 sun{tp.sun[0], tp.sun[1], tp.sun[2]};
+    uint32_t st = 0u, cn = 0u, ct = 0u;
+    bool exhausted = false;
+    while (true) {
+        const uint32_t idx = warp_refill(fetch, n, true, exhausted);
+        if (!__any_sync(0xFFFFFFFFu, idx != kMiss)) break;
+        if (idx == kMiss) continue;
+        const PathRay pr = q[idx];
+        const uint32_t pix = __float_as_uint(pr.o_pix.w);
+        f3 o{pr.o_pix.x, pr.o_pix.y, pr.o_pix.z}, d{pr.d.x, pr.d.y, pr.d.z}, beta{pr.beta.x, pr.beta.y, pr.beta.z};
+        for (uint32_t b = first;; ++b) {
+            uint32_t prim;
+            float t;
+            trace_bvh8<false, false, kStackDepth>(sc, o, d, 0.0f, INFINITY, prim, t, my, kTraceBlock, st, cn, ct);
+            if (prim == kMiss) {
+                add_L(wb.L, pix, mul_rn(beta, escape_radiance(tp, d)));
+                break;
+            }
+            uint32_t rng = wb.rng[pix];
+            const VertexOut vo = shade_vertex(sc, tp, bn, width, b, pix, ray_at(o, d, t), d, prim, beta, rng, status);
+            wb.rng[pix] = rng;
+            if (vo.shadow) {
+                atomicAdd(wb.counters + kCntShadow + b, 1u);
+                uint32_t sp;
+                float stt;
+                trace_bvh8<true, false, kStackDepth>(sc, f3{vo.sr.o_pix.x, vo.sr.o_pix.y, vo.sr.o_pix.z}, sun, 0.0f,
+                                                     INFINITY, sp, stt, my, kTraceBlock, st, cn, ct);
+                if (sp == kMiss) add_L(wb.L, pix, f3{vo.sr.contrib.x, vo.sr.contrib.y, vo.sr.contrib.z});
+            }
+            if (!vo.ext) break;
+            atomicAdd(wb.counters + kCntExt + b + 1u, 1u);
+            o = f3{vo.pr.o_pix.x, vo.pr.o_pix.y, vo.pr.o_pix.z};
+            d = f3{vo.pr.d.x, vo.pr.d.y, vo.pr.d.z};
+            beta = f3{vo.pr.beta.x, vo.pr.beta.y, vo.pr.beta.z};
+        }
+    }
+    if (st) atomicOr(status, st);
+}
+
 __global__ void k_tally(WaveBuffers wb) {
     const uint32_t j = threadIdx.x;
     if (j < kCntFetchExt) atomicAdd(wb.totals + j, (unsigned long long)wb.counters[j]);
@@ -704,6 +762,12 @@ cudaError_t launch_trace_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t
         if (dyn) k_trace_ext<false, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
         else k_trace_ext<false, false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tail(const DevScene& sc, const TraceParams& tp, BlueNoise bn, const WaveBuffers& wb,
+                        uint32_t width, uint32_t first, int blocks, uint32_t* status, cudaStream_t s) {
+    k_tail<<<blocks, kTraceBlock, 0, s>>>(sc, tp, bn, wb, width, first, status);
     return cudaGetLastError();
 }
 
