@@ -248,34 +248,31 @@ def run_mine(args, world, rank, local, dist):
     def bytes_per_ray(nn, nt):  # algorithmic bytes per ray: ray + hit + nodes + triangles
         return 32 + 16 + 128 * nn + 48 * nt
 
-    kernels = {
-        "extend": (st.ms_extend, ext_rays and sum(ext) * bytes_per_ray(n_node_ext, n_tri_ext)),
-        "primary": (st.ms_primary, prim * bytes_per_ray(n_node_prim, n_tri_prim)),
-        "shadow": (st.ms_shadow, int(st.shadow_rays) * bytes_per_ray(n_node_sh, n_tri_sh)),
-        "shade": (st.ms_shade, None),
-    }
-    dom = max(kernels, key=lambda k: kernels[k][0])
+    # roofline of the dominant launch: the bounce-1 extension kernel
+    # (k_trace_ext, one launch per frame, the largest in the launch list),
+    # bytes from its own node/triangle counts, time from its CUDA events
     peaks = _peaks()
-    dk_ms, dk_bytes = kernels["extend"] if kernels[dom][1] is None else kernels[dom]
-    dname = "extend" if kernels[dom][1] is None else dom
-    achieved = dk_bytes / (dk_ms / 1e3) / 1e9 if dk_ms > 0 else 0.0
-    launches_per_frame = {"extend": s.bounces, "primary": 1, "shadow": s.bounces + 1}[dname]
+    b1_rays = ext[0] / args.steps
+    b1_ms = st.ms_extend_b[0] / args.steps
+    n_node_b1 = int(cs.nodes_extension[0]) / max(int(cs.extension_rays[0]), 1)
+    n_tri_b1 = int(cs.tris_extension[0]) / max(int(cs.extension_rays[0]), 1)
+    dk_bytes = b1_rays * bytes_per_ray(n_node_b1, n_tri_b1)
+    achieved = dk_bytes / (b1_ms / 1e3) / 1e9 if b1_ms > 0 else 0.0
     traffic = None
     tfile = ROOT / "profiles" / "traffic.json"
     if tfile.exists():
-        tj = json.loads(tfile.read_text()).get(wl.name, {}).get(dname)
+        tj = json.loads(tfile.read_text()).get(wl.name, {}).get("extend")
         if tj:
-            traffic = tj["bytes_per_ray"] * (dk_bytes / bytes_per_ray(
-                *{"extend": (n_node_ext, n_tri_ext), "primary": (n_node_prim, n_tri_prim),
-                  "shadow": (n_node_sh, n_tri_sh)}[dname])) / (args.steps * launches_per_frame)
-    roofline = {"bound": "hbm", "kernel": f"k_trace_{'ext' if dname == 'extend' else dname}",
+            traffic = tj["bytes_per_ray"] * b1_rays
+    roofline = {"bound": "hbm", "kernel": "k_trace_ext (bounce 1)",
                 "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
-                "traffic": traffic, "bytes_per_ray": bytes_per_ray(
-                    *{"extend": (n_node_ext, n_tri_ext), "primary": (n_node_prim, n_tri_prim),
-                      "shadow": (n_node_sh, n_tri_sh)}[dname]),
-                "nodes_per_ray": {"primary": n_node_prim, "extension": n_node_ext, "shadow": n_node_sh},
-                "tris_per_ray": {"primary": n_tri_prim, "extension": n_tri_ext, "shadow": n_tri_sh},
+                "traffic": traffic, "bytes_per_ray": bytes_per_ray(n_node_b1, n_tri_b1),
+                "rays_per_launch": b1_rays, "ms_per_launch": b1_ms,
+                "nodes_per_ray": {"primary": n_node_prim, "extension": n_node_ext, "extension_b1": n_node_b1,
+                                  "shadow": n_node_sh},
+                "tris_per_ray": {"primary": n_tri_prim, "extension": n_tri_ext, "extension_b1": n_tri_b1,
+                                 "shadow": n_tri_sh},
                 "note": "bytes/ray = 32 + 16 + 128 N_node + 48 N_tri with N from the counting kernels "
                         "(equal to the oracle's counts); the scene (69 MB) is L2-resident, so a fraction "
                         "above 1 of the HBM copy peak means the traversal runs out of L2"}
@@ -292,6 +289,10 @@ def run_mine(args, world, rank, local, dist):
                            "shadow": st.shadow_rays / args.steps},
         "ms_per_frame": {"primary": st.ms_primary / args.steps, "extend": st.ms_extend / args.steps,
                          "shadow": st.ms_shadow / args.steps, "shade": st.ms_shade / args.steps},
+        "note": "tail_bounce %d: the paths alive at that bounce finish in one persistent launch (k_tail), "
+                "timed as extension of that bounce; its shading and shadow rays are inside that time, so "
+                "shadow_mrays_s divides all shadow rays by the wavefront shadow launches' time only"
+                % int(ctx.tuning().tail_bounce),
     }
 
     # end to end through the C ABI with host buffers
