@@ -182,12 +182,14 @@ MRT_DEV bool next_node(const DevScene& sc, Trav& s, uint2* stk, uint32_t stride,
     return true;
 }
 
-// Box tests of the 8 children of one node: the hit interior children become
-// the ray's current group (s.g_*); the triangles of the hit leaves are
-// returned as a bit mask relative to tri_base.
-MRT_DEV uint32_t visit_node(const DevScene& sc, Trav& s, uint32_t node, uint32_t& tri_base) {
-    const RayPre& r = s.r;
-    const float tmin = s.tmin, tbest = s.tbest;
+// Box tests of the 8 children of one node against ray r with [tmin, tbest]:
+// the hit interior children as bit keys (slot ^ oct, so that the lowest key
+// is the nearest child for rays in octant oct), the triangles of the hit
+// leaves as a bit mask relative to tri_base; child_base and imask describe
+// the node's interior children.
+MRT_DEV void node_test(const DevScene& sc, const RayPre& r, float tmin, float tbest, uint32_t oct, uint32_t node,
+                       uint32_t& int_keys, uint32_t& tri_mask, uint32_t& child_base, uint32_t& tri_base,
+                       uint32_t& imask_out) {
     const bool negx = r.ix < 0.0f, negy = r.iy < 0.0f, negz = r.iz < 0.0f;
 
     const uint4* np = sc.nodes + size_t(node) * 8u;
@@ -210,7 +212,8 @@ MRT_DEV uint32_t visit_node(const DevScene& sc, Trav& s, uint32_t node, uint32_t
     const uint32_t nz0 = negz ? L4.z : L3.x, nz1 = negz ? L4.w : L3.y;
     const uint32_t fz0 = negz ? L3.x : L4.z, fz1 = negz ? L3.y : L4.w;
 
-    uint32_t int_keys = 0u, tri_mask = 0u;
+    int_keys = 0u;
+    tri_mask = 0u;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         const uint32_t k = uint32_t(i & 3);
@@ -224,14 +227,24 @@ MRT_DEV uint32_t visit_node(const DevScene& sc, Trav& s, uint32_t node, uint32_t
         const float tf = min3f(tfx, tfy, fminf(tfz, tbest));
         if (tn <= __fmul_rn(tf, kRobustScale)) {
             const uint32_t meta = ((i < 4 ? L1.z : L1.w) >> (8 * k)) & 0xFFu;
-            if ((imask >> i) & 1u) int_keys |= 1u << (uint32_t(i) ^ r.oct);
+            if ((imask >> i) & 1u) int_keys |= 1u << (uint32_t(i) ^ oct);
             else tri_mask |= (meta >> 5) << (meta & 31u);
         }
     }
-    s.g_base = L1.x;
+    child_base = L1.x;
+    tri_base = L1.y;
+    imask_out = imask;
+}
+
+// Box tests of the 8 children of one node: the hit interior children become
+// the ray's current group (s.g_*); the triangles of the hit leaves are
+// returned as a bit mask relative to tri_base.
+MRT_DEV uint32_t visit_node(const DevScene& sc, Trav& s, uint32_t node, uint32_t& tri_base) {
+    uint32_t int_keys, tri_mask, child_base, imask;
+    node_test(sc, s.r, s.tmin, s.tbest, s.r.oct, node, int_keys, tri_mask, child_base, tri_base, imask);
+    s.g_base = child_base;
     s.g_hits = int_keys;
     s.g_imask = imask;
-    tri_base = L1.y;
     return tri_mask;
 }
 
