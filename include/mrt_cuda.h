@@ -55,6 +55,7 @@ enum {
 #define MRT_STATUS_BAD_TRI   0x08u /* triangle index out of range            */
 #define MRT_STATUS_QUEUE_OVF 0x10u /* a wavefront queue overflowed           */
 #define MRT_STATUS_BAD_SCENE 0x20u /* batched launch: scene index invalid    */
+#define MRT_STATUS_PIPE_TIMEOUT 0x40u /* a tensor-core pipeline wait ran out */
 
 /* ---- scene data formats ------------------------------------------------ */
 

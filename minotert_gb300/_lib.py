@@ -15,7 +15,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libmrt.so"
 
 MRT_OK, MRT_EINVAL, MRT_ECUDA, MRT_ENOMEM, MRT_ETIMEOUT, MRT_EDEVICE, MRT_ESTATE, MRT_ERANGE = 0, -1, -2, -3, -4, -5, -6, -7
 MRT_STATUS_ITER_CAP, MRT_STATUS_STACK_OVF, MRT_STATUS_BAD_NODE, MRT_STATUS_BAD_TRI = 1, 2, 4, 8
-MRT_STATUS_QUEUE_OVF, MRT_STATUS_BAD_SCENE = 0x10, 0x20
+MRT_STATUS_QUEUE_OVF, MRT_STATUS_BAD_SCENE, MRT_STATUS_PIPE_TIMEOUT = 0x10, 0x20, 0x40
 MRT_MISS = 0xFFFFFFFF
 MRT_RNG_REFERENCE, MRT_RNG_PER_PIXEL = 0, 1
 MRT_EST_ESCAPE, MRT_EST_NEE = 0, 1

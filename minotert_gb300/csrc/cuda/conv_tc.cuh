@@ -26,7 +26,7 @@ constexpr int kTcPix = 128;             // output pixels per row of a CTA (MMA M
 constexpr int kTcHalo = kTcPix + 2;     // input pixels per halo row
 constexpr int kTcPlane = kTcHalo * 16;  // bytes of one 8-channel halo plane
 __host__ __device__ constexpr int tc_abytes(int rows) { return (rows + 2) * 2 * kTcPlane; }
-constexpr uint32_t kTcSpin = 1u << 26;  // mbarrier wait cap (polls)
+constexpr uint32_t kTcSpin = 1u << 20;  // mbarrier wait cap (polls; a poll may suspend ~1 us)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
         if (j < nk) {
             if (k >= 1 && !tc_wait(smem_u32(mbar + (k - 1) % kStages), uint32_t((k - 1) / kStages) & 1u)) {
                 timed_out = true;
-                atomicOr(status, MRT_STATUS_ITER_CAP);
+                atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
             }
             timed_out = __syncthreads_or(timed_out) != 0;
             if (timed_out) break;
@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
     for (int c = issued - kStages < 0 ? 0 : issued - kStages; c < issued; ++c)
         if (!tc_wait(smem_u32(mbar + c % kStages), uint32_t(c / kStages) & 1u)) {
             timed_out = true;
-            atomicOr(status, MRT_STATUS_ITER_CAP);
+            atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
         }
     timed_out = __syncthreads_or(timed_out) != 0;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -244,6 +244,286 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(uint32_t(kCols))
                      : "memory");
+}
+
+// ---- TMA form, for layers whose inputs are not upsampled ------------------
+//
+// One thread streams the slices with the Tensor Memory Accelerator and issues
+// the MMAs.  Per slice: two tiled tensor loads of the halo (box 8 channels x
+// 130 pixels x (ROWS + 2) rows from the NHWC source; rows and pixels outside
+// the image read as zeros) and one bulk copy of the slice's weights from a
+// copy laid out as [slice][tap][half][cout][8] (k_tc_weights), all
+// completing on the stage's `full` mbarrier (expect_tx).  In shared memory
+// the two 8-channel halves of the halo are each ROWS + 2 consecutive planes,
+// each half starting on a 128-byte boundary (a tensor copy's shared-memory
+// destination must be 128-byte aligned), so the A operand's leading byte
+// offset (between K halves) is the padded half size.  Slices k+1 .. k+STAGES-1 are in flight while the MMAs of slice k
+// run; a stage is refilled once the MMAs of the slice before have retired
+// (its `empty` mbarrier, signalled by tcgen05.commit).  Every wait is
+// bounded; on a timeout the thread sets the status bit, waits (bounded) for
+// the copies and MMAs it issued and skips the epilogue.
+template <int ROWS>
+__host__ __device__ constexpr uint32_t tma_half_bytes() { return (uint32_t((ROWS + 2) * kTcPlane) + 127u) & ~127u; }
+template <int ROWS>
+__host__ __device__ constexpr uint32_t tma_halo_bytes() { return 2u * tma_half_bytes<ROWS>(); }
+template <int COUT, int ROWS>
+__host__ __device__ constexpr uint32_t tma_stage_bytes() {
+    return (tma_halo_bytes<ROWS>() + uint32_t(9 * 2 * COUT * 16) + 127u) & ~127u;
+}
+
+__device__ __forceinline__ void tma_load_halo(uint32_t dst, const CUtensorMap* map, int c, int x, int y, int n,
+                                              uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c), "r"(x), "r"(y), "r"(n), "r"(mbar)
+        : "memory");
+}
+
+template <int COUT, int ROWS, int STAGES>
+__global__ void __launch_bounds__(128) k_conv_tma(ConvArgs a, const __grid_constant__ CUtensorMap map_a,
+                                                  const __grid_constant__ CUtensorMap map_b, const bf16* wt,
+                                                  uint32_t* status) {
+    constexpr int kAcc = ROWS * COUT;
+    constexpr int kCols = kAcc < 32 ? 32 : kAcc;
+    static_assert(kCols <= 512 && (kCols & (kCols - 1)) == 0, "tensor memory columns");
+    constexpr uint32_t kHalo = tma_halo_bytes<ROWS>(), kHalf = tma_half_bytes<ROWS>();
+    static_assert(kHalf % 128u == 0u && kHalo % 128u == 0u, "tensor copy destinations are 128-byte aligned");
+    // bytes the two halo boxes deliver (the halves' padding is not written)
+    constexpr uint32_t kHaloTx = 2u * uint32_t((ROWS + 2) * kTcPlane);
+    constexpr uint32_t kWBytes = uint32_t(9 * 2 * COUT * 16);
+    constexpr uint32_t kStage = tma_stage_bytes<COUT, ROWS>();
+    extern __shared__ __align__(128) unsigned char tsm[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(tsm + STAGES * kStage);
+    uint64_t* empty = full + STAGES;
+    uint32_t* slot = reinterpret_cast<uint32_t*>(empty + STAGES);
+    uint32_t* ok_flag = slot + 1;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tiles_x = (a.w_ + kTcPix - 1) / kTcPix, rows_per_img = (a.h + ROWS - 1) / ROWS;
+    const int tx = blockIdx.x % tiles_x, rb = blockIdx.x / tiles_x;
+    const int y0 = (rb % rows_per_img) * ROWS, n = rb / rows_per_img;
+    const int x0 = tx * kTcPix;
+    const int cin = a.ca + a.cb, nk = cin / 16;
+    const uint32_t smem0 = smem_u32(tsm);
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                     "r"(uint32_t(kCols))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(full + s)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(empty + s)) : "memory");
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = *slot;
+
+    if (tid == 0) {
+        // after a timeout anywhere in this launch (or an earlier one) the
+        // remaining CTAs skip their work, so a stuck pipeline costs one wave
+        const bool skip = (*reinterpret_cast<volatile uint32_t*>(status) & MRT_STATUS_PIPE_TIMEOUT) != 0u;
+        auto load = [&](int j) -> bool {  // slice j into stage j % STAGES
+            const uint32_t st = smem0 + uint32_t(j % STAGES) * kStage, mb = smem_u32(full + j % STAGES);
+            const int c = 16 * j;
+            const CUtensorMap* map = c < a.ca ? &map_a : &map_b;
+            const int cc = c < a.ca ? c : c - a.ca;
+            // the copies' alignment rules, checked before anything is issued
+            if ((st & 127u) != 0u || (cc & 7) != 0) return false;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(kHaloTx + kWBytes)
+                         : "memory");
+            tma_load_halo(st, map, cc, x0 - 1, y0 - 1, n, mb);
+            tma_load_halo(st + kHalf, map, cc + 8, x0 - 1, y0 - 1, n, mb);
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                             st + kHalo),
+                         "l"(wt + size_t(j) * (kWBytes / 2)), "r"(kWBytes), "r"(mb)
+                         : "memory");
+            return true;
+        };
+        constexpr uint32_t idesc = tc_idesc(kTcPix, COUT);
+        bool ok = !skip;
+        int loaded = 0, issued = 0;
+        for (; ok && loaded < STAGES && loaded < nk; ++loaded) ok = load(loaded);
+        if (!ok && !skip) --loaded;  // the refused load was not issued
+        for (int k = 0; ok && k < nk; ++k) {
+            const int s = k % STAGES;
+            if (!tc_wait(smem_u32(full + s), uint32_t(k / STAGES) & 1u)) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t abase = smem0 + uint32_t(s) * kStage, bbase = abase + kHalo;
+#pragma unroll
+            for (int r = 0; r < ROWS; ++r)
+#pragma unroll
+                for (int t = 0; t < 9; ++t) {
+                    const int ky = t / 3, kx = t % 3;
+                    const uint64_t ad = tc_sdesc(abase + (r + ky) * kTcPlane + kx * 16, kHalf, 128);
+                    const uint64_t bd = tc_sdesc(bbase + (t * 2) * COUT * 16, COUT * 16, 128);
+                    const uint32_t acc = (k > 0 || t > 0) ? 1u : 0u;
+                    asm volatile(
+                        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr + uint32_t(r * COUT)),
+                        "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                        : "memory");
+                }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_u32(empty + s))
+                         : "memory");
+            issued = k + 1;
+            // refill the stage of slice k - 1 once its MMAs have retired
+            if (k >= 1 && loaded < nk) {
+                if (!tc_wait(smem_u32(empty + (k - 1) % STAGES), uint32_t((k - 1) / STAGES) & 1u) ||
+                    !load(loaded)) {
+                    ok = false;
+                    break;
+                }
+                ++loaded;
+            }
+        }
+        // drain what was issued: the last commit covers every MMA; loads
+        // not consumed by an MMA are waited for on their full barriers
+        if (issued > 0 && !tc_wait(smem_u32(empty + (issued - 1) % STAGES), uint32_t((issued - 1) / STAGES) & 1u))
+            ok = false;
+        for (int j = issued; j < loaded; ++j)
+            if (!tc_wait(smem_u32(full + j % STAGES), uint32_t(j / STAGES) & 1u)) ok = false;
+        if (!ok || issued < nk) {
+            atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
+            *ok_flag = 0u;
+        } else {
+            *ok_flag = 1u;
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (*ok_flag) {
+        const int m = 32 * warp + lane, x = x0 + m;
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+            const int y = y0 + r;
+            bf16* dst = a.y + ((size_t(n) * a.h + y) * a.w_ + x) * COUT;
+#pragma unroll
+            for (int jj = 0; jj < COUT / 16; ++jj) {
+                uint32_t v[16];
+                const uint32_t ta = taddr + (uint32_t(32 * warp) << 16) + uint32_t(r * COUT + 16 * jj);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                    "[%16];\n"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15])
+                    : "r"(ta));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (x < a.w_ && y < a.h) {
+                    uint32_t packed[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        float f0 = __uint_as_float(v[2 * q]) + a.bias[16 * jj + 2 * q];
+                        float f1 = __uint_as_float(v[2 * q + 1]) + a.bias[16 * jj + 2 * q + 1];
+                        if (a.relu) {
+                            f0 = fmaxf(f0, 0.0f);
+                            f1 = fmaxf(f1, 0.0f);
+                        }
+                        const __nv_bfloat162 hv = __floats2bfloat162_rn(f0, f1);
+                        packed[q] = *reinterpret_cast<const uint32_t*>(&hv);
+                    }
+                    uint4* o = reinterpret_cast<uint4*>(dst + 16 * jj);
+                    o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                    o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(uint32_t(kCols))
+                     : "memory");
+}
+
+// Weights of every layer re-laid out for the TMA form: per layer,
+// [slice of 16 input channels][tap][half][cout][8 channels].
+struct TcLayerTable {
+    int cin[16], cout[16];
+    size_t off[16];
+    int count;
+};
+__global__ void k_tc_weights(const bf16* w16, bf16* wt, TcLayerTable t) {
+    for (int l = 0; l < t.count; ++l) {
+        const int cin = t.cin[l], cout = t.cout[l];
+        const size_t total = size_t(9) * cin * cout;
+        for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+            const int e = int(i % 8);
+            size_t q = i / 8;
+            const int co = int(q % cout);
+            q /= cout;
+            const int hf = int(q % 2);
+            q /= 2;
+            const int tap = int(q % 9);
+            const int k = int(q / 9);
+            wt[t.off[l] + i] = w16[t.off[l] + (size_t(co) * 9 + tap) * cin + 16 * k + 8 * hf + e];
+        }
+    }
+}
+
+// Shapes of the TMA form per COUT, from a sweep on the 1080p denoiser (ms per
+// inference, upsampling layers on the cp.async kernel: cp.async everywhere
+// 1.607; TMA with 4 / 8 rows 1.369, 3 stages 1.640; 2 rows at COUT 128
+// 1.345): rows per CTA and two stages, two CTAs per SM.
+__host__ __device__ constexpr int tma_rows(int cout) { return cout >= 128 ? 2 : (cout >= 64 ? 4 : 8); }
+__host__ __device__ constexpr int tma_stages(int) { return 2; }
+
+// NHWC BF16 tensor map with the halo box of one 8-channel half
+inline bool tma_encode(CUtensorMap* map, const bf16* base, int c, int w, int h, int n, int rows) {
+    using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static EncodeFn fn = nullptr;
+    if (!fn) {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !f)
+            return false;
+        fn = reinterpret_cast<EncodeFn>(f);
+    }
+    const cuuint64_t dims[4] = {cuuint64_t(c), cuuint64_t(w), cuuint64_t(h), cuuint64_t(n)};
+    const cuuint64_t strides[3] = {cuuint64_t(c) * 2, cuuint64_t(c) * 2 * w, cuuint64_t(c) * 2 * w * h};
+    const cuuint32_t box[4] = {8u, cuuint32_t(kTcHalo), cuuint32_t(rows + 2), 1u};
+    const cuuint32_t estr[4] = {1u, 1u, 1u, 1u};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(base), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int COUT>
+cudaError_t launch_conv_tma(const ConvArgs& ca, const bf16* wt, uint32_t* status, cudaStream_t s) {
+    constexpr int kRows = tma_rows(COUT), kStages = tma_stages(COUT);
+    static bool configured = false;
+    const size_t smem = size_t(kStages) * tma_stage_bytes<COUT, kRows>() + 128;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_conv_tma<COUT, kRows, kStages>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    CUtensorMap ma, mb;
+    if (!tma_encode(&ma, ca.a, ca.ca, ca.w_, ca.h, ca.n, kRows)) return cudaErrorInvalidValue;
+    if (ca.cb > 0) {
+        if (!tma_encode(&mb, ca.b, ca.cb, ca.w_, ca.h, ca.n, kRows)) return cudaErrorInvalidValue;
+    } else {
+        mb = ma;
+    }
+    const int blocks = ((ca.w_ + kTcPix - 1) / kTcPix) * ((ca.h + kRows - 1) / kRows) * ca.n;
+    k_conv_tma<COUT, kRows, kStages><<<blocks, 128, smem, s>>>(ca, ma, mb, wt, status);
+    return cudaGetLastError();
 }
 
 template <int COUT>

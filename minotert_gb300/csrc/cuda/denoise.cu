@@ -25,6 +25,7 @@
 // gradients, reading the stored BF16 activations.
 #include "internal.hpp"
 
+#include <cuda.h>  // CUtensorMap (the encoder is fetched through the runtime)
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -361,6 +362,7 @@ struct mrt_denoiser {
     size_t n_w = 0, n_b = 0;
     float *w = nullptr, *wm = nullptr, *wv = nullptr, *wg = nullptr;  // weights + biases, FP32
     bf16* w16 = nullptr;
+    bf16* wtc = nullptr;          // w16 re-laid out per 16-channel slice for the TMA convolution
     // activation tensors (bf16) and their gradients (fp32), sized for n*h*w
     size_t cap_pix = 0, grad_pix = 0;
     bf16* act[kLayers] = {};
@@ -419,6 +421,15 @@ int ensure_acts(mrt_ctx* ctx, mrt_denoiser* d, size_t pix, bool grads) {
 cudaError_t conv(const mrt_denoiser* d, int l, const bf16* a, const bf16* b, int n, int h, int w, cudaStream_t s) {
     const ConvDesc& L = d->layers[l];
     ConvArgs ca{a, b, d->w16 + L.w_off, d->w + L.b_off, d->act[l], n, h, w, L.ca, L.cb, L.cout, L.ups, L.relu};
+    if (d->tcgen05 && !L.ups) {
+        const bf16* wt = d->wtc + L.w_off;
+        switch (L.cout) {
+        case 16: return launch_conv_tma<16>(ca, wt, d->status, s);
+        case 32: return launch_conv_tma<32>(ca, wt, d->status, s);
+        case 64: return launch_conv_tma<64>(ca, wt, d->status, s);
+        default: return launch_conv_tma<128>(ca, wt, d->status, s);
+        }
+    }
     if (d->tcgen05) {
         switch (L.cout) {
         case 16: return launch_conv_tc<16>(ca, d->status, s);
@@ -440,6 +451,16 @@ cudaError_t conv(const mrt_denoiser* d, int l, const bf16* a, const bf16* b, int
 // forward of the whole network over n images of h x w (h, w multiples of 4)
 cudaError_t forward(const mrt_denoiser* d, const bf16* in, int n, int h, int w, cudaStream_t s) {
     cudaError_t e;
+    if (d->tcgen05) {  // the TMA convolutions read the weights per slice
+        TcLayerTable t{};
+        t.count = kLayers;
+        for (int l = 0; l < kLayers; ++l) {
+            t.cin[l] = d->layers[l].ca + d->layers[l].cb;
+            t.cout[l] = d->layers[l].cout;
+            t.off[l] = d->layers[l].w_off;
+        }
+        k_tc_weights<<<304, 256, 0, s>>>(d->w16, d->wtc, t);
+    }
     if ((e = conv(d, 0, in, nullptr, n, h, w, s))) return e;
     if ((e = conv(d, 1, d->act[0], nullptr, n, h, w, s))) return e;
     k_pool<<<grid_for(size_t(n) * h * w * 4 / 4), 256, 0, s>>>(d->act[1], d->pool0, n, h, w, 32);
@@ -499,7 +520,8 @@ int mrt_cuda_denoiser_create(mrt_ctx* ctx, uint32_t seed, mrt_denoiser** out) {
     const size_t total = wo;
     bool ok = cudaMalloc(&d->w, total * 4) == cudaSuccess && cudaMalloc(&d->wm, total * 4) == cudaSuccess &&
               cudaMalloc(&d->wv, total * 4) == cudaSuccess && cudaMalloc(&d->wg, total * 4) == cudaSuccess &&
-              cudaMalloc(&d->w16, d->n_w * 2) == cudaSuccess && cudaMalloc(&d->loss, 4) == cudaSuccess &&
+              cudaMalloc(&d->w16, d->n_w * 2) == cudaSuccess && cudaMalloc(&d->wtc, d->n_w * 2) == cudaSuccess &&
+              cudaMalloc(&d->loss, 4) == cudaSuccess &&
               cudaMallocHost(&d->h_loss, 4) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
@@ -547,7 +569,8 @@ int mrt_cuda_denoiser_destroy(mrt_ctx* ctx, mrt_denoiser* d) {
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
     for (int l = 0; l < kLayers; ++l) { cudaFree(d->act[l]); cudaFree(d->grad[l]); }
-    void* ps[] = {d->w, d->wm, d->wv, d->wg, d->w16, d->pool0, d->pool1, d->gpool0, d->gpool1, d->gin, d->loss};
+    void* ps[] = {d->w, d->wm, d->wv, d->wg, d->w16, d->wtc, d->pool0, d->pool1, d->gpool0, d->gpool1, d->gin,
+                  d->loss};
     for (void* p : ps) cudaFree(p);
     if (d->h_loss) cudaFreeHost(d->h_loss);
     delete d;
