@@ -1,5 +1,9 @@
 // tcgen05 implicit-GEMM 3x3 convolution for the denoiser (included inside
-// denoise.cu's anonymous namespace, after ConvArgs).
+// denoise.cu's anonymous namespace, after ConvArgs), in two forms that share
+// the shared-memory operand layout, the MMAs and the epilogue: k_conv_tc
+// gathers the halo with per-thread cp.async (any source, including the
+// nearest-upsampled one), k_conv_tma with tensor copies (sources at the
+// output's resolution).
 //
 // One CTA (4 warps) computes ROWS output rows x 128 consecutive pixels x all
 // COUT channels as ROWS GEMMs on the 5th-generation tensor cores: M = 128
@@ -103,6 +107,50 @@ __device__ __forceinline__ void tc_load_slice(const ConvArgs& a, uint32_t As, ui
     }
 }
 
+// Epilogue shared by the convolution kernels: warp w reads TMEM lanes
+// 32w..32w+31 (pixels x0 + 32w ..), ROWS x COUT FP32 accumulators, adds the
+// bias, applies ReLU and stores BF16 with 16-byte stores.
+template <int COUT, int ROWS>
+__device__ __forceinline__ void tc_epilogue(const ConvArgs& a, uint32_t taddr, int n, int y0, int x0, int warp,
+                                            int lane) {
+    const int m = 32 * warp + lane, x = x0 + m;
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+        const int y = y0 + r;
+        bf16* dst = a.y + ((size_t(n) * a.h + y) * a.w_ + x) * COUT;
+#pragma unroll
+        for (int jj = 0; jj < COUT / 16; ++jj) {
+            uint32_t v[16];
+            const uint32_t ta = taddr + (uint32_t(32 * warp) << 16) + uint32_t(r * COUT + 16 * jj);
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];\n"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15])
+                : "r"(ta));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (x < a.w_ && y < a.h) {
+                uint32_t packed[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    float f0 = __uint_as_float(v[2 * q]) + a.bias[16 * jj + 2 * q];
+                    float f1 = __uint_as_float(v[2 * q + 1]) + a.bias[16 * jj + 2 * q + 1];
+                    if (a.relu) {
+                        f0 = fmaxf(f0, 0.0f);
+                        f1 = fmaxf(f1, 0.0f);
+                    }
+                    const __nv_bfloat162 hv = __floats2bfloat162_rn(f0, f1);
+                    packed[q] = *reinterpret_cast<const uint32_t*>(&hv);
+                }
+                uint4* o = reinterpret_cast<uint4*>(dst + 16 * jj);
+                o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+            }
+        }
+    }
+}
+
 template <int COUT, int ROWS, int STAGES>
 __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
     constexpr int kAcc = ROWS * COUT;
@@ -202,42 +250,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a, uint32_t* status) {
     timed_out = __syncthreads_or(timed_out) != 0;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (!timed_out) {
-        const int m = 32 * warp + lane, x = x0 + m;
-#pragma unroll
-        for (int r = 0; r < ROWS; ++r) {
-            const int y = y0 + r;
-            bf16* dst = a.y + ((size_t(n) * a.h + y) * a.w_ + x) * COUT;
-#pragma unroll
-            for (int jj = 0; jj < COUT / 16; ++jj) {
-                uint32_t v[16];
-                const uint32_t ta = taddr + (uint32_t(32 * warp) << 16) + uint32_t(r * COUT + 16 * jj);
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                    "[%16];\n"
-                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                      "=r"(v[15])
-                    : "r"(ta));
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (x < a.w_ && y < a.h) {
-                    uint32_t packed[8];
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) {
-                        float f0 = __uint_as_float(v[2 * q]) + a.bias[16 * jj + 2 * q];
-                        float f1 = __uint_as_float(v[2 * q + 1]) + a.bias[16 * jj + 2 * q + 1];
-                        if (a.relu) {
-                            f0 = fmaxf(f0, 0.0f);
-                            f1 = fmaxf(f1, 0.0f);
-                        }
-                        const __nv_bfloat162 hv = __floats2bfloat162_rn(f0, f1);
-                        packed[q] = *reinterpret_cast<const uint32_t*>(&hv);
-                    }
-                    uint4* o = reinterpret_cast<uint4*>(dst + 16 * jj);
-                    o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-                    o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
-                }
-            }
-        }
+        tc_epilogue<COUT, ROWS>(a, taddr, n, y0, x0, warp, lane);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -403,42 +416,7 @@ __global__ void __launch_bounds__(128) k_conv_tma(ConvArgs a, const __grid_const
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (*ok_flag) {
-        const int m = 32 * warp + lane, x = x0 + m;
-#pragma unroll
-        for (int r = 0; r < ROWS; ++r) {
-            const int y = y0 + r;
-            bf16* dst = a.y + ((size_t(n) * a.h + y) * a.w_ + x) * COUT;
-#pragma unroll
-            for (int jj = 0; jj < COUT / 16; ++jj) {
-                uint32_t v[16];
-                const uint32_t ta = taddr + (uint32_t(32 * warp) << 16) + uint32_t(r * COUT + 16 * jj);
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                    "[%16];\n"
-                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                      "=r"(v[15])
-                    : "r"(ta));
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (x < a.w_ && y < a.h) {
-                    uint32_t packed[8];
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) {
-                        float f0 = __uint_as_float(v[2 * q]) + a.bias[16 * jj + 2 * q];
-                        float f1 = __uint_as_float(v[2 * q + 1]) + a.bias[16 * jj + 2 * q + 1];
-                        if (a.relu) {
-                            f0 = fmaxf(f0, 0.0f);
-                            f1 = fmaxf(f1, 0.0f);
-                        }
-                        const __nv_bfloat162 hv = __floats2bfloat162_rn(f0, f1);
-                        packed[q] = *reinterpret_cast<const uint32_t*>(&hv);
-                    }
-                    uint4* o = reinterpret_cast<uint4*>(dst + 16 * jj);
-                    o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-                    o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
-                }
-            }
-        }
+        tc_epilogue<COUT, ROWS>(a, taddr, n, y0, x0, warp, lane);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
