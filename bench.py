@@ -692,6 +692,12 @@ def run_denoise_experiment(args, world, rank, local, dist):
     out = ctx.alloc(12 * W * H)
     curve_plain, curve_den = [], []
     cum_ms = 0.0
+    # one untimed pass of the denoising path first: kernel loading and the
+    # one-time launch configuration are not part of a frame's cost
+    gb = pt.primaryRays((W, H), cam, cam, stream)
+    den.features(ds, gb, col, diag, f_buf, stream)
+    den.infer(f_buf, 1, W, H, out, stream)
+    ctx.sync(stream)
     for f in range(64):
         a, b, c = ctx.event(), ctx.event(), ctx.event()
         ctx.record(a, stream)
