@@ -115,9 +115,10 @@ def _peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def _workload():
+def _workload(name="icospheres_1080p"):
     from minotert_gb300 import scene, workloads
-    wl = workloads.icospheres_1080p()
+    wl = {"icospheres_1080p": workloads.icospheres_1080p,
+          "heightfield_boxes_256": workloads.heightfield_boxes_256}[name]()
     t0 = time.perf_counter()
     mesh = wl.mesh()
     t1 = time.perf_counter()
@@ -129,7 +130,8 @@ def _config(wl, mesh, bvh, extra=None):
     c = {"workload": wl.name, "triangles": mesh.tri_count, "bvh8_nodes": int(len(bvh.nodes)),
          "width": wl.width, "height": wl.height, "spp": wl.settings.samples, "bounces": wl.settings.bounces,
          "rr_after_bounce": wl.settings.rr_start, "light": "directional (shadow ray per vertex) + constant sky",
-         "l2": "256 MiB memset between timed steps (scene 69 MB < L2 129 MB)", "parallelism": "replicas"}
+         "l2": "256 MiB memset between timed steps (scene %.0f MB < L2 129 MB)"
+               % ((bvh.nodes.nbytes + bvh.tris.nbytes + mesh.mats.nbytes) / 1e6), "parallelism": "replicas"}
     if extra:
         c.update(extra)
     return c
@@ -179,7 +181,7 @@ def run_mine(args, world, rank, local, dist):
     from minotert_gb300.pathtracer import Pathtracer, TraceSettings, camera_consts
     import ctypes as C
 
-    wl, mesh, bvh, build_info = _workload()
+    wl, mesh, bvh, build_info = _workload(args.workload)
     bn = scene.blue_noise(1, 64)
     ctx = Context(local)
     ds = scene.DeviceScene.triangles(ctx, mesh, bvh)
@@ -752,14 +754,17 @@ def run_denoise_experiment(args, world, rank, local, dist):
 
 
 def run_reference(args, world, rank, local, dist):
-    """The reference path on the host cores: MinoteRT's own implementation
-    is Vulkan + MSVC only and cannot run here, so its CPU restatement (the
-    oracle) runs the same frame, a bounded band of rows per step."""
+    """The reference path on the host cores.  MinoteRT's own implementation
+    dispatches Vulkan compute shaders (no graphics stack here) and has no
+    triangle or BVH path, so its CPU restatement (the oracle, pinned to the
+    reference's shaders compiled for the host) runs the same frame, a
+    bounded band of rows per step."""
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
         return
-    wl, mesh, bvh, build_info = _workload()
+    wl, mesh, bvh, build_info = _workload(args.workload if args.workload == "heightfield_boxes_256"
+                                          else "icospheres_1080p")
     from minotert_gb300 import scene
     bn = scene.blue_noise(1, 64)
     per_step = max(1.0, min(6.0, 150.0 / max(1, args.steps + args.warmup)))
@@ -931,8 +936,8 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["icospheres_1080p", "batched64", "radiance_cache", "denoiser",
-                                           "network_kernels", "post_kernels"],
+    ap.add_argument("--workload", choices=["icospheres_1080p", "heightfield_boxes_256", "batched64",
+                                           "radiance_cache", "denoiser", "network_kernels", "post_kernels"],
                     default="icospheres_1080p")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
