@@ -259,6 +259,10 @@ typedef struct mrt_tuning {
                                      at bounce b finish in one persistent
                                      launch (trace, shade, shadow ray and
                                      the later bounces per lane; same image) */
+    uint32_t stack_depth;         /* traversal stack entries of the batched
+                                     kernels (mrt_cuda_batch_*): 16, 24 or
+                                     32; 0 = 24.  Must cover the batch's
+                                     deepest BVH (depth - 1 entries)         */
 } mrt_tuning;
 int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning);
 int mrt_cuda_get_tuning(mrt_ctx* ctx, mrt_tuning* tuning);

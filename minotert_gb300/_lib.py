@@ -70,7 +70,8 @@ class FrameStats(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("trace_blocks_per_sm", C.c_uint32), ("dynamic_fetch", C.c_uint32),
-                ("primary_persistent", C.c_uint32), ("sort_min_rays", C.c_uint32), ("tail_bounce", C.c_uint32)]
+                ("primary_persistent", C.c_uint32), ("sort_min_rays", C.c_uint32), ("tail_bounce", C.c_uint32),
+                ("stack_depth", C.c_uint32)]
 
 
 class CacheConfig(C.Structure):

@@ -17,7 +17,7 @@ import json
 import statistics
 from pathlib import Path
 
-from ._lib import Context
+from ._lib import Context, MrtError
 
 DEFAULT_CACHE = Path(__file__).resolve().parent / "_build" / "autotune.json"
 
@@ -69,13 +69,18 @@ def autotune(ctx: Context, run_frame, stream=None, key: str = "default", frames:
     max_b = max(1, int(info.trace_blocks_per_sm_max))
     results = []
     for cand in (space or candidates(max_b, sort)):
-        ctx.set_tuning(**cand)
-        ms = time_frames(ctx, run_frame, stream, frames, warmup)
+        try:
+            ctx.set_tuning(**cand)
+            ms = time_frames(ctx, run_frame, stream, frames, warmup)
+        except MrtError as e:  # a schedule this workload cannot run (e.g. a stack below its BVH depth)
+            results.append({"tuning": cand, "ms": None, "refused": str(e)})
+            continue
         results.append({"tuning": cand, "ms": ms})
-    best = min(results, key=lambda r: r["ms"])
+    best = min((r for r in results if r["ms"] is not None), key=lambda r: r["ms"])
     ctx.set_tuning(**best["tuning"])
     out = {"tuning": best["tuning"], "ms": best["ms"], "results": results,
-           "default_ms": next((r["ms"] for r in results if r["tuning"] == _as_dict(saved)), None)}
+           "default_ms": next((r["ms"] for r in results
+                               if all(_as_dict(saved).get(k) == v for k, v in r["tuning"].items())), None)}
     if cache is not None:
         cache.parent.mkdir(parents=True, exist_ok=True)
         db[full_key] = out

@@ -151,6 +151,17 @@ int trace_blocks(mrt_ctx* ctx) {
     return per_sm * ctx->sm_count;
 }
 
+
+int check_gbuffer(mrt_ctx* ctx, const mrt_gbuffer* g) {
+    if (!g || !g->visibility) return fail(ctx, MRT_EINVAL, "gbuffer.visibility is NULL");
+    if (g->width == 0 || g->height == 0) return fail(ctx, MRT_EINVAL, "gbuffer has zero size");
+    if (uint64_t(g->width) * g->height > (1ull << 28)) return fail(ctx, MRT_ERANGE, "gbuffer larger than 2^28 pixels");
+    return MRT_OK;
+}
+
+} // namespace
+
+namespace mrt {
 // Depth of a BVH8 along in-range child links, each node counted once (a
 // corrupt blob with cycles still terminates; traversal bounds-checks the
 // rest at run time).  The traversal stack holds at most depth - 1 entries.
@@ -177,16 +188,6 @@ uint32_t bvh8_depth(const mrt_bvh8_node* nodes, uint32_t n) {
     return depth;
 }
 
-int check_gbuffer(mrt_ctx* ctx, const mrt_gbuffer* g) {
-    if (!g || !g->visibility) return fail(ctx, MRT_EINVAL, "gbuffer.visibility is NULL");
-    if (g->width == 0 || g->height == 0) return fail(ctx, MRT_EINVAL, "gbuffer has zero size");
-    if (uint64_t(g->width) * g->height > (1ull << 28)) return fail(ctx, MRT_ERANGE, "gbuffer larger than 2^28 pixels");
-    return MRT_OK;
-}
-
-} // namespace
-
-namespace mrt {
 // learned radiance cache (nrc.cu)
 cudaError_t cache_infer(const mrt_cache* c, const float* q, uint32_t n, const uint32_t* n_dev, float* out,
                         cudaStream_t s);
@@ -289,7 +290,9 @@ int mrt_cuda_set_timing(mrt_ctx* ctx, int enable) {
 int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning) {
     if (!ctx || !tuning) return fail(ctx, MRT_EINVAL, "set_tuning: null argument");
     if (tuning->trace_blocks_per_sm > 64 || tuning->dynamic_fetch > 3 || tuning->primary_persistent > 1 ||
-        tuning->tail_bounce > MRT_MAX_BOUNCES)
+        tuning->tail_bounce > MRT_MAX_BOUNCES ||
+        (tuning->stack_depth != 0u && tuning->stack_depth != 16u && tuning->stack_depth != 24u &&
+         tuning->stack_depth != 32u))
         return fail(ctx, MRT_EINVAL, "set_tuning: value out of range");
     ctx->tuning = *tuning;
     return MRT_OK;

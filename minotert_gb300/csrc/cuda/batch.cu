@@ -23,9 +23,19 @@ TraceParams make_trace_params(const mrt_trace_params* p);
 using namespace mrt;
 
 constexpr uint32_t kMaxBatchScenes = 4096;
+constexpr int kMaxBatchStack = 32;  // stack entries of the deepest kernel variant
+
+// Stack entries the batched traversal uses: mrt_tuning.stack_depth (16, 24
+// or 32; 0 = the default 24).  Returns 0 when it is below what the batch's
+// deepest BVH needs (depth - 1 entries).
+int batch_stack(const mrt_ctx* ctx, uint32_t max_depth) {
+    const int want = ctx->tuning.stack_depth ? int(ctx->tuning.stack_depth) : kStackDepth;
+    return uint32_t(want) + 1u >= max_depth ? want : 0;
+}
 
 struct mrt_batch {
     uint32_t scenes = 0;
+    uint32_t max_depth = 0;          // deepest scene BVH (levels)
     DevScene dev{};
     void* d_nodes = nullptr;
     void* d_tris = nullptr;
@@ -49,6 +59,7 @@ struct mrt_batch {
     const void* g_rays = nullptr;
     float* g_radiance = nullptr;
     uint32_t g_n = 0, g_bounces = 0, g_blocks = 0, g_dyn = 0;
+    int g_stack = 0;
 };
 
 namespace {
@@ -78,12 +89,13 @@ __device__ __forceinline__ uint32_t refill(uint32_t* fetch, uint32_t n, bool nee
     return i < n ? i : kMiss;
 }
 
-// One persistent launch over the rays of all scenes (per-lane refill).
-template <bool kAnyHit>
+// One persistent launch over the rays of all scenes (per-lane refill);
+// kStack: traversal stack entries per ray (a tuning choice: 16, 24 or 32).
+template <bool kAnyHit, int kStack>
 __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
 k_batch_trace(DevScene sc, const uint32_t* roots, const uint32_t* ray_off, uint32_t scenes, const mrt_ray* rays,
               uint32_t n, mrt_hit* hits, uint32_t* fetch, uint32_t* status) {
-    __shared__ uint2 stk[kStackDepth * kTraceBlock];
+    __shared__ uint2 stk[kStack * kTraceBlock];
     extern __shared__ uint32_t off[];  // scenes + 1 ray offsets
     for (uint32_t i = threadIdx.x; i <= scenes; i += blockDim.x) off[i] = ray_off[i];
     __syncthreads();
@@ -102,7 +114,7 @@ k_batch_trace(DevScene sc, const uint32_t* roots, const uint32_t* ray_off, uint3
             have = true;
         }
         if (!__any_sync(0xFFFFFFFFu, have)) break;
-        if (have && trav_step<kAnyHit, false, kStackDepth>(sc, s, my, kTraceBlock, st, cn, ct)) {
+        if (have && trav_step<kAnyHit, false, kStack>(sc, s, my, kTraceBlock, st, cn, ct)) {
             hits[ri].prim = s.best;
             hits[ri].t = s.best == kMiss ? s.tmax : s.tbest;
             have = false;
@@ -137,10 +149,11 @@ k_batch_init(const mrt_ray* rays, const uint32_t* ray_off, uint32_t scenes, uint
     if (blockIdx.x == 0 && threadIdx.x == 0) counters[kCntExt] = n;
 }
 
+template <int kStack>
 __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
 k_batch_trace_queue(DevScene sc, const uint32_t* roots, const PathRay* q, uint2* hits, uint32_t* counters,
                     uint32_t bounce, uint32_t* status) {
-    __shared__ uint2 stk[kStackDepth * kTraceBlock];
+    __shared__ uint2 stk[kStack * kTraceBlock];
     const uint32_t n = counters[kCntExt + bounce];
     uint32_t* fetch = counters + kCntFetchExt + bounce;
     uint2* my = stk + threadIdx.x;
@@ -158,7 +171,7 @@ k_batch_trace_queue(DevScene sc, const uint32_t* roots, const PathRay* q, uint2*
             have = true;
         }
         if (!__any_sync(0xFFFFFFFFu, have)) break;
-        if (have && trav_step<false, false, kStackDepth>(sc, s, my, kTraceBlock, st, cn, ct)) {
+        if (have && trav_step<false, false, kStack>(sc, s, my, kTraceBlock, st, cn, ct)) {
             hits[ri] = make_uint2(s.best, __float_as_uint(s.best == kMiss ? s.tmax : s.tbest));
             have = false;
         }
@@ -291,12 +304,16 @@ int mrt_cuda_batch_create(mrt_ctx* ctx, uint32_t count, const mrt_bvh8_node* con
     if (count > kMaxBatchScenes) return set_error(ctx, MRT_ERANGE, "batch_create: more than 4096 scenes");
     *out = nullptr;
     uint64_t nn = 0, nt = 0;
+    uint32_t max_depth = 0;
     for (uint32_t s = 0; s < count; ++s) {
         if (!nodes[s] || !tris[s] || !materials[s] || node_counts[s] == 0 || tri_counts[s] == 0)
             return set_error(ctx, MRT_EINVAL, "batch_create: empty scene");
         nn += node_counts[s];
         nt += tri_counts[s];
+        max_depth = std::max(max_depth, bvh8_depth(nodes[s], node_counts[s]));
     }
+    if (max_depth > uint32_t(kMaxBatchStack) + 1u)
+        return set_error(ctx, MRT_ERANGE, "batch_create: a BVH8 deeper than the largest traversal stack (33 levels)");
     if (nn >= 0xFFFFFFFFull || nt >= 0xFFFFFFFFull) return set_error(ctx, MRT_ERANGE, "batch_create: too large");
     std::vector<mrt_bvh8_node> an;
     std::vector<mrt_tri> at;
@@ -346,6 +363,7 @@ int mrt_cuda_batch_create(mrt_ctx* ctx, uint32_t count, const mrt_bvh8_node* con
     b->dev.nodes = static_cast<const uint4*>(b->d_nodes);
     b->dev.tris = static_cast<const float4*>(b->d_tris);
     b->dev.mats = static_cast<const mrt_material*>(b->d_mats);
+    b->max_depth = max_depth;
     b->dev.node_count = uint32_t(an.size());
     b->dev.tri_count = uint32_t(at.size());
     b->dev.mat_count = uint32_t(am.size());
@@ -381,12 +399,16 @@ int mrt_cuda_batch_trace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, const 
         return set_error(ctx, MRT_ECUDA, "batch_trace: memset failed");
     const int blocks = persistent_blocks(ctx);
     const size_t dsm = (b->scenes + 1u) * sizeof(uint32_t);
-    if (flags & MRT_TRACE_ANY_HIT)
-        k_batch_trace<true><<<blocks, kTraceBlock, dsm, s>>>(b->dev, b->d_roots, b->d_ray_off, b->scenes, rays, n,
-                                                             hits, ctx->d_prim_fetch, ctx->d_status);
-    else
-        k_batch_trace<false><<<blocks, kTraceBlock, dsm, s>>>(b->dev, b->d_roots, b->d_ray_off, b->scenes, rays, n,
-                                                              hits, ctx->d_prim_fetch, ctx->d_status);
+    const int stack = batch_stack(ctx, b->max_depth);
+    if (!stack) return set_error(ctx, MRT_ERANGE, "batch_trace: stack_depth below the batch's BVH depth");
+    const bool any = (flags & MRT_TRACE_ANY_HIT) != 0u;
+#define MRT_BT(K, S)                                                                                             \
+    k_batch_trace<K, S><<<blocks, kTraceBlock, dsm, s>>>(b->dev, b->d_roots, b->d_ray_off, b->scenes, rays, n, hits, \
+                                                         ctx->d_prim_fetch, ctx->d_status)
+    if (stack == 16) { if (any) MRT_BT(true, 16); else MRT_BT(false, 16); }
+    else if (stack == 32) { if (any) MRT_BT(true, 32); else MRT_BT(false, 32); }
+    else { if (any) MRT_BT(true, 24); else MRT_BT(false, 24); }
+#undef MRT_BT
     if (cudaGetLastError() != cudaSuccess) return set_error(ctx, MRT_ECUDA, "batch_trace: launch failed");
     ctx->launches++;
     return MRT_OK;
@@ -427,6 +449,8 @@ int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, co
         return set_error(ctx, MRT_ECUDA, "batch_pathtrace: parameter upload failed");
 
     const int blocks = persistent_blocks(ctx);
+    const int stack = batch_stack(ctx, b->max_depth);
+    if (!stack) return set_error(ctx, MRT_ERANGE, "batch_pathtrace: stack_depth below the batch's BVH depth");
     const uint32_t bounces = params->max_bounces;
     const int sblocks = int(std::min<size_t>((n + kShadeBlock - 1) / kShadeBlock, 8192));
     auto enqueue = [&](cudaStream_t st) -> bool {
@@ -434,8 +458,15 @@ int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, co
         k_batch_init<<<sblocks, kShadeBlock, (b->scenes + 1u) * sizeof(uint32_t), st>>>(
             rays, b->d_ray_off, b->scenes, n, b->q[0], b->rng, radiance, b->counters, b->d_frame);
         for (uint32_t v = 0; v <= bounces; ++v) {
-            k_batch_trace_queue<<<blocks, kTraceBlock, 0, st>>>(b->dev, b->d_roots, b->q[v & 1u], b->hits,
-                                                                b->counters, v, ctx->d_status);
+            if (stack == 16)
+                k_batch_trace_queue<16><<<blocks, kTraceBlock, 0, st>>>(b->dev, b->d_roots, b->q[v & 1u], b->hits,
+                                                                        b->counters, v, ctx->d_status);
+            else if (stack == 32)
+                k_batch_trace_queue<32><<<blocks, kTraceBlock, 0, st>>>(b->dev, b->d_roots, b->q[v & 1u], b->hits,
+                                                                        b->counters, v, ctx->d_status);
+            else
+                k_batch_trace_queue<24><<<blocks, kTraceBlock, 0, st>>>(b->dev, b->d_roots, b->q[v & 1u], b->hits,
+                                                                        b->counters, v, ctx->d_status);
             k_batch_shade<<<sblocks, kShadeBlock, 0, st>>>(b->dev, b->d_tp, b->q[v & 1u], b->q[(v + 1u) & 1u],
                                                            b->hits, b->rng, radiance, b->counters, v,
                                                            ctx->d_status);
@@ -450,7 +481,7 @@ int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, co
         return MRT_OK;
     }
     const bool same = b->exec && b->g_rays == rays && b->g_radiance == radiance && b->g_n == n &&
-                      b->g_bounces == bounces && b->g_blocks == uint32_t(blocks);
+                      b->g_bounces == bounces && b->g_blocks == uint32_t(blocks) && b->g_stack == stack;
     if (!same) {
         if (b->exec) cudaGraphExecDestroy(b->exec);
         b->exec = nullptr;
@@ -477,6 +508,7 @@ int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, co
         b->g_n = n;
         b->g_bounces = bounces;
         b->g_blocks = uint32_t(blocks);
+        b->g_stack = stack;
     }
     if (cudaGraphLaunch(b->exec, s) != cudaSuccess) return set_error(ctx, MRT_ECUDA, "batch_pathtrace: graph launch");
     ctx->launches += 2 + 2 * (bounces + 1);

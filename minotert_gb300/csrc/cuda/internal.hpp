@@ -131,6 +131,10 @@ struct BlueNoise {
 };
 
 // Launchers (kernels.cu).  All return cudaError_t of the launch.
+// Depth of a BVH8 (levels along in-range child links, each node counted
+// once); the traversal stack holds at most depth - 1 entries.
+uint32_t bvh8_depth(const mrt_bvh8_node* nodes, uint32_t n);
+
 // fetch != nullptr selects the persistent dynamic-fetch kernel (`blocks`
 // blocks); otherwise one thread per pixel.
 cudaError_t launch_primary_tri(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g,
@@ -213,7 +217,7 @@ struct mrt_ctx {
     // timing
     bool timing = false;
     bool counters = false;
-    mrt_tuning tuning{0u, 1u, 0u, mrt::kSortNever, 3u};  // autotuned on GB300 (icosphere field, 1080p)
+    mrt_tuning tuning{0u, 1u, 0u, mrt::kSortNever, 3u, 0u};  // autotuned on GB300 (icosphere field, 1080p)
     uint32_t* d_prim_fetch = nullptr;  // work counter of the persistent primary kernel
     int occ_blocks = 0;                // traversal blocks per SM at full occupancy
     unsigned long long* d_totals = nullptr;  // kTotSlots accumulated totals

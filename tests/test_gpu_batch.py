@@ -82,3 +82,33 @@ def test_batch_graph_equals_direct_launch(ctx, small_batch):
     batch.pathtrace(d_rays, offsets, params, 9, b, use_graph=True)
     ra, rb = a.download(np.float32, (len(rays), 3)), b.download(np.float32, (len(rays), 3))
     assert np.array_equal(ra.view(np.uint32), rb.view(np.uint32))
+
+
+def test_batch_stack_depths_agree(ctx, small_batch):
+    # the traversal stack size is a tuning choice (16, 24, 32 entries): the
+    # hits and the path-traced radiance do not depend on it; a size below the
+    # batch's BVH depth is refused
+    import ctypes as C
+    from minotert_gb300._lib import MrtError, lib
+    wl, scenes, batch, rays, offsets = small_batch
+    d_rays = ctx.to_device(rays)
+    d_hits = ctx.alloc(8 * len(rays))
+    d_rad = ctx.alloc(12 * len(rays))
+    params = wl.settings.params(wl.sky)
+    saved = ctx.tuning()
+    outs = {}
+    try:
+        for depth in (16, 24, 32):
+            ctx.set_tuning(stack_depth=depth)
+            batch.trace(d_rays, offsets, d_hits)
+            batch.pathtrace(d_rays, offsets, params, 5, d_rad, use_graph=True)
+            outs[depth] = (d_hits.download(HIT_DTYPE, (len(rays),)).copy(),
+                           d_rad.download(np.float32, (len(rays), 3)).copy())
+        assert ctx.status() == 0
+        for depth in (16, 32):
+            assert np.array_equal(outs[depth][0], outs[24][0]), depth
+            assert np.array_equal(outs[depth][1].view(np.uint32), outs[24][1].view(np.uint32)), depth
+        with pytest.raises(MrtError):
+            ctx.set_tuning(stack_depth=20)
+    finally:
+        lib().mrt_cuda_set_tuning(ctx.handle, C.byref(saved))
