@@ -793,6 +793,163 @@ def run_reference(args, world, rank, local, dist):
         dist.destroy_process_group()
 
 
+REF_SCENE_UNIT = "Msamples/s"
+
+
+def _reference_scene_cpu(W, H, frame, budget_s, threads):
+    """The reference's own primaryRay.comp + secondaryRays.comp (compiled for
+    the host from its GLSL, oracle/glsl) on `threads` host cores over a band
+    of rows of the W x H frame; returns Msamples/s and what was timed.  None
+    where no translation of the shaders is available."""
+    import ctypes as C
+    from oracle import post
+    from oracle.glsl import build_ref
+    from minotert_gb300.pathtracer import Camera
+    from minotert_gb300.scene import blue_noise
+    sys.path.insert(0, str(ROOT / "tests"))
+    from conftest import oracle_consts
+    L = build_ref.lib()
+    if L is None:
+        return None
+    p = lambda a: a.ctypes.data_as(C.c_void_p)
+    cam = Camera.reference(W, H)
+    consts = np.ascontiguousarray(oracle_consts(cam, frame)).view(np.float32)
+    atmo = post.earth()
+    trans = np.zeros((64, 256, 4), np.float32)
+    L.ref_sky_transmittance(p(atmo), p(trans))
+    ms = np.zeros((32, 32, 4), np.float32)
+    L.ref_sky_multiscatter(p(atmo), p(trans), p(ms))
+    sun = np.array([-0.435286462, 0.818654716, 0.374606609], np.float32)
+    sun_e = np.full(3, 8.0, np.float32)
+    probe = np.asarray(cam.position, np.float32)
+    view = np.zeros((108, 192, 4), np.float32)
+    L.ref_sky_view(p(atmo), p(trans), p(ms), p(probe), p(sun), p(sun_e), p(view))
+    bn4 = np.ascontiguousarray(blue_noise(1, 64).astype(np.float32) / np.float32(255.0))
+    L.ref_dispatch_threads(threads)
+    # the g-buffer of the whole frame, then bands of rows of the secondary
+    # pass (the shader reads only its own pixel of the g-buffer)
+    vis4 = np.zeros((H, W, 4), np.uint32)
+    d4, n4, m4 = (np.zeros((H, W, 4), np.float32) for _ in range(3))
+    t0 = time.perf_counter()
+    L.ref_primary_rays(p(consts), W, H, p(vis4), p(d4), p(n4), p(m4))
+    t_prim = time.perf_counter() - t0
+    dep4 = np.zeros_like(d4)
+    dep4[..., 0] = np.where(vis4[..., 0] == 0xFFFFFFFF, 0.0, d4[..., 0]).astype(np.float16).astype(np.float32)
+    nrm4 = np.ascontiguousarray(n4.astype(np.float16).astype(np.float32))
+    rows, secs = 0, 0.0
+    band = 16
+    col = np.zeros((H, W, 4), np.float32)
+    while secs < budget_s and rows < H:
+        h = min(band, H - rows)
+        t0 = time.perf_counter()
+        L.ref_secondary_rays_rows(p(consts), W, H, p(vis4), p(dep4), p(nrm4), p(bn4), 64, 64, p(trans), 256, 64,
+                                  p(view), 192, 108, p(atmo), p(col), rows, rows + h)
+        secs += time.perf_counter() - t0
+        rows += h
+        band *= 2
+    L.ref_dispatch_threads(1)
+    return None if rows == 0 else {"rows": rows, "seconds": secs, "primary_s": t_prim}
+
+
+def run_reference_scene(args, world, rank, local, dist):
+    """MinoteRT's own scene and settings (scene.glsl's five spheres, the
+    start-up camera, secondaryRays.comp's 8 samples x 8 bounces, sky LUT +
+    sun disc) at 1920x1080: this build's sphere path on the GPU against the
+    reference's own compute shaders compiled for the host cores."""
+    W, H, SPP = 1920, 1080, 8
+    cores = os.cpu_count() or 1
+    if args.impl == "reference":
+        if rank != 0:
+            if dist is not None:
+                dist.destroy_process_group()
+            return
+        r = None
+        vals, secs = [], 0.0
+        for k in range(args.warmup + args.steps):
+            r = _reference_scene_cpu(W, H, k, 4.0 if k >= args.warmup else 1.0, cores)
+            if r is None:
+                print(json.dumps({"impl": "reference", "unavailable": "no translation of the reference's shaders "
+                                  "(oracle/_ref) on this host"}))
+                return
+            if k >= args.warmup:
+                vals.append(r["rows"] * W * SPP / r["seconds"] / 1e6)
+                secs += r["seconds"]
+        value = statistics.mean(vals)
+        print(json.dumps({"metric": "Msamples/s (reference scene, 1920x1080, 8 spp x 8 bounces)", "value": value,
+                          "unit": REF_SCENE_UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f32", "data": "the reference's own scene",
+                          "config": {"workload": "reference_spheres_1080p", "spp": SPP, "bounces": 8},
+                          "impl": "reference",
+                          "cpu_baseline": {"value": value, "unit": REF_SCENE_UNIT, "cores": cores,
+                                           "kind": "reference",
+                                           "sample": "bands of rows of the secondary pass, the reference's "
+                                                     "secondaryRays.comp compiled for the host (oracle/glsl)"},
+                          "e2e": {"value": value, "unit": REF_SCENE_UNIT, "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    from minotert_gb300 import build as _build
+    _build.build()
+    from minotert_gb300._lib import Context
+    from minotert_gb300.pathtracer import Camera, Pathtracer, Sky as ConstSky, TraceSettings
+    from minotert_gb300.scene import DeviceScene, blue_noise, reference_spheres
+    from minotert_gb300.sky import Atmosphere, Sky
+    ctx = Context(local)
+    ds = DeviceScene.from_spheres(ctx, reference_spheres())
+    bn = blue_noise(1, 64)
+    cam = Camera.reference(W, H)
+    stream = ctx.stream()
+    atmo = Atmosphere(ctx)
+    view = Sky().createView(atmo, np.asarray(cam.position, np.float32))
+    pt = Pathtracer(ctx, ds)
+    col = ctx.alloc(12 * W * H)
+    flush = ctx.alloc(256 << 20)
+    settings = TraceSettings(samples=SPP, bounces=8)
+    none_sky = ConstSky(radiance=(0.0, 0.0, 0.0), sun_dir=None)
+
+    def frame(k):
+        pt.frame_counter = k
+        gb = pt.primaryRays((W, H), cam, cam, stream)
+        pt.secondaryRays(gb, cam, none_sky, bn, settings, color=col, stream=stream, skyView=view)
+
+    for k in range(args.warmup):
+        frame(k)
+    ctx.sync(stream)
+    ms = []
+    for k in range(args.steps):
+        flush.zero(stream)
+        a, b = ctx.event(), ctx.event()
+        ctx.record(a, stream)
+        frame(args.warmup + k)
+        ctx.record(b, stream)
+        ctx.sync(stream)
+        ms.append(ctx.elapsed_ms(a, b))
+    t = _allmax(dist, sum(ms) / 1e3)
+    samples = _allsum(dist, float(W * H * SPP * args.steps))
+    value = samples / t / 1e6
+    out = {"metric": "Msamples/s (reference scene, 1920x1080, 8 spp x 8 bounces)", "value": value,
+           "unit": REF_SCENE_UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": t * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "the reference's own scene (scene.glsl), camera (app.ixx) and settings",
+           "config": {"workload": "reference_spheres_1080p", "width": W, "height": H, "spp": SPP, "bounces": 8,
+                      "l2": "256 MiB memset between timed steps"},
+           "device_status": ctx.status()}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        r = _reference_scene_cpu(W, H, 0, 8.0, cores)
+        if r is not None:
+            v = r["rows"] * W * SPP / r["seconds"] / 1e6
+            out["cpu_baseline"] = {"value": v, "unit": REF_SCENE_UNIT, "cores": cores, "kind": "reference",
+                                   "sample": f"{r['rows']} rows of the secondary pass in {r['seconds']:.1f} s, "
+                                             "the reference's secondaryRays.comp compiled for the host"}
+    atmo.close()
+    if rank == 0:
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def run_network_kernels(args, world, rank, local, dist):
     """Inference time of the two networks at 1920x1080 with random weights
     and inputs: the CNN denoiser on one frame of features and the radiance
@@ -939,12 +1096,15 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", choices=["icospheres_1080p", "heightfield_boxes_256", "batched64",
-                                           "radiance_cache", "denoiser", "network_kernels", "post_kernels"],
+                                           "radiance_cache", "denoiser", "network_kernels", "post_kernels",
+                                           "reference_spheres_1080p"],
                     default="icospheres_1080p")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
     world, rank, local, dist = _dist()
-    if args.impl == "reference":
+    if args.workload == "reference_spheres_1080p":
+        run_reference_scene(args, world, rank, local, dist)
+    elif args.impl == "reference":
         run_reference(args, world, rank, local, dist)
     elif args.workload == "batched64":
         run_batched(args, world, rank, local, dist)

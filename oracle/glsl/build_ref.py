@@ -1,12 +1,14 @@
 """Build recipe: the reference's own compute shaders, compiled for the host.
 
-Test infrastructure only.  Reads the shader sources where they lie in the
-reference tree (src/gpu/ of MinoteRT), rewrites each into C++ against
-glsl.hpp (translate.py), appends the entry-point shim from this folder and
-compiles everything with g++ into oracle/_ref/libglsl_ref.so.  Outputs go to
-oracle/_ref/ only (git-ignored).  Nothing here is copied into the
-repository: without the reference tree `build()` returns None and the tests
-fall back to the committed vectors in tests/golden/.
+Test infrastructure and the CPU baseline of the reference's own code only.
+Reads the shader sources where they lie in the reference tree (src/gpu/ of
+MinoteRT), rewrites each into C++ against glsl.hpp (translate.py), appends
+the entry-point shim from this folder and compiles everything with g++ into
+oracle/_ref/libglsl_ref.so.  Outputs go to oracle/_ref/ only (git-ignored,
+carried to the GPU host with the rest of the tree, where the translation is
+compiled again for its CPU).  Nothing here is copied into the repository:
+with neither the reference tree nor a translation `build()` returns None
+and the tests fall back to the committed vectors in tests/golden/.
 
 Compiler settings that make the C++ evaluate the GLSL as written:
 -ffp-contract=off (no fused multiply-add), -fsingle-precision-constant
@@ -83,11 +85,17 @@ def _unit_source(name: str, rel: str | None, shim: str, pre: str, defines: str, 
 
 
 def build(force: bool = False) -> Path | None:
-    """Compile the shaders; returns the library path, or None without the reference tree."""
-    if not available():
-        return None
+    """Compile the shaders; returns the library path, or None when neither the
+    reference tree nor an earlier translation (oracle/_ref/glsl/*.cpp, which
+    travels with the rest of oracle/_ref) is there."""
     (OUT / "glsl").mkdir(parents=True, exist_ok=True)
-    srcs = {u[0]: _unit_source(*u) for u in UNITS}
+    if available():
+        srcs = {u[0]: _unit_source(*u) for u in UNITS}
+    else:
+        files = {u[0]: OUT / "glsl" / f"{u[0]}.cpp" for u in UNITS}
+        if not all(f.is_file() for f in files.values()):
+            return None
+        srcs = {n: f.read_text() for n, f in files.items()}
     key = hashlib.sha256(("".join(srcs[n] for n in sorted(srcs)) + (HERE / "glsl.hpp").read_text() +
                           " ".join(_FLAGS)).encode()).hexdigest()[:16]
     lib = OUT / "libglsl_ref.so"
@@ -137,6 +145,9 @@ def lib() -> C.CDLL | None:
         L.ref_primary_rays.argtypes, L.ref_primary_rays.restype = [vp, i, i, vp, vp, vp, vp], i
         L.ref_secondary_rays.argtypes = [vp, i, i, vp, vp, vp, vp, i, i, vp, i, i, vp, i, i, vp, vp]
         L.ref_secondary_rays.restype = i
+        L.ref_dispatch_threads.argtypes, L.ref_dispatch_threads.restype = [i], i
+        L.ref_secondary_rays_rows.argtypes = [vp, i, i, vp, vp, vp, vp, i, i, vp, i, i, vp, i, i, vp, vp, i, i]
+        L.ref_secondary_rays_rows.restype = i
         L.ref_sky_transmittance.argtypes, L.ref_sky_transmittance.restype = [vp, vp], i
         L.ref_sky_multiscatter.argtypes, L.ref_sky_multiscatter.restype = [vp, vp, vp], i
         L.ref_sky_view.argtypes, L.ref_sky_view.restype = [vp, vp, vp, vp, vp, vp, vp], i

@@ -23,7 +23,10 @@
 #include <cmath>
 #include <cstddef>
 #include <cstdint>
+#include <atomic>
 #include <initializer_list>
+#include <thread>
+#include <vector>
 #include <type_traits>
 
 namespace glsl {
@@ -386,10 +389,48 @@ inline void barrier() {
     if (gl_workgroup_barrier) gl_workgroup_barrier->wait();
 }
 
+// ---- dispatch of a w x h grid of invocations: rows spread over `threads`
+// host threads (the invocation ids are thread-local; a shader's globals are
+// set before and only read during the dispatch)
+template <class F> void dispatch_rows(int w, int y0, int y1, int threads, F&& f);
+template <class F> void dispatch_2d(int w, int h, int threads, F&& f);
+// the thread count the shims dispatch with (shared by every translation unit)
+inline std::atomic<int>& ref_thread_count() {
+    static std::atomic<int> n{1};
+    return n;
+}
+inline int ref_threads() { return ref_thread_count().load(); }
+inline int ref_dispatch_threads_set(int n) {
+    if (n >= 1) ref_thread_count().store(n);
+    return ref_threads();
+}
+
 // ---- invocation ids (set by the dispatcher before each invocation)
 inline thread_local uvec3 gl_GlobalInvocationID;
 inline thread_local uvec3 gl_LocalInvocationID;
 inline thread_local uvec3 gl_WorkGroupID;
 inline thread_local uint gl_LocalInvocationIndex;
+
+template <class F> void dispatch_rows(int w, int y0, int y1, int threads, F&& f) {
+    auto rows = [&](int r0, int r1) {
+        for (int y = r0; y < r1; ++y)
+            for (int x = 0; x < w; ++x) {
+                gl_GlobalInvocationID = uvec3(uint(x), uint(y), 0u);
+                f();
+            }
+    };
+    if (threads <= 1 || y1 - y0 < 2) {
+        rows(y0, y1);
+        return;
+    }
+    std::vector<std::thread> pool;
+    std::atomic<int> next{y0};
+    for (int t = 0; t < threads; ++t)
+        pool.emplace_back([&] {
+            for (int y; (y = next.fetch_add(1)) < y1;) rows(y, y + 1);
+        });
+    for (auto& t : pool) t.join();
+}
+template <class F> void dispatch_2d(int w, int h, int threads, F&& f) { dispatch_rows(w, 0, h, threads, f); }
 
 } // namespace glsl
