@@ -450,11 +450,14 @@ __global__ void k_tc_weights(const bf16* w16, bf16* wt, TcLayerTable t) {
     }
 }
 
-// Shapes of the TMA form per COUT, from a sweep on the 1080p denoiser (ms per
+// Shapes of the TMA form per COUT, from sweeps on the 1080p denoiser (ms per
 // inference, upsampling layers on the cp.async kernel: cp.async everywhere
-// 1.607; TMA with 4 / 8 rows 1.369, 3 stages 1.640; 2 rows at COUT 128
-// 1.345): rows per CTA and two stages, two CTAs per SM.
-__host__ __device__ constexpr int tma_rows(int cout) { return cout >= 128 ? 2 : (cout >= 64 ? 4 : 8); }
+// 1.607; TMA with 2 / 4 / 8 rows at COUT 128 / 64 / <= 32 1.341; 2 rows at
+// COUT >= 64 and 4 below 1.307; 2 rows everywhere 1.350; 1 row at COUT >= 64
+// 1.401; three stages 1.42-1.64): rows per CTA and two stages, two CTAs per
+// SM.  With one thread driving a CTA's pipeline, more and smaller CTAs keep
+// more copies and MMAs in flight.
+__host__ __device__ constexpr int tma_rows(int cout) { return cout >= 64 ? 2 : 4; }
 __host__ __device__ constexpr int tma_stages(int) { return 2; }
 
 // NHWC BF16 tensor map with the halo box of one 8-channel half
