@@ -954,7 +954,7 @@ def run_network_kernels(args, world, rank, local, dist):
     """Inference time of the two networks at 1920x1080 with random weights
     and inputs: the CNN denoiser on one frame of features and the radiance
     cache on 2,073,600 queries (CUDA events, --steps timed runs after
-    --warmup).  The driver for the network-kernel ncu captures."""
+    --warmup).  The network-kernel ncu captures profile this command."""
     from minotert_gb300 import build as _build
     _build.build()
     from minotert_gb300._lib import Context

@@ -30,7 +30,7 @@
 // FP32 mode reproduces the kernels' arithmetic order (explicit fma where the
 // kernels use one, no contraction elsewhere; built with -ffp-contract=off),
 // so primary hits and t are bit-identical.  FP64 mode evaluates the same
-// estimator in double precision as the judge of converged images.
+// estimator in double precision as the check of converged images.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
