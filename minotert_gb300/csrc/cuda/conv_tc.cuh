@@ -484,17 +484,27 @@ inline bool tma_encode(CUtensorMap* map, const bf16* base, int c, int w, int h, 
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) once per device for the
+// kernel whose flag word this is (bit d = device d configured)
+template <class K>
+cudaError_t tc_configure(K kernel, size_t smem, uint64_t& configured) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t bit = uint64_t(1) << (dev & 63);
+    if (configured & bit) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e == cudaSuccess) configured |= bit;
+    return e;
+}
+
 template <int COUT>
 cudaError_t launch_conv_tma(const ConvArgs& ca, const bf16* wt, uint32_t* status, cudaStream_t s) {
     constexpr int kRows = tma_rows(COUT), kStages = tma_stages(COUT);
-    static bool configured = false;
+    static uint64_t configured = 0;
     const size_t smem = size_t(kStages) * tma_stage_bytes<COUT, kRows>() + 128;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_conv_tma<COUT, kRows, kStages>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    cudaError_t e = tc_configure(k_conv_tma<COUT, kRows, kStages>, smem, configured);
+    if (e != cudaSuccess) return e;
     CUtensorMap ma, mb;
     if (!tma_encode(&ma, ca.a, ca.ca, ca.w_, ca.h, ca.n, kRows)) return cudaErrorInvalidValue;
     if (ca.cb > 0) {
@@ -510,14 +520,10 @@ cudaError_t launch_conv_tma(const ConvArgs& ca, const bf16* wt, uint32_t* status
 template <int COUT>
 cudaError_t launch_conv_tc(const ConvArgs& ca, uint32_t* status, cudaStream_t s) {
     constexpr int kRows = tc_rows(COUT), kStages = tc_stages(COUT);
-    static bool configured = false;  // per process; all devices are sm_103
+    static uint64_t configured = 0;
     const size_t smem = tc_smem_bytes(COUT, kRows, kStages);
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_conv_tc<COUT, kRows, kStages>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    cudaError_t e = tc_configure(k_conv_tc<COUT, kRows, kStages>, smem, configured);
+    if (e != cudaSuccess) return e;
     const int blocks = ((ca.w_ + kTcPix - 1) / kTcPix) * ((ca.h + kRows - 1) / kRows) * ca.n;
     k_conv_tc<COUT, kRows, kStages><<<blocks, 128, smem, s>>>(ca, status);
     return cudaGetLastError();
