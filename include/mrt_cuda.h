@@ -263,6 +263,13 @@ typedef struct mrt_tuning {
                                      kernels (mrt_cuda_batch_*): 16, 24 or
                                      32; 0 = 24.  Must cover the batch's
                                      deepest BVH (depth - 1 entries)         */
+    uint32_t tri_spread;          /* bit 0: extension rays, bit 1: shadow rays
+                                     (with dynamic_fetch set for them), bit 2:
+                                     primary rays (one thread per pixel): the
+                                     triangle tests of a traversal step are
+                                     spread over the warp's lanes instead of
+                                     each lane testing its own leaves' (same
+                                     hits)                                   */
 } mrt_tuning;
 int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning);
 int mrt_cuda_get_tuning(mrt_ctx* ctx, mrt_tuning* tuning);

@@ -1,8 +1,9 @@
 """Autotuner for the traversal launch schedule (mrt_tuning).
 
 Sweeps persistent blocks per SM (warps per SM = 4 x blocks), the work-fetch
-mode of the persistent kernels, the primary-ray kernel form and the
-ray-sort threshold on a caller-supplied frame function, timing each
+mode of the persistent kernels, the primary-ray kernel form, the ray-sort
+threshold, the path tail and the spreading of triangle tests over the warp
+on a caller-supplied frame function, timing each
 candidate with CUDA events on the frame's stream, and keeps the fastest.
 Results are cached as JSON keyed by GPU and workload, so a renderer pays
 for the sweep once.
@@ -31,9 +32,10 @@ def candidates(max_blocks_per_sm: int, sort: bool = False):
     # dynamic_fetch bit 0: extension rays, bit 1: shadow rays
     # tail_bounce: 0 = wavefront passes for every bounce, 3 = one persistent
     # launch finishes the paths alive at bounce 3
-    for b, dyn, prim, thr, tail in itertools.product(blocks, (1, 3, 0, 2), (0, 1), sort_thr, (3, 0)):
+    # tri_spread bit 0: the extension rays' triangle tests spread over the warp
+    for b, dyn, prim, thr, tail, spread in itertools.product(blocks, (1, 3, 0, 2), (0, 1), sort_thr, (3, 0), (1, 0)):
         yield {"trace_blocks_per_sm": b, "dynamic_fetch": dyn, "primary_persistent": prim, "sort_min_rays": thr,
-               "tail_bounce": tail}
+               "tail_bounce": tail, "tri_spread": spread}
 
 
 def time_frames(ctx: Context, run_frame, stream, frames: int, warmup: int) -> float:

@@ -287,10 +287,18 @@ int mrt_cuda_set_timing(mrt_ctx* ctx, int enable) {
     return MRT_OK;
 }
 
+// Work schedule of the extension (which = 0) or shadow (which = 1) trace
+// kernels from mrt_tuning.dynamic_fetch and tri_spread.
+static int fetch_mode(const mrt_ctx* ctx, uint32_t which) {
+    const bool spread = ((ctx->tuning.tri_spread >> which) & 1u) != 0u;
+    if (!((ctx->tuning.dynamic_fetch >> which) & 1u)) return spread ? mrt::kFetchBatchSpread : mrt::kFetchBatch;
+    return spread ? mrt::kFetchSpread : mrt::kFetchDynamic;
+}
+
 int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning) {
     if (!ctx || !tuning) return fail(ctx, MRT_EINVAL, "set_tuning: null argument");
     if (tuning->trace_blocks_per_sm > 64 || tuning->dynamic_fetch > 3 || tuning->primary_persistent > 1 ||
-        tuning->tail_bounce > MRT_MAX_BOUNCES ||
+        tuning->tail_bounce > MRT_MAX_BOUNCES || tuning->tri_spread > 7 ||
         (tuning->stack_depth != 0u && tuning->stack_depth != 16u && tuning->stack_depth != 24u &&
          tuning->stack_depth != 32u))
         return fail(ctx, MRT_EINVAL, "set_tuning: value out of range");
@@ -611,7 +619,7 @@ int mrt_cuda_primary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_camera
                             ? launch_primary_tri(scene->dev, fp, *gbuffer, ctx->d_status,
                                                  ctx->counters ? ctx->d_totals : nullptr,
                                                  ctx->tuning.primary_persistent ? ctx->d_prim_fetch : nullptr,
-                                                 trace_blocks(ctx), s)
+                                                 trace_blocks(ctx), (ctx->tuning.tri_spread & 4u) != 0u, s)
                             : launch_primary_sphere(scene->dev, fp, *gbuffer, s);
         if (e != cudaSuccess) return fail(ctx, MRT_ECUDA, "primary rays launch: %s", cudaGetErrorString(e));
     }
@@ -655,7 +663,7 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
     WaveBuffers& wb = ctx->wb;
     const int tblocks = trace_blocks(ctx);
     const bool nee = tp.estimator == MRT_EST_NEE;
-    const bool dyn = (ctx->tuning.dynamic_fetch & 1u) != 0u, dyn_sh = (ctx->tuning.dynamic_fetch & 2u) != 0u;
+    const int dyn = fetch_mode(ctx, 0u), dyn_sh = fetch_mode(ctx, 1u);
 #define MRT_LAUNCH(kind, bounce, expr)                                                                   \
     do {                                                                                                 \
         Scope sc_(ctx, s, kind, bounce);                                                                 \
@@ -733,7 +741,7 @@ int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
     tp.max_bounces = 1;  // the path ends in the cache at the first bounce's hit
     const int tblocks = trace_blocks(ctx);
     const bool nee = tp.estimator == MRT_EST_NEE;
-    const bool dyn = (ctx->tuning.dynamic_fetch & 1u) != 0u, dyn_sh = (ctx->tuning.dynamic_fetch & 2u) != 0u;
+    const int dyn = fetch_mode(ctx, 0u), dyn_sh = fetch_mode(ctx, 1u);
 #define MRT_LAUNCH(kind, bounce, expr)                                                                   \
     do {                                                                                                 \
         Scope sc_(ctx, s, kind, bounce);                                                                 \

@@ -60,6 +60,7 @@ struct mrt_batch {
     float* g_radiance = nullptr;
     uint32_t g_n = 0, g_bounces = 0, g_blocks = 0, g_dyn = 0;
     int g_stack = 0;
+    bool g_spread = false;
 };
 
 namespace {
@@ -90,18 +91,21 @@ __device__ __forceinline__ uint32_t refill(uint32_t* fetch, uint32_t n, bool nee
 }
 
 // One persistent launch over the rays of all scenes (per-lane refill);
-// kStack: traversal stack entries per ray (a tuning choice: 16, 24 or 32).
-template <bool kAnyHit, int kStack>
+// kStack: traversal stack entries per ray (a tuning choice: 16, 24 or 32);
+// kSpread: the triangle tests of each step spread over the warp
+// (trav_step_spread; same hits).
+template <bool kAnyHit, int kStack, bool kSpread>
 __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
 k_batch_trace(DevScene sc, const uint32_t* roots, const uint32_t* ray_off, uint32_t scenes, const mrt_ray* rays,
               uint32_t n, mrt_hit* hits, uint32_t* fetch, uint32_t* status) {
     __shared__ uint2 stk[kStack * kTraceBlock];
+    __shared__ unsigned long long slots[kSpread ? kTraceBlock : 1];
     extern __shared__ uint32_t off[];  // scenes + 1 ray offsets
     for (uint32_t i = threadIdx.x; i <= scenes; i += blockDim.x) off[i] = ray_off[i];
     __syncthreads();
     uint2* my = stk + threadIdx.x;
     uint32_t st = 0u, cn = 0u, ct = 0u, ri = 0u;
-    Trav s;
+    Trav s{};
     bool have = false, exhausted = false;
     while (true) {
         const uint32_t idx = refill(fetch, n, !have, exhausted);
@@ -114,7 +118,12 @@ k_batch_trace(DevScene sc, const uint32_t* roots, const uint32_t* ray_off, uint3
             have = true;
         }
         if (!__any_sync(0xFFFFFFFFu, have)) break;
-        if (have && trav_step<kAnyHit, false, kStack>(sc, s, my, kTraceBlock, st, cn, ct)) {
+        bool fin;
+        if (kSpread)
+            fin = trav_step_spread<kAnyHit, kStack>(sc, s, have, my, kTraceBlock, st, slots + (threadIdx.x & ~31u));
+        else
+            fin = have && trav_step<kAnyHit, false, kStack>(sc, s, my, kTraceBlock, st, cn, ct);
+        if (have && fin) {
             hits[ri].prim = s.best;
             hits[ri].t = s.best == kMiss ? s.tmax : s.tbest;
             have = false;
@@ -149,16 +158,17 @@ k_batch_init(const mrt_ray* rays, const uint32_t* ray_off, uint32_t scenes, uint
     if (blockIdx.x == 0 && threadIdx.x == 0) counters[kCntExt] = n;
 }
 
-template <int kStack>
+template <int kStack, bool kSpread>
 __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
 k_batch_trace_queue(DevScene sc, const uint32_t* roots, const PathRay* q, uint2* hits, uint32_t* counters,
                     uint32_t bounce, uint32_t* status) {
     __shared__ uint2 stk[kStack * kTraceBlock];
+    __shared__ unsigned long long slots[kSpread ? kTraceBlock : 1];
     const uint32_t n = counters[kCntExt + bounce];
     uint32_t* fetch = counters + kCntFetchExt + bounce;
     uint2* my = stk + threadIdx.x;
     uint32_t st = 0u, cn = 0u, ct = 0u, ri = 0u;
-    Trav s;
+    Trav s{};
     bool have = false, exhausted = false;
     while (true) {
         const uint32_t idx = refill(fetch, n, !have, exhausted);
@@ -171,7 +181,12 @@ k_batch_trace_queue(DevScene sc, const uint32_t* roots, const PathRay* q, uint2*
             have = true;
         }
         if (!__any_sync(0xFFFFFFFFu, have)) break;
-        if (have && trav_step<false, false, kStack>(sc, s, my, kTraceBlock, st, cn, ct)) {
+        bool fin;
+        if (kSpread)
+            fin = trav_step_spread<false, kStack>(sc, s, have, my, kTraceBlock, st, slots + (threadIdx.x & ~31u));
+        else
+            fin = have && trav_step<false, false, kStack>(sc, s, my, kTraceBlock, st, cn, ct);
+        if (have && fin) {
             hits[ri] = make_uint2(s.best, __float_as_uint(s.best == kMiss ? s.tmax : s.tbest));
             have = false;
         }
@@ -402,12 +417,16 @@ int mrt_cuda_batch_trace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, const 
     const int stack = batch_stack(ctx, b->max_depth);
     if (!stack) return set_error(ctx, MRT_ERANGE, "batch_trace: stack_depth below the batch's BVH depth");
     const bool any = (flags & MRT_TRACE_ANY_HIT) != 0u;
-#define MRT_BT(K, S)                                                                                             \
-    k_batch_trace<K, S><<<blocks, kTraceBlock, dsm, s>>>(b->dev, b->d_roots, b->d_ray_off, b->scenes, rays, n, hits, \
-                                                         ctx->d_prim_fetch, ctx->d_status)
-    if (stack == 16) { if (any) MRT_BT(true, 16); else MRT_BT(false, 16); }
-    else if (stack == 32) { if (any) MRT_BT(true, 32); else MRT_BT(false, 32); }
-    else { if (any) MRT_BT(true, 24); else MRT_BT(false, 24); }
+    const bool spread = ((ctx->tuning.tri_spread >> (any ? 1u : 0u)) & 1u) != 0u;
+#define MRT_BT(K, S, P)                                                                                   \
+    k_batch_trace<K, S, P><<<blocks, kTraceBlock, dsm, s>>>(b->dev, b->d_roots, b->d_ray_off, b->scenes, rays, \
+                                                            n, hits, ctx->d_prim_fetch, ctx->d_status)
+#define MRT_BT2(K, S) \
+    do { if (spread) MRT_BT(K, S, true); else MRT_BT(K, S, false); } while (0)
+    if (stack == 16) { if (any) MRT_BT2(true, 16); else MRT_BT2(false, 16); }
+    else if (stack == 32) { if (any) MRT_BT2(true, 32); else MRT_BT2(false, 32); }
+    else { if (any) MRT_BT2(true, 24); else MRT_BT2(false, 24); }
+#undef MRT_BT2
 #undef MRT_BT
     if (cudaGetLastError() != cudaSuccess) return set_error(ctx, MRT_ECUDA, "batch_trace: launch failed");
     ctx->launches++;
@@ -452,21 +471,20 @@ int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, co
     const int stack = batch_stack(ctx, b->max_depth);
     if (!stack) return set_error(ctx, MRT_ERANGE, "batch_pathtrace: stack_depth below the batch's BVH depth");
     const uint32_t bounces = params->max_bounces;
+    const bool spread = (ctx->tuning.tri_spread & 1u) != 0u;
     const int sblocks = int(std::min<size_t>((n + kShadeBlock - 1) / kShadeBlock, 8192));
     auto enqueue = [&](cudaStream_t st) -> bool {
         if (cudaMemsetAsync(b->counters, 0, kCntSlots * sizeof(uint32_t), st) != cudaSuccess) return false;
         k_batch_init<<<sblocks, kShadeBlock, (b->scenes + 1u) * sizeof(uint32_t), st>>>(
             rays, b->d_ray_off, b->scenes, n, b->q[0], b->rng, radiance, b->counters, b->d_frame);
         for (uint32_t v = 0; v <= bounces; ++v) {
-            if (stack == 16)
-                k_batch_trace_queue<16><<<blocks, kTraceBlock, 0, st>>>(b->dev, b->d_roots, b->q[v & 1u], b->hits,
-                                                                        b->counters, v, ctx->d_status);
-            else if (stack == 32)
-                k_batch_trace_queue<32><<<blocks, kTraceBlock, 0, st>>>(b->dev, b->d_roots, b->q[v & 1u], b->hits,
-                                                                        b->counters, v, ctx->d_status);
-            else
-                k_batch_trace_queue<24><<<blocks, kTraceBlock, 0, st>>>(b->dev, b->d_roots, b->q[v & 1u], b->hits,
-                                                                        b->counters, v, ctx->d_status);
+#define MRT_BQ(S, P)                                                                                       \
+    k_batch_trace_queue<S, P><<<blocks, kTraceBlock, 0, st>>>(b->dev, b->d_roots, b->q[v & 1u], b->hits, \
+                                                              b->counters, v, ctx->d_status)
+            if (stack == 16) { if (spread) MRT_BQ(16, true); else MRT_BQ(16, false); }
+            else if (stack == 32) { if (spread) MRT_BQ(32, true); else MRT_BQ(32, false); }
+            else { if (spread) MRT_BQ(24, true); else MRT_BQ(24, false); }
+#undef MRT_BQ
             k_batch_shade<<<sblocks, kShadeBlock, 0, st>>>(b->dev, b->d_tp, b->q[v & 1u], b->q[(v + 1u) & 1u],
                                                            b->hits, b->rng, radiance, b->counters, v,
                                                            ctx->d_status);
@@ -481,7 +499,8 @@ int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, co
         return MRT_OK;
     }
     const bool same = b->exec && b->g_rays == rays && b->g_radiance == radiance && b->g_n == n &&
-                      b->g_bounces == bounces && b->g_blocks == uint32_t(blocks) && b->g_stack == stack;
+                      b->g_bounces == bounces && b->g_blocks == uint32_t(blocks) && b->g_stack == stack &&
+                      b->g_spread == spread;
     if (!same) {
         if (b->exec) cudaGraphExecDestroy(b->exec);
         b->exec = nullptr;
@@ -509,6 +528,7 @@ int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, co
         b->g_bounces = bounces;
         b->g_blocks = uint32_t(blocks);
         b->g_stack = stack;
+        b->g_spread = spread;
     }
     if (cudaGraphLaunch(b->exec, s) != cudaSuccess) return set_error(ctx, MRT_ECUDA, "batch_pathtrace: graph launch");
     ctx->launches += 2 + 2 * (bounces + 1);

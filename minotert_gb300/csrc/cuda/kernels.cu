@@ -71,23 +71,42 @@ MRT_DEV bool tile_pixel(uint32_t w, uint32_t h, uint32_t& x, uint32_t& y) {
     return x < w && y < h;
 }
 
-template <bool kCount>
+// kSpread: the warp steps its 32 rays together with the triangle tests of
+// each step spread over its lanes (trav_step_spread).
+template <bool kCount, bool kSpread = false>
 __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
 k_primary_tri(DevScene sc, FrameParams fp, mrt_gbuffer g, uint32_t* status, unsigned long long* totals) {
     __shared__ uint2 stk[kStackDepth * kTraceBlock];
+    __shared__ unsigned long long slots[kSpread ? kTraceBlock : 1];
     uint32_t x, y;
-    if (!tile_pixel(fp.width, fp.height, x, y)) return;
-    f3 o, d;
-    primary_ray(fp, x, y, o, d);
+    const bool inside = tile_pixel(fp.width, fp.height, x, y);
+    if (!kSpread && !inside) return;
+    if (kSpread && !__any_sync(0xFFFFFFFFu, inside)) return;  // warp-uniform
+    f3 o{0.0f, 0.0f, 0.0f}, d{0.0f, 0.0f, 1.0f};
+    if (inside) primary_ray(fp, x, y, o, d);
     uint32_t prim, st = 0u, cn = 0u, ct = 0u;
     float t;
-    trace_bvh8<false, kCount, kStackDepth>(sc, o, d, 0.0f, INFINITY, prim, t, stk + threadIdx.x, kTraceBlock,
-                                           st, cn, ct);
-    if (st) atomicOr(status, st);
+    if (kSpread) {
+        Trav s{};
+        trav_init(s, o, d, 0.0f, INFINITY);
+        bool have = inside;
+        while (__any_sync(0xFFFFFFFFu, have)) {
+            if (trav_step_spread<false, kStackDepth>(sc, s, have, stk + threadIdx.x, kTraceBlock, st,
+                                                     slots + (threadIdx.x & ~31u)))
+                have = false;
+        }
+        prim = s.best;
+        t = prim == kMiss ? s.tmax : s.tbest;
+    } else {
+        trace_bvh8<false, kCount, kStackDepth>(sc, o, d, 0.0f, INFINITY, prim, t, stk + threadIdx.x, kTraceBlock,
+                                               st, cn, ct);
+    }
+    if (st) atomicOr(status, st);  // (a lane outside the image may have tested another lane's triangle)
     if (kCount) {
         atomicAdd(totals + kTotNodesPrim, (unsigned long long)cn);
         atomicAdd(totals + kTotTrisPrim, (unsigned long long)ct);
     }
+    if (!inside) return;
     const size_t pi = size_t(y) * fp.width + x;
     g.visibility[pi] = prim;
     if (g.hit_t) g.hit_t[pi] = t;
@@ -458,17 +477,18 @@ MRT_DEV uint32_t warp_refill(uint32_t* fetch, uint32_t n, bool need, bool& exhau
 // Persistent closest-hit over the extension queue of bounce `bounce`.
 // kDyn: idle lanes refill after every traversal step; otherwise each warp
 // fetches 32 rays and runs them all to completion.
-template <bool kCount, bool kDyn>
+template <bool kCount, bool kDyn, bool kSpread = false>
 __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
 k_trace_ext(DevScene sc, WaveBuffers wb, uint32_t bounce, uint32_t* status) {
     __shared__ uint2 stk[kStackDepth * kTraceBlock];
+    __shared__ unsigned long long slots[kSpread ? kTraceBlock : 1];
     const uint32_t n = wb.counters[kCntExt + bounce];
     const PathRay* q = ext_queue(wb, bounce);
     uint32_t* fetch = wb.counters + kCntFetchExt + bounce;
     uint2* my = stk + threadIdx.x;
     uint32_t st = 0u, cn = 0u, ct = 0u;
     if (kDyn) {
-        Trav s;
+        Trav s{};
         bool have = false, exhausted = false;
         uint32_t ri = 0u;
         while (true) {
@@ -480,7 +500,13 @@ k_trace_ext(DevScene sc, WaveBuffers wb, uint32_t bounce, uint32_t* status) {
                 have = true;
             }
             if (!__any_sync(0xFFFFFFFFu, have)) break;
-            if (have && trav_step<false, kCount, kStackDepth>(sc, s, my, kTraceBlock, st, cn, ct)) {
+            bool fin;
+            if (kSpread)
+                fin = trav_step_spread<false, kStackDepth>(sc, s, have, my, kTraceBlock, st,
+                                                           slots + (threadIdx.x & ~31u));
+            else
+                fin = have && trav_step<false, kCount, kStackDepth>(sc, s, my, kTraceBlock, st, cn, ct);
+            if (have && fin) {
                 wb.hits[ri] = make_uint2(s.best, __float_as_uint(s.best == kMiss ? s.tmax : s.tbest));
                 have = false;
             }
@@ -493,7 +519,21 @@ k_trace_ext(DevScene sc, WaveBuffers wb, uint32_t bounce, uint32_t* status) {
             base = __shfl_sync(0xFFFFFFFFu, base, 0);
             if (base >= n) break;
             const uint32_t i = base + lane;
-            if (i < n) {
+            if (kSpread) {  // the warp steps its rays together; finished lanes keep testing triangles
+                Trav s{};
+                bool have = i < n;
+                if (have) {
+                    const float4 a = q[i].o_pix, b = q[i].d;
+                    trav_init(s, f3{a.x, a.y, a.z}, f3{b.x, b.y, b.z}, 0.0f, INFINITY);
+                }
+                while (__any_sync(0xFFFFFFFFu, have)) {
+                    if (trav_step_spread<false, kStackDepth>(sc, s, have, my, kTraceBlock, st,
+                                                             slots + (threadIdx.x & ~31u))) {
+                        wb.hits[i] = make_uint2(s.best, __float_as_uint(s.best == kMiss ? s.tmax : s.tbest));
+                        have = false;
+                    }
+                }
+            } else if (i < n) {
                 const float4 a = q[i].o_pix, b = q[i].d;
                 uint32_t prim;
                 float t;
@@ -512,17 +552,18 @@ k_trace_ext(DevScene sc, WaveBuffers wb, uint32_t bounce, uint32_t* status) {
 
 // Persistent any-hit over the shadow queue of vertex `vertex`; unoccluded
 // rays add their contribution to the pixel's radiance.
-template <bool kCount, bool kDyn>
+template <bool kCount, bool kDyn, bool kSpread = false>
 __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
 k_trace_shadow(DevScene sc, WaveBuffers wb, TraceParams tp, uint32_t vertex, uint32_t* status) {
     __shared__ uint2 stk[kStackDepth * kTraceBlock];
+    __shared__ unsigned long long slots[kSpread ? kTraceBlock : 1];
     const uint32_t n = wb.counters[kCntShadow + vertex];
     uint32_t* fetch = wb.counters + kCntFetchShadow + vertex;
     const f3 sun{tp.sun[0], tp.sun[1], tp.sun[2]};
     uint2* my = stk + threadIdx.x;
     uint32_t st = 0u, cn = 0u, ct = 0u;
     if (kDyn) {
-        Trav s;
+        Trav s{};
         bool have = false, exhausted = false;
         uint32_t ri = 0u;
         while (true) {
@@ -534,7 +575,13 @@ k_trace_shadow(DevScene sc, WaveBuffers wb, TraceParams tp, uint32_t vertex, uin
                 have = true;
             }
             if (!__any_sync(0xFFFFFFFFu, have)) break;
-            if (have && trav_step<true, kCount, kStackDepth>(sc, s, my, kTraceBlock, st, cn, ct)) {
+            bool fin;
+            if (kSpread)
+                fin = trav_step_spread<true, kStackDepth>(sc, s, have, my, kTraceBlock, st,
+                                                          slots + (threadIdx.x & ~31u));
+            else
+                fin = have && trav_step<true, kCount, kStackDepth>(sc, s, my, kTraceBlock, st, cn, ct);
+            if (have && fin) {
                 if (s.best == kMiss) {
                     const ShadowRay sr = wb.sq[ri];
                     add_L(wb.L, __float_as_uint(sr.o_pix.w), f3{sr.contrib.x, sr.contrib.y, sr.contrib.z});
@@ -550,7 +597,24 @@ k_trace_shadow(DevScene sc, WaveBuffers wb, TraceParams tp, uint32_t vertex, uin
             base = __shfl_sync(0xFFFFFFFFu, base, 0);
             if (base >= n) break;
             const uint32_t i = base + lane;
-            if (i < n) {
+            if (kSpread) {  // the warp steps its rays together; finished lanes keep testing triangles
+                Trav s{};
+                bool have = i < n;
+                if (have) {
+                    const float4 a = wb.sq[i].o_pix;
+                    trav_init(s, f3{a.x, a.y, a.z}, sun, 0.0f, INFINITY);
+                }
+                while (__any_sync(0xFFFFFFFFu, have)) {
+                    if (trav_step_spread<true, kStackDepth>(sc, s, have, my, kTraceBlock, st,
+                                                            slots + (threadIdx.x & ~31u))) {
+                        if (s.best == kMiss) {
+                            const ShadowRay sr = wb.sq[i];
+                            add_L(wb.L, __float_as_uint(sr.o_pix.w), f3{sr.contrib.x, sr.contrib.y, sr.contrib.z});
+                        }
+                        have = false;
+                    }
+                }
+            } else if (i < n) {
                 const ShadowRay sr = wb.sq[i];
                 uint32_t prim;
                 float t;
@@ -696,7 +760,7 @@ k_trace_rays_sphere(DevScene sc, const mrt_ray* rays, uint32_t n, mrt_hit* hits)
 // ------------------------------------------------------------------ launchers
 
 cudaError_t launch_primary_tri(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g, uint32_t* status,
-                               unsigned long long* totals, uint32_t* fetch, int blocks, cudaStream_t s) {
+                               unsigned long long* totals, uint32_t* fetch, int blocks, bool spread, cudaStream_t s) {
     if (fetch) {
         cudaError_t e = cudaMemsetAsync(fetch, 0, sizeof(uint32_t), s);
         if (e != cudaSuccess) return e;
@@ -706,6 +770,7 @@ cudaError_t launch_primary_tri(const DevScene& sc, const FrameParams& fp, const 
     }
     dim3 grid((fp.width + 15) / 16, (fp.height + 7) / 8);
     if (totals) k_primary_tri<true><<<grid, kTraceBlock, 0, s>>>(sc, fp, g, status, totals);
+    else if (spread) k_primary_tri<false, true><<<grid, kTraceBlock, 0, s>>>(sc, fp, g, status, nullptr);
     else k_primary_tri<false><<<grid, kTraceBlock, 0, s>>>(sc, fp, g, status, nullptr);
     return cudaGetLastError();
 }
@@ -754,12 +819,17 @@ cudaError_t launch_shade_primary(const DevScene& sc, const FrameParams& fp, cons
 }
 
 cudaError_t launch_trace_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t bounce, int blocks, uint32_t* status,
-                             bool count, bool dyn, cudaStream_t s) {
-    if (count) {
-        if (dyn) k_trace_ext<true, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
+                             bool count, int mode, cudaStream_t s) {
+    if (count) {  // the counting kernels test each lane's own triangles
+        if (mode == kFetchDynamic || mode == kFetchSpread)
+            k_trace_ext<true, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
         else k_trace_ext<true, false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
+    } else if (mode == kFetchSpread) {
+        k_trace_ext<false, true, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
+    } else if (mode == kFetchBatchSpread) {
+        k_trace_ext<false, false, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
     } else {
-        if (dyn) k_trace_ext<false, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
+        if (mode == kFetchDynamic) k_trace_ext<false, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
         else k_trace_ext<false, false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
     }
     return cudaGetLastError();
@@ -772,12 +842,17 @@ cudaError_t launch_tail(const DevScene& sc, const TraceParams& tp, BlueNoise bn,
 }
 
 cudaError_t launch_trace_shadow(const DevScene& sc, const WaveBuffers& wb, const TraceParams& tp, uint32_t vertex,
-                                int blocks, uint32_t* status, bool count, bool dyn, cudaStream_t s) {
-    if (count) {
-        if (dyn) k_trace_shadow<true, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
+                                int blocks, uint32_t* status, bool count, int mode, cudaStream_t s) {
+    if (count) {  // the counting kernels test each lane's own triangles
+        if (mode == kFetchDynamic || mode == kFetchSpread)
+            k_trace_shadow<true, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
         else k_trace_shadow<true, false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
+    } else if (mode == kFetchSpread) {
+        k_trace_shadow<false, true, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
+    } else if (mode == kFetchBatchSpread) {
+        k_trace_shadow<false, false, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
     } else {
-        if (dyn) k_trace_shadow<false, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
+        if (mode == kFetchDynamic) k_trace_shadow<false, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
         else k_trace_shadow<false, false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
     }
     return cudaGetLastError();

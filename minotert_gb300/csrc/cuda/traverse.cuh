@@ -291,6 +291,122 @@ MRT_DEV bool trav_step(const DevScene& sc, Trav& s, uint2* stk, uint32_t stride,
     return s.g_hits == 0u && s.sp == 0;
 }
 
+// Unsigned key with the order of the floats (any non-NaN value).
+MRT_DEV uint32_t float_key(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return u ^ ((u >> 31) ? 0xFFFFFFFFu : 0x80000000u);
+}
+MRT_DEV float key_float(uint32_t k) { return __uint_as_float(k ^ ((k >> 31) ? 0x80000000u : 0xFFFFFFFFu)); }
+
+// trav_step with the triangle tests of the step spread over the warp.  In
+// the per-lane loop a step tests a leaf's triangles one per pass, and the
+// warp runs as many passes as its busiest lane needs while the other lanes
+// idle.  Here all 32 lanes call the step (`have` marks those holding a
+// ray); each visits its next node as trav_step does, then the n_i triangles
+// of lane i's hit leaves (T in all) become T (ray, triangle) pairs tested 32
+// per pass: pair p goes to lane p mod 32, which finds the ray's owner by a
+// binary search over the exclusive prefix sum of n_i and reads the owner's
+// sheared ray with shuffles.  Hits meet in the owner's 64-bit shared slot
+// (`slot`, 32 per warp) by atomicMin: (ordered t, id) for closest hit,
+// which is test_tri's order-independent rule, so the result is identical;
+// (leaf bit + 1, t) for any hit, which keeps the hit the per-lane loop
+// would have met first.  Key 0 marks a triangle index out of range (no real key
+// is 0), which ends the ray as test_tri does.  Returns true for a lane
+// whose ray is finished.  Counting kernels keep the per-lane loop, whose
+// per-ray counts are the oracle's.
+template <bool kAnyHit, int kStack>
+MRT_DEV bool trav_step_spread(const DevScene& sc, Trav& s, bool have, uint2* stk, uint32_t stride,
+                              uint32_t& status, unsigned long long* slot) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t tri_mask = 0u, tri_base = 0u;
+    bool done = false;
+    if (have) {
+        uint32_t node;
+        if (next_node<kStack>(sc, s, stk, stride, status, node)) tri_mask = visit_node(sc, s, node, tri_base);
+        else done = true;
+    }
+    const uint32_t cnt = __popc(tri_mask);
+    uint32_t incl = cnt;
+#pragma unroll
+    for (uint32_t o = 1; o < 32u; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    if (total) {
+        const uint32_t excl = incl - cnt;
+        if (cnt)
+            slot[lane] = kAnyHit ? ~0ull
+                                 : ((unsigned long long)float_key(s.tbest) << 32) | (unsigned long long)s.best;
+        __syncwarp();
+        const uint32_t kpack = uint32_t(s.r.kx) | (uint32_t(s.r.ky) << 2) | (uint32_t(s.r.kz) << 4);
+        for (uint32_t c = 0; c < total; c += 32u) {
+            const uint32_t p = c + lane;
+            uint32_t own = 0u;  // the last lane whose exclusive sum is <= p
+#pragma unroll
+            for (uint32_t step = 16u; step >= 1u; step >>= 1) {
+                const uint32_t e = __shfl_sync(0xFFFFFFFFu, excl, int(own + step));
+                if (e <= p) own += step;
+            }
+            RayPre r;
+            r.okx = __shfl_sync(0xFFFFFFFFu, s.r.okx, int(own));
+            r.oky = __shfl_sync(0xFFFFFFFFu, s.r.oky, int(own));
+            r.okz = __shfl_sync(0xFFFFFFFFu, s.r.okz, int(own));
+            r.sx = __shfl_sync(0xFFFFFFFFu, s.r.sx, int(own));
+            r.sy = __shfl_sync(0xFFFFFFFFu, s.r.sy, int(own));
+            r.sz = __shfl_sync(0xFFFFFFFFu, s.r.sz, int(own));
+            const uint32_t kp = __shfl_sync(0xFFFFFFFFu, kpack, int(own));
+            r.kx = int(kp & 3u);
+            r.ky = int((kp >> 2) & 3u);
+            r.kz = int(kp >> 4);
+            const float tmin = __shfl_sync(0xFFFFFFFFu, s.tmin, int(own));
+            const float tmax = kAnyHit ? __shfl_sync(0xFFFFFFFFu, s.tmax, int(own)) : 0.0f;
+            const uint32_t m = __shfl_sync(0xFFFFFFFFu, tri_mask, int(own));
+            const uint32_t base = __shfl_sync(0xFFFFFFFFu, tri_base, int(own));
+            const uint32_t e0 = __shfl_sync(0xFFFFFFFFu, excl, int(own));
+            if (p < total) {
+                const uint32_t bit = __fns(m, 0u, int(p - e0) + 1);
+                const uint32_t ti = base + bit;
+                if (ti >= sc.tri_count) {
+                    status |= MRT_STATUS_BAD_TRI;
+                    atomicMin(slot + own, 0ull);
+                } else {
+                    const float4* tp = sc.tris + size_t(ti) * 3u;
+                    const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), cc = __ldg(tp + 2);
+                    float t;
+                    if (intersect_tri(r, a, b, cc, tmin, t)) {
+                        if (kAnyHit) {
+                            if (t < tmax)
+                                atomicMin(slot + own, ((unsigned long long)(bit + 1u) << 32) | __float_as_uint(t));
+                        } else {
+                            atomicMin(slot + own, ((unsigned long long)float_key(t) << 32) |
+                                                      (unsigned long long)__float_as_uint(a.w));
+                        }
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if (cnt) {
+            const unsigned long long k = slot[lane];
+            if (k == 0ull) {
+                done = true;
+            } else if (kAnyHit) {
+                if (k != ~0ull) {
+                    s.tbest = __uint_as_float(uint32_t(k));
+                    s.best = __float_as_uint(__ldg(sc.tris + size_t(tri_base + uint32_t(k >> 32) - 1u) * 3u).w);
+                    done = true;
+                }
+            } else {
+                s.tbest = key_float(uint32_t(k >> 32));
+                s.best = uint32_t(k);
+            }
+        }
+    }
+    if (have && !done) done = s.g_hits == 0u && s.sp == 0;
+    return done;
+}
+
 // Closest hit (kAnyHit = false) or first hit with t < tmax (kAnyHit = true)
 // of one ray, run to completion.
 template <bool kAnyHit, bool kCount, int kStack>

@@ -320,18 +320,20 @@ def test_errors_are_codes_not_crashes(ctx, hf_scene):
     assert rc != 0
 
 
-@pytest.mark.parametrize("dyn,prim,blocks", [(0, 0, 0), (1, 1, 0), (1, 0, 2), (0, 1, 1)])
-def test_schedule_variants_are_bit_identical(ctx, hf_workload, hf_scene, blue_noise, dyn, prim, blocks):
-    # the launch schedule (fetch mode, persistent primary, blocks per SM)
-    # changes which thread traces a ray, never the result
+@pytest.mark.parametrize("dyn,prim,blocks,spread", [(0, 0, 0, 0), (1, 1, 0, 0), (1, 0, 2, 0), (0, 1, 1, 0),
+                                                     (3, 0, 0, 7), (1, 0, 3, 7), (0, 0, 0, 3)])
+def test_schedule_variants_are_bit_identical(ctx, hf_workload, hf_scene, blue_noise, dyn, prim, blocks, spread):
+    # the launch schedule (fetch mode, persistent primary, blocks per SM,
+    # triangle tests spread over the warp) changes which thread traces a
+    # ray, never the result
     wl, mesh, bvh = hf_workload
     saved = ctx.tuning()
     try:
-        ctx.set_tuning(dynamic_fetch=dyn, primary_persistent=prim, trace_blocks_per_sm=blocks)
+        ctx.set_tuning(dynamic_fetch=dyn, primary_persistent=prim, trace_blocks_per_sm=blocks, tri_spread=spread)
         img, g = _pathtrace_gpu(ctx, wl, hf_scene, blue_noise, frame=2)
     finally:
         lib().mrt_cuda_set_tuning(ctx.handle, saved)
-    ctx.set_tuning(dynamic_fetch=1, primary_persistent=1, trace_blocks_per_sm=0)
+    ctx.set_tuning(dynamic_fetch=1, primary_persistent=1, trace_blocks_per_sm=0, tri_spread=0)
     ref_img, ref_g = _pathtrace_gpu(ctx, wl, hf_scene, blue_noise, frame=2)
     lib().mrt_cuda_set_tuning(ctx.handle, saved)
     assert np.array_equal(g["visibility"], ref_g["visibility"])

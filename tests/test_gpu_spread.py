@@ -1,0 +1,77 @@
+"""Triangle tests spread over the warp (mrt_tuning.tri_spread): the primary,
+extension and shadow kernels that test a step's triangles as (ray, triangle)
+pairs across all 32 lanes, with either work schedule, give the per-lane
+loop's hits, image and ray counts, bit for bit, through the C ABI."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import oracle_consts
+from minotert_gb300.pathtracer import Camera, Pathtracer, TraceSettings
+from minotert_gb300.scene import DeviceScene
+
+pytestmark = pytest.mark.gpu
+
+
+def _render(ctx, ds, wl, bn, settings, spread, tail, dyn=3):
+    saved = ctx.tuning()
+    ctx.set_tuning(tri_spread=spread, tail_bounce=tail, dynamic_fetch=dyn)
+    try:
+        pt = Pathtracer(ctx, ds, full_gbuffer=False)
+        pt.frame_counter = 5
+        gb = pt.primaryRays((wl.width, wl.height), wl.camera, wl.camera)
+        ctx.frame_stats()  # reset
+        col = pt.secondaryRays(gb, wl.camera, wl.sky, bn, settings)
+        img = col.download(np.float32, (wl.height, wl.width, 3))
+        st = ctx.frame_stats()
+    finally:
+        ctx.set_tuning(**{f: getattr(saved, f) for f, _ in saved._fields_})
+    return img, list(st.extension_rays), int(st.shadow_rays)
+
+
+@pytest.mark.parametrize("settings", [TraceSettings(samples=1, bounces=4, rr_start=2, rng_mode=1),
+                                      TraceSettings(samples=2, bounces=6, rr_start=0, rng_mode=0)])
+def test_spread_matches_per_lane(ctx, hf_workload, blue_noise, settings):
+    wl, mesh, bvh = hf_workload
+    ds = DeviceScene.triangles(ctx, mesh, bvh)
+    ref, ext, shadow = _render(ctx, ds, wl, blue_noise, settings, 0, 0)
+    assert ext[0] > 0 and shadow > 0 and np.isfinite(ref).all()
+    for spread in (1, 2, 3):
+        for dyn in (3, 0):
+            img, e, sh = _render(ctx, ds, wl, blue_noise, settings, spread, 0, dyn)
+            assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), (spread, dyn)
+            assert e == ext and sh == shadow, (spread, dyn)
+    # with the path tail finishing bounces >= 2
+    img, e, sh = _render(ctx, ds, wl, blue_noise, settings, 3, 2)
+    assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+    assert e == ext and sh == shadow
+    assert ctx.status() == 0
+
+
+def test_spread_range(ctx):
+    from minotert_gb300._lib import MrtError
+    saved = int(ctx.tuning().tri_spread)
+    with pytest.raises(MrtError):
+        ctx.set_tuning(tri_spread=8)
+    ctx.set_tuning(tri_spread=saved)
+
+
+@pytest.mark.parametrize("size", [(256, 256), (77, 45), (31, 3)])
+def test_spread_primary_matches_oracle(ctx, hf_workload, size):
+    # one thread per pixel, warps stepping together; odd sizes leave lanes
+    # outside the image that still test other lanes' triangles
+    wl, mesh, bvh = hf_workload
+    ds = DeviceScene.triangles(ctx, mesh, bvh)
+    c = wl.camera
+    cam = Camera(viewport=size, verticalFov=c.verticalFov, nearPlane=c.nearPlane, position=c.position, yaw=c.yaw,
+                 pitch=c.pitch)
+    saved = ctx.tuning()
+    try:
+        ctx.set_tuning(tri_spread=4, primary_persistent=0)
+        g = Pathtracer(ctx, ds, full_gbuffer=False).primaryRays(size, cam, cam).download()
+    finally:
+        ctx.set_tuning(**{f: getattr(saved, f) for f, _ in saved._fields_})
+    ref = oracle.primary(oracle_consts(cam), size[0], size[1], bvh.nodes, bvh.tris, mesh.mats)
+    assert np.array_equal(g["visibility"], ref["visibility"])
+    assert np.array_equal(g["hit_t"].view(np.uint32), ref["hit_t"].view(np.uint32))
+    assert ctx.status() == 0
