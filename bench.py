@@ -367,11 +367,12 @@ def run_batched(args, world, rank, local, dist):
         batch.pathtrace(d_rays, offsets, params, frame[0], d_rad, use_graph=graph, stream=st)
 
     # schedule sweep: persistent blocks per SM x traversal stack entries x
-    # triangle tests spread over the warp
+    # triangle tests spread over the warp x idle lanes before a refill
     tune = autotune.autotune(ctx, step, stream, key=wl.name, frames=3, warmup=1, cache=None,
                              space=[{"trace_blocks_per_sm": b, "dynamic_fetch": 1, "primary_persistent": 0,
-                                     "sort_min_rays": autotune.SORT_NEVER, "stack_depth": sd, "tri_spread": sp}
-                                    for b in (4, 6, 8) for sd in (16, 24, 32) for sp in (1, 0)])
+                                     "sort_min_rays": autotune.SORT_NEVER, "stack_depth": sd, "tri_spread": sp,
+                                     "refill_min": rm}
+                                    for b in (4, 6, 8) for sd in (16, 24, 32) for sp in (1, 0) for rm in (8, 1)])
     for _ in range(args.warmup):
         step(stream)
     ctx.sync(stream)

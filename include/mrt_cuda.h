@@ -270,6 +270,11 @@ typedef struct mrt_tuning {
                                      spread over the warp's lanes instead of
                                      each lane testing its own leaves' (same
                                      hits)                                   */
+    uint32_t refill_min;          /* extension rays with dynamic fetch and
+                                     the batched kernels: a warp fetches new
+                                     rays once at least this many of its
+                                     lanes are idle (or all are); 0 or 1 =
+                                     whenever one is (up to 32)              */
 } mrt_tuning;
 int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning);
 int mrt_cuda_get_tuning(mrt_ctx* ctx, mrt_tuning* tuning);

@@ -2,8 +2,8 @@
 
 Sweeps persistent blocks per SM (warps per SM = 4 x blocks), the work-fetch
 mode of the persistent kernels, the primary-ray kernel form, the ray-sort
-threshold, the path tail and the spreading of triangle tests over the warp
-on a caller-supplied frame function, timing each
+threshold, the path tail, the spreading of triangle tests over the warp and
+the refill threshold on a caller-supplied frame function, timing each
 candidate with CUDA events on the frame's stream, and keeps the fastest.
 Results are cached as JSON keyed by GPU and workload, so a renderer pays
 for the sweep once.
@@ -33,9 +33,11 @@ def candidates(max_blocks_per_sm: int, sort: bool = False):
     # tail_bounce: 0 = wavefront passes for every bounce, 3 = one persistent
     # launch finishes the paths alive at bounce 3
     # tri_spread bit 0: the extension rays' triangle tests spread over the warp
-    for b, dyn, prim, thr, tail, spread in itertools.product(blocks, (1, 3, 0, 2), (0, 1), sort_thr, (3, 0), (1, 0)):
+    # refill_min: idle lanes a warp waits for before fetching new rays
+    for b, dyn, prim, thr, tail, spread, rmin in itertools.product(blocks, (1, 3, 0, 2), (0, 1), sort_thr, (3, 0),
+                                                                   (1, 0), (8, 1)):
         yield {"trace_blocks_per_sm": b, "dynamic_fetch": dyn, "primary_persistent": prim, "sort_min_rays": thr,
-               "tail_bounce": tail, "tri_spread": spread}
+               "tail_bounce": tail, "tri_spread": spread, "refill_min": rmin}
 
 
 def time_frames(ctx: Context, run_frame, stream, frames: int, warmup: int) -> float:

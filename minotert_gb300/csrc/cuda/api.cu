@@ -295,10 +295,12 @@ static int fetch_mode(const mrt_ctx* ctx, uint32_t which) {
     return spread ? mrt::kFetchSpread : mrt::kFetchDynamic;
 }
 
+static uint32_t refill_min(const mrt_ctx* ctx) { return ctx->tuning.refill_min ? ctx->tuning.refill_min : 1u; }
+
 int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning) {
     if (!ctx || !tuning) return fail(ctx, MRT_EINVAL, "set_tuning: null argument");
     if (tuning->trace_blocks_per_sm > 64 || tuning->dynamic_fetch > 3 || tuning->primary_persistent > 1 ||
-        tuning->tail_bounce > MRT_MAX_BOUNCES || tuning->tri_spread > 7 ||
+        tuning->tail_bounce > MRT_MAX_BOUNCES || tuning->tri_spread > 7 || tuning->refill_min > 32 ||
         (tuning->stack_depth != 0u && tuning->stack_depth != 16u && tuning->stack_depth != 24u &&
          tuning->stack_depth != 32u))
         return fail(ctx, MRT_EINVAL, "set_tuning: value out of range");
@@ -692,7 +694,8 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
                                                       params->sort_rays ? 0u : ctx->tuning.sort_min_rays, s));
                 ctx->launches += 2;  // histogram, scan, scatter
             }
-            MRT_LAUNCH(1, int(b), launch_trace_ext(scene->dev, wb, b, tblocks, ctx->d_status, ctx->counters, dyn, s));
+            MRT_LAUNCH(1, int(b), launch_trace_ext(scene->dev, wb, b, tblocks, ctx->d_status, ctx->counters, dyn,
+                                                   refill_min(ctx), s));
             MRT_LAUNCH(3, int(b), launch_shade(scene->dev, tp, bn, wb, W, b, ctx->d_status, s));
         }
         if (nee && !tail_done)
@@ -766,7 +769,8 @@ int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
         MRT_LAUNCH(3, 0, launch_shade_primary(scene->dev, fp, *gbuffer, tp, bn, wb, 0, ctx->d_status, s));
         if (nee)
             MRT_LAUNCH(2, 0, launch_trace_shadow(scene->dev, wb, tp, 0, tblocks, ctx->d_status, ctx->counters, dyn_sh, s));
-        MRT_LAUNCH(1, 1, launch_trace_ext(scene->dev, wb, 1, tblocks, ctx->d_status, ctx->counters, dyn, s));
+        MRT_LAUNCH(1, 1, launch_trace_ext(scene->dev, wb, 1, tblocks, ctx->d_status, ctx->counters, dyn,
+                                          refill_min(ctx), s));
         MRT_LAUNCH(3, 1, launch_shade(scene->dev, tp, bn, wb, W, 1, ctx->d_status, s));
         if (nee)
             MRT_LAUNCH(2, 1, launch_trace_shadow(scene->dev, wb, tp, 1, tblocks, ctx->d_status, ctx->counters, dyn_sh, s));

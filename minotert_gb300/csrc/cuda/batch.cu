@@ -61,6 +61,7 @@ struct mrt_batch {
     uint32_t g_n = 0, g_bounces = 0, g_blocks = 0, g_dyn = 0;
     int g_stack = 0;
     bool g_spread = false;
+    uint32_t g_refill = 0;
 };
 
 namespace {
@@ -76,10 +77,13 @@ MRT_DEV uint32_t scene_of(const uint32_t* off, uint32_t scenes, uint32_t i) {
     return lo;
 }
 
-__device__ __forceinline__ uint32_t refill(uint32_t* fetch, uint32_t n, bool need, bool& exhausted) {
+// As warp_refill (kernels.cu), with the same min_idle rule.
+__device__ __forceinline__ uint32_t refill(uint32_t* fetch, uint32_t n, bool need, bool& exhausted,
+                                           uint32_t min_idle) {
     if (exhausted) return kMiss;
     const uint32_t mask = __ballot_sync(0xFFFFFFFFu, need);
     if (!mask) return kMiss;
+    if (mask != 0xFFFFFFFFu && uint32_t(__popc(mask)) < min_idle) return kMiss;
     const uint32_t lane = lane_id(), leader = __ffs(mask) - 1u, cnt = __popc(mask);
     uint32_t base = 0u;
     if (lane == leader) base = atomicAdd(fetch, cnt);
@@ -97,7 +101,7 @@ __device__ __forceinline__ uint32_t refill(uint32_t* fetch, uint32_t n, bool nee
 template <bool kAnyHit, int kStack, bool kSpread>
 __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
 k_batch_trace(DevScene sc, const uint32_t* roots, const uint32_t* ray_off, uint32_t scenes, const mrt_ray* rays,
-              uint32_t n, mrt_hit* hits, uint32_t* fetch, uint32_t* status) {
+              uint32_t n, mrt_hit* hits, uint32_t* fetch, uint32_t* status, uint32_t refill_min) {
     __shared__ uint2 stk[kStack * kTraceBlock];
     __shared__ unsigned long long slots[kSpread ? kTraceBlock : 1];
     extern __shared__ uint32_t off[];  // scenes + 1 ray offsets
@@ -108,7 +112,7 @@ k_batch_trace(DevScene sc, const uint32_t* roots, const uint32_t* ray_off, uint3
     Trav s{};
     bool have = false, exhausted = false;
     while (true) {
-        const uint32_t idx = refill(fetch, n, !have, exhausted);
+        const uint32_t idx = refill(fetch, n, !have, exhausted, refill_min);
         if (idx != kMiss) {
             const float4* rp = reinterpret_cast<const float4*>(rays + idx);
             const float4 a = rp[0], b = rp[1];
@@ -161,7 +165,7 @@ k_batch_init(const mrt_ray* rays, const uint32_t* ray_off, uint32_t scenes, uint
 template <int kStack, bool kSpread>
 __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
 k_batch_trace_queue(DevScene sc, const uint32_t* roots, const PathRay* q, uint2* hits, uint32_t* counters,
-                    uint32_t bounce, uint32_t* status) {
+                    uint32_t bounce, uint32_t* status, uint32_t refill_min) {
     __shared__ uint2 stk[kStack * kTraceBlock];
     __shared__ unsigned long long slots[kSpread ? kTraceBlock : 1];
     const uint32_t n = counters[kCntExt + bounce];
@@ -171,7 +175,7 @@ k_batch_trace_queue(DevScene sc, const uint32_t* roots, const PathRay* q, uint2*
     Trav s{};
     bool have = false, exhausted = false;
     while (true) {
-        const uint32_t idx = refill(fetch, n, !have, exhausted);
+        const uint32_t idx = refill(fetch, n, !have, exhausted, refill_min);
         if (idx != kMiss) {
             const PathRay pr = q[idx];
             const float tmax = bounce == 0u ? pr.beta.w : INFINITY;
@@ -418,9 +422,10 @@ int mrt_cuda_batch_trace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, const 
     if (!stack) return set_error(ctx, MRT_ERANGE, "batch_trace: stack_depth below the batch's BVH depth");
     const bool any = (flags & MRT_TRACE_ANY_HIT) != 0u;
     const bool spread = ((ctx->tuning.tri_spread >> (any ? 1u : 0u)) & 1u) != 0u;
+    const uint32_t rmin = ctx->tuning.refill_min ? ctx->tuning.refill_min : 1u;
 #define MRT_BT(K, S, P)                                                                                   \
     k_batch_trace<K, S, P><<<blocks, kTraceBlock, dsm, s>>>(b->dev, b->d_roots, b->d_ray_off, b->scenes, rays, \
-                                                            n, hits, ctx->d_prim_fetch, ctx->d_status)
+                                                            n, hits, ctx->d_prim_fetch, ctx->d_status, rmin)
 #define MRT_BT2(K, S) \
     do { if (spread) MRT_BT(K, S, true); else MRT_BT(K, S, false); } while (0)
     if (stack == 16) { if (any) MRT_BT2(true, 16); else MRT_BT2(false, 16); }
@@ -472,6 +477,7 @@ int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, co
     if (!stack) return set_error(ctx, MRT_ERANGE, "batch_pathtrace: stack_depth below the batch's BVH depth");
     const uint32_t bounces = params->max_bounces;
     const bool spread = (ctx->tuning.tri_spread & 1u) != 0u;
+    const uint32_t rmin = ctx->tuning.refill_min ? ctx->tuning.refill_min : 1u;
     const int sblocks = int(std::min<size_t>((n + kShadeBlock - 1) / kShadeBlock, 8192));
     auto enqueue = [&](cudaStream_t st) -> bool {
         if (cudaMemsetAsync(b->counters, 0, kCntSlots * sizeof(uint32_t), st) != cudaSuccess) return false;
@@ -480,7 +486,7 @@ int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, co
         for (uint32_t v = 0; v <= bounces; ++v) {
 #define MRT_BQ(S, P)                                                                                       \
     k_batch_trace_queue<S, P><<<blocks, kTraceBlock, 0, st>>>(b->dev, b->d_roots, b->q[v & 1u], b->hits, \
-                                                              b->counters, v, ctx->d_status)
+                                                              b->counters, v, ctx->d_status, rmin)
             if (stack == 16) { if (spread) MRT_BQ(16, true); else MRT_BQ(16, false); }
             else if (stack == 32) { if (spread) MRT_BQ(32, true); else MRT_BQ(32, false); }
             else { if (spread) MRT_BQ(24, true); else MRT_BQ(24, false); }
@@ -500,7 +506,7 @@ int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, co
     }
     const bool same = b->exec && b->g_rays == rays && b->g_radiance == radiance && b->g_n == n &&
                       b->g_bounces == bounces && b->g_blocks == uint32_t(blocks) && b->g_stack == stack &&
-                      b->g_spread == spread;
+                      b->g_spread == spread && b->g_refill == rmin;
     if (!same) {
         if (b->exec) cudaGraphExecDestroy(b->exec);
         b->exec = nullptr;
@@ -529,6 +535,7 @@ int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, co
         b->g_blocks = uint32_t(blocks);
         b->g_stack = stack;
         b->g_spread = spread;
+        b->g_refill = rmin;
     }
     if (cudaGraphLaunch(b->exec, s) != cudaSuccess) return set_error(ctx, MRT_ECUDA, "batch_pathtrace: graph launch");
     ctx->launches += 2 + 2 * (bounces + 1);

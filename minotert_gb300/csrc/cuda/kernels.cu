@@ -121,7 +121,8 @@ k_primary_tri(DevScene sc, FrameParams fp, mrt_gbuffer g, uint32_t* status, unsi
     }
 }
 
-MRT_DEV uint32_t warp_refill(uint32_t* fetch, uint32_t n, bool need, bool& exhausted);
+MRT_DEV uint32_t warp_refill(uint32_t* fetch, uint32_t n, bool need, bool& exhausted,
+                             uint32_t min_idle = 1u);
 
 // Persistent primary rays with per-lane refill.  Ray index i maps to pixel
 // tile i/32 (8x4 pixels, row-major tiles) and lane i%32 inside it, so the
@@ -459,11 +460,14 @@ k_shade(DevScene sc, TraceParams tp, BlueNoise bn, WaveBuffers wb, uint32_t widt
 // lanes that `need` a ray share one atomic on the work counter.  Returns the
 // lane's new ray index or kMiss.  `exhausted` is warp-uniform and stops all
 // further fetches once the counter has passed n, so the counter grows by at
-// most n + 32 per warp.  Must be called by all 32 lanes.
-MRT_DEV uint32_t warp_refill(uint32_t* fetch, uint32_t n, bool need, bool& exhausted) {
+// most n + 32 per warp.  While fewer than `min_idle` lanes need a ray (and
+// not all do) nobody fetches: the warp pays for the fetch and the ray setup
+// once for several lanes.  Must be called by all 32 lanes.
+MRT_DEV uint32_t warp_refill(uint32_t* fetch, uint32_t n, bool need, bool& exhausted, uint32_t min_idle) {
     if (exhausted) return kMiss;
     const uint32_t mask = __ballot_sync(0xFFFFFFFFu, need);
     if (!mask) return kMiss;
+    if (mask != 0xFFFFFFFFu && uint32_t(__popc(mask)) < min_idle) return kMiss;  // wait for more idle lanes
     const uint32_t lane = lane_id(), leader = __ffs(mask) - 1u, cnt = __popc(mask);
     uint32_t base = 0u;
     if (lane == leader) base = atomicAdd(fetch, cnt);
@@ -479,7 +483,7 @@ MRT_DEV uint32_t warp_refill(uint32_t* fetch, uint32_t n, bool need, bool& exhau
 // fetches 32 rays and runs them all to completion.
 template <bool kCount, bool kDyn, bool kSpread = false>
 __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
-k_trace_ext(DevScene sc, WaveBuffers wb, uint32_t bounce, uint32_t* status) {
+k_trace_ext(DevScene sc, WaveBuffers wb, uint32_t bounce, uint32_t* status, uint32_t refill_min) {
     __shared__ uint2 stk[kStackDepth * kTraceBlock];
     __shared__ unsigned long long slots[kSpread ? kTraceBlock : 1];
     const uint32_t n = wb.counters[kCntExt + bounce];
@@ -492,7 +496,7 @@ k_trace_ext(DevScene sc, WaveBuffers wb, uint32_t bounce, uint32_t* status) {
         bool have = false, exhausted = false;
         uint32_t ri = 0u;
         while (true) {
-            const uint32_t idx = warp_refill(fetch, n, !have, exhausted);
+            const uint32_t idx = warp_refill(fetch, n, !have, exhausted, refill_min);
             if (idx != kMiss) {
                 const float4 a = q[idx].o_pix, b = q[idx].d;
                 trav_init(s, f3{a.x, a.y, a.z}, f3{b.x, b.y, b.z}, 0.0f, INFINITY);
@@ -819,18 +823,18 @@ cudaError_t launch_shade_primary(const DevScene& sc, const FrameParams& fp, cons
 }
 
 cudaError_t launch_trace_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t bounce, int blocks, uint32_t* status,
-                             bool count, int mode, cudaStream_t s) {
+                             bool count, int mode, uint32_t refill_min, cudaStream_t s) {
     if (count) {  // the counting kernels test each lane's own triangles
         if (mode == kFetchDynamic || mode == kFetchSpread)
-            k_trace_ext<true, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
-        else k_trace_ext<true, false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
+            k_trace_ext<true, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status, refill_min);
+        else k_trace_ext<true, false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status, refill_min);
     } else if (mode == kFetchSpread) {
-        k_trace_ext<false, true, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
+        k_trace_ext<false, true, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status, refill_min);
     } else if (mode == kFetchBatchSpread) {
-        k_trace_ext<false, false, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
+        k_trace_ext<false, false, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status, refill_min);
     } else {
-        if (mode == kFetchDynamic) k_trace_ext<false, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
-        else k_trace_ext<false, false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status);
+        if (mode == kFetchDynamic) k_trace_ext<false, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status, refill_min);
+        else k_trace_ext<false, false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status, refill_min);
     }
     return cudaGetLastError();
 }

@@ -112,3 +112,35 @@ def test_batch_stack_depths_agree(ctx, small_batch):
             ctx.set_tuning(stack_depth=20)
     finally:
         lib().mrt_cuda_set_tuning(ctx.handle, C.byref(saved))
+
+
+def test_batch_schedules_agree(ctx, small_batch):
+    # per-lane or spread triangle tests, refill whenever one lane is idle or
+    # once 8 / 32 are: same hits (closest and any) and radiance, bit for bit
+    import ctypes as C
+    from minotert_gb300._lib import lib
+    wl, scenes, batch, rays, offsets = small_batch
+    d_rays = ctx.to_device(rays)
+    d_hits = ctx.alloc(8 * len(rays))
+    d_rad = ctx.alloc(12 * len(rays))
+    params = wl.settings.params(wl.sky)
+    saved = ctx.tuning()
+    outs = {}
+    try:
+        for spread, rmin in ((0, 1), (3, 1), (3, 8), (0, 32), (1, 8)):
+            ctx.set_tuning(tri_spread=spread, refill_min=rmin)
+            batch.trace(d_rays, offsets, d_hits)
+            closest = d_hits.download(HIT_DTYPE, (len(rays),)).copy()
+            batch.trace(d_rays, offsets, d_hits, any_hit=True)
+            anyhit = d_hits.download(HIT_DTYPE, (len(rays),)).copy()
+            batch.pathtrace(d_rays, offsets, params, 5, d_rad, use_graph=True)
+            outs[(spread, rmin)] = (closest, anyhit, d_rad.download(np.float32, (len(rays), 3)).copy())
+        assert ctx.status() == 0
+        ref = outs[(0, 1)]
+        assert (ref[0]["prim"] != 0xFFFFFFFF).any() and (ref[1]["prim"] != 0xFFFFFFFF).any()
+        for k, v in outs.items():
+            assert np.array_equal(v[0], ref[0]), k
+            assert np.array_equal(v[1], ref[1]), k
+            assert np.array_equal(v[2].view(np.uint32), ref[2].view(np.uint32)), k
+    finally:
+        lib().mrt_cuda_set_tuning(ctx.handle, C.byref(saved))

@@ -320,20 +320,23 @@ def test_errors_are_codes_not_crashes(ctx, hf_scene):
     assert rc != 0
 
 
-@pytest.mark.parametrize("dyn,prim,blocks,spread", [(0, 0, 0, 0), (1, 1, 0, 0), (1, 0, 2, 0), (0, 1, 1, 0),
-                                                     (3, 0, 0, 7), (1, 0, 3, 7), (0, 0, 0, 3)])
-def test_schedule_variants_are_bit_identical(ctx, hf_workload, hf_scene, blue_noise, dyn, prim, blocks, spread):
+@pytest.mark.parametrize("dyn,prim,blocks,spread,rmin", [(0, 0, 0, 0, 1), (1, 1, 0, 0, 1), (1, 0, 2, 0, 8),
+                                                          (0, 1, 1, 0, 1), (3, 0, 0, 7, 8), (1, 0, 3, 7, 32),
+                                                          (0, 0, 0, 3, 1), (1, 0, 0, 1, 4)])
+def test_schedule_variants_are_bit_identical(ctx, hf_workload, hf_scene, blue_noise, dyn, prim, blocks, spread,
+                                             rmin):
     # the launch schedule (fetch mode, persistent primary, blocks per SM,
-    # triangle tests spread over the warp) changes which thread traces a
-    # ray, never the result
+    # triangle tests spread over the warp, idle lanes before a refill)
+    # changes which thread traces a ray, never the result
     wl, mesh, bvh = hf_workload
     saved = ctx.tuning()
     try:
-        ctx.set_tuning(dynamic_fetch=dyn, primary_persistent=prim, trace_blocks_per_sm=blocks, tri_spread=spread)
+        ctx.set_tuning(dynamic_fetch=dyn, primary_persistent=prim, trace_blocks_per_sm=blocks, tri_spread=spread,
+                       refill_min=rmin)
         img, g = _pathtrace_gpu(ctx, wl, hf_scene, blue_noise, frame=2)
     finally:
         lib().mrt_cuda_set_tuning(ctx.handle, saved)
-    ctx.set_tuning(dynamic_fetch=1, primary_persistent=1, trace_blocks_per_sm=0, tri_spread=0)
+    ctx.set_tuning(dynamic_fetch=1, primary_persistent=1, trace_blocks_per_sm=0, tri_spread=0, refill_min=1)
     ref_img, ref_g = _pathtrace_gpu(ctx, wl, hf_scene, blue_noise, frame=2)
     lib().mrt_cuda_set_tuning(ctx.handle, saved)
     assert np.array_equal(g["visibility"], ref_g["visibility"])

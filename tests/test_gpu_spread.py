@@ -54,6 +54,10 @@ def test_spread_range(ctx):
     with pytest.raises(MrtError):
         ctx.set_tuning(tri_spread=8)
     ctx.set_tuning(tri_spread=saved)
+    saved = int(ctx.tuning().refill_min)
+    with pytest.raises(MrtError):
+        ctx.set_tuning(refill_min=33)
+    ctx.set_tuning(refill_min=saved)
 
 
 @pytest.mark.parametrize("size", [(256, 256), (77, 45), (31, 3)])
