@@ -270,10 +270,10 @@ typedef struct mrt_tuning {
                                      spread over the warp's lanes instead of
                                      each lane testing its own leaves' (same
                                      hits)                                   */
-    uint32_t refill_min;          /* extension rays with dynamic fetch and
-                                     the batched kernels: a warp fetches new
-                                     rays once at least this many of its
-                                     lanes are idle (or all are); 0 or 1 =
+    uint32_t refill_min;          /* kernels with dynamic fetch (and the
+                                     batched ones): a warp fetches new rays
+                                     once at least this many of its lanes
+                                     are idle (or all are); 0 or 1 =
                                      whenever one is (up to 32)              */
 } mrt_tuning;
 int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning);

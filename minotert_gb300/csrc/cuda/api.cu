@@ -621,7 +621,8 @@ int mrt_cuda_primary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_camera
                             ? launch_primary_tri(scene->dev, fp, *gbuffer, ctx->d_status,
                                                  ctx->counters ? ctx->d_totals : nullptr,
                                                  ctx->tuning.primary_persistent ? ctx->d_prim_fetch : nullptr,
-                                                 trace_blocks(ctx), (ctx->tuning.tri_spread & 4u) != 0u, s)
+                                                 trace_blocks(ctx), (ctx->tuning.tri_spread & 4u) != 0u,
+                                                 refill_min(ctx), s)
                             : launch_primary_sphere(scene->dev, fp, *gbuffer, s);
         if (e != cudaSuccess) return fail(ctx, MRT_ECUDA, "primary rays launch: %s", cudaGetErrorString(e));
     }
@@ -683,7 +684,7 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
         for (uint32_t b = 1; b <= tp.max_bounces; ++b) {
             if (nee)
                 MRT_LAUNCH(2, int(b - 1), launch_trace_shadow(scene->dev, wb, tp, b - 1, tblocks, ctx->d_status,
-                                                              ctx->counters, dyn_sh, s));
+                                                              ctx->counters, dyn_sh, refill_min(ctx), s));
             if (tail != 0u && b >= tail) {
                 MRT_LAUNCH(1, int(b), launch_tail(scene->dev, tp, bn, wb, W, b, tblocks, ctx->d_status, s));
                 tail_done = true;
@@ -699,8 +700,9 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
             MRT_LAUNCH(3, int(b), launch_shade(scene->dev, tp, bn, wb, W, b, ctx->d_status, s));
         }
         if (nee && !tail_done)
-            MRT_LAUNCH(2, int(tp.max_bounces), launch_trace_shadow(scene->dev, wb, tp, tp.max_bounces, tblocks,
-                                                                   ctx->d_status, ctx->counters, dyn_sh, s));
+            MRT_LAUNCH(2, int(tp.max_bounces),
+                       launch_trace_shadow(scene->dev, wb, tp, tp.max_bounces, tblocks, ctx->d_status, ctx->counters,
+                                           dyn_sh, refill_min(ctx), s));
         MRT_LAUNCH(3, 0, launch_tally(wb, s));
     }
     MRT_LAUNCH(3, 0, launch_finalize(wb, color, tp.samples, params->accumulate, params->frame_index, s));
@@ -758,7 +760,8 @@ int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
         tp.max_bounces = 0;
         MRT_LAUNCH(3, 0, launch_shade_primary(scene->dev, fp, *gbuffer, tp, bn, wb, 0, ctx->d_status, s));
         if (nee)
-            MRT_LAUNCH(2, 0, launch_trace_shadow(scene->dev, wb, tp, 0, tblocks, ctx->d_status, ctx->counters, dyn_sh, s));
+            MRT_LAUNCH(2, 0, launch_trace_shadow(scene->dev, wb, tp, 0, tblocks, ctx->d_status, ctx->counters, dyn_sh,
+                                                 refill_min(ctx), s));
         const uint32_t npix = W * H;
         MRT_LAUNCH(3, 0, launch_cache_query_primary(scene->dev, fp, *gbuffer, q, pb, ctx->d_status, s));
         MRT_LAUNCH(7, 0, cache_infer(cache, q, npix, nullptr, pred, s));
@@ -768,12 +771,14 @@ int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
         // that hit; both hits' direct light comes from shadow rays
         MRT_LAUNCH(3, 0, launch_shade_primary(scene->dev, fp, *gbuffer, tp, bn, wb, 0, ctx->d_status, s));
         if (nee)
-            MRT_LAUNCH(2, 0, launch_trace_shadow(scene->dev, wb, tp, 0, tblocks, ctx->d_status, ctx->counters, dyn_sh, s));
+            MRT_LAUNCH(2, 0, launch_trace_shadow(scene->dev, wb, tp, 0, tblocks, ctx->d_status, ctx->counters, dyn_sh,
+                                                 refill_min(ctx), s));
         MRT_LAUNCH(1, 1, launch_trace_ext(scene->dev, wb, 1, tblocks, ctx->d_status, ctx->counters, dyn,
                                           refill_min(ctx), s));
         MRT_LAUNCH(3, 1, launch_shade(scene->dev, tp, bn, wb, W, 1, ctx->d_status, s));
         if (nee)
-            MRT_LAUNCH(2, 1, launch_trace_shadow(scene->dev, wb, tp, 1, tblocks, ctx->d_status, ctx->counters, dyn_sh, s));
+            MRT_LAUNCH(2, 1, launch_trace_shadow(scene->dev, wb, tp, 1, tblocks, ctx->d_status, ctx->counters, dyn_sh,
+                                                 refill_min(ctx), s));
         MRT_LAUNCH(3, 1, launch_cache_query(scene->dev, tp, wb, q, pb, ctx->d_status, s));
         MRT_LAUNCH(7, 1, cache_infer(cache, q, uint32_t(wb.cap), wb.counters + kCntExt + 1, pred, s));
         MRT_LAUNCH(3, 1, launch_cache_apply(wb, wb.counters + kCntExt + 1, uint32_t(wb.cap), pred, pb, s));

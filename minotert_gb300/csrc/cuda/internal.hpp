@@ -140,7 +140,7 @@ uint32_t bvh8_depth(const mrt_bvh8_node* nodes, uint32_t n);
 // over each warp when `spread` is set (not while counting).
 cudaError_t launch_primary_tri(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g,
                                uint32_t* status, unsigned long long* totals, uint32_t* fetch, int blocks,
-                               bool spread, cudaStream_t s);
+                               bool spread, uint32_t refill_min, cudaStream_t s);
 cudaError_t launch_primary_sphere(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g,
                                   cudaStream_t s);
 cudaError_t launch_secondary_sphere(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g,
@@ -159,13 +159,13 @@ cudaError_t launch_shade_primary(const DevScene& sc, const FrameParams& fp, cons
 // (dynamic); each of the two with the step's triangle tests spread over the
 // warp (trav_step_spread).
 enum : int { kFetchBatch = 0, kFetchDynamic = 1, kFetchSpread = 2, kFetchBatchSpread = 3 };
-// refill_min: idle lanes a warp waits for before it fetches new rays (1:
-// refill whenever a lane is idle)
+// refill_min (dynamic fetch): idle lanes a warp waits for before it fetches
+// new rays (1: refill whenever a lane is idle)
 cudaError_t launch_trace_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t bounce, int blocks,
                              uint32_t* status, bool count, int mode, uint32_t refill_min, cudaStream_t s);
 cudaError_t launch_trace_shadow(const DevScene& sc, const WaveBuffers& wb, const TraceParams& tp,
                                 uint32_t vertex, int blocks, uint32_t* status, bool count, int mode,
-                                cudaStream_t s);
+                                uint32_t refill_min, cudaStream_t s);
 cudaError_t launch_shade(const DevScene& sc, const TraceParams& tp, BlueNoise bn, const WaveBuffers& wb,
                          uint32_t width, uint32_t bounce, uint32_t* status, cudaStream_t s);
 // every path of the bounce-`first` extension queue to its end (k_tail)
@@ -225,7 +225,7 @@ struct mrt_ctx {
     // timing
     bool timing = false;
     bool counters = false;
-    mrt_tuning tuning{0u, 1u, 0u, mrt::kSortNever, 3u, 0u, 1u, 8u};  // autotuned on GB300 (icosphere field, 1080p)
+    mrt_tuning tuning{0u, 3u, 0u, mrt::kSortNever, 3u, 0u, 3u, 8u};  // autotuned on GB300 (icosphere field, 1080p)
     uint32_t* d_prim_fetch = nullptr;  // work counter of the persistent primary kernel
     int occ_blocks = 0;                // traversal blocks per SM at full occupancy
     unsigned long long* d_totals = nullptr;  // kTotSlots accumulated totals

@@ -130,7 +130,7 @@ MRT_DEV uint32_t warp_refill(uint32_t* fetch, uint32_t n, bool need, bool& exhau
 template <bool kCount>
 __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
 k_primary_tri_dyn(DevScene sc, FrameParams fp, mrt_gbuffer g, uint32_t* status, unsigned long long* totals,
-                  uint32_t* fetch) {
+                  uint32_t* fetch, uint32_t refill_min) {
     __shared__ uint2 stk[kStackDepth * kTraceBlock];
     const uint32_t tiles_x = (fp.width + 7u) / 8u, tiles_y = (fp.height + 3u) / 4u;
     const uint32_t n = tiles_x * tiles_y * 32u;
@@ -139,7 +139,7 @@ k_primary_tri_dyn(DevScene sc, FrameParams fp, mrt_gbuffer g, uint32_t* status, 
     Trav s;
     bool have = false, exhausted = false;
     while (true) {
-        const uint32_t idx = warp_refill(fetch, n, !have, exhausted);
+        const uint32_t idx = warp_refill(fetch, n, !have, exhausted, refill_min);
         if (idx != kMiss) {
             const uint32_t tile = idx >> 5, l = idx & 31u;
             const uint32_t x = (tile % tiles_x) * 8u + (l & 7u), y = (tile / tiles_x) * 4u + (l >> 3);
@@ -558,7 +558,7 @@ k_trace_ext(DevScene sc, WaveBuffers wb, uint32_t bounce, uint32_t* status, uint
 // rays add their contribution to the pixel's radiance.
 template <bool kCount, bool kDyn, bool kSpread = false>
 __global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
-k_trace_shadow(DevScene sc, WaveBuffers wb, TraceParams tp, uint32_t vertex, uint32_t* status) {
+k_trace_shadow(DevScene sc, WaveBuffers wb, TraceParams tp, uint32_t vertex, uint32_t* status, uint32_t refill_min) {
     __shared__ uint2 stk[kStackDepth * kTraceBlock];
     __shared__ unsigned long long slots[kSpread ? kTraceBlock : 1];
     const uint32_t n = wb.counters[kCntShadow + vertex];
@@ -571,7 +571,7 @@ k_trace_shadow(DevScene sc, WaveBuffers wb, TraceParams tp, uint32_t vertex, uin
         bool have = false, exhausted = false;
         uint32_t ri = 0u;
         while (true) {
-            const uint32_t idx = warp_refill(fetch, n, !have, exhausted);
+            const uint32_t idx = warp_refill(fetch, n, !have, exhausted, refill_min);
             if (idx != kMiss) {
                 const float4 a = wb.sq[idx].o_pix;
                 trav_init(s, f3{a.x, a.y, a.z}, sun, 0.0f, INFINITY);
@@ -764,12 +764,15 @@ k_trace_rays_sphere(DevScene sc, const mrt_ray* rays, uint32_t n, mrt_hit* hits)
 // ------------------------------------------------------------------ launchers
 
 cudaError_t launch_primary_tri(const DevScene& sc, const FrameParams& fp, const mrt_gbuffer& g, uint32_t* status,
-                               unsigned long long* totals, uint32_t* fetch, int blocks, bool spread, cudaStream_t s) {
+                               unsigned long long* totals, uint32_t* fetch, int blocks, bool spread,
+                               uint32_t refill_min, cudaStream_t s) {
     if (fetch) {
         cudaError_t e = cudaMemsetAsync(fetch, 0, sizeof(uint32_t), s);
         if (e != cudaSuccess) return e;
-        if (totals) k_primary_tri_dyn<true><<<blocks, kTraceBlock, 0, s>>>(sc, fp, g, status, totals, fetch);
-        else k_primary_tri_dyn<false><<<blocks, kTraceBlock, 0, s>>>(sc, fp, g, status, nullptr, fetch);
+        if (totals)
+            k_primary_tri_dyn<true><<<blocks, kTraceBlock, 0, s>>>(sc, fp, g, status, totals, fetch, refill_min);
+        else
+            k_primary_tri_dyn<false><<<blocks, kTraceBlock, 0, s>>>(sc, fp, g, status, nullptr, fetch, refill_min);
         return cudaGetLastError();
     }
     dim3 grid((fp.width + 15) / 16, (fp.height + 7) / 8);
@@ -824,18 +827,19 @@ cudaError_t launch_shade_primary(const DevScene& sc, const FrameParams& fp, cons
 
 cudaError_t launch_trace_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t bounce, int blocks, uint32_t* status,
                              bool count, int mode, uint32_t refill_min, cudaStream_t s) {
+#define MRT_EXT(C, D, P) k_trace_ext<C, D, P><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status, refill_min)
     if (count) {  // the counting kernels test each lane's own triangles
-        if (mode == kFetchDynamic || mode == kFetchSpread)
-            k_trace_ext<true, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status, refill_min);
-        else k_trace_ext<true, false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status, refill_min);
-    } else if (mode == kFetchSpread) {
-        k_trace_ext<false, true, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status, refill_min);
-    } else if (mode == kFetchBatchSpread) {
-        k_trace_ext<false, false, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status, refill_min);
+        if (mode == kFetchDynamic || mode == kFetchSpread) MRT_EXT(true, true, false);
+        else MRT_EXT(true, false, false);
     } else {
-        if (mode == kFetchDynamic) k_trace_ext<false, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status, refill_min);
-        else k_trace_ext<false, false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, bounce, status, refill_min);
+        switch (mode) {
+        case kFetchDynamic: MRT_EXT(false, true, false); break;
+        case kFetchSpread: MRT_EXT(false, true, true); break;
+        case kFetchBatchSpread: MRT_EXT(false, false, true); break;
+        default: MRT_EXT(false, false, false); break;
+        }
     }
+#undef MRT_EXT
     return cudaGetLastError();
 }
 
@@ -846,19 +850,22 @@ cudaError_t launch_tail(const DevScene& sc, const TraceParams& tp, BlueNoise bn,
 }
 
 cudaError_t launch_trace_shadow(const DevScene& sc, const WaveBuffers& wb, const TraceParams& tp, uint32_t vertex,
-                                int blocks, uint32_t* status, bool count, int mode, cudaStream_t s) {
+                                int blocks, uint32_t* status, bool count, int mode, uint32_t refill_min,
+                                cudaStream_t s) {
+#define MRT_SH(C, D, P) \
+    k_trace_shadow<C, D, P><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status, refill_min)
     if (count) {  // the counting kernels test each lane's own triangles
-        if (mode == kFetchDynamic || mode == kFetchSpread)
-            k_trace_shadow<true, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
-        else k_trace_shadow<true, false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
-    } else if (mode == kFetchSpread) {
-        k_trace_shadow<false, true, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
-    } else if (mode == kFetchBatchSpread) {
-        k_trace_shadow<false, false, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
+        if (mode == kFetchDynamic || mode == kFetchSpread) MRT_SH(true, true, false);
+        else MRT_SH(true, false, false);
     } else {
-        if (mode == kFetchDynamic) k_trace_shadow<false, true><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
-        else k_trace_shadow<false, false><<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, vertex, status);
+        switch (mode) {
+        case kFetchDynamic: MRT_SH(false, true, false); break;
+        case kFetchSpread: MRT_SH(false, true, true); break;
+        case kFetchBatchSpread: MRT_SH(false, false, true); break;
+        default: MRT_SH(false, false, false); break;
+        }
     }
+#undef MRT_SH
     return cudaGetLastError();
 }
 

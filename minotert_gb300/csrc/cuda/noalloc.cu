@@ -92,7 +92,8 @@ extern "C" int mrt_cuda_primary_rays_noalloc(const mrt_bvh8_node* nodes, uint32_
     sc.sphere_count = 0;
     const mrt::FrameParams fp = mrt::make_frame_params(consts, gbuffer->width, gbuffer->height);
     // the launcher clears the work counter (scratch[0]) on `st` first
-    cudaError_t e = mrt::launch_primary_tri(sc, fp, *gbuffer, stat, nullptr, s.scratch, s.blocks, false, st);
+    cudaError_t e = mrt::launch_primary_tri(sc, fp, *gbuffer, stat, nullptr, s.scratch, s.blocks, false, 1u,
+                                           st);
     if (e != cudaSuccess) return MRT_ECUDA;
     return MRT_OK;
 }
