@@ -252,10 +252,25 @@ def run_mine(args, world, rank, local, dist):
 
     # roofline of the dominant launch: the bounce-1 extension kernel
     # (k_trace_ext, one launch per frame, the largest in the launch list),
-    # bytes from its own node/triangle counts, time from its CUDA events
+    # bytes from its own node/triangle counts, time from its CUDA events.
+    # With overlap_shadow it shares the GPU with the shadow rays of vertex 0,
+    # so its events would not time the kernel alone: a few more frames with
+    # the overlap off (and L2 flushed before each) time it by itself.
     peaks = _peaks()
-    b1_rays = ext[0] / args.steps
-    b1_ms = st.ms_extend_b[0] / args.steps
+    saved_overlap = int(ctx.tuning().overlap_shadow)
+    ctx.set_tuning(overlap_shadow=0)
+    ctx.frame_stats()
+    ctx.set_timing(True)
+    n_alone = 3
+    for k in range(n_alone):
+        flush.zero(stream)
+        frame(args.warmup + args.steps + 1 + k)
+    ctx.sync(stream)
+    alone = ctx.frame_stats()
+    ctx.set_timing(False)
+    ctx.set_tuning(overlap_shadow=saved_overlap)
+    b1_rays = int(alone.extension_rays[0]) / n_alone
+    b1_ms = alone.ms_extend_b[0] / n_alone
     n_node_b1 = int(cs.nodes_extension[0]) / max(int(cs.extension_rays[0]), 1)
     n_tri_b1 = int(cs.tris_extension[0]) / max(int(cs.extension_rays[0]), 1)
     dk_bytes = b1_rays * bytes_per_ray(n_node_b1, n_tri_b1)
@@ -277,7 +292,8 @@ def run_mine(args, world, rank, local, dist):
                                  "shadow": n_tri_sh},
                 "note": "bytes/ray = 32 + 16 + 128 N_node + 48 N_tri with N from the counting kernels "
                         "(equal to the oracle's counts); the scene (69 MB) is L2-resident, so a fraction "
-                        "above 1 of the HBM copy peak means the traversal runs out of L2"}
+                        "above 1 of the HBM copy peak means the traversal runs out of L2; the launch is "
+                        "timed alone (overlap_shadow off) over %d frames after the timed ones" % n_alone}
 
     b2 = sum(ext[1:])
     b2_ms = sum(st.ms_extend_b[1:s.bounces])
@@ -293,8 +309,10 @@ def run_mine(args, world, rank, local, dist):
                          "shadow": st.ms_shadow / args.steps, "shade": st.ms_shade / args.steps},
         "note": "tail_bounce %d: the paths alive at that bounce finish in one persistent launch (k_tail), "
                 "timed as extension of that bounce; its shading and shadow rays are inside that time, so "
-                "shadow_mrays_s divides all shadow rays by the wavefront shadow launches' time only"
-                % int(ctx.tuning().tail_bounce),
+                "shadow_mrays_s divides all shadow rays by the wavefront shadow launches' time only. "
+                "overlap_shadow %d: the shadow launches run on a second stream beside the next extension "
+                "launch, so the per-kind times overlap and the shadow time is the part on that stream"
+                % (int(ctx.tuning().tail_bounce), int(ctx.tuning().overlap_shadow)),
     }
 
     # end to end through the C ABI with host buffers: camera and trace

@@ -275,6 +275,11 @@ typedef struct mrt_tuning {
                                      once at least this many of its lanes
                                      are idle (or all are); 0 or 1 =
                                      whenever one is (up to 32)              */
+    uint32_t overlap_shadow;      /* 1: the shadow rays of vertex b - 1 and
+                                     the extension rays of bounce b trace on
+                                     two streams at once (a stream of the
+                                     context joined before shading; same
+                                     image)                                  */
 } mrt_tuning;
 int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning);
 int mrt_cuda_get_tuning(mrt_ctx* ctx, mrt_tuning* tuning);

@@ -234,6 +234,14 @@ int mrt_cuda_create(mrt_ctx** out, int device) {
         delete ctx;
         return MRT_ENOMEM;
     }
+    // the side stream of overlap_shadow exists from the start, so that a
+    // frame captured into a graph by the caller never creates it
+    if (cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        mrt_cuda_destroy(ctx);
+        return MRT_ECUDA;
+    }
     *out = ctx;
     return MRT_OK;
 }
@@ -253,6 +261,9 @@ int mrt_cuda_destroy(mrt_ctx* ctx) {
     cudaFree(ctx->d_color);
     for (auto& r : ctx->recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     for (auto e : ctx->ev_pool) cudaEventDestroy(e);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     delete ctx;
     return MRT_OK;
 }
@@ -297,10 +308,12 @@ static int fetch_mode(const mrt_ctx* ctx, uint32_t which) {
 
 static uint32_t refill_min(const mrt_ctx* ctx) { return ctx->tuning.refill_min ? ctx->tuning.refill_min : 1u; }
 
+
+
 int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning) {
     if (!ctx || !tuning) return fail(ctx, MRT_EINVAL, "set_tuning: null argument");
     if (tuning->trace_blocks_per_sm > 64 || tuning->dynamic_fetch > 3 || tuning->primary_persistent > 1 ||
-        tuning->tail_bounce > MRT_MAX_BOUNCES || tuning->tri_spread > 7 || tuning->refill_min > 32 ||
+        tuning->tail_bounce > MRT_MAX_BOUNCES || tuning->tri_spread > 7 || tuning->refill_min > 32 || tuning->overlap_shadow > 1 ||
         (tuning->stack_depth != 0u && tuning->stack_depth != 16u && tuning->stack_depth != 24u &&
          tuning->stack_depth != 32u))
         return fail(ctx, MRT_EINVAL, "set_tuning: value out of range");
@@ -667,6 +680,7 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
     const int tblocks = trace_blocks(ctx);
     const bool nee = tp.estimator == MRT_EST_NEE;
     const int dyn = fetch_mode(ctx, 0u), dyn_sh = fetch_mode(ctx, 1u);
+    const bool overlap_sh = ctx->tuning.overlap_shadow != 0u && !ctx->counters;
 #define MRT_LAUNCH(kind, bounce, expr)                                                                   \
     do {                                                                                                 \
         Scope sc_(ctx, s, kind, bounce);                                                                 \
@@ -682,10 +696,25 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
         const uint32_t tail = ctx->counters ? 0u : ctx->tuning.tail_bounce;
         bool tail_done = false;
         for (uint32_t b = 1; b <= tp.max_bounces; ++b) {
-            if (nee)
+            // The shadow rays of vertex b - 1 and the extension rays of
+            // bounce b are independent (different queues; only the shadow
+            // rays add radiance, and shade(b) after the join adds the next):
+            // with overlap_shadow they run on two streams, so each fills the
+            // GPU while the other drains.  Not before the path tail, whose
+            // radiance additions must follow the shadow rays'.
+            const bool tail_now = tail != 0u && b >= tail;
+            const bool overlap = nee && overlap_sh && !tail_now;
+            if (overlap) {
+                MRT_CK(cudaEventRecord(ctx->ev_fork, s));
+                MRT_CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+                MRT_LAUNCH(2, int(b - 1), launch_trace_shadow(scene->dev, wb, tp, b - 1, tblocks, ctx->d_status,
+                                                              ctx->counters, dyn_sh, refill_min(ctx), ctx->side));
+                MRT_CK(cudaEventRecord(ctx->ev_join, ctx->side));
+            } else if (nee) {
                 MRT_LAUNCH(2, int(b - 1), launch_trace_shadow(scene->dev, wb, tp, b - 1, tblocks, ctx->d_status,
                                                               ctx->counters, dyn_sh, refill_min(ctx), s));
-            if (tail != 0u && b >= tail) {
+            }
+            if (tail_now) {
                 MRT_LAUNCH(1, int(b), launch_tail(scene->dev, tp, bn, wb, W, b, tblocks, ctx->d_status, s));
                 tail_done = true;
                 break;
@@ -697,6 +726,7 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
             }
             MRT_LAUNCH(1, int(b), launch_trace_ext(scene->dev, wb, b, tblocks, ctx->d_status, ctx->counters, dyn,
                                                    refill_min(ctx), s));
+            if (overlap) MRT_CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
             MRT_LAUNCH(3, int(b), launch_shade(scene->dev, tp, bn, wb, W, b, ctx->d_status, s));
         }
         if (nee && !tail_done)

@@ -225,7 +225,7 @@ struct mrt_ctx {
     // timing
     bool timing = false;
     bool counters = false;
-    mrt_tuning tuning{0u, 3u, 0u, mrt::kSortNever, 3u, 0u, 3u, 8u};  // autotuned on GB300 (icosphere field, 1080p)
+    mrt_tuning tuning{0u, 3u, 0u, mrt::kSortNever, 3u, 0u, 3u, 8u, 1u};  // autotuned on GB300 (icosphere field, 1080p)
     uint32_t* d_prim_fetch = nullptr;  // work counter of the persistent primary kernel
     int occ_blocks = 0;                // traversal blocks per SM at full occupancy
     unsigned long long* d_totals = nullptr;  // kTotSlots accumulated totals
@@ -234,4 +234,8 @@ struct mrt_ctx {
     mrt_frame_stats acc{};
     uint32_t launches = 0;
     const mrt_sky* sky = nullptr;  // miss shader bound by mrt_cuda_set_sky
+    // second stream for the shadow rays that overlap the next extension
+    // trace (mrt_tuning.overlap_shadow), with its fork / join events
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };

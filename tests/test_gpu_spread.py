@@ -79,3 +79,24 @@ def test_spread_primary_matches_oracle(ctx, hf_workload, size):
     assert np.array_equal(g["visibility"], ref["visibility"])
     assert np.array_equal(g["hit_t"].view(np.uint32), ref["hit_t"].view(np.uint32))
     assert ctx.status() == 0
+
+
+@pytest.mark.parametrize("tail", [0, 3])
+def test_overlapped_shadow_rays_same_image(ctx, hf_workload, blue_noise, tail):
+    # shadow rays of vertex b - 1 on a second stream beside the extension
+    # rays of bounce b: the same image and ray counts
+    wl, mesh, bvh = hf_workload
+    ds = DeviceScene.triangles(ctx, mesh, bvh)
+    settings = TraceSettings(samples=2, bounces=5, rr_start=1, rng_mode=1)
+    saved = ctx.tuning()
+    try:
+        ctx.set_tuning(overlap_shadow=0)
+        ref, ext, shadow = _render(ctx, ds, wl, blue_noise, settings, 3, tail)
+        ctx.set_tuning(overlap_shadow=1)
+        img, e, sh = _render(ctx, ds, wl, blue_noise, settings, 3, tail)
+        assert int(ctx.tuning().overlap_shadow) == 1
+    finally:
+        ctx.set_tuning(**{f: getattr(saved, f) for f, _ in saved._fields_})
+    assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+    assert e == ext and sh == shadow
+    assert ctx.status() == 0
