@@ -92,6 +92,24 @@ MRT_DEV f3 offset_ray(f3 p, f3 n) { return f3{offset_axis(p.x, n.x), offset_axis
 // r^8/8! < 6e-9 relative), then an exact scale by 2^n.  Results below
 // 2^-126 flush to 0.  Used where an expression cancels and would turn
 // a last-bit difference between two exp implementations into a visible one.
+// exp_cw without its range handling: equal to exp_cw for -87 < x <= 88
+// (there n = rint(x / ln 2) lies in [-125, 127], so the scale is a normal
+// power of two).
+MRT_DEV float exp_cw_core(float x) {
+    const float n = rintf(__fmul_rn(x, 1.44269502f));
+    float r = fmaf(-n, 0.693145752f, x);
+    r = fmaf(-n, 1.42860677e-6f, r);
+    float p = 1.98412701e-4f;
+    p = fmaf(p, r, 1.38888892e-3f);
+    p = fmaf(p, r, 8.33333377e-3f);
+    p = fmaf(p, r, 4.16666679e-2f);
+    p = fmaf(p, r, 1.66666672e-1f);
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = fmaf(p, r, 1.0f);
+    return __fmul_rn(p, __int_as_float((int(n) + 127) << 23));
+}
+
 MRT_DEV float exp_cw(float x) {
     if (!(x > -87.0f)) return x != x ? x : 0.0f;
     if (x > 88.0f) return __int_as_float(0x7F800000);

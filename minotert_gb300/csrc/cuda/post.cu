@@ -11,6 +11,7 @@
 // bilateral weights use exp_cw (common.cuh), so the CPU oracle reproduces
 // the filter and reprojection bit for bit; the tonemap curves keep CUDA's
 // powf / expf and agree with the oracle to within one 8-bit step.
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -83,15 +84,31 @@ bool make_table(const mrt_bilateral_params& p, BilateralTable& t) {
 
 // One block filters a 16x16 tile from a shared-memory window of the colour,
 // depth and normal planes covering every tap (radius columns either side,
-// radius rows above, radius + 1 below for the bilinear row pair).
+// radius rows above, radius + 1 below for the bilinear row pair).  Every tap
+// of column c interpolates between two whole rows at the column's fraction
+// fr[c], so the interpolated sample at (row s, column x) -- depth turned
+// into near / depth, normal and colour -- is the same for all the up to
+// 2r + 1 threads of the column whose taps land on it.  Each column's samples
+// are therefore computed once into a second shared-memory window
+// (16 columns x 16 + count - 1 rows, two float4 per sample) and the taps
+// read them:
+// the same operations on the same operands as a per-tap evaluation, so the
+// same bits, for a fraction of the arithmetic.  kExpChecked: the weights'
+// exponential keeps its range handling (only needed when the argument can
+// leave (-87, 88], i.e. 0.5 / threshold^2 > 88).
+template <bool kExpChecked>
 __global__ void __launch_bounds__(kBilTile * kBilTile)
 k_bilateral(BilateralTable T, const float* __restrict__ color, const uint16_t* __restrict__ depth,
             const ushort4* __restrict__ normal, uint32_t W, uint32_t H, float* __restrict__ out) {
     extern __shared__ float sm[];
     const int r = T.radius;
     const int tw = kBilTile + 2 * r, th = kBilTile + 2 * r + 1, plane = tw * th;
+    const int splane = kBilTile * (kBilTile + 2 * r);
     float *cr = sm, *cg = sm + plane, *cb = sm + 2 * plane, *zz = sm + 3 * plane;
     float *nx = sm + 4 * plane, *ny = sm + 5 * plane, *nz = sm + 6 * plane;
+    // samples: (near / depth, normal) and (colour, 0), 16-byte aligned
+    float4* sa = reinterpret_cast<float4*>(sm + ((7 * plane + 3) & ~3));
+    float4* sb = sa + splane;
     const int bx = int(blockIdx.x) * kBilTile - r, by = int(blockIdx.y) * kBilTile - r;
     for (int i = threadIdx.x; i < plane; i += blockDim.x) {
         const int gx = min(max(bx + i % tw, 0), int(W) - 1), gy = min(max(by + i / tw, 0), int(H) - 1);
@@ -108,45 +125,52 @@ k_bilateral(BilateralTable T, const float* __restrict__ color, const uint16_t* _
     __syncthreads();
     const int tx = threadIdx.x % kBilTile, ty = threadIdx.x / kBilTile;
     const uint32_t x = blockIdx.x * kBilTile + tx, y = blockIdx.y * kBilTile + ty;
-    if (x >= W || y >= H) return;
-    const int lx = tx + r, ly = ty + r, ic = ly * tw + lx;
+    const bool inside = x < W && y < H;
+    const int ic = (ty + r) * tw + tx + r;
     const float cz = zz[ic];
     f3 res{cr[ic], cg[ic], cb[ic]};
-    if (!(cz < 0.0f)) {
-        const f3 cn{nx[ic], ny[ic], nz[ic]};
-        const float ncz = fd(T.near_plane, cz);
-        float zb = 0.0f, ar = 0.0f, ag = 0.0f, ab = 0.0f;
-        for (int c = 0; c < T.ncols; ++c) {
-            const int col = lx + c - r;
-            const float fr = T.fr[c], gr = fs(1.0f, fr);
-            const int t0 = T.first[c], cnt = T.count[c];
-            int ia = (ly + T.r0[c]) * tw + col;
-            // consecutive taps of a column share a row: the lower row of
-            // tap k is the upper row of tap k + 1, so it is loaded once
-            float a_z = zz[ia], a_nx = nx[ia], a_ny = ny[ia], a_nz = nz[ia];
-            float a_r = cr[ia], a_g = cg[ia], a_b = cb[ia];
-            for (int k = 0; k < cnt; ++k, ia += tw) {
-                const int ib = ia + tw;
-                const float b_z = zz[ib], b_nx = nx[ib], b_ny = ny[ib], b_nz = nz[ib];
-                const float b_r = cr[ib], b_g = cg[ib], b_b = cb[ib];
-                const float wz = fa(fm(a_z, gr), fm(b_z, fr));
-                const f3 wn{fa(fm(a_nx, gr), fm(b_nx, fr)), fa(fm(a_ny, gr), fm(b_ny, fr)),
-                            fa(fm(a_nz, gr), fm(b_nz, fr))};
-                float dz = fs(fd(T.near_plane, wz), ncz);
-                dz = fm(dz, 100.0f);
-                const float dn = dot_rn(wn, cn);
+    const bool filt = inside && !(cz < 0.0f);  // (all threads build the samples)
+    const f3 cn{nx[ic], ny[ic], nz[ic]};
+    const float ncz = filt ? fd(T.near_plane, cz) : 0.0f;
+    float zb = 0.0f, ar = 0.0f, ag = 0.0f, ab = 0.0f;
+    for (int c = 0; c < T.ncols; ++c) {
+        const float fr = T.fr[c], gr = fs(1.0f, fr);
+        const int t0 = T.first[c], cnt = T.count[c];
+        // sample (s, xx): rows r + r0 + s and + 1 of tile column xx + c;
+        // thread (tx, ty)'s tap k reads sample (ty + k, tx)
+        const int ns = (kBilTile + cnt - 1) * kBilTile, base = (r + T.r0[c]) * tw + c;
+        __syncthreads();  // the previous column's samples have been read
+        for (int i = threadIdx.x; i < ns; i += blockDim.x) {
+            const int ia = base + (i / kBilTile) * tw + i % kBilTile, ib = ia + tw;
+            sa[i] = make_float4(fd(T.near_plane, fa(fm(zz[ia], gr), fm(zz[ib], fr))),
+                                fa(fm(nx[ia], gr), fm(nx[ib], fr)), fa(fm(ny[ia], gr), fm(ny[ib], fr)),
+                                fa(fm(nz[ia], gr), fm(nz[ib], fr)));
+            sb[i] = make_float4(fa(fm(cr[ia], gr), fm(cr[ib], fr)), fa(fm(cg[ia], gr), fm(cg[ib], fr)),
+                                fa(fm(cb[ia], gr), fm(cb[ib], fr)), 0.0f);
+        }
+        __syncthreads();
+        if (filt) {
+            // a warp's 32 threads read 32 consecutive samples: conflict-free
+            const float4* pa = sa + ty * kBilTile + tx;
+            const float4* pb = sb + ty * kBilTile + tx;
+            const float* blur = T.blur + t0;
+#pragma unroll 2
+            for (int k = 0; k < cnt; ++k) {
+                const float4 a = pa[k * kBilTile], b = pb[k * kBilTile];
+                const float dz = fm(fs(a.x, ncz), 100.0f);
+                const float dn = dot_rn(f3{a.y, a.z, a.w}, cn);
                 const float arg = fm(fclamp(fs(dn, fm(dz, dz)), 0.0f, 1.0f), T.inv_thr_sq2);
-                const float df = fm(fm(exp_cw(arg), T.inv_thr_sqrt2pi), T.blur[t0 + k]);
+                const float e = kExpChecked ? exp_cw(arg) : exp_cw_core(arg);
+                const float df = fm(fm(e, T.inv_thr_sqrt2pi), blur[k]);
                 zb = fa(zb, df);
-                ar = fa(ar, fm(df, fa(fm(a_r, gr), fm(b_r, fr))));
-                ag = fa(ag, fm(df, fa(fm(a_g, gr), fm(b_g, fr))));
-                ab = fa(ab, fm(df, fa(fm(a_b, gr), fm(b_b, fr))));
-                a_z = b_z; a_nx = b_nx; a_ny = b_ny; a_nz = b_nz;
-                a_r = b_r; a_g = b_g; a_b = b_b;
+                ar = fa(ar, fm(df, b.x));
+                ag = fa(ag, fm(df, b.y));
+                ab = fa(ab, fm(df, b.z));
             }
         }
-        res = f3{fd(ar, zb), fd(ag, zb), fd(ab, zb)};
     }
+    if (!inside) return;
+    if (filt) res = f3{fd(ar, zb), fd(ag, zb), fd(ab, zb)};
     if (T.dither) {
         uint32_t seed = x * 709u + y * 1153u + T.frame * 1361u;
         const float nz0 = fm(random_float(seed), 0.005f);
@@ -156,6 +180,13 @@ k_bilateral(BilateralTable T, const float* __restrict__ color, const uint16_t* _
     out[3 * p] = res.x;
     out[3 * p + 1] = res.y;
     out[3 * p + 2] = res.z;
+}
+
+// Shared memory of k_bilateral for radius r: the texel window (seven
+// planes, padded to 16 bytes) and the samples of one column (two float4).
+constexpr size_t bilateral_smem(int r) {
+    return (size_t((7 * (kBilTile + 2 * r) * (kBilTile + 2 * r + 1) + 3) & ~3) +
+            size_t(8) * kBilTile * (kBilTile + 2 * r)) * sizeof(float);
 }
 
 // ------------------------------------------------------------------- tonemap
@@ -359,17 +390,29 @@ int mrt_cuda_bilateral(mrt_ctx* ctx, const mrt_gbuffer* g, const float* color, c
     static thread_local BilateralTable table;
     if (!make_table(*params, table)) return set_error(ctx, MRT_ERANGE, "bilateral: radius above the maximum");
     cudaSetDevice(ctx->device);
-    const int r = table.radius;
-    const size_t smem = size_t(7) * (kBilTile + 2 * r) * (kBilTile + 2 * r + 1) * sizeof(float);
-    static thread_local int configured_smem = 0;
-    if (smem > 48 * 1024 && int(smem) > configured_smem) {
-        if (cudaFuncSetAttribute(k_bilateral, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
-            return set_error(ctx, MRT_ECUDA, "bilateral: shared memory size");
-        configured_smem = int(smem);
+    const size_t smem = bilateral_smem(table.radius);
+    // the exponential's argument lies in [0, 0.5 / threshold^2]
+    const bool checked = !(table.inv_thr_sq2 <= 88.0f);
+    // the shared-memory limit is raised to the largest radius's need once per
+    // device and kernel form
+    static std::atomic<uint64_t> configured[2];
+    const uint64_t bit = uint64_t(1) << (ctx->device & 63);
+    if ((configured[checked].load() & bit) == 0) {
+        const int most = int(bilateral_smem(MRT_BILATERAL_MAX_RADIUS));
+        const cudaError_t e = checked
+            ? cudaFuncSetAttribute(k_bilateral<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, most)
+            : cudaFuncSetAttribute(k_bilateral<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+        if (e != cudaSuccess) return set_error(ctx, MRT_ECUDA, "bilateral: shared memory size");
+        configured[checked].fetch_or(bit);
     }
     const dim3 grid((g->width + kBilTile - 1) / kBilTile, (g->height + kBilTile - 1) / kBilTile);
-    k_bilateral<<<grid, kBilTile * kBilTile, smem, as_stream(stream)>>>(
-        table, color, g->depth, reinterpret_cast<const ushort4*>(g->normal), g->width, g->height, out);
+    const ushort4* nrm = reinterpret_cast<const ushort4*>(g->normal);
+    if (checked)
+        k_bilateral<true><<<grid, kBilTile * kBilTile, smem, as_stream(stream)>>>(table, color, g->depth, nrm,
+                                                                                 g->width, g->height, out);
+    else
+        k_bilateral<false><<<grid, kBilTile * kBilTile, smem, as_stream(stream)>>>(table, color, g->depth, nrm,
+                                                                                  g->width, g->height, out);
     if (cudaGetLastError() != cudaSuccess) return set_error(ctx, MRT_ECUDA, "bilateral: launch");
     ctx->launches++;
     return MRT_OK;

@@ -37,17 +37,28 @@ def hf_frame(ctx, hf_workload, blue_noise):
     return cam, ds, pt, gb, col, W, H
 
 
-@pytest.mark.parametrize("sigma,k_sigma,dither", [(5.0, 2.0, True), (2.0, 1.5, False), (8.0, 3.0, False)])
-def test_bilateral_vs_oracle(ctx, hf_frame, sigma, k_sigma, dither):
+@pytest.mark.parametrize("sigma,k_sigma,dither,thr", [(5.0, 2.0, True, 0.12), (2.0, 1.5, False, 0.12),
+                                                      (8.0, 3.0, False, 0.12), (4.0, 2.0, False, 0.05),
+                                                      (1.0, 0.4, True, 0.3)])
+def test_bilateral_vs_oracle(ctx, hf_frame, sigma, k_sigma, dither, thr):
+    # threshold 0.05 puts the weights' exponent beyond 88, the kernel form
+    # that keeps the exponential's range handling (the shader's weights then
+    # overflow where neighbours agree, giving inf / NaN like the oracle's;
+    # NaN payloads differ between machines, so those pixels compare by
+    # class); sigma 1 x 0.4 rounds to radius 0 (the centre tap alone)
     cam, ds, pt, gb, col, W, H = hf_frame
-    out = Denoiser(ctx).bilateral(col, gb, cam, BilateralParams(sigma, k_sigma, 0.12), frame_counter=7,
+    out = Denoiser(ctx).bilateral(col, gb, cam, BilateralParams(sigma, k_sigma, thr), frame_counter=7,
                                   dither=dither)
     got = out.download(np.float32, (H, W, 3))
     g = gb.download()
     src = col.download(np.float32, (H, W, 3))
-    ref = post.bilateral(src, g["depth"], g["normal"], sigma, k_sigma, 0.12, cam.nearPlane, 7, dither)
-    assert np.isfinite(got).all()
-    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+    ref = post.bilateral(src, g["depth"], g["normal"], sigma, k_sigma, thr, cam.nearPlane, 7, dither)
+    fin = np.isfinite(ref)
+    if thr >= 0.1:
+        assert fin.all()
+    assert np.array_equal(np.isfinite(got), fin) and np.array_equal(np.isnan(got), np.isnan(ref))
+    assert np.array_equal(got[fin].view(np.uint32), ref[fin].view(np.uint32))
+    assert fin.mean() > 0.01
 
 
 def test_bilateral_smooths_a_flat_surface(ctx):
