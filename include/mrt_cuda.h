@@ -280,6 +280,10 @@ typedef struct mrt_tuning {
                                      two streams at once (a stream of the
                                      context joined before shading; same
                                      image)                                  */
+    uint32_t tail_from_hits;      /* 1: bounce tail_bounce is traced by the
+                                     wavefront kernel and the path tail
+                                     starts from its hits (shading that
+                                     bounce, its shadow rays and the rest)   */
 } mrt_tuning;
 int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning);
 int mrt_cuda_get_tuning(mrt_ctx* ctx, mrt_tuning* tuning);

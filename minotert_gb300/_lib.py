@@ -72,7 +72,7 @@ class Tuning(C.Structure):
     _fields_ = [("trace_blocks_per_sm", C.c_uint32), ("dynamic_fetch", C.c_uint32),
                 ("primary_persistent", C.c_uint32), ("sort_min_rays", C.c_uint32), ("tail_bounce", C.c_uint32),
                 ("stack_depth", C.c_uint32), ("tri_spread", C.c_uint32), ("refill_min", C.c_uint32),
-                ("overlap_shadow", C.c_uint32)]
+                ("overlap_shadow", C.c_uint32), ("tail_from_hits", C.c_uint32)]
 
 
 class CacheConfig(C.Structure):

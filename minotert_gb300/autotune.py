@@ -2,8 +2,9 @@
 
 Tunes persistent blocks per SM (warps per SM = 4 x blocks), the work-fetch
 mode of the persistent kernels, the primary-ray kernel form, the ray-sort
-threshold, the path tail, the spreading of triangle tests over the warp,
-the refill threshold and the overlapped shadow rays on a caller-supplied
+threshold, the path tail (and whether it starts from the wavefront's hits),
+the spreading of triangle tests over the warp, the refill threshold and the
+overlapped shadow rays on a caller-supplied
 frame function, timing each candidate with CUDA events on the frame's
 stream, and keeps the fastest.  The default search is coordinate-wise: from
 the current schedule, each knob in turn takes each of its values with the
@@ -41,6 +42,7 @@ def knobs(max_blocks_per_sm: int, sort: bool = False) -> dict:
         "refill_min": [8, 4, 12, 1],              # idle lanes before a refill
         "overlap_shadow": [1, 0],                 # shadow rays beside the next extension trace
         "tail_bounce": [3, 0, 2, 4],              # paths alive at this bounce finish in one launch
+        "tail_from_hits": [1, 0],                 # ... starting from that bounce's wavefront hits
         "primary_persistent": [0, 1],
         "sort_min_rays": [SORT_NEVER, 1 << 18, 1 << 14] if sort else [SORT_NEVER],
     }

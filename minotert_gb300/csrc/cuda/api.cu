@@ -314,6 +314,7 @@ int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning) {
     if (!ctx || !tuning) return fail(ctx, MRT_EINVAL, "set_tuning: null argument");
     if (tuning->trace_blocks_per_sm > 64 || tuning->dynamic_fetch > 3 || tuning->primary_persistent > 1 ||
         tuning->tail_bounce > MRT_MAX_BOUNCES || tuning->tri_spread > 7 || tuning->refill_min > 32 || tuning->overlap_shadow > 1 ||
+        tuning->tail_from_hits > 1 ||
         (tuning->stack_depth != 0u && tuning->stack_depth != 16u && tuning->stack_depth != 24u &&
          tuning->stack_depth != 32u))
         return fail(ctx, MRT_EINVAL, "set_tuning: value out of range");
@@ -702,7 +703,10 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
             // with overlap_shadow they run on two streams, so each fills the
             // GPU while the other drains.  Not before the path tail, whose
             // radiance additions must follow the shadow rays'.
-            const bool tail_now = tail != 0u && b >= tail;
+            // tail_from_hits: bounce b is still traced by the wavefront
+            // kernel and the tail starts from its hits (shading b onwards)
+            const bool tail_from_hits = ctx->tuning.tail_from_hits != 0u;
+            const bool tail_now = tail != 0u && b >= tail && !tail_from_hits;
             const bool overlap = nee && overlap_sh && !tail_now;
             if (overlap) {
                 MRT_CK(cudaEventRecord(ctx->ev_fork, s));
@@ -715,7 +719,7 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
                                                               ctx->counters, dyn_sh, refill_min(ctx), s));
             }
             if (tail_now) {
-                MRT_LAUNCH(1, int(b), launch_tail(scene->dev, tp, bn, wb, W, b, tblocks, ctx->d_status, s));
+                MRT_LAUNCH(1, int(b), launch_tail(scene->dev, tp, bn, wb, W, b, false, tblocks, ctx->d_status, s));
                 tail_done = true;
                 break;
             }
@@ -727,6 +731,11 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
             MRT_LAUNCH(1, int(b), launch_trace_ext(scene->dev, wb, b, tblocks, ctx->d_status, ctx->counters, dyn,
                                                    refill_min(ctx), s));
             if (overlap) MRT_CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
+            if (tail != 0u && b >= tail) {  // (tail_from_hits)
+                MRT_LAUNCH(1, int(b), launch_tail(scene->dev, tp, bn, wb, W, b, true, tblocks, ctx->d_status, s));
+                tail_done = true;
+                break;
+            }
             MRT_LAUNCH(3, int(b), launch_shade(scene->dev, tp, bn, wb, W, b, ctx->d_status, s));
         }
         if (nee && !tail_done)

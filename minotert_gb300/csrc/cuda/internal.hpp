@@ -168,9 +168,11 @@ cudaError_t launch_trace_shadow(const DevScene& sc, const WaveBuffers& wb, const
                                 uint32_t refill_min, cudaStream_t s);
 cudaError_t launch_shade(const DevScene& sc, const TraceParams& tp, BlueNoise bn, const WaveBuffers& wb,
                          uint32_t width, uint32_t bounce, uint32_t* status, cudaStream_t s);
-// every path of the bounce-`first` extension queue to its end (k_tail)
+// every path of the bounce-`first` extension queue to its end (k_tail);
+// from_hits: that queue's hits are already in wb.hits (traced by k_trace_ext)
 cudaError_t launch_tail(const DevScene& sc, const TraceParams& tp, BlueNoise bn, const WaveBuffers& wb,
-                        uint32_t width, uint32_t first, int blocks, uint32_t* status, cudaStream_t s);
+                        uint32_t width, uint32_t first, bool from_hits, int blocks, uint32_t* status,
+                        cudaStream_t s);
 cudaError_t launch_tally(const WaveBuffers& wb, cudaStream_t s);
 cudaError_t launch_sort_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t bounce, uint32_t min_rays,
                             cudaStream_t s);
@@ -225,7 +227,7 @@ struct mrt_ctx {
     // timing
     bool timing = false;
     bool counters = false;
-    mrt_tuning tuning{0u, 3u, 0u, mrt::kSortNever, 3u, 0u, 3u, 8u, 1u};  // autotuned on GB300 (icosphere field, 1080p)
+    mrt_tuning tuning{0u, 3u, 0u, mrt::kSortNever, 3u, 0u, 3u, 8u, 1u, 1u};  // autotuned on GB300 (icosphere field, 1080p)
     uint32_t* d_prim_fetch = nullptr;  // work counter of the persistent primary kernel
     int occ_blocks = 0;                // traversal blocks per SM at full occupancy
     unsigned long long* d_totals = nullptr;  // kTotSlots accumulated totals

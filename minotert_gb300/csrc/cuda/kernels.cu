@@ -649,11 +649,15 @@ k_trace_shadow(DevScene sc, WaveBuffers wb, TraceParams tp, uint32_t vertex, uin
 // resident blocks per SM): the tail is latency bound, and the traversal and
 // shading code together spill at 64.
 __global__ void __launch_bounds__(kTraceBlock, 4)
-k_tail(DevScene sc, TraceParams tp, BlueNoise bn, WaveBuffers wb, uint32_t width, uint32_t first, uint32_t* status) {
+k_tail(DevScene sc, TraceParams tp, BlueNoise bn, WaveBuffers wb, uint32_t width, uint32_t first, uint32_t from_hits,
+       uint32_t* status) {
     __shared__ uint2 stk[kStackDepth * kTraceBlock];
     const uint32_t n = wb.counters[kCntExt + first];
     const PathRay* q = ext_queue(wb, first);
-    uint32_t* fetch = wb.counters + kCntFetchExt + first;
+    // from_hits: k_trace_ext has used the queue's own work counter; the
+    // shadow-ray counter of vertex `first` is free (the tail traces those
+    // shadow rays itself)
+    uint32_t* fetch = wb.counters + (from_hits ? kCntFetchShadow : kCntFetchExt) + first;
     uint2* my = stk + threadIdx.x;
     const f3 sun{tp.sun[0], tp.sun[1], tp.sun[2]};
     uint32_t st = 0u, cn = 0u, ct = 0u;
@@ -668,7 +672,13 @@ k_tail(DevScene sc, TraceParams tp, BlueNoise bn, WaveBuffers wb, uint32_t width
         for (uint32_t b = first;; ++b) {
             uint32_t prim;
             float t;
-            trace_bvh8<false, false, kStackDepth>(sc, o, d, 0.0f, INFINITY, prim, t, my, kTraceBlock, st, cn, ct);
+            if (from_hits && b == first) {  // bounce `first` was traced by the wavefront kernel
+                const uint2 h = wb.hits[idx];
+                prim = h.x;
+                t = __uint_as_float(h.y);
+            } else {
+                trace_bvh8<false, false, kStackDepth>(sc, o, d, 0.0f, INFINITY, prim, t, my, kTraceBlock, st, cn, ct);
+            }
             if (prim == kMiss) {
                 add_L(wb.L, pix, mul_rn(beta, escape_radiance(tp, d)));
                 break;
@@ -844,8 +854,9 @@ cudaError_t launch_trace_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t
 }
 
 cudaError_t launch_tail(const DevScene& sc, const TraceParams& tp, BlueNoise bn, const WaveBuffers& wb,
-                        uint32_t width, uint32_t first, int blocks, uint32_t* status, cudaStream_t s) {
-    k_tail<<<blocks, kTraceBlock, 0, s>>>(sc, tp, bn, wb, width, first, status);
+                        uint32_t width, uint32_t first, bool from_hits, int blocks, uint32_t* status,
+                        cudaStream_t s) {
+    k_tail<<<blocks, kTraceBlock, 0, s>>>(sc, tp, bn, wb, width, first, from_hits ? 1u : 0u, status);
     return cudaGetLastError();
 }
 

@@ -10,9 +10,10 @@ from minotert_gb300.scene import DeviceScene
 pytestmark = pytest.mark.gpu
 
 
-def _render(ctx, ds, wl, bn, settings, tail):
+def _render(ctx, ds, wl, bn, settings, tail, from_hits=0):
     saved = int(ctx.tuning().tail_bounce)
-    ctx.set_tuning(tail_bounce=tail)
+    saved_fh = int(ctx.tuning().tail_from_hits)
+    ctx.set_tuning(tail_bounce=tail, tail_from_hits=from_hits)
     try:
         pt = Pathtracer(ctx, ds, full_gbuffer=False)
         pt.frame_counter = 4
@@ -22,7 +23,7 @@ def _render(ctx, ds, wl, bn, settings, tail):
         img = col.download(np.float32, (wl.height, wl.width, 3))
         st = ctx.frame_stats()
     finally:
-        ctx.set_tuning(tail_bounce=saved)
+        ctx.set_tuning(tail_bounce=saved, tail_from_hits=saved_fh)
     return img, list(st.extension_rays), int(st.shadow_rays)
 
 
@@ -31,12 +32,13 @@ def _render(ctx, ds, wl, bn, settings, tail):
 def test_tail_matches_wavefront(ctx, hf_workload, blue_noise, settings):
     wl, mesh, bvh = hf_workload
     ds = DeviceScene.triangles(ctx, mesh, bvh)
-    ref, ext, shadow = _render(ctx, ds, wl, blue_noise, settings, 0)
+    ref, ext, shadow = _render(ctx, ds, wl, blue_noise, settings, 0, 0)
     assert ext[0] > 0 and shadow > 0 and np.isfinite(ref).all()
     for tail in (1, 2, settings.bounces):
-        img, e, sh = _render(ctx, ds, wl, blue_noise, settings, tail)
-        assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), tail
-        assert e == ext and sh == shadow, tail
+        for fh in (0, 1):  # the tail traces bounce `tail` itself, or starts from its hits
+            img, e, sh = _render(ctx, ds, wl, blue_noise, settings, tail, fh)
+            assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), (tail, fh)
+            assert e == ext and sh == shadow, (tail, fh)
     assert ctx.status() == 0
 
 
