@@ -27,6 +27,9 @@ constexpr int kTraceBlock = 128;   // threads per traversal block
 constexpr int kStackDepth = MRT_TRACE_STACK;
 constexpr int kTraceMinBlocks = MRT_TRACE_MIN_BLOCKS;
 constexpr int kShadeBlock = 256;
+// The shading kernels wait on scattered loads (materials, RNG state, blue
+// noise): 4 blocks per SM (<= 64 registers) keep more of them in flight.
+constexpr int kShadeMinBlocks = 4;
 constexpr uint32_t kSortNever = 0xFFFFFFFFu;  // mrt_tuning.sort_min_rays: never sort
 
 // Wavefront records

@@ -396,7 +396,7 @@ MRT_DEV void emit(const VertexOut& vo, const WaveBuffers& wb, uint32_t vertex) {
 }
 
 // Vertex 0: the primary hit from the g-buffer (visibility + FP32 hit_t).
-__global__ void __launch_bounds__(kShadeBlock)
+__global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks)
 k_shade_primary(DevScene sc, FrameParams fp, mrt_gbuffer g, TraceParams tp, BlueNoise bn, WaveBuffers wb,
                 uint32_t sample, uint32_t* status) {
     const uint32_t npix = fp.width * fp.height;
@@ -426,7 +426,7 @@ k_shade_primary(DevScene sc, FrameParams fp, mrt_gbuffer g, TraceParams tp, Blue
 }
 
 // Vertex `vertex` >= 1: hits of the extension rays of bounce `vertex`.
-__global__ void __launch_bounds__(kShadeBlock)
+__global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks)
 k_shade(DevScene sc, TraceParams tp, BlueNoise bn, WaveBuffers wb, uint32_t width, uint32_t vertex,
         uint32_t* status) {
     const uint32_t n = wb.counters[kCntExt + vertex];
