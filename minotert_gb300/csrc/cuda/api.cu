@@ -682,13 +682,14 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
     const bool nee = tp.estimator == MRT_EST_NEE;
     const int dyn = fetch_mode(ctx, 0u), dyn_sh = fetch_mode(ctx, 1u);
     const bool overlap_sh = ctx->tuning.overlap_shadow != 0u && !ctx->counters;
-#define MRT_LAUNCH(kind, bounce, expr)                                                                   \
+#define MRT_LAUNCH_ON(st_, kind, bounce, expr)                                                           \
     do {                                                                                                 \
-        Scope sc_(ctx, s, kind, bounce);                                                                 \
+        Scope sc_(ctx, st_, kind, bounce);                                                               \
         cudaError_t e_ = (expr);                                                                         \
         if (e_ != cudaSuccess) return fail(ctx, MRT_ECUDA, "%s: %s", #expr, cudaGetErrorString(e_));    \
         ctx->launches++;                                                                                 \
     } while (0)
+#define MRT_LAUNCH(kind, bounce, expr) MRT_LAUNCH_ON(s, kind, bounce, expr)
     for (uint32_t smp = 0; smp < tp.samples; ++smp) {
         MRT_CK(cudaMemsetAsync(wb.counters, 0, kCntSlots * sizeof(uint32_t), s));
         MRT_LAUNCH(3, 0, launch_shade_primary(scene->dev, fp, *gbuffer, tp, bn, wb, smp, ctx->d_status, s));
@@ -711,8 +712,9 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
             if (overlap) {
                 MRT_CK(cudaEventRecord(ctx->ev_fork, s));
                 MRT_CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-                MRT_LAUNCH(2, int(b - 1), launch_trace_shadow(scene->dev, wb, tp, b - 1, tblocks, ctx->d_status,
-                                                              ctx->counters, dyn_sh, refill_min(ctx), ctx->side));
+                MRT_LAUNCH_ON(ctx->side, 2, int(b - 1),
+                              launch_trace_shadow(scene->dev, wb, tp, b - 1, tblocks, ctx->d_status, ctx->counters,
+                                                  dyn_sh, refill_min(ctx), ctx->side));
                 MRT_CK(cudaEventRecord(ctx->ev_join, ctx->side));
             } else if (nee) {
                 MRT_LAUNCH(2, int(b - 1), launch_trace_shadow(scene->dev, wb, tp, b - 1, tblocks, ctx->d_status,
@@ -746,6 +748,7 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
     }
     MRT_LAUNCH(3, 0, launch_finalize(wb, color, tp.samples, params->accumulate, params->frame_index, s));
 #undef MRT_LAUNCH
+#undef MRT_LAUNCH_ON
     return MRT_OK;
 }
 
