@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import oracle
-from conftest import oracle_consts
+from conftest import oracle_consts, random_rays
 from minotert_gb300.pathtracer import Camera, Pathtracer, TraceSettings
 from minotert_gb300.scene import DeviceScene
 
@@ -100,3 +100,43 @@ def test_overlapped_shadow_rays_same_image(ctx, hf_workload, blue_noise, tail):
     assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
     assert e == ext and sh == shadow
     assert ctx.status() == 0
+
+
+def test_corrupt_bvh_in_the_path_tracer(ctx, hf_workload, blue_noise):
+    # host-side fault injection through the default schedule (spread
+    # triangle tests, overlapped shadow rays, path tail) and the batched
+    # kernels: a child or triangle index out of range, or a self-referencing
+    # child, ends in a status flag; the context keeps working
+    from minotert_gb300._lib import MRT_STATUS_BAD_NODE, MRT_STATUS_BAD_TRI
+    from minotert_gb300.scene import Bvh8, DeviceBatch
+    wl, mesh, bvh = hf_workload
+    settings = TraceSettings(samples=1, bounces=4, rr_start=2, rng_mode=1)
+    ref, ext, shadow = _render(ctx, DeviceScene.triangles(ctx, mesh, bvh), wl, blue_noise, settings, 3, 3)
+    assert ctx.status() == 0
+    cases = []
+    nodes = bvh.nodes.copy()
+    nodes["child_base"][0] = len(nodes) + 1000
+    cases.append((nodes, MRT_STATUS_BAD_NODE))
+    nodes = bvh.nodes.copy()
+    nodes["tri_base"][:] = len(bvh.tris) + 7
+    cases.append((nodes, MRT_STATUS_BAD_TRI))
+    nodes = bvh.nodes.copy()
+    nodes["child_base"][:] = 0
+    cases.append((nodes, 0))
+    for nodes, flag in cases:
+        bad = Bvh8(nodes, bvh.tris, bvh.depth, bvh.leaf_count, 0.0)
+        _render(ctx, DeviceScene.triangles(ctx, mesh, bad), wl, blue_noise, settings, 3, 3)
+        ctx.sync(timeout_s=30.0)
+        st = ctx.status()
+        assert st != 0 and (flag == 0 or st & flag), (flag, st)
+        batch = DeviceBatch(ctx, [(mesh, bvh), (mesh, bad)])
+        rays = np.concatenate([random_rays(2048, mesh.lo, mesh.hi, seed=3)] * 2)
+        offsets = np.array([0, 2048, 4096], np.uint32)
+        d_rays = ctx.to_device(rays)
+        batch.trace(d_rays, offsets, ctx.alloc(8 * len(rays)))
+        batch.pathtrace(d_rays, offsets, settings.params(wl.sky), 1, ctx.alloc(12 * len(rays)), use_graph=False)
+        ctx.sync(timeout_s=30.0)
+        assert ctx.status() != 0
+    img, e, sh = _render(ctx, DeviceScene.triangles(ctx, mesh, bvh), wl, blue_noise, settings, 3, 3)
+    assert ctx.status() == 0
+    assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)) and e == ext and sh == shadow
