@@ -265,11 +265,11 @@ typedef struct mrt_tuning {
                                      deepest BVH (depth - 1 entries)         */
     uint32_t tri_spread;          /* bit 0: extension rays, bit 1: shadow rays
                                      (with dynamic_fetch set for them), bit 2:
-                                     primary rays (one thread per pixel): the
-                                     triangle tests of a traversal step are
-                                     spread over the warp's lanes instead of
-                                     each lane testing its own leaves' (same
-                                     hits)                                   */
+                                     primary rays (one thread per pixel), bit
+                                     3: the path tail: the triangle tests of
+                                     a traversal step are spread over the
+                                     warp's lanes instead of each lane
+                                     testing its own leaves' (same hits)     */
     uint32_t refill_min;          /* kernels with dynamic fetch (and the
                                      batched ones): a warp fetches new rays
                                      once at least this many of its lanes

@@ -38,7 +38,7 @@ def knobs(max_blocks_per_sm: int, sort: bool = False) -> dict:
     return {
         "trace_blocks_per_sm": blocks,            # 0 = occupancy maximum
         "dynamic_fetch": [3, 1, 0, 2],            # bit 0 extension, bit 1 shadow rays
-        "tri_spread": [3, 1, 0, 7],               # bit 0 extension, 1 shadow, 2 primary rays
+        "tri_spread": [11, 3, 1, 0, 15],          # bit 0 extension, 1 shadow, 2 primary rays, 3 the tail
         "refill_min": [8, 4, 12, 1],              # idle lanes before a refill
         "overlap_shadow": [1, 0],                 # shadow rays beside the next extension trace
         "tail_bounce": [3, 0, 2, 4],              # paths alive at this bounce finish in one launch

@@ -313,7 +313,7 @@ static uint32_t refill_min(const mrt_ctx* ctx) { return ctx->tuning.refill_min ?
 int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning) {
     if (!ctx || !tuning) return fail(ctx, MRT_EINVAL, "set_tuning: null argument");
     if (tuning->trace_blocks_per_sm > 64 || tuning->dynamic_fetch > 3 || tuning->primary_persistent > 1 ||
-        tuning->tail_bounce > MRT_MAX_BOUNCES || tuning->tri_spread > 7 || tuning->refill_min > 32 || tuning->overlap_shadow > 1 ||
+        tuning->tail_bounce > MRT_MAX_BOUNCES || tuning->tri_spread > 15 || tuning->refill_min > 32 || tuning->overlap_shadow > 1 ||
         tuning->tail_from_hits > 1 ||
         (tuning->stack_depth != 0u && tuning->stack_depth != 16u && tuning->stack_depth != 24u &&
          tuning->stack_depth != 32u))
@@ -721,7 +721,8 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
                                                               ctx->counters, dyn_sh, refill_min(ctx), s));
             }
             if (tail_now) {
-                MRT_LAUNCH(1, int(b), launch_tail(scene->dev, tp, bn, wb, W, b, false, tblocks, ctx->d_status, s));
+                MRT_LAUNCH(1, int(b), launch_tail(scene->dev, tp, bn, wb, W, b, false, (ctx->tuning.tri_spread & 8u) != 0u,
+                                                  tblocks, ctx->d_status, s));
                 tail_done = true;
                 break;
             }
@@ -734,7 +735,8 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
                                                    refill_min(ctx), s));
             if (overlap) MRT_CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
             if (tail != 0u && b >= tail) {  // (tail_from_hits)
-                MRT_LAUNCH(1, int(b), launch_tail(scene->dev, tp, bn, wb, W, b, true, tblocks, ctx->d_status, s));
+                MRT_LAUNCH(1, int(b), launch_tail(scene->dev, tp, bn, wb, W, b, true, (ctx->tuning.tri_spread & 8u) != 0u,
+                                                  tblocks, ctx->d_status, s));
                 tail_done = true;
                 break;
             }

@@ -174,7 +174,7 @@ cudaError_t launch_shade(const DevScene& sc, const TraceParams& tp, BlueNoise bn
 // every path of the bounce-`first` extension queue to its end (k_tail);
 // from_hits: that queue's hits are already in wb.hits (traced by k_trace_ext)
 cudaError_t launch_tail(const DevScene& sc, const TraceParams& tp, BlueNoise bn, const WaveBuffers& wb,
-                        uint32_t width, uint32_t first, bool from_hits, int blocks, uint32_t* status,
+                        uint32_t width, uint32_t first, bool from_hits, bool spread, int blocks, uint32_t* status,
                         cudaStream_t s);
 cudaError_t launch_tally(const WaveBuffers& wb, cudaStream_t s);
 cudaError_t launch_sort_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t bounce, uint32_t min_rays,
@@ -230,7 +230,7 @@ struct mrt_ctx {
     // timing
     bool timing = false;
     bool counters = false;
-    mrt_tuning tuning{0u, 3u, 0u, mrt::kSortNever, 3u, 0u, 3u, 8u, 1u, 1u};  // autotuned on GB300 (icosphere field, 1080p)
+    mrt_tuning tuning{0u, 3u, 0u, mrt::kSortNever, 3u, 0u, 11u, 8u, 1u, 1u};  // autotuned on GB300 (icosphere field, 1080p)
     uint32_t* d_prim_fetch = nullptr;  // work counter of the persistent primary kernel
     int occ_blocks = 0;                // traversal blocks per SM at full occupancy
     unsigned long long* d_totals = nullptr;  // kTotSlots accumulated totals

@@ -853,10 +853,105 @@ cudaError_t launch_trace_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t
     return cudaGetLastError();
 }
 
+// The path tail with the traversal steps of a warp's lanes taken together
+// (trav_step_spread_mixed): each lane is a small state machine -- idle,
+// tracing its path's extension ray (closest hit) or its vertex's shadow ray
+// (any hit) -- and every iteration the warp refills idle lanes, then takes
+// one traversal step of all its rays with the triangle tests spread over
+// the lanes.  The shading, the counters and a pixel's radiance additions
+// happen in k_tail's order, so the image is the same.
+__global__ void __launch_bounds__(kTraceBlock, 4)
+k_tail_spread(DevScene sc, TraceParams tp, BlueNoise bn, WaveBuffers wb, uint32_t width, uint32_t first,
+              uint32_t from_hits, uint32_t* status) {
+    __shared__ uint2 stk[kStackDepth * kTraceBlock];
+    __shared__ unsigned long long slots[kTraceBlock];
+    const uint32_t n = wb.counters[kCntExt + first];
+    const PathRay* q = ext_queue(wb, first);
+    uint32_t* fetch = wb.counters + (from_hits ? kCntFetchShadow : kCntFetchExt) + first;
+    uint2* my = stk + threadIdx.x;
+    unsigned long long* wslots = slots + (threadIdx.x & ~31u);
+    const f3 sun{tp.sun[0], tp.sun[1], tp.sun[2]};
+    uint32_t st = 0u;
+    bool exhausted = false;
+    int mode = 0;  // 0 idle, 1 extension ray, 2 shadow ray
+    Trav s{};
+    uint32_t pix = 0u, b = 0u;
+    f3 o{0.0f, 0.0f, 0.0f}, d{0.0f, 0.0f, 1.0f}, beta{0.0f, 0.0f, 0.0f}, contrib{0.0f, 0.0f, 0.0f};
+    bool next_ext = false;
+    f3 no{0.0f, 0.0f, 0.0f}, nd{0.0f, 0.0f, 1.0f}, nbeta{0.0f, 0.0f, 0.0f};
+    // after the shadow ray of vertex b (or without one): the next bounce
+    auto cont = [&]() {
+        if (!next_ext) { mode = 0; return; }
+        atomicAdd(wb.counters + kCntExt + b + 1u, 1u);
+        o = no; d = nd; beta = nbeta;
+        ++b;
+        trav_init(s, o, d, 0.0f, INFINITY);
+        mode = 1;
+    };
+    // the extension ray of bounce b found `prim` at t (or escaped)
+    auto hit = [&](uint32_t prim, float t) {
+        if (prim == kMiss) {
+            add_L(wb.L, pix, mul_rn(beta, escape_radiance(tp, d)));
+            mode = 0;
+            return;
+        }
+        uint32_t rng = wb.rng[pix];
+        const VertexOut vo = shade_vertex(sc, tp, bn, width, b, pix, ray_at(o, d, t), d, prim, beta, rng, status);
+        wb.rng[pix] = rng;
+        next_ext = vo.ext;
+        no = f3{vo.pr.o_pix.x, vo.pr.o_pix.y, vo.pr.o_pix.z};
+        nd = f3{vo.pr.d.x, vo.pr.d.y, vo.pr.d.z};
+        nbeta = f3{vo.pr.beta.x, vo.pr.beta.y, vo.pr.beta.z};
+        if (vo.shadow) {
+            atomicAdd(wb.counters + kCntShadow + b, 1u);
+            contrib = f3{vo.sr.contrib.x, vo.sr.contrib.y, vo.sr.contrib.z};
+            trav_init(s, f3{vo.sr.o_pix.x, vo.sr.o_pix.y, vo.sr.o_pix.z}, sun, 0.0f, INFINITY);
+            mode = 2;
+        } else {
+            cont();
+        }
+    };
+    while (true) {
+        const uint32_t idx = warp_refill(fetch, n, mode == 0, exhausted);
+        if (idx != kMiss) {
+            const PathRay pr = q[idx];
+            pix = __float_as_uint(pr.o_pix.w);
+            o = f3{pr.o_pix.x, pr.o_pix.y, pr.o_pix.z};
+            d = f3{pr.d.x, pr.d.y, pr.d.z};
+            beta = f3{pr.beta.x, pr.beta.y, pr.beta.z};
+            b = first;
+            if (from_hits) {
+                const uint2 h = wb.hits[idx];
+                hit(h.x, __uint_as_float(h.y));
+            } else {
+                trav_init(s, o, d, 0.0f, INFINITY);
+                mode = 1;
+            }
+        }
+        if (!__any_sync(0xFFFFFFFFu, mode != 0)) {
+            if (exhausted) break;
+            continue;
+        }
+        const bool busy = mode != 0;
+        if (trav_step_spread_mixed<kStackDepth>(sc, s, busy, mode == 2, my, kTraceBlock, st, wslots) && busy) {
+            if (mode == 1) {
+                hit(s.best, s.best == kMiss ? s.tmax : s.tbest);
+            } else {
+                if (s.best == kMiss) add_L(wb.L, pix, contrib);
+                cont();
+            }
+        }
+    }
+    if (st) atomicOr(status, st);
+}
+
 cudaError_t launch_tail(const DevScene& sc, const TraceParams& tp, BlueNoise bn, const WaveBuffers& wb,
-                        uint32_t width, uint32_t first, bool from_hits, int blocks, uint32_t* status,
+                        uint32_t width, uint32_t first, bool from_hits, bool spread, int blocks, uint32_t* status,
                         cudaStream_t s) {
-    k_tail<<<blocks, kTraceBlock, 0, s>>>(sc, tp, bn, wb, width, first, from_hits ? 1u : 0u, status);
+    if (spread)
+        k_tail_spread<<<blocks, kTraceBlock, 0, s>>>(sc, tp, bn, wb, width, first, from_hits ? 1u : 0u, status);
+    else
+        k_tail<<<blocks, kTraceBlock, 0, s>>>(sc, tp, bn, wb, width, first, from_hits ? 1u : 0u, status);
     return cudaGetLastError();
 }
 

@@ -407,6 +407,103 @@ MRT_DEV bool trav_step_spread(const DevScene& sc, Trav& s, bool have, uint2* stk
     return done;
 }
 
+// trav_step_spread for lanes that mix closest-hit and any-hit queries
+// (any_hit per lane; the path tail's lanes are at different points of
+// their paths).  The same steps, with the owner's kind read by a shuffle.
+template <int kStack>
+MRT_DEV bool trav_step_spread_mixed(const DevScene& sc, Trav& s, bool have, bool any_hit, uint2* stk,
+                                    uint32_t stride, uint32_t& status, unsigned long long* slot) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t tri_mask = 0u, tri_base = 0u;
+    bool done = false;
+    if (have) {
+        uint32_t node;
+        if (next_node<kStack>(sc, s, stk, stride, status, node)) tri_mask = visit_node(sc, s, node, tri_base);
+        else done = true;
+    }
+    const uint32_t cnt = __popc(tri_mask);
+    uint32_t incl = cnt;
+#pragma unroll
+    for (uint32_t o = 1; o < 32u; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    if (total) {
+        const uint32_t excl = incl - cnt;
+        if (cnt)
+            slot[lane] = any_hit ? ~0ull
+                                 : ((unsigned long long)float_key(s.tbest) << 32) | (unsigned long long)s.best;
+        __syncwarp();
+        const uint32_t kpack = uint32_t(s.r.kx) | (uint32_t(s.r.ky) << 2) | (uint32_t(s.r.kz) << 4);
+        for (uint32_t c = 0; c < total; c += 32u) {
+            const uint32_t p = c + lane;
+            uint32_t own = 0u;  // the last lane whose exclusive sum is <= p
+#pragma unroll
+            for (uint32_t step = 16u; step >= 1u; step >>= 1) {
+                const uint32_t e = __shfl_sync(0xFFFFFFFFu, excl, int(own + step));
+                if (e <= p) own += step;
+            }
+            RayPre r;
+            r.okx = __shfl_sync(0xFFFFFFFFu, s.r.okx, int(own));
+            r.oky = __shfl_sync(0xFFFFFFFFu, s.r.oky, int(own));
+            r.okz = __shfl_sync(0xFFFFFFFFu, s.r.okz, int(own));
+            r.sx = __shfl_sync(0xFFFFFFFFu, s.r.sx, int(own));
+            r.sy = __shfl_sync(0xFFFFFFFFu, s.r.sy, int(own));
+            r.sz = __shfl_sync(0xFFFFFFFFu, s.r.sz, int(own));
+            const uint32_t kp = __shfl_sync(0xFFFFFFFFu, kpack, int(own));
+            r.kx = int(kp & 3u);
+            r.ky = int((kp >> 2) & 3u);
+            r.kz = int(kp >> 4);
+            const float tmin = __shfl_sync(0xFFFFFFFFu, s.tmin, int(own));
+            const bool own_any = __shfl_sync(0xFFFFFFFFu, uint32_t(any_hit), int(own)) != 0u;
+            const float tmax = __shfl_sync(0xFFFFFFFFu, s.tmax, int(own));
+            const uint32_t m = __shfl_sync(0xFFFFFFFFu, tri_mask, int(own));
+            const uint32_t base = __shfl_sync(0xFFFFFFFFu, tri_base, int(own));
+            const uint32_t e0 = __shfl_sync(0xFFFFFFFFu, excl, int(own));
+            if (p < total) {
+                const uint32_t bit = __fns(m, 0u, int(p - e0) + 1);
+                const uint32_t ti = base + bit;
+                if (ti >= sc.tri_count) {
+                    status |= MRT_STATUS_BAD_TRI;
+                    atomicMin(slot + own, 0ull);
+                } else {
+                    const float4* tp = sc.tris + size_t(ti) * 3u;
+                    const float4 a = __ldg(tp + 0), b = __ldg(tp + 1), cc = __ldg(tp + 2);
+                    float t;
+                    if (intersect_tri(r, a, b, cc, tmin, t)) {
+                        if (own_any) {
+                            if (t < tmax)
+                                atomicMin(slot + own, ((unsigned long long)(bit + 1u) << 32) | __float_as_uint(t));
+                        } else {
+                            atomicMin(slot + own, ((unsigned long long)float_key(t) << 32) |
+                                                      (unsigned long long)__float_as_uint(a.w));
+                        }
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if (cnt) {
+            const unsigned long long k = slot[lane];
+            if (k == 0ull) {
+                done = true;
+            } else if (any_hit) {
+                if (k != ~0ull) {
+                    s.tbest = __uint_as_float(uint32_t(k));
+                    s.best = __float_as_uint(__ldg(sc.tris + size_t(tri_base + uint32_t(k >> 32) - 1u) * 3u).w);
+                    done = true;
+                }
+            } else {
+                s.tbest = key_float(uint32_t(k >> 32));
+                s.best = uint32_t(k);
+            }
+        }
+    }
+    if (have && !done) done = s.g_hits == 0u && s.sp == 0;
+    return done;
+}
+
 // Closest hit (kAnyHit = false) or first hit with t < tmax (kAnyHit = true)
 // of one ray, run to completion.
 template <bool kAnyHit, bool kCount, int kStack>

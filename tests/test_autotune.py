@@ -40,6 +40,6 @@ def test_knob_values_are_valid_tuning_fields():
     k = autotune.knobs(8, sort=True)
     assert set(k) <= fields
     assert all(0 <= v <= 64 for v in k["trace_blocks_per_sm"])
-    assert set(k["dynamic_fetch"]) <= {0, 1, 2, 3} and set(k["tri_spread"]) <= set(range(8))
+    assert set(k["dynamic_fetch"]) <= {0, 1, 2, 3} and set(k["tri_spread"]) <= set(range(16))
     assert all(1 <= v <= 32 for v in k["refill_min"]) and set(k["overlap_shadow"]) <= {0, 1}
     assert all(0 <= v <= 16 for v in k["tail_bounce"]) and set(k["tail_from_hits"]) <= {0, 1}

@@ -52,7 +52,7 @@ def test_spread_range(ctx):
     from minotert_gb300._lib import MrtError
     saved = int(ctx.tuning().tri_spread)
     with pytest.raises(MrtError):
-        ctx.set_tuning(tri_spread=8)
+        ctx.set_tuning(tri_spread=16)
     ctx.set_tuning(tri_spread=saved)
     saved = int(ctx.tuning().refill_min)
     with pytest.raises(MrtError):

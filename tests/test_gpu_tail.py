@@ -10,10 +10,11 @@ from minotert_gb300.scene import DeviceScene
 pytestmark = pytest.mark.gpu
 
 
-def _render(ctx, ds, wl, bn, settings, tail, from_hits=0):
+def _render(ctx, ds, wl, bn, settings, tail, from_hits=0, spread=0):
     saved = int(ctx.tuning().tail_bounce)
     saved_fh = int(ctx.tuning().tail_from_hits)
-    ctx.set_tuning(tail_bounce=tail, tail_from_hits=from_hits)
+    saved_sp = int(ctx.tuning().tri_spread)
+    ctx.set_tuning(tail_bounce=tail, tail_from_hits=from_hits, tri_spread=(saved_sp & 7) | (8 if spread else 0))
     try:
         pt = Pathtracer(ctx, ds, full_gbuffer=False)
         pt.frame_counter = 4
@@ -23,7 +24,7 @@ def _render(ctx, ds, wl, bn, settings, tail, from_hits=0):
         img = col.download(np.float32, (wl.height, wl.width, 3))
         st = ctx.frame_stats()
     finally:
-        ctx.set_tuning(tail_bounce=saved, tail_from_hits=saved_fh)
+        ctx.set_tuning(tail_bounce=saved, tail_from_hits=saved_fh, tri_spread=saved_sp)
     return img, list(st.extension_rays), int(st.shadow_rays)
 
 
@@ -36,9 +37,10 @@ def test_tail_matches_wavefront(ctx, hf_workload, blue_noise, settings):
     assert ext[0] > 0 and shadow > 0 and np.isfinite(ref).all()
     for tail in (1, 2, settings.bounces):
         for fh in (0, 1):  # the tail traces bounce `tail` itself, or starts from its hits
-            img, e, sh = _render(ctx, ds, wl, blue_noise, settings, tail, fh)
-            assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), (tail, fh)
-            assert e == ext and sh == shadow, (tail, fh)
+            for sp in (0, 1):  # per-lane paths, or the warp's steps taken together
+                img, e, sh = _render(ctx, ds, wl, blue_noise, settings, tail, fh, sp)
+                assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), (tail, fh, sp)
+                assert e == ext and sh == shadow, (tail, fh, sp)
     assert ctx.status() == 0
 
 
