@@ -180,7 +180,14 @@ typedef struct mrt_trace_params {
     uint32_t frame_index;  /* frames already in the running mean             */
     uint32_t sort_rays;    /* 1: sort extension rays between bounces         */
     float    sun_dir[3];   /* unit vector toward the directional light       */
-    float    pad0;
+    uint32_t exact_trig;   /* 1: the sphere-point sampler's sine and cosine
+                              (random.glsl:10-19) are evaluated in binary64
+                              and rounded once to binary32, as the CPU
+                              oracle does, so path-traced colour matches it
+                              bit for bit (up to a binary64 result lying
+                              within a few binary64 ulps of a binary32
+                              rounding boundary, about 1e-8 of calls);
+                              0: CUDA sincosf (default, faster)             */
     float    sun_irradiance[3];
     float    pad1;
     float    sky_radiance[3]; /* constant radiance of escaping rays          */
@@ -297,6 +304,15 @@ typedef struct mrt_device_info {
     uint64_t l2_bytes;
 } mrt_device_info;
 int mrt_cuda_device_info(mrt_ctx* ctx, mrt_device_info* out);
+
+/* Read-bandwidth sweep (new; a measurement aid with no counterpart in the
+ * reference): `passes` sweeps of 16-byte loads that bypass L1 over `bytes`
+ * of the device buffer `buf` (16-byte aligned), by min(sink_words, 8 x SMs)
+ * blocks, each XOR-folding what it read into sink[block].  On a buffer that
+ * fits in L2, time it with events to get the L2 read bandwidth that bounds
+ * the traversal kernels, whose scene stays L2-resident. */
+int mrt_cuda_read_sweep(mrt_ctx* ctx, const void* buf, size_t bytes, uint32_t passes,
+                        uint32_t* sink, uint32_t sink_words, void* stream);
 
 /* ---- memory and streams (the reference's vuk allocator role,
  *      renderer.ixx:42-43) --------------------------------------------- */
@@ -636,24 +652,30 @@ int mrt_cuda_reproject(mrt_ctx* ctx, const mrt_gbuffer* cur, const mrt_gbuffer* 
  * cudaFree, no allocating library call.
  *
  * It runs the persistent dynamic-fetch primary-ray kernel, whose work
- * counter (and, when `status` is NULL, its status word) live in a
- * file-scope device array of 256 bytes that every GPU loading the library
- * holds until the process exits.  The results equal mrt_cuda_primary_rays.
+ * counter lives in a file-scope device array of 256 bytes that every GPU
+ * loading the library holds until the process exits.  The results equal
+ * mrt_cuda_primary_rays.
  *
- *   - Works on the calling thread's current CUDA device.  The first call on
- *     a device looks up that device's copy of the array and its launch
- *     size; make that first call before any stream capture.
+ *   - Works in the calling thread's current CUDA context (the runtime's
+ *     primary context of the current device when none is current).  The
+ *     first call in a context looks up that context's copy of the array and
+ *     the launch size; make that first call before any stream capture.  A
+ *     context created later (after cudaDeviceReset, or a caller's own
+ *     driver-API context) gets its own look-up on its first call.
  *   - width * height must be at most MRT_NOALLOC_MAX_PIXELS; larger images
  *     return MRT_ERANGE and launch nothing.
- *   - All calls on a device share the one array, which keeps the previous
+ *   - All calls in a context share the one array, which keeps the previous
  *     call's contents; each call clears what must start at zero on
  *     `stream`.  Calls whose work overlaps on the GPU (other streams, other
  *     threads) race on the array: serialise them.
- *   - `status` (device, may be NULL) receives MRT_STATUS_* bits ORed in;
- *     the caller clears it.  BVH depth is not checked on the host here (the
- *     device stack check reports MRT_STATUS_STACK_OVF instead).
- * Returns MRT_OK, MRT_EINVAL (null pointer, zero size), MRT_ERANGE (too
- * large) or MRT_ECUDA. */
+ *   - `status` (device, required) receives MRT_STATUS_* bits ORed in; the
+ *     caller clears it and reads it back.  BVH depth is not checked on the
+ *     host here: a BVH deeper than the traversal stack reports
+ *     MRT_STATUS_STACK_OVF in `status`, and out-of-range node or triangle
+ *     indices report MRT_STATUS_BAD_NODE / MRT_STATUS_BAD_TRI; the g-buffer
+ *     is not to be trusted when any bit is set.
+ * Returns MRT_OK, MRT_EINVAL (null pointer, including `status`, or zero
+ * size), MRT_ERANGE (too large) or MRT_ECUDA. */
 #define MRT_NOALLOC_MAX_PIXELS (1u << 26)
 int mrt_cuda_primary_rays_noalloc(const mrt_bvh8_node* nodes, uint32_t node_count,
                                   const mrt_tri* tris, uint32_t tri_count,

@@ -54,7 +54,7 @@ class TraceParams(C.Structure):
     _fields_ = [("samples", C.c_uint32), ("max_bounces", C.c_uint32), ("rr_start", C.c_uint32),
                 ("rng_mode", C.c_uint32), ("estimator", C.c_uint32), ("accumulate", C.c_uint32),
                 ("frame_index", C.c_uint32), ("sort_rays", C.c_uint32), ("sun_dir", C.c_float * 3),
-                ("pad0", C.c_float), ("sun_irradiance", C.c_float * 3), ("pad1", C.c_float),
+                ("exact_trig", C.c_uint32), ("sun_irradiance", C.c_float * 3), ("pad1", C.c_float),
                 ("sky_radiance", C.c_float * 3), ("pad2", C.c_float)]
 
 
@@ -157,6 +157,7 @@ def lib() -> C.CDLL:
             "mrt_cuda_get_tuning": ([vp, C.POINTER(Tuning)], i32),
             "mrt_cuda_device_info": ([vp, C.POINTER(DeviceInfo)], i32),
             "mrt_cuda_frame_stats": ([vp, C.POINTER(FrameStats)], i32),
+            "mrt_cuda_read_sweep": ([vp, vp, sz, u32, vp, u32, vp], i32),
             "mrt_cuda_alloc": ([vp, sz, pp], i32),
             "mrt_cuda_free": ([vp, vp], i32),
             "mrt_cuda_host_alloc": ([vp, sz, pp], i32),

@@ -68,6 +68,7 @@ TraceParams trace_params(const mrt_trace_params* p) {
     t.rr_start = p->rr_start;
     t.rng_mode = p->rng_mode;
     t.estimator = p->estimator;
+    t.exact_trig = p->exact_trig;
     for (int k = 0; k < 3; ++k) {
         t.sun[k] = p->sun_dir[k];
         t.sun_e[k] = p->sun_irradiance[k];

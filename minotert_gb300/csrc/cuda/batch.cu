@@ -244,7 +244,7 @@ k_batch_shade(DevScene sc, const TraceParams* tpp, const PathRay* qin, PathRay* 
                     uint32_t s = rng[idx];
                     const float u1 = random_float(s), u2 = random_float(s);
                     const f3 sp = random_sphere_point(__fsub_rn(__fmul_rn(u1, 2.0f), 1.0f),
-                                                      __fsub_rn(__fmul_rn(u2, 2.0f), 1.0f));
+                                                      __fsub_rn(__fmul_rn(u2, 2.0f), 1.0f), tp.exact_trig);
                     f3 nd = add_rn(nrm, sp);
                     if (dot_rn(nd, nd) == 0.0f) nd = nrm;
                     nd = normalize_rn(nd);

@@ -62,15 +62,25 @@ MRT_DEV float rotated_random(uint32_t& s, float rot) {
     float x = __fadd_rn(random_float(s), rot);
     return __fsub_rn(x, floorf(x));
 }
-// uniform point on the unit sphere from (x, y) in [-1,1)^2 (random.glsl:10-19)
-MRT_DEV f3 random_sphere_point(float rx, float ry) {
+// sin and cos of a binary32 angle evaluated in binary64 and rounded once
+// to binary32 -- the CPU oracle's evaluation.  Out of line so the default
+// (sincosf) path of the register-capped kernels does not carry it.
+static __device__ __noinline__ void sincos_binary64(float a, float* sn, float* cs) {
+    *sn = float(sin(double(a)));
+    *cs = float(cos(double(a)));
+}
+
+// uniform point on the unit sphere from (x, y) in [-1,1)^2 (random.glsl:10-19);
+// exact: sin/cos through sincos_binary64 (mrt_trace_params.exact_trig)
+MRT_DEV f3 random_sphere_point(float rx, float ry, uint32_t exact = 0u) {
     const float Pi = 3.14159265359f;
     float ang1 = __fmul_rn(__fadd_rn(rx, 1.0f), Pi);
     float u = ry;
     float u2 = __fmul_rn(u, u);
     float s = __fsqrt_rn(__fsub_rn(1.0f, u2));
     float sn, cs;
-    sincosf(ang1, &sn, &cs);
+    if (exact) sincos_binary64(ang1, &sn, &cs);
+    else sincosf(ang1, &sn, &cs);
     return f3{__fmul_rn(s, cs), __fmul_rn(s, sn), u};
 }
 

@@ -114,6 +114,7 @@ MRT_DEV f3 ray_at(f3 o, f3 d, float t) { return add_rn(o, scale_rn(d, t)); } // 
 
 struct TraceParams {
     uint32_t samples, max_bounces, rr_start, rng_mode, estimator;
+    uint32_t exact_trig;  // mrt_trace_params.exact_trig
     float sun[3], sun_e[3], sky[3];
     SkyDev atmo;  // atmosphere miss shader; atmo.view == nullptr: constant sky
 };

@@ -263,7 +263,7 @@ k_secondary_sphere(DevScene sc, FrameParams fp, mrt_gbuffer g, TraceParams tp, B
                 const float u1 = rotated_random(rng, rot.x);
                 const float u2 = rotated_random(rng, rot.y);
                 const f3 sp = random_sphere_point(__fsub_rn(__fmul_rn(u1, 2.0f), 1.0f),
-                                                  __fsub_rn(__fmul_rn(u2, 2.0f), 1.0f));
+                                                  __fsub_rn(__fmul_rn(u2, 2.0f), 1.0f), tp.exact_trig);
                 const f3 rd = normalize_rn(add_rn(hn, sp));
                 hprim = kMiss;
                 float ht = -1.0f;
@@ -360,7 +360,8 @@ MRT_DEV VertexOut shade_vertex(const DevScene& sc, const TraceParams& tp, const 
     const float2 rot = bn_rot(bn, pix % width, pix / width);
     const float u1 = rotated_random(rng, rot.x);
     const float u2 = rotated_random(rng, rot.y);
-    const f3 sp = random_sphere_point(__fsub_rn(__fmul_rn(u1, 2.0f), 1.0f), __fsub_rn(__fmul_rn(u2, 2.0f), 1.0f));
+    const f3 sp = random_sphere_point(__fsub_rn(__fmul_rn(u1, 2.0f), 1.0f), __fsub_rn(__fmul_rn(u2, 2.0f), 1.0f),
+                                      tp.exact_trig);
     f3 nd = add_rn(n, sp);
     if (dot_rn(nd, nd) == 0.0f) nd = n;
     nd = normalize_rn(nd);
@@ -1048,7 +1049,7 @@ k_cache_train_paths(DevScene sc, FrameParams fp, TraceParams tp, uint32_t bounce
         if (v >= maxb) break;
         const float u1 = random_float(rng), u2 = random_float(rng);
         f3 nd = add_rn(n, random_sphere_point(__fsub_rn(__fmul_rn(u1, 2.0f), 1.0f),
-                                              __fsub_rn(__fmul_rn(u2, 2.0f), 1.0f)));
+                                              __fsub_rn(__fmul_rn(u2, 2.0f), 1.0f), tp.exact_trig));
         if (dot_rn(nd, nd) == 0.0f) nd = n;
         nd = normalize_rn(nd);
         float w = 1.0f;

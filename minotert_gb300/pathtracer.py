@@ -95,6 +95,7 @@ class TraceSettings:
     accumulate: bool = False
     frame_index: int = 0
     sort_rays: bool = False
+    exact_trig: bool = False  # sphere-point sin/cos in binary64 (the oracle's), see mrt_trace_params
 
     def params(self, sky: Sky) -> TraceParams:
         p = TraceParams()
@@ -102,6 +103,7 @@ class TraceSettings:
         p.rng_mode = self.rng_mode
         p.estimator = MRT_EST_NEE if sky.sun_dir is not None else MRT_EST_ESCAPE
         p.accumulate, p.frame_index, p.sort_rays = int(self.accumulate), self.frame_index, int(self.sort_rays)
+        p.exact_trig = int(self.exact_trig)
         sd = np.asarray(sky.sun_dir if sky.sun_dir is not None else (0.0, 0.0, 1.0), np.float64)
         sd = (sd / np.linalg.norm(sd)).astype(np.float32)
         for k in range(3):
