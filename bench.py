@@ -115,10 +115,86 @@ def _peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def _workload(name="icospheres_1080p"):
+def l2_read_peak(ctx, stream, mib: int = 64, passes: int = 16, reps: int = 5) -> dict:
+    """L2 read bandwidth measured in this process: `passes` sweeps of 16-byte
+    L1-bypassing loads over a buffer of about half the L2 (mrt_cuda_read_sweep),
+    best of `reps` launches timed with CUDA events on the launch stream."""
+    import ctypes as C
+    from minotert_gb300._lib import lib
+    nbytes = mib << 20
+    buf = ctx.alloc(nbytes)
+    words = 8192
+    sink = ctx.alloc(4 * words)
+    buf.zero(stream)
+    sink.zero(stream)
+
+    def sweep():
+        ctx.check(lib().mrt_cuda_read_sweep(ctx.handle, C.c_void_p(buf.ptr), nbytes, passes, C.c_void_p(sink.ptr),
+                                            words, C.c_void_p(stream)), "read_sweep")
+
+    sweep()  # first touch brings the buffer into L2
+    ev = [(ctx.event(), ctx.event()) for _ in range(reps)]
+    for a, b in ev:
+        ctx.record(a, stream)
+        sweep()
+        ctx.record(b, stream)
+    ctx.sync(stream)
+    ms = [ctx.elapsed_ms(a, b) for a, b in ev]
+    best = min(ms)
+    buf.free()
+    sink.free()
+    return {"gbs": nbytes * passes / (best / 1e3) / 1e9, "buffer_mib": mib, "passes": passes,
+            "ms_best": best, "how": "mrt_cuda_read_sweep: %d sweeps of ld.global.cg 16-byte loads over a %d MiB "
+                                   "buffer (L2-resident after the first), best of %d launches, CUDA events"
+                                   % (passes, mib, reps)}
+
+
+def roofline_record(kernel: str, rays: float, bpr: float, ms: float, peaks: dict, l2: dict, traffic,
+                    working_set: float, l2_bytes: float, extra=None) -> dict:
+    """Roofline of one launch: algorithmic bytes (rays x bytes per ray) over
+    its event time, against the roof that binds it.  The roof is the L2 read
+    bandwidth when the data is served on chip -- DRAM traffic per launch (ncu)
+    well below the algorithmic bytes, or, without a capture, a working set
+    inside L2 or an achieved rate above the HBM peak -- and the HBM copy
+    bandwidth otherwise."""
+    alg = rays * bpr
+    achieved = alg / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+    over_hbm = achieved > peaks["hbm_gbs"]  # more than HBM can deliver: served on chip
+    on_chip = (traffic < 0.5 * alg) if traffic is not None else (working_set < l2_bytes or over_hbm)
+    peak = l2["gbs"] if on_chip else peaks["hbm_gbs"]
+    rec = {"bound": "l2" if on_chip else "hbm", "kernel": kernel, "achieved": achieved, "peak": peak,
+           "unit": "GB/s", "frac": achieved / peak,
+           "peak_source": ("measured in-process (%s)" % l2["how"]) if on_chip else peaks["source"],
+           "frac_l2": achieved / l2["gbs"], "frac_hbm": achieved / peaks["hbm_gbs"],
+           "peak_l2_gbs": l2["gbs"], "peak_hbm_gbs": peaks["hbm_gbs"], "traffic": traffic,
+           "bound_evidence": ("DRAM traffic %.1f%% of the algorithmic bytes (ncu)" % (100 * traffic / alg))
+           if traffic is not None else ("working set %.0f MB vs L2 %.0f MB%s" % (
+               working_set / 1e6, l2_bytes / 1e6,
+               "; achieved exceeds the HBM copy peak, so most bytes come from L2" if over_hbm else "")),
+           "bytes_per_ray": bpr, "rays_per_launch": rays, "ms_per_launch": ms, "l2_sweep": l2}
+    if extra:
+        rec.update(extra)
+    return rec
+
+
+def _blue_noise(full: bool = False) -> np.ndarray:
+    """The reference's blue-noise texture (assets/blue_noise.png, decoded into
+    tests/golden/blue_noise_asset.npz by golden/make_blue_noise.py): the whole
+    256 x 256 for the reference's own scene (fetched at Gid % 256 like
+    secondaryRays.comp:125), its top-left 64 x 64 crop for the configurations."""
+    from minotert_gb300 import scene
+    rgba = np.load(ROOT / "tests" / "golden" / "blue_noise_asset.npz")["rgba"]
+    return rgba if full else scene.blue_noise_tile(rgba, 64)
+
+
+def _workload(name="icospheres_1080p", resolution=None):
     from minotert_gb300 import scene, workloads
-    wl = {"icospheres_1080p": workloads.icospheres_1080p,
-          "heightfield_boxes_256": workloads.heightfield_boxes_256}[name]()
+    if resolution and name == "icospheres_1080p":
+        # the same scene and camera at another image size (small profiling case)
+        wl = workloads.icospheres_1080p(width=resolution[0], height=resolution[1])
+    else:
+        wl = {"icospheres_1080p": workloads.icospheres_1080p,
+              "heightfield_boxes_256": workloads.heightfield_boxes_256}[name]()
     t0 = time.perf_counter()
     mesh = wl.mesh()
     t1 = time.perf_counter()
@@ -173,7 +249,9 @@ def cpu_baseline(wl, mesh, bvh, bn, budget_s: float = 12.0, threads: int | None 
                       f"FP32 oracle, all host threads), {secs:.1f} s", "rays": rays, "seconds": secs}
 
 
-def run_mine(args, world, rank, local, dist):
+def frame_record(args, name, steps, warmup, world, rank, local, dist, cpu=True, l2=None):
+    """One workload's JSON record: K frames timed on the device, the
+    roofline of its dominant launch, and `e2e` through the C ABI."""
     from minotert_gb300 import build as _build
     _build.build()
     from minotert_gb300 import scene
@@ -181,8 +259,8 @@ def run_mine(args, world, rank, local, dist):
     from minotert_gb300.pathtracer import Pathtracer, TraceSettings, camera_consts
     import ctypes as C
 
-    wl, mesh, bvh, build_info = _workload(args.workload)
-    bn = scene.blue_noise(1, 64)
+    wl, mesh, bvh, build_info = _workload(name, getattr(args, "resolution", None))
+    bn = _blue_noise()
     ctx = Context(local)
     ds = scene.DeviceScene.triangles(ctx, mesh, bvh)
     ctx.blue_noise(bn)
@@ -199,23 +277,23 @@ def run_mine(args, world, rank, local, dist):
         pt.secondaryRays(gb, wl.camera, wl.sky, bn, TraceSettings(s.samples, s.bounces, s.rr_start, s.rng_mode),
                          color=color, stream=stream)
 
-    for f in range(args.warmup):
+    for f in range(warmup):
         frame(f)
     ctx.sync(stream)
     ctx.frame_stats()
     assert ctx.status() == 0
 
-    ev = [(ctx.event(), ctx.event()) for _ in range(args.steps)]
+    ev = [(ctx.event(), ctx.event()) for _ in range(steps)]
     ctx.set_timing(True)
     if dist is not None:
         dist.barrier()
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
-    for k in range(args.steps):
+    for k in range(steps):
         flush.zero(stream)
         ctx.record(ev[k][0], stream)
-        frame(args.warmup + k)
+        frame(warmup + k)
         ctx.record(ev[k][1], stream)
     ctx.sync(stream)
     clk = clocks.stop()
@@ -235,7 +313,7 @@ def run_mine(args, world, rank, local, dist):
 
     # traversal work per ray (counting form of the same kernels, one frame)
     ctx.set_counters(True)
-    frame(args.warmup + args.steps)
+    frame(warmup + steps)
     ctx.sync(stream)
     cs = ctx.frame_stats()
     ctx.set_counters(False)
@@ -257,6 +335,8 @@ def run_mine(args, world, rank, local, dist):
     # so its events would not time the kernel alone: a few more frames with
     # the overlap off (and L2 flushed before each) time it by itself.
     peaks = _peaks()
+    if l2 is None:
+        l2 = l2_read_peak(ctx, stream)
     saved_overlap = int(ctx.tuning().overlap_shadow)
     ctx.set_tuning(overlap_shadow=0)
     ctx.frame_stats()
@@ -264,7 +344,7 @@ def run_mine(args, world, rank, local, dist):
     n_alone = 3
     for k in range(n_alone):
         flush.zero(stream)
-        frame(args.warmup + args.steps + 1 + k)
+        frame(warmup + steps + 1 + k)
     ctx.sync(stream)
     alone = ctx.frame_stats()
     ctx.set_timing(False)
@@ -277,23 +357,26 @@ def run_mine(args, world, rank, local, dist):
     achieved = dk_bytes / (b1_ms / 1e3) / 1e9 if b1_ms > 0 else 0.0
     traffic = None
     tfile = ROOT / "profiles" / "traffic.json"
+    prof = {}
     if tfile.exists():
-        tj = json.loads(tfile.read_text()).get(wl.name, {}).get("extend")
-        if tj:
-            traffic = tj["bytes_per_ray"] * b1_rays
-    roofline = {"bound": "hbm", "kernel": "k_trace_ext (bounce 1)",
-                "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
-                "traffic": traffic, "bytes_per_ray": bytes_per_ray(n_node_b1, n_tri_b1),
-                "rays_per_launch": b1_rays, "ms_per_launch": b1_ms,
-                "nodes_per_ray": {"primary": n_node_prim, "extension": n_node_ext, "extension_b1": n_node_b1,
-                                  "shadow": n_node_sh},
-                "tris_per_ray": {"primary": n_tri_prim, "extension": n_tri_ext, "extension_b1": n_tri_b1,
-                                 "shadow": n_tri_sh},
-                "note": "bytes/ray = 32 + 16 + 128 N_node + 48 N_tri with N from the counting kernels "
-                        "(equal to the oracle's counts); the scene (69 MB) is L2-resident, so a fraction "
-                        "above 1 of the HBM copy peak means the traversal runs out of L2; the launch is "
-                        "timed alone (overlap_shadow off) over %d frames after the timed ones" % n_alone}
+        prof = json.loads(tfile.read_text()).get(wl.name, {}).get("extend") or {}
+        if "bytes_per_ray" in prof:
+            traffic = prof["bytes_per_ray"] * b1_rays
+    info = ctx.device_info()
+    working_set = float(bvh.nodes.nbytes + bvh.tris.nbytes + mesh.mats.nbytes)
+    roofline = roofline_record(
+        "k_trace_ext (bounce 1)", b1_rays, bytes_per_ray(n_node_b1, n_tri_b1), b1_ms, peaks, l2, traffic,
+        working_set, float(info.l2_bytes),
+        {"nodes_per_ray": {"primary": n_node_prim, "extension": n_node_ext, "extension_b1": n_node_b1,
+                           "shadow": n_node_sh},
+         "tris_per_ray": {"primary": n_tri_prim, "extension": n_tri_ext, "extension_b1": n_tri_b1,
+                          "shadow": n_tri_sh},
+         "issue_ncu": {k: prof[k] for k in ("issue_active", "simd_efficiency", "warp_inst_per_ray", "source_issue")
+                       if k in prof} or None,
+         "note": "bytes/ray = 32 + 16 + 128 N_node + 48 N_tri with N from the counting kernels (equal to the "
+                 "oracle's counts); the launch is timed alone (overlap_shadow off) over %d frames after the "
+                 "timed ones; issue_ncu: issue-slot use and SIMD efficiency of the same kernel from the "
+                 "committed ncu summary (the binding resource once the data is on chip)" % n_alone})
 
     b2 = sum(ext[1:])
     b2_ms = sum(st.ms_extend_b[1:s.bounces])
@@ -303,10 +386,10 @@ def run_mine(args, world, rank, local, dist):
         "bounce2plus_mrays_s": b2 / (b2_ms / 1e3) / 1e6 if b2_ms else None,
         "shadow_mrays_s": st.shadow_rays / (st.ms_shadow / 1e3) / 1e6 if st.ms_shadow else None,
         "all_rays_incl_shadow_mrays_s": (rays + int(st.shadow_rays)) / (total_ms / 1e3) / 1e6,
-        "rays_per_frame": {"primary": prim / args.steps, "extension": [e / args.steps for e in ext[:s.bounces]],
-                           "shadow": st.shadow_rays / args.steps},
-        "ms_per_frame": {"primary": st.ms_primary / args.steps, "extend": st.ms_extend / args.steps,
-                         "shadow": st.ms_shadow / args.steps, "shade": st.ms_shade / args.steps},
+        "rays_per_frame": {"primary": prim / steps, "extension": [e / steps for e in ext[:s.bounces]],
+                           "shadow": st.shadow_rays / steps},
+        "ms_per_frame": {"primary": st.ms_primary / steps, "extend": st.ms_extend / steps,
+                         "shadow": st.ms_shadow / steps, "shade": st.ms_shade / steps},
         "note": "tail_bounce %d: the paths alive at that bounce finish in one persistent launch (k_tail), "
                 "timed as extension of that bounce; its shading and shadow rays are inside that time, so "
                 "shadow_mrays_s divides all shadow rays by the wavefront shadow launches' time only. "
@@ -322,14 +405,14 @@ def run_mine(args, world, rank, local, dist):
     params = TraceSettings(s.samples, s.bounces, s.rr_start, s.rng_mode).params(wl.sky)
     e2e_ms = []
     ctx.frame_stats()
-    for k in range(args.warmup + args.steps):
+    for k in range(warmup + steps):
         consts = camera_consts(wl.camera, wl.camera, k)
-        if k == args.warmup:
+        if k == warmup:
             ctx.frame_stats()
         t0 = time.perf_counter()
         ctx.check(lib().mrt_cuda_render_frame_host(ctx.handle, ds.handle, C.byref(consts), C.byref(params), W, H,
                                                    None, None, ptr(col_h), C.c_void_p(stream)), "frame")
-        if k >= args.warmup:
+        if k >= warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
     est = ctx.frame_stats()
     e2e_rays = int(est.primary_rays) + sum(int(x) for x in est.extension_rays)
@@ -338,23 +421,44 @@ def run_mine(args, world, rank, local, dist):
            "d2h_bytes_per_step": W * H * 12, "ms_per_step": statistics.mean(e2e_ms),
            "api": "mrt_cuda_render_frame_host"}
 
-    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": _allmax(dist, total_ms / args.steps), "higher_is_better": True,
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
+           "warmup": warmup, "ms_per_step": _allmax(dist, total_ms / steps), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
            "config": _config(wl, mesh, bvh, build_info), "breakdown": breakdown, "roofline": roofline,
            "e2e": e2e, "gpu_launches": int(st.launches), "clocks": clk, "device_status": status}
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if cpu and rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(wl, mesh, bvh, bn)
+    ctx.close()
+    return out
+
+
+def run_mine(args, world, rank, local, dist):
+    out = frame_record(args, args.workload, args.steps, args.warmup, world, rank, local, dist)
+    if args.workload == "icospheres_1080p" and not args.no_sub_records:
+        # the other single-GPU configurations as sub-records of the same line,
+        # each with its own roofline: the 256x256 heightfield (one bounce) and
+        # the 64-scene batch (fixed tuned schedule, no sweep)
+        l2 = out["roofline"]["l2_sweep"]
+        subs = {}
+        subs["heightfield_boxes_256"] = frame_record(args, "heightfield_boxes_256", min(args.steps, 500),
+                                                     args.warmup, world, rank, local, dist, cpu=False, l2=l2)
+        subs["batched64"] = batched_record(args, min(args.steps, 10), args.warmup, world, rank, local, dist,
+                                           sweep=False, e2e_on=False, l2=l2)
+        for rec in subs.values():
+            for k in ("metric", "n_gpus", "higher_is_better", "scaling", "vs_baseline", "dtype"):
+                rec.pop(k, None)
+        out["sub_records"] = subs
     if rank == 0:
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()
 
 
-def run_batched(args, world, rank, local, dist):
+def batched_record(args, steps, warmup, world, rank, local, dist, sweep=True, e2e_on=True, l2=None):
     """64 scenes (heightfields and icosphere clusters, 1k-500k triangles,
     16k-2M rays each) path traced closest-hit over 3 bounces in one
-    persistent launch per bounce, the bounce loop replayed as a CUDA graph."""
+    persistent launch per bounce, the bounce loop replayed as a CUDA graph.
+    sweep: run the schedule autotuner first (else the tuned defaults)."""
     from minotert_gb300 import build as _build
     _build.build()
     from minotert_gb300 import autotune, workloads
@@ -385,21 +489,26 @@ def run_batched(args, world, rank, local, dist):
         batch.pathtrace(d_rays, offsets, params, frame[0], d_rad, use_graph=graph, stream=st)
 
     # schedule sweep: persistent blocks per SM x traversal stack entries x
-    # triangle tests spread over the warp x idle lanes before a refill
-    tune = autotune.autotune(ctx, step, stream, key=wl.name, frames=3, warmup=1, cache=None,
-                             space=[{"trace_blocks_per_sm": b, "dynamic_fetch": 1, "primary_persistent": 0,
-                                     "sort_min_rays": autotune.SORT_NEVER, "stack_depth": sd, "tri_spread": sp,
-                                     "refill_min": rm}
-                                    for b in (4, 6, 8) for sd in (16, 24, 32) for sp in (1, 0) for rm in (8, 1)])
-    for _ in range(args.warmup):
+    # triangle tests spread over the warp x in-warp compaction threshold (idle
+    # lanes a warp waits for before it compacts fresh rays into them; the
+    # queues between bounces are always compacted by warp-aggregated appends)
+    tune = None
+    if sweep:
+        tune = autotune.autotune(ctx, step, stream, key=wl.name, frames=3, warmup=1, cache=None,
+                                 space=[{"trace_blocks_per_sm": b, "dynamic_fetch": 1, "primary_persistent": 0,
+                                         "sort_min_rays": autotune.SORT_NEVER, "stack_depth": sd, "tri_spread": sp,
+                                         "refill_min": rm}
+                                        for b in (4, 6, 8) for sd in (16, 24, 32) for sp in (1, 0)
+                                        for rm in (1, 4, 8, 16, 24)])
+    for _ in range(warmup):
         step(stream)
     ctx.sync(stream)
     ctx.frame_stats()
     assert ctx.status() == 0
 
     def timed(graph):
-        ev = [(ctx.event(), ctx.event()) for _ in range(args.steps)]
-        for k in range(args.steps):
+        ev = [(ctx.event(), ctx.event()) for _ in range(steps)]
+        for k in range(steps):
             flush.zero(stream)
             ctx.record(ev[k][0], stream)
             step(stream, graph)
@@ -419,38 +528,90 @@ def run_batched(args, world, rank, local, dist):
     total_rays = int(st.primary_rays) + sum(int(x) for x in st.extension_rays)
     value = _allsum(dist, float(total_rays)) / _allmax(dist, sum(ms) / 1e3) / 1e6
 
-    # end to end: rays host -> device, radiance device -> host, every step
-    rays_h = ctx.host_alloc((n,), rays.dtype)
-    rays_h[:] = rays
-    rad_h = ctx.host_alloc((n, 3), np.float32)
-    from minotert_gb300._lib import lib, ptr
+    e2e = None
+    if e2e_on:
+        # end to end: rays host -> device, radiance device -> host, every step
+        rays_h = ctx.host_alloc((n,), rays.dtype)
+        rays_h[:] = rays
+        rad_h = ctx.host_alloc((n, 3), np.float32)
+        from minotert_gb300._lib import lib, ptr
+        import ctypes as C
+        e2e_ms = []
+        for k in range(steps):
+            t1 = time.perf_counter()
+            ctx.check(lib().mrt_cuda_copy_h2d(ctx.handle, C.c_void_p(d_rays.ptr), ptr(rays_h), rays_h.nbytes,
+                                              C.c_void_p(stream)), "h2d")
+            step(stream)
+            ctx.check(lib().mrt_cuda_copy_d2h(ctx.handle, ptr(rad_h), C.c_void_p(d_rad.ptr), rad_h.nbytes,
+                                              C.c_void_p(stream)), "d2h")
+            ctx.sync(stream)
+            e2e_ms.append((time.perf_counter() - t1) * 1e3)
+        per_step_rays = total_rays / steps
+        e2e = {"value": per_step_rays * steps / (sum(e2e_ms) / 1e3) / 1e6, "unit": UNIT,
+               "h2d_bytes_per_step": int(rays_h.nbytes), "d2h_bytes_per_step": int(rad_h.nbytes),
+               "api": "mrt_cuda_batch_pathtrace + mrt_cuda_copy_h2d/d2h"}
+
+    # roofline of the largest launch: the closest-hit trace of the primary
+    # rays of all scenes (k_batch_trace), timed alone with the L2 flushed,
+    # bytes per ray from the counting traversal kernel (whose per-ray counts
+    # equal the oracle's) on about 1024 rays of each scene, weighted by its
+    # ray count
     import ctypes as C
-    e2e_ms = []
-    for k in range(args.steps):
-        t1 = time.perf_counter()
-        ctx.check(lib().mrt_cuda_copy_h2d(ctx.handle, C.c_void_p(d_rays.ptr), ptr(rays_h), rays_h.nbytes,
-                                          C.c_void_p(stream)), "h2d")
-        step(stream)
-        ctx.check(lib().mrt_cuda_copy_d2h(ctx.handle, ptr(rad_h), C.c_void_p(d_rad.ptr), rad_h.nbytes,
-                                          C.c_void_p(stream)), "d2h")
-        ctx.sync(stream)
-        e2e_ms.append((time.perf_counter() - t1) * 1e3)
-    per_step_rays = total_rays / args.steps
-    e2e = {"value": per_step_rays * args.steps / (sum(e2e_ms) / 1e3) / 1e6, "unit": UNIT,
-           "h2d_bytes_per_step": int(rays_h.nbytes), "d2h_bytes_per_step": int(rad_h.nbytes),
-           "api": "mrt_cuda_batch_pathtrace + mrt_cuda_copy_h2d/d2h"}
-    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": _allmax(dist, sum(ms) / args.steps), "higher_is_better": True,
+    from minotert_gb300._lib import lib, ptr
+    from minotert_gb300.scene import DeviceScene
+    if l2 is None:
+        l2 = l2_read_peak(ctx, stream)
+    d_hits = ctx.alloc(8 * n)
+    evr = [(ctx.event(), ctx.event()) for _ in range(3)]
+    for a_, b_ in evr:
+        flush.zero(stream)
+        ctx.record(a_, stream)
+        batch.trace(d_rays, offsets, d_hits, stream=stream)
+        ctx.record(b_, stream)
+    ctx.sync(stream)
+    tr_ms = statistics.mean(ctx.elapsed_ms(a_, b_) for a_, b_ in evr)
+    nn = nt = 0.0
+    for k, (sc, m, bv) in enumerate(scenes):
+        r = rays[offsets[k]:offsets[k + 1]]
+        smp = np.ascontiguousarray(r[:: max(1, len(r) // 1024)])
+        ds = DeviceScene.triangles(ctx, m, bv)
+        d_s, d_h = ctx.to_device(smp), ctx.alloc(8 * len(smp))
+        d_nv, d_tv = ctx.alloc(4 * len(smp)), ctx.alloc(4 * len(smp))
+        ctx.check(lib().mrt_cuda_trace_rays_counted(ctx.handle, ds.handle, ptr(d_s), len(smp), ptr(d_h), ptr(d_nv),
+                                                    ptr(d_tv), None), "counted")
+        w = len(r) / n
+        nn += w * float(d_nv.download(np.uint32, (len(smp),)).mean())
+        nt += w * float(d_tv.download(np.uint32, (len(smp),)).mean())
+        for b_ in (d_s, d_h, d_nv, d_tv):
+            b_.free()
+        ds.close()
+    working = float(sum(bv.nodes.nbytes + bv.tris.nbytes + m.mats.nbytes for _, m, bv in scenes))
+    roofline = roofline_record("k_batch_trace (primary rays, closest hit)", float(n), 32 + 16 + 128 * nn + 48 * nt,
+                               tr_ms, _peaks(), l2, None, working, float(ctx.device_info().l2_bytes),
+                               {"nodes_per_ray": nn, "tris_per_ray": nt,
+                                "note": "bytes/ray = 32 + 16 + 128 N_node + 48 N_tri with N from the counting "
+                                        "traversal on about 1024 rays of each scene"})
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
+           "warmup": warmup, "ms_per_step": _allmax(dist, sum(ms) / steps), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes)",
            "config": {"workload": wl.name, "scenes": len(scenes), "triangles": int(sum(m.tri_count for _, m, _ in scenes)),
                       "primary_rays": n, "bounces": wl.settings.bounces, "query": "closest hit",
                       "l2": "256 MiB memset between timed steps", "parallelism": "replicas",
                       "host_build_s": build_s},
-           "breakdown": {"rays_per_step": {"primary": n, "extension": [int(x) / args.steps for x in
+           "breakdown": {"rays_per_step": {"primary": n, "extension": [int(x) / steps for x in
                                                                        st.extension_rays[:wl.settings.bounces]]},
                          "ms_per_step_graph": statistics.mean(ms), "ms_per_step_direct": statistics.mean(ms_direct),
-                         "autotune": {"best": tune["tuning"], "results": tune["results"]}},
-           "e2e": e2e, "gpu_launches": int(st.launches), "clocks": clk, "device_status": status}
+                         "autotune": ({"best": tune["tuning"], "results": tune["results"]} if tune else
+                                      {"best": "tuned defaults, no sweep"})},
+           "roofline": roofline, "gpu_launches": int(st.launches), "clocks": clk, "device_status": status}
+    if e2e is not None:
+        out["e2e"] = e2e
+    ctx.close()
+    return out
+
+
+def run_batched(args, world, rank, local, dist):
+    out = batched_record(args, args.steps, args.warmup, world, rank, local, dist)
     if rank == 0:
         print(json.dumps(out))
     if dist is not None:
@@ -476,7 +637,7 @@ def run_cache_experiment(args, world, rank, local, dist):
     cam = Camera((W, H), c0.verticalFov, c0.nearPlane, c0.position, c0.yaw, c0.pitch)
     mesh = base.mesh()
     bvh = scene.build_bvh8(mesh)
-    bn = scene.blue_noise(1, 64)
+    bn = _blue_noise()
     ctx = Context(local)
     ds = scene.DeviceScene.triangles(ctx, mesh, bvh)
     ctx.blue_noise(bn)
@@ -586,6 +747,61 @@ def run_cache_experiment(args, world, rank, local, dist):
     ctx.sync(stream)
     warm.close()
     curves = {name: learned_curve(*v) for name, v in variants.items()}
+
+    def bounds(query_vertex, train_frames=256, k=16):
+        """What a cache could gain at best: after `train_frames` of online
+        training the cache is frozen; single frames and a k-frame mean give its
+        per-frame variance and its bias (MSE_1 = b^2 + v, MSE_k = b^2 + v/k),
+        and frames without training time the tracing and the inference alone."""
+        cfg = default_config(query_vertex=query_vertex, train_paths=65536, train_steps=4)
+        cache = RadianceCache(ctx, cfg, bounds=(mesh.lo, mesh.hi))
+
+        def fn(train, accumulate):
+            def f_(gb, col, f):
+                params = TraceSettings(1, 1, 2, 1, accumulate, f).params(sky)
+                cache.frame(ds, gb, camera_consts(cam, cam, pt.frame_counter), params, col, train=train,
+                            stream=stream)
+            return f_
+
+        run(train_frames, 30000, fn(True, True))
+        singles = []
+        for f in range(k):
+            img, _, _ = run(1, 40000 + f, fn(False, False))
+            singles.append(float(np.mean((img - ref) ** 2)))
+        mean_k, ms_k, _ = run(k, 40000, fn(False, True))
+        mse1, msek = float(np.mean(singles)), float(np.mean((mean_k - ref) ** 2))
+        var = max((mse1 - msek) * k / (k - 1), 0.0)
+        bias2 = max(mse1 - var, 0.0)
+        ctx.set_timing(True)
+        ctx.frame_stats()
+        run(k, 50000, fn(False, True))
+        st_frozen = ctx.frame_stats()
+        run(k, 60000, fn(True, True))
+        st_train = ctx.frame_stats()
+        ctx.set_timing(False)
+        cache.close()
+        return {"mse_single_frame": mse1, "var_per_frame": var, "bias_rmse": float(np.sqrt(bias2)),
+                "ms_frame_frozen": float(ms_k[-1] / k), "ms_infer": st_frozen.ms_cache_infer / k,
+                "ms_trace_only": (float(ms_k[-1]) - st_frozen.ms_cache_infer) / k,
+                "ms_train": st_train.ms_cache_train / k}
+
+    # plain: single-frame MSE (no bias) from k independent frames
+    plain_single = []
+    for f in range(16):
+        img, ms1, _ = run(1, 70000 + f, plain_fn)
+        plain_single.append(float(np.mean((img - ref) ** 2)))
+    var_p, t_p = float(np.mean(plain_single)), float(plain_ms[-1] / nmax)
+    lower = {}
+    for qv in (1, 0):
+        b = bounds(qv)
+        # time to RMSE tau: plain t_p var_p / tau^2; learned (t_trace + t_net) var_c / (tau^2 - bias^2).
+        # The most a cache could give, with a free network (t_net = 0) and
+        # this variance, at a target far above its bias:
+        s_max = (t_p / max(b["ms_trace_only"], 1e-9)) * (var_p / max(b["var_per_frame"], 1e-12))
+        lower[f"query_vertex_{qv}"] = dict(b, speedup_bound_free_network=s_max,
+                                           var_ratio_needed_for_4x_free_network=4.0 * b["ms_trace_only"] / t_p,
+                                           var_ratio_measured=var_p / max(b["var_per_frame"], 1e-12))
+    lower["plain"] = {"var_per_frame": var_p, "ms_frame": t_p}
     targets = (0.02, 0.01, 0.007, 0.005)
     table = {}
     for t in targets:
@@ -609,7 +825,7 @@ def run_cache_experiment(args, world, rank, local, dist):
                       "indirect radiance, shadow rays give direct light; query_vertex 1 = paths end at the first "
                       "bounce's hit, 0 = at the primary hit",
                       "reference": f"{ref_frames} frames of 1-spp plain path tracing ({ref_s:.1f} s)"},
-           "reference_check": ref_check, "curve_plain": curve_p,
+           "reference_check": ref_check, "curve_plain": curve_p, "bounds": lower,
            "curves_learned": {name: c[0] for name, c in curves.items()},
            "passes_learned": {name: c[1] for name, c in curves.items()},
            "device_status": ctx.status()}
@@ -632,7 +848,7 @@ def run_denoise_experiment(args, world, rank, local, dist):
 
     ctx = Context(local)
     stream = ctx.stream()
-    bn = scene.blue_noise(1, 64)
+    bn = _blue_noise()
     ctx.blue_noise(bn)
     sky = Sky((0.25, 0.32, 0.45), (0.45, -0.35, 0.82), (2.5, 2.5, 2.5))
     SET = dict(bounces=8, rr_start=2, rng_mode=1)
@@ -788,7 +1004,7 @@ def run_reference(args, world, rank, local, dist):
     wl, mesh, bvh, build_info = _workload(args.workload if args.workload == "heightfield_boxes_256"
                                           else "icospheres_1080p")
     from minotert_gb300 import scene
-    bn = scene.blue_noise(1, 64)
+    bn = _blue_noise()
     per_step = max(1.0, min(6.0, 150.0 / max(1, args.steps + args.warmup)))
     for _ in range(args.warmup):
         cpu_baseline(wl, mesh, bvh, bn, budget_s=min(per_step, 2.0))
@@ -825,7 +1041,6 @@ def _reference_scene_cpu(W, H, frame, budget_s, threads):
     from oracle import post
     from oracle.glsl import build_ref
     from minotert_gb300.pathtracer import Camera
-    from minotert_gb300.scene import blue_noise
     sys.path.insert(0, str(ROOT / "tests"))
     from conftest import oracle_consts
     L = build_ref.lib()
@@ -844,7 +1059,8 @@ def _reference_scene_cpu(W, H, frame, budget_s, threads):
     probe = np.asarray(cam.position, np.float32)
     view = np.zeros((108, 192, 4), np.float32)
     L.ref_sky_view(p(atmo), p(trans), p(ms), p(probe), p(sun), p(sun_e), p(view))
-    bn4 = np.ascontiguousarray(blue_noise(1, 64).astype(np.float32) / np.float32(255.0))
+    bnt = _blue_noise(full=True)
+    bn4 = np.ascontiguousarray(bnt.astype(np.float32) / np.float32(255.0))
     L.ref_dispatch_threads(threads)
     # the g-buffer of the whole frame, then bands of rows of the secondary
     # pass (the shader reads only its own pixel of the g-buffer)
@@ -862,7 +1078,7 @@ def _reference_scene_cpu(W, H, frame, budget_s, threads):
     while secs < budget_s and rows < H:
         h = min(band, H - rows)
         t0 = time.perf_counter()
-        L.ref_secondary_rays_rows(p(consts), W, H, p(vis4), p(dep4), p(nrm4), p(bn4), 64, 64, p(trans), 256, 64,
+        L.ref_secondary_rays_rows(p(consts), W, H, p(vis4), p(dep4), p(nrm4), p(bn4), bnt.shape[1], bnt.shape[0], p(trans), 256, 64,
                                   p(view), 192, 108, p(atmo), p(col), rows, rows + h)
         secs += time.perf_counter() - t0
         rows += h
@@ -914,11 +1130,11 @@ def run_reference_scene(args, world, rank, local, dist):
     _build.build()
     from minotert_gb300._lib import Context
     from minotert_gb300.pathtracer import Camera, Pathtracer, Sky as ConstSky, TraceSettings
-    from minotert_gb300.scene import DeviceScene, blue_noise, reference_spheres
+    from minotert_gb300.scene import DeviceScene, reference_spheres
     from minotert_gb300.sky import Atmosphere, Sky
     ctx = Context(local)
     ds = DeviceScene.from_spheres(ctx, reference_spheres())
-    bn = blue_noise(1, 64)
+    bn = _blue_noise(full=True)
     cam = Camera.reference(W, H)
     stream = ctx.stream()
     atmo = Atmosphere(ctx)
@@ -1076,7 +1292,7 @@ def run_post_kernels(args, world, rank, local, dist):
     cam = Camera((W, H), c0.verticalFov, c0.nearPlane, c0.position, c0.yaw, c0.pitch)
     mesh = base.mesh()
     ds = scene.DeviceScene.triangles(ctx, mesh, scene.build_bvh8(mesh))
-    bn = scene.blue_noise(1, 64)
+    bn = _blue_noise()
     pt = Pathtracer(ctx, ds, full_gbuffer=True)
     gb = pt.primaryRays((W, H), cam, cam)
     col = pt.secondaryRays(gb, cam, base.sky, bn, TraceSettings(1, 4, 2, 1))
@@ -1111,10 +1327,14 @@ def run_post_kernels(args, world, rank, local, dist):
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--resolution", type=lambda v: tuple(int(x) for x in v.lower().split("x")), default=None,
+                    help="WxH: the icosphere workload at another image size (a small case for ncu captures)")
+    ap.add_argument("--no-sub-records", action="store_true",
+                    help="headline workload only (no heightfield_boxes_256 / batched64 sub-records)")
     ap.add_argument("--workload", choices=["icospheres_1080p", "heightfield_boxes_256", "batched64",
                                            "radiance_cache", "denoiser", "network_kernels", "post_kernels",
                                            "reference_spheres_1080p"],

@@ -10,8 +10,8 @@
  *     BVH8 of mrt_cuda.h (new: the reference has no BVH);
  *   - procedural scenes from a seed (new: the reference's scene is a
  *     5-sphere constant, scene.glsl:4-11, returned by mrt_scene_reference);
- *   - a blue-noise tile generator (void-and-cluster) standing in for the
- *     reference's assets/blue_noise.png (renderer.ixx:101-110).
+ *   - the blue-noise asset loader (a PNG decoder, renderer.ixx:101-110)
+ *     and a blue-noise tile generator (void-and-cluster).
  * All entry points return MRT_OK or a negative MRT_E* code.
  */
 #ifndef MRT_HOST_H
@@ -165,6 +165,20 @@ int mrt_write_pfm(const char* path, const float* rgb, uint32_t width, uint32_t h
 /* size x size RGBA8 blue-noise tile by void-and-cluster (Ulichney 1993),
  * one independent rank map per channel, seeded. size <= 256. */
 int mrt_blue_noise_generate(uint32_t seed, uint32_t size, uint8_t* rgba_out);
+
+/* The reference's blue-noise asset loader (renderer.ixx:101-110, which
+ * calls lodepng::decode(..., LCT_RGBA, 8) on assets/blue_noise.png):
+ * decodes an 8-bit, non-interlaced PNG -- greyscale, greyscale + alpha,
+ * RGB or RGBA -- to RGBA8 rows, top row first, widening grey to (g, g, g)
+ * and a missing alpha to 255.  With rgba == NULL only *width / *height
+ * are set; otherwise rgba must hold 4 * width * height bytes.  Returns
+ * MRT_OK, MRT_EINVAL (not a PNG this decoder reads, or corrupt: chunk
+ * CRC-32 and zlib Adler-32 are checked; a missing file for _load) or
+ * MRT_ERANGE (rgba_bytes too small). */
+int mrt_png_decode_rgba8(const uint8_t* data, size_t size, uint8_t* rgba, size_t rgba_bytes,
+                         uint32_t* width, uint32_t* height);
+int mrt_png_load_rgba8(const char* path, uint8_t* rgba, size_t rgba_bytes,
+                       uint32_t* width, uint32_t* height);
 
 #ifdef __cplusplus
 }

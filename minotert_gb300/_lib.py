@@ -235,6 +235,8 @@ def lib() -> C.CDLL:
             "mrt_scene_reference": ([vp], u32),
             "mrt_camera_reference": ([u32, u32, C.POINTER(Camera_C)], None),
             "mrt_blue_noise_generate": ([u32, u32, vp], i32),
+            "mrt_png_decode_rgba8": ([vp, sz, vp, sz, C.POINTER(u32), C.POINTER(u32)], i32),
+            "mrt_png_load_rgba8": ([C.c_char_p, vp, sz, C.POINTER(u32), C.POINTER(u32)], i32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)

@@ -55,13 +55,20 @@ def _bind():
 
 
 class Renderer:
-    def __init__(self, ctx: Context, scene, width: int, height: int):
+    """Renderer_impl (renderer.ixx:39-68) without window, ImGui or swapchain.
+    blue_noise: an RGBA8 texture to sample instead of the generated 64 x 64
+    tile -- the reference's constructor loads assets/blue_noise.png
+    (renderer.ixx:101-110; scene.load_png decodes it the same way)."""
+
+    def __init__(self, ctx: Context, scene, width: int, height: int, blue_noise: np.ndarray | None = None):
         L = _bind()
         self.ctx, self.scene, self.width, self.height = ctx, scene, int(width), int(height)
         h = C.c_void_p()
         ctx.check(L.mrt_renderer_create(ctx.handle, scene.handle, self.width, self.height, C.byref(h)),
                   "renderer_create")
         self._h = h
+        if blue_noise is not None:
+            ctx.blue_noise(blue_noise)
 
     def draw(self, camera: Camera, settings: RenderSettings | None = None, stream=None):
         s = settings or RenderSettings.defaults()

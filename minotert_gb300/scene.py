@@ -92,6 +92,34 @@ def reference_spheres() -> np.ndarray:
     return s
 
 
+def load_png(path_or_bytes) -> np.ndarray:
+    """RGBA8 image (h, w, 4) from a PNG file or its bytes, decoded like the
+    reference's asset loader (renderer.ixx:101-110, lodepng to RGBA8)."""
+    w, h = C.c_uint32(0), C.c_uint32(0)
+    if isinstance(path_or_bytes, (bytes, bytearray)):
+        data = np.frombuffer(bytes(path_or_bytes), np.uint8)
+        call = lambda out, n: lib().mrt_png_decode_rgba8(ptr(data), data.nbytes, out, n, C.byref(w), C.byref(h))
+    else:
+        path = str(path_or_bytes).encode()
+        call = lambda out, n: lib().mrt_png_load_rgba8(path, out, n, C.byref(w), C.byref(h))
+    rc = call(None, 0)
+    if rc:
+        raise MrtError(rc, "PNG decode")
+    out = np.zeros((h.value, w.value, 4), np.uint8)
+    rc = call(ptr(out), out.nbytes)
+    if rc:
+        raise MrtError(rc, "PNG decode")
+    return out
+
+
+def blue_noise_tile(rgba: np.ndarray, size: int = 64) -> np.ndarray:
+    """The top-left size x size crop of an RGBA8 blue-noise texture: the tile
+    the measured workloads sample at Gid % size (the reference samples its
+    whole 256 x 256 texture at Gid % 256, secondaryRays.comp:125; kernels
+    read channels R and G)."""
+    return np.ascontiguousarray(rgba[:size, :size])
+
+
 def blue_noise(seed: int = 1, size: int = 64) -> np.ndarray:
     """size x size x 4 RGBA8 blue-noise tile (void-and-cluster)."""
     out = np.zeros((size, size, 4), dtype=np.uint8)

@@ -71,10 +71,23 @@ def ico_workload(built_lib):
     return wl, mesh, bvh
 
 
+def asset_blue_noise() -> np.ndarray:
+    """The reference's blue-noise texture (assets/blue_noise.png, 256 x 256
+    RGBA8), decoded into the committed fixture by golden/make_blue_noise.py."""
+    return np.load(ROOT / "tests" / "golden" / "blue_noise_asset.npz")["rgba"]
+
+
 @pytest.fixture(scope="session")
 def blue_noise(built_lib):
+    """The measured configurations' 64 x 64 tile: the asset's top-left crop."""
     from minotert_gb300 import scene
-    return scene.blue_noise(1, 64)
+    return scene.blue_noise_tile(asset_blue_noise(), 64)
+
+
+@pytest.fixture(scope="session")
+def reference_blue_noise(built_lib):
+    """The whole 256 x 256 asset, fetched at Gid % 256 like secondaryRays.comp:125."""
+    return asset_blue_noise()
 
 
 def oracle_consts(camera, frame=0, prev=None):

@@ -67,7 +67,7 @@ def main():
     from oracle import post
     from oracle.glsl import build_ref
     from minotert_gb300.pathtracer import Camera
-    from minotert_gb300.scene import blue_noise, reference_spheres
+    from minotert_gb300.scene import reference_spheres
 
     L = build_ref.lib()
     if L is None:
@@ -131,9 +131,12 @@ def main():
     dep4 = np.zeros_like(d4)
     dep4[..., 0] = d4[..., 0].astype(np.float16).astype(np.float32)
     nrm4 = np.ascontiguousarray(n4.astype(np.float16).astype(np.float32))
-    bn4 = np.ascontiguousarray(blue_noise(1, 64).astype(np.float32) / np.float32(255.0))
+    # the reference's own blue-noise texture, fetched at Gid % 256 (secondaryRays.comp:125)
+    bnt = np.load(Path(__file__).resolve().parent / "blue_noise_asset.npz")["rgba"]
+    bn4 = np.ascontiguousarray(bnt.astype(np.float32) / np.float32(255.0))
     col = np.zeros((H2, W2, 4), np.float32)
-    L.ref_secondary_rays(_p(c2), W2, H2, _p(vis4), _p(dep4), _p(nrm4), _p(bn4), 64, 64, _p(trans), 256, 64,
+    L.ref_secondary_rays(_p(c2), W2, H2, _p(vis4), _p(dep4), _p(nrm4), _p(bn4), bnt.shape[1], bnt.shape[0], _p(trans),
+                         256, 64,
                          _p(view), 192, 108, _p(atmo), _p(col))
     v["sec_color"] = col[..., :3].copy()
     # tonemappers

@@ -19,7 +19,7 @@ from conftest import oracle_consts  # noqa: F401  (registers the tests dir on sy
 from minotert_gb300._lib import MRT_MISS
 from minotert_gb300.pathtracer import Camera, Pathtracer, Sky as ConstSky, TraceSettings
 from minotert_gb300.post import AMDParams, Tonemapper, UchimuraParams
-from minotert_gb300.scene import DeviceScene, blue_noise, reference_spheres
+from minotert_gb300.scene import DeviceScene, reference_spheres
 
 pytestmark = pytest.mark.gpu
 
@@ -58,7 +58,7 @@ def test_tonemappers_match_reference_shaders(ctx):
         assert diff.max() <= 1 and (diff == 0).mean() > 0.99, name
 
 
-def test_secondary_pass_matches_reference_shader(ctx):
+def test_secondary_pass_matches_reference_shader(ctx, reference_blue_noise):
     from minotert_gb300.sky import Atmosphere, Sky
     W, H = 48, 27
     ds = DeviceScene.from_spheres(ctx, reference_spheres())
@@ -70,7 +70,7 @@ def test_secondary_pass_matches_reference_shader(ctx):
     try:
         sky = Sky()
         view = sky.createView(atmo, np.asarray(cam.position, np.float32))
-        col = pt.secondaryRays(gb, cam, ConstSky(radiance=(0.0, 0.0, 0.0), sun_dir=None), blue_noise(1, 64),
+        col = pt.secondaryRays(gb, cam, ConstSky(radiance=(0.0, 0.0, 0.0), sun_dir=None), reference_blue_noise,
                                TraceSettings(samples=8, bounces=8), skyView=view)
         img = col.download(np.float32, (H, W, 3))
     finally:

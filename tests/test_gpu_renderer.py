@@ -16,11 +16,13 @@ from minotert_gb300.sky import Atmosphere, Sky
 pytestmark = pytest.mark.gpu
 
 
-def test_reference_frame_matches_the_call_chain(ctx, blue_noise, tmp_path):
+def test_reference_frame_matches_the_call_chain(ctx, reference_blue_noise, tmp_path):
+    # the reference's scene with its own blue-noise texture, as
+    # Renderer_impl's constructor loads it
     W, H = 192, 108
     ds = DeviceScene.from_spheres(ctx, reference_spheres())
     cam = Camera.reference(W, H)
-    r = Renderer(ctx, ds, W, H)
+    r = Renderer(ctx, ds, W, H, blue_noise=reference_blue_noise)
     frames = 2
     for f in range(frames):
         r.draw(cam)
@@ -33,7 +35,7 @@ def test_reference_frame_matches_the_call_chain(ctx, blue_noise, tmp_path):
     pt = Pathtracer(ctx, ds)
     pt.frame_counter = frames - 1
     gb = pt.primaryRays((W, H), cam, cam)
-    col = pt.secondaryRays(gb, cam, ConstSky(radiance=(0.0, 0.0, 0.0), sun_dir=None), blue_noise,
+    col = pt.secondaryRays(gb, cam, ConstSky(radiance=(0.0, 0.0, 0.0), sun_dir=None), reference_blue_noise,
                            TraceSettings(samples=8, bounces=8), skyView=view)
     den = Denoiser(ctx).bilateral(col, gb, cam, BilateralParams(), frame_counter=frames - 1)
     out = Tonemapper(ctx).amd(den, W, H, 1.0)
@@ -64,7 +66,7 @@ def test_reprojected_accumulation_matches_the_call_chain(ctx, hf_workload, blue_
     s.sky_mode, s.accumulation, s.denoise = SKY_CONSTANT, ACCUM_REPROJECT, DENOISE_NONE
     for k in range(3):
         s.trace.sky_radiance[k] = (0.25, 0.32, 0.45)[k]
-    r = Renderer(ctx, ds, W, H)
+    r = Renderer(ctx, ds, W, H, blue_noise=blue_noise)
     for cam in cams:
         r.draw(cam, s)
     rgba, hdr = r.read()

@@ -110,7 +110,7 @@ def test_sky_lut_vectors():
 
 
 def test_secondary_pass_vectors():
-    from minotert_gb300.scene import blue_noise
+    from conftest import asset_blue_noise
     atmo, trans, ms = _sky()
     W, H = 48, 27
     cam = _camera(W, H)
@@ -120,7 +120,7 @@ def test_secondary_pass_vectors():
     post.bind_sky(atmo, trans, view, probe, mk.SUN, mk.SUN_E)
     try:
         col = oracle.secondary_spheres(_spheres(), oracle_consts(cam, 3), W, H, g["visibility"], g["depth"],
-                                       g["normal"], blue_noise(1, 64), oracle.params_array(8, 8))
+                                       g["normal"], asset_blue_noise(), oracle.params_array(8, 8))
     finally:
         post.bind_sky()
     assert np.array_equal(col.view(np.uint32), GOLD["sec_color"].view(np.uint32))
