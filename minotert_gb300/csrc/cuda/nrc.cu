@@ -96,12 +96,14 @@ __device__ __forceinline__ void level_corners(const GridSpec& g, int l, float px
     }
 }
 
-// 64 input halves of one query: 32 features, normal, direction, zeros
-__device__ void encode_row(const GridSpec& g, const __half2* grid, const float* q, __half* row) {
+// Encoded features of levels [l0, l1) of one query (position p in [0,1]^3,
+// clamped) into row[2l], row[2l+1].  Two levels at a time, so 16 corner
+// loads are in flight per lane.
+__device__ void encode_levels(const GridSpec& g, const __half2* grid, const float* q, __half* row, int l0, int l1) {
     const float px = fminf(fmaxf(q[0], 0.0f), 1.0f), py = fminf(fmaxf(q[1], 0.0f), 1.0f),
                 pz = fminf(fmaxf(q[2], 0.0f), 1.0f);
-#pragma unroll 1
-    for (int l = 0; l < kLevels; ++l) {
+#pragma unroll 2
+    for (int l = l0; l < l1; ++l) {
         uint32_t idx[8];
         float w[8];
         level_corners(g, l, px, py, pz, idx, w);
@@ -115,8 +117,26 @@ __device__ void encode_row(const GridSpec& g, const __half2* grid, const float* 
         row[2 * l] = __float2half_rn(f0);
         row[2 * l + 1] = __float2half_rn(f1);
     }
+}
+
+// Normal, direction and the zero padding of an input row.
+__device__ void encode_tail(const float* q, __half* row) {
     for (int k = 0; k < 6; ++k) row[kEnc + k] = __float2half_rn(q[3 + k]);
     for (int k = kEnc + 6; k < kWidth; ++k) row[k] = __float2half_rn(0.0f);
+}
+
+// The 16 rows of a warp's tile encoded by all 32 lanes: lane i takes row
+// i mod 16 and half of its levels (i < 16: levels 0-7 and the normal /
+// direction / padding; i >= 16: levels 8-15), so twice as many hash-grid
+// gathers are in flight as with one lane per row.  q_row(r, qq) fills the 9
+// floats of tile row r (zeros past the end).
+template <class QRow>
+__device__ __forceinline__ void encode_tile(const GridSpec& g, const __half2* grid, __half* X, QRow q_row) {
+    const int lane = int(lane_id()), r = lane & 15, half = lane >> 4;
+    float qq[9];
+    q_row(r, qq);
+    encode_levels(g, grid, qq, X + r * kWidth, half * (kLevels / 2), (half + 1) * (kLevels / 2));
+    if (!half) encode_tail(qq, X + r * kWidth);
 }
 
 // ------------------------------------------------------------ MLP on mma
@@ -245,12 +265,10 @@ k_cache_infer(CacheDev c, const float* q, uint32_t n_max, const uint32_t* n_dev,
     __half* X = sX + warp * 16 * kWidth;
     float* O = sO + warp * 16 * 3;
     for (uint32_t base = (blockIdx.x * kMlpWarps + warp) * 16u; base < n; base += gridDim.x * kMlpWarps * 16u) {
-        if (lane < 16) {
-            const uint32_t r = base + lane;
-            float qq[9];
+        encode_tile(c.spec, c.grid, X, [&](int rr, float* qq) {
+            const uint32_t r = base + uint32_t(rr);
             for (int k = 0; k < 9; ++k) qq[k] = r < n ? q[size_t(r) * 9 + k] : 0.0f;
-            encode_row(c.spec, c.grid, qq, X + lane * kWidth);
-        }
+        });
         __syncwarp();
         mlp_forward_tile(sW, X, nullptr, 0, O);
         __syncwarp();
@@ -280,13 +298,13 @@ k_cache_train_fwd(CacheDev c, const float* q, const float* target, uint32_t n, _
     float loss = 0.0f;
     for (uint32_t base = (blockIdx.x * kMlpWarps + warp) * 16u; base + 16u <= n;
          base += gridDim.x * kMlpWarps * 16u) {
-        if (lane < 16) {
-            const uint32_t r = base + lane;
-            float qq[9];
-            for (int k = 0; k < 9; ++k) qq[k] = q[size_t(r) * 9 + k];
-            encode_row(c.spec, c.grid, qq, X + lane * kWidth);
-            for (int k = 0; k < kWidth; ++k) inputs[size_t(r) * kWidth + k] = X[lane * kWidth + k];
-        }
+        encode_tile(c.spec, c.grid, X, [&](int rr, float* qq) {
+            for (int k = 0; k < 9; ++k) qq[k] = q[size_t(base + uint32_t(rr)) * 9 + k];
+        });
+        __syncwarp();
+        // the tile's input rows, kept for the backward (16 x 64 halves)
+        for (int i = lane; i < 16 * kWidth / 2; i += 32)
+            reinterpret_cast<uint32_t*>(inputs + size_t(base) * kWidth)[i] = reinterpret_cast<const uint32_t*>(X)[i];
         __syncwarp();
         mlp_forward_tile(sW, X, acts + size_t(base) * kWidth, act_ld, O);
         __syncwarp();

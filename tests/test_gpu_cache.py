@@ -134,3 +134,70 @@ def test_trained_cache_beats_plain_path_tracing_at_equal_frames(ctx, hf_workload
     print(f"RMSE after 8 frames: plain {r_plain:.4f}, learned (query vertex {query_vertex}) {r_learned:.4f}")
     assert np.isfinite(learned8).all()
     assert r_learned < r_plain
+
+
+def test_cache_against_plain_path_tracing_at_equal_gpu_time(ctx, hf_workload, blue_noise):
+    # 480x270 view of the heightfield scene; reference: plain path tracer
+    # (8 bounces, roulette after 2), 1024 frames.  The learned path (paths end
+    # at the first bounce's hit, online training every frame, from an
+    # untrained cache) and the plain path each get the same GPU time, the
+    # learned path's 24 frames timed with CUDA events, training included.
+    # The cache lowers each frame's variance but costs more per frame than
+    # the bounces it replaces, so in this scene it does not beat the plain
+    # tracer at equal time (the bench's radiance_cache workload gives the
+    # bounds).  The test checks that it stays within 2x of the plain
+    # tracer's RMSE at equal time and reports the ratio.
+    from minotert_gb300.pathtracer import Camera, Pathtracer, TraceSettings, camera_consts
+    from minotert_gb300.scene import DeviceScene
+    wl, mesh, bvh = hf_workload
+    W, H = 480, 270
+    c = wl.camera
+    cam = Camera((W, H), c.verticalFov, c.nearPlane, c.position, c.yaw, c.pitch)
+    ds = DeviceScene.triangles(ctx, mesh, bvh)
+    pt = Pathtracer(ctx, ds, full_gbuffer=False)
+    ctx.blue_noise(blue_noise)
+    stream = ctx.stream()
+
+    def accumulate(frames, fn, start):
+        col = ctx.alloc(12 * W * H)
+        a, b = ctx.event(), ctx.event()
+        ctx.record(a, stream)
+        for f in range(frames):
+            pt.frame_counter = start + f
+            gb = pt.primaryRays((W, H), cam, cam, stream)
+            fn(gb, col, f)
+        ctx.record(b, stream)
+        ctx.sync(stream)
+        return col.download(np.float32, (H, W, 3)), ctx.elapsed_ms(a, b)
+
+    def plain(gb, col, f):
+        pt.secondaryRays(gb, cam, wl.sky, blue_noise, TraceSettings(1, 8, 2, 1, True, f), color=col, stream=stream)
+
+    ref, _ = accumulate(1024, plain, start=10000)
+    accumulate(4, plain, start=500)  # kernels loaded before anything is timed
+    cache = RadianceCache(ctx, default_config(query_vertex=1), bounds=(mesh.lo, mesh.hi))
+
+    def learned(gb, col, f):
+        params = TraceSettings(1, 1, 2, 1, True, f).params(wl.sky)
+        cache.frame(ds, gb, camera_consts(cam, cam, pt.frame_counter), params, col, train=True, stream=stream)
+
+    warm = RadianceCache(ctx, default_config(query_vertex=1), bounds=(mesh.lo, mesh.hi))
+    col = ctx.alloc(12 * W * H)
+    gb = pt.primaryRays((W, H), cam, cam, stream)
+    warm.frame(ds, gb, camera_consts(cam, cam, 0), TraceSettings(1, 1, 2, 1, True, 0).params(wl.sky), col,
+               train=True, stream=stream)
+    ctx.sync(stream)
+    warm.close()
+    img_l, ms_l = accumulate(24, learned, start=0)
+    # plain frames in the same GPU time (per-frame time from 16 timed frames)
+    _, ms16 = accumulate(16, plain, start=2000)
+    n_plain = max(1, int(ms_l / (ms16 / 16)))
+    img_p, ms_p = accumulate(n_plain, plain, start=0)
+    cache.close()
+    assert ctx.status() == 0
+    assert np.isfinite(img_l).all()
+    r_l, r_p = _rmse(img_l, ref), _rmse(img_p, ref)
+    print(f"equal GPU time: learned 24 frames {ms_l:.2f} ms RMSE {r_l:.4f}; plain {n_plain} frames {ms_p:.2f} ms "
+          f"RMSE {r_p:.4f}; RMSE ratio {r_l / r_p:.2f}")
+    assert abs(ms_p - ms_l) < 0.25 * ms_l
+    assert r_l < 2.0 * r_p
