@@ -667,6 +667,11 @@ def run_cache_experiment(args, world, rank, local, dist):
         pt.secondaryRays(gb, cam, sky, bn, TraceSettings(1, PLAIN["bounces"], PLAIN["rr_start"], PLAIN["rng_mode"],
                                                         True, f), color=col, stream=stream)
 
+    t_start = time.perf_counter()
+
+    def progress(what):
+        print(f"[radiance_cache {time.perf_counter() - t_start:7.1f} s] {what}", file=sys.stderr, flush=True)
+
     t0 = time.perf_counter()
     ref_frames = 4096
     ref, ref_ms, _ = run(ref_frames, 1 << 20, plain_fn)
@@ -681,6 +686,7 @@ def run_cache_experiment(args, world, rank, local, dist):
                               sun_e=sky.sun_irradiance, sky=sky.radiance)
     crop64, _, _ = oracle.pathtrace(bvh.nodes, bvh.tris, mesh.mats, consts, W, H, p["visibility"], p["hit_t"], bn, prm,
                                     precision=64, y0=y0, y1=y1)
+    progress("reference and its FP64 crop check")
     a, b = ref[y0:y1, x0:x1], crop64[y0:y1, x0:x1]
     ref_check = {"crop": [y0, y1, x0, x1], "rmse_vs_fp64": float(np.sqrt(np.mean((a - b) ** 2))),
                  "mean": float(b.mean()), "relative": float(np.sqrt(np.mean((a - b) ** 2)) / max(b.mean(), 1e-9))}
@@ -746,7 +752,10 @@ def run_cache_experiment(args, world, rank, local, dist):
                ctx.alloc(12 * W * H), train=True, stream=stream)
     ctx.sync(stream)
     warm.close()
-    curves = {name: learned_curve(*v) for name, v in variants.items()}
+    curves = {}
+    for name, v in variants.items():
+        curves[name] = learned_curve(*v)
+        progress(f"learned curve {name}")
 
     def bounds(query_vertex, train_frames=256, k=16):
         """What a cache could gain at best: after `train_frames` of online
@@ -792,8 +801,10 @@ def run_cache_experiment(args, world, rank, local, dist):
         plain_single.append(float(np.mean((img - ref) ** 2)))
     var_p, t_p = float(np.mean(plain_single)), float(plain_ms[-1] / nmax)
     lower = {}
+    progress("plain single frames")
     for qv in (1, 0):
         b = bounds(qv)
+        progress(f"bounds, query vertex {qv}")
         # time to RMSE tau: plain t_p var_p / tau^2; learned (t_trace + t_net) var_c / (tau^2 - bias^2).
         # The most a cache could give, with a free network (t_net = 0) and
         # this variance, at a target far above its bias:

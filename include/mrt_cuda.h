@@ -447,9 +447,14 @@ int mrt_cuda_cache_destroy(mrt_ctx* ctx, mrt_cache* cache);
 /* Scene box the positions are normalised by (queries use [0,1]^3). */
 int mrt_cuda_cache_set_bounds(mrt_ctx* ctx, mrt_cache* cache, const float lo[3], const float hi[3]);
 /* Queries: device rows of 9 floats (position in [0,1]^3, unit normal,
- * unit outgoing direction); out: device rows of 3 floats. */
+ * unit outgoing direction); out: device rows of 3 floats.  Inference runs
+ * on tcgen05 (128-query tiles, FP32 accumulators in tensor memory); a
+ * tensor-core wait that runs out sets MRT_STATUS_PIPE_TIMEOUT. */
 int mrt_cuda_cache_infer(mrt_ctx* ctx, mrt_cache* cache, const float* queries, uint32_t n,
                          float* out, void* stream);
+/* enable = 0: inference on mma.sync instead (the earlier kernel, kept for
+ * comparison); 1 (default): tcgen05. */
+int mrt_cuda_cache_set_tcgen05(mrt_cache* cache, int enable);
 /* One training step on n device samples (queries + 3-float targets; n is
  * rounded down to a multiple of 16): forward, loss, backward; with
  * apply_update an Adam step (gradients are cleared), otherwise gradients

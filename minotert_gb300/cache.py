@@ -45,6 +45,10 @@ class RadianceCache:
         hi = (C.c_float * 3)(*map(float, hi))
         self.ctx.check(lib().mrt_cuda_cache_set_bounds(self.ctx.handle, self._h, lo, hi), "cache_set_bounds")
 
+    def set_tcgen05(self, enable: bool):
+        """Inference on tcgen05 (default) or on the mma.sync kernel."""
+        self.ctx.check(lib().mrt_cuda_cache_set_tcgen05(self._h, int(enable)), "cache_set_tcgen05")
+
     def infer(self, d_queries, n: int, d_out, stream=None):
         self.ctx.check(lib().mrt_cuda_cache_infer(self.ctx.handle, self._h, ptr(d_queries), n, ptr(d_out),
                                                   ptr(stream)), "cache_infer")

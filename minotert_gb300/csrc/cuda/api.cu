@@ -191,7 +191,7 @@ uint32_t bvh8_depth(const mrt_bvh8_node* nodes, uint32_t n) {
 
 // learned radiance cache (nrc.cu)
 cudaError_t cache_infer(const mrt_cache* c, const float* q, uint32_t n, const uint32_t* n_dev, float* out,
-                        cudaStream_t s);
+                        uint32_t* status, cudaStream_t s);
 int cache_frame_buffers(mrt_ctx* ctx, mrt_cache* c, size_t n, float** q, float4** pb, float** pred);
 int cache_train_frame(mrt_ctx* ctx, mrt_cache* c, const DevScene& sc, const FrameParams& fp, const TraceParams& tp,
                       uint32_t* status, cudaStream_t s);
@@ -809,7 +809,7 @@ int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
                                                  refill_min(ctx), s));
         const uint32_t npix = W * H;
         MRT_LAUNCH(3, 0, launch_cache_query_primary(scene->dev, fp, *gbuffer, q, pb, ctx->d_status, s));
-        MRT_LAUNCH(7, 0, cache_infer(cache, q, npix, nullptr, pred, s));
+        MRT_LAUNCH(7, 0, cache_infer(cache, q, npix, nullptr, pred, ctx->d_status, s));
         MRT_LAUNCH(3, 0, launch_cache_apply(wb, nullptr, npix, pred, pb, s));
     } else {
         // one diffuse bounce, then the cache supplies the indirect light at
@@ -825,7 +825,7 @@ int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
             MRT_LAUNCH(2, 1, launch_trace_shadow(scene->dev, wb, tp, 1, tblocks, ctx->d_status, ctx->counters, dyn_sh,
                                                  refill_min(ctx), s));
         MRT_LAUNCH(3, 1, launch_cache_query(scene->dev, tp, wb, q, pb, ctx->d_status, s));
-        MRT_LAUNCH(7, 1, cache_infer(cache, q, uint32_t(wb.cap), wb.counters + kCntExt + 1, pred, s));
+        MRT_LAUNCH(7, 1, cache_infer(cache, q, uint32_t(wb.cap), wb.counters + kCntExt + 1, pred, ctx->d_status, s));
         MRT_LAUNCH(3, 1, launch_cache_apply(wb, wb.counters + kCntExt + 1, uint32_t(wb.cap), pred, pb, s));
     }
     MRT_LAUNCH(3, 0, launch_tally(wb, s));

@@ -30,17 +30,6 @@ constexpr int kTcPix = 128;             // output pixels per row of a CTA (MMA M
 constexpr int kTcHalo = kTcPix + 2;     // input pixels per halo row
 constexpr int kTcPlane = kTcHalo * 16;  // bytes of one 8-channel halo plane
 __host__ __device__ constexpr int tc_abytes(int rows) { return (rows + 2) * 2 * kTcPlane; }
-constexpr uint32_t kTcSpin = 1u << 20;  // mbarrier wait cap (polls; a poll may suspend ~1 us)
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-// shared-memory matrix descriptor: start, leading (K) and stride (M/N) byte
-// offsets, descriptor version 1, no swizzle
-__device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-    return uint64_t((saddr >> 4) & 0x3FFFu) | (uint64_t((lbo >> 4) & 0x3FFFu) << 16) |
-           (uint64_t((sbo >> 4) & 0x3FFFu) << 32) | (uint64_t(1) << 46);
-}
 // instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
 // K-major, N and M
 __host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
@@ -59,18 +48,6 @@ __host__ __device__ constexpr size_t tc_stage_bytes(int cout, int rows) {
 }
 __host__ __device__ constexpr size_t tc_smem_bytes(int cout, int rows, int stages) {
     return stages * tc_stage_bytes(cout, rows) + 64;
-}
-
-// Bounded wait for phase `parity` of an mbarrier; false when the cap ran out.
-__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
-    uint32_t done = 0;
-    for (uint32_t spins = 0; !done && spins < kTcSpin; ++spins)
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(mbar), "r"(parity)
-            : "memory");
-    return done != 0;
 }
 
 // 16-byte asynchronous copy global -> shared; zero-filled when !valid (the

@@ -24,6 +24,7 @@
 // Backward: FP32 kernels on the CUDA cores for the data, weight and bias
 // gradients, reading the stored BF16 activations.
 #include "internal.hpp"
+#include "tcgen05.cuh"
 
 #include <cuda.h>  // CUtensorMap (the encoder is fetched through the runtime)
 #include <cuda_bf16.h>

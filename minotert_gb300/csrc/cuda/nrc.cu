@@ -17,6 +17,7 @@
 // Weight gradients are FP32 sums over rows on the CUDA cores; the grid's
 // gradients are FP32 atomics; Adam keeps FP32 master weights.
 #include "internal.hpp"
+#include "tcgen05.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -276,6 +277,201 @@ k_cache_infer(CacheDev c, const float* q, uint32_t n_max, const uint32_t* n_dev,
             for (int k = 0; k < 3; ++k) out[size_t(base + lane) * 3 + k] = O[lane * 3 + k];
         __syncwarp();
     }
+}
+
+// ---------------------------------------------------------- MLP on tcgen05
+//
+// Inference on the 5th-generation tensor cores.  A CTA of 256 threads owns
+// a tile of 128 queries at a time (persistent over the tiles): the encoded
+// input rows are written into shared memory in the canonical K-major layout
+// (eight 2 KB planes, plane k holding elements 8k..8k+7 of each of the 128
+// rows), then each layer is one 128 x 64 x 64 product issued by one thread
+// as four tcgen05.mma kind::f16 (K = 16 each: FP16 A and B, FP32 accumulator
+// in 64 tensor-memory columns) and committed to an mbarrier; all 8 warps
+// read the accumulators back (warp w: lanes 32 (w mod 4) .., columns
+// 32 (w / 4) ..), apply ReLU, round to FP16 and write them over the tile as
+// the next layer's A operand.  The output layer is N = 16 (3 used).  The
+// weights sit in shared memory in the same layout for the whole launch
+// (4 x 8 KB + 2 KB).  Every wait is bounded: on a timeout the CTA sets
+// MRT_STATUS_PIPE_TIMEOUT, stops, waits (bounded) for its last commit and
+// frees its tensor memory.
+
+constexpr int kTcRows = 128;                               // queries per tile (MMA M)
+constexpr int kTcPlaneA = kTcRows * 16;                    // bytes of one 8-element K plane of the tile
+constexpr int kTcLayerB = kWidth * 16 * (kWidth / 8);      // 8 KB: one hidden layer's weights
+constexpr int kTcOutB = kOutRows * 16 * (kWidth / 8);      // 2 KB: the output layer's weights
+constexpr int kTcWBytes = kHidden * kTcLayerB + kTcOutB;   // 34 KB
+constexpr int kTcSmem = kTcWBytes + (kWidth / 8) * kTcPlaneA + 64;
+constexpr int kTcThreads = 256;
+
+// instruction descriptor of kind::f16 with FP16 A and B, FP32 accumulator,
+// both operands K-major
+__host__ __device__ constexpr uint32_t mlp_idesc(int m, int n) {
+    return (1u << 4) | (uint32_t(n >> 3) << 17) | (uint32_t(m >> 4) << 24);
+}
+
+// The weights (row-major [out][64] halves, hidden layers then the output
+// rows) into the K-plane layout: hidden layer l at l * 8 KB, plane kc of it
+// holding element 8 kc .. 8 kc + 7 of its 64 rows; the output layer after
+// them with planes of 16 rows.
+__device__ void tc_load_weights(const __half* W, unsigned char* sW) {
+    for (int i = threadIdx.x; i < (kHidden * kWidth + kOutRows) * (kWidth / 8); i += blockDim.x) {
+        const int kc = i % (kWidth / 8), row = i / (kWidth / 8);  // row over all layers' output rows
+        const int l = row / kWidth, n = row % kWidth;
+        const uint4 v = *reinterpret_cast<const uint4*>(W + size_t(row) * kWidth + kc * 8);
+        const int off = l < kHidden ? l * kTcLayerB + kc * (kWidth * 16) + n * 16
+                                    : kHidden * kTcLayerB + kc * (kOutRows * 16) + (row - kHidden * kWidth) * 16;
+        *reinterpret_cast<uint4*>(sW + off) = v;
+    }
+}
+
+__device__ __forceinline__ void tc_tmem_ld16(uint32_t taddr, uint32_t v[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr));
+}
+
+__global__ void __launch_bounds__(kTcThreads)
+k_cache_infer_tc(CacheDev c, const float* q, uint32_t n_max, const uint32_t* n_dev, float* out, uint32_t* status) {
+    extern __shared__ __align__(128) unsigned char tsm[];
+    unsigned char* sW = tsm;
+    unsigned char* sA = tsm + kTcWBytes;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(sA + (kWidth / 8) * kTcPlaneA);
+    uint32_t* slot = reinterpret_cast<uint32_t*>(mbar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t n = n_dev ? min(*n_dev, n_max) : n_max;
+    const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                     "r"(uint32_t(kWidth))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc_load_weights(c.W, sW);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = *slot;
+    const uint32_t a0 = smem_u32(sA), w0 = smem_u32(sW), mb = smem_u32(mbar);
+    uint32_t phase = 0u;
+    bool timed_out = false;
+    bool pending = false;  // a commit not yet seen complete
+
+    const int r = tid & (kTcRows - 1), half = tid >> 7;  // encoding: row, half of the levels
+    const int quad = warp & 3, ch = warp >> 2;           // epilogue: TMEM lane quadrant, column half
+    const int er = 32 * quad + lane;                     // epilogue row
+    for (uint32_t tile = blockIdx.x; tile < tiles && !timed_out; tile += gridDim.x) {
+        const uint32_t row = tile * kTcRows + uint32_t(r);
+        // encode row r: levels 8 half .. 8 half + 7 (and the tail in half 0)
+        float qq[9];
+        for (int k = 0; k < 9; ++k) qq[k] = row < n ? q[size_t(row) * 9 + k] : 0.0f;
+        {
+            const float px = fminf(fmaxf(qq[0], 0.0f), 1.0f), py = fminf(fmaxf(qq[1], 0.0f), 1.0f),
+                        pz = fminf(fmaxf(qq[2], 0.0f), 1.0f);
+            // 8 levels = 16 features: element 2l of the row is in plane l / 4,
+            // 4 (l mod 4) bytes into the row's 16
+#pragma unroll 2
+            for (int j = 0; j < 8; ++j) {
+                const int l = 8 * half + j;
+                uint32_t idx[8];
+                float w[8];
+                level_corners(c.spec, l, px, py, pz, idx, w);
+                float f0 = 0.0f, f1 = 0.0f;
+#pragma unroll
+                for (int cc = 0; cc < 8; ++cc) {
+                    const float2 v = __half22float2(c.grid[idx[cc]]);
+                    f0 = fmaf(w[cc], v.x, f0);
+                    f1 = fmaf(w[cc], v.y, f1);
+                }
+                *reinterpret_cast<uint32_t*>(sA + (l >> 2) * kTcPlaneA + r * 16 + (l & 3) * 4) = pack_half2(f0, f1);
+            }
+            if (half == 0) {  // normal and direction: elements 32..37 (plane 4), 38..39 zero
+                *reinterpret_cast<uint4*>(sA + 4 * kTcPlaneA + r * 16) =
+                    make_uint4(pack_half2(qq[3], qq[4]), pack_half2(qq[5], qq[6]), pack_half2(qq[7], qq[8]), 0u);
+            } else {          // zero padding: planes 5..7
+#pragma unroll
+                for (int pl = 5; pl < 8; ++pl)
+                    *reinterpret_cast<uint4*>(sA + pl * kTcPlaneA + r * 16) = make_uint4(0u, 0u, 0u, 0u);
+            }
+        }
+        for (int L = 0; L <= kHidden; ++L) {
+            const int nn = L < kHidden ? kWidth : kOutRows;
+            // the tile's A operand is in shared memory: hand it to the tensor cores
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncthreads();
+            if (tid == 0) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t wb = w0 + uint32_t(L * kTcLayerB);
+                const uint32_t idesc = L < kHidden ? mlp_idesc(kTcRows, kWidth) : mlp_idesc(kTcRows, kOutRows);
+#pragma unroll
+                for (int k = 0; k < kWidth / 16; ++k) {
+                    const uint64_t ad = tc_sdesc(a0 + uint32_t(2 * k * kTcPlaneA), kTcPlaneA, 128);
+                    const uint64_t bd = tc_sdesc(wb + uint32_t(2 * k * nn * 16), uint32_t(nn * 16), 128);
+                    asm volatile(
+                        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr),
+                        "l"(ad), "l"(bd), "r"(idesc), "r"(uint32_t(k > 0))
+                        : "memory");
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)
+                             : "memory");
+            }
+            pending = true;
+            const bool ok = tc_wait(mb, phase);
+            if (ok) {
+                phase ^= 1u;
+                pending = false;
+            }
+            if (__syncthreads_or(!ok)) {
+                timed_out = true;
+                if (tid == 0) atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (L < kHidden) {
+                // warp w: rows 32 quad .., columns 32 ch .. 32 ch + 31 -> planes 4 ch .. 4 ch + 3
+                uint32_t v[32];
+                const uint32_t ta = taddr + (uint32_t(32 * quad) << 16) + uint32_t(32 * ch);
+                tc_tmem_ld16(ta, v);
+                tc_tmem_ld16(ta + 16u, v + 16);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int pl = 0; pl < 4; ++pl) {
+                    uint32_t h[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        h[e] = pack_half2(fmaxf(__uint_as_float(v[8 * pl + 2 * e]), 0.0f),
+                                          fmaxf(__uint_as_float(v[8 * pl + 2 * e + 1]), 0.0f));
+                    *reinterpret_cast<uint4*>(sA + (4 * ch + pl) * kTcPlaneA + er * 16) =
+                        make_uint4(h[0], h[1], h[2], h[3]);
+                }
+            } else if (ch == 0) {
+                uint32_t v[16];
+                tc_tmem_ld16(taddr + (uint32_t(32 * quad) << 16), v);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                const uint32_t orow = tile * kTcRows + uint32_t(er);
+                if (orow < n)
+                    for (int k = 0; k < 3; ++k) out[size_t(orow) * 3 + k] = __uint_as_float(v[k]);
+            }
+        }
+    }
+    // a commit still outstanding after a timeout: wait for it (bounded)
+    // before the tensor memory is freed
+    if (pending && !tc_wait(mb, phase)) atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(uint32_t(kWidth))
+                     : "memory");
 }
 
 // Training forward: stores the input rows and hidden activations, the
@@ -548,6 +744,9 @@ struct mrt_cache {
     size_t qcap = 0;
     float *qq = nullptr, *qpred = nullptr;
     float4* qpb = nullptr;
+    // inference on tcgen05 (k_cache_infer_tc, default) or mma.sync (k_cache_infer)
+    bool tcgen05 = true;
+    int sm_count = 0;
 };
 
 namespace {
@@ -587,8 +786,14 @@ uint32_t cache_query_vertex(const mrt_cache* c) { return c->cfg.query_vertex; }
 // Inference over device rows of 9 floats; with n_dev the row count is read
 // on the device (at most n).
 cudaError_t cache_infer(const mrt_cache* c, const float* q, uint32_t n, const uint32_t* n_dev, float* out,
-                        cudaStream_t s) {
+                        uint32_t* status, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
+    if (c->tcgen05) {  // persistent: up to 4 CTAs (51 KB of shared memory, 64 TMEM columns each) per SM
+        const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
+        const uint32_t blocks = std::min<uint32_t>(tiles, uint32_t(c->sm_count) * 4u);
+        k_cache_infer_tc<<<blocks, kTcThreads, kTcSmem, s>>>(c->dev, q, n, n_dev, out, status);
+        return cudaGetLastError();
+    }
     const uint32_t tiles = (n + 15u) / 16u;
     const uint32_t blocks = std::min<uint32_t>((tiles + kMlpWarps - 1) / kMlpWarps, 4096u);
     k_cache_infer<<<blocks, kMlpWarps * 32, smem_infer(), s>>>(c->dev, q, n, n_dev, out);
@@ -723,6 +928,7 @@ int mrt_cuda_cache_create(mrt_ctx* ctx, const mrt_cache_config* cfg, mrt_cache**
     }
     if (!ok ||
         cudaFuncSetAttribute(k_cache_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_infer())) != cudaSuccess ||
+        cudaFuncSetAttribute(k_cache_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) != cudaSuccess ||
         cudaFuncSetAttribute(k_cache_train_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_infer())) != cudaSuccess ||
         cudaFuncSetAttribute(k_cache_train_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bwd())) != cudaSuccess) {
         cudaGetLastError();
@@ -732,7 +938,14 @@ int mrt_cuda_cache_create(mrt_ctx* ctx, const mrt_cache_config* cfg, mrt_cache**
     c->dev.grid = c->g16;
     c->dev.W = c->w16;
     c->dev.WT = c->wt16;
+    c->sm_count = ctx->sm_count;
     *out = c;
+    return MRT_OK;
+}
+
+int mrt_cuda_cache_set_tcgen05(mrt_cache* c, int enable) {
+    if (!c) return MRT_EINVAL;
+    c->tcgen05 = enable != 0;
     return MRT_OK;
 }
 
@@ -761,7 +974,7 @@ int mrt_cuda_cache_set_bounds(mrt_ctx* ctx, mrt_cache* c, const float lo[3], con
 int mrt_cuda_cache_infer(mrt_ctx* ctx, mrt_cache* c, const float* queries, uint32_t n, float* out, void* stream) {
     if (!ctx || !c || (n && (!queries || !out))) return set_error(ctx, MRT_EINVAL, "cache_infer: bad arguments");
     cudaSetDevice(ctx->device);
-    if (cache_infer(c, queries, n, nullptr, out, static_cast<cudaStream_t>(stream)) != cudaSuccess)
+    if (cache_infer(c, queries, n, nullptr, out, ctx->d_status, static_cast<cudaStream_t>(stream)) != cudaSuccess)
         return set_error(ctx, MRT_ECUDA, "cache_infer: launch failed");
     ctx->launches++;
     return MRT_OK;

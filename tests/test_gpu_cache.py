@@ -48,6 +48,33 @@ def test_cache_forward_matches_oracle(ctx):
     assert np.mean(err) < 2e-3 * max(1.0, np.mean(np.abs(ref)))
 
 
+@pytest.mark.parametrize("n", [1, 127, 1000, 200001])
+def test_cache_inference_tcgen05_matches_mma_sync_and_oracle(ctx, n):
+    # the tcgen05 kernel (128-query tiles, accumulators in tensor memory) and
+    # the mma.sync kernel on the same weights: both FP16 operands with FP32
+    # accumulation, so they differ only where an FP32 sum rounds to another
+    # FP16 activation.  Ragged sizes cover partial tiles; 200,001 queries
+    # (1,563 tiles) take the persistent CTAs (4 per SM) round the tile loop
+    c, W, G = _cache(ctx, seed=9)
+    q = _queries(n, 10)
+    d_q, d_tc, d_mma = ctx.to_device(q), ctx.alloc(12 * n), ctx.alloc(12 * n)
+    c.infer(d_q, n, d_tc)
+    c.set_tcgen05(False)
+    c.infer(d_q, n, d_mma)
+    c.set_tcgen05(True)
+    assert ctx.status() == 0
+    y_tc, y_mma = d_tc.download(np.float32, (n, 3)), d_mma.download(np.float32, (n, 3))
+    assert np.all(np.isfinite(y_tc))
+    scale = max(1.0, float(np.max(np.abs(y_mma))))
+    assert np.max(np.abs(y_tc - y_mma)) < 1e-2 * scale
+    assert np.mean(np.abs(y_tc - y_mma)) < 1e-3 * scale
+    sub = slice(0, min(n, 1000))
+    ref = nrc.predict(G.astype(np.float64), W.astype(np.float64), q[sub].astype(np.float64), LOG2_T, 16.0, 512.0)
+    err = np.abs(y_tc[sub] - ref)
+    assert np.max(err) < 2e-2 * max(1.0, np.max(np.abs(ref)))
+    assert np.mean(err) < 2e-3 * max(1.0, np.mean(np.abs(ref)))
+
+
 def test_cache_gradients_match_oracle(ctx):
     c, W, G = _cache(ctx, seed=3)
     q = _queries(512, 4)
