@@ -83,6 +83,13 @@ typedef struct mrt_bvh_build_params {
                                 triangle test, percent (0 = 50: splitting
                                 small leaves is cheap, the collapse packs
                                 the pieces into the same 8-wide node)        */
+    uint32_t collapse;       /* BVH2 -> BVH8: 0 = greedy (open the child of
+                                largest area until 8 slots are used), 1 =
+                                SAH-optimal (dynamic programming over how
+                                many child slots each subtree gets)          */
+    uint32_t prim_cost_pct;  /* SAH-optimal collapse: cost of a triangle
+                                test relative to visiting an 8-wide node,
+                                percent (0 = 30)                             */
 } mrt_bvh_build_params;
 
 typedef struct mrt_bvh8 {

@@ -98,7 +98,7 @@ class Mesh_C(C.Structure):
 
 class BvhBuildParams(C.Structure):
     _fields_ = [("sah_bins", C.c_uint32), ("max_leaf_tris", C.c_uint32), ("threads", C.c_uint32),
-                ("trav_cost_pct", C.c_uint32)]
+                ("trav_cost_pct", C.c_uint32), ("collapse", C.c_uint32), ("prim_cost_pct", C.c_uint32)]
 
 
 class Bvh8_C(C.Structure):

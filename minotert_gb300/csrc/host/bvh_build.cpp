@@ -4,11 +4,14 @@
 // 77-83); this module is new and follows published methods:
 //   - binned SAH construction (Wald, "On fast construction of SAH-based
 //     bounding volume hierarchies", RT 2007), 64 bins per axis;
-//   - top-down collapse to 8-wide nodes by repeatedly opening the child of
-//     largest surface area, leaves of <= 3 triangles, <= 24 per node, and
-//     octant-ordered child slots with 8-bit quantised boxes (Ylitie, Karras
-//     & Laine, "Efficient incoherent ray traversal on GPUs through
-//     compressed wide BVHs", HPG 2017).
+//   - collapse to 8-wide nodes by the SAH-optimal dynamic programme of
+//     Ylitie, Karras & Laine, "Efficient incoherent ray traversal on GPUs
+//     through compressed wide BVHs", HPG 2017 (for every BVH2 subtree and
+//     every slot budget 1..8, the cheapest way to represent it as one leaf,
+//     one 8-wide node or a forest over the budget), or greedily by opening
+//     the child of largest surface area; leaves of <= 3 triangles, <= 24 per
+//     node, octant-ordered child slots with 8-bit quantised boxes (same
+//     paper).
 // Quantised boxes are conservative by construction: every child box is
 // rounded outward and widened by one quantum when it lands on the grid, so
 // a zero-thickness child (a flat triangle, a box face) still has a slab of
@@ -22,6 +25,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <future>
+#include <memory>
 #include <thread>
 #include <vector>
 
@@ -156,9 +160,89 @@ struct Builder2 {
     }
 };
 
+// SAH-optimal collapse (Ylitie et al. 2017, section 3.2).  cost[x][i] is
+// the least SAH cost of representing BVH2 subtree x by at most i child
+// slots of an 8-wide node: one slot (x as a leaf of <= 3 triangles, cost
+// area * tris * c_prim, or as an 8-wide node, cost area * c_node plus the
+// best distribution of its two children over 8 slots), or, for i >= 2, its
+// two children sharing the i slots.  Costs are relative (areas are not
+// divided by the root's).
+struct CollapseDP {
+    struct Entry {
+        float cost[9];     // [1..8]
+        int8_t split[9];   // [2..8]: slots of the left child when x is opened over i slots (0: x is one slot)
+        int8_t dsplit[9];  // [2..8]: the best left/right share when x is opened over i slots
+        bool leaf;         // as one slot: a leaf (else an 8-wide node)
+    };
+    const std::vector<Node2>& n2;
+    double c_node, c_prim;
+    std::vector<Entry> e;
+
+    CollapseDP(const std::vector<Node2>& nodes, size_t count, double cn, double cp)
+        : n2(nodes), c_node(cn), c_prim(cp), e(count) {}
+
+    void solve(uint32_t x) {
+        const Node2& n = n2[x];
+        Entry& E = e[x];
+        const double A = n.box.area();
+        if (n.count) {  // a BVH2 leaf is always one leaf slot
+            E.leaf = true;
+            for (int i = 1; i <= 8; ++i) {
+                E.cost[i] = float(A * double(n.count) * c_prim);
+                E.split[i] = 0;
+                E.dsplit[i] = 0;
+            }
+            return;
+        }
+        solve(n.left);
+        solve(n.right);
+        const Entry& L = e[n.left];
+        const Entry& R = e[n.right];
+        double dist[9];
+        for (int j = 2; j <= 8; ++j) {
+            double best = INFINITY;
+            int bk = 1;
+            for (int k = 1; k < j; ++k) {
+                const double c = double(L.cost[k]) + double(R.cost[j - k]);
+                if (c < best) { best = c; bk = k; }
+            }
+            dist[j] = best;
+            E.dsplit[j] = int8_t(bk);
+        }
+        const double as_node = A * c_node + dist[8];
+        const double as_leaf = n.tris <= 3 ? A * double(n.tris) * c_prim : INFINITY;
+        E.leaf = as_leaf <= as_node;
+        E.cost[1] = float(std::min(as_leaf, as_node));
+        for (int i = 2; i <= 8; ++i) {
+            if (dist[i] < double(E.cost[1])) {
+                E.cost[i] = float(dist[i]);
+                E.split[i] = E.dsplit[i];
+            } else {
+                E.cost[i] = E.cost[1];
+                E.split[i] = 0;
+            }
+        }
+    }
+
+    // the slots of subtree x under a budget of i
+    void slots(uint32_t x, int i, std::vector<uint32_t>& out) const {
+        const Entry& E = e[x];
+        if (i <= 1 || E.split[i] == 0) { out.push_back(x); return; }
+        slots(n2[x].left, E.split[i], out);
+        slots(n2[x].right, i - E.split[i], out);
+    }
+    // the children of x made an 8-wide node
+    void children(uint32_t x, std::vector<uint32_t>& out) const {
+        const Entry& E = e[x];
+        slots(n2[x].left, E.dsplit[8], out);
+        slots(n2[x].right, 8 - E.dsplit[8], out);
+    }
+};
+
 struct Collapser {
     const Builder2& b2;
     const float* verts;
+    const CollapseDP* dp = nullptr;  // null: greedy collapse
     std::vector<mrt_bvh8_node> nodes;
     std::vector<mrt_tri> tris;
     uint32_t max_depth = 0;
@@ -167,6 +251,13 @@ struct Collapser {
     double root_area = 1.0;
 
     explicit Collapser(const Builder2& b, const float* v) : b2(b), verts(v) {}
+
+    // a child slot holding subtree c2 is a leaf (else an 8-wide node)
+    bool is_leaf(uint32_t c2) const {
+        const Node2& c = b2.nodes[c2];
+        if (c.count) return true;
+        return dp ? dp->e[c2].leaf : c.tris <= 3;
+    }
 
     void collect_tris(uint32_t ni, std::vector<uint32_t>& out) const {
         const Node2& n = b2.nodes[ni];
@@ -203,8 +294,9 @@ struct Collapser {
         // 1) gather up to 8 child subtrees by opening the largest ones
         std::vector<uint32_t> cand;
         if (r.count) cand.push_back(root2);
+        else if (dp) dp->children(root2, cand);
         else { cand.push_back(r.left); cand.push_back(r.right); }
-        for (int pass = 0; pass < 2; ++pass) {
+        for (int pass = 0; pass < 2 && !dp; ++pass) {
             while (cand.size() < 8) {
                 int pick = -1;
                 double best = -1.0;
@@ -263,7 +355,7 @@ struct Collapser {
         // internal children get a contiguous block in slot order
         uint32_t n_int = 0;
         for (int s = 0; s < 8; ++s)
-            if (child_at[s] >= 0 && b2.nodes[cand[child_at[s]]].tris > 3) n_int++;
+            if (child_at[s] >= 0 && !is_leaf(cand[child_at[s]])) n_int++;
         uint32_t child_base = uint32_t(nodes.size());
         nodes.resize(nodes.size() + n_int);
         nd.child_base = child_base;
@@ -285,7 +377,7 @@ struct Collapser {
                 qlo[a][s] = uint8_t(fl);
                 qhi[a][s] = uint8_t(ch);
             }
-            if (c.tris > 3) {
+            if (!is_leaf(c2)) {
                 nd.imask |= uint8_t(1u << s);
                 nd.meta[s] = uint8_t(0x20 | (24 + s));
                 recurse.push_back({child_base + k_int, c2});
@@ -364,6 +456,13 @@ int mrt_bvh8_build(const float* verts, uint32_t tri_count, const mrt_bvh_build_p
 
     Collapser c(b, verts);
     c.root_area = std::max(1e-30, b.nodes[root].box.area());
+    std::unique_ptr<CollapseDP> dp;
+    if (params && params->collapse == 1) {
+        const double cp = params && params->prim_cost_pct ? double(params->prim_cost_pct) / 100.0 : 0.3;
+        dp.reset(new CollapseDP(b.nodes, b.next.load(), 1.0, cp));
+        dp->solve(root);
+        c.dp = dp.get();
+    }
     c.nodes.reserve(tri_count / 3 + 16);
     c.tris.reserve(tri_count);
     c.nodes.resize(1);

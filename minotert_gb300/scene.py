@@ -70,11 +70,15 @@ class Bvh8:
     build_ms: float
 
 
-def build_bvh8(mesh_or_verts, bins: int = 64, threads: int = 0, trav_cost: float = 0.5) -> Bvh8:
+def build_bvh8(mesh_or_verts, bins: int = 64, threads: int = 0, trav_cost: float = 0.5, collapse: int = 0,
+               prim_cost: float = 0.3) -> Bvh8:
+    """SAH BVH2 collapsed to BVH8: collapse 0 = greedy largest-area
+    opening (default), 1 = SAH-optimal (dynamic programming, with prim_cost
+    the cost of a triangle test relative to an 8-wide node visit)."""
     verts = mesh_or_verts.verts if isinstance(mesh_or_verts, Mesh) else np.asarray(mesh_or_verts)
     verts = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 9)
     out = Bvh8_C()
-    params = BvhBuildParams(bins, 3, threads, int(round(trav_cost * 100)))
+    params = BvhBuildParams(bins, 3, threads, int(round(trav_cost * 100)), collapse, int(round(prim_cost * 100)))
     rc = lib().mrt_bvh8_build(ptr(verts), verts.shape[0], C.byref(params), C.byref(out))
     if rc:
         raise MrtError(rc, "mrt_bvh8_build")

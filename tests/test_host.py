@@ -102,6 +102,28 @@ def test_bvh_build_quality_and_validity(built_lib, ico_workload):
     assert len(bvh.nodes) < mesh.tri_count / 6
 
 
+def test_sah_optimal_collapse_is_valid_and_exact(built_lib, hf_workload):
+    # the dynamic-programming collapse (Ylitie et al. 2017) builds a valid
+    # BVH8 whose closest hits equal brute force, as the greedy one does, and
+    # degenerate inputs still build
+    from minotert_gb300 import scene
+    from conftest import random_rays
+    _, mesh, greedy = hf_workload
+    for prim_cost in (0.3, 0.5):
+        b = scene.build_bvh8(mesh, collapse=1, prim_cost=prim_cost)
+        assert oracle.bvh8_validate(b.nodes, b.tris, mesh.verts)["error"] == 0
+        assert len(b.tris) == mesh.tri_count and b.depth <= 24
+        rays = random_rays(2000, mesh.lo, mesh.hi, seed=21)
+        h, st = oracle.trace_bvh8(b.nodes, b.tris, rays)
+        assert st == 0
+        assert np.array_equal(h["prim"], oracle.trace_brute(mesh.verts, rays)["prim"])
+        assert np.array_equal(h["t"].view(np.uint32), oracle.trace_bvh8(greedy.nodes, greedy.tris, rays)[0]["t"].view(np.uint32))
+    one = np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32)
+    for v in (one, np.repeat(one, 100, axis=0)):
+        b = scene.build_bvh8(v, collapse=1)
+        assert oracle.bvh8_validate(b.nodes, b.tris, v)["error"] == 0
+
+
 def test_bvh_degenerate_inputs(built_lib):
     from minotert_gb300 import scene
     # one triangle, coincident triangles, zero-area triangles
