@@ -500,6 +500,12 @@ def batched_record(args, steps, warmup, world, rank, local, dist, sweep=True, e2
                                          "refill_min": rm}
                                         for b in (4, 6, 8) for sd in (16, 24, 32) for sp in (1, 0)
                                         for rm in (1, 4, 8, 16, 24)])
+    else:
+        # the schedule the sweep picks on GB300 (10.52 ms per step; 24 stack
+        # entries 10.55): 8 blocks per SM, 16 stack entries, spread triangle
+        # tests, compaction once 8 lanes are idle
+        ctx.set_tuning(trace_blocks_per_sm=8, dynamic_fetch=1, primary_persistent=0,
+                       sort_min_rays=autotune.SORT_NEVER, stack_depth=16, tri_spread=1, refill_min=8)
     for _ in range(warmup):
         step(stream)
     ctx.sync(stream)
@@ -602,7 +608,7 @@ def batched_record(args, steps, warmup, world, rank, local, dist, sweep=True, e2
                                                                        st.extension_rays[:wl.settings.bounces]]},
                          "ms_per_step_graph": statistics.mean(ms), "ms_per_step_direct": statistics.mean(ms_direct),
                          "autotune": ({"best": tune["tuning"], "results": tune["results"]} if tune else
-                                      {"best": "tuned defaults, no sweep"})},
+                                      {"best": "the schedule the sweep picks (8 blocks/SM, 16 stack entries, spread tests, refill at 8), no sweep"})},
            "roofline": roofline, "gpu_launches": int(st.launches), "clocks": clk, "device_status": status}
     if e2e is not None:
         out["e2e"] = e2e
@@ -1199,9 +1205,10 @@ def run_reference_scene(args, world, rank, local, dist):
 
 def run_network_kernels(args, world, rank, local, dist):
     """Inference time of the two networks at 1920x1080 with random weights
-    and inputs: the CNN denoiser on one frame of features and the radiance
-    cache on 2,073,600 queries (CUDA events, --steps timed runs after
-    --warmup).  The network-kernel ncu captures profile this command."""
+    and inputs: the CNN denoiser on one frame of features (default kernels,
+    and the per-tile tcgen05 and mma.sync kernels for comparison) and the
+    radiance cache on 2,073,600 queries (tcgen05, and mma.sync) (CUDA
+    events, --steps timed runs after --warmup).  The network-kernel ncu captures profile this command."""
     from minotert_gb300 import build as _build
     _build.build()
     from minotert_gb300._lib import Context
@@ -1238,12 +1245,22 @@ def run_network_kernels(args, world, rank, local, dist):
         return float(np.median(ts))
 
     den_ms = timed(lambda: den.infer(dx, 1, W, H, do))
+    den_modes = {}
+    for mode, name in ((1, "tcgen05_per_tile"), (0, "mma_sync")):
+        den.set_tcgen05(mode)
+        den_modes[name] = timed(lambda: den.infer(dx, 1, W, H, do))
+    den.set_tcgen05(2)
     cache_ms = timed(lambda: cache.infer(dq, n, dout))
+    cache.set_tcgen05(False)
+    cache_mma_ms = timed(lambda: cache.infer(dq, n, dout))
+    cache.set_tcgen05(True)
     flop = 2 * 9 * sum((ca + cb) * co * (W * H) // (4 ** sc) for ca, cb, co, ups, relu, sc in
                        __import__("minotert_gb300.denoiser", fromlist=["TOPOLOGY"]).TOPOLOGY)
     print(json.dumps({"metric": "network inference ms at 1920x1080", "unit": "ms", "denoiser_ms": den_ms,
                       "denoiser_tflops": flop / den_ms / 1e9, "denoiser_gflop": flop / 1e9,
+                      "denoiser_ms_other_kernels": den_modes,
                       "cache_ms_2073600_queries": cache_ms, "cache_mqueries_s": n / cache_ms / 1e3,
+                      "cache_ms_mma_sync": cache_mma_ms, "cache_mlp_tflops": n * 29824 / cache_ms / 1e9,
                       "steps": args.steps, "warmup": args.warmup, "data": "random weights and inputs"}))
 
 

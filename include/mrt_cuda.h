@@ -495,10 +495,14 @@ typedef struct mrt_denoiser mrt_denoiser;
 int mrt_cuda_denoiser_create(mrt_ctx* ctx, uint32_t seed, mrt_denoiser** out);
 int mrt_cuda_denoiser_destroy(mrt_ctx* ctx, mrt_denoiser* den);
 int mrt_cuda_denoiser_param_count(mrt_denoiser* den, size_t* weights, size_t* biases);
-/* Forward convolutions on the tcgen05 tensor cores with the accumulators in
- * tensor memory (enable != 0, the default) or on mma.sync (the previous
- * kernels, kept for comparison). */
-int mrt_cuda_denoiser_set_tcgen05(mrt_denoiser* den, int enable);
+/* Forward convolutions: mode 2 (default) on the tcgen05 tensor cores with
+ * persistent, warp-specialised CTAs for the layers without upsampling (a
+ * producer warp streaming tensor copies, an MMA warp, four epilogue warps,
+ * two tensor-memory accumulators), mode 1 tcgen05 with one CTA per output
+ * tile, mode 0 mma.sync (the earliest kernels, kept for comparison).  The
+ * two upsampling layers run the per-tile tcgen05 kernel in modes 1 and 2.
+ * Returns MRT_EINVAL for another mode. */
+int mrt_cuda_denoiser_set_tcgen05(mrt_denoiser* den, int mode);
 /* Features of one frame from its g-buffer (visibility + hit_t) and colour
  * (float RGB); scene_diagonal normalises depth.  features: device,
  * width*height*16 BF16. */

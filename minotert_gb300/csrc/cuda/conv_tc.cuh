@@ -494,6 +494,255 @@ cudaError_t launch_conv_tma(const ConvArgs& ca, const bf16* wt, uint32_t* status
     return cudaGetLastError();
 }
 
+// ---- persistent, warp-specialised TMA form ---------------------------------
+//
+// The same implicit GEMM with each CTA resident for the whole layer: it walks
+// the output tiles (ROWS rows x 128 pixels) blockIdx.x, blockIdx.x +
+// gridDim.x, ..., and its six warps split the work.  Warp 4 (one thread)
+// streams the (tile, 16-channel slice) pairs into a ring of STAGES
+// shared-memory stages with tensor copies (halo) and bulk copies (weights),
+// each completing on the stage's `full` mbarrier; warp 5 (one thread) waits
+// for a stage, issues its 9 x ROWS MMAs into one of two tensor-memory
+// accumulators and commits them to the stage's `empty` mbarrier (releasing it
+// to the producer) and, after a tile's last slice, to the accumulator's
+// `acc_full` mbarrier; warps 0-3 (TMEM lanes 0-127) wait for `acc_full`, run
+// the epilogue and arrive on `acc_empty`.  So the copies of the next tiles,
+// the MMAs of this tile and the epilogue of the previous one overlap, and a
+// layer with one or two slices per tile no longer pays a CTA's set-up,
+// tensor-memory allocation and epilogue in series per tile.  Every wait is
+// bounded and also ends when another role has given up (a shared abort
+// word); the CTA then sets MRT_STATUS_PIPE_TIMEOUT, waits (bounded) for the
+// copies and MMAs it issued and frees its tensor memory.
+template <int COUT, int ROWS, int STAGES>
+__host__ __device__ constexpr size_t ws_smem_bytes() {
+    return size_t(STAGES) * tma_stage_bytes<COUT, ROWS>() + size_t(2 * STAGES + 5) * 8 + 16;
+}
+
+__device__ __forceinline__ bool ws_wait(uint32_t mbar, uint32_t parity, const volatile uint32_t* abort) {
+    for (uint32_t spins = 0; spins < kTcSpin; ++spins) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (*abort) return false;
+    }
+    return false;
+}
+
+template <int COUT, int ROWS, int STAGES>
+__global__ void __launch_bounds__(192) k_conv_ws(ConvArgs a, const __grid_constant__ CUtensorMap map_a,
+                                                 const __grid_constant__ CUtensorMap map_b, const bf16* wt,
+                                                 uint32_t* status) {
+    constexpr int kAcc = ROWS * COUT;  // TMEM columns of one accumulator
+    constexpr int kCols = 2 * kAcc < 32 ? 32 : 2 * kAcc;
+    static_assert(kCols <= 512 && (kCols & (kCols - 1)) == 0, "tensor memory columns");
+    constexpr uint32_t kHalo = tma_halo_bytes<ROWS>(), kHalf = tma_half_bytes<ROWS>();
+    constexpr uint32_t kHaloTx = 2u * uint32_t((ROWS + 2) * kTcPlane);
+    constexpr uint32_t kWBytes = uint32_t(9 * 2 * COUT * 16);
+    constexpr uint32_t kStage = tma_stage_bytes<COUT, ROWS>();
+    extern __shared__ __align__(128) unsigned char tsm[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(tsm + STAGES * kStage);
+    uint64_t* empty = full + STAGES;
+    uint64_t* acc_full = empty + STAGES;    // [2]
+    uint64_t* acc_empty = acc_full + 2;     // [2]
+    uint64_t* fin = acc_empty + 2;          // the MMA thread's final commit
+    uint32_t* slot = reinterpret_cast<uint32_t*>(fin + 1);
+    volatile uint32_t* abort = slot + 1;
+    uint32_t* consumed = slot + 2;          // slices the MMA thread waited for
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tiles_x = (a.w_ + kTcPix - 1) / kTcPix, rows_per_img = (a.h + ROWS - 1) / ROWS;
+    const int tiles = tiles_x * rows_per_img * a.n;
+    const int cin = a.ca + a.cb, nk = cin / 16;
+    const uint32_t smem0 = smem_u32(tsm);
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                     "r"(uint32_t(kCols))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(full + s)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(empty + s)) : "memory");
+        }
+        for (int b = 0; b < 2; ++b) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(acc_full + b)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(smem_u32(acc_empty + b)) : "memory");
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(fin)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        // after a timeout anywhere in this launch (or an earlier one) the
+        // remaining CTAs skip their work
+        *abort = (*reinterpret_cast<volatile uint32_t*>(status) & MRT_STATUS_PIPE_TIMEOUT) != 0u ? 2u : 0u;
+        *consumed = 0u;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = *slot;
+    auto give_up = [&]() {
+        if (*abort == 0u) atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
+        *abort = 1u;
+    };
+
+    int produced = 0;
+    if (warp == 4) {
+        if (lane == 0 && *abort == 0u) {  // producer: (tile, slice) pairs into the stage ring
+            int g = 0;
+            for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+                const int tx = tile % tiles_x, rb = tile / tiles_x;
+                const int y0 = (rb % rows_per_img) * ROWS, n = rb / rows_per_img, x0 = tx * kTcPix;
+                bool ok = true;
+                for (int k = 0; k < nk; ++k, ++g) {
+                    const int s = g % STAGES;
+                    const uint32_t u = uint32_t(g / STAGES);
+                    if (!ws_wait(smem_u32(empty + s), (u & 1u) ^ 1u, abort)) { ok = false; break; }
+                    const uint32_t st = smem0 + uint32_t(s) * kStage, mb = smem_u32(full + s);
+                    const int c = 16 * k;
+                    const CUtensorMap* map = c < a.ca ? &map_a : &map_b;
+                    const int cc = c < a.ca ? c : c - a.ca;
+                    // the copies' alignment rules, checked before anything is issued
+                    if ((st & 127u) != 0u || (cc & 7) != 0) { ok = false; break; }
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb),
+                                 "r"(kHaloTx + kWBytes)
+                                 : "memory");
+                    tma_load_halo(st, map, cc, x0 - 1, y0 - 1, n, mb);
+                    tma_load_halo(st + kHalf, map, cc + 8, x0 - 1, y0 - 1, n, mb);
+                    asm volatile(
+                        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                            st + kHalo),
+                        "l"(wt + size_t(k) * (kWBytes / 2)), "r"(kWBytes), "r"(mb)
+                        : "memory");
+                    produced = g + 1;
+                }
+                if (!ok) { give_up(); break; }
+            }
+        }
+    } else if (warp == 5) {
+        if (lane == 0 && *abort == 0u) {  // MMA issuer
+            constexpr uint32_t idesc = tc_idesc(kTcPix, COUT);
+            int g = 0, it = 0;
+            bool ok = true, any = false;
+            for (int tile = blockIdx.x; ok && tile < tiles; tile += gridDim.x, ++it) {
+                const int b = it & 1;
+                const uint32_t ub = uint32_t(it >> 1);
+                if (!ws_wait(smem_u32(acc_empty + b), (ub & 1u) ^ 1u, abort)) { ok = false; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t tacc = taddr + uint32_t(b * kAcc);
+                for (int k = 0; k < nk; ++k, ++g) {
+                    const int s = g % STAGES;
+                    const uint32_t u = uint32_t(g / STAGES);
+                    if (!ws_wait(smem_u32(full + s), u & 1u, abort)) { ok = false; break; }
+                    *consumed = uint32_t(g + 1);
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t abase = smem0 + uint32_t(s) * kStage, bbase = abase + kHalo;
+#pragma unroll
+                    for (int r = 0; r < ROWS; ++r)
+#pragma unroll
+                        for (int t = 0; t < 9; ++t) {
+                            const int ky = t / 3, kx = t % 3;
+                            const uint64_t ad = tc_sdesc(abase + (r + ky) * kTcPlane + kx * 16, kHalf, 128);
+                            const uint64_t bd = tc_sdesc(bbase + (t * 2) * COUT * 16, COUT * 16, 128);
+                            const uint32_t acc = (k > 0 || t > 0) ? 1u : 0u;
+                            asm volatile(
+                                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+                                    tacc + uint32_t(r * COUT)),
+                                "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                                : "memory");
+                        }
+                    any = true;
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                     smem_u32(empty + s))
+                                 : "memory");
+                }
+                if (!ok) break;
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_u32(acc_full + b))
+                             : "memory");
+            }
+            if (!ok) give_up();
+            // every MMA this thread issued has completed once this commit has
+            if (any) {
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_u32(fin))
+                             : "memory");
+                if (!tc_wait(smem_u32(fin), 0u) && *abort == 0u) {
+                    atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
+                    *abort = 1u;
+                }
+            }
+        }
+    } else {  // epilogue: warps 0-3, TMEM lanes 32 warp ..
+        int it = 0;
+        for (int tile = blockIdx.x; tile < tiles && *abort == 0u; tile += gridDim.x, ++it) {
+            const int tx = tile % tiles_x, rb = tile / tiles_x;
+            const int y0 = (rb % rows_per_img) * ROWS, n = rb / rows_per_img, x0 = tx * kTcPix;
+            const int b = it & 1;
+            const uint32_t ub = uint32_t(it >> 1);
+            const bool ok = ws_wait(smem_u32(acc_full + b), ub & 1u, abort);
+            if (!__all_sync(0xFFFFFFFFu, ok)) {
+                if (lane == 0) give_up();
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            tc_epilogue<COUT, ROWS>(a, taddr + uint32_t(b * kAcc), n, y0, x0, warp, lane);
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(acc_empty + b)) : "memory");
+        }
+    }
+    __syncthreads();
+    // after an abort: the copies issued but never consumed land before the
+    // shared memory is released
+    if (warp == 4 && lane == 0) {
+        for (int g = int(*consumed); g < produced; ++g)
+            if (!tc_wait(smem_u32(full + g % STAGES), uint32_t(g / STAGES) & 1u)) atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(uint32_t(kCols))
+                     : "memory");
+}
+
+// Shape of the persistent form per COUT: rows per tile and ring stages
+// (two accumulators of ROWS x COUT columns must fit the 512 TMEM columns)
+__host__ __device__ constexpr int ws_rows(int cout) { return cout >= 128 ? 2 : (cout >= 64 ? 2 : 4); }
+__host__ __device__ constexpr int ws_stages(int cout) { return cout >= 128 ? 4 : 4; }
+
+template <int COUT>
+cudaError_t launch_conv_ws(const ConvArgs& ca, const bf16* wt, uint32_t* status, int sm_count, cudaStream_t s) {
+    constexpr int kRows = ws_rows(COUT), kStages = ws_stages(COUT);
+    constexpr int kCols = 2 * kRows * COUT < 32 ? 32 : 2 * kRows * COUT;
+    static uint64_t configured = 0;
+    static int per_sm = 0;
+    const size_t smem = ws_smem_bytes<COUT, kRows, kStages>();
+    cudaError_t e = tc_configure(k_conv_ws<COUT, kRows, kStages>, smem, configured);
+    if (e != cudaSuccess) return e;
+    if (per_sm == 0) {
+        int occ = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv_ws<COUT, kRows, kStages>, 192, smem);
+        if (e != cudaSuccess) return e;
+        per_sm = std::max(1, std::min(occ, 512 / kCols));
+    }
+    CUtensorMap ma, mb;
+    if (!tma_encode(&ma, ca.a, ca.ca, ca.w_, ca.h, ca.n, kRows)) return cudaErrorInvalidValue;
+    if (ca.cb > 0) {
+        if (!tma_encode(&mb, ca.b, ca.cb, ca.w_, ca.h, ca.n, kRows)) return cudaErrorInvalidValue;
+    } else {
+        mb = ma;
+    }
+    const int tiles = ((ca.w_ + kTcPix - 1) / kTcPix) * ((ca.h + kRows - 1) / kRows) * ca.n;
+    const int blocks = std::max(1, std::min(tiles, sm_count * per_sm));
+    k_conv_ws<COUT, kRows, kStages><<<blocks, 192, smem, s>>>(ca, ma, mb, wt, status);
+    return cudaGetLastError();
+}
+
 template <int COUT>
 cudaError_t launch_conv_tc(const ConvArgs& ca, uint32_t* status, cudaStream_t s) {
     constexpr int kRows = tc_rows(COUT), kStages = tc_stages(COUT);

@@ -373,7 +373,11 @@ struct mrt_denoiser {
     float* loss = nullptr;
     float* h_loss = nullptr;
     uint32_t step = 0;
-    bool tcgen05 = true;          // forward convolutions on tcgen05 (else mma.sync)
+    // forward convolutions: 0 mma.sync, 1 tcgen05 with one CTA per tile
+    // (k_conv_tma / k_conv_tc), 2 tcgen05 with persistent warp-specialised
+    // CTAs for the layers without upsampling (k_conv_ws; default)
+    int tc_mode = 2;
+    int sm_count = 0;
     uint32_t* status = nullptr;   // the context's device status word
 };
 
@@ -422,7 +426,16 @@ int ensure_acts(mrt_ctx* ctx, mrt_denoiser* d, size_t pix, bool grads) {
 cudaError_t conv(const mrt_denoiser* d, int l, const bf16* a, const bf16* b, int n, int h, int w, cudaStream_t s) {
     const ConvDesc& L = d->layers[l];
     ConvArgs ca{a, b, d->w16 + L.w_off, d->w + L.b_off, d->act[l], n, h, w, L.ca, L.cb, L.cout, L.ups, L.relu};
-    if (d->tcgen05 && !L.ups) {
+    if (d->tc_mode == 2 && !L.ups) {
+        const bf16* wt = d->wtc + L.w_off;
+        switch (L.cout) {
+        case 16: return launch_conv_ws<16>(ca, wt, d->status, d->sm_count, s);
+        case 32: return launch_conv_ws<32>(ca, wt, d->status, d->sm_count, s);
+        case 64: return launch_conv_ws<64>(ca, wt, d->status, d->sm_count, s);
+        default: return launch_conv_ws<128>(ca, wt, d->status, d->sm_count, s);
+        }
+    }
+    if (d->tc_mode == 1 && !L.ups) {
         const bf16* wt = d->wtc + L.w_off;
         switch (L.cout) {
         case 16: return launch_conv_tma<16>(ca, wt, d->status, s);
@@ -431,7 +444,7 @@ cudaError_t conv(const mrt_denoiser* d, int l, const bf16* a, const bf16* b, int
         default: return launch_conv_tma<128>(ca, wt, d->status, s);
         }
     }
-    if (d->tcgen05) {
+    if (d->tc_mode != 0) {
         switch (L.cout) {
         case 16: return launch_conv_tc<16>(ca, d->status, s);
         case 32: return launch_conv_tc<32>(ca, d->status, s);
@@ -452,7 +465,7 @@ cudaError_t conv(const mrt_denoiser* d, int l, const bf16* a, const bf16* b, int
 // forward of the whole network over n images of h x w (h, w multiples of 4)
 cudaError_t forward(const mrt_denoiser* d, const bf16* in, int n, int h, int w, cudaStream_t s) {
     cudaError_t e;
-    if (d->tcgen05) {  // the TMA convolutions read the weights per slice
+    if (d->tc_mode != 0) {  // the TMA convolutions read the weights per slice
         TcLayerTable t{};
         t.count = kLayers;
         for (int l = 0; l < kLayers; ++l) {
@@ -504,6 +517,7 @@ int mrt_cuda_denoiser_create(mrt_ctx* ctx, uint32_t seed, mrt_denoiser** out) {
     mrt_denoiser* d = new (std::nothrow) mrt_denoiser;
     if (!d) return MRT_ENOMEM;
     d->status = ctx->d_status;
+    d->sm_count = ctx->sm_count;
     size_t wo = 0;
     for (int l = 0; l < kLayers; ++l) {
         ConvDesc& L = d->layers[l];
@@ -580,7 +594,8 @@ int mrt_cuda_denoiser_destroy(mrt_ctx* ctx, mrt_denoiser* d) {
 
 int mrt_cuda_denoiser_set_tcgen05(mrt_denoiser* d, int enable) {
     if (!d) return MRT_EINVAL;
-    d->tcgen05 = enable != 0;
+    if (enable < 0 || enable > 2) return MRT_EINVAL;
+    d->tc_mode = enable;
     return MRT_OK;
 }
 

@@ -29,9 +29,12 @@ class Denoiser:
     def handle(self):
         return self._h
 
-    def set_tcgen05(self, enable: bool):
-        """Forward convolutions on tcgen05 (default) or on mma.sync."""
-        self.ctx.check(lib().mrt_cuda_denoiser_set_tcgen05(self._h, int(enable)), "denoiser_set_tcgen05")
+    def set_tcgen05(self, mode):
+        """Forward convolutions: 2 (or True) persistent warp-specialised
+        tcgen05 kernels (default), 1 tcgen05 with one CTA per tile, 0 (or
+        False) mma.sync."""
+        mode = 2 if mode is True else int(mode)
+        self.ctx.check(lib().mrt_cuda_denoiser_set_tcgen05(self._h, mode), "denoiser_set_tcgen05")
 
     def features(self, scene, gbuffer, d_color, diagonal: float, d_features, stream=None):
         self.ctx.check(lib().mrt_cuda_denoiser_features(self.ctx.handle, scene.handle, C.byref(gbuffer.c()),

@@ -133,12 +133,16 @@ def test_denoiser_inference_is_size_and_batch_consistent(ctx):
     assert np.array_equal(pair[1], one_o.download(np.float32, (128, 128, 3)))
 
 
-@pytest.mark.parametrize("shape", [(2, 16, 24), (1, 64, 200), (1, 540, 960)])
+@pytest.mark.parametrize("shape", [(2, 16, 24), (1, 64, 200), (1, 540, 960), (1, 1080, 1920)])
 def test_denoiser_tcgen05_matches_mma_sync(ctx, shape):
-    # the same network on the two tensor-core paths: tcgen05 (accumulators
-    # in tensor memory, operands staged in shared memory) and mma.sync;
-    # only the FP32 summation order differs, so layer outputs agree to BF16
-    # rounding and the decoded radiance to ~1 %
+    # the same network on the three forward paths: persistent warp-
+    # specialised tcgen05 kernels (mode 2, default), tcgen05 with one CTA
+    # per tile (mode 1) and mma.sync (mode 0).  Modes 2 and 1 issue the same
+    # MMAs in the same order into tensor memory and share the epilogue, so
+    # they agree bit for bit (the persistent CTAs loop over many tiles at
+    # the two larger sizes); against mma.sync only the FP32 summation order
+    # differs, so layer outputs agree to BF16 rounding and the decoded
+    # radiance to ~1 %
     n, h, w = shape
     d = Denoiser(ctx, seed=7)
     rng = np.random.default_rng(3)
@@ -147,14 +151,16 @@ def test_denoiser_tcgen05_matches_mma_sync(ctx, shape):
     xb = to_bf16_bits(x)
     d_x = ctx.to_device(xb)
     outs = []
-    for tc in (True, False):
-        d.set_tcgen05(tc)
+    for mode in (2, 1, 0):
+        d.set_tcgen05(mode)
         d_o = ctx.alloc(n * h * w * 12)
         d.infer(d_x, n, w, h, d_o)
         outs.append(d_o.download(np.float32, (n, h, w, 3)))
+    d.set_tcgen05(2)
     assert ctx.status() == 0
-    a, b = outs
-    assert np.isfinite(a).all()
-    err = np.abs(a - b)
+    ws, tile, b = outs
+    assert np.isfinite(ws).all()
+    assert np.array_equal(ws.view(np.uint32), tile.view(np.uint32))
+    err = np.abs(ws - b)
     assert err.max() < 3e-2 * max(1.0, np.abs(b).max()), err.max()
     assert err.mean() < 2e-3 * max(1.0, np.abs(b).mean())
