@@ -515,7 +515,7 @@ cudaError_t launch_conv_tma(const ConvArgs& ca, const bf16* wt, uint32_t* status
 // copies and MMAs it issued and frees its tensor memory.
 template <int COUT, int ROWS, int STAGES>
 __host__ __device__ constexpr size_t ws_smem_bytes() {
-    return size_t(STAGES) * tma_stage_bytes<COUT, ROWS>() + size_t(2 * STAGES + 5) * 8 + 16;
+    return size_t(STAGES) * tma_stage_bytes<COUT, ROWS>() + size_t(2 * STAGES + 5) * 8 + 32;
 }
 
 __device__ __forceinline__ bool ws_wait(uint32_t mbar, uint32_t parity, const volatile uint32_t* abort) {
@@ -532,10 +532,16 @@ __device__ __forceinline__ bool ws_wait(uint32_t mbar, uint32_t parity, const vo
     return false;
 }
 
-template <int COUT, int ROWS, int STAGES>
-__global__ void __launch_bounds__(192) k_conv_ws(ConvArgs a, const __grid_constant__ CUtensorMap map_a,
-                                                 const __grid_constant__ CUtensorMap map_b, const bf16* wt,
-                                                 uint32_t* status) {
+// Threads of the persistent form: four epilogue warps, the producer warps
+// (one for tensor copies; four when the layer's first source is upsampled
+// and its halo is gathered with cp.async), one MMA warp.
+__host__ __device__ constexpr int ws_prod_warps(bool ups) { return ups ? 4 : 1; }
+__host__ __device__ constexpr int ws_threads(bool ups) { return 32 * (5 + ws_prod_warps(ups)); }
+
+template <int COUT, int ROWS, int STAGES, bool UPS>
+__global__ void __launch_bounds__(ws_threads(UPS)) k_conv_ws(ConvArgs a, const __grid_constant__ CUtensorMap map_a,
+                                                            const __grid_constant__ CUtensorMap map_b, const bf16* wt,
+                                                            uint32_t* status) {
     constexpr int kAcc = ROWS * COUT;  // TMEM columns of one accumulator
     constexpr int kCols = 2 * kAcc < 32 ? 32 : 2 * kAcc;
     static_assert(kCols <= 512 && (kCols & (kCols - 1)) == 0, "tensor memory columns");
@@ -543,6 +549,8 @@ __global__ void __launch_bounds__(192) k_conv_ws(ConvArgs a, const __grid_consta
     constexpr uint32_t kHaloTx = 2u * uint32_t((ROWS + 2) * kTcPlane);
     constexpr uint32_t kWBytes = uint32_t(9 * 2 * COUT * 16);
     constexpr uint32_t kStage = tma_stage_bytes<COUT, ROWS>();
+    constexpr int kProdWarps = ws_prod_warps(UPS), kProdThreads = 32 * kProdWarps;
+    constexpr int kMmaWarp = 4 + kProdWarps;
     extern __shared__ __align__(128) unsigned char tsm[];
     uint64_t* full = reinterpret_cast<uint64_t*>(tsm + STAGES * kStage);
     uint64_t* empty = full + STAGES;
@@ -552,6 +560,7 @@ __global__ void __launch_bounds__(192) k_conv_ws(ConvArgs a, const __grid_consta
     uint32_t* slot = reinterpret_cast<uint32_t*>(fin + 1);
     volatile uint32_t* abort = slot + 1;
     uint32_t* consumed = slot + 2;          // slices the MMA thread waited for
+    volatile uint32_t* prod_go = slot + 3;  // [2]: producer thread 0's go / stop, by slice parity
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tiles_x = (a.w_ + kTcPix - 1) / kTcPix, rows_per_img = (a.h + ROWS - 1) / ROWS;
     const int tiles = tiles_x * rows_per_img * a.n;
@@ -565,8 +574,12 @@ __global__ void __launch_bounds__(192) k_conv_ws(ConvArgs a, const __grid_consta
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
+        // a stage is full after the expect_tx arrival and, with gathered
+        // copies, one arrival per producer thread
+        const uint32_t full_count = UPS ? 1u + uint32_t(kProdThreads) : 1u;
         for (int s = 0; s < STAGES; ++s) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(full + s)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(full + s)), "r"(full_count)
+                         : "memory");
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(empty + s)) : "memory");
         }
         for (int b = 0; b < 2; ++b) {
@@ -590,39 +603,76 @@ __global__ void __launch_bounds__(192) k_conv_ws(ConvArgs a, const __grid_consta
     };
 
     int produced = 0;
-    if (warp == 4) {
-        if (lane == 0 && *abort == 0u) {  // producer: (tile, slice) pairs into the stage ring
+    if (warp >= 4 && warp < kMmaWarp) {
+        // producer: (tile, slice) pairs into the stage ring
+        const int ptid = tid - 128;
+        const int ha = UPS ? a.h >> 1 : a.h, wa = UPS ? a.w_ >> 1 : a.w_;
+        if (UPS || ptid == 0) {
             int g = 0;
-            for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+            bool ok = *abort == 0u;
+            for (int tile = blockIdx.x; ok && tile < tiles; tile += gridDim.x) {
                 const int tx = tile % tiles_x, rb = tile / tiles_x;
                 const int y0 = (rb % rows_per_img) * ROWS, n = rb / rows_per_img, x0 = tx * kTcPix;
-                bool ok = true;
                 for (int k = 0; k < nk; ++k, ++g) {
                     const int s = g % STAGES;
                     const uint32_t u = uint32_t(g / STAGES);
-                    if (!ws_wait(smem_u32(empty + s), (u & 1u) ^ 1u, abort)) { ok = false; break; }
                     const uint32_t st = smem0 + uint32_t(s) * kStage, mb = smem_u32(full + s);
                     const int c = 16 * k;
+                    const bool gathered = UPS && c < a.ca;
                     const CUtensorMap* map = c < a.ca ? &map_a : &map_b;
                     const int cc = c < a.ca ? c : c - a.ca;
-                    // the copies' alignment rules, checked before anything is issued
-                    if ((st & 127u) != 0u || (cc & 7) != 0) { ok = false; break; }
-                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb),
-                                 "r"(kHaloTx + kWBytes)
-                                 : "memory");
-                    tma_load_halo(st, map, cc, x0 - 1, y0 - 1, n, mb);
-                    tma_load_halo(st + kHalf, map, cc + 8, x0 - 1, y0 - 1, n, mb);
-                    asm volatile(
-                        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                            st + kHalo),
-                        "l"(wt + size_t(k) * (kWBytes / 2)), "r"(kWBytes), "r"(mb)
-                        : "memory");
+                    // thread 0 waits for the stage and decides for the group;
+                    // the decision goes through a word per slice parity so
+                    // every producer thread reads the same one (thread 0
+                    // cannot rewrite it before all have passed the next
+                    // group barrier)
+                    if (ptid == 0) {
+                        if (!ws_wait(smem_u32(empty + s), (u & 1u) ^ 1u, abort) || (st & 127u) != 0u ||
+                            (cc & 7) != 0)
+                            give_up();
+                        prod_go[g & 1] = *abort == 0u ? 1u : 0u;
+                    }
+                    if (UPS) asm volatile("bar.sync 1, %0;" ::"n"(kProdThreads) : "memory");
+                    if (prod_go[g & 1] == 0u) { ok = false; break; }
+                    if (ptid == 0) {
+                        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb),
+                                     "r"(gathered ? kWBytes : kHaloTx + kWBytes)
+                                     : "memory");
+                        if (!gathered) {
+                            tma_load_halo(st, map, cc, x0 - 1, y0 - 1, n, mb);
+                            tma_load_halo(st + kHalf, map, cc + 8, x0 - 1, y0 - 1, n, mb);
+                        }
+                        asm volatile(
+                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                                st + kHalo),
+                            "l"(wt + size_t(k) * (kWBytes / 2)), "r"(kWBytes), "r"(mb)
+                            : "memory");
+                    }
+                    if (UPS) {
+                        if (gathered) {
+                            // the nearest-upsampled halo: rows y0-1 .. y0+ROWS,
+                            // pixels x0-1 .. x0+128 of source A at half
+                            // resolution, zero outside the image
+                            for (int i = ptid; i < (ROWS + 2) * 2 * kTcHalo; i += kProdThreads) {
+                                const int hf = i & 1, p = (i >> 1) % kTcHalo, r = (i >> 1) / kTcHalo;
+                                const int yy = y0 - 1 + r, xx = x0 - 1 + p;
+                                const bool in = yy >= 0 && yy < a.h && xx >= 0 && xx < a.w_;
+                                const bf16* src = in ? a.a + ((size_t(n) * ha + (yy >> 1)) * wa + (xx >> 1)) * a.ca +
+                                                           c + 8 * hf
+                                                     : a.w;  // any valid address when zero-filling
+                                cp16(st + uint32_t(hf) * kHalf + uint32_t(r * kTcPlane + p * 16), src, in);
+                            }
+                            asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(mb) : "memory");
+                        } else {
+                            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mb) : "memory");
+                        }
+                    }
                     produced = g + 1;
                 }
-                if (!ok) { give_up(); break; }
             }
+            if (UPS) asm volatile("cp.async.wait_all;" ::: "memory");
         }
-    } else if (warp == 5) {
+    } else if (warp == kMmaWarp) {
         if (lane == 0 && *abort == 0u) {  // MMA issuer
             constexpr uint32_t idesc = tc_idesc(kTcPix, COUT);
             int g = 0, it = 0;
@@ -699,7 +749,7 @@ __global__ void __launch_bounds__(192) k_conv_ws(ConvArgs a, const __grid_consta
     __syncthreads();
     // after an abort: the copies issued but never consumed land before the
     // shared memory is released
-    if (warp == 4 && lane == 0) {
+    if (tid == 128) {
         for (int g = int(*consumed); g < produced; ++g)
             if (!tc_wait(smem_u32(full + g % STAGES), uint32_t(g / STAGES) & 1u)) atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
     }
@@ -710,36 +760,43 @@ __global__ void __launch_bounds__(192) k_conv_ws(ConvArgs a, const __grid_consta
                      : "memory");
 }
 
-// Shape of the persistent form per COUT: rows per tile and ring stages
-// (two accumulators of ROWS x COUT columns must fit the 512 TMEM columns)
-__host__ __device__ constexpr int ws_rows(int cout) { return cout >= 128 ? 2 : (cout >= 64 ? 2 : 4); }
-__host__ __device__ constexpr int ws_stages(int cout) { return cout >= 128 ? 4 : 4; }
+// Shape of the persistent form per COUT: rows per tile (two accumulators of
+// ROWS x COUT columns within the 512 TMEM columns) and ring stages (three
+// keep two CTAs per SM up to COUT 64)
+__host__ __device__ constexpr int ws_rows(int cout) { return cout >= 64 ? 2 : 4; }
+__host__ __device__ constexpr int ws_stages(int cout) { return cout >= 128 ? 4 : 3; }
 
-template <int COUT>
+template <int COUT, bool UPS>
 cudaError_t launch_conv_ws(const ConvArgs& ca, const bf16* wt, uint32_t* status, int sm_count, cudaStream_t s) {
     constexpr int kRows = ws_rows(COUT), kStages = ws_stages(COUT);
     constexpr int kCols = 2 * kRows * COUT < 32 ? 32 : 2 * kRows * COUT;
+    constexpr int kThreads = ws_threads(UPS);
     static uint64_t configured = 0;
     static int per_sm = 0;
     const size_t smem = ws_smem_bytes<COUT, kRows, kStages>();
-    cudaError_t e = tc_configure(k_conv_ws<COUT, kRows, kStages>, smem, configured);
+    cudaError_t e = tc_configure(k_conv_ws<COUT, kRows, kStages, UPS>, smem, configured);
     if (e != cudaSuccess) return e;
     if (per_sm == 0) {
         int occ = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv_ws<COUT, kRows, kStages>, 192, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv_ws<COUT, kRows, kStages, UPS>, kThreads, smem);
         if (e != cudaSuccess) return e;
         per_sm = std::max(1, std::min(occ, 512 / kCols));
     }
     CUtensorMap ma, mb;
-    if (!tma_encode(&ma, ca.a, ca.ca, ca.w_, ca.h, ca.n, kRows)) return cudaErrorInvalidValue;
-    if (ca.cb > 0) {
-        if (!tma_encode(&mb, ca.b, ca.cb, ca.w_, ca.h, ca.n, kRows)) return cudaErrorInvalidValue;
+    if (UPS) {  // source A is gathered; only the skip source has a tensor map
+        if (ca.cb <= 0 || !tma_encode(&mb, ca.b, ca.cb, ca.w_, ca.h, ca.n, kRows)) return cudaErrorInvalidValue;
+        ma = mb;
     } else {
-        mb = ma;
+        if (!tma_encode(&ma, ca.a, ca.ca, ca.w_, ca.h, ca.n, kRows)) return cudaErrorInvalidValue;
+        if (ca.cb > 0) {
+            if (!tma_encode(&mb, ca.b, ca.cb, ca.w_, ca.h, ca.n, kRows)) return cudaErrorInvalidValue;
+        } else {
+            mb = ma;
+        }
     }
     const int tiles = ((ca.w_ + kTcPix - 1) / kTcPix) * ((ca.h + kRows - 1) / kRows) * ca.n;
     const int blocks = std::max(1, std::min(tiles, sm_count * per_sm));
-    k_conv_ws<COUT, kRows, kStages><<<blocks, 192, smem, s>>>(ca, ma, mb, wt, status);
+    k_conv_ws<COUT, kRows, kStages, UPS><<<blocks, kThreads, smem, s>>>(ca, ma, mb, wt, status);
     return cudaGetLastError();
 }
 

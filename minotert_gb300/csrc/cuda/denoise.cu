@@ -426,13 +426,18 @@ int ensure_acts(mrt_ctx* ctx, mrt_denoiser* d, size_t pix, bool grads) {
 cudaError_t conv(const mrt_denoiser* d, int l, const bf16* a, const bf16* b, int n, int h, int w, cudaStream_t s) {
     const ConvDesc& L = d->layers[l];
     ConvArgs ca{a, b, d->w16 + L.w_off, d->w + L.b_off, d->act[l], n, h, w, L.ca, L.cb, L.cout, L.ups, L.relu};
-    if (d->tc_mode == 2 && !L.ups) {
+    if (d->tc_mode == 2) {
         const bf16* wt = d->wtc + L.w_off;
-        switch (L.cout) {
-        case 16: return launch_conv_ws<16>(ca, wt, d->status, d->sm_count, s);
-        case 32: return launch_conv_ws<32>(ca, wt, d->status, d->sm_count, s);
-        case 64: return launch_conv_ws<64>(ca, wt, d->status, d->sm_count, s);
-        default: return launch_conv_ws<128>(ca, wt, d->status, d->sm_count, s);
+        if (L.ups) {  // the decoder's two upsampling layers
+            if (L.cout == 32) return launch_conv_ws<32, true>(ca, wt, d->status, d->sm_count, s);
+            if (L.cout == 64) return launch_conv_ws<64, true>(ca, wt, d->status, d->sm_count, s);
+        } else {
+            switch (L.cout) {
+            case 16: return launch_conv_ws<16, false>(ca, wt, d->status, d->sm_count, s);
+            case 32: return launch_conv_ws<32, false>(ca, wt, d->status, d->sm_count, s);
+            case 64: return launch_conv_ws<64, false>(ca, wt, d->status, d->sm_count, s);
+            default: return launch_conv_ws<128, false>(ca, wt, d->status, d->sm_count, s);
+            }
         }
     }
     if (d->tc_mode == 1 && !L.ups) {
