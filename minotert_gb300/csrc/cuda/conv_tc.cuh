@@ -653,14 +653,17 @@ __global__ void __launch_bounds__(ws_threads(UPS)) k_conv_ws(ConvArgs a, const _
                             // the nearest-upsampled halo: rows y0-1 .. y0+ROWS,
                             // pixels x0-1 .. x0+128 of source A at half
                             // resolution, zero outside the image
-                            for (int i = ptid; i < (ROWS + 2) * 2 * kTcHalo; i += kProdThreads) {
-                                const int hf = i & 1, p = (i >> 1) % kTcHalo, r = (i >> 1) / kTcHalo;
+                            // (both 8-channel halves of a pixel per thread: one
+                            // address computation for two copies)
+                            for (int i = ptid; i < (ROWS + 2) * kTcHalo; i += kProdThreads) {
+                                const int r = i / kTcHalo, p = i - r * kTcHalo;
                                 const int yy = y0 - 1 + r, xx = x0 - 1 + p;
                                 const bool in = yy >= 0 && yy < a.h && xx >= 0 && xx < a.w_;
-                                const bf16* src = in ? a.a + ((size_t(n) * ha + (yy >> 1)) * wa + (xx >> 1)) * a.ca +
-                                                           c + 8 * hf
+                                const bf16* src = in ? a.a + ((size_t(n) * ha + (yy >> 1)) * wa + (xx >> 1)) * a.ca + c
                                                      : a.w;  // any valid address when zero-filling
-                                cp16(st + uint32_t(hf) * kHalf + uint32_t(r * kTcPlane + p * 16), src, in);
+                                const uint32_t dst = st + uint32_t(r * kTcPlane + p * 16);
+                                cp16(dst, src, in);
+                                cp16(dst + kHalf, in ? src + 8 : src, in);
                             }
                             asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(mb) : "memory");
                         } else {

@@ -308,18 +308,6 @@ k_secondary_sphere(DevScene sc, FrameParams fp, mrt_gbuffer g, TraceParams tp, B
 
 // ---------------------------------------------------------------- wavefront
 
-// Warp-aggregated slot reservation: one atomic per warp for all lanes that
-// `want` a slot.  Must be called by all 32 lanes.
-MRT_DEV uint32_t warp_reserve(uint32_t* counter, bool want) {
-    const uint32_t mask = __ballot_sync(0xFFFFFFFFu, want);
-    if (!mask) return 0u;
-    const uint32_t lane = lane_id();
-    const uint32_t leader = __ffs(mask) - 1u;
-    uint32_t base = 0u;
-    if (lane == leader) base = atomicAdd(counter, uint32_t(__popc(mask)));
-    base = __shfl_sync(0xFFFFFFFFu, base, leader);
-    return base + __popc(mask & ((1u << lane) - 1u));
-}
 
 struct VertexOut {
     bool shadow;
@@ -388,12 +376,40 @@ MRT_DEV void add_L(float4* L, uint32_t pix, f3 v) {
     L[pix] = a;
 }
 
-MRT_DEV void emit(const VertexOut& vo, const WaveBuffers& wb, uint32_t vertex) {
-    const uint32_t si = warp_reserve(wb.counters + kCntShadow + vertex, vo.shadow);
-    if (vo.shadow) wb.sq[si] = vo.sr;
-    const uint32_t ei = warp_reserve(wb.counters + kCntExt + vertex + 1u, vo.ext);
+
+// emit for a whole block: the shadow and extension rays of the block's
+// threads get their queue slots with one global atomic per queue and block
+// instead of one per warp (the shading kernels' warps otherwise queue on
+// the two counters' atomics).  All threads of the block must call it the
+// same number of times.
+MRT_DEV void emit_block(const VertexOut& vo, const WaveBuffers& wb, uint32_t vertex) {
+    constexpr int kWarps = kShadeBlock / 32;
+    __shared__ uint32_t wsum[2][kWarps];
+    __shared__ uint32_t base[2];
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    const uint32_t m0 = __ballot_sync(0xFFFFFFFFu, vo.shadow), m1 = __ballot_sync(0xFFFFFFFFu, vo.ext);
+    if (lane == 0u) {
+        wsum[0][warp] = __popc(m0);
+        wsum[1][warp] = __popc(m1);
+    }
+    __syncthreads();
+    if (threadIdx.x < 2u) {  // thread q: exclusive scan of the warps' counts of queue q, one atomic
+        const uint32_t q = threadIdx.x;
+        uint32_t acc = 0u;
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t c = wsum[q][w];
+            wsum[q][w] = acc;
+            acc += c;
+        }
+        uint32_t* counter = q ? wb.counters + kCntExt + vertex + 1u : wb.counters + kCntShadow + vertex;
+        base[q] = acc ? atomicAdd(counter, acc) : 0u;
+    }
+    __syncthreads();
+    const uint32_t lt = (1u << lane) - 1u;
+    if (vo.shadow) wb.sq[base[0] + wsum[0][warp] + __popc(m0 & lt)] = vo.sr;
     PathRay* q = ((vertex + 1u) & 1u) ? wb.q[1] : wb.q[0];
-    if (vo.ext) q[ei] = vo.pr;
+    if (vo.ext) q[base[1] + wsum[1][warp] + __popc(m1 & lt)] = vo.pr;
+    __syncthreads();  // wsum and base are reused by the next call
 }
 
 // Vertex 0: the primary hit from the g-buffer (visibility + FP32 hit_t).
@@ -402,7 +418,7 @@ k_shade_primary(DevScene sc, FrameParams fp, mrt_gbuffer g, TraceParams tp, Blue
                 uint32_t sample, uint32_t* status) {
     const uint32_t npix = fp.width * fp.height;
     const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t rounded = (npix + 31u) & ~31u;
+    const uint32_t rounded = (npix + kShadeBlock - 1u) / kShadeBlock * kShadeBlock;  // same trip count per block
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < rounded; i += stride) {
         const bool valid = i < npix;
         VertexOut vo;
@@ -422,7 +438,7 @@ k_shade_primary(DevScene sc, FrameParams fp, mrt_gbuffer g, TraceParams tp, Blue
             }
             wb.rng[i] = rng;
         }
-        emit(vo, wb, 0u);
+        emit_block(vo, wb, 0u);
     }
 }
 
@@ -433,7 +449,7 @@ k_shade(DevScene sc, TraceParams tp, BlueNoise bn, WaveBuffers wb, uint32_t widt
     const uint32_t n = wb.counters[kCntExt + vertex];
     const PathRay* q = ext_queue(wb, vertex);
     const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t rounded = (n + 31u) & ~31u;
+    const uint32_t rounded = (n + kShadeBlock - 1u) / kShadeBlock * kShadeBlock;  // same trip count per block
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < rounded; i += stride) {
         VertexOut vo;
         vo.shadow = vo.ext = false;
@@ -452,7 +468,7 @@ k_shade(DevScene sc, TraceParams tp, BlueNoise bn, WaveBuffers wb, uint32_t widt
                 wb.rng[pix] = rng;
             }
         }
-        emit(vo, wb, vertex);
+        emit_block(vo, wb, vertex);
     }
 }
 
