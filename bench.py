@@ -289,7 +289,7 @@ def frame_record(args, name, steps, warmup, world, rank, local, dist, cpu=True, 
         dist.barrier()
     clocks = ClockSampler(local)
     clocks.start()
-    time.sleep(0.3)
+    time.sleep(1.0)  # nvidia-smi's start-up stays out of the timed frames
     for k in range(steps):
         flush.zero(stream)
         ctx.record(ev[k][0], stream)
@@ -388,6 +388,8 @@ def frame_record(args, name, steps, warmup, world, rank, local, dist, cpu=True, 
         "all_rays_incl_shadow_mrays_s": (rays + int(st.shadow_rays)) / (total_ms / 1e3) / 1e6,
         "rays_per_frame": {"primary": prim / steps, "extension": [e / steps for e in ext[:s.bounces]],
                            "shadow": st.shadow_rays / steps},
+        "frame_ms": {"median": statistics.median(ms), "min": min(ms), "max": max(ms),
+                     "first_10_mean": statistics.mean(ms[:10])},
         "ms_per_frame": {"primary": st.ms_primary / steps, "extend": st.ms_extend / steps,
                          "shadow": st.ms_shadow / steps, "shade": st.ms_shade / steps},
         "note": "tail_bounce %d: the paths alive at that bounce finish in one persistent launch (k_tail), "
