@@ -429,7 +429,9 @@ def frame_record(args, name, steps, warmup, world, rank, local, dist, cpu=True, 
            "config": _config(wl, mesh, bvh, build_info), "breakdown": breakdown, "roofline": roofline,
            "e2e": e2e, "gpu_launches": int(st.launches), "clocks": clk, "device_status": status}
     if cpu and rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(wl, mesh, bvh, bn)
+        # timed by the caller after every GPU measurement of the line (the GPU
+        # idles for its 12 s): keep what it needs
+        out["_cpu_baseline_inputs"] = (wl, mesh, bvh, bn)
     ctx.close()
     return out
 
@@ -450,6 +452,9 @@ def run_mine(args, world, rank, local, dist):
             for k in ("metric", "n_gpus", "higher_is_better", "scaling", "vs_baseline", "dtype"):
                 rec.pop(k, None)
         out["sub_records"] = subs
+    cpu_inputs = out.pop("_cpu_baseline_inputs", None)
+    if cpu_inputs is not None:
+        out["cpu_baseline"] = cpu_baseline(*cpu_inputs)
     if rank == 0:
         print(json.dumps(out))
     if dist is not None:

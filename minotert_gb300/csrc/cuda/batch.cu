@@ -198,14 +198,31 @@ k_batch_trace_queue(DevScene sc, const uint32_t* roots, const PathRay* q, uint2*
     if (st) atomicOr(status, st);
 }
 
-__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want) {
+// Queue slot of this thread among the block's threads that `want` one:
+// one global atomic per block (a warp-level atomic per warp makes the
+// warps of a large bounce queue up on the counter).  All threads of the
+// block must call it the same number of times.
+__device__ __forceinline__ uint32_t block_append(uint32_t* counter, bool want) {
+    constexpr int kWarps = kShadeBlock / 32;
+    __shared__ uint32_t wsum[kWarps];
+    __shared__ uint32_t base;
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
     const uint32_t mask = __ballot_sync(0xFFFFFFFFu, want);
-    if (!mask) return 0u;
-    const uint32_t lane = lane_id(), leader = __ffs(mask) - 1u;
-    uint32_t base = 0u;
-    if (lane == leader) base = atomicAdd(counter, uint32_t(__popc(mask)));
-    base = __shfl_sync(0xFFFFFFFFu, base, leader);
-    return base + __popc(mask & ((1u << lane) - 1u));
+    if (lane == 0u) wsum[warp] = __popc(mask);
+    __syncthreads();
+    if (threadIdx.x == 0u) {  // exclusive scan of the warps' counts, one atomic
+        uint32_t acc = 0u;
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t c = wsum[w];
+            wsum[w] = acc;
+            acc += c;
+        }
+        base = acc ? atomicAdd(counter, acc) : 0u;
+    }
+    __syncthreads();
+    const uint32_t slot = base + wsum[warp] + __popc(mask & ((1u << lane) - 1u));
+    __syncthreads();  // wsum and base are reused by the next call
+    return slot;
 }
 
 // Shade vertex `bounce`: escape adds throughput x sky; a hit multiplies the
@@ -217,7 +234,7 @@ k_batch_shade(DevScene sc, const TraceParams* tpp, const PathRay* qin, PathRay* 
               uint32_t* rng, float* radiance, uint32_t* counters, uint32_t bounce, uint32_t* status) {
     const TraceParams tp = *tpp;
     const uint32_t n = counters[kCntExt + bounce];
-    const uint32_t rounded = (n + 31u) & ~31u;
+    const uint32_t rounded = (n + kShadeBlock - 1u) / kShadeBlock * kShadeBlock;  // same trip count per block
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < rounded; i += gridDim.x * blockDim.x) {
         bool want = false;
         PathRay out;
@@ -268,7 +285,7 @@ k_batch_shade(DevScene sc, const TraceParams* tpp, const PathRay* qin, PathRay* 
                 atomicOr(status, MRT_STATUS_BAD_TRI);
             }
         }
-        const uint32_t slot = warp_append(counters + kCntExt + bounce + 1u, want);
+        const uint32_t slot = block_append(counters + kCntExt + bounce + 1u, want);
         if (want) qout[slot] = out;
     }
 }

@@ -1020,6 +1020,7 @@ k_cache_train_paths(DevScene sc, FrameParams fp, TraceParams tp, uint32_t bounce
                     uint32_t frame, float* out_q, float* out_t, uint32_t* count, uint32_t cap, uint32_t* status) {
     __shared__ uint2 stk[kStackDepth * kTraceBlock];
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t alive = __ballot_sync(0xFFFFFFFFu, p < n_paths);  // a prefix of the warp's lanes
     if (p >= n_paths) return;
     uint32_t st = 0u, cn = 0u, ct = 0u;
     uint32_t h = p * 0x9E3779B1u + frame * 0x85EBCA6Bu + 0x632BE5ABu;
@@ -1084,10 +1085,24 @@ k_cache_train_paths(DevScene sc, FrameParams fp, TraceParams tp, uint32_t bounce
     // indirect outgoing radiance (the suffix without its own direct light,
     // which the frame adds exactly with a shadow ray)
     f3 next = escaped ? escape_radiance(tp, d) : f3{0.0f, 0.0f, 0.0f};
+    // the warp's samples get their slots with one atomic: an inclusive scan
+    // of nv over the warp's live lanes (a prefix of the lanes)
+    __syncwarp(alive);
+    const uint32_t lane = lane_id();
+    uint32_t incl = uint32_t(nv);
+    for (uint32_t off = 1; off < 32u; off <<= 1) {
+        const uint32_t v = __shfl_up_sync(alive, incl, int(off));
+        if (lane >= off) incl += v;
+    }
+    const uint32_t last = 31u - uint32_t(__clz(alive));
+    const uint32_t total = __shfl_sync(alive, incl, int(last));
+    uint32_t base = 0u;
+    if (lane == 0u && total) base = atomicAdd(count, total);
+    base = __shfl_sync(alive, base, 0) + incl - uint32_t(nv);
     for (int v = nv - 1; v >= 0; --v) {
         const float w = wcont[v];
         const f3 Li{rho[v].x * w * next.x, rho[v].y * w * next.y, rho[v].z * w * next.z};
-        const uint32_t slot = atomicAdd(count, 1u);
+        const uint32_t slot = base++;
         if (slot < cap) {
             for (int k = 0; k < 9; ++k) out_q[size_t(slot) * 9 + k] = qv[v][k];
             out_t[size_t(slot) * 3 + 0] = Li.x;
