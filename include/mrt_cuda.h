@@ -488,7 +488,8 @@ int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
  * A 3-level U-Net (3x3 convolutions, 32/64/128 channels, skip
  * connections) over 16-channel BF16 NHWC features: log(1 + radiance /
  * albedo), albedo, normal, depth, zero padding.  Forward on the tensor cores (BF16,
- * FP32 accumulate); training backward in FP32; Adam.  The network predicts
+ * FP32 accumulate); training backward on the tensor cores with BF16
+ * gradients (or in FP32, see the modes below); Adam on FP32 master weights.  The network predicts
  * a correction to the input's log(1 + radiance), with an L1 loss.  Width and height must be multiples
  * of 4. */
 typedef struct mrt_denoiser mrt_denoiser;
@@ -499,8 +500,14 @@ int mrt_cuda_denoiser_param_count(mrt_denoiser* den, size_t* weights, size_t* bi
  * persistent, warp-specialised CTAs for the layers without upsampling (a
  * producer warp streaming tensor copies, an MMA warp, four epilogue warps,
  * two tensor-memory accumulators), mode 1 tcgen05 with one CTA per output
- * tile, mode 0 mma.sync (the earliest kernels, kept for comparison).  The
- * two upsampling layers run the per-tile tcgen05 kernel in modes 1 and 2.
+ * tile, mode 0 mma.sync (the earliest kernels, kept for comparison).  In
+ * mode 2 the two upsampling layers gather their halo with four cp.async
+ * producer warps; in mode 1 they run the per-tile cp.async kernel.
+ * The training step's backward follows the mode too: mode 2 runs it on the
+ * tensor cores (BF16 gradients at each layer's pre-activation, data
+ * gradients as convolutions with the mirrored, transposed weights on the
+ * persistent kernel, weight and bias gradients as tcgen05 GEMMs reducing
+ * over the pixels), modes 1 and 0 on FP32 CUDA-core kernels.
  * Returns MRT_EINVAL for another mode. */
 int mrt_cuda_denoiser_set_tcgen05(mrt_denoiser* den, int mode);
 /* Features of one frame from its g-buffer (visibility + hit_t) and colour

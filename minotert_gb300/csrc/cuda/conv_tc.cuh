@@ -86,7 +86,8 @@ __device__ __forceinline__ void tc_load_slice(const ConvArgs& a, uint32_t As, ui
 
 // Epilogue shared by the convolution kernels: warp w reads TMEM lanes
 // 32w..32w+31 (pixels x0 + 32w ..), ROWS x COUT FP32 accumulators, adds the
-// bias, applies ReLU and stores BF16 with 16-byte stores.
+// bias, applies ReLU, zeroes the outputs whose gate is not positive (when the
+// arguments carry a gate tensor) and stores BF16 with 16-byte stores.
 template <int COUT, int ROWS>
 __device__ __forceinline__ void tc_epilogue(const ConvArgs& a, uint32_t taddr, int n, int y0, int x0, int warp,
                                             int lane) {
@@ -108,7 +109,14 @@ __device__ __forceinline__ void tc_epilogue(const ConvArgs& a, uint32_t taddr, i
                 : "r"(ta));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (x < a.w_ && y < a.h) {
-                uint32_t packed[8];
+                uint32_t packed[8], gv[8];
+                if (a.gate) {
+                    const uint4* gp = reinterpret_cast<const uint4*>(
+                        a.gate + ((size_t(n) * a.h + y) * a.w_ + x) * COUT + 16 * jj);
+                    const uint4 g0 = gp[0], g1 = gp[1];
+                    gv[0] = g0.x; gv[1] = g0.y; gv[2] = g0.z; gv[3] = g0.w;
+                    gv[4] = g1.x; gv[5] = g1.y; gv[6] = g1.z; gv[7] = g1.w;
+                }
 #pragma unroll
                 for (int q = 0; q < 8; ++q) {
                     float f0 = __uint_as_float(v[2 * q]) + a.bias[16 * jj + 2 * q];
@@ -116,6 +124,11 @@ __device__ __forceinline__ void tc_epilogue(const ConvArgs& a, uint32_t taddr, i
                     if (a.relu) {
                         f0 = fmaxf(f0, 0.0f);
                         f1 = fmaxf(f1, 0.0f);
+                    }
+                    if (a.gate) {
+                        const float2 g = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&gv[q]));
+                        if (!(g.x > 0.0f)) f0 = 0.0f;
+                        if (!(g.y > 0.0f)) f1 = 0.0f;
                     }
                     const __nv_bfloat162 hv = __floats2bfloat162_rn(f0, f1);
                     packed[q] = *reinterpret_cast<const uint32_t*>(&hv);

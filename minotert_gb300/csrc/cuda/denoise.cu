@@ -21,8 +21,15 @@
 // m16n8k16 (k_conv_fwd: a warp computes 16 consecutive pixels of a row x
 // all output channels); both fold the decoder's 2x upsampling and skip
 // concatenation into their operand loads.
-// Backward: FP32 kernels on the CUDA cores for the data, weight and bias
-// gradients, reading the stored BF16 activations.
+// Backward (tcgen05 mode, the default): BF16 gradients at each layer's
+// pre-activation; the data gradient of a layer is a forward convolution of
+// its output gradient with the mirrored, transposed weights (the same
+// persistent tensor-core kernel, whose epilogue applies the source's ReLU
+// derivative), the gradient through an upsampling or a pooling is an
+// elementwise pass, and the weight and bias gradients are tcgen05 GEMMs that
+// reduce over the pixels (wgrad_tc.cuh).  The other modes keep FP32 kernels
+// on the CUDA cores for the data, weight and bias gradients, reading the
+// stored BF16 activations.
 #include "internal.hpp"
 #include "tcgen05.cuh"
 
@@ -83,6 +90,10 @@ struct ConvArgs {
     const float* bias;
     bf16* y;         // N x H x W x cout
     int n, h, w_, ca, cb, cout, ups, relu;
+    // tensor-core epilogue only: when set, an output is kept where this
+    // N x H x W x cout tensor is positive and zeroed elsewhere (the ReLU
+    // derivative of a data-gradient convolution)
+    const bf16* gate = nullptr;
 };
 
 // channel pair (c, c+1) of the virtual concatenated input at (n, y, x)
@@ -145,6 +156,7 @@ __global__ void __launch_bounds__(128) k_conv_fwd(ConvArgs a) {
 }
 
 #include "conv_tc.cuh"
+#include "wgrad_tc.cuh"
 
 // 2x2 average pool, NHWC
 __global__ void k_pool(const bf16* x, bf16* y, int n, int h, int w, int c) {
@@ -286,21 +298,125 @@ __device__ __forceinline__ float demod_albedo(const bf16* feat, size_t p, int k)
 // L1 loss in log(1 + irradiance) space on channels 0..2 (irradiance =
 // radiance / albedo): the network predicts a correction added to the
 // input's own log(1 + irradiance) (features 0..2)
+// (gradient written as FP32 to dy, or as BF16 to dy16 when that is set)
 __global__ void k_l1_loss(const bf16* y, const bf16* feat, const float* target, size_t pixels, float* dy,
-                          float* loss) {
+                          bf16* dy16, float* loss) {
     float l = 0.0f;
     const float inv = 1.0f / float(pixels * 3);
     for (size_t p = blockIdx.x * size_t(blockDim.x) + threadIdx.x; p < pixels; p += size_t(gridDim.x) * blockDim.x) {
-        for (int k = 0; k < 16; ++k) dy[p * 16 + k] = 0.0f;
+        float g[16] = {};
         for (int k = 0; k < 3; ++k) {
             const float pred = __bfloat162float(y[p * 16 + k]) + __bfloat162float(feat[p * 16 + k]);
             const float d = pred - log1pf(fmaxf(target[p * 3 + k], 0.0f) / demod_albedo(feat, p, k));
             l += fabsf(d);
-            dy[p * 16 + k] = (d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f)) * inv;
+            g[k] = (d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f)) * inv;
+        }
+        if (dy16) {
+            for (int k = 0; k < 16; k += 2)
+                *reinterpret_cast<__nv_bfloat162*>(dy16 + p * 16 + k) = __floats2bfloat162_rn(g[k], g[k + 1]);
+        } else {
+            for (int k = 0; k < 16; ++k) dy[p * 16 + k] = g[k];
         }
     }
     for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xFFFFFFFFu, l, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(loss, l * inv);
+}
+
+// ---- backward (BF16, tensor-core mode) ------------------------------------
+
+// Weights of the data-gradient convolutions in the TMA form's layout.  The
+// data gradient of a 3x3 convolution is a 3x3 convolution of its output
+// gradient with the taps mirrored and inputs and outputs swapped:
+// W'[ci][tap][co] = W[co][8 - tap][ci].  Per layer and source part (a: input
+// channels [0, ca), b: [ca, ca + cb)) the part's W' is stored as
+// [slice of 16 co][tap][half][ci][8 co] at dst_off.
+struct BwdTable {
+    int parts;
+    int cp[2 * kLayers], cout[2 * kLayers], ci0[2 * kLayers], cin[2 * kLayers];
+    size_t src_off[2 * kLayers], dst_off[2 * kLayers];
+};
+__global__ void k_bwd_weights(const bf16* w16, bf16* wt, BwdTable t) {
+    for (int e = 0; e < t.parts; ++e) {
+        const int cp = t.cp[e], cin = t.cin[e], ci0 = t.ci0[e];
+        const size_t total = size_t(9) * cp * t.cout[e];
+        for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+            const int e8 = int(i % 8);
+            size_t q = i / 8;
+            const int ci = int(q % cp);
+            q /= cp;
+            const int hf = int(q % 2);
+            q /= 2;
+            const int tap = int(q % 9);
+            const int k = int(q / 9);
+            const int co = 16 * k + 8 * hf + e8;
+            wt[t.dst_off[e] + i] = w16[t.src_off[e] + (size_t(co) * 9 + (8 - tap)) * cin + ci0 + ci];
+        }
+    }
+}
+
+// Gradient of a source read through the nearest 2x upsampling: the sum of
+// the 2x2 children of t (2h x 2w, full-resolution data gradient), kept where
+// the source's stored activation is positive (its ReLU), into dz (h x w).
+// One thread per 8 channels of a pixel.
+__global__ void k_bwd_unup(const bf16* t, const bf16* act, bf16* dz, int n, int h, int w, int c) {
+    const int c8 = c / 8;
+    const size_t total = size_t(n) * h * w * c8;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+        const int cg = int(i % c8);
+        const size_t p = i / c8;
+        const int x = int(p % w), y = int((p / w) % h), nn = int(p / (size_t(w) * h));
+        float s[8] = {};
+        for (int k = 0; k < 4; ++k) {
+            const uint4 v = *reinterpret_cast<const uint4*>(
+                t + ((size_t(nn) * 2 * h + 2 * y + (k >> 1)) * 2 * w + 2 * x + (k & 1)) * c + 8 * cg);
+            const __nv_bfloat162* b = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float2 f = __bfloat1622float2(b[q]);
+                s[2 * q] += f.x;
+                s[2 * q + 1] += f.y;
+            }
+        }
+        const uint4 gv = *reinterpret_cast<const uint4*>(act + p * c + 8 * cg);
+        const __nv_bfloat162* g = reinterpret_cast<const __nv_bfloat162*>(&gv);
+        uint4 o;
+        __nv_bfloat162* ob = reinterpret_cast<__nv_bfloat162*>(&o);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float2 gf = __bfloat1622float2(g[q]);
+            ob[q] = __floats2bfloat162_rn(gf.x > 0.0f ? s[2 * q] : 0.0f, gf.y > 0.0f ? s[2 * q + 1] : 0.0f);
+        }
+        *reinterpret_cast<uint4*>(dz + p * c + 8 * cg) = o;
+    }
+}
+
+// Gradient of a skip source that is also pooled: its data gradient through
+// the skip concatenation plus a quarter of the pooled input's gradient
+// (h/2 x w/2), kept where the source's activation is positive, into dz.
+__global__ void k_bwd_unpool(const bf16* skip, const bf16* gp, const bf16* act, bf16* dz, int n, int h, int w,
+                             int c) {
+    const int c8 = c / 8;
+    const size_t total = size_t(n) * h * w * c8;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+        const int cg = int(i % c8);
+        const size_t p = i / c8;
+        const int x = int(p % w), y = int((p / w) % h), nn = int(p / (size_t(w) * h));
+        const uint4 sv = *reinterpret_cast<const uint4*>(skip + p * c + 8 * cg);
+        const uint4 pv = *reinterpret_cast<const uint4*>(
+            gp + ((size_t(nn) * (h / 2) + y / 2) * (w / 2) + x / 2) * c + 8 * cg);
+        const uint4 gv = *reinterpret_cast<const uint4*>(act + p * c + 8 * cg);
+        const __nv_bfloat162* sb = reinterpret_cast<const __nv_bfloat162*>(&sv);
+        const __nv_bfloat162* pb = reinterpret_cast<const __nv_bfloat162*>(&pv);
+        const __nv_bfloat162* gb = reinterpret_cast<const __nv_bfloat162*>(&gv);
+        uint4 o;
+        __nv_bfloat162* ob = reinterpret_cast<__nv_bfloat162*>(&o);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float2 a = __bfloat1622float2(sb[q]), b = __bfloat1622float2(pb[q]), g = __bfloat1622float2(gb[q]);
+            ob[q] = __floats2bfloat162_rn(g.x > 0.0f ? a.x + 0.25f * b.x : 0.0f, g.y > 0.0f ? a.y + 0.25f * b.y : 0.0f);
+        }
+        *reinterpret_cast<uint4*>(dz + p * c + 8 * cg) = o;
+    }
 }
 
 __global__ void k_adam_bf16(float* p, float* m, float* v, float* g, bf16* p16, size_t n, float lr, float b1, float b2,
@@ -370,6 +486,17 @@ struct mrt_denoiser {
     bf16 *pool0 = nullptr, *pool1 = nullptr;
     float* grad[kLayers] = {};
     float *gpool0 = nullptr, *gpool1 = nullptr, *gin = nullptr;
+    // tensor-core backward: BF16 gradients at each layer's pre-activation
+    // (gz), the data gradients of the decoder's upsampled sources at the
+    // consumer's resolution (up8: d0a's, 64 channels at full resolution; up6:
+    // d1a's, 128 at half), of the skip sources (skip8: S0 from d0a, skip6: S1
+    // from d1a) and of the pooled inputs (gp0, gp1); the mirrored, transposed
+    // weights of the data-gradient convolutions (wbt) and zero biases
+    size_t gz_pix = 0;
+    bf16* gz[kLayers] = {};
+    bf16 *up8 = nullptr, *up6 = nullptr, *skip8 = nullptr, *skip6 = nullptr, *gp0 = nullptr, *gp1 = nullptr;
+    bf16* wbt = nullptr;
+    float* zeros = nullptr;
     float* loss = nullptr;
     float* h_loss = nullptr;
     uint32_t step = 0;
@@ -403,7 +530,27 @@ int ensure_acts(mrt_ctx* ctx, mrt_denoiser* d, size_t pix, bool grads) {
         }
         d->cap_pix = pix;
     }
-    if (grads && d->grad_pix < pix) {
+    if (grads && d->tc_mode == 2 && d->gz_pix < pix) {
+        for (int l = 0; l < kLayers; ++l) { cudaFree(d->gz[l]); d->gz[l] = nullptr; }
+        bf16** tmp[] = {&d->up8, &d->up6, &d->skip8, &d->skip6, &d->gp0, &d->gp1};
+        for (bf16** t : tmp) { cudaFree(*t); *t = nullptr; }
+        d->gz_pix = 0;
+        bool ok = true;
+        for (int l = 0; l < kLayers && ok; ++l)
+            ok = cudaMalloc(&d->gz[l], layer_pixels(pix, d->layers[l].scale) * d->layers[l].cout * 2) == cudaSuccess;
+        ok = ok && cudaMalloc(&d->up8, pix * 64 * 2) == cudaSuccess &&
+             cudaMalloc(&d->up6, layer_pixels(pix, 1) * 128 * 2) == cudaSuccess &&
+             cudaMalloc(&d->skip8, pix * 32 * 2) == cudaSuccess &&
+             cudaMalloc(&d->skip6, layer_pixels(pix, 1) * 64 * 2) == cudaSuccess &&
+             cudaMalloc(&d->gp0, layer_pixels(pix, 1) * 32 * 2) == cudaSuccess &&
+             cudaMalloc(&d->gp1, layer_pixels(pix, 2) * 64 * 2) == cudaSuccess;
+        if (!ok) {
+            cudaGetLastError();
+            return set_error(ctx, MRT_ENOMEM, "denoiser: gradient buffers");
+        }
+        d->gz_pix = pix;
+    }
+    if (grads && d->tc_mode != 2 && d->grad_pix < pix) {
         for (int l = 0; l < kLayers; ++l) { cudaFree(d->grad[l]); d->grad[l] = nullptr; }
         cudaFree(d->gpool0); cudaFree(d->gpool1); cudaFree(d->gin);
         d->gpool0 = d->gpool1 = d->gin = nullptr;
@@ -512,6 +659,108 @@ void bwd_layer(mrt_denoiser* d, int l, const bf16* xa, const bf16* xb, float* ga
                                                                       L.cb, L.cout, L.ups, ga, gb);
 }
 
+// data-gradient convolution of layer l for source part `part` (0: a, 1: b):
+// from the layer's pre-activation gradient dz (cout channels) to the part's
+// channels at the layer's resolution, zeroed where `gate` (the source's
+// activation) is not positive when that is set
+cudaError_t dgrad(const mrt_denoiser* d, int l, int part, const bf16* dz, bf16* out, const bf16* gate, int n, int h,
+                  int w, cudaStream_t s) {
+    const ConvDesc& L = d->layers[l];
+    const int cp = part ? L.cb : L.ca;
+    ConvArgs ca{dz, nullptr, d->w16, d->zeros, out, n, h, w, L.cout, 0, cp, 0, 0};
+    ca.gate = gate;
+    const bf16* wt = d->wbt + L.w_off + (part ? size_t(9) * L.cout * L.ca : 0);
+    switch (cp) {
+    case 32: return launch_conv_ws<32, false>(ca, wt, d->status, d->sm_count, s);
+    case 64: return launch_conv_ws<64, false>(ca, wt, d->status, d->sm_count, s);
+    case 128: return launch_conv_ws<128, false>(ca, wt, d->status, d->sm_count, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+// weight and bias gradients of layer l from its pre-activation gradient dz
+// and its sources
+cudaError_t wgrad(const mrt_denoiser* d, int l, const bf16* dz, const bf16* xa, const bf16* xb, int n, int h, int w,
+                  cudaStream_t s) {
+    const ConvDesc& L = d->layers[l];
+    const WgArgs wa{dz, xa, xb, d->wg + L.w_off, d->wg + L.b_off, n, h, w, L.ca, L.cb, L.cout, L.ups};
+    if (L.ca + L.cb == 16) return L.cout == 32 ? launch_conv_wgrad<32, 16>(wa, d->status, d->sm_count, s)
+                                               : cudaErrorInvalidValue;
+    switch (L.cout) {
+    case 16: return launch_conv_wgrad<16, 32>(wa, d->status, d->sm_count, s);
+    case 32: return launch_conv_wgrad<32, 32>(wa, d->status, d->sm_count, s);
+    case 64: return launch_conv_wgrad<64, 32>(wa, d->status, d->sm_count, s);
+    case 128: return launch_conv_wgrad<128, 32>(wa, d->status, d->sm_count, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+// Backward of the whole network on the tensor cores, from the loss gradient
+// in gz[10]; accumulates the weight and bias gradients into wg.  Returns the
+// number of kernels launched through *launches.
+cudaError_t backward_tc(mrt_denoiser* d, const bf16* in, int n, int h, int w, cudaStream_t s, int* launches) {
+    BwdTable t{};
+    for (int l = 1; l < kLayers; ++l) {
+        const ConvDesc& L = d->layers[l];
+        for (int part = 0; part < (L.cb ? 2 : 1); ++part) {
+            const int e = t.parts++;
+            t.cp[e] = part ? L.cb : L.ca;
+            t.cout[e] = L.cout;
+            t.ci0[e] = part ? L.ca : 0;
+            t.cin[e] = L.ca + L.cb;
+            t.src_off[e] = L.w_off;
+            t.dst_off[e] = L.w_off + (part ? size_t(9) * L.cout * L.ca : 0);
+        }
+    }
+    k_bwd_weights<<<304, 256, 0, s>>>(d->w16, d->wbt, t);
+    bf16* const* z = d->gz;
+    bf16* const* x = d->act;
+    const int h1 = h / 2, w1 = w / 2, h2 = h / 4, w2 = w / 4;
+    cudaError_t e;
+    int k = 1;
+#define MRT_TRY(call) do { if ((e = (call)) != cudaSuccess) return e; ++k; } while (0)
+    // out (no ReLU: its pre-activation gradient is the loss gradient), d0b
+    MRT_TRY(wgrad(d, 10, z[10], x[9], nullptr, n, h, w, s));
+    MRT_TRY(dgrad(d, 10, 0, z[10], z[9], x[9], n, h, w, s));
+    MRT_TRY(wgrad(d, 9, z[9], x[8], nullptr, n, h, w, s));
+    MRT_TRY(dgrad(d, 9, 0, z[9], z[8], x[8], n, h, w, s));
+    // d0a: up(d1b) ++ S0
+    MRT_TRY(wgrad(d, 8, z[8], x[7], x[1], n, h, w, s));
+    MRT_TRY(dgrad(d, 8, 0, z[8], d->up8, nullptr, n, h, w, s));
+    k_bwd_unup<<<grid_for(size_t(n) * h1 * w1 * 8), 256, 0, s>>>(d->up8, x[7], z[7], n, h1, w1, 64);
+    ++k;
+    MRT_TRY(dgrad(d, 8, 1, z[8], d->skip8, nullptr, n, h, w, s));
+    // d1b; d1a: up(e2b) ++ S1
+    MRT_TRY(wgrad(d, 7, z[7], x[6], nullptr, n, h1, w1, s));
+    MRT_TRY(dgrad(d, 7, 0, z[7], z[6], x[6], n, h1, w1, s));
+    MRT_TRY(wgrad(d, 6, z[6], x[5], x[3], n, h1, w1, s));
+    MRT_TRY(dgrad(d, 6, 0, z[6], d->up6, nullptr, n, h1, w1, s));
+    k_bwd_unup<<<grid_for(size_t(n) * h2 * w2 * 16), 256, 0, s>>>(d->up6, x[5], z[5], n, h2, w2, 128);
+    ++k;
+    MRT_TRY(dgrad(d, 6, 1, z[6], d->skip6, nullptr, n, h1, w1, s));
+    // e2b; e2a (input: pooled S1)
+    MRT_TRY(wgrad(d, 5, z[5], x[4], nullptr, n, h2, w2, s));
+    MRT_TRY(dgrad(d, 5, 0, z[5], z[4], x[4], n, h2, w2, s));
+    MRT_TRY(wgrad(d, 4, z[4], d->pool1, nullptr, n, h2, w2, s));
+    MRT_TRY(dgrad(d, 4, 0, z[4], d->gp1, nullptr, n, h2, w2, s));
+    k_bwd_unpool<<<grid_for(size_t(n) * h1 * w1 * 8), 256, 0, s>>>(d->skip6, d->gp1, x[3], z[3], n, h1, w1, 64);
+    ++k;
+    // e1b; e1a (input: pooled S0)
+    MRT_TRY(wgrad(d, 3, z[3], x[2], nullptr, n, h1, w1, s));
+    MRT_TRY(dgrad(d, 3, 0, z[3], z[2], x[2], n, h1, w1, s));
+    MRT_TRY(wgrad(d, 2, z[2], d->pool0, nullptr, n, h1, w1, s));
+    MRT_TRY(dgrad(d, 2, 0, z[2], d->gp0, nullptr, n, h1, w1, s));
+    k_bwd_unpool<<<grid_for(size_t(n) * h * w * 4), 256, 0, s>>>(d->skip8, d->gp0, x[1], z[1], n, h, w, 32);
+    ++k;
+    // e0b; e0a (input: the features)
+    MRT_TRY(wgrad(d, 1, z[1], x[0], nullptr, n, h, w, s));
+    MRT_TRY(dgrad(d, 1, 0, z[1], z[0], x[0], n, h, w, s));
+    MRT_TRY(wgrad(d, 0, z[0], in, nullptr, n, h, w, s));
+#undef MRT_TRY
+    *launches = k;
+    return cudaGetLastError();
+}
+
 } // namespace
 
 extern "C" {
@@ -541,6 +790,7 @@ int mrt_cuda_denoiser_create(mrt_ctx* ctx, uint32_t seed, mrt_denoiser** out) {
     bool ok = cudaMalloc(&d->w, total * 4) == cudaSuccess && cudaMalloc(&d->wm, total * 4) == cudaSuccess &&
               cudaMalloc(&d->wv, total * 4) == cudaSuccess && cudaMalloc(&d->wg, total * 4) == cudaSuccess &&
               cudaMalloc(&d->w16, d->n_w * 2) == cudaSuccess && cudaMalloc(&d->wtc, d->n_w * 2) == cudaSuccess &&
+              cudaMalloc(&d->wbt, d->n_w * 2) == cudaSuccess && cudaMalloc(&d->zeros, 128 * 4) == cudaSuccess &&
               cudaMalloc(&d->loss, 4) == cudaSuccess &&
               cudaMallocHost(&d->h_loss, 4) == cudaSuccess;
     if (!ok) {
@@ -575,7 +825,7 @@ int mrt_cuda_denoiser_create(mrt_ctx* ctx, uint32_t seed, mrt_denoiser** out) {
     ok = cudaMemcpy(d->w, w.data(), total * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(d->w16, w16.data(), d->n_w * 2, cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemset(d->wm, 0, total * 4) == cudaSuccess && cudaMemset(d->wv, 0, total * 4) == cudaSuccess &&
-         cudaMemset(d->wg, 0, total * 4) == cudaSuccess;
+         cudaMemset(d->wg, 0, total * 4) == cudaSuccess && cudaMemset(d->zeros, 0, 128 * 4) == cudaSuccess;
     if (!ok) {
         mrt_cuda_denoiser_destroy(ctx, d);
         return set_error(ctx, MRT_ECUDA, "denoiser_create: upload failed");
@@ -588,9 +838,9 @@ int mrt_cuda_denoiser_destroy(mrt_ctx* ctx, mrt_denoiser* d) {
     if (!ctx || !d) return MRT_EINVAL;
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
-    for (int l = 0; l < kLayers; ++l) { cudaFree(d->act[l]); cudaFree(d->grad[l]); }
+    for (int l = 0; l < kLayers; ++l) { cudaFree(d->act[l]); cudaFree(d->grad[l]); cudaFree(d->gz[l]); }
     void* ps[] = {d->w, d->wm, d->wv, d->wg, d->w16, d->wtc, d->pool0, d->pool1, d->gpool0, d->gpool1, d->gin,
-                  d->loss};
+                  d->loss, d->wbt, d->zeros, d->up8, d->up6, d->skip8, d->skip6, d->gp0, d->gp1};
     for (void* p : ps) cudaFree(p);
     if (d->h_loss) cudaFreeHost(d->h_loss);
     delete d;
@@ -655,27 +905,37 @@ int mrt_cuda_denoiser_train_step(mrt_ctx* ctx, mrt_denoiser* d, const uint16_t* 
     const bf16* in = reinterpret_cast<const bf16*>(features);
     if (forward(d, in, n, h, w, s) != cudaSuccess) return set_error(ctx, MRT_ECUDA, "denoiser_train: forward");
     cudaMemsetAsync(d->loss, 0, 4, s);
-    k_l1_loss<<<grid_for(pix), 256, 0, s>>>(d->act[kLayers - 1], in, targets, pix, d->grad[kLayers - 1], d->loss);
-    // zero the gradient buffers that accumulate from several consumers
-    for (int l = 0; l < kLayers - 1; ++l)
-        cudaMemsetAsync(d->grad[l], 0, layer_pixels(pix, d->layers[l].scale) * d->layers[l].cout * 4, s);
-    cudaMemsetAsync(d->gpool0, 0, layer_pixels(pix, 1) * 32 * 4, s);
-    cudaMemsetAsync(d->gpool1, 0, layer_pixels(pix, 2) * 64 * 4, s);
-    cudaMemsetAsync(d->gin, 0, pix * 16 * 4, s);
-    bwd_layer(d, 10, d->act[9], nullptr, d->grad[9], nullptr, n, h, w, s);
-    bwd_layer(d, 9, d->act[8], nullptr, d->grad[8], nullptr, n, h, w, s);
-    bwd_layer(d, 8, d->act[7], d->act[1], d->grad[7], d->grad[1], n, h, w, s);
-    bwd_layer(d, 7, d->act[6], nullptr, d->grad[6], nullptr, n, h / 2, w / 2, s);
-    bwd_layer(d, 6, d->act[5], d->act[3], d->grad[5], d->grad[3], n, h / 2, w / 2, s);
-    bwd_layer(d, 5, d->act[4], nullptr, d->grad[4], nullptr, n, h / 4, w / 4, s);
-    bwd_layer(d, 4, d->pool1, nullptr, d->gpool1, nullptr, n, h / 4, w / 4, s);
-    k_pool_bwd<<<grid_for(pix / 4 * 64), 256, 0, s>>>(d->gpool1, d->grad[3], n, h / 2, w / 2, 64);
-    bwd_layer(d, 3, d->act[2], nullptr, d->grad[2], nullptr, n, h / 2, w / 2, s);
-    bwd_layer(d, 2, d->pool0, nullptr, d->gpool0, nullptr, n, h / 2, w / 2, s);
-    k_pool_bwd<<<grid_for(pix * 32), 256, 0, s>>>(d->gpool0, d->grad[1], n, h, w, 32);
-    bwd_layer(d, 1, d->act[0], nullptr, d->grad[0], nullptr, n, h, w, s);
-    bwd_layer(d, 0, in, nullptr, nullptr, nullptr, n, h, w, s);
-    ctx->launches += 40;
+    if (d->tc_mode == 2) {
+        k_l1_loss<<<grid_for(pix), 256, 0, s>>>(d->act[kLayers - 1], in, targets, pix, nullptr, d->gz[kLayers - 1],
+                                               d->loss);
+        int launched = 0;
+        if (backward_tc(d, in, n, h, w, s, &launched) != cudaSuccess)
+            return set_error(ctx, MRT_ECUDA, "denoiser_train: backward");
+        ctx->launches += 15 + launched;  // forward 14, loss 1
+    } else {
+        k_l1_loss<<<grid_for(pix), 256, 0, s>>>(d->act[kLayers - 1], in, targets, pix, d->grad[kLayers - 1], nullptr,
+                                               d->loss);
+        // zero the gradient buffers that accumulate from several consumers
+        for (int l = 0; l < kLayers - 1; ++l)
+            cudaMemsetAsync(d->grad[l], 0, layer_pixels(pix, d->layers[l].scale) * d->layers[l].cout * 4, s);
+        cudaMemsetAsync(d->gpool0, 0, layer_pixels(pix, 1) * 32 * 4, s);
+        cudaMemsetAsync(d->gpool1, 0, layer_pixels(pix, 2) * 64 * 4, s);
+        cudaMemsetAsync(d->gin, 0, pix * 16 * 4, s);
+        bwd_layer(d, 10, d->act[9], nullptr, d->grad[9], nullptr, n, h, w, s);
+        bwd_layer(d, 9, d->act[8], nullptr, d->grad[8], nullptr, n, h, w, s);
+        bwd_layer(d, 8, d->act[7], d->act[1], d->grad[7], d->grad[1], n, h, w, s);
+        bwd_layer(d, 7, d->act[6], nullptr, d->grad[6], nullptr, n, h / 2, w / 2, s);
+        bwd_layer(d, 6, d->act[5], d->act[3], d->grad[5], d->grad[3], n, h / 2, w / 2, s);
+        bwd_layer(d, 5, d->act[4], nullptr, d->grad[4], nullptr, n, h / 4, w / 4, s);
+        bwd_layer(d, 4, d->pool1, nullptr, d->gpool1, nullptr, n, h / 4, w / 4, s);
+        k_pool_bwd<<<grid_for(pix / 4 * 64), 256, 0, s>>>(d->gpool1, d->grad[3], n, h / 2, w / 2, 64);
+        bwd_layer(d, 3, d->act[2], nullptr, d->grad[2], nullptr, n, h / 2, w / 2, s);
+        bwd_layer(d, 2, d->pool0, nullptr, d->gpool0, nullptr, n, h / 2, w / 2, s);
+        k_pool_bwd<<<grid_for(pix * 32), 256, 0, s>>>(d->gpool0, d->grad[1], n, h, w, 32);
+        bwd_layer(d, 1, d->act[0], nullptr, d->grad[0], nullptr, n, h, w, s);
+        bwd_layer(d, 0, in, nullptr, nullptr, nullptr, n, h, w, s);
+        ctx->launches += 40;
+    }
     if (apply_update) {
         d->step++;
         const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;

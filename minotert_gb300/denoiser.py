@@ -32,7 +32,8 @@ class Denoiser:
     def set_tcgen05(self, mode):
         """Forward convolutions: 2 (or True) persistent warp-specialised
         tcgen05 kernels (default), 1 tcgen05 with one CTA per tile, 0 (or
-        False) mma.sync."""
+        False) mma.sync.  The training backward runs on the tensor cores in
+        mode 2 and on FP32 CUDA-core kernels in modes 1 and 0."""
         mode = 2 if mode is True else int(mode)
         self.ctx.check(lib().mrt_cuda_denoiser_set_tcgen05(self._h, mode), "denoiser_set_tcgen05")
 

@@ -164,3 +164,43 @@ def test_denoiser_tcgen05_matches_mma_sync(ctx, shape):
     err = np.abs(ws - b)
     assert err.max() < 3e-2 * max(1.0, np.abs(b).max()), err.max()
     assert err.mean() < 2e-3 * max(1.0, np.abs(b).mean())
+
+
+@pytest.mark.parametrize("shape", [(2, 16, 16), (1, 36, 200), (8, 128, 128)])
+def test_denoiser_tensor_core_backward_matches_fp32(ctx, shape):
+    # one training step's gradients from the tcgen05 backward (mode 2: BF16
+    # pre-activation gradients, data gradients as mirrored convolutions,
+    # weight and bias gradients as GEMMs over the pixels) against the FP32
+    # CUDA-core backward (mode 1, whose forward issues the same MMAs in the
+    # same order, so both start from the same activations and loss); per
+    # layer, weights and biases separately, so a broken tap, channel chunk
+    # or bias column shows by name.  Shapes: the gradient test's tiny
+    # images, a width of two 128-pixel segments with a ragged end, and the
+    # training batch (8 crops of 128 x 128)
+    n, h, w = shape
+    x, t = _inputs(n, h, w, 7)
+    d_x, d_t = ctx.to_device(to_bf16_bits(x)), ctx.to_device(t)
+    res = {}
+    for mode in (2, 1):
+        d = Denoiser(ctx, seed=9)
+        d.set_tcgen05(mode)
+        loss = d.train_step(d_x, d_t, n, w, h, update=False, want_loss=True)
+        res[mode] = (loss, d.params(1).astype(np.float64))
+        d.close()
+    assert ctx.status() == 0
+    (l_tc, g_tc), (l_fp, g_fp) = res[2], res[1]
+    assert abs(l_tc - l_fp) <= 1e-6 * abs(l_fp), (l_tc, l_fp)
+    assert np.isfinite(g_tc).all()
+    ws_tc, bs_tc = cnn.split(g_tc)
+    ws_fp, bs_fp = cnn.split(g_fp)
+    for l, (a, b) in enumerate(zip(ws_tc + bs_tc, ws_fp + bs_fp)):
+        name = f"{'w' if l < len(ws_tc) else 'b'}{l % len(ws_tc)}"
+        a, b = a.ravel(), b.ravel()
+        nb = np.linalg.norm(b)
+        if nb == 0:
+            assert np.linalg.norm(a) == 0, name
+            continue
+        rel = np.linalg.norm(a - b) / nb
+        assert rel < 3e-2, (name, rel)
+    cos = g_tc @ g_fp / (np.linalg.norm(g_tc) * np.linalg.norm(g_fp))
+    assert cos > 0.999, cos
