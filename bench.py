@@ -858,17 +858,28 @@ def run_cache_experiment(args, world, rank, local, dist):
 
 def run_denoise_experiment(args, world, rank, local, dist):
     """GPU milliseconds to RMSE 0.01 on a held-out 1920x1080 frame: plain
-    accumulation vs the CNN denoiser applied to the accumulated image.  The
-    denoiser is trained first on pairs the path tracer renders itself:
-    seeded heightfield + boxes scenes at random cameras rendered at
-    1920x1080, 1-spp inputs and 256-spp targets, 16 random 128x128 crops
-    per scene."""
+    accumulation vs the CNN denoiser applied to the accumulated image.
+
+    Training set (the configuration's 2,000 seeded procedural scenes with
+    4,096-spp targets): MRT_DENOISE_SCENES (default 2,000) seeded heightfield
+    + boxes scenes, each seen by a random camera whose 1080p frustum is cut to
+    a random 256 x 256 window (an off-centre projection, so a pixel covers the
+    scene area it covers in the 1080p evaluation frame).  Inputs: the
+    single-scene tracer's 1-spp frame of the window, as denoiser features.
+    Targets: the 4,096-sample mean of the same pixels from the batched tracer
+    (32 scenes per launch, 16 copies of each primary ray, 256 launches).
+    Constant sky plus a directional light sampled with shadow rays at every
+    vertex (both tracers' next-event estimator: they estimate the same
+    radiance), 8 bounces, Russian roulette after bounce 2."""
+    from concurrent.futures import ThreadPoolExecutor
+    from dataclasses import replace
+
     from minotert_gb300 import build as _build
     _build.build()
     from minotert_gb300 import scene
     from minotert_gb300._lib import Context
     from minotert_gb300.denoiser import Denoiser
-    from minotert_gb300.pathtracer import Camera, Pathtracer, Sky, TraceSettings
+    from minotert_gb300.pathtracer import Camera, Pathtracer, Sky, TraceSettings, primary_rays_host
 
     ctx = Context(local)
     stream = ctx.stream()
@@ -886,62 +897,110 @@ def run_denoise_experiment(args, world, rank, local, dist):
         pitch = -np.arctan2(z, r) + rng.uniform(-0.15, 0.15)
         return Camera((w, h), np.radians(60.0), 0.01, pos, float(yaw), float(pitch))
 
+    def settings(frame, samples=1):
+        return TraceSettings(samples, SET["bounces"], SET["rr_start"], SET["rng_mode"], True, frame)
+
     def render(pt, cam, w, h, frames, start):
         col = ctx.alloc(12 * w * h)
         for f in range(frames):
             pt.frame_counter = start + f
             gb = pt.primaryRays((w, h), cam, cam, stream)
-            pt.secondaryRays(gb, cam, sky, bn, TraceSettings(1, SET["bounces"], SET["rr_start"], SET["rng_mode"],
-                                                             True, f), color=col, stream=stream)
+            pt.secondaryRays(gb, cam, sky, bn, settings(f), color=col, stream=stream)
         return col, gb
 
-    # ---- training data: 1-spp frames and TSPP-spp targets rendered at the
-    # evaluation resolution (so a pixel covers the same scene area), cut into
-    # K random 128x128 crops per scene, stored in shuffled order
+    def diagonal(mesh):
+        return float(np.linalg.norm(mesh.hi - mesh.lo))
+
+    # ---- training set
     t0 = time.perf_counter()
-    S, K, CW, TSPP = int(os.environ.get("MRT_DENOISE_SCENES", "48")), 16, 128, 256
+    S = int(os.environ.get("MRT_DENOISE_SCENES", "2000"))
+    T, TSPP, COPIES, G = 256, 4096, 16, 32
     FW, FH = 1920, 1080
-    N = S * K
-    feats = ctx.alloc(N * CW * CW * 16 * 2)
-    targets = ctx.alloc(N * CW * CW * 3 * 4)
-    f_full = ctx.alloc(FW * FH * 16 * 2)
+    px = T * T
+    feats = ctx.alloc(S * px * 16 * 2)
+    targets = ctx.alloc(S * px * 3 * 4)
+    slot = np.random.default_rng(3).permutation(S)   # storage order: batches of consecutive tiles mix scenes
+    col = ctx.alloc(12 * px)
+    n_rays = G * COPIES * px
+    d_rays, d_rad, acc = ctx.alloc(32 * n_rays), ctx.alloc(12 * n_rays), ctx.alloc(12 * G * px)
+    params = TraceSettings(1, SET["bounces"], SET["rr_start"]).params(sky)
     from minotert_gb300._lib import lib
     import ctypes as C
-    slot = np.random.default_rng(3).permutation(N)
     d2d = lib().mrt_cuda_copy_d2d
-    for s_ in range(S):
-        rng = np.random.default_rng(1000 + s_)
-        mesh = scene.heightfield_boxes(2000 + s_, 64, 32)
-        ds = scene.DeviceScene.triangles(ctx, mesh)
-        pt = Pathtracer(ctx, ds, full_gbuffer=False)
-        cam = camera(rng, FW, FH)
-        noisy, gb = render(pt, cam, FW, FH, 1, 50_000 + s_)
-        den.features(ds, gb, noisy, float(np.linalg.norm(mesh.hi - mesh.lo)), f_full, stream)
-        ref, _ = render(pt, cam, FW, FH, TSPP, 90_000 + s_ * TSPP)
-        for k in range(K):
-            y0 = 4 * int(rng.integers(0, (FH - CW) // 4 + 1))
-            x0 = 4 * int(rng.integers(0, (FW - CW) // 4 + 1))
-            i = int(slot[s_ * K + k])
-            for r in range(CW):
-                src = (y0 + r) * FW + x0
-                d2d(ctx.handle, C.c_void_p(feats.ptr + (i * CW * CW + r * CW) * 32), C.c_void_p(f_full.ptr + src * 32),
-                    CW * 32, C.c_void_p(stream))
-                d2d(ctx.handle, C.c_void_p(targets.ptr + (i * CW * CW + r * CW) * 12), C.c_void_p(ref.ptr + src * 12),
-                    CW * 12, C.c_void_p(stream))
-        ctx.sync(stream)
-    data_s = time.perf_counter() - t0
+    pt = None
+    in_sum = tg_sum = 0.0
+    t_inputs = t_targets = 0.0
+    calls = 0
 
-    # ---- training
+    def make(s):
+        m = scene.heightfield_boxes(2000 + s, 64, 32)
+        return m, scene.build_bvh8(m)
+
+    with ThreadPoolExecutor(max(1, min(16, os.cpu_count() or 1))) as ex:
+        pending = ex.map(make, range(0, min(G, S)))
+        for g0 in range(0, S, G):
+            ids = list(range(g0, min(S, g0 + G)))
+            built = list(pending)
+            if g0 + G < S:  # the next group's meshes and BVHs while this one renders
+                pending = ex.map(make, range(g0 + G, min(S, g0 + 2 * G)))
+            ta = time.perf_counter()
+            rays, keep = [], []
+            for s_, (mesh, bvh) in zip(ids, built):
+                rng = np.random.default_rng(1000 + s_)
+                cam = camera(rng, FW, FH)
+                cam = replace(cam, window=(int(rng.integers(0, FW - T + 1)), int(rng.integers(0, FH - T + 1)), T, T))
+                ds = scene.DeviceScene.triangles(ctx, mesh, bvh)
+                if pt is None:
+                    pt = Pathtracer(ctx, ds, full_gbuffer=False)
+                pt.scene = ds
+                pt.frame_counter = 50_000 + s_
+                col.zero(stream)
+                gb = pt.primaryRays((T, T), cam, cam, stream)
+                pt.secondaryRays(gb, cam, sky, bn, settings(0), color=col, stream=stream)
+                den.features(ds, gb, col, diagonal(mesh), feats.ptr + int(slot[s_]) * px * 32, stream)
+                in_sum += float(col.download(np.float32, (px * 3,), stream).astype(np.float64).sum())
+                rays.append(np.tile(primary_rays_host(cam, T, T), COPIES))
+                keep.append(ds)
+            ctx.sync(stream)
+            keep.clear()
+            tb = time.perf_counter()
+            t_inputs += tb - ta
+            batch = scene.DeviceBatch(ctx, built)
+            allr = np.concatenate(rays)
+            d_rays.upload(allr)
+            offs = (np.arange(len(ids) + 1, dtype=np.uint32) * np.uint32(COPIES * px))
+            acc.zero(stream)
+            for c in range(TSPP // COPIES):
+                batch.pathtrace(d_rays, offs, params, 1_000_003 * g0 + c, d_rad, use_graph=True, stream=stream)
+                scene.accumulate_copies(ctx, acc, d_rad, len(ids), COPIES, 3 * px, 1.0 / TSPP, stream)
+                calls += 1
+            for j, s_ in enumerate(ids):
+                d2d(ctx.handle, C.c_void_p(targets.ptr + int(slot[s_]) * px * 12), C.c_void_p(acc.ptr + j * px * 12),
+                    px * 12, C.c_void_p(stream))
+            tg_sum += float(acc.download(np.float32, (len(ids) * px * 3,), stream).astype(np.float64).sum())
+            batch.close()
+            t_targets += time.perf_counter() - tb
+            if g0 // G % 8 == 0:
+                print(f"[denoise] training set: {g0 + len(ids)}/{S} scenes, inputs {t_inputs:.1f} s, "
+                      f"targets {t_targets:.1f} s", file=sys.stderr, flush=True)
+    ctx.sync(stream)
+    del d_rays, d_rad, acc
+    data_s = time.perf_counter() - t0
+    # the two tracers estimate the same radiance: the 1-spp inputs' mean over
+    # the whole set against the targets' (131M pixels each)
+    mean_ratio = in_sum / tg_sum if tg_sum > 0 else None
+
+    # ---- training: batches of B consecutive tiles of the shuffled set
     t1 = time.perf_counter()
-    steps, B = int(os.environ.get("MRT_DENOISE_STEPS", "3000")), 8
+    steps, B = int(os.environ.get("MRT_DENOISE_STEPS", "8000")), 4
     losses = []
     ev0, ev1 = ctx.event(), ctx.event()
     ctx.record(ev0, stream)
     for k in range(steps):
-        i0 = (k * B) % (N - B + 1)
+        i0 = (k * B) % (S - B + 1)
         lr = 5e-4 if k < steps * 0.7 else 1e-4
-        want = (k % 250 == 0) or k == steps - 1
-        loss = den.train_step(feats.ptr + i0 * CW * CW * 16 * 2, targets.ptr + i0 * CW * CW * 12, B, CW, CW, lr=lr,
+        want = (k % 500 == 0) or k == steps - 1
+        loss = den.train_step(feats.ptr + i0 * px * 16 * 2, targets.ptr + i0 * px * 12, B, T, T, lr=lr,
                               want_loss=want, stream=stream)
         if want:
             losses.append((k, loss))
@@ -949,6 +1008,7 @@ def run_denoise_experiment(args, world, rank, local, dist):
     ctx.sync(stream)
     train_ms = ctx.elapsed_ms(ev0, ev1)
     train_s = time.perf_counter() - t1
+    del feats, targets
 
     # ---- evaluation on a held-out scene at 1080p
     W, H = 1920, 1080
@@ -1006,10 +1066,14 @@ def run_denoise_experiment(args, world, rank, local, dist):
     res = {"metric": "GPU ms to RMSE 0.01: CNN denoiser vs plain accumulation", "unit": "ms", "value": td,
            "higher_is_better": False, "target_rmse": target, "plain_ms": tp, "denoiser_ms": td,
            "speedup": tp / td if td > 0 else None, "curve_plain": curve_plain, "curve_denoised": curve_den,
-           "training": {"scenes": S, "crops_per_scene": K, "render": [FW, FH], "crop": CW, "target_spp": TSPP,
-                        "steps": steps, "batch": B,
-                        "gpu_train_ms": train_ms, "wall_train_s": train_s, "data_gen_s": data_s, "loss": losses},
+           "training": {"scenes": S, "window": [T, T], "frustum": [FW, FH], "target_spp": TSPP,
+                        "target_tracer": f"batched, {G} scenes x {COPIES} ray copies per launch, {calls} launches",
+                        "input_to_target_mean_ratio": mean_ratio,
+                        "steps": steps, "batch_tiles": B, "gpu_train_ms": train_ms,
+                        "gpu_ms_per_step": train_ms / max(steps, 1), "wall_train_s": train_s,
+                        "data_gen_s": data_s, "inputs_s": t_inputs, "targets_s": t_targets, "loss": losses},
            "config": {"workload": "heightfield_boxes_1080p_denoiser", "width": W, "height": H,
+                      "light": "constant sky + directional light (shadow ray per vertex)",
                       "reference": "4096 frames of 1-spp plain path tracing", "plain": SET},
            "device_status": ctx.status()}
     print(json.dumps(res))

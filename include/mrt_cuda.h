@@ -408,8 +408,10 @@ int mrt_cuda_batch_trace(mrt_ctx* ctx, mrt_batch* batch, const mrt_ray* rays,
                          void* stream);
 /* Closest-hit Lambertian path trace of the given primary rays over
  * params->max_bounces diffuse bounces: throughput x albedo, sky radiance on
- * escape, a per-ray PCG stream seeded by (ray index, frame), compaction of
- * live paths after every bounce.  radiance: device float RGB per ray.
+ * escape and, with params->estimator = MRT_EST_NEE, a shadow ray toward the
+ * directional light at every vertex (the single-scene tracer's estimator),
+ * a per-ray PCG stream seeded by (ray index, frame), compaction of live
+ * paths after every bounce.  radiance: device float RGB per ray.
  * use_graph != 0: the first call captures the whole bounce loop into a
  * CUDA graph (kept in the batch for these buffers and sizes) and later
  * calls replay it with one launch; make that first call outside any
@@ -417,6 +419,13 @@ int mrt_cuda_batch_trace(mrt_ctx* ctx, mrt_batch* batch, const mrt_ray* rays,
 int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* batch, const mrt_ray* rays,
                              const uint32_t* ray_offsets, const mrt_trace_params* params,
                              uint32_t frame, float* radiance, int use_graph, void* stream);
+/* Running sums over copies of the same rays: acc[g][i] += scale *
+ * sum_c x[g][c][i] for g < groups, c < copies, i < count floats (device
+ * pointers, 16-byte aligned, count a multiple of 4).  With the rays of a
+ * batched path trace laid out [scene][copy][pixel] and scale = 1 / (copies x
+ * calls) this accumulates per-pixel sample means. */
+int mrt_cuda_accumulate_copies(mrt_ctx* ctx, float* acc, const float* x, uint32_t groups,
+                               uint32_t copies, size_t count, float scale, void* stream);
 
 /* ---- learned radiance cache (new: the reference has no learned part) -- */
 /* A multiresolution hash grid over position (16 levels x 2 FP16 features,

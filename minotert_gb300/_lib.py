@@ -221,6 +221,7 @@ def lib() -> C.CDLL:
             "mrt_cuda_batch_destroy": ([vp, vp], i32),
             "mrt_cuda_batch_trace": ([vp, vp, vp, vp, vp, u32, vp], i32),
             "mrt_cuda_batch_pathtrace": ([vp, vp, vp, vp, C.POINTER(TraceParams), u32, vp, i32, vp], i32),
+            "mrt_cuda_accumulate_copies": ([vp, vp, vp, u32, u32, C.c_size_t, C.c_float, vp], i32),
             # host modules
             "mrt_camera_view": ([C.POINTER(Camera_C), C.POINTER(C.c_float)], None),
             "mrt_camera_projection": ([C.POINTER(Camera_C), C.POINTER(C.c_float)], None),

@@ -46,6 +46,7 @@ struct mrt_batch {
     // path-trace state (sized for the largest call so far)
     size_t cap = 0;
     PathRay* q[2] = {nullptr, nullptr};
+    ShadowRay* sq = nullptr;         // shadow rays of one vertex (next-event estimation)
     uint2* hits = nullptr;
     uint32_t* rng = nullptr;
     uint32_t* counters = nullptr;
@@ -60,7 +61,7 @@ struct mrt_batch {
     float* g_radiance = nullptr;
     uint32_t g_n = 0, g_bounces = 0, g_blocks = 0, g_dyn = 0;
     int g_stack = 0;
-    bool g_spread = false;
+    bool g_spread = false, g_nee = false;
     uint32_t g_refill = 0;
 };
 
@@ -225,29 +226,39 @@ __device__ __forceinline__ uint32_t block_append(uint32_t* counter, bool want) {
     return slot;
 }
 
-// Shade vertex `bounce`: escape adds throughput x sky; a hit multiplies the
+// Shade vertex `bounce`: escape adds throughput x sky; a hit (with
+// next-event estimation) emits a shadow ray toward the directional light
+// carrying throughput x albedo x irradiance x cos / pi, multiplies the
 // albedo and, below the bounce limit, appends a cosine-weighted bounce ray
 // (normalize(n + uniform sphere point), random.glsl:10-19 with per-ray PCG
-// numbers) with Russian roulette past rr_start.
+// numbers) with Russian roulette past rr_start: the single-scene
+// wavefront's estimator (shade_vertex) with per-ray random numbers.
+// kNee: compiled per estimator (the escape-only form keeps its registers).
+template <bool kNee>
 __global__ void __launch_bounds__(kShadeBlock)
-k_batch_shade(DevScene sc, const TraceParams* tpp, const PathRay* qin, PathRay* qout, const uint2* hits,
-              uint32_t* rng, float* radiance, uint32_t* counters, uint32_t bounce, uint32_t* status) {
+k_batch_shade(DevScene sc, const TraceParams* tpp, const PathRay* qin, PathRay* qout, ShadowRay* sq,
+              const uint2* hits, uint32_t* rng, float* radiance, uint32_t* counters, uint32_t bounce,
+              uint32_t* status) {
     const TraceParams tp = *tpp;
     const uint32_t n = counters[kCntExt + bounce];
     const uint32_t rounded = (n + kShadeBlock - 1u) / kShadeBlock * kShadeBlock;  // same trip count per block
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < rounded; i += gridDim.x * blockDim.x) {
-        bool want = false;
+        bool want = false, want_sh = false;
         PathRay out;
+        ShadowRay sr;
         if (i < n) {
             const PathRay pr = qin[i];
             const uint2 h = hits[i];
             const uint32_t idx = __float_as_uint(pr.o_pix.w);
             f3 beta{pr.beta.x, pr.beta.y, pr.beta.z};
             if (h.x == kMiss) {
+                // the path's only addition without next-event estimation
+                // (radiance starts at zero); after its shadow rays' otherwise
                 float* r = radiance + 3 * size_t(idx);
-                r[0] = __fmul_rn(beta.x, tp.sky[0]);
-                r[1] = __fmul_rn(beta.y, tp.sky[1]);
-                r[2] = __fmul_rn(beta.z, tp.sky[2]);
+                const f3 e{__fmul_rn(beta.x, tp.sky[0]), __fmul_rn(beta.y, tp.sky[1]), __fmul_rn(beta.z, tp.sky[2])};
+                r[0] = kNee ? __fadd_rn(r[0], e.x) : e.x;
+                r[1] = kNee ? __fadd_rn(r[1], e.y) : e.y;
+                r[2] = kNee ? __fadd_rn(r[2], e.z) : e.z;
             } else if (h.x < sc.mat_count) {
                 const mrt_material m = sc.mats[h.x];
                 const f3 d{pr.d.x, pr.d.y, pr.d.z};
@@ -256,6 +267,19 @@ k_batch_shade(DevScene sc, const TraceParams* tpp, const PathRay* qin, PathRay* 
                 const f3 rho{__fdiv_rn(float(m.albedo_rgba8 & 0xFFu), 255.0f),
                              __fdiv_rn(float((m.albedo_rgba8 >> 8) & 0xFFu), 255.0f),
                              __fdiv_rn(float((m.albedo_rgba8 >> 16) & 0xFFu), 255.0f)};
+                const f3 p = add_rn(f3{pr.o_pix.x, pr.o_pix.y, pr.o_pix.z}, scale_rn(d, __uint_as_float(h.y)));
+                if (kNee) {
+                    const f3 sun{tp.sun[0], tp.sun[1], tp.sun[2]};
+                    const float cosl = dot_rn(nrm, sun);
+                    if (cosl > 0.0f) {
+                        const f3 os = offset_ray(p, nrm);
+                        const f3 c = scale_rn(mul_rn(mul_rn(beta, rho), f3{tp.sun_e[0], tp.sun_e[1], tp.sun_e[2]}),
+                                              __fmul_rn(cosl, kInvPi));
+                        want_sh = true;
+                        sr.o_pix = make_float4(os.x, os.y, os.z, pr.o_pix.w);
+                        sr.contrib = make_float4(c.x, c.y, c.z, pr.d.w);  // w: the scene (bits)
+                    }
+                }
                 beta = mul_rn(beta, rho);
                 if (bounce < tp.max_bounces) {
                     uint32_t s = rng[idx];
@@ -273,7 +297,6 @@ k_batch_shade(DevScene sc, const TraceParams* tpp, const PathRay* qin, PathRay* 
                     }
                     rng[idx] = s;
                     if (live) {
-                        const f3 p = add_rn(f3{pr.o_pix.x, pr.o_pix.y, pr.o_pix.z}, scale_rn(d, __uint_as_float(h.y)));
                         const f3 o = offset_ray(p, nrm);
                         want = true;
                         out.o_pix = make_float4(o.x, o.y, o.z, pr.o_pix.w);
@@ -287,7 +310,51 @@ k_batch_shade(DevScene sc, const TraceParams* tpp, const PathRay* qin, PathRay* 
         }
         const uint32_t slot = block_append(counters + kCntExt + bounce + 1u, want);
         if (want) qout[slot] = out;
+        if (kNee) {
+            const uint32_t ss = block_append(counters + kCntShadow + bounce, want_sh);
+            if (want_sh) sq[ss] = sr;
+        }
     }
+}
+
+// Any-hit trace of the shadow rays of vertex `vertex` (each from its own
+// scene's root toward the directional light); unoccluded rays add their
+// contribution to their path's radiance (one shadow ray per path and
+// vertex, so no two threads add to the same path).
+template <int kStack>
+__global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
+k_batch_trace_shadow(DevScene sc, const uint32_t* roots, const TraceParams* tpp, const ShadowRay* sq,
+                     float* radiance, uint32_t* counters, uint32_t vertex, uint32_t* status, uint32_t refill_min) {
+    __shared__ uint2 stk[kStack * kTraceBlock];
+    const uint32_t n = counters[kCntShadow + vertex];
+    uint32_t* fetch = counters + kCntFetchShadow + vertex;
+    const f3 sun{tpp->sun[0], tpp->sun[1], tpp->sun[2]};
+    uint2* my = stk + threadIdx.x;
+    uint32_t st = 0u, cn = 0u, ct = 0u, ri = 0u;
+    Trav s{};
+    bool have = false, exhausted = false;
+    while (true) {
+        const uint32_t idx = refill(fetch, n, !have, exhausted, refill_min);
+        if (idx != kMiss) {
+            const float4 a = sq[idx].o_pix;
+            trav_init(s, f3{a.x, a.y, a.z}, sun, 0.0f, INFINITY, roots[__float_as_uint(sq[idx].contrib.w)]);
+            ri = idx;
+            have = true;
+        }
+        if (!__any_sync(0xFFFFFFFFu, have)) break;
+        const bool fin = have && trav_step<true, false, kStack>(sc, s, my, kTraceBlock, st, cn, ct);
+        if (have && fin) {
+            if (s.best == kMiss) {
+                const ShadowRay r = sq[ri];
+                float* L = radiance + 3 * size_t(__float_as_uint(r.o_pix.w));
+                L[0] = __fadd_rn(L[0], r.contrib.x);
+                L[1] = __fadd_rn(L[1], r.contrib.y);
+                L[2] = __fadd_rn(L[2], r.contrib.z);
+            }
+            have = false;
+        }
+    }
+    if (st) atomicOr(status, st);
 }
 
 // ray counts of the bounce loop into the context's totals (frame stats)
@@ -299,10 +366,12 @@ __global__ void k_batch_tally(const uint32_t* counters, unsigned long long* tota
 int free_batch_state(mrt_batch* b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
-    cudaFree(b->q[0]); cudaFree(b->q[1]); cudaFree(b->hits); cudaFree(b->rng); cudaFree(b->counters);
+    cudaFree(b->q[0]); cudaFree(b->q[1]); cudaFree(b->sq); cudaFree(b->hits); cudaFree(b->rng);
+    cudaFree(b->counters);
     b->exec = nullptr;
     b->cap_stream = nullptr;
     b->q[0] = b->q[1] = nullptr;
+    b->sq = nullptr;
     b->hits = nullptr;
     b->rng = nullptr;
     b->counters = nullptr;
@@ -328,9 +397,47 @@ int upload_offsets(mrt_ctx* ctx, mrt_batch* b, const uint32_t* ray_offsets, uint
     return MRT_OK;
 }
 
+// acc[g][i] += scale * sum_c x[g][c][i] (g < groups, c < copies, i < count),
+// four floats per thread
+__global__ void k_accumulate_copies(float* acc, const float* x, uint32_t groups, uint32_t copies, size_t count,
+                                    float scale) {
+    const size_t q = count / 4, total = size_t(groups) * q;
+    for (size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x; k < total; k += size_t(gridDim.x) * blockDim.x) {
+        const size_t g = k / q, i = k - g * q;
+        const float4* src = reinterpret_cast<const float4*>(x) + g * copies * q + i;
+        float4 s = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (uint32_t c = 0; c < copies; ++c) {
+            const float4 v = src[size_t(c) * q];
+            s.x += v.x; s.y += v.y; s.z += v.z; s.w += v.w;
+        }
+        float4* d = reinterpret_cast<float4*>(acc) + g * q + i;
+        float4 a = *d;
+        a.x = fmaf(scale, s.x, a.x);
+        a.y = fmaf(scale, s.y, a.y);
+        a.z = fmaf(scale, s.z, a.z);
+        a.w = fmaf(scale, s.w, a.w);
+        *d = a;
+    }
+}
+
 } // namespace
 
 extern "C" {
+
+int mrt_cuda_accumulate_copies(mrt_ctx* ctx, float* acc, const float* x, uint32_t groups, uint32_t copies,
+                               size_t count, float scale, void* stream) {
+    if (!ctx || !acc || !x || groups == 0 || copies == 0 || count % 4 ||
+        (reinterpret_cast<uintptr_t>(acc) | reinterpret_cast<uintptr_t>(x)) % 16)
+        return set_error(ctx, MRT_EINVAL, "accumulate_copies: bad arguments");
+    cudaSetDevice(ctx->device);
+    const size_t total = size_t(groups) * (count / 4);
+    const int blocks = int(std::min<size_t>((total + 255) / 256, size_t(ctx->sm_count) * 16));
+    k_accumulate_copies<<<std::max(blocks, 1), 256, 0, static_cast<cudaStream_t>(stream)>>>(acc, x, groups, copies,
+                                                                                            count, scale);
+    if (cudaGetLastError() != cudaSuccess) return set_error(ctx, MRT_ECUDA, "accumulate_copies: launch");
+    ctx->launches++;
+    return MRT_OK;
+}
 
 int mrt_cuda_batch_create(mrt_ctx* ctx, uint32_t count, const mrt_bvh8_node* const* nodes,
                           const uint32_t* node_counts, const mrt_tri* const* tris, const uint32_t* tri_counts,
@@ -471,6 +578,7 @@ int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, co
         free_batch_state(b);
         bool ok = cudaMalloc(&b->q[0], n * sizeof(PathRay)) == cudaSuccess &&
                   cudaMalloc(&b->q[1], n * sizeof(PathRay)) == cudaSuccess &&
+                  cudaMalloc(&b->sq, n * sizeof(ShadowRay)) == cudaSuccess &&
                   cudaMalloc(&b->hits, n * sizeof(uint2)) == cudaSuccess &&
                   cudaMalloc(&b->rng, n * sizeof(uint32_t)) == cudaSuccess &&
                   cudaMalloc(&b->counters, kCntSlots * sizeof(uint32_t)) == cudaSuccess;
@@ -495,6 +603,7 @@ int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, co
     const uint32_t bounces = params->max_bounces;
     const bool spread = (ctx->tuning.tri_spread & 1u) != 0u;
     const uint32_t rmin = ctx->tuning.refill_min ? ctx->tuning.refill_min : 1u;
+    const bool nee = params->estimator == MRT_EST_NEE;
     const int sblocks = int(std::min<size_t>((n + kShadeBlock - 1) / kShadeBlock, 8192));
     auto enqueue = [&](cudaStream_t st) -> bool {
         if (cudaMemsetAsync(b->counters, 0, kCntSlots * sizeof(uint32_t), st) != cudaSuccess) return false;
@@ -508,9 +617,23 @@ int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, co
             else if (stack == 32) { if (spread) MRT_BQ(32, true); else MRT_BQ(32, false); }
             else { if (spread) MRT_BQ(24, true); else MRT_BQ(24, false); }
 #undef MRT_BQ
-            k_batch_shade<<<sblocks, kShadeBlock, 0, st>>>(b->dev, b->d_tp, b->q[v & 1u], b->q[(v + 1u) & 1u],
-                                                           b->hits, b->rng, radiance, b->counters, v,
-                                                           ctx->d_status);
+            if (nee)
+                k_batch_shade<true><<<sblocks, kShadeBlock, 0, st>>>(b->dev, b->d_tp, b->q[v & 1u],
+                                                                     b->q[(v + 1u) & 1u], b->sq, b->hits, b->rng,
+                                                                     radiance, b->counters, v, ctx->d_status);
+            else
+                k_batch_shade<false><<<sblocks, kShadeBlock, 0, st>>>(b->dev, b->d_tp, b->q[v & 1u],
+                                                                      b->q[(v + 1u) & 1u], b->sq, b->hits, b->rng,
+                                                                      radiance, b->counters, v, ctx->d_status);
+            if (nee) {
+#define MRT_BS(S)                                                                                          \
+    k_batch_trace_shadow<S><<<blocks, kTraceBlock, 0, st>>>(b->dev, b->d_roots, b->d_tp, b->sq, radiance, \
+                                                            b->counters, v, ctx->d_status, rmin)
+                if (stack == 16) MRT_BS(16);
+                else if (stack == 32) MRT_BS(32);
+                else MRT_BS(24);
+#undef MRT_BS
+            }
         }
         k_batch_tally<<<1, 32, 0, st>>>(b->counters, ctx->d_totals, bounces);
         return cudaGetLastError() == cudaSuccess;
@@ -518,12 +641,12 @@ int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, co
     ctx->acc.primary_rays += n;
     if (!use_graph) {
         if (!enqueue(s)) return set_error(ctx, MRT_ECUDA, "batch_pathtrace: launch failed");
-        ctx->launches += 2 + 2 * (bounces + 1);
+        ctx->launches += 2 + (nee ? 3 : 2) * (bounces + 1);
         return MRT_OK;
     }
     const bool same = b->exec && b->g_rays == rays && b->g_radiance == radiance && b->g_n == n &&
                       b->g_bounces == bounces && b->g_blocks == uint32_t(blocks) && b->g_stack == stack &&
-                      b->g_spread == spread && b->g_refill == rmin;
+                      b->g_spread == spread && b->g_refill == rmin && b->g_nee == nee;
     if (!same) {
         if (b->exec) cudaGraphExecDestroy(b->exec);
         b->exec = nullptr;
@@ -553,9 +676,10 @@ int mrt_cuda_batch_pathtrace(mrt_ctx* ctx, mrt_batch* b, const mrt_ray* rays, co
         b->g_stack = stack;
         b->g_spread = spread;
         b->g_refill = rmin;
+        b->g_nee = nee;
     }
     if (cudaGraphLaunch(b->exec, s) != cudaSuccess) return set_error(ctx, MRT_ECUDA, "batch_pathtrace: graph launch");
-    ctx->launches += 2 + 2 * (bounces + 1);
+    ctx->launches += 2 + (nee ? 3 : 2) * (bounces + 1);
     return MRT_OK;
 }
 

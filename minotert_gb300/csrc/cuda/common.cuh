@@ -93,6 +93,8 @@ MRT_DEV float offset_axis(float p, float n) {
     float pi = __int_as_float(__float_as_int(p) + (p < 0.0f ? -of : of));
     return fabsf(p) < kOrigin ? fmaf(kFloatScale, n, p) : pi;
 }
+constexpr float kInvPi = 0.318309886183790671538f;  // 1 / pi, Lambertian BRDF normalisation
+
 MRT_DEV f3 offset_ray(f3 p, f3 n) { return f3{offset_axis(p.x, n.x), offset_axis(p.y, n.y), offset_axis(p.z, n.z)}; }
 
 // e^x reproducible bit for bit on the CPU: Cody-Waite reduction

@@ -17,8 +17,6 @@
 
 namespace mrt {
 
-constexpr float kInvPi = 0.318309886183790671538f;
-
 
 // g-buffer extras: depth = (P V hit).z / w as R16F, normal RGBA16F (the ray
 // direction on a miss), motion = (proj - prev proj).xy / pitch as RG16F

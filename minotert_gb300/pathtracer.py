@@ -38,6 +38,11 @@ class Camera:
     position: tuple
     yaw: float
     pitch: float
+    # (x0, y0, width, height): render only this pixel window of the
+    # viewport's frustum (an off-centre projection: pixel (x, y) of the
+    # window sees what pixel (x0 + x, y0 + y) of the full viewport sees).
+    # New; the reference always renders the whole viewport.
+    window: tuple | None = None
 
     def direction(self) -> np.ndarray:
         cp, sp = math.cos(self.pitch), math.sin(self.pitch)
@@ -70,11 +75,61 @@ class Camera:
 
 
 def camera_consts(camera: Camera, prev: Camera | None = None, frame_counter: int = 0) -> CameraConsts:
-    """The per-dispatch constants of pathtracer.ixx:86-105 / 171-184."""
+    """The per-dispatch constants of pathtracer.ixx:86-105 / 171-184; with a
+    camera window, the projection narrowed to that window."""
     out = CameraConsts()
     pc = (prev or camera)._c()
     lib().mrt_camera_consts_make(C.byref(camera._c()), C.byref(pc), frame_counter, C.byref(out))
+    if camera.window is not None:
+        window_projection(out, camera.viewport, camera.window)
     return out
+
+
+def window_projection(consts: CameraConsts, viewport, window) -> None:
+    """Narrow the projection of `consts` (made for the full `viewport`) to
+    the pixel window (x0, y0, w, h), in place.  The kernels map pixel (x, y)
+    of a w x h image to NDC (2 (x + 0.5) / w - 1, 1 - 2 (y + 0.5) / h); the
+    full viewport's NDC of pixel (x0 + x, y0 + y) is the affine map
+    ndc_full = a * ndc_window + b per axis with a = (w / W, h / H),
+    b = ((w + 2 x0) / W - 1, 1 - (2 y0 + h) / H).  So the window's inverse
+    projection is inv_projection * T (T: that map on x and y, identity on z
+    and w) and its projection T^-1 * projection (depth is unchanged)."""
+    W, H = float(viewport[0]), float(viewport[1])
+    x0, y0, w, h = (float(v) for v in window)
+    ax, ay = w / W, h / H
+    bx, by = (w + 2.0 * x0) / W - 1.0, 1.0 - (2.0 * y0 + h) / H
+    # column-major 4x4 (m[col * 4 + row])
+    P = np.array(consts.projection[:], np.float64).reshape(4, 4).T
+    Pi = np.array(consts.inv_projection[:], np.float64).reshape(4, 4).T
+    T = np.array([[ax, 0, 0, bx], [0, ay, 0, by], [0, 0, 1, 0], [0, 0, 0, 1]], np.float64)
+    Pw = np.linalg.inv(T) @ P
+    Piw = Pi @ T
+    consts.projection[:] = [float(v) for v in Pw.T.reshape(-1).astype(np.float32)]
+    consts.inv_projection[:] = [float(v) for v in Piw.T.reshape(-1).astype(np.float32)]
+
+
+def primary_rays_host(camera: Camera, width: int, height: int) -> np.ndarray:
+    """The pinhole rays primaryRays traces (primaryRay.comp:46-51), for a
+    width x height image of `camera` (or of its window), computed on the host
+    in FP64 and stored as RAY_DTYPE (tmin 0, tmax inf): the primary rays of
+    a batched path trace that is to see what primaryRays sees."""
+    from ._lib import RAY_DTYPE
+    c = camera_consts(camera)
+    iv = np.array(c.inv_view[:], np.float64).reshape(4, 4).T
+    ip = np.array(c.inv_projection[:], np.float64).reshape(4, 4).T
+    xs = (np.arange(width, dtype=np.float64) + 0.5) / width * 2.0 - 1.0
+    ys = (1.0 - (np.arange(height, dtype=np.float64) + 0.5) / height) * 2.0 - 1.0
+    ndc = np.stack(np.broadcast_arrays(xs[None, :], ys[:, None], 1.0, 1.0), -1).reshape(-1, 4)
+    vd = ndc @ ip.T
+    vd[:, 3] = 0.0
+    wd = (vd @ iv.T)[:, :3]
+    wd /= np.linalg.norm(wd, axis=1, keepdims=True)
+    rays = np.zeros(width * height, RAY_DTYPE)
+    rays["org"] = (iv @ np.array([0.0, 0.0, 0.0, 1.0]))[:3].astype(np.float32)
+    rays["dir"] = wd.astype(np.float32)
+    rays["tmin"] = 0.0
+    rays["tmax"] = np.inf
+    return rays
 
 
 @dataclass

@@ -133,6 +133,14 @@ def blue_noise(seed: int = 1, size: int = 64) -> np.ndarray:
     return out
 
 
+def accumulate_copies(ctx: Context, acc, x, groups: int, copies: int, count: int, scale: float, stream=None):
+    """acc[g][i] += scale * sum_c x[g][c][i] on the device (float32 buffers,
+    count a multiple of 4): per-pixel sample means of ray copies laid out
+    [scene][copy][pixel]."""
+    ctx.check(lib().mrt_cuda_accumulate_copies(ctx.handle, ptr(acc), ptr(x), groups, copies, count, float(scale),
+                                               ptr(stream)), "accumulate_copies")
+
+
 class DeviceBatch:
     """Many scenes concatenated into one device BVH (mrt_batch): rays of all
     scenes trace in one persistent launch.  Hit ids are batch-wide:
@@ -173,6 +181,10 @@ class DeviceBatch:
         self.ctx.check(lib().mrt_cuda_batch_pathtrace(self.ctx.handle, self._h, ptr(rays), ptr(off),
                                                       C.byref(params), frame, ptr(radiance), int(use_graph),
                                                       ptr(stream)), "batch_pathtrace")
+
+    def accumulate(self, acc, radiance, groups: int, copies: int, count: int, scale: float, stream=None):
+        """acc[g][i] += scale * sum_c radiance[g][c][i] (mrt_cuda_accumulate_copies)."""
+        accumulate_copies(self.ctx, acc, radiance, groups, copies, count, scale, stream)
 
     def close(self):
         if self._h and self.ctx.handle:
