@@ -1335,6 +1335,53 @@ def run_network_kernels(args, world, rank, local, dist):
                       "steps": args.steps, "warmup": args.warmup, "data": "random weights and inputs"}))
 
 
+def run_denoiser_train(args, world, rank, local, dist):
+    """One training step of the CNN denoiser at the training set's batch (4
+    tiles of 256 x 256, random weights, inputs and targets): forward,
+    L1 loss, backward and Adam, on the tensor-core kernels (default) and on
+    the FP32 CUDA-core backward for comparison.  CUDA events over --steps
+    steps after --warmup.  The training-step launch list profiles this
+    command."""
+    from minotert_gb300 import build as _build
+    _build.build()
+    from minotert_gb300._lib import Context
+    from minotert_gb300.denoiser import TOPOLOGY, Denoiser, to_bf16_bits
+
+    ctx = Context(local)
+    stream = ctx.stream()
+    n, h, w = 4, 256, 256
+    rng = np.random.default_rng(1)
+    x = np.zeros((n, h, w, 16), np.float32)
+    x[..., :10] = rng.uniform(0, 1, (n, h, w, 10))
+    t = rng.uniform(0, 2, (n, h, w, 3)).astype(np.float32)
+    d_x, d_t = ctx.to_device(to_bf16_bits(x)), ctx.to_device(t)
+    px = n * h * w
+    # forward, data gradients (every layer but the first) and weight
+    # gradients: 2 x MACs each
+    macs = [9 * (ca + cb) * co * px // (4 ** sc) for ca, cb, co, ups, relu, sc in TOPOLOGY]
+    flop = 2 * (2 * sum(macs) + sum(macs[1:]))
+    out = {}
+    for mode, name in ((2, "tcgen05"), (1, "fp32_backward")):
+        den = Denoiser(ctx, seed=3)
+        den.set_tcgen05(mode)
+        steps = args.steps if mode == 2 else max(1, min(args.steps, 5))
+        for _ in range(max(args.warmup, 1)):
+            den.train_step(d_x, d_t, n, w, h, lr=1e-4, stream=stream)
+        ctx.sync(stream)
+        a, b = ctx.event(), ctx.event()
+        ctx.record(a, stream)
+        for _ in range(steps):
+            den.train_step(d_x, d_t, n, w, h, lr=1e-4, stream=stream)
+        ctx.record(b, stream)
+        ctx.sync(stream)
+        out[name] = ctx.elapsed_ms(a, b) / steps
+        den.close()
+    print(json.dumps({"metric": "denoiser training step ms (4 x 256 x 256)", "unit": "ms", "value": out["tcgen05"],
+                      "higher_is_better": False, "tflops": flop / out["tcgen05"] / 1e9, "gflop_per_step": flop / 1e9,
+                      "fp32_backward_ms": out["fp32_backward"], "steps": args.steps, "warmup": args.warmup,
+                      "data": "random weights, inputs and targets", "device_status": ctx.status()}))
+
+
 def run_post_kernels(args, world, rank, local, dist):
     """Per-frame cost at 1920x1080 of the passes around the path tracer:
     atmosphere + sky-view LUTs, the sky miss shader on 2,073,600
@@ -1435,7 +1482,7 @@ def main(argv=None):
     ap.add_argument("--no-sub-records", action="store_true",
                     help="headline workload only (no heightfield_boxes_256 / batched64 sub-records)")
     ap.add_argument("--workload", choices=["icospheres_1080p", "heightfield_boxes_256", "batched64",
-                                           "radiance_cache", "denoiser", "network_kernels", "post_kernels",
+                                           "radiance_cache", "denoiser", "denoiser_train", "network_kernels", "post_kernels",
                                            "reference_spheres_1080p"],
                     default="icospheres_1080p")
     args = ap.parse_args(argv)
@@ -1453,6 +1500,8 @@ def main(argv=None):
         run_denoise_experiment(args, world, rank, local, dist)
     elif args.workload == "network_kernels":
         run_network_kernels(args, world, rank, local, dist)
+    elif args.workload == "denoiser_train":
+        run_denoiser_train(args, world, rank, local, dist)
     elif args.workload == "post_kernels":
         run_post_kernels(args, world, rank, local, dist)
     else:

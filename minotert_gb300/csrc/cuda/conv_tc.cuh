@@ -827,3 +827,435 @@ cudaError_t launch_conv_tc(const ConvArgs& ca, uint32_t* status, cudaStream_t s)
     k_conv_tc<COUT, kRows, kStages><<<blocks, 128, smem, s>>>(ca, status);
     return cudaGetLastError();
 }
+
+// ---- phase-decomposed form of the decoder's upsampling layers -------------
+//
+// Layers d1a / d0a read [nearest-2x-upsampled source A ++ skip source B].
+// An output pixel (2Y + py, 2X + px) sees, through the 3x3 window over the
+// upsampled A, only the 2 x 2 low-resolution pixels (Y + py - 1 + ry,
+// X + px - 1 + rx), ry, rx in {0, 1}, with merged weights
+//   W_{py,px}[ry][rx] = sum_{ky in S(py,ry)} sum_{kx in S(px,rx)} W[ky][kx],
+// S(0,0) = {0}, S(0,1) = {1,2}, S(1,0) = {0,1}, S(1,1) = {2}: four 2x2
+// convolutions on the low-resolution source instead of one 3x3 on four
+// copies of each of its pixels (4/9 of the MMAs for A's channels), and the
+// halo of A comes with tensor copies at its own resolution instead of a
+// gather.  A tile is R low-resolution rows x 126 low-resolution columns,
+// i.e. 2R output rows x 252 output columns in four phases (py, px); each
+// phase's accumulator holds 128 lanes = output pixels (2(X0 + i) + px) of
+// one output row (lanes 126, 127 compute beyond the tile and are not
+// stored).  Accumulator blocks are laid out [row r][py][px] x COUT columns,
+// so the two phases px of a row are adjacent and one MMA with N = 2 COUT
+// serves both where they read the same shifted A operand: per (r, py, ry)
+// the column shift s = px + rx takes the values 0 (px 0), 1 (px 0 with
+// rx 1, px 1 with rx 0) and 2 (px 1): three MMAs of N = COUT, 2 COUT, COUT.
+// The skip source B at full resolution is gathered with cp.async into two
+// planes per row, even and odd pixels (entry e of parity q = pixel
+// 2(X0 - 1 + e) + q), so that a phase's tap reads consecutive entries; per
+// (r, py, ky) the taps of both phases read four distinct (parity, shift)
+// operands: (1,0) px0 kx0; (0,1) px0 kx1 + px1 kx0; (1,1) px0 kx2 +
+// px1 kx1; (0,2) px1 kx2 — four MMAs of N = COUT, 2 COUT, 2 COUT, COUT with
+// the unmerged tap weights.  Weights per 16-channel slice come from a copy
+// laid out per MMA in that order (k_up_weights; [half][N rows][8]).  Roles,
+// waits and abort handling are those of k_conv_ws with the gathered slices
+// now the skip source's.
+constexpr int kUpCols = 126;  // low-resolution columns of a tile
+template <int COUT>
+__host__ __device__ constexpr uint32_t up_wbytes_a() { return uint32_t(16 * COUT * 32); }  // 4 x (1+2+1) x COUT rows
+template <int COUT>
+__host__ __device__ constexpr uint32_t up_wbytes_b() { return uint32_t(18 * COUT * 32); }  // 3 x (1+2+2+1) x COUT rows
+template <int R>
+__host__ __device__ constexpr uint32_t up_half_a() { return (uint32_t((R + 2) * kTcPlane) + 127u) & ~127u; }
+template <int R>
+__host__ __device__ constexpr uint32_t up_half_b() { return uint32_t((2 * R + 2) * 2 * kTcPlane); }
+template <int COUT, int R>
+__host__ __device__ constexpr uint32_t up_stage_bytes() {
+    const uint32_t a = 2u * up_half_a<R>() + up_wbytes_a<COUT>();
+    const uint32_t b = 2u * up_half_b<R>() + up_wbytes_b<COUT>();
+    return ((a > b ? a : b) + 127u) & ~127u;
+}
+template <int COUT, int R, int STAGES>
+__host__ __device__ constexpr size_t up_smem_bytes() {
+    return size_t(STAGES) * up_stage_bytes<COUT, R>() + size_t(2 * STAGES + 5) * 8 + 32;
+}
+// weight rows (in COUT units) before each MMA's block of a slice
+__host__ __device__ constexpr int up_pre_a(int s) { return s == 0 ? 0 : (s == 1 ? 1 : 3); }   // s = 0, 1, 2
+__host__ __device__ constexpr int up_pre_b(int g) { return g == 0 ? 0 : (g == 1 ? 1 : (g == 2 ? 3 : 5)); }
+
+// Per-slice weights of the phase-decomposed form for one layer: slice k of
+// the virtual input (A's channels first) at wup + k * (up_wbytes_b / 2)
+// elements.  A slice: blocks (py, ry, s) in that order, each [half][N][8]
+// with N = COUT x (1, 2, 1) rows for s = 0, 1, 2 (s = 1: the px = 0 rows,
+// then px = 1), merged over the taps of S(py, ry) x S(px, rx) in FP32 and
+// rounded to BF16.  B slice: blocks (ky, g), g = 0..3 as in the kernel, rows
+// the members' unmerged taps.
+__global__ void k_up_weights(const bf16* w16, bf16* wup, int ca, int cb, int cout) {
+    const int cin = ca + cb, nk = cin / 16, nka = ca / 16;
+    const size_t slice = size_t(18) * cout * 16;  // elements of the larger (B) slice layout
+    const size_t total = size_t(nk) * slice;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+        const int k = int(i / slice);
+        int rem = int(i % slice);
+        const int c0 = 16 * k;
+        if (k < nka) {
+            if (rem >= 16 * cout * 16) continue;  // an A slice uses 16 COUT rows
+            const int blk_rows = 4 * cout;         // rows of one (py, ry) group: s = 0, 1, 2
+            const int grp = rem / (blk_rows * 16);
+            rem %= blk_rows * 16;
+            const int py = grp >> 1, ry = grp & 1;
+            int s = 0, base = 0, nrows = cout;
+            if (rem >= 1 * cout * 16 && rem < 3 * cout * 16) { s = 1; base = cout * 16; nrows = 2 * cout; }
+            else if (rem >= 3 * cout * 16) { s = 2; base = 3 * cout * 16; nrows = cout; }
+            const int e = rem - base;             // [half][nrows][8]
+            const int hf = e / (nrows * 8), row = (e / 8) % nrows, ci = c0 + 8 * hf + (e % 8);
+            const int px = s == 1 ? row / cout : s / 2, co = row % cout, rx = s - px;
+            const int ky0 = py == 0 ? (ry == 0 ? 0 : 1) : (ry == 0 ? 0 : 2);
+            const int ky1 = py == 0 ? (ry == 0 ? 0 : 2) : (ry == 0 ? 1 : 2);
+            const int kx0 = px == 0 ? (rx == 0 ? 0 : 1) : (rx == 0 ? 0 : 2);
+            const int kx1 = px == 0 ? (rx == 0 ? 0 : 2) : (rx == 0 ? 1 : 2);
+            float acc = 0.0f;
+            for (int ky = ky0; ky <= ky1; ++ky)
+                for (int kx = kx0; kx <= kx1; ++kx)
+                    acc += __bfloat162float(w16[(size_t(co) * 9 + ky * 3 + kx) * cin + ci]);
+            wup[i] = __float2bfloat16_rn(acc);
+        } else {
+            const int blk_rows = 6 * cout;         // rows of one ky group: g = 0..3
+            const int ky = rem / (blk_rows * 16);
+            rem %= blk_rows * 16;
+            int g, base, nrows;
+            if (rem < cout * 16) { g = 0; base = 0; nrows = cout; }
+            else if (rem < 3 * cout * 16) { g = 1; base = cout * 16; nrows = 2 * cout; }
+            else if (rem < 5 * cout * 16) { g = 2; base = 3 * cout * 16; nrows = 2 * cout; }
+            else { g = 3; base = 5 * cout * 16; nrows = cout; }
+            const int e = rem - base;
+            const int hf = e / (nrows * 8), row = (e / 8) % nrows, ci = c0 + 8 * hf + (e % 8);
+            const int j = row / cout, co = row % cout;
+            // members in px order: g0 (px0 kx0); g1 (px0 kx1, px1 kx0); g2 (px0 kx2, px1 kx1); g3 (px1 kx2)
+            const int kx = g == 0 ? 0 : (g == 3 ? 2 : (g == 1 ? (j == 0 ? 1 : 0) : (j == 0 ? 2 : 1)));
+            wup[i] = w16[(size_t(co) * 9 + ky * 3 + kx) * cin + ci];
+        }
+    }
+}
+
+// Epilogue of the phase-decomposed form: warp w reads TMEM lanes
+// 32w..32w+31 (low-resolution column X0 + i, i = 32w + lane), the 4R
+// accumulator blocks [r][py][px], adds the bias, applies ReLU and stores
+// output pixel (2(Y0 + r) + py, 2(X0 + i) + px) as BF16.
+template <int COUT, int R>
+__device__ __forceinline__ void up_epilogue(const ConvArgs& a, uint32_t taddr, int n, int Y0, int X0, int warp,
+                                            int lane) {
+    const int i = 32 * warp + lane;
+#pragma unroll
+    for (int blk = 0; blk < 4 * R; ++blk) {
+        const int r = blk >> 2, py = (blk >> 1) & 1, px = blk & 1;
+        const int y = 2 * (Y0 + r) + py, x = 2 * (X0 + i) + px;
+        bf16* dst = a.y + ((size_t(n) * a.h + y) * a.w_ + x) * COUT;
+#pragma unroll
+        for (int jj = 0; jj < COUT / 16; ++jj) {
+            uint32_t v[16];
+            const uint32_t ta = taddr + (uint32_t(32 * warp) << 16) + uint32_t(blk * COUT + 16 * jj);
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];\n"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15])
+                : "r"(ta));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (i < kUpCols && x < a.w_ && y < a.h) {
+                uint32_t packed[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    float f0 = __uint_as_float(v[2 * q]) + a.bias[16 * jj + 2 * q];
+                    float f1 = __uint_as_float(v[2 * q + 1]) + a.bias[16 * jj + 2 * q + 1];
+                    if (a.relu) {
+                        f0 = fmaxf(f0, 0.0f);
+                        f1 = fmaxf(f1, 0.0f);
+                    }
+                    const __nv_bfloat162 hv = __floats2bfloat162_rn(f0, f1);
+                    packed[q] = *reinterpret_cast<const uint32_t*>(&hv);
+                }
+                uint4* o = reinterpret_cast<uint4*>(dst + 16 * jj);
+                o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+            }
+        }
+    }
+}
+
+template <int COUT, int R, int STAGES>
+__global__ void __launch_bounds__(ws_threads(true)) k_conv_up(ConvArgs a, const __grid_constant__ CUtensorMap map_a,
+                                                             const bf16* wup, uint32_t* status) {
+    constexpr int kAcc = 4 * R * COUT;  // TMEM columns of one accumulator set
+    constexpr int kCols = 2 * kAcc < 32 ? 32 : 2 * kAcc;
+    static_assert(kCols <= 512 && (kCols & (kCols - 1)) == 0, "tensor memory columns");
+    constexpr uint32_t kHalfA = up_half_a<R>(), kHalfB = up_half_b<R>();
+    constexpr uint32_t kHaloTxA = 2u * uint32_t((R + 2) * kTcPlane);
+    constexpr uint32_t kWA = up_wbytes_a<COUT>(), kWB = up_wbytes_b<COUT>();
+    constexpr uint32_t kStage = up_stage_bytes<COUT, R>();
+    constexpr int kProdWarps = ws_prod_warps(true), kProdThreads = 32 * kProdWarps;
+    constexpr int kMmaWarp = 4 + kProdWarps;
+    extern __shared__ __align__(128) unsigned char tsm[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(tsm + STAGES * kStage);
+    uint64_t* empty = full + STAGES;
+    uint64_t* acc_full = empty + STAGES;    // [2]
+    uint64_t* acc_empty = acc_full + 2;     // [2]
+    uint64_t* fin = acc_empty + 2;
+    uint32_t* slot = reinterpret_cast<uint32_t*>(fin + 1);
+    volatile uint32_t* abort = slot + 1;
+    uint32_t* consumed = slot + 2;
+    volatile uint32_t* prod_go = slot + 3;  // [2]
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int hl = a.h >> 1, wl = a.w_ >> 1;  // low resolution (source A)
+    const int tiles_x = (wl + kUpCols - 1) / kUpCols, rows_per_img = (hl + R - 1) / R;
+    const int tiles = tiles_x * rows_per_img * a.n;
+    const int cin = a.ca + a.cb, nk = cin / 16, nka = a.ca / 16;
+    const uint32_t smem0 = smem_u32(tsm);
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                     "r"(uint32_t(kCols))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(full + s)),
+                         "r"(1u + uint32_t(kProdThreads))
+                         : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(empty + s)) : "memory");
+        }
+        for (int b = 0; b < 2; ++b) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(acc_full + b)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(smem_u32(acc_empty + b)) : "memory");
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(fin)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        *abort = (*reinterpret_cast<volatile uint32_t*>(status) & MRT_STATUS_PIPE_TIMEOUT) != 0u ? 2u : 0u;
+        *consumed = 0u;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = *slot;
+    auto give_up = [&]() {
+        if (*abort == 0u) atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
+        *abort = 1u;
+    };
+
+    int produced = 0;
+    if (warp >= 4 && warp < kMmaWarp) {
+        // producers: A slices by tensor copies (thread 0), skip slices
+        // gathered by all producer threads into even / odd pixel planes
+        const int ptid = tid - 128;
+        int g = 0;
+        for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+            const int tx = tile % tiles_x, rb = tile / tiles_x;
+            const int Y0 = (rb % rows_per_img) * R, n = rb / rows_per_img, X0 = tx * kUpCols;
+            bool stop = false;
+            for (int k = 0; k < nk; ++k, ++g) {
+                const int s = g % STAGES;
+                const uint32_t u = uint32_t(g / STAGES);
+                const uint32_t st = smem0 + uint32_t(s) * kStage, mb = smem_u32(full + s);
+                const bool is_a = k < nka;
+                if (ptid == 0) {
+                    if (!ws_wait(smem_u32(empty + s), (u & 1u) ^ 1u, abort) || (st & 127u) != 0u) give_up();
+                    prod_go[g & 1] = *abort == 0u ? 1u : 0u;
+                }
+                asm volatile("bar.sync 1, %0;" ::"n"(kProdThreads) : "memory");
+                if (prod_go[g & 1] == 0u) { stop = true; break; }
+                if (ptid == 0) {
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb),
+                                 "r"(is_a ? kHaloTxA + kWA : kWB)
+                                 : "memory");
+                    if (is_a) {
+                        tma_load_halo(st, &map_a, 16 * k, X0 - 1, Y0 - 1, n, mb);
+                        tma_load_halo(st + kHalfA, &map_a, 16 * k + 8, X0 - 1, Y0 - 1, n, mb);
+                    }
+                    asm volatile(
+                        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                            st + (is_a ? 2u * kHalfA : 2u * kHalfB)),
+                        "l"(wup + size_t(k) * (kWB / 2)), "r"(is_a ? kWA : kWB), "r"(mb)
+                        : "memory");
+                }
+                if (is_a) {
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mb) : "memory");
+                } else {
+                    // full-resolution rows 2 Y0 - 1 .. 2 Y0 + 2R, pixels 2 (X0 - 1 + e) + q,
+                    // e < 130, channels c .. c + 15 of B (two 16-byte halves)
+                    const int c = 16 * k - a.ca;
+                    for (int i = ptid; i < (2 * R + 2) * kTcHalo * 4; i += kProdThreads) {
+                        const int hf = i & 1, q = (i >> 1) & 1, e = (i >> 2) % kTcHalo, fr = (i >> 2) / kTcHalo;
+                        const int yy = 2 * Y0 - 1 + fr, xx = 2 * (X0 - 1 + e) + q;
+                        const bool in = yy >= 0 && yy < a.h && xx >= 0 && xx < a.w_;
+                        const bf16* src = in ? a.b + ((size_t(n) * a.h + yy) * a.w_ + xx) * a.cb + c + 8 * hf
+                                             : a.b;  // any valid address when zero-filling
+                        cp16(st + uint32_t(hf) * kHalfB + uint32_t((fr * 2 + q) * kTcPlane + e * 16), src, in);
+                    }
+                    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(mb) : "memory");
+                }
+                produced = g + 1;
+            }
+            if (stop) break;
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+    } else if (warp == kMmaWarp) {
+        if (lane == 0 && *abort == 0u) {
+            int g = 0, it = 0;
+            bool ok = true, any = false;
+            // stage-0 descriptors: A-source halo, skip halo, weight blocks of
+            // N = COUT and 2 COUT rows (leading byte offset = one K half)
+            const uint64_t da_a = tc_sdesc(smem0, kHalfA, 128), da_b = tc_sdesc(smem0, kHalfB, 128);
+            const uint64_t dw_a1 = tc_sdesc(smem0 + 2u * kHalfA, COUT * 16, 128);
+            const uint64_t dw_a2 = tc_sdesc(smem0 + 2u * kHalfA, 2 * COUT * 16, 128);
+            const uint64_t dw_b1 = tc_sdesc(smem0 + 2u * kHalfB, COUT * 16, 128);
+            const uint64_t dw_b2 = tc_sdesc(smem0 + 2u * kHalfB, 2 * COUT * 16, 128);
+            for (int tile = blockIdx.x; ok && tile < tiles; tile += gridDim.x, ++it) {
+                const int b = it & 1;
+                const uint32_t ub = uint32_t(it >> 1);
+                if (!ws_wait(smem_u32(acc_empty + b), (ub & 1u) ^ 1u, abort)) { ok = false; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t tacc = taddr + uint32_t(b * kAcc);
+                for (int k = 0; k < nk; ++k, ++g) {
+                    const int s = g % STAGES;
+                    const uint32_t u = uint32_t(g / STAGES);
+                    if (!ws_wait(smem_u32(full + s), u & 1u, abort)) { ok = false; break; }
+                    *consumed = uint32_t(g + 1);
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    // descriptors are the stage-0 bases plus (byte offset / 16):
+                    // only the 14-bit start field changes (no carry: shared
+                    // addresses stay below 2^18)
+                    const uint64_t so = uint64_t((uint32_t(s) * kStage) >> 4);
+                    auto mma = [&](uint32_t col, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+                        asm volatile(
+                            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tacc + col),
+                            "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                            : "memory");
+                    };
+                    if (k < nka) {
+                        const uint64_t a0 = da_a + so, w1 = dw_a1 + so, w2 = dw_a2 + so;
+#pragma unroll
+                        for (int r = 0; r < R; ++r)
+#pragma unroll
+                            for (int py = 0; py < 2; ++py)
+#pragma unroll
+                                for (int ry = 0; ry < 2; ++ry) {
+                                    const uint64_t row = a0 + uint64_t(((r + py + ry) * kTcPlane) >> 4);
+                                    const uint32_t col0 = uint32_t((r * 2 + py) * 2 * COUT);
+                                    const uint64_t wg = uint64_t(((py * 2 + ry) * 4 * COUT * 32) >> 4);
+                                    // s = 1 first: it covers both phases' blocks and
+                                    // starts them on the first slice
+                                    const uint32_t acc1 = (k > 0 || ry > 0) ? 1u : 0u;
+                                    mma(col0, row + 1u, w2 + wg + uint64_t((up_pre_a(1) * COUT * 32) >> 4),
+                                        tc_idesc(kTcPix, 2 * COUT), acc1);
+                                    mma(col0, row, w1 + wg + uint64_t((up_pre_a(0) * COUT * 32) >> 4),
+                                        tc_idesc(kTcPix, COUT), 1u);
+                                    mma(col0 + uint32_t(COUT), row + 2u,
+                                        w1 + wg + uint64_t((up_pre_a(2) * COUT * 32) >> 4), tc_idesc(kTcPix, COUT), 1u);
+                                }
+                    } else {
+                        const uint64_t a0 = da_b + so, w1 = dw_b1 + so, w2 = dw_b2 + so;
+#pragma unroll
+                        for (int r = 0; r < R; ++r)
+#pragma unroll
+                            for (int py = 0; py < 2; ++py)
+#pragma unroll
+                                for (int ky = 0; ky < 3; ++ky) {
+                                    const int fr = 2 * r + py + ky;
+                                    const uint32_t col0 = uint32_t((r * 2 + py) * 2 * COUT);
+                                    const uint64_t wg = uint64_t((ky * 6 * COUT * 32) >> 4);
+                                    // (parity, shift) per group: (1,0) (0,1) (1,1) (0,2)
+#pragma unroll
+                                    for (int gi = 0; gi < 4; ++gi) {
+                                        const int q = (gi == 0 || gi == 2) ? 1 : 0;
+                                        const int o = gi == 0 ? 0 : (gi == 3 ? 2 : 1);
+                                        const bool two = gi == 1 || gi == 2;
+                                        const uint64_t ad = a0 + uint64_t(((fr * 2 + q) * kTcPlane + o * 16) >> 4);
+                                        const uint64_t bd = (two ? w2 : w1) + wg + uint64_t((up_pre_b(gi) * COUT * 32) >> 4);
+                                        mma(col0 + (gi == 3 ? uint32_t(COUT) : 0u), ad, bd,
+                                            tc_idesc(kTcPix, two ? 2 * COUT : COUT), 1u);
+                                    }
+                                }
+                    }
+                    any = true;
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                     smem_u32(empty + s))
+                                 : "memory");
+                }
+                if (!ok) break;
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_u32(acc_full + b))
+                             : "memory");
+            }
+            if (!ok) give_up();
+            if (any) {
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_u32(fin))
+                             : "memory");
+                if (!tc_wait(smem_u32(fin), 0u) && *abort == 0u) {
+                    atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
+                    *abort = 1u;
+                }
+            }
+        }
+    } else {  // epilogue: warps 0-3
+        int it = 0;
+        for (int tile = blockIdx.x; tile < tiles && *abort == 0u; tile += gridDim.x, ++it) {
+            const int tx = tile % tiles_x, rb = tile / tiles_x;
+            const int Y0 = (rb % rows_per_img) * R, n = rb / rows_per_img, X0 = tx * kUpCols;
+            const int b = it & 1;
+            const uint32_t ub = uint32_t(it >> 1);
+            const bool ok = ws_wait(smem_u32(acc_full + b), ub & 1u, abort);
+            if (!__all_sync(0xFFFFFFFFu, ok)) {
+                if (lane == 0) give_up();
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            up_epilogue<COUT, R>(a, taddr + uint32_t(b * kAcc), n, Y0, X0, warp, lane);
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(acc_empty + b)) : "memory");
+        }
+    }
+    __syncthreads();
+    if (tid == 128) {
+        for (int g = int(*consumed); g < produced; ++g)
+            if (!tc_wait(smem_u32(full + g % STAGES), uint32_t(g / STAGES) & 1u)) atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(uint32_t(kCols))
+                     : "memory");
+}
+
+// Shape of the phase-decomposed form per COUT: low-resolution rows per tile
+// (two accumulator sets of 4 R COUT columns within the 512 TMEM columns)
+// and ring stages
+__host__ __device__ constexpr int up_rows(int cout) { return cout >= 64 ? 1 : 2; }
+__host__ __device__ constexpr int up_stages(int cout) { return 2; }
+
+template <int COUT>
+cudaError_t launch_conv_up(const ConvArgs& ca, const bf16* wup, uint32_t* status, int sm_count, cudaStream_t s) {
+    constexpr int kR = up_rows(COUT), kStages = up_stages(COUT);
+    constexpr int kCols = 2 * 4 * kR * COUT;
+    constexpr int kThreads = ws_threads(true);
+    static uint64_t configured = 0;
+    static int per_sm = 0;
+    const size_t smem = up_smem_bytes<COUT, kR, kStages>();
+    cudaError_t e = tc_configure(k_conv_up<COUT, kR, kStages>, smem, configured);
+    if (e != cudaSuccess) return e;
+    if (per_sm == 0) {
+        int occ = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv_up<COUT, kR, kStages>, kThreads, smem);
+        if (e != cudaSuccess) return e;
+        per_sm = std::max(1, std::min(occ, 512 / kCols));
+    }
+    if (!ca.ups || ca.cb <= 0 || (ca.h & 1) || (ca.w_ & 1) || ca.ca % 16 || ca.cb % 16) return cudaErrorInvalidValue;
+    CUtensorMap ma;
+    if (!tma_encode(&ma, ca.a, ca.ca, ca.w_ / 2, ca.h / 2, ca.n, kR)) return cudaErrorInvalidValue;
+    const int tiles = ((ca.w_ / 2 + kUpCols - 1) / kUpCols) * ((ca.h / 2 + kR - 1) / kR) * ca.n;
+    const int blocks = std::max(1, std::min(tiles, sm_count * per_sm));
+    k_conv_up<COUT, kR, kStages><<<blocks, kThreads, smem, s>>>(ca, ma, wup, status);
+    return cudaGetLastError();
+}

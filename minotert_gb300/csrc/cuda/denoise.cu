@@ -480,6 +480,8 @@ struct mrt_denoiser {
     float *w = nullptr, *wm = nullptr, *wv = nullptr, *wg = nullptr;  // weights + biases, FP32
     bf16* w16 = nullptr;
     bf16* wtc = nullptr;          // w16 re-laid out per 16-channel slice for the TMA convolution
+    bf16* wup = nullptr;          // per-slice weights of the phase-decomposed upsampling layers
+    size_t up_off[kLayers] = {};  // their offsets in wup (upsampling layers only)
     // activation tensors (bf16) and their gradients (fp32), sized for n*h*w
     size_t cap_pix = 0, grad_pix = 0;
     bf16* act[kLayers] = {};
@@ -575,9 +577,10 @@ cudaError_t conv(const mrt_denoiser* d, int l, const bf16* a, const bf16* b, int
     ConvArgs ca{a, b, d->w16 + L.w_off, d->w + L.b_off, d->act[l], n, h, w, L.ca, L.cb, L.cout, L.ups, L.relu};
     if (d->tc_mode == 2) {
         const bf16* wt = d->wtc + L.w_off;
-        if (L.ups) {  // the decoder's two upsampling layers
-            if (L.cout == 32) return launch_conv_ws<32, true>(ca, wt, d->status, d->sm_count, s);
-            if (L.cout == 64) return launch_conv_ws<64, true>(ca, wt, d->status, d->sm_count, s);
+        if (L.ups) {  // the decoder's two upsampling layers: phase-decomposed
+            const bf16* wu = d->wup + d->up_off[l];
+            if (L.cout == 32) return launch_conv_up<32>(ca, wu, d->status, d->sm_count, s);
+            if (L.cout == 64) return launch_conv_up<64>(ca, wu, d->status, d->sm_count, s);
         } else {
             switch (L.cout) {
             case 16: return launch_conv_ws<16, false>(ca, wt, d->status, d->sm_count, s);
@@ -614,6 +617,9 @@ cudaError_t conv(const mrt_denoiser* d, int l, const bf16* a, const bf16* b, int
     return cudaGetLastError();
 }
 
+// kernels forward() launches
+int forward_launches(const mrt_denoiser* d) { return 13 + (d->tc_mode != 0 ? 1 : 0) + (d->tc_mode == 2 ? 2 : 0); }
+
 // forward of the whole network over n images of h x w (h, w multiples of 4)
 cudaError_t forward(const mrt_denoiser* d, const bf16* in, int n, int h, int w, cudaStream_t s) {
     cudaError_t e;
@@ -626,6 +632,11 @@ cudaError_t forward(const mrt_denoiser* d, const bf16* in, int n, int h, int w, 
             t.off[l] = d->layers[l].w_off;
         }
         k_tc_weights<<<304, 256, 0, s>>>(d->w16, d->wtc, t);
+        if (d->tc_mode == 2)
+            for (int l = 0; l < kLayers; ++l)
+                if (d->layers[l].ups)
+                    k_up_weights<<<152, 256, 0, s>>>(d->w16 + d->layers[l].w_off, d->wup + d->up_off[l],
+                                                     d->layers[l].ca, d->layers[l].cb, d->layers[l].cout);
     }
     if ((e = conv(d, 0, in, nullptr, n, h, w, s))) return e;
     if ((e = conv(d, 1, d->act[0], nullptr, n, h, w, s))) return e;
@@ -787,10 +798,17 @@ int mrt_cuda_denoiser_create(mrt_ctx* ctx, uint32_t seed, mrt_denoiser** out) {
     }
     d->n_b = wo - d->n_w;
     const size_t total = wo;
+    size_t n_up = 0;
+    for (int l = 0; l < kLayers; ++l)
+        if (d->layers[l].ups) {
+            d->up_off[l] = n_up;
+            n_up += size_t((d->layers[l].ca + d->layers[l].cb) / 16) * 18 * d->layers[l].cout * 16;
+        }
     bool ok = cudaMalloc(&d->w, total * 4) == cudaSuccess && cudaMalloc(&d->wm, total * 4) == cudaSuccess &&
               cudaMalloc(&d->wv, total * 4) == cudaSuccess && cudaMalloc(&d->wg, total * 4) == cudaSuccess &&
               cudaMalloc(&d->w16, d->n_w * 2) == cudaSuccess && cudaMalloc(&d->wtc, d->n_w * 2) == cudaSuccess &&
               cudaMalloc(&d->wbt, d->n_w * 2) == cudaSuccess && cudaMalloc(&d->zeros, 128 * 4) == cudaSuccess &&
+              cudaMalloc(&d->wup, std::max<size_t>(n_up, 1) * 2) == cudaSuccess &&
               cudaMalloc(&d->loss, 4) == cudaSuccess &&
               cudaMallocHost(&d->h_loss, 4) == cudaSuccess;
     if (!ok) {
@@ -840,7 +858,7 @@ int mrt_cuda_denoiser_destroy(mrt_ctx* ctx, mrt_denoiser* d) {
     cudaDeviceSynchronize();
     for (int l = 0; l < kLayers; ++l) { cudaFree(d->act[l]); cudaFree(d->grad[l]); cudaFree(d->gz[l]); }
     void* ps[] = {d->w, d->wm, d->wv, d->wg, d->w16, d->wtc, d->pool0, d->pool1, d->gpool0, d->gpool1, d->gin,
-                  d->loss, d->wbt, d->zeros, d->up8, d->up6, d->skip8, d->skip6, d->gp0, d->gp1};
+                  d->loss, d->wbt, d->zeros, d->up8, d->up6, d->skip8, d->skip6, d->gp0, d->gp1, d->wup};
     for (void* p : ps) cudaFree(p);
     if (d->h_loss) cudaFreeHost(d->h_loss);
     delete d;
@@ -887,7 +905,7 @@ int mrt_cuda_denoiser_infer(mrt_ctx* ctx, mrt_denoiser* d, const uint16_t* featu
     if (forward(d, reinterpret_cast<const bf16*>(features), int(batch), int(height), int(width), s) != cudaSuccess)
         return set_error(ctx, MRT_ECUDA, "denoiser_infer: launch");
     k_decode<<<grid_for(pix), 256, 0, s>>>(d->act[kLayers - 1], reinterpret_cast<const bf16*>(features), pix, out);
-    ctx->launches += 14;
+    ctx->launches += forward_launches(d) + 1;  // + decode
     return MRT_OK;
 }
 
@@ -911,7 +929,7 @@ int mrt_cuda_denoiser_train_step(mrt_ctx* ctx, mrt_denoiser* d, const uint16_t* 
         int launched = 0;
         if (backward_tc(d, in, n, h, w, s, &launched) != cudaSuccess)
             return set_error(ctx, MRT_ECUDA, "denoiser_train: backward");
-        ctx->launches += 15 + launched;  // forward 14, loss 1
+        ctx->launches += forward_launches(d) + 1 + launched;  // + loss
     } else {
         k_l1_loss<<<grid_for(pix), 256, 0, s>>>(d->act[kLayers - 1], in, targets, pix, d->grad[kLayers - 1], nullptr,
                                                d->loss);

@@ -172,36 +172,41 @@ __global__ void __launch_bounds__(160) k_conv_wgrad(WgArgs a, int chunks, int sl
         constexpr uint32_t idesc = tc_idesc(128, NC) | (1u << 15) | (1u << 16);    // A and B MN-major
         constexpr uint32_t idesc_b = tc_idesc(128, 16) | (1u << 15) | (1u << 16);
         bool ok = true;
+        // descriptors of stage 0, segment 0, tap 0: the others differ only in
+        // the start address, so they are these plus the byte offset / 16
+        // (smem addresses stay below 2^18: no carry out of the 14-bit field)
+        const uint64_t a00 = tc_sdesc_mn(smem0, 256u, 128u);
+        const uint64_t b00 = tc_sdesc_mn(smem0 + S::kA, kWgPlane, 128u);
+        const uint64_t od = tc_sdesc_mn(ones_s, 256u, 128u);
         for (int g = 0, r = r0; r < r1; ++r, ++g) {
             const int s = g % kStages;
             const uint32_t u = uint32_t(g / kStages);
             if (!ws_wait(smem_u32(full + s), u & 1u, abort)) { ok = false; break; }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const int segs = segments((r % tiles_x) * kWgPix);
-            const uint32_t st = smem0 + uint32_t(s) * S::kStage;
-            for (int j = 0; j < segs; ++j) {
-                const uint64_t ad = tc_sdesc_mn(st + uint32_t(j * S::kCo8 * 256), 256u, 128u);
+            const uint64_t sd = uint64_t((uint32_t(s) * S::kStage) >> 4);
+            const uint64_t a0 = a00 + sd, b0 = b00 + sd;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                if (j >= segs) break;
+                const uint64_t ad = a0 + uint64_t((j * S::kCo8 * 256) >> 4);
                 const uint32_t acc = (g > 0 || j > 0) ? 1u : 0u;
 #pragma unroll
                 for (int t = 0; t < 9; ++t) {
-                    const int ky = t / 3, kx = t % 3;
-                    const uint64_t bd =
-                        tc_sdesc_mn(st + S::kA + uint32_t(ky) * S::kRow + uint32_t(16 * j + kx) * 16u, kWgPlane, 128u);
+                    const uint64_t bd = b0 + uint64_t(((t / 3) * S::kRow + uint32_t(16 * j + t % 3) * 16u) >> 4);
                     asm volatile(
                         "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
                         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr + uint32_t(t * NC)),
                         "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
                         : "memory");
                 }
-                if (chunk == 0) {
-                    const uint64_t od = tc_sdesc_mn(ones_s, 256u, 128u);
+                if (chunk == 0)
                     asm volatile(
                         "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
                         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
                             taddr + uint32_t(S::kTapCols)),
                         "l"(ad), "l"(od), "r"(idesc_b), "r"(acc)
                         : "memory");
-                }
             }
             mma_any = true;
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(

@@ -137,12 +137,14 @@ def test_denoiser_inference_is_size_and_batch_consistent(ctx):
 def test_denoiser_tcgen05_matches_mma_sync(ctx, shape):
     # the same network on the three forward paths: persistent warp-
     # specialised tcgen05 kernels (mode 2, default), tcgen05 with one CTA
-    # per tile (mode 1) and mma.sync (mode 0).  Modes 2 and 1 issue the same
-    # MMAs in the same order into tensor memory and share the epilogue, so
-    # they agree bit for bit (the persistent CTAs loop over many tiles at
-    # the two larger sizes); against mma.sync only the FP32 summation order
-    # differs, so layer outputs agree to BF16 rounding and the decoded
-    # radiance to ~1 %
+    # per tile (mode 1) and mma.sync (mode 0).  The layers without
+    # upsampling issue the same MMAs in the same order in modes 2 and 1; the
+    # two upsampling layers of mode 2 are phase-decomposed (2 x 2 merged
+    # weights, rounded to BF16), so mode 2 agrees with the others to BF16
+    # rounding, like mma.sync, whose FP32 summation order differs: layer
+    # outputs to BF16 rounding, the decoded radiance to ~1 %.  The shapes
+    # cover partial and multiple 126-column tiles of the phase-decomposed
+    # layers and the persistent CTAs' loops over many tiles
     n, h, w = shape
     d = Denoiser(ctx, seed=7)
     rng = np.random.default_rng(3)
@@ -160,10 +162,10 @@ def test_denoiser_tcgen05_matches_mma_sync(ctx, shape):
     assert ctx.status() == 0
     ws, tile, b = outs
     assert np.isfinite(ws).all()
-    assert np.array_equal(ws.view(np.uint32), tile.view(np.uint32))
-    err = np.abs(ws - b)
-    assert err.max() < 3e-2 * max(1.0, np.abs(b).max()), err.max()
-    assert err.mean() < 2e-3 * max(1.0, np.abs(b).mean())
+    for other in (tile, b):
+        err = np.abs(ws - other)
+        assert err.max() < 3e-2 * max(1.0, np.abs(other).max()), err.max()
+        assert err.mean() < 2e-3 * max(1.0, np.abs(other).mean())
 
 
 @pytest.mark.parametrize("shape", [(2, 16, 16), (1, 36, 200), (8, 128, 128)])
@@ -171,10 +173,10 @@ def test_denoiser_tensor_core_backward_matches_fp32(ctx, shape):
     # one training step's gradients from the tcgen05 backward (mode 2: BF16
     # pre-activation gradients, data gradients as mirrored convolutions,
     # weight and bias gradients as GEMMs over the pixels) against the FP32
-    # CUDA-core backward (mode 1, whose forward issues the same MMAs in the
-    # same order, so both start from the same activations and loss); per
-    # layer, weights and biases separately, so a broken tap, channel chunk
-    # or bias column shows by name.  Shapes: the gradient test's tiny
+    # CUDA-core backward (mode 1, whose forward differs from mode 2's only in
+    # the upsampling layers' BF16 rounding of merged weights); per layer,
+    # weights and biases separately, so a broken tap, channel chunk or bias
+    # column shows by name.  Shapes: the gradient test's tiny
     # images, a width of two 128-pixel segments with a ragged end, and the
     # training batch (8 crops of 128 x 128)
     n, h, w = shape
@@ -189,10 +191,13 @@ def test_denoiser_tensor_core_backward_matches_fp32(ctx, shape):
         d.close()
     assert ctx.status() == 0
     (l_tc, g_tc), (l_fp, g_fp) = res[2], res[1]
-    assert abs(l_tc - l_fp) <= 1e-6 * abs(l_fp), (l_tc, l_fp)
+    assert abs(l_tc - l_fp) <= 1e-3 * abs(l_fp), (l_tc, l_fp)
     assert np.isfinite(g_tc).all()
     ws_tc, bs_tc = cnn.split(g_tc)
     ws_fp, bs_fp = cnn.split(g_fp)
+    # the two forwards differ by the upsampling layers' merged-weight
+    # rounding, which the 512 pixels of the smallest case average least
+    tol = 6e-2 if n * h * w < 4096 else 3e-2
     for l, (a, b) in enumerate(zip(ws_tc + bs_tc, ws_fp + bs_fp)):
         name = f"{'w' if l < len(ws_tc) else 'b'}{l % len(ws_tc)}"
         a, b = a.ravel(), b.ravel()
@@ -201,6 +206,6 @@ def test_denoiser_tensor_core_backward_matches_fp32(ctx, shape):
             assert np.linalg.norm(a) == 0, name
             continue
         rel = np.linalg.norm(a - b) / nb
-        assert rel < 3e-2, (name, rel)
+        assert rel < tol, (name, rel)
     cos = g_tc @ g_fp / (np.linalg.norm(g_tc) * np.linalg.norm(g_fp))
     assert cos > 0.999, cos
