@@ -777,9 +777,10 @@ __global__ void __launch_bounds__(ws_threads(UPS)) k_conv_ws(ConvArgs a, const _
 }
 
 // Shape of the persistent form per COUT: rows per tile (two accumulators of
-// ROWS x COUT columns within the 512 TMEM columns) and ring stages (three
-// keep two CTAs per SM up to COUT 64)
-__host__ __device__ constexpr int ws_rows(int cout) { return cout >= 64 ? 2 : 4; }
+// ROWS x COUT columns within the 512 TMEM columns) and ring stages, from
+// sweeps of the 1080p inference (ms: 2 rows at COUT 64 1.008, 4 rows
+// 0.981; 8 rows below COUT 64 no change)
+__host__ __device__ constexpr int ws_rows(int cout) { return cout >= 128 ? 2 : 4; }
 __host__ __device__ constexpr int ws_stages(int cout) { return cout >= 128 ? 4 : 3; }
 
 template <int COUT, bool UPS>
@@ -1231,9 +1232,10 @@ __global__ void __launch_bounds__(ws_threads(true)) k_conv_up(ConvArgs a, const 
 
 // Shape of the phase-decomposed form per COUT: low-resolution rows per tile
 // (two accumulator sets of 4 R COUT columns within the 512 TMEM columns)
-// and ring stages
+// and ring stages, from sweeps of the 1080p inference (ms with the above:
+// 2 stages 0.981, 3 stages 0.966; one row at COUT 32 0.994)
 __host__ __device__ constexpr int up_rows(int cout) { return cout >= 64 ? 1 : 2; }
-__host__ __device__ constexpr int up_stages(int cout) { return 2; }
+__host__ __device__ constexpr int up_stages(int) { return 3; }
 
 template <int COUT>
 cudaError_t launch_conv_up(const ConvArgs& ca, const bf16* wup, uint32_t* status, int sm_count, cudaStream_t s) {
