@@ -440,6 +440,29 @@ __global__ void k_tc_weights(const bf16* w16, bf16* wt, TcLayerTable t) {
     }
 }
 
+// Weights of the layers with COUT <= 32 for the row-stacked persistent form:
+// per layer [slice of 16 input channels][kx][half][ky = 2, 1, 0][cout][8
+// channels], so one tap column's three taps are one N = 3 COUT operand.
+__global__ void k_tc_weights_stack(const bf16* w16, bf16* wt, TcLayerTable t) {
+    for (int l = 0; l < t.count; ++l) {
+        const int cin = t.cin[l], cout = t.cout[l];
+        if (cout > 32) continue;
+        const size_t total = size_t(9) * cin * cout;
+        for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+            const int e = int(i % 8);
+            size_t q = i / 8;
+            const int row = int(q % (3 * cout));
+            q /= 3 * cout;
+            const int hf = int(q % 2);
+            q /= 2;
+            const int kx = int(q % 3);
+            const int k = int(q / 3);
+            const int ky = 2 - row / cout, co = row % cout;
+            wt[t.off[l] + i] = w16[t.off[l] + (size_t(co) * 9 + ky * 3 + kx) * cin + 16 * k + 8 * hf + e];
+        }
+    }
+}
+
 // Shapes of the TMA form per COUT, from sweeps on the 1080p denoiser (ms per
 // inference, upsampling layers on the cp.async kernel: cp.async everywhere
 // 1.607; TMA with 2 / 4 / 8 rows at COUT 128 / 64 / <= 32 1.341; 2 rows at
@@ -526,9 +549,26 @@ cudaError_t launch_conv_tma(const ConvArgs& ca, const bf16* wt, uint32_t* status
 // bounded and also ends when another role has given up (a shared abort
 // word); the CTA then sets MRT_STATUS_PIPE_TIMEOUT, waits (bounded) for the
 // copies and MMAs it issued and frees its tensor memory.
-template <int COUT, int ROWS, int STAGES>
+// Row-stacked form (STACK, the 16- and 32-channel layers): an MMA costs a
+// fixed ~46 cycles up to N = 64, so instead of one MMA per (output row, tap)
+// with N = COUT, one MMA per (halo row h, tap column kx) feeds the three
+// output rows h - 2, h - 1, h at once: N = 3 COUT with the weights of taps
+// (2, kx), (1, kx), (0, kx) stacked, into accumulator blocks laid out per
+// output row r at columns (r + 2) COUT, r = -2 .. ROWS + 1 (the four outer
+// blocks only collect the edge rows' unused products).  Per slice (ROWS + 2)
+// x 3 MMAs instead of 9 ROWS.  Blocks are written by overlapping MMAs, so a
+// tile's accumulator is first cleared by one MMA of zero operands (N = the
+// whole accumulator) and every real MMA accumulates.
+template <int COUT, int ROWS, bool STACK>
+__host__ __device__ constexpr int ws_acc_cols() { return STACK ? (ROWS + 4) * COUT : ROWS * COUT; }
+template <int COUT, int ROWS, bool STACK>
+__host__ __device__ constexpr uint32_t ws_zero_bytes() {
+    return STACK ? uint32_t(128 * 32 + ws_acc_cols<COUT, ROWS, STACK>() * 32) : 0u;  // A and B zero operands
+}
+template <int COUT, int ROWS, int STAGES, bool STACK = false>
 __host__ __device__ constexpr size_t ws_smem_bytes() {
-    return size_t(STAGES) * tma_stage_bytes<COUT, ROWS>() + size_t(2 * STAGES + 5) * 8 + 32;
+    return size_t(STAGES) * tma_stage_bytes<COUT, ROWS>() + ws_zero_bytes<COUT, ROWS, STACK>() +
+           size_t(2 * STAGES + 5) * 8 + 32;
 }
 
 __device__ __forceinline__ bool ws_wait(uint32_t mbar, uint32_t parity, const volatile uint32_t* abort) {
@@ -551,11 +591,13 @@ __device__ __forceinline__ bool ws_wait(uint32_t mbar, uint32_t parity, const vo
 __host__ __device__ constexpr int ws_prod_warps(bool ups) { return ups ? 4 : 1; }
 __host__ __device__ constexpr int ws_threads(bool ups) { return 32 * (5 + ws_prod_warps(ups)); }
 
-template <int COUT, int ROWS, int STAGES, bool UPS>
+template <int COUT, int ROWS, int STAGES, bool UPS, bool STACK = false>
 __global__ void __launch_bounds__(ws_threads(UPS)) k_conv_ws(ConvArgs a, const __grid_constant__ CUtensorMap map_a,
                                                             const __grid_constant__ CUtensorMap map_b, const bf16* wt,
                                                             uint32_t* status) {
-    constexpr int kAcc = ROWS * COUT;  // TMEM columns of one accumulator
+    static_assert(!(STACK && UPS), "the row-stacked form reads sources at the output's resolution");
+    constexpr int kAcc = ws_acc_cols<COUT, ROWS, STACK>();  // TMEM columns of one accumulator
+    constexpr uint32_t kZero = ws_zero_bytes<COUT, ROWS, STACK>();
     constexpr int kCols = 2 * kAcc < 32 ? 32 : 2 * kAcc;
     static_assert(kCols <= 512 && (kCols & (kCols - 1)) == 0, "tensor memory columns");
     constexpr uint32_t kHalo = tma_halo_bytes<ROWS>(), kHalf = tma_half_bytes<ROWS>();
@@ -565,7 +607,7 @@ __global__ void __launch_bounds__(ws_threads(UPS)) k_conv_ws(ConvArgs a, const _
     constexpr int kProdWarps = ws_prod_warps(UPS), kProdThreads = 32 * kProdWarps;
     constexpr int kMmaWarp = 4 + kProdWarps;
     extern __shared__ __align__(128) unsigned char tsm[];
-    uint64_t* full = reinterpret_cast<uint64_t*>(tsm + STAGES * kStage);
+    uint64_t* full = reinterpret_cast<uint64_t*>(tsm + STAGES * kStage + kZero);
     uint64_t* empty = full + STAGES;
     uint64_t* acc_full = empty + STAGES;    // [2]
     uint64_t* acc_empty = acc_full + 2;     // [2]
@@ -605,6 +647,11 @@ __global__ void __launch_bounds__(ws_threads(UPS)) k_conv_ws(ConvArgs a, const _
         // remaining CTAs skip their work
         *abort = (*reinterpret_cast<volatile uint32_t*>(status) & MRT_STATUS_PIPE_TIMEOUT) != 0u ? 2u : 0u;
         *consumed = 0u;
+    }
+    if (STACK) {  // the zero operands of the accumulator-clearing MMA
+        for (uint32_t i = tid; i < kZero / 16u; i += blockDim.x)
+            reinterpret_cast<uint4*>(tsm + STAGES * kStage)[i] = make_uint4(0u, 0u, 0u, 0u);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -699,6 +746,14 @@ __global__ void __launch_bounds__(ws_threads(UPS)) k_conv_ws(ConvArgs a, const _
                 if (!ws_wait(smem_u32(acc_empty + b), (ub & 1u) ^ 1u, abort)) { ok = false; break; }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t tacc = taddr + uint32_t(b * kAcc);
+                if (STACK) {  // clear the accumulator: zero A (128 x 16) times zero B (kAcc x 16)
+                    const uint32_t za = smem0 + uint32_t(STAGES) * kStage;
+                    asm volatile(
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, 0;\n" ::"r"(tacc),
+                        "l"(tc_sdesc(za, 128 * 16, 128)), "l"(tc_sdesc(za + 128 * 32, kAcc * 16, 128)),
+                        "r"(tc_idesc(kTcPix, kAcc))
+                        : "memory");
+                }
                 for (int k = 0; k < nk; ++k, ++g) {
                     const int s = g % STAGES;
                     const uint32_t u = uint32_t(g / STAGES);
@@ -706,21 +761,40 @@ __global__ void __launch_bounds__(ws_threads(UPS)) k_conv_ws(ConvArgs a, const _
                     *consumed = uint32_t(g + 1);
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint32_t abase = smem0 + uint32_t(s) * kStage, bbase = abase + kHalo;
+                    if (STACK) {
+                        // halo row h, tap column kx -> output rows h - 2 .. h
+                        // (accumulator blocks h .. h + 2), weights of taps
+                        // (2, kx), (1, kx), (0, kx) stacked along N
+                        constexpr uint32_t idesc3 = tc_idesc(kTcPix, 3 * COUT);
 #pragma unroll
-                    for (int r = 0; r < ROWS; ++r)
+                        for (int hrow = 0; hrow < ROWS + 2; ++hrow)
 #pragma unroll
-                        for (int t = 0; t < 9; ++t) {
-                            const int ky = t / 3, kx = t % 3;
-                            const uint64_t ad = tc_sdesc(abase + (r + ky) * kTcPlane + kx * 16, kHalf, 128);
-                            const uint64_t bd = tc_sdesc(bbase + (t * 2) * COUT * 16, COUT * 16, 128);
-                            const uint32_t acc = (k > 0 || t > 0) ? 1u : 0u;
-                            asm volatile(
-                                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-                                    tacc + uint32_t(r * COUT)),
-                                "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-                                : "memory");
-                        }
+                            for (int kx = 0; kx < 3; ++kx) {
+                                const uint64_t ad = tc_sdesc(abase + hrow * kTcPlane + kx * 16, kHalf, 128);
+                                const uint64_t bd = tc_sdesc(bbase + kx * 2 * 3 * COUT * 16, 3 * COUT * 16, 128);
+                                asm volatile(
+                                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, 1;\n" ::"r"(
+                                        tacc + uint32_t(hrow * COUT)),
+                                    "l"(ad), "l"(bd), "r"(idesc3)
+                                    : "memory");
+                            }
+                    } else {
+#pragma unroll
+                        for (int r = 0; r < ROWS; ++r)
+#pragma unroll
+                            for (int t = 0; t < 9; ++t) {
+                                const int ky = t / 3, kx = t % 3;
+                                const uint64_t ad = tc_sdesc(abase + (r + ky) * kTcPlane + kx * 16, kHalf, 128);
+                                const uint64_t bd = tc_sdesc(bbase + (t * 2) * COUT * 16, COUT * 16, 128);
+                                const uint32_t acc = (k > 0 || t > 0) ? 1u : 0u;
+                                asm volatile(
+                                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+                                        tacc + uint32_t(r * COUT)),
+                                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                                    : "memory");
+                            }
+                    }
                     any = true;
                     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                                      smem_u32(empty + s))
@@ -756,7 +830,8 @@ __global__ void __launch_bounds__(ws_threads(UPS)) k_conv_ws(ConvArgs a, const _
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            tc_epilogue<COUT, ROWS>(a, taddr + uint32_t(b * kAcc), n, y0, x0, warp, lane);
+            // (row-stacked: output row r is accumulator block r + 2)
+            tc_epilogue<COUT, ROWS>(a, taddr + uint32_t(b * kAcc + (STACK ? 2 * COUT : 0)), n, y0, x0, warp, lane);
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
             if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(acc_empty + b)) : "memory");
@@ -783,19 +858,23 @@ __global__ void __launch_bounds__(ws_threads(UPS)) k_conv_ws(ConvArgs a, const _
 __host__ __device__ constexpr int ws_rows(int cout) { return cout >= 128 ? 2 : 4; }
 __host__ __device__ constexpr int ws_stages(int cout) { return cout >= 128 ? 4 : 3; }
 
-template <int COUT, bool UPS>
+// STACK: the row-stacked form; its weights come as
+// [slice][kx][half][ky = 2, 1, 0][COUT][8] (k_tc_weights_stack).
+template <int COUT, bool UPS, bool STACK = false>
 cudaError_t launch_conv_ws(const ConvArgs& ca, const bf16* wt, uint32_t* status, int sm_count, cudaStream_t s) {
     constexpr int kRows = ws_rows(COUT), kStages = ws_stages(COUT);
-    constexpr int kCols = 2 * kRows * COUT < 32 ? 32 : 2 * kRows * COUT;
+    constexpr int kAccCols = 2 * ws_acc_cols<COUT, kRows, STACK>();
+    constexpr int kCols = kAccCols < 32 ? 32 : kAccCols;
     constexpr int kThreads = ws_threads(UPS);
     static uint64_t configured = 0;
     static int per_sm = 0;
-    const size_t smem = ws_smem_bytes<COUT, kRows, kStages>();
-    cudaError_t e = tc_configure(k_conv_ws<COUT, kRows, kStages, UPS>, smem, configured);
+    const size_t smem = ws_smem_bytes<COUT, kRows, kStages, STACK>();
+    cudaError_t e = tc_configure(k_conv_ws<COUT, kRows, kStages, UPS, STACK>, smem, configured);
     if (e != cudaSuccess) return e;
     if (per_sm == 0) {
         int occ = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv_ws<COUT, kRows, kStages, UPS>, kThreads, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv_ws<COUT, kRows, kStages, UPS, STACK>, kThreads,
+                                                          smem);
         if (e != cudaSuccess) return e;
         per_sm = std::max(1, std::min(occ, 512 / kCols));
     }
@@ -813,7 +892,7 @@ cudaError_t launch_conv_ws(const ConvArgs& ca, const bf16* wt, uint32_t* status,
     }
     const int tiles = ((ca.w_ + kTcPix - 1) / kTcPix) * ((ca.h + kRows - 1) / kRows) * ca.n;
     const int blocks = std::max(1, std::min(tiles, sm_count * per_sm));
-    k_conv_ws<COUT, kRows, kStages, UPS><<<blocks, kThreads, smem, s>>>(ca, ma, mb, wt, status);
+    k_conv_ws<COUT, kRows, kStages, UPS, STACK><<<blocks, kThreads, smem, s>>>(ca, ma, mb, wt, status);
     return cudaGetLastError();
 }
 

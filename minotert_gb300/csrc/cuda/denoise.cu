@@ -480,6 +480,7 @@ struct mrt_denoiser {
     float *w = nullptr, *wm = nullptr, *wv = nullptr, *wg = nullptr;  // weights + biases, FP32
     bf16* w16 = nullptr;
     bf16* wtc = nullptr;          // w16 re-laid out per 16-channel slice for the TMA convolution
+    bf16* wst = nullptr;          // the 16/32-channel layers' weights for the row-stacked form
     bf16* wup = nullptr;          // per-slice weights of the phase-decomposed upsampling layers
     size_t up_off[kLayers] = {};  // their offsets in wup (upsampling layers only)
     // activation tensors (bf16) and their gradients (fp32), sized for n*h*w
@@ -582,9 +583,9 @@ cudaError_t conv(const mrt_denoiser* d, int l, const bf16* a, const bf16* b, int
             if (L.cout == 32) return launch_conv_up<32>(ca, wu, d->status, d->sm_count, s);
             if (L.cout == 64) return launch_conv_up<64>(ca, wu, d->status, d->sm_count, s);
         } else {
-            switch (L.cout) {
-            case 16: return launch_conv_ws<16, false>(ca, wt, d->status, d->sm_count, s);
-            case 32: return launch_conv_ws<32, false>(ca, wt, d->status, d->sm_count, s);
+            switch (L.cout) {  // 16 and 32 channels: row-stacked
+            case 16: return launch_conv_ws<16, false, true>(ca, d->wst + L.w_off, d->status, d->sm_count, s);
+            case 32: return launch_conv_ws<32, false, true>(ca, d->wst + L.w_off, d->status, d->sm_count, s);
             case 64: return launch_conv_ws<64, false>(ca, wt, d->status, d->sm_count, s);
             default: return launch_conv_ws<128, false>(ca, wt, d->status, d->sm_count, s);
             }
@@ -618,7 +619,7 @@ cudaError_t conv(const mrt_denoiser* d, int l, const bf16* a, const bf16* b, int
 }
 
 // kernels forward() launches
-int forward_launches(const mrt_denoiser* d) { return 13 + (d->tc_mode != 0 ? 1 : 0) + (d->tc_mode == 2 ? 2 : 0); }
+int forward_launches(const mrt_denoiser* d) { return 13 + (d->tc_mode != 0 ? 1 : 0) + (d->tc_mode == 2 ? 3 : 0); }
 
 // forward of the whole network over n images of h x w (h, w multiples of 4)
 cudaError_t forward(const mrt_denoiser* d, const bf16* in, int n, int h, int w, cudaStream_t s) {
@@ -632,6 +633,7 @@ cudaError_t forward(const mrt_denoiser* d, const bf16* in, int n, int h, int w, 
             t.off[l] = d->layers[l].w_off;
         }
         k_tc_weights<<<304, 256, 0, s>>>(d->w16, d->wtc, t);
+        if (d->tc_mode == 2) k_tc_weights_stack<<<304, 256, 0, s>>>(d->w16, d->wst, t);
         if (d->tc_mode == 2)
             for (int l = 0; l < kLayers; ++l)
                 if (d->layers[l].ups)
@@ -809,6 +811,7 @@ int mrt_cuda_denoiser_create(mrt_ctx* ctx, uint32_t seed, mrt_denoiser** out) {
               cudaMalloc(&d->w16, d->n_w * 2) == cudaSuccess && cudaMalloc(&d->wtc, d->n_w * 2) == cudaSuccess &&
               cudaMalloc(&d->wbt, d->n_w * 2) == cudaSuccess && cudaMalloc(&d->zeros, 128 * 4) == cudaSuccess &&
               cudaMalloc(&d->wup, std::max<size_t>(n_up, 1) * 2) == cudaSuccess &&
+              cudaMalloc(&d->wst, d->n_w * 2) == cudaSuccess &&
               cudaMalloc(&d->loss, 4) == cudaSuccess &&
               cudaMallocHost(&d->h_loss, 4) == cudaSuccess;
     if (!ok) {
@@ -858,7 +861,7 @@ int mrt_cuda_denoiser_destroy(mrt_ctx* ctx, mrt_denoiser* d) {
     cudaDeviceSynchronize();
     for (int l = 0; l < kLayers; ++l) { cudaFree(d->act[l]); cudaFree(d->grad[l]); cudaFree(d->gz[l]); }
     void* ps[] = {d->w, d->wm, d->wv, d->wg, d->w16, d->wtc, d->pool0, d->pool1, d->gpool0, d->gpool1, d->gin,
-                  d->loss, d->wbt, d->zeros, d->up8, d->up6, d->skip8, d->skip6, d->gp0, d->gp1, d->wup};
+                  d->loss, d->wbt, d->zeros, d->up8, d->up6, d->skip8, d->skip6, d->gp0, d->gp1, d->wup, d->wst};
     for (void* p : ps) cudaFree(p);
     if (d->h_loss) cudaFreeHost(d->h_loss);
     delete d;
