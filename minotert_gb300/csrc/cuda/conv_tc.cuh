@@ -548,7 +548,9 @@ cudaError_t launch_conv_tma(const ConvArgs& ca, const bf16* wt, uint32_t* status
 // tensor-memory allocation and epilogue in series per tile.  Every wait is
 // bounded and also ends when another role has given up (a shared abort
 // word); the CTA then sets MRT_STATUS_PIPE_TIMEOUT, waits (bounded) for the
-// copies and MMAs it issued and frees its tensor memory.
+// copies and MMAs it issued and frees its tensor memory.  Sources are read
+// at the output's resolution (the decoder's upsampling layers run k_conv_up).
+//
 // Row-stacked form (STACK, the 16- and 32-channel layers): an MMA costs a
 // fixed ~46 cycles up to N = 64, so instead of one MMA per (output row, tap)
 // with N = COUT, one MMA per (halo row h, tap column kx) feeds the three
@@ -585,17 +587,16 @@ __device__ __forceinline__ bool ws_wait(uint32_t mbar, uint32_t parity, const vo
     return false;
 }
 
-// Threads of the persistent form: four epilogue warps, the producer warps
-// (one for tensor copies; four when the layer's first source is upsampled
-// and its halo is gathered with cp.async), one MMA warp.
-__host__ __device__ constexpr int ws_prod_warps(bool ups) { return ups ? 4 : 1; }
-__host__ __device__ constexpr int ws_threads(bool ups) { return 32 * (5 + ws_prod_warps(ups)); }
+// Threads of the persistent forms: four epilogue warps, the producer warps
+// (one thread of one warp issuing tensor copies in k_conv_ws; four warps in
+// k_conv_up, whose skip source is gathered with cp.async), one MMA warp.
+__host__ __device__ constexpr int ws_prod_warps(bool gathers) { return gathers ? 4 : 1; }
+__host__ __device__ constexpr int ws_threads(bool gathers) { return 32 * (5 + ws_prod_warps(gathers)); }
 
-template <int COUT, int ROWS, int STAGES, bool UPS, bool STACK = false>
-__global__ void __launch_bounds__(ws_threads(UPS)) k_conv_ws(ConvArgs a, const __grid_constant__ CUtensorMap map_a,
-                                                            const __grid_constant__ CUtensorMap map_b, const bf16* wt,
-                                                            uint32_t* status) {
-    static_assert(!(STACK && UPS), "the row-stacked form reads sources at the output's resolution");
+template <int COUT, int ROWS, int STAGES, bool STACK = false>
+__global__ void __launch_bounds__(ws_threads(false)) k_conv_ws(ConvArgs a, const __grid_constant__ CUtensorMap map_a,
+                                                              const __grid_constant__ CUtensorMap map_b, const bf16* wt,
+                                                              uint32_t* status) {
     constexpr int kAcc = ws_acc_cols<COUT, ROWS, STACK>();  // TMEM columns of one accumulator
     constexpr uint32_t kZero = ws_zero_bytes<COUT, ROWS, STACK>();
     constexpr int kCols = 2 * kAcc < 32 ? 32 : 2 * kAcc;
@@ -604,8 +605,7 @@ __global__ void __launch_bounds__(ws_threads(UPS)) k_conv_ws(ConvArgs a, const _
     constexpr uint32_t kHaloTx = 2u * uint32_t((ROWS + 2) * kTcPlane);
     constexpr uint32_t kWBytes = uint32_t(9 * 2 * COUT * 16);
     constexpr uint32_t kStage = tma_stage_bytes<COUT, ROWS>();
-    constexpr int kProdWarps = ws_prod_warps(UPS), kProdThreads = 32 * kProdWarps;
-    constexpr int kMmaWarp = 4 + kProdWarps;
+    constexpr int kMmaWarp = 5;
     extern __shared__ __align__(128) unsigned char tsm[];
     uint64_t* full = reinterpret_cast<uint64_t*>(tsm + STAGES * kStage + kZero);
     uint64_t* empty = full + STAGES;
@@ -629,12 +629,8 @@ __global__ void __launch_bounds__(ws_threads(UPS)) k_conv_ws(ConvArgs a, const _
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        // a stage is full after the expect_tx arrival and, with gathered
-        // copies, one arrival per producer thread
-        const uint32_t full_count = UPS ? 1u + uint32_t(kProdThreads) : 1u;
-        for (int s = 0; s < STAGES; ++s) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(full + s)), "r"(full_count)
-                         : "memory");
+        for (int s = 0; s < STAGES; ++s) {  // full: the producer's expect_tx arrival
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(full + s)) : "memory");
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(empty + s)) : "memory");
         }
         for (int b = 0; b < 2; ++b) {
@@ -663,11 +659,9 @@ __global__ void __launch_bounds__(ws_threads(UPS)) k_conv_ws(ConvArgs a, const _
     };
 
     int produced = 0;
-    if (warp >= 4 && warp < kMmaWarp) {
-        // producer: (tile, slice) pairs into the stage ring
-        const int ptid = tid - 128;
-        const int ha = UPS ? a.h >> 1 : a.h, wa = UPS ? a.w_ >> 1 : a.w_;
-        if (UPS || ptid == 0) {
+    if (warp == 4) {
+        // producer (one thread): (tile, slice) pairs into the stage ring
+        if (lane == 0) {
             int g = 0;
             bool ok = *abort == 0u;
             for (int tile = blockIdx.x; ok && tile < tiles; tile += gridDim.x) {
@@ -678,62 +672,24 @@ __global__ void __launch_bounds__(ws_threads(UPS)) k_conv_ws(ConvArgs a, const _
                     const uint32_t u = uint32_t(g / STAGES);
                     const uint32_t st = smem0 + uint32_t(s) * kStage, mb = smem_u32(full + s);
                     const int c = 16 * k;
-                    const bool gathered = UPS && c < a.ca;
                     const CUtensorMap* map = c < a.ca ? &map_a : &map_b;
                     const int cc = c < a.ca ? c : c - a.ca;
-                    // thread 0 waits for the stage and decides for the group;
-                    // the decision goes through a word per slice parity so
-                    // every producer thread reads the same one (thread 0
-                    // cannot rewrite it before all have passed the next
-                    // group barrier)
-                    if (ptid == 0) {
-                        if (!ws_wait(smem_u32(empty + s), (u & 1u) ^ 1u, abort) || (st & 127u) != 0u ||
-                            (cc & 7) != 0)
-                            give_up();
-                        prod_go[g & 1] = *abort == 0u ? 1u : 0u;
-                    }
-                    if (UPS) asm volatile("bar.sync 1, %0;" ::"n"(kProdThreads) : "memory");
-                    if (prod_go[g & 1] == 0u) { ok = false; break; }
-                    if (ptid == 0) {
-                        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb),
-                                     "r"(gathered ? kWBytes : kHaloTx + kWBytes)
-                                     : "memory");
-                        if (!gathered) {
-                            tma_load_halo(st, map, cc, x0 - 1, y0 - 1, n, mb);
-                            tma_load_halo(st + kHalf, map, cc + 8, x0 - 1, y0 - 1, n, mb);
-                        }
-                        asm volatile(
-                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                                st + kHalo),
-                            "l"(wt + size_t(k) * (kWBytes / 2)), "r"(kWBytes), "r"(mb)
-                            : "memory");
-                    }
-                    if (UPS) {
-                        if (gathered) {
-                            // the nearest-upsampled halo: rows y0-1 .. y0+ROWS,
-                            // pixels x0-1 .. x0+128 of source A at half
-                            // resolution, zero outside the image
-                            // (both 8-channel halves of a pixel per thread: one
-                            // address computation for two copies)
-                            for (int i = ptid; i < (ROWS + 2) * kTcHalo; i += kProdThreads) {
-                                const int r = i / kTcHalo, p = i - r * kTcHalo;
-                                const int yy = y0 - 1 + r, xx = x0 - 1 + p;
-                                const bool in = yy >= 0 && yy < a.h && xx >= 0 && xx < a.w_;
-                                const bf16* src = in ? a.a + ((size_t(n) * ha + (yy >> 1)) * wa + (xx >> 1)) * a.ca + c
-                                                     : a.w;  // any valid address when zero-filling
-                                const uint32_t dst = st + uint32_t(r * kTcPlane + p * 16);
-                                cp16(dst, src, in);
-                                cp16(dst + kHalf, in ? src + 8 : src, in);
-                            }
-                            asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(mb) : "memory");
-                        } else {
-                            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mb) : "memory");
-                        }
-                    }
+                    if (!ws_wait(smem_u32(empty + s), (u & 1u) ^ 1u, abort) || (st & 127u) != 0u || (cc & 7) != 0)
+                        give_up();
+                    if (*abort != 0u) { ok = false; break; }
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb),
+                                 "r"(kHaloTx + kWBytes)
+                                 : "memory");
+                    tma_load_halo(st, map, cc, x0 - 1, y0 - 1, n, mb);
+                    tma_load_halo(st + kHalf, map, cc + 8, x0 - 1, y0 - 1, n, mb);
+                    asm volatile(
+                        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                            st + kHalo),
+                        "l"(wt + size_t(k) * (kWBytes / 2)), "r"(kWBytes), "r"(mb)
+                        : "memory");
                     produced = g + 1;
                 }
             }
-            if (UPS) asm volatile("cp.async.wait_all;" ::: "memory");
         }
     } else if (warp == kMmaWarp) {
         if (lane == 0 && *abort == 0u) {  // MMA issuer
@@ -860,39 +816,34 @@ __host__ __device__ constexpr int ws_stages(int cout) { return cout >= 128 ? 4 :
 
 // STACK: the row-stacked form; its weights come as
 // [slice][kx][half][ky = 2, 1, 0][COUT][8] (k_tc_weights_stack).
-template <int COUT, bool UPS, bool STACK = false>
+template <int COUT, bool STACK = false>
 cudaError_t launch_conv_ws(const ConvArgs& ca, const bf16* wt, uint32_t* status, int sm_count, cudaStream_t s) {
     constexpr int kRows = ws_rows(COUT), kStages = ws_stages(COUT);
     constexpr int kAccCols = 2 * ws_acc_cols<COUT, kRows, STACK>();
     constexpr int kCols = kAccCols < 32 ? 32 : kAccCols;
-    constexpr int kThreads = ws_threads(UPS);
+    constexpr int kThreads = ws_threads(false);
     static uint64_t configured = 0;
     static int per_sm = 0;
     const size_t smem = ws_smem_bytes<COUT, kRows, kStages, STACK>();
-    cudaError_t e = tc_configure(k_conv_ws<COUT, kRows, kStages, UPS, STACK>, smem, configured);
+    cudaError_t e = tc_configure(k_conv_ws<COUT, kRows, kStages, STACK>, smem, configured);
     if (e != cudaSuccess) return e;
     if (per_sm == 0) {
         int occ = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv_ws<COUT, kRows, kStages, UPS, STACK>, kThreads,
-                                                          smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv_ws<COUT, kRows, kStages, STACK>, kThreads, smem);
         if (e != cudaSuccess) return e;
         per_sm = std::max(1, std::min(occ, 512 / kCols));
     }
+    if (ca.ups) return cudaErrorInvalidValue;  // upsampled sources: k_conv_up
     CUtensorMap ma, mb;
-    if (UPS) {  // source A is gathered; only the skip source has a tensor map
-        if (ca.cb <= 0 || !tma_encode(&mb, ca.b, ca.cb, ca.w_, ca.h, ca.n, kRows)) return cudaErrorInvalidValue;
-        ma = mb;
+    if (!tma_encode(&ma, ca.a, ca.ca, ca.w_, ca.h, ca.n, kRows)) return cudaErrorInvalidValue;
+    if (ca.cb > 0) {
+        if (!tma_encode(&mb, ca.b, ca.cb, ca.w_, ca.h, ca.n, kRows)) return cudaErrorInvalidValue;
     } else {
-        if (!tma_encode(&ma, ca.a, ca.ca, ca.w_, ca.h, ca.n, kRows)) return cudaErrorInvalidValue;
-        if (ca.cb > 0) {
-            if (!tma_encode(&mb, ca.b, ca.cb, ca.w_, ca.h, ca.n, kRows)) return cudaErrorInvalidValue;
-        } else {
-            mb = ma;
-        }
+        mb = ma;
     }
     const int tiles = ((ca.w_ + kTcPix - 1) / kTcPix) * ((ca.h + kRows - 1) / kRows) * ca.n;
     const int blocks = std::max(1, std::min(tiles, sm_count * per_sm));
-    k_conv_ws<COUT, kRows, kStages, UPS, STACK><<<blocks, kThreads, smem, s>>>(ca, ma, mb, wt, status);
+    k_conv_ws<COUT, kRows, kStages, STACK><<<blocks, kThreads, smem, s>>>(ca, ma, mb, wt, status);
     return cudaGetLastError();
 }
 

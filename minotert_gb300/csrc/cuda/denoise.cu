@@ -584,10 +584,10 @@ cudaError_t conv(const mrt_denoiser* d, int l, const bf16* a, const bf16* b, int
             if (L.cout == 64) return launch_conv_up<64>(ca, wu, d->status, d->sm_count, s);
         } else {
             switch (L.cout) {  // 16 and 32 channels: row-stacked
-            case 16: return launch_conv_ws<16, false, true>(ca, d->wst + L.w_off, d->status, d->sm_count, s);
-            case 32: return launch_conv_ws<32, false, true>(ca, d->wst + L.w_off, d->status, d->sm_count, s);
-            case 64: return launch_conv_ws<64, false>(ca, wt, d->status, d->sm_count, s);
-            default: return launch_conv_ws<128, false>(ca, wt, d->status, d->sm_count, s);
+            case 16: return launch_conv_ws<16, true>(ca, d->wst + L.w_off, d->status, d->sm_count, s);
+            case 32: return launch_conv_ws<32, true>(ca, d->wst + L.w_off, d->status, d->sm_count, s);
+            case 64: return launch_conv_ws<64>(ca, wt, d->status, d->sm_count, s);
+            default: return launch_conv_ws<128>(ca, wt, d->status, d->sm_count, s);
             }
         }
     }
@@ -684,9 +684,9 @@ cudaError_t dgrad(const mrt_denoiser* d, int l, int part, const bf16* dz, bf16* 
     ca.gate = gate;
     const bf16* wt = d->wbt + L.w_off + (part ? size_t(9) * L.cout * L.ca : 0);
     switch (cp) {
-    case 32: return launch_conv_ws<32, false>(ca, wt, d->status, d->sm_count, s);
-    case 64: return launch_conv_ws<64, false>(ca, wt, d->status, d->sm_count, s);
-    case 128: return launch_conv_ws<128, false>(ca, wt, d->status, d->sm_count, s);
+    case 32: return launch_conv_ws<32>(ca, wt, d->status, d->sm_count, s);
+    case 64: return launch_conv_ws<64>(ca, wt, d->status, d->sm_count, s);
+    case 128: return launch_conv_ws<128>(ca, wt, d->status, d->sm_count, s);
     default: return cudaErrorInvalidValue;
     }
 }
