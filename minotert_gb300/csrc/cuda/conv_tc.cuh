@@ -473,8 +473,10 @@ __global__ void k_tc_weights_stack(const bf16* w16, bf16* wt, TcLayerTable t) {
 __host__ __device__ constexpr int tma_rows(int cout) { return cout >= 64 ? 2 : 4; }
 __host__ __device__ constexpr int tma_stages(int) { return 2; }
 
-// NHWC BF16 tensor map with the halo box of one 8-channel half
-inline bool tma_encode(CUtensorMap* map, const bf16* base, int c, int w, int h, int n, int rows) {
+// NHWC BF16 tensor map with a box of one 8-channel half x box_x pixels x
+// box_rows rows; x_stride 2 loads every other pixel (box_x / 2 of them)
+inline bool tma_encode_box(CUtensorMap* map, const bf16* base, int c, int w, int h, int n, int box_x, int box_rows,
+                           int x_stride) {
     using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -490,11 +492,16 @@ inline bool tma_encode(CUtensorMap* map, const bf16* base, int c, int w, int h, 
     }
     const cuuint64_t dims[4] = {cuuint64_t(c), cuuint64_t(w), cuuint64_t(h), cuuint64_t(n)};
     const cuuint64_t strides[3] = {cuuint64_t(c) * 2, cuuint64_t(c) * 2 * w, cuuint64_t(c) * 2 * w * h};
-    const cuuint32_t box[4] = {8u, cuuint32_t(kTcHalo), cuuint32_t(rows + 2), 1u};
-    const cuuint32_t estr[4] = {1u, 1u, 1u, 1u};
+    const cuuint32_t box[4] = {8u, cuuint32_t(box_x), cuuint32_t(box_rows), 1u};
+    const cuuint32_t estr[4] = {1u, cuuint32_t(x_stride), 1u, 1u};
     return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(base), dims, strides, box, estr,
               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// the halo box of the convolutions: 130 pixels x (rows + 2) rows
+inline bool tma_encode(CUtensorMap* map, const bf16* base, int c, int w, int h, int n, int rows) {
+    return tma_encode_box(map, base, c, w, h, n, kTcHalo, rows + 2, 1);
 }
 
 // cudaFuncSetAttribute(MaxDynamicSharedMemorySize) once per device for the
@@ -587,14 +594,12 @@ __device__ __forceinline__ bool ws_wait(uint32_t mbar, uint32_t parity, const vo
     return false;
 }
 
-// Threads of the persistent forms: four epilogue warps, the producer warps
-// (one thread of one warp issuing tensor copies in k_conv_ws; four warps in
-// k_conv_up, whose skip source is gathered with cp.async), one MMA warp.
-__host__ __device__ constexpr int ws_prod_warps(bool gathers) { return gathers ? 4 : 1; }
-__host__ __device__ constexpr int ws_threads(bool gathers) { return 32 * (5 + ws_prod_warps(gathers)); }
+// Threads of the persistent forms: four epilogue warps, a producer warp (one
+// thread issuing tensor and bulk copies), an MMA warp (one thread).
+constexpr int kWsThreads = 6 * 32;
 
 template <int COUT, int ROWS, int STAGES, bool STACK = false>
-__global__ void __launch_bounds__(ws_threads(false)) k_conv_ws(ConvArgs a, const __grid_constant__ CUtensorMap map_a,
+__global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __grid_constant__ CUtensorMap map_a,
                                                               const __grid_constant__ CUtensorMap map_b, const bf16* wt,
                                                               uint32_t* status) {
     constexpr int kAcc = ws_acc_cols<COUT, ROWS, STACK>();  // TMEM columns of one accumulator
@@ -615,7 +620,6 @@ __global__ void __launch_bounds__(ws_threads(false)) k_conv_ws(ConvArgs a, const
     uint32_t* slot = reinterpret_cast<uint32_t*>(fin + 1);
     volatile uint32_t* abort = slot + 1;
     uint32_t* consumed = slot + 2;          // slices the MMA thread waited for
-    volatile uint32_t* prod_go = slot + 3;  // [2]: producer thread 0's go / stop, by slice parity
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tiles_x = (a.w_ + kTcPix - 1) / kTcPix, rows_per_img = (a.h + ROWS - 1) / ROWS;
     const int tiles = tiles_x * rows_per_img * a.n;
@@ -821,7 +825,7 @@ cudaError_t launch_conv_ws(const ConvArgs& ca, const bf16* wt, uint32_t* status,
     constexpr int kRows = ws_rows(COUT), kStages = ws_stages(COUT);
     constexpr int kAccCols = 2 * ws_acc_cols<COUT, kRows, STACK>();
     constexpr int kCols = kAccCols < 32 ? 32 : kAccCols;
-    constexpr int kThreads = ws_threads(false);
+    constexpr int kThreads = kWsThreads;
     static uint64_t configured = 0;
     static int per_sm = 0;
     const size_t smem = ws_smem_bytes<COUT, kRows, kStages, STACK>();
@@ -879,17 +883,19 @@ cudaError_t launch_conv_tc(const ConvArgs& ca, uint32_t* status, cudaStream_t s)
 // serves both where they read the same shifted A operand: per (r, py, ry)
 // the column shift s = px + rx takes the values 0 (px 0), 1 (px 0 with
 // rx 1, px 1 with rx 0) and 2 (px 1): three MMAs of N = COUT, 2 COUT, COUT.
-// The skip source B at full resolution is gathered with cp.async into two
-// planes per row, even and odd pixels (entry e of parity q = pixel
-// 2(X0 - 1 + e) + q), so that a phase's tap reads consecutive entries; per
+// The skip source B at full resolution comes by tensor copies with an
+// element stride of 2 into two planes per row, even and odd pixels (entry e
+// of parity q = pixel 2(X0 - 1 + e) + q; a 256-pixel box loads 128 entries,
+// which cover the 126 columns' taps; lanes 126, 127 read past them into the
+// next row, unused), so that a phase's tap reads consecutive entries; per
 // (r, py, ky) the taps of both phases read four distinct (parity, shift)
 // operands: (1,0) px0 kx0; (0,1) px0 kx1 + px1 kx0; (1,1) px0 kx2 +
 // px1 kx1; (0,2) px1 kx2 — four MMAs of N = COUT, 2 COUT, 2 COUT, COUT with
 // the unmerged tap weights.  Weights per 16-channel slice come from a copy
 // laid out per MMA in that order (k_up_weights; [half][N rows][8]).  Roles,
-// waits and abort handling are those of k_conv_ws with the gathered slices
-// now the skip source's.
-constexpr int kUpCols = 126;  // low-resolution columns of a tile
+// waits and abort handling are those of k_conv_ws.
+constexpr int kUpCols = 126;    // low-resolution columns of a tile
+constexpr int kUpEntries = 128; // skip-source entries per plane row: one 256-pixel, stride-2 tensor box
 template <int COUT>
 __host__ __device__ constexpr uint32_t up_wbytes_a() { return uint32_t(16 * COUT * 32); }  // 4 x (1+2+1) x COUT rows
 template <int COUT>
@@ -897,11 +903,11 @@ __host__ __device__ constexpr uint32_t up_wbytes_b() { return uint32_t(18 * COUT
 template <int R>
 __host__ __device__ constexpr uint32_t up_half_a() { return (uint32_t((R + 2) * kTcPlane) + 127u) & ~127u; }
 template <int R>
-__host__ __device__ constexpr uint32_t up_half_b() { return uint32_t((2 * R + 2) * 2 * kTcPlane); }
+__host__ __device__ constexpr uint32_t up_half_b() { return uint32_t((2 * R + 2) * 2 * kUpEntries * 16); }
 template <int COUT, int R>
 __host__ __device__ constexpr uint32_t up_stage_bytes() {
     const uint32_t a = 2u * up_half_a<R>() + up_wbytes_a<COUT>();
-    const uint32_t b = 2u * up_half_b<R>() + up_wbytes_b<COUT>();
+    const uint32_t b = 2u * up_half_b<R>() + 128u + up_wbytes_b<COUT>();  // 128: the garbage rows' overrun
     return ((a > b ? a : b) + 127u) & ~127u;
 }
 template <int COUT, int R, int STAGES>
@@ -1014,8 +1020,9 @@ __device__ __forceinline__ void up_epilogue(const ConvArgs& a, uint32_t taddr, i
 }
 
 template <int COUT, int R, int STAGES>
-__global__ void __launch_bounds__(ws_threads(true)) k_conv_up(ConvArgs a, const __grid_constant__ CUtensorMap map_a,
-                                                             const bf16* wup, uint32_t* status) {
+__global__ void __launch_bounds__(kWsThreads) k_conv_up(ConvArgs a, const __grid_constant__ CUtensorMap map_a,
+                                                              const __grid_constant__ CUtensorMap map_b, const bf16* wup,
+                                                              uint32_t* status) {
     constexpr int kAcc = 4 * R * COUT;  // TMEM columns of one accumulator set
     constexpr int kCols = 2 * kAcc < 32 ? 32 : 2 * kAcc;
     static_assert(kCols <= 512 && (kCols & (kCols - 1)) == 0, "tensor memory columns");
@@ -1023,8 +1030,10 @@ __global__ void __launch_bounds__(ws_threads(true)) k_conv_up(ConvArgs a, const 
     constexpr uint32_t kHaloTxA = 2u * uint32_t((R + 2) * kTcPlane);
     constexpr uint32_t kWA = up_wbytes_a<COUT>(), kWB = up_wbytes_b<COUT>();
     constexpr uint32_t kStage = up_stage_bytes<COUT, R>();
-    constexpr int kProdWarps = ws_prod_warps(true), kProdThreads = 32 * kProdWarps;
-    constexpr int kMmaWarp = 4 + kProdWarps;
+    constexpr uint32_t kPlaneB = uint32_t((2 * R + 2) * kUpEntries * 16);  // one (half, parity) plane set
+    constexpr uint32_t kHaloTxB = 4u * kPlaneB;
+    constexpr uint32_t kWOffB = 2u * kHalfB + 128u;
+    constexpr int kMmaWarp = 5;
     extern __shared__ __align__(128) unsigned char tsm[];
     uint64_t* full = reinterpret_cast<uint64_t*>(tsm + STAGES * kStage);
     uint64_t* empty = full + STAGES;
@@ -1034,7 +1043,6 @@ __global__ void __launch_bounds__(ws_threads(true)) k_conv_up(ConvArgs a, const 
     uint32_t* slot = reinterpret_cast<uint32_t*>(fin + 1);
     volatile uint32_t* abort = slot + 1;
     uint32_t* consumed = slot + 2;
-    volatile uint32_t* prod_go = slot + 3;  // [2]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int hl = a.h >> 1, wl = a.w_ >> 1;  // low resolution (source A)
     const int tiles_x = (wl + kUpCols - 1) / kUpCols, rows_per_img = (hl + R - 1) / R;
@@ -1050,9 +1058,7 @@ __global__ void __launch_bounds__(ws_threads(true)) k_conv_up(ConvArgs a, const 
     }
     if (tid == 0) {
         for (int s = 0; s < STAGES; ++s) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(full + s)),
-                         "r"(1u + uint32_t(kProdThreads))
-                         : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(full + s)) : "memory");
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(empty + s)) : "memory");
         }
         for (int b = 0; b < 2; ++b) {
@@ -1074,61 +1080,49 @@ __global__ void __launch_bounds__(ws_threads(true)) k_conv_up(ConvArgs a, const 
     };
 
     int produced = 0;
-    if (warp >= 4 && warp < kMmaWarp) {
-        // producers: A slices by tensor copies (thread 0), skip slices
-        // gathered by all producer threads into even / odd pixel planes
-        const int ptid = tid - 128;
-        int g = 0;
-        for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-            const int tx = tile % tiles_x, rb = tile / tiles_x;
-            const int Y0 = (rb % rows_per_img) * R, n = rb / rows_per_img, X0 = tx * kUpCols;
-            bool stop = false;
-            for (int k = 0; k < nk; ++k, ++g) {
-                const int s = g % STAGES;
-                const uint32_t u = uint32_t(g / STAGES);
-                const uint32_t st = smem0 + uint32_t(s) * kStage, mb = smem_u32(full + s);
-                const bool is_a = k < nka;
-                if (ptid == 0) {
+    if (warp == 4) {
+        // producer (one thread): per slice, tensor copies of the upsampled
+        // source's low-resolution halo (A slices) or of the skip source's
+        // even and odd pixels (element stride 2: entry e of parity q =
+        // pixel 2 (X0 - 1 + e) + q, rows 2 Y0 - 1 .. 2 Y0 + 2R), and a bulk
+        // copy of the slice's weights, all completing on the stage's `full`
+        if (lane == 0) {
+            int g = 0;
+            bool ok = *abort == 0u;
+            for (int tile = blockIdx.x; ok && tile < tiles; tile += gridDim.x) {
+                const int tx = tile % tiles_x, rb = tile / tiles_x;
+                const int Y0 = (rb % rows_per_img) * R, n = rb / rows_per_img, X0 = tx * kUpCols;
+                for (int k = 0; k < nk; ++k, ++g) {
+                    const int s = g % STAGES;
+                    const uint32_t u = uint32_t(g / STAGES);
+                    const uint32_t st = smem0 + uint32_t(s) * kStage, mb = smem_u32(full + s);
+                    const bool is_a = k < nka;
                     if (!ws_wait(smem_u32(empty + s), (u & 1u) ^ 1u, abort) || (st & 127u) != 0u) give_up();
-                    prod_go[g & 1] = *abort == 0u ? 1u : 0u;
-                }
-                asm volatile("bar.sync 1, %0;" ::"n"(kProdThreads) : "memory");
-                if (prod_go[g & 1] == 0u) { stop = true; break; }
-                if (ptid == 0) {
+                    if (*abort != 0u) { ok = false; break; }
                     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb),
-                                 "r"(is_a ? kHaloTxA + kWA : kWB)
+                                 "r"(is_a ? kHaloTxA + kWA : kHaloTxB + kWB)
                                  : "memory");
                     if (is_a) {
                         tma_load_halo(st, &map_a, 16 * k, X0 - 1, Y0 - 1, n, mb);
                         tma_load_halo(st + kHalfA, &map_a, 16 * k + 8, X0 - 1, Y0 - 1, n, mb);
+                    } else {
+                        const int c = 16 * k - a.ca;
+#pragma unroll
+                        for (int hf = 0; hf < 2; ++hf)
+#pragma unroll
+                            for (int q = 0; q < 2; ++q)
+                                tma_load_halo(st + uint32_t(hf) * kHalfB + uint32_t(q) * kPlaneB, &map_b, c + 8 * hf,
+                                              2 * (X0 - 1) + q, 2 * Y0 - 1, n, mb);
                     }
                     asm volatile(
                         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                            st + (is_a ? 2u * kHalfA : 2u * kHalfB)),
+                            st + (is_a ? 2u * kHalfA : kWOffB)),
                         "l"(wup + size_t(k) * (kWB / 2)), "r"(is_a ? kWA : kWB), "r"(mb)
                         : "memory");
+                    produced = g + 1;
                 }
-                if (is_a) {
-                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mb) : "memory");
-                } else {
-                    // full-resolution rows 2 Y0 - 1 .. 2 Y0 + 2R, pixels 2 (X0 - 1 + e) + q,
-                    // e < 130, channels c .. c + 15 of B (two 16-byte halves)
-                    const int c = 16 * k - a.ca;
-                    for (int i = ptid; i < (2 * R + 2) * kTcHalo * 4; i += kProdThreads) {
-                        const int hf = i & 1, q = (i >> 1) & 1, e = (i >> 2) % kTcHalo, fr = (i >> 2) / kTcHalo;
-                        const int yy = 2 * Y0 - 1 + fr, xx = 2 * (X0 - 1 + e) + q;
-                        const bool in = yy >= 0 && yy < a.h && xx >= 0 && xx < a.w_;
-                        const bf16* src = in ? a.b + ((size_t(n) * a.h + yy) * a.w_ + xx) * a.cb + c + 8 * hf
-                                             : a.b;  // any valid address when zero-filling
-                        cp16(st + uint32_t(hf) * kHalfB + uint32_t((fr * 2 + q) * kTcPlane + e * 16), src, in);
-                    }
-                    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(mb) : "memory");
-                }
-                produced = g + 1;
             }
-            if (stop) break;
         }
-        asm volatile("cp.async.wait_all;" ::: "memory");
     } else if (warp == kMmaWarp) {
         if (lane == 0 && *abort == 0u) {
             int g = 0, it = 0;
@@ -1138,8 +1132,8 @@ __global__ void __launch_bounds__(ws_threads(true)) k_conv_up(ConvArgs a, const 
             const uint64_t da_a = tc_sdesc(smem0, kHalfA, 128), da_b = tc_sdesc(smem0, kHalfB, 128);
             const uint64_t dw_a1 = tc_sdesc(smem0 + 2u * kHalfA, COUT * 16, 128);
             const uint64_t dw_a2 = tc_sdesc(smem0 + 2u * kHalfA, 2 * COUT * 16, 128);
-            const uint64_t dw_b1 = tc_sdesc(smem0 + 2u * kHalfB, COUT * 16, 128);
-            const uint64_t dw_b2 = tc_sdesc(smem0 + 2u * kHalfB, 2 * COUT * 16, 128);
+            const uint64_t dw_b1 = tc_sdesc(smem0 + kWOffB, COUT * 16, 128);
+            const uint64_t dw_b2 = tc_sdesc(smem0 + kWOffB, 2 * COUT * 16, 128);
             for (int tile = blockIdx.x; ok && tile < tiles; tile += gridDim.x, ++it) {
                 const int b = it & 1;
                 const uint32_t ub = uint32_t(it >> 1);
@@ -1201,7 +1195,8 @@ __global__ void __launch_bounds__(ws_threads(true)) k_conv_up(ConvArgs a, const 
                                         const int q = (gi == 0 || gi == 2) ? 1 : 0;
                                         const int o = gi == 0 ? 0 : (gi == 3 ? 2 : 1);
                                         const bool two = gi == 1 || gi == 2;
-                                        const uint64_t ad = a0 + uint64_t(((fr * 2 + q) * kTcPlane + o * 16) >> 4);
+                                        const uint64_t ad =
+                                            a0 + uint64_t((uint32_t(q) * kPlaneB + uint32_t(fr * kUpEntries + o) * 16u) >> 4);
                                         const uint64_t bd = (two ? w2 : w1) + wg + uint64_t((up_pre_b(gi) * COUT * 32) >> 4);
                                         mma(col0 + (gi == 3 ? uint32_t(COUT) : 0u), ad, bd,
                                             tc_idesc(kTcPix, two ? 2 * COUT : COUT), 1u);
@@ -1271,7 +1266,7 @@ template <int COUT>
 cudaError_t launch_conv_up(const ConvArgs& ca, const bf16* wup, uint32_t* status, int sm_count, cudaStream_t s) {
     constexpr int kR = up_rows(COUT), kStages = up_stages(COUT);
     constexpr int kCols = 2 * 4 * kR * COUT;
-    constexpr int kThreads = ws_threads(true);
+    constexpr int kThreads = kWsThreads;
     static uint64_t configured = 0;
     static int per_sm = 0;
     const size_t smem = up_smem_bytes<COUT, kR, kStages>();
@@ -1284,10 +1279,12 @@ cudaError_t launch_conv_up(const ConvArgs& ca, const bf16* wup, uint32_t* status
         per_sm = std::max(1, std::min(occ, 512 / kCols));
     }
     if (!ca.ups || ca.cb <= 0 || (ca.h & 1) || (ca.w_ & 1) || ca.ca % 16 || ca.cb % 16) return cudaErrorInvalidValue;
-    CUtensorMap ma;
-    if (!tma_encode(&ma, ca.a, ca.ca, ca.w_ / 2, ca.h / 2, ca.n, kR)) return cudaErrorInvalidValue;
+    CUtensorMap ma, mb;
+    if (!tma_encode(&ma, ca.a, ca.ca, ca.w_ / 2, ca.h / 2, ca.n, kR) ||
+        !tma_encode_box(&mb, ca.b, ca.cb, ca.w_, ca.h, ca.n, 2 * kUpEntries, 2 * kR + 2, 2))
+        return cudaErrorInvalidValue;
     const int tiles = ((ca.w_ / 2 + kUpCols - 1) / kUpCols) * ((ca.h / 2 + kR - 1) / kR) * ca.n;
     const int blocks = std::max(1, std::min(tiles, sm_count * per_sm));
-    k_conv_up<COUT, kR, kStages><<<blocks, kThreads, smem, s>>>(ca, ma, wup, status);
+    k_conv_up<COUT, kR, kStages><<<blocks, kThreads, smem, s>>>(ca, ma, mb, wup, status);
     return cudaGetLastError();
 }
