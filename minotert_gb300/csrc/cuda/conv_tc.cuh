@@ -875,25 +875,28 @@ cudaError_t launch_conv_tc(const ConvArgs& ca, uint32_t* status, cudaStream_t s)
 // copies of each of its pixels (4/9 of the MMAs for A's channels), and the
 // halo of A comes with tensor copies at its own resolution instead of a
 // gather.  A tile is R low-resolution rows x 126 low-resolution columns,
-// i.e. 2R output rows x 252 output columns in four phases (py, px); each
-// phase's accumulator holds 128 lanes = output pixels (2(X0 + i) + px) of
-// one output row (lanes 126, 127 compute beyond the tile and are not
-// stored).  Accumulator blocks are laid out [row r][py][px] x COUT columns,
-// so the two phases px of a row are adjacent and one MMA with N = 2 COUT
-// serves both where they read the same shifted A operand: per (r, py, ry)
-// the column shift s = px + rx takes the values 0 (px 0), 1 (px 0 with
-// rx 1, px 1 with rx 0) and 2 (px 1): three MMAs of N = COUT, 2 COUT, COUT.
+// i.e. 2R output rows x 252 output columns in two column phases px; an
+// accumulator block holds 128 lanes = output pixels (2(X0 + i) + px) of one
+// output row j (lanes 126, 127 compute beyond the tile and are not stored).
+// Blocks are laid out [px][j] x COUT columns so that one MMA serves every
+// output row a halo row feeds (row-stacked along N, as in k_conv_ws): low-
+// resolution halo row t feeds output rows j = 2t - py - 2ry, i.e. 2t - 3
+// .. 2t, and for each (column shift s = px + rx, phase px) — (0,0), (1,0),
+// (1,1), (2,1) — one MMA with the merged weights of those rows stacked.  The
+// blocks are written by overlapping MMAs, so a tile's accumulator is
+// cleared first by one MMA of zero operands.
 // The skip source B at full resolution comes by tensor copies with an
 // element stride of 2 into two planes per row, even and odd pixels (entry e
 // of parity q = pixel 2(X0 - 1 + e) + q; a 256-pixel box loads 128 entries,
 // which cover the 126 columns' taps; lanes 126, 127 read past them into the
 // next row, unused), so that a phase's tap reads consecutive entries; per
-// (r, py, ky) the taps of both phases read four distinct (parity, shift)
-// operands: (1,0) px0 kx0; (0,1) px0 kx1 + px1 kx0; (1,1) px0 kx2 +
-// px1 kx1; (0,2) px1 kx2 — four MMAs of N = COUT, 2 COUT, 2 COUT, COUT with
-// the unmerged tap weights.  Weights per 16-channel slice come from a copy
-// laid out per MMA in that order (k_up_weights; [half][N rows][8]).  Roles,
-// waits and abort handling are those of k_conv_ws.
+// full-resolution halo row fr and member (px, kx) the tap reads plane
+// parity q = (px + kx + 1) & 1 at shift o = (px + kx - 1 - q) / 2 + 1 and
+// feeds output rows fr - 2 .. fr: one MMA with the unmerged weights of
+// taps ky = 2, 1, 0 stacked.  Weights per 16-channel slice come from a copy
+// laid out per MMA (k_up_weights; [half][rows][8]), of which an MMA reads
+// the rows of the output rows inside the tile.  Roles, waits and abort
+// handling are those of k_conv_ws.
 constexpr int kUpCols = 126;    // low-resolution columns of a tile
 constexpr int kUpEntries = 128; // skip-source entries per plane row: one 256-pixel, stride-2 tensor box
 template <int COUT>
@@ -910,21 +913,22 @@ __host__ __device__ constexpr uint32_t up_stage_bytes() {
     const uint32_t b = 2u * up_half_b<R>() + 128u + up_wbytes_b<COUT>();  // 128: the garbage rows' overrun
     return ((a > b ? a : b) + 127u) & ~127u;
 }
+// zero operands of the accumulator-clearing MMA: A (128 x 16) and B (4 R COUT x 16)
+template <int COUT, int R>
+__host__ __device__ constexpr uint32_t up_zero_bytes() { return uint32_t(128 * 32 + 4 * R * COUT * 32); }
 template <int COUT, int R, int STAGES>
 __host__ __device__ constexpr size_t up_smem_bytes() {
-    return size_t(STAGES) * up_stage_bytes<COUT, R>() + size_t(2 * STAGES + 5) * 8 + 32;
+    return size_t(STAGES) * up_stage_bytes<COUT, R>() + up_zero_bytes<COUT, R>() + size_t(2 * STAGES + 5) * 8 + 32;
 }
-// weight rows (in COUT units) before each MMA's block of a slice
-__host__ __device__ constexpr int up_pre_a(int s) { return s == 0 ? 0 : (s == 1 ? 1 : 3); }   // s = 0, 1, 2
-__host__ __device__ constexpr int up_pre_b(int g) { return g == 0 ? 0 : (g == 1 ? 1 : (g == 2 ? 3 : 5)); }
-
 // Per-slice weights of the phase-decomposed form for one layer: slice k of
 // the virtual input (A's channels first) at wup + k * (up_wbytes_b / 2)
-// elements.  A slice: blocks (py, ry, s) in that order, each [half][N][8]
-// with N = COUT x (1, 2, 1) rows for s = 0, 1, 2 (s = 1: the px = 0 rows,
-// then px = 1), merged over the taps of S(py, ry) x S(px, rx) in FP32 and
-// rounded to BF16.  B slice: blocks (ky, g), g = 0..3 as in the kernel, rows
-// the members' unmerged taps.
+// elements.  A slice: four variants v = (shift s, phase px) = (0,0), (1,0),
+// (1,1), (2,1) (rx = s - px), each [half][4 COUT rows][8] with the rows in
+// output-row order of one halo row t: (py, ry) = (1,1), (0,1), (1,0), (0,0)
+// feed output rows 2t - 3 .. 2t; merged over the taps of S(py, ry) x
+// S(px, rx) in FP32 and rounded to BF16.  B slice: six members (px, kx) =
+// (0,0) .. (1,2), each [half][3 COUT rows][8] with ky = 2, 1, 0 (output rows
+// fr - 2 .. fr of full-resolution halo row fr), the unmerged taps.
 __global__ void k_up_weights(const bf16* w16, bf16* wup, int ca, int cb, int cout) {
     const int cin = ca + cb, nk = cin / 16, nka = ca / 16;
     const size_t slice = size_t(18) * cout * 16;  // elements of the larger (B) slice layout
@@ -934,17 +938,13 @@ __global__ void k_up_weights(const bf16* w16, bf16* wup, int ca, int cb, int cou
         int rem = int(i % slice);
         const int c0 = 16 * k;
         if (k < nka) {
-            if (rem >= 16 * cout * 16) continue;  // an A slice uses 16 COUT rows
-            const int blk_rows = 4 * cout;         // rows of one (py, ry) group: s = 0, 1, 2
-            const int grp = rem / (blk_rows * 16);
-            rem %= blk_rows * 16;
-            const int py = grp >> 1, ry = grp & 1;
-            int s = 0, base = 0, nrows = cout;
-            if (rem >= 1 * cout * 16 && rem < 3 * cout * 16) { s = 1; base = cout * 16; nrows = 2 * cout; }
-            else if (rem >= 3 * cout * 16) { s = 2; base = 3 * cout * 16; nrows = cout; }
-            const int e = rem - base;             // [half][nrows][8]
-            const int hf = e / (nrows * 8), row = (e / 8) % nrows, ci = c0 + 8 * hf + (e % 8);
-            const int px = s == 1 ? row / cout : s / 2, co = row % cout, rx = s - px;
+            const int vsize = 4 * cout * 16;  // elements of one variant
+            if (rem >= 4 * vsize) continue;
+            const int v = rem / vsize, e = rem % vsize;
+            const int hf = e / (4 * cout * 8), row = (e / 8) % (4 * cout), ci = c0 + 8 * hf + (e % 8);
+            const int s = v == 0 ? 0 : (v == 3 ? 2 : 1), px = v >= 2 ? 1 : 0, rx = s - px;
+            const int b = row / cout, co = row % cout;
+            const int py = (b == 0 || b == 2) ? 1 : 0, ry = b <= 1 ? 1 : 0;
             const int ky0 = py == 0 ? (ry == 0 ? 0 : 1) : (ry == 0 ? 0 : 2);
             const int ky1 = py == 0 ? (ry == 0 ? 0 : 2) : (ry == 0 ? 1 : 2);
             const int kx0 = px == 0 ? (rx == 0 ? 0 : 1) : (rx == 0 ? 0 : 2);
@@ -955,19 +955,10 @@ __global__ void k_up_weights(const bf16* w16, bf16* wup, int ca, int cb, int cou
                     acc += __bfloat162float(w16[(size_t(co) * 9 + ky * 3 + kx) * cin + ci]);
             wup[i] = __float2bfloat16_rn(acc);
         } else {
-            const int blk_rows = 6 * cout;         // rows of one ky group: g = 0..3
-            const int ky = rem / (blk_rows * 16);
-            rem %= blk_rows * 16;
-            int g, base, nrows;
-            if (rem < cout * 16) { g = 0; base = 0; nrows = cout; }
-            else if (rem < 3 * cout * 16) { g = 1; base = cout * 16; nrows = 2 * cout; }
-            else if (rem < 5 * cout * 16) { g = 2; base = 3 * cout * 16; nrows = 2 * cout; }
-            else { g = 3; base = 5 * cout * 16; nrows = cout; }
-            const int e = rem - base;
-            const int hf = e / (nrows * 8), row = (e / 8) % nrows, ci = c0 + 8 * hf + (e % 8);
-            const int j = row / cout, co = row % cout;
-            // members in px order: g0 (px0 kx0); g1 (px0 kx1, px1 kx0); g2 (px0 kx2, px1 kx1); g3 (px1 kx2)
-            const int kx = g == 0 ? 0 : (g == 3 ? 2 : (g == 1 ? (j == 0 ? 1 : 0) : (j == 0 ? 2 : 1)));
+            const int msize = 3 * cout * 16;  // elements of one member
+            const int m = rem / msize, e = rem % msize;
+            const int hf = e / (3 * cout * 8), row = (e / 8) % (3 * cout), ci = c0 + 8 * hf + (e % 8);
+            const int kx = m % 3, ky = 2 - row / cout, co = row % cout;
             wup[i] = w16[(size_t(co) * 9 + ky * 3 + kx) * cin + ci];
         }
     }
@@ -975,16 +966,16 @@ __global__ void k_up_weights(const bf16* w16, bf16* wup, int ca, int cb, int cou
 
 // Epilogue of the phase-decomposed form: warp w reads TMEM lanes
 // 32w..32w+31 (low-resolution column X0 + i, i = 32w + lane), the 4R
-// accumulator blocks [r][py][px], adds the bias, applies ReLU and stores
-// output pixel (2(Y0 + r) + py, 2(X0 + i) + px) as BF16.
+// accumulator blocks [px][j] (j = output row 2Y0 + j), adds the bias,
+// applies ReLU and stores output pixel (2 Y0 + j, 2(X0 + i) + px) as BF16.
 template <int COUT, int R>
 __device__ __forceinline__ void up_epilogue(const ConvArgs& a, uint32_t taddr, int n, int Y0, int X0, int warp,
                                             int lane) {
     const int i = 32 * warp + lane;
 #pragma unroll
     for (int blk = 0; blk < 4 * R; ++blk) {
-        const int r = blk >> 2, py = (blk >> 1) & 1, px = blk & 1;
-        const int y = 2 * (Y0 + r) + py, x = 2 * (X0 + i) + px;
+        const int px = blk / (2 * R), j = blk % (2 * R);
+        const int y = 2 * Y0 + j, x = 2 * (X0 + i) + px;
         bf16* dst = a.y + ((size_t(n) * a.h + y) * a.w_ + x) * COUT;
 #pragma unroll
         for (int jj = 0; jj < COUT / 16; ++jj) {
@@ -1034,8 +1025,10 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_up(ConvArgs a, const __grid
     constexpr uint32_t kHaloTxB = 4u * kPlaneB;
     constexpr uint32_t kWOffB = 2u * kHalfB + 128u;
     constexpr int kMmaWarp = 5;
+    constexpr uint32_t kZero = up_zero_bytes<COUT, R>();
+    static_assert(kAcc <= 256, "the clearing MMA spans the accumulator with N <= 256");
     extern __shared__ __align__(128) unsigned char tsm[];
-    uint64_t* full = reinterpret_cast<uint64_t*>(tsm + STAGES * kStage);
+    uint64_t* full = reinterpret_cast<uint64_t*>(tsm + STAGES * kStage + kZero);
     uint64_t* empty = full + STAGES;
     uint64_t* acc_full = empty + STAGES;    // [2]
     uint64_t* acc_empty = acc_full + 2;     // [2]
@@ -1070,6 +1063,9 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_up(ConvArgs a, const __grid
         *abort = (*reinterpret_cast<volatile uint32_t*>(status) & MRT_STATUS_PIPE_TIMEOUT) != 0u ? 2u : 0u;
         *consumed = 0u;
     }
+    for (uint32_t i = tid; i < kZero / 16u; i += blockDim.x)
+        reinterpret_cast<uint4*>(tsm + STAGES * kStage)[i] = make_uint4(0u, 0u, 0u, 0u);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the zero operands, for the tensor cores
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -1127,19 +1123,25 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_up(ConvArgs a, const __grid
         if (lane == 0 && *abort == 0u) {
             int g = 0, it = 0;
             bool ok = true, any = false;
-            // stage-0 descriptors: A-source halo, skip halo, weight blocks of
-            // N = COUT and 2 COUT rows (leading byte offset = one K half)
+            // stage-0 descriptors: A-source halo, skip planes, weight
+            // blocks (leading byte offset = one K half of the whole variant /
+            // member block, whose row sub-range an MMA reads)
             const uint64_t da_a = tc_sdesc(smem0, kHalfA, 128), da_b = tc_sdesc(smem0, kHalfB, 128);
-            const uint64_t dw_a1 = tc_sdesc(smem0 + 2u * kHalfA, COUT * 16, 128);
-            const uint64_t dw_a2 = tc_sdesc(smem0 + 2u * kHalfA, 2 * COUT * 16, 128);
-            const uint64_t dw_b1 = tc_sdesc(smem0 + kWOffB, COUT * 16, 128);
-            const uint64_t dw_b2 = tc_sdesc(smem0 + kWOffB, 2 * COUT * 16, 128);
+            const uint64_t dw_a = tc_sdesc(smem0 + 2u * kHalfA, 4 * COUT * 16, 128);
+            const uint64_t dw_b = tc_sdesc(smem0 + kWOffB, 3 * COUT * 16, 128);
+            const uint32_t za = smem0 + uint32_t(STAGES) * kStage;
             for (int tile = blockIdx.x; ok && tile < tiles; tile += gridDim.x, ++it) {
                 const int b = it & 1;
                 const uint32_t ub = uint32_t(it >> 1);
                 if (!ws_wait(smem_u32(acc_empty + b), (ub & 1u) ^ 1u, abort)) { ok = false; break; }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t tacc = taddr + uint32_t(b * kAcc);
+                // the blocks are written by overlapping MMAs: clear them
+                // first (zero A times zero B, N = the whole accumulator)
+                asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, 0;\n" ::"r"(tacc),
+                             "l"(tc_sdesc(za, 128 * 16, 128)), "l"(tc_sdesc(za + 128 * 32, kAcc * 16, 128)),
+                             "r"(tc_idesc(kTcPix, kAcc))
+                             : "memory");
                 for (int k = 0; k < nk; ++k, ++g) {
                     const int s = g % STAGES;
                     const uint32_t u = uint32_t(g / STAGES);
@@ -1150,58 +1152,47 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_up(ConvArgs a, const __grid
                     // only the 14-bit start field changes (no carry: shared
                     // addresses stay below 2^18)
                     const uint64_t so = uint64_t((uint32_t(s) * kStage) >> 4);
-                    auto mma = [&](uint32_t col, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
-                        asm volatile(
-                            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tacc + col),
-                            "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-                            : "memory");
+                    auto mma = [&](int blk0, int nblk, uint64_t ad, uint64_t bd) {
+                        asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, 1;\n" ::"r"(
+                                         tacc + uint32_t(blk0 * COUT)),
+                                     "l"(ad), "l"(bd), "r"(tc_idesc(kTcPix, nblk * COUT))
+                                     : "memory");
                     };
                     if (k < nka) {
-                        const uint64_t a0 = da_a + so, w1 = dw_a1 + so, w2 = dw_a2 + so;
+                        // halo row t feeds output rows 2t - 3 .. 2t (those in the
+                        // tile); per variant (shift, phase) one MMA
+                        const uint64_t a0 = da_a + so, w0 = dw_a + so;
 #pragma unroll
-                        for (int r = 0; r < R; ++r)
+                        for (int t = 0; t < R + 2; ++t) {
+                            const int jlo = 2 * t - 3 < 0 ? 0 : 2 * t - 3, jhi = 2 * t < 2 * R - 1 ? 2 * t : 2 * R - 1;
+                            const uint64_t row = a0 + uint64_t((t * kTcPlane) >> 4);
+                            const uint64_t roff = uint64_t(((jlo - (2 * t - 3)) * COUT * 16) >> 4);
 #pragma unroll
-                            for (int py = 0; py < 2; ++py)
-#pragma unroll
-                                for (int ry = 0; ry < 2; ++ry) {
-                                    const uint64_t row = a0 + uint64_t(((r + py + ry) * kTcPlane) >> 4);
-                                    const uint32_t col0 = uint32_t((r * 2 + py) * 2 * COUT);
-                                    const uint64_t wg = uint64_t(((py * 2 + ry) * 4 * COUT * 32) >> 4);
-                                    // s = 1 first: it covers both phases' blocks and
-                                    // starts them on the first slice
-                                    const uint32_t acc1 = (k > 0 || ry > 0) ? 1u : 0u;
-                                    mma(col0, row + 1u, w2 + wg + uint64_t((up_pre_a(1) * COUT * 32) >> 4),
-                                        tc_idesc(kTcPix, 2 * COUT), acc1);
-                                    mma(col0, row, w1 + wg + uint64_t((up_pre_a(0) * COUT * 32) >> 4),
-                                        tc_idesc(kTcPix, COUT), 1u);
-                                    mma(col0 + uint32_t(COUT), row + 2u,
-                                        w1 + wg + uint64_t((up_pre_a(2) * COUT * 32) >> 4), tc_idesc(kTcPix, COUT), 1u);
-                                }
+                            for (int v = 0; v < 4; ++v) {
+                                const int sh = v == 0 ? 0 : (v == 3 ? 2 : 1), px = v >= 2 ? 1 : 0;
+                                mma(px * 2 * R + jlo, jhi - jlo + 1, row + uint64_t(sh),
+                                    w0 + uint64_t((v * 4 * COUT * 32) >> 4) + roff);
+                            }
+                        }
                     } else {
-                        const uint64_t a0 = da_b + so, w1 = dw_b1 + so, w2 = dw_b2 + so;
+                        // full-resolution halo row fr feeds output rows fr - 2 .. fr;
+                        // per member (phase, tap column) one MMA on its (parity,
+                        // shift) plane
+                        const uint64_t a0 = da_b + so, w0 = dw_b + so;
 #pragma unroll
-                        for (int r = 0; r < R; ++r)
+                        for (int fr = 0; fr < 2 * R + 2; ++fr) {
+                            const int jlo = fr - 2 < 0 ? 0 : fr - 2, jhi = fr < 2 * R - 1 ? fr : 2 * R - 1;
+                            const uint64_t roff = uint64_t(((jlo - (fr - 2)) * COUT * 16) >> 4);
 #pragma unroll
-                            for (int py = 0; py < 2; ++py)
-#pragma unroll
-                                for (int ky = 0; ky < 3; ++ky) {
-                                    const int fr = 2 * r + py + ky;
-                                    const uint32_t col0 = uint32_t((r * 2 + py) * 2 * COUT);
-                                    const uint64_t wg = uint64_t((ky * 6 * COUT * 32) >> 4);
-                                    // (parity, shift) per group: (1,0) (0,1) (1,1) (0,2)
-#pragma unroll
-                                    for (int gi = 0; gi < 4; ++gi) {
-                                        const int q = (gi == 0 || gi == 2) ? 1 : 0;
-                                        const int o = gi == 0 ? 0 : (gi == 3 ? 2 : 1);
-                                        const bool two = gi == 1 || gi == 2;
-                                        const uint64_t ad =
-                                            a0 + uint64_t((uint32_t(q) * kPlaneB + uint32_t(fr * kUpEntries + o) * 16u) >> 4);
-                                        const uint64_t bd = (two ? w2 : w1) + wg + uint64_t((up_pre_b(gi) * COUT * 32) >> 4);
-                                        mma(col0 + (gi == 3 ? uint32_t(COUT) : 0u), ad, bd,
-                                            tc_idesc(kTcPix, two ? 2 * COUT : COUT), 1u);
-                                    }
-                                }
+                            for (int m = 0; m < 6; ++m) {
+                                const int px = m / 3, kx = m % 3;
+                                const int q = (px + kx + 1) & 1, o = (px + kx - 1 - q) / 2 + 1;
+                                const uint64_t ad =
+                                    a0 + uint64_t((uint32_t(q) * kPlaneB + uint32_t(fr * kUpEntries + o) * 16u) >> 4);
+                                mma(px * 2 * R + jlo, jhi - jlo + 1, ad,
+                                    w0 + uint64_t((m * 2 * 3 * COUT * 16) >> 4) + roff);
+                            }
+                        }
                     }
                     any = true;
                     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
