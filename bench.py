@@ -798,14 +798,18 @@ def run_cache_experiment(args, world, rank, local, dist):
         ctx.frame_stats()
         run(k, 50000, fn(False, True))
         st_frozen = ctx.frame_stats()
-        run(k, 60000, fn(True, True))
+        _, ms_t, _ = run(k, 60000, fn(True, True))
         st_train = ctx.frame_stats()
         ctx.set_timing(False)
         cache.close()
+        # ms_train is the training's own span (paths + Adam steps; on the
+        # context's second stream it overlaps the frame's tracing), and
+        # ms_train_added what it adds to a frame: trained minus frozen frame
         return {"mse_single_frame": mse1, "var_per_frame": var, "bias_rmse": float(np.sqrt(bias2)),
                 "ms_frame_frozen": float(ms_k[-1] / k), "ms_infer": st_frozen.ms_cache_infer / k,
                 "ms_trace_only": (float(ms_k[-1]) - st_frozen.ms_cache_infer) / k,
-                "ms_train": st_train.ms_cache_train / k}
+                "ms_train": st_train.ms_cache_train / k, "ms_frame_trained": float(ms_t[-1] / k),
+                "ms_train_added": float(ms_t[-1] - ms_k[-1]) / k}
 
     # plain: single-frame MSE (no bias) from k independent frames
     plain_single = []

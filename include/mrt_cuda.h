@@ -461,9 +461,16 @@ int mrt_cuda_cache_set_bounds(mrt_ctx* ctx, mrt_cache* cache, const float lo[3],
  * tensor-core wait that runs out sets MRT_STATUS_PIPE_TIMEOUT. */
 int mrt_cuda_cache_infer(mrt_ctx* ctx, mrt_cache* cache, const float* queries, uint32_t n,
                          float* out, void* stream);
-/* enable = 0: inference on mma.sync instead (the earlier kernel, kept for
- * comparison); 1 (default): tcgen05. */
+/* enable = 0: inference and training on mma.sync instead (the earlier
+ * kernels, kept for comparison); 1 (default): tcgen05 (training: the
+ * forward writes each 128-row tile's activations, the backward accumulates
+ * the weight gradients of its tiles in tensor memory and scatters the hash
+ * grid's gradients from its last epilogue). */
 int mrt_cuda_cache_set_tcgen05(mrt_cache* cache, int enable);
+/* enable = 1 (default): mrt_cuda_cache_frame trains on the context's
+ * second stream while the frame's rays are traced, joined before the cache
+ * is queried (same image); 0: training first, on the caller's stream. */
+int mrt_cuda_cache_set_overlap(mrt_cache* cache, int enable);
 /* One training step on n device samples (queries + 3-float targets; n is
  * rounded down to a multiple of 16): forward, loss, backward; with
  * apply_update an Adam step (gradients are cleared), otherwise gradients
@@ -475,7 +482,9 @@ int mrt_cuda_cache_train_step(mrt_ctx* ctx, mrt_cache* cache, const float* queri
 /* Host copies of parameters and gradients: which = 0 MLP weights (17408
  * FP32: 4 layers of 64x64 [out][in], then 16x64 output rows), 1 their
  * gradients, 2 grid features (16 * 2^log2_table * 2 FP32), 3 their
- * gradients.  set != 0 writes host -> device (and refreshes FP16 copies). */
+ * gradients.  set != 0 writes host -> device (and refreshes FP16 copies;
+ * setting the grid gradients also marks their nonzero entries for the
+ * grid's next Adam step, which updates only entries with a gradient). */
 int mrt_cuda_cache_params(mrt_ctx* ctx, mrt_cache* cache, int which, float* host,
                           size_t count, int set);
 /* One frame of cache-terminated path tracing (replaces the secondary pass):

@@ -198,6 +198,7 @@ def lib() -> C.CDLL:
             "mrt_cuda_denoiser_param_count": ([vp, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)], i32),
             "mrt_cuda_denoiser_set_tcgen05": ([vp, i32], i32),
             "mrt_cuda_cache_set_tcgen05": ([vp, i32], i32),
+            "mrt_cuda_cache_set_overlap": ([vp, i32], i32),
             "mrt_cuda_denoiser_features": ([vp, vp, C.POINTER(GBuffer), vp, C.c_float, vp, vp], i32),
             "mrt_cuda_denoiser_infer": ([vp, vp, vp, u32, u32, u32, vp, vp], i32),
             "mrt_cuda_denoiser_train_step": ([vp, vp, vp, vp, u32, u32, u32, C.c_float, i32, C.POINTER(C.c_float),

@@ -46,8 +46,13 @@ class RadianceCache:
         self.ctx.check(lib().mrt_cuda_cache_set_bounds(self.ctx.handle, self._h, lo, hi), "cache_set_bounds")
 
     def set_tcgen05(self, enable: bool):
-        """Inference on tcgen05 (default) or on the mma.sync kernel."""
+        """Inference and training on tcgen05 (default) or on the mma.sync kernels."""
         self.ctx.check(lib().mrt_cuda_cache_set_tcgen05(self._h, int(enable)), "cache_set_tcgen05")
+
+    def set_overlap(self, enable: bool):
+        """frame(): train on the context's second stream while the frame's rays
+        are traced (default), or first, on the caller's stream."""
+        self.ctx.check(lib().mrt_cuda_cache_set_overlap(self._h, int(enable)), "cache_set_overlap")
 
     def infer(self, d_queries, n: int, d_out, stream=None):
         self.ctx.check(lib().mrt_cuda_cache_infer(self.ctx.handle, self._h, ptr(d_queries), n, ptr(d_out),

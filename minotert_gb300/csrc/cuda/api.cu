@@ -775,11 +775,25 @@ int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
     tp.atmo = sky_dev(ctx->sky, consts->camera_pos);
     const BlueNoise bn{ctx->d_bn, ctx->bn_w, ctx->bn_h};
     Scope total(ctx, s, 5, 0);
+    // Training (its own paths, then the Adam steps) needs nothing of this
+    // frame's rays and the rays need nothing of the cache until it is
+    // queried: with overlap the training goes to the context's side stream
+    // and the main stream waits for it just before the query is answered,
+    // so the latency-bound training kernels and the ray tracing fill each
+    // other's idle SMs.  Same image.
+    const bool overlap_train = train && cache_overlap_training(cache);
     if (train) {
-        Scope sc(ctx, s, 6, 0);
-        rc = cache_train_frame(ctx, cache, scene->dev, fp, tp, ctx->d_status, s);
+        cudaStream_t ts = s;
+        if (overlap_train) {
+            MRT_CK(cudaEventRecord(ctx->ev_fork, s));
+            MRT_CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+            ts = ctx->side;
+        }
+        Scope sc(ctx, ts, 6, 0);
+        rc = cache_train_frame(ctx, cache, scene->dev, fp, tp, ctx->d_status, ts);
         if (rc) return rc;
     }
+    if (overlap_train) MRT_CK(cudaEventRecord(ctx->ev_join, ctx->side));
     rc = ensure_wave(ctx, size_t(W) * H);
     if (rc) return rc;
     WaveBuffers& wb = ctx->wb;
@@ -809,6 +823,7 @@ int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
                                                  refill_min(ctx), s));
         const uint32_t npix = W * H;
         MRT_LAUNCH(3, 0, launch_cache_query_primary(scene->dev, fp, *gbuffer, q, pb, ctx->d_status, s));
+        if (overlap_train) MRT_CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
         MRT_LAUNCH(7, 0, cache_infer(cache, q, npix, nullptr, pred, ctx->d_status, s));
         MRT_LAUNCH(3, 0, launch_cache_apply(wb, nullptr, npix, pred, pb, s));
     } else {
@@ -825,6 +840,7 @@ int mrt_cuda_cache_frame(mrt_ctx* ctx, mrt_cache* cache, const mrt_scene* scene,
             MRT_LAUNCH(2, 1, launch_trace_shadow(scene->dev, wb, tp, 1, tblocks, ctx->d_status, ctx->counters, dyn_sh,
                                                  refill_min(ctx), s));
         MRT_LAUNCH(3, 1, launch_cache_query(scene->dev, tp, wb, q, pb, ctx->d_status, s));
+        if (overlap_train) MRT_CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
         MRT_LAUNCH(7, 1, cache_infer(cache, q, uint32_t(wb.cap), wb.counters + kCntExt + 1, pred, ctx->d_status, s));
         MRT_LAUNCH(3, 1, launch_cache_apply(wb, wb.counters + kCntExt + 1, uint32_t(wb.cap), pred, pb, s));
     }

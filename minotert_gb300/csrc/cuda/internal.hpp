@@ -194,6 +194,7 @@ cudaError_t launch_cache_query_primary(const DevScene& sc, const FrameParams& fp
 cudaError_t launch_cache_apply(const WaveBuffers& wb, const uint32_t* n_dev, uint32_t n_max, const float* pred,
                                const float4* pb, cudaStream_t s);
 uint32_t cache_query_vertex(const mrt_cache* c);  // nrc.cu
+bool cache_overlap_training(const mrt_cache* c);  // nrc.cu
 
 int trace_blocks_per_sm();  // occupancy of the traversal kernels
 

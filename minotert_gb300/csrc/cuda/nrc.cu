@@ -10,12 +10,15 @@
 // Network: input 64 halves = 32 hash features (16 levels x 2) + normal (3)
 // + direction (3) + zero padding; 4 hidden layers of width 64 with ReLU,
 // no biases; a linear output of 3 (padded to 16 rows of weights).  FP16
-// weights and activations, FP32 accumulation, on the tensor cores through
-// mma.sync.m16n8k16: a warp owns 16 rows, and the FP32 accumulator tiles of
-// one layer (16 x 64) are, element for element, the A fragments of the next
-// layer's product after packing to half2, so activations stay in registers.
-// Weight gradients are FP32 sums over rows on the CUDA cores; the grid's
-// gradients are FP32 atomics; Adam keeps FP32 master weights.
+// weights and activations, FP32 accumulation.  By default inference, the
+// training forward and the backward run on the 5th-generation tensor cores
+// (tcgen05: 128-row tiles, accumulators and the weight-gradient sums in
+// tensor memory; k_cache_fwd_tc, k_cache_bwd_tc).  The earlier mma.sync
+// kernels stay selectable for comparison: there a warp owns 16 rows, and
+// the FP32 accumulator tiles of one layer (16 x 64) are, element for
+// element, the A fragments of the next layer's product after packing to
+// half2.  The grid's gradients are FP32 atomics; Adam keeps FP32 master
+// weights.
 #include "internal.hpp"
 #include "tcgen05.cuh"
 
@@ -244,6 +247,7 @@ struct CacheDev {
     const __half2* grid;  // levels * 2^log2_t entries of 2 features
     const __half* W;      // kWeights halves (hidden layers, then output rows)
     const __half* WT;     // transposes of the hidden layers + output ([in][out], 64 x 16)
+    const __half* Wimg;   // the weights in the tcgen05 kernels' shared-memory layout (wimg_off)
     float lo[3], inv_ext[3];
 };
 
@@ -260,6 +264,7 @@ k_cache_infer(CacheDev c, const float* q, uint32_t n_max, const uint32_t* n_dev,
     __half* sX = sW + kWeights;  // kMlpWarps x 16 x 64
     float* sO = reinterpret_cast<float*>(sX + kMlpWarps * 16 * kWidth);  // kMlpWarps x 16 x 3
     const uint32_t n = n_dev ? min(*n_dev, n_max) : n_max;
+    if (blockIdx.x * kMlpWarps * 16u >= n) return;  // no rows for this block
     load_weights_smem(sW, c.W, kWeights);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = lane_id();
@@ -310,19 +315,21 @@ __host__ __device__ constexpr uint32_t mlp_idesc(int m, int n) {
     return (1u << 4) | (uint32_t(n >> 3) << 17) | (uint32_t(m >> 4) << 24);
 }
 
-// The weights (row-major [out][64] halves, hidden layers then the output
-// rows) into the K-plane layout: hidden layer l at l * 8 KB, plane kc of it
-// holding element 8 kc .. 8 kc + 7 of its 64 rows; the output layer after
-// them with planes of 16 rows.
-__device__ void tc_load_weights(const __half* W, unsigned char* sW) {
-    for (int i = threadIdx.x; i < (kHidden * kWidth + kOutRows) * (kWidth / 8); i += blockDim.x) {
-        const int kc = i % (kWidth / 8), row = i / (kWidth / 8);  // row over all layers' output rows
-        const int l = row / kWidth, n = row % kWidth;
-        const uint4 v = *reinterpret_cast<const uint4*>(W + size_t(row) * kWidth + kc * 8);
-        const int off = l < kHidden ? l * kTcLayerB + kc * (kWidth * 16) + n * 16
-                                    : kHidden * kTcLayerB + kc * (kOutRows * 16) + (row - kHidden * kWidth) * 16;
-        *reinterpret_cast<uint4*>(sW + off) = v;
-    }
+// Byte offset of weight (layer L, output row o, input i) in the K-plane
+// layout the tcgen05 kernels keep in shared memory: hidden layer L at
+// L * 8 KB, plane i / 8 of it holding inputs 8 (i / 8) .. + 7 of its 64 rows
+// (16 bytes a row); the output layer after them with planes of 16 rows.
+// Adam writes this image beside the FP16 weights, so a CTA fetches it with
+// one bulk copy.
+__host__ __device__ constexpr uint32_t wimg_off(int L, int o, int i) {
+    return L < kHidden ? uint32_t(L * kTcLayerB + (i / 8) * (kWidth * 16) + o * 16 + (i % 8) * 2)
+                       : uint32_t(kHidden * kTcLayerB + (i / 8) * (kOutRows * 16) + o * 16 + (i % 8) * 2);
+}
+
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t mb) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(mb)
+                 : "memory");
 }
 
 __device__ __forceinline__ void tc_tmem_ld16(uint32_t taddr, uint32_t v[16]) {
@@ -333,16 +340,61 @@ __device__ __forceinline__ void tc_tmem_ld16(uint32_t taddr, uint32_t v[16]) {
         : "r"(taddr));
 }
 
+// Training outputs of the tcgen05 forward: per 128-row tile, the five
+// 16 KB shared-memory images of the layers' A operands (the encoded input
+// rows, then the hidden activations after ReLU, in the K-plane layout
+// above) and the 4 KB image of dL/dy (16 FP16 columns, 3 used, scaled by
+// kGradScale), which are what the tcgen05 backward reads; plus the loss.
+constexpr int kImg = kTcRows * kWidth * 2;       // 16 KB: one tile's 64 FP16 columns
+constexpr int kDyImg = kTcRows * kOutRows * 2;   // 4 KB: one tile's dL/dy
+constexpr int kImgs = kHidden + 1;               // images per tile: input rows, 4 hidden layers
+struct TrainTc {
+    const float* target;  // rows x 3
+    uint4* img;           // tiles x kImgs x kImg bytes
+    uint4* dy;            // tiles x kDyImg bytes
+    float* loss_acc;
+};
+
+// Rows of a training step: the whole buffer (slice == null: rows
+// [0, n_max)) or the device-side slice {first row, count} that a frame's
+// training step takes from the samples its paths produced.
+struct Rows {
+    uint32_t off, n;
+};
+__device__ __forceinline__ Rows rows_of(const uint32_t* slice, uint32_t n_max) {
+    return slice ? Rows{slice[0], min(slice[1], n_max)} : Rows{0u, n_max};
+}
+
+// Inference (kTrain = false: n_dev, when set, holds the query count) and
+// the training forward (kTrain = true: n_dev, when set, is a training
+// slice {first row, count}; the tile images and dL/dy are written instead
+// of the outputs).
+template <bool kTrain>
 __global__ void __launch_bounds__(kTcThreads)
-k_cache_infer_tc(CacheDev c, const float* q, uint32_t n_max, const uint32_t* n_dev, float* out, uint32_t* status) {
+k_cache_fwd_tc(CacheDev c, const float* q, uint32_t n_max, const uint32_t* n_dev, float* out, uint32_t* status,
+               TrainTc tr) {
     extern __shared__ __align__(128) unsigned char tsm[];
     unsigned char* sW = tsm;
     unsigned char* sA = tsm + kTcWBytes;
     uint64_t* mbar = reinterpret_cast<uint64_t*>(sA + (kWidth / 8) * kTcPlaneA);
     uint32_t* slot = reinterpret_cast<uint32_t*>(mbar + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t n = n_dev ? min(*n_dev, n_max) : n_max;
+    uint32_t n;
+    if (kTrain) {
+        const Rows rs = rows_of(n_dev, n_max);
+        n = rs.n;
+        q += size_t(rs.off) * 9;
+        tr.target += size_t(rs.off) * 3;
+    } else {
+        n = n_dev ? min(*n_dev, n_max) : n_max;
+    }
     const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
+    // grids are sized by the capacity; with a device-side count the CTAs
+    // past the last tile leave before loading weights or taking tensor
+    // memory (uniform over the CTA)
+    if (blockIdx.x >= tiles) return;
+    const float dy_scale = kTrain ? kGradScale / float(max(n, 1u)) : 0.0f;
+    float loss = 0.0f;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
@@ -350,12 +402,17 @@ k_cache_infer_tc(CacheDev c, const float* q, uint32_t n_max, const uint32_t* n_d
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
+    uint64_t* wbar = mbar + 2;  // the weights' bulk copy
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(wbar)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        // the weights come in while the first tile is encoded
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(wbar)),
+                     "r"(uint32_t(kTcWBytes))
+                     : "memory");
+        bulk_load(smem_u32(sW), c.Wimg, kTcWBytes, smem_u32(wbar));
     }
-    tc_load_weights(c.W, sW);
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -363,7 +420,8 @@ k_cache_infer_tc(CacheDev c, const float* q, uint32_t n_max, const uint32_t* n_d
     const uint32_t a0 = smem_u32(sA), w0 = smem_u32(sW), mb = smem_u32(mbar);
     uint32_t phase = 0u;
     bool timed_out = false;
-    bool pending = false;  // a commit not yet seen complete
+    bool pending = false;   // a commit not yet seen complete
+    bool w_wait = true;     // the weights' copy not yet seen complete
 
     const int r = tid & (kTcRows - 1), half = tid >> 7;  // encoding: row, half of the levels
     const int quad = warp & 3, ch = warp >> 2;           // epilogue: TMEM lane quadrant, column half
@@ -407,7 +465,23 @@ k_cache_infer_tc(CacheDev c, const float* q, uint32_t n_max, const uint32_t* n_d
             // the tile's A operand is in shared memory: hand it to the tensor cores
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            __syncthreads();
+            if (w_wait) {  // first product of the launch: the weights must have landed
+                const bool wok = tid != 0 || tc_wait(smem_u32(wbar), 0u);
+                if (__syncthreads_or(!wok)) {
+                    timed_out = true;
+                    if (tid == 0) atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
+                    break;
+                }
+                w_wait = false;
+            } else {
+                __syncthreads();
+            }
+            if (kTrain) {  // the operand image goes out for the backward (read while the MMAs read it too)
+                uint4* dst = tr.img + (size_t(tile) * kImgs + size_t(L)) * (kImg / 16);
+                const uint4* src = reinterpret_cast<const uint4*>(sA);
+#pragma unroll
+                for (int i = 0; i < kImg / 16 / kTcThreads; ++i) dst[tid + i * kTcThreads] = src[tid + i * kTcThreads];
+            }
             if (tid == 0) {
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t wb = w0 + uint32_t(L * kTcLayerB);
@@ -459,14 +533,37 @@ k_cache_infer_tc(CacheDev c, const float* q, uint32_t n_max, const uint32_t* n_d
                 tc_tmem_ld16(taddr + (uint32_t(32 * quad) << 16), v);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 const uint32_t orow = tile * kTcRows + uint32_t(er);
-                if (orow < n)
-                    for (int k = 0; k < 3; ++k) out[size_t(orow) * 3 + k] = __uint_as_float(v[k]);
+                if (!kTrain) {
+                    if (orow < n)
+                        for (int k = 0; k < 3; ++k) out[size_t(orow) * 3 + k] = __uint_as_float(v[k]);
+                } else {
+                    // relative L2 loss L = mean_r sum_k (y - t)^2 / (sg(y)^2 + 0.01) and
+                    // dL/dy (scaled by kGradScale so the FP16 operands of the
+                    // backward stay out of the subnormal range); zero past n
+                    float dy[3] = {0.0f, 0.0f, 0.0f};
+                    if (orow < n) {
+                        for (int k = 0; k < 3; ++k) {
+                            const float y = __uint_as_float(v[k]), t = tr.target[size_t(orow) * 3 + k];
+                            const float den = y * y + 0.01f;
+                            loss += (y - t) * (y - t) / den;
+                            dy[k] = 2.0f * (y - t) / den * dy_scale;
+                        }
+                    }
+                    uint4* d = tr.dy + size_t(tile) * (kDyImg / 16);
+                    d[er] = make_uint4(pack_half2(dy[0], dy[1]), pack_half2(dy[2], 0.0f), 0u, 0u);
+                    d[kTcRows + er] = make_uint4(0u, 0u, 0u, 0u);
+                }
             }
         }
     }
-    // a commit still outstanding after a timeout: wait for it (bounded)
-    // before the tensor memory is freed
+    if (kTrain) {
+        for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xFFFFFFFFu, loss, o);
+        if (lane == 0 && loss != 0.0f) atomicAdd(tr.loss_acc, loss);
+    }
+    // a commit or the weights' copy still outstanding after a timeout: wait
+    // for it (bounded) before the tensor memory and shared memory are freed
     if (pending && !tc_wait(mb, phase)) atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
+    if (w_wait && tid == 0 && !tc_wait(smem_u32(wbar), 0u)) atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0)
@@ -474,14 +571,310 @@ k_cache_infer_tc(CacheDev c, const float* q, uint32_t n_max, const uint32_t* n_d
                      : "memory");
 }
 
+// Training state of one hash-grid entry, one 32-byte sector: FP32 master
+// features, Adam moments and the gradient, so that the grid's Adam step
+// reads and writes one sector per entry it updates (the FP16 features the
+// encodings gather stay in their own compact table).
+struct __align__(32) GridEntry {
+    float2 p, m, v, g;
+};
+static_assert(sizeof(GridEntry) == 32, "one sector per grid entry");
+
+// Adds (a0, a1) to grid entry e's gradient and marks the entry in the
+// touched bitmap (bit e) for the grid's Adam step (k_adam_grid).
+__device__ __forceinline__ void grid_grad_add(GridEntry* gs, uint32_t* touched, uint32_t e, float a0, float a1) {
+    if (a0 == 0.0f && a1 == 0.0f) return;
+    atomicAdd(&gs[e].g, make_float2(a0, a1));
+    atomicOr(touched + (e >> 5), 1u << (e & 31u));
+}
+
+// ------------------------------------------- training backward on tcgen05
+//
+// One CTA of 256 threads (two per SM) per run of 128-row tiles.  A tile
+// takes five phases from the output layer down; phase p works on the layer
+// whose output gradient dZ (FP16, scaled by kGradScale) sits in shared
+// memory as a K-plane image:
+//   dW += dZ^T H  M = 128 over the layer's outputs, N = 64 inputs, K = the
+//                 tile's 128 rows: 8 MMAs, both operands MN-major (the
+//                 K-plane images read along their rows);
+//   dH  = dZ W    M = 128 rows, N = 64, K = the layer's outputs: 4 MMAs (1
+//                 for the output layer), W read MN-major from the layout
+//                 the forward reads K-major;
+// then the epilogue writes the next dZ = dH where the layer's input H > 0
+// (ReLU), or, below the first layer, scatters dL/d(encoded features) into
+// the hash grid's gradients.  H is the layer's input image written by the
+// forward, brought in by a bulk copy as soon as the previous phase's MMAs
+// are done with the buffer; the epilogue reads its ReLU mask from the same
+// image in global memory.  The weight gradients of all the CTA's tiles
+// accumulate in tensor memory and are added to the FP32 gradients once.
+// Tensor memory, 256 columns: [0, 64) dH; [64, 128) dW of hidden layer 3
+// (lanes 0-63) and 2 (lanes 64-127); [128, 192) dW of layers 1 and 0;
+// [192, 256) dW of the output layer (lanes 0-15).  Two layers share columns
+// by lanes: the 128 A rows of the dW product are [dZ ; zeros] for the lower
+// layer and [zeros ; dZ] for the upper one, so each adds exactly zero to
+// the other's lanes.  Shared memory holds dZ1 | 16 KB of zeros | dZ2, and
+// the phases alternate between dZ1 (lower) and dZ2 (upper).
+constexpr int kBwThreads = 256;
+constexpr uint32_t kBwCols = 256;
+constexpr int kBwDy = 0;                      // dL/dy image; the weights follow it
+constexpr int kBwW = kBwDy + kDyImg;
+constexpr int kBwD1 = kBwW + kTcWBytes;       // dZ of phases 1 and 3 (lower lanes)
+constexpr int kBwZ = kBwD1 + kImg;            // zeros
+constexpr int kBwD2 = kBwZ + kImg;            // dZ of phases 2 and 4 (upper lanes)
+constexpr int kBwH = kBwD2 + kImg;            // the phase's layer input H
+constexpr int kBwBar = kBwH + kImg;
+constexpr int kBwSmem = kBwBar + 64;
+// The output layer's dW product reads 128 A rows of which the first 16 are
+// dL/dy: the other 14 row groups (2 KB apart) fall on the weights.
+static_assert(kBwDy + 16 * kTcPlaneA <= kBwD1, "the output layer's dW rows stay inside the weights");
+static_assert(2 * (kBwSmem + 1024) <= 228 * 1024, "two CTAs per SM");
+
+__device__ __forceinline__ void bw_load(uint32_t s0, uint32_t mb, const uint4* img, const uint4* dyimg, uint32_t tile,
+                                        int p, const __half* wimg = nullptr) {
+    const uint32_t bytes = (p == 0 ? uint32_t(kImg + kDyImg) : uint32_t(kImg)) + (wimg ? uint32_t(kTcWBytes) : 0u);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
+    if (wimg) bulk_load(s0 + uint32_t(kBwW), wimg, kTcWBytes, mb);
+    if (p == 0)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         s0 + uint32_t(kBwDy)),
+                     "l"(dyimg + size_t(tile) * (kDyImg / 16)), "r"(uint32_t(kDyImg)), "r"(mb)
+                     : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     s0 + uint32_t(kBwH)),
+                 "l"(img + (size_t(tile) * kImgs + size_t(kHidden - p)) * (kImg / 16)), "r"(uint32_t(kImg)), "r"(mb)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bw_mma(uint32_t d, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__global__ void __launch_bounds__(kBwThreads)
+k_cache_bwd_tc(CacheDev c, const float* q, uint32_t n_max, const uint32_t* slice, const uint4* img,
+               const uint4* dyimg, float* gW, GridEntry* gs, uint32_t* touched, uint32_t* status) {
+    extern __shared__ __align__(128) unsigned char bsm[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(bsm + kBwBar);  // [0] bulk loads, [1] MMAs
+    uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const Rows rs = rows_of(slice, n_max);
+    const uint32_t n = rs.n;
+    q += size_t(rs.off) * 9;
+    const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
+    if (blockIdx.x >= tiles) return;  // uniform over the CTA, before any allocation
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                     "r"(kBwCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar + 1)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int i = tid; i < kImg / 16; i += kBwThreads) reinterpret_cast<uint4*>(bsm + kBwZ)[i] = make_uint4(0, 0, 0, 0);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = *slot, s0 = smem_u32(bsm), mb_ld = smem_u32(bar), mb_mma = smem_u32(bar + 1);
+    uint32_t ld_phase = 0u, mma_phase = 0u;
+    bool ld_pending = false, mma_pending = false, failed = false, first = true;
+    const int quad = warp & 3, ch = warp >> 2, er = 32 * quad + lane;
+    constexpr uint32_t idesc_w = mlp_idesc(kTcRows, kWidth) | (1u << 15) | (1u << 16);  // A, B MN-major
+    constexpr uint32_t idesc_x = mlp_idesc(kTcRows, kWidth) | (1u << 16);               // B MN-major
+    if (tid == 0) {  // the weights come with the first tile's images
+        bw_load(s0, mb_ld, img, dyimg, blockIdx.x, 0, c.Wimg);
+        ld_pending = true;
+    }
+    for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
+        const uint32_t row = tile * kTcRows + uint32_t(er);
+        const bool valid = row < n;
+        float px = 0.0f, py = 0.0f, pz = 0.0f;
+        if (valid) {
+            px = fminf(fmaxf(q[size_t(row) * 9 + 0], 0.0f), 1.0f);
+            py = fminf(fmaxf(q[size_t(row) * 9 + 1], 0.0f), 1.0f);
+            pz = fminf(fmaxf(q[size_t(row) * 9 + 2], 0.0f), 1.0f);
+        }
+        for (int p = 0; p <= kHidden; ++p) {
+            // this thread's ReLU mask: row er, columns 32 ch .. 32 ch + 31 of H
+            uint4 hm[4];
+            if (p < kHidden) {
+                const uint4* h = img + (size_t(tile) * kImgs + size_t(kHidden - p)) * (kImg / 16);
+#pragma unroll
+                for (int pl = 0; pl < 4; ++pl) hm[pl] = h[(4 * ch + pl) * kTcRows + er];
+            }
+            bool ok = true;
+            if (tid == 0) {
+                ok = tc_wait(mb_ld, ld_phase);
+                if (ok) {
+                    ld_phase ^= 1u;
+                    ld_pending = false;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    // phase p's dZ: dL/dy, then dZ1 / dZ2 alternately
+                    const bool upper = p == 2 || p == 4;
+                    const uint32_t dz = p == 0 ? s0 + kBwDy : (p & 1) ? s0 + kBwD1 : s0 + kBwD2;
+                    const uint32_t a_dw = upper ? s0 + kBwZ : dz;
+                    const uint32_t col = p == 0 ? 192u : p <= 2 ? 64u : 128u;
+                    const bool clears = first && !upper;  // the column range's first product this launch
+#pragma unroll
+                    for (int k = 0; k < kTcRows / 16; ++k)
+                        bw_mma(taddr + col, tc_sdesc(a_dw + 256u * k, 128, kTcPlaneA),
+                               tc_sdesc(s0 + kBwH + 256u * k, 128, kTcPlaneA), idesc_w,
+                               uint32_t(k > 0 || !clears));
+                    if (p == 0) {
+                        bw_mma(taddr, tc_sdesc(dz, kTcPlaneA, 128),
+                               tc_sdesc(s0 + kBwW + kHidden * kTcLayerB, 128, kOutRows * 16), idesc_x, 0u);
+                    } else {
+                        const uint32_t wl = s0 + kBwW + uint32_t(kHidden - p) * kTcLayerB;
+#pragma unroll
+                        for (int k = 0; k < kWidth / 16; ++k)
+                            bw_mma(taddr, tc_sdesc(dz + 2u * k * kTcPlaneA, kTcPlaneA, 128),
+                                   tc_sdesc(wl + 256u * k, 128, kWidth * 16), idesc_x, uint32_t(k > 0));
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                     mb_mma)
+                                 : "memory");
+                }
+            }
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            mma_pending = true;
+            const bool ok2 = tc_wait(mb_mma, mma_phase);
+            if (ok2) {
+                mma_phase ^= 1u;
+                mma_pending = false;
+            }
+            if (__syncthreads_or(!ok2)) {
+                failed = true;
+                break;
+            }
+            // the MMAs are done with H (and dL/dy): the next image comes in
+            if (tid == 0) {
+                if (p < kHidden) {
+                    bw_load(s0, mb_ld, img, dyimg, tile, p + 1);
+                    ld_pending = true;
+                } else if (tile + gridDim.x < tiles) {
+                    bw_load(s0, mb_ld, img, dyimg, tile + gridDim.x, 0);
+                    ld_pending = true;
+                }
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (p < kHidden) {
+                uint32_t v[32];
+                const uint32_t ta = taddr + (uint32_t(32 * quad) << 16) + uint32_t(32 * ch);
+                tc_tmem_ld16(ta, v);
+                tc_tmem_ld16(ta + 16u, v + 16);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                unsigned char* dst = bsm + ((p & 1) ? kBwD2 : kBwD1);
+#pragma unroll
+                for (int pl = 0; pl < 4; ++pl) {
+                    const uint32_t hw[4] = {hm[pl].x, hm[pl].y, hm[pl].z, hm[pl].w};
+                    uint32_t h[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const float h0 = __half2float(__ushort_as_half(uint16_t(hw[e] & 0xFFFFu))),
+                                    h1 = __half2float(__ushort_as_half(uint16_t(hw[e] >> 16)));
+                        h[e] = pack_half2(h0 > 0.0f ? __uint_as_float(v[8 * pl + 2 * e]) : 0.0f,
+                                          h1 > 0.0f ? __uint_as_float(v[8 * pl + 2 * e + 1]) : 0.0f);
+                    }
+                    *reinterpret_cast<uint4*>(dst + (4 * ch + pl) * kTcPlaneA + er * 16) =
+                        make_uint4(h[0], h[1], h[2], h[3]);
+                }
+            } else {
+                // dL/d(encoded features) of row er: columns 16 ch .. 16 ch + 15,
+                // i.e. levels 8 ch .. 8 ch + 7, to the 8 corners of each
+                uint32_t v[16];
+                tc_tmem_ld16(taddr + (uint32_t(32 * quad) << 16) + uint32_t(16 * ch), v);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (valid) {
+#pragma unroll
+                    for (int j = 0; j < kLevels / 2; ++j) {
+                        const float d0 = __uint_as_float(v[2 * j]) * (1.0f / kGradScale),
+                                    d1 = __uint_as_float(v[2 * j + 1]) * (1.0f / kGradScale);
+                        if (d0 == 0.0f && d1 == 0.0f) continue;
+                        uint32_t idx[8];
+                        float w[8];
+                        level_corners(c.spec, 8 * ch + j, px, py, pz, idx, w);
+#pragma unroll
+                        for (int k = 0; k < 8; ++k)
+                            grid_grad_add(gs, touched, idx[k], w[k] * d0, w[k] * d1);
+                    }
+                }
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncthreads();
+        }
+        first = false;
+    }
+    // anything still in flight after a timeout: bounded waits before the
+    // buffers and the tensor memory are released
+    if (tid == 0 && ld_pending && !tc_wait(mb_ld, ld_phase)) atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
+    if (mma_pending && !tc_wait(mb_mma, mma_phase) && tid == 0) atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
+    if (failed) {
+        if (tid == 0) atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
+    } else {
+        // the CTA's weight gradients (unscaled) into the FP32 sums
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const float inv = 1.0f / kGradScale;
+#pragma unroll 1
+        for (int R = 0; R < 2; ++R) {
+            uint32_t v[32];
+            const uint32_t ta = taddr + (uint32_t(32 * quad) << 16) + uint32_t(64 + 64 * R + 32 * ch);
+            tc_tmem_ld16(ta, v);
+            tc_tmem_ld16(ta + 16u, v + 16);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            const int layer = R == 0 ? (quad < 2 ? 3 : 2) : (quad < 2 ? 1 : 0);
+            float4* g = reinterpret_cast<float4*>(gW + layer * kLayerW + (er & 63) * kWidth + 32 * ch);
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                atomicAdd(g + j, make_float4(__uint_as_float(v[4 * j]) * inv, __uint_as_float(v[4 * j + 1]) * inv,
+                                             __uint_as_float(v[4 * j + 2]) * inv,
+                                             __uint_as_float(v[4 * j + 3]) * inv));
+        }
+        if (quad == 0) {  // output layer: rows 0-2 (the padding rows' gradients are zero)
+            uint32_t v[32];
+            const uint32_t ta = taddr + uint32_t(192 + 32 * ch);
+            tc_tmem_ld16(ta, v);
+            tc_tmem_ld16(ta + 16u, v + 16);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (lane < 3) {
+                float4* g = reinterpret_cast<float4*>(gW + kHidden * kLayerW + lane * kWidth + 32 * ch);
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                    atomicAdd(g + j, make_float4(__uint_as_float(v[4 * j]) * inv, __uint_as_float(v[4 * j + 1]) * inv,
+                                                 __uint_as_float(v[4 * j + 2]) * inv,
+                                                 __uint_as_float(v[4 * j + 3]) * inv));
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(kBwCols) : "memory");
+}
+
 // Training forward: stores the input rows and hidden activations, the
 // output, and dL/dout of the relative L2 loss
 //   L = mean_r sum_k (y_rk - t_rk)^2 / (sg(y_rk)^2 + 0.01)
 // (sg = stop-gradient), plus the loss sum into loss_acc.
 __global__ void __launch_bounds__(kMlpWarps * 32)
-k_cache_train_fwd(CacheDev c, const float* q, const float* target, uint32_t n, __half* inputs, __half* acts,
-                  float* dout, float* loss_acc) {
+k_cache_train_fwd(CacheDev c, const float* q, const float* target, uint32_t n_max, const uint32_t* slice,
+                  __half* inputs, __half* acts, float* dout, float* loss_acc) {
     extern __shared__ __align__(16) unsigned char smem[];
+    const Rows rs = rows_of(slice, n_max);
+    const uint32_t n = rs.n;
+    q += size_t(rs.off) * 9;
+    target += size_t(rs.off) * 3;
+    if (blockIdx.x * kMlpWarps * 16u + 16u > n) return;  // no whole tile for this block
     __half* sW = reinterpret_cast<__half*>(smem);
     __half* sX = sW + kWeights;
     float* sO = reinterpret_cast<float*>(sX + kMlpWarps * 16 * kWidth);
@@ -526,9 +919,11 @@ k_cache_train_fwd(CacheDev c, const float* q, const float* target, uint32_t n, _
 // the stored activations, weight gradients dW_l = dz_l^T h_{l-1} summed in
 // FP32 per warp and added to gW, and dL/d(input) written for the grid.
 __global__ void __launch_bounds__(kMlpWarps * 32)
-k_cache_train_bwd(CacheDev c, uint32_t n, const __half* inputs, const __half* acts, const float* dout, float* gW,
-                  float* d_in) {
+k_cache_train_bwd(CacheDev c, uint32_t n_max, const uint32_t* slice, const __half* inputs, const __half* acts,
+                  const float* dout, float* gW, float* d_in) {
     extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t n = rows_of(slice, n_max).n;
+    if (blockIdx.x * kMlpWarps * 16u + 16u > n) return;  // no whole tile for this block
     __half* sWT = reinterpret_cast<__half*>(smem);                 // kWeights halves of transposes
     float* sD = reinterpret_cast<float*>(sWT + kWeights);           // kMlpWarps x 16 x 64 dz tile
     __half* sH = reinterpret_cast<__half*>(sD + kMlpWarps * 16 * kWidth);  // kMlpWarps x 16 x 64 h tile
@@ -636,10 +1031,14 @@ k_cache_train_bwd(CacheDev c, uint32_t n, const __half* inputs, const __half* ac
         if (sG[i] != 0.0f) atomicAdd(&gW[i], sG[i] * (1.0f / kGradScale));
 }
 
-// Hash-grid gradient: scatter dL/d(features) to the 8 corners per level.
-__global__ void k_grid_bwd(CacheDev c, const float* q, const float* d_in, uint32_t n, float* g_grid) {
+// Hash-grid gradient: scatter dL/d(features) to the 8 corners per level
+// (flagging the entries for the grid's Adam step).
+__global__ void k_grid_bwd(CacheDev c, const float* q, const float* d_in, uint32_t n_max, const uint32_t* slice,
+                           GridEntry* gs, uint32_t* touched) {
+    const Rows rs = rows_of(slice, n_max);
+    q += size_t(rs.off) * 9;
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n) return;
+    if (r >= rs.n) return;
     const float px = fminf(fmaxf(q[size_t(r) * 9 + 0], 0.0f), 1.0f);
     const float py = fminf(fmaxf(q[size_t(r) * 9 + 1], 0.0f), 1.0f);
     const float pz = fminf(fmaxf(q[size_t(r) * 9 + 2], 0.0f), 1.0f);
@@ -650,18 +1049,19 @@ __global__ void k_grid_bwd(CacheDev c, const float* q, const float* d_in, uint32
         float w[8];
         level_corners(c.spec, l, px, py, pz, idx, w);
         for (int k = 0; k < 8; ++k) {
-            atomicAdd(&g_grid[2 * size_t(idx[k])], w[k] * d0);
-            atomicAdd(&g_grid[2 * size_t(idx[k]) + 1], w[k] * d1);
+            grid_grad_add(gs, touched, idx[k], w[k] * d0, w[k] * d1);
         }
     }
 }
 
 // Adam on FP32 masters, writing the FP16 copies (and the transposed MLP
-// layout when `wt` is set).  Gradients are cleared after use.
-__global__ void k_adam(float* p, float* m, float* v, float* grad, __half* p16, __half* wt, uint32_t n, float lr,
-                       float b1, float b2, float eps, float bc1, float bc2) {
+// layout when `wt` is set, the tcgen05 image when `wimg` is).  Gradients are cleared after use.  A training
+// slice that came out empty (a frame whose paths left fewer than 16
+// samples per step) updates nothing.
+__global__ void k_adam(float* p, float* m, float* v, float* grad, __half* p16, __half* wt, __half* wimg, uint32_t n,
+                       float lr, float b1, float b2, float eps, float bc1, float bc2, const uint32_t* slice) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || (slice && slice[1] == 0u)) return;
     const float gr = grad[i];
     grad[i] = 0.0f;
     const float mi = b1 * m[i] + (1.0f - b1) * gr;
@@ -672,6 +1072,7 @@ __global__ void k_adam(float* p, float* m, float* v, float* grad, __half* p16, _
     p[i] = pi;
     const __half h = __float2half_rn(pi);
     p16[i] = h;
+    if (wimg) wimg[wimg_off(int(i / kLayerW), int((i % kLayerW) / kWidth), int(i % kWidth)) / 2] = h;
     if (wt) {
         // hidden layers: [L][o][i] -> [L][i][o]; output rows: [o][i] -> [i][o] (64 x 16)
         const uint32_t L = i / kLayerW, e = i % kLayerW;
@@ -685,33 +1086,74 @@ __global__ void k_adam(float* p, float* m, float* v, float* grad, __half* p16, _
     }
 }
 
-// Adam on the grid features, four at a time, lazily: a group whose four
-// gradients are all zero (no training sample touched those corners this
-// step) keeps its parameters and moments, so a step reads the whole
-// gradient array but only the touched part of the rest.
-__global__ void k_adam_grid4(float4* p, float4* m, float4* v, float4* grad, __half2* p16, uint32_t n4, float lr,
-                             float b1, float b2, float eps, float bc1, float bc2) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n4) return;
-    const float4 g = grad[i];
-    if (g.x == 0.0f && g.y == 0.0f && g.z == 0.0f && g.w == 0.0f) return;
-    grad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    float4 mi = m[i], vi = v[i], pi = p[i];
-    const float gs[4] = {g.x, g.y, g.z, g.w};
-    float* ms = &mi.x;
-    float* vs = &vi.x;
-    float* ps = &pi.x;
+// Adam on the grid features, lazily and per entry (its 2 features): the
+// gradient scatter marks every entry it adds a nonzero amount to in a
+// bitmap, and only marked entries whose gradient is nonzero are updated;
+// the rest keep their parameters and moments.  A warp takes a bitmap word
+// (32 consecutive entries, 1 KB of training state): each lane whose bit is
+// set reads its entry's sector, updates it with the gradient cleared, and
+// writes its FP16 features; the word is cleared.  kAdamWords words in
+// flight per warp.
+constexpr int kAdamWords = 4;
+
+__global__ void k_adam_grid(GridEntry* gs, __half2* p16, uint32_t* touched, uint32_t nwords, float lr, float b1,
+                            float b2, float eps, float bc1, float bc2) {
+    const uint32_t lane = lane_id();
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t w0 = warp; w0 < nwords; w0 += warps * kAdamWords) {
+        uint32_t word[kAdamWords];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        ms[k] = b1 * ms[k] + (1.0f - b1) * gs[k];
-        vs[k] = b2 * vs[k] + (1.0f - b2) * gs[k] * gs[k];
-        ps[k] = ps[k] - lr * (ms[k] / bc1) / (sqrtf(vs[k] / bc2) + eps);
+        for (int j = 0; j < kAdamWords; ++j) {
+            const uint32_t w = w0 + uint32_t(j) * warps;
+            const uint32_t x = (lane == 0u && w < nwords) ? touched[w] : 0u;
+            word[j] = __shfl_sync(0xFFFFFFFFu, x, 0);
+        }
+        GridEntry en[kAdamWords];
+#pragma unroll
+        for (int j = 0; j < kAdamWords; ++j)
+            if ((word[j] >> lane) & 1u) en[j] = gs[32u * (w0 + uint32_t(j) * warps) + lane];
+#pragma unroll
+        for (int j = 0; j < kAdamWords; ++j) {
+            if (lane == 0u && word[j] != 0u) touched[w0 + uint32_t(j) * warps] = 0u;
+            if (!((word[j] >> lane) & 1u)) continue;
+            GridEntry x = en[j];
+            const float2 g = x.g;
+            if (g.x == 0.0f && g.y == 0.0f) continue;
+            x.m.x = b1 * x.m.x + (1.0f - b1) * g.x;
+            x.m.y = b1 * x.m.y + (1.0f - b1) * g.y;
+            x.v.x = b2 * x.v.x + (1.0f - b2) * g.x * g.x;
+            x.v.y = b2 * x.v.y + (1.0f - b2) * g.y * g.y;
+            x.p.x = x.p.x - lr * (x.m.x / bc1) / (sqrtf(x.v.x / bc2) + eps);
+            x.p.y = x.p.y - lr * (x.m.y / bc1) / (sqrtf(x.v.y / bc2) + eps);
+            x.g = make_float2(0.0f, 0.0f);
+            const uint32_t e = 32u * (w0 + uint32_t(j) * warps) + lane;
+            gs[e] = x;
+            p16[e] = __floats2half2_rn(x.p.x, x.p.y);
+        }
     }
-    m[i] = mi;
-    v[i] = vi;
-    p[i] = pi;
-    p16[2 * i] = __floats2half2_rn(pi.x, pi.y);
-    p16[2 * i + 1] = __floats2half2_rn(pi.z, pi.w);
+}
+
+// Copies one float2 field (at float offset `field`: 0 features, 6
+// gradient) of every grid entry from (to_state = 0) or into the training
+// state, for parameter access and initialisation.
+__global__ void k_grid_field(GridEntry* gs, float2* flat, uint32_t n, int field, int to_state) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    float2* f = reinterpret_cast<float2*>(reinterpret_cast<float*>(gs + e) + field);
+    if (to_state) *f = flat[e];
+    else flat[e] = *f;
+}
+
+// A frame's training slices from the sample count its paths left on the
+// device (at most cap): `steps` consecutive runs of equal length, a
+// multiple of 16 rows, all empty below 16 rows per step.  Slice k is
+// {first row, rows} at slices[2k].
+__global__ void k_cache_slices(const uint32_t* count, uint32_t cap, uint32_t steps, uint32_t* slices) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= steps) return;
+    const uint32_t per = (min(*count, cap) / steps) & ~15u;
+    slices[2 * k] = k * per;
+    slices[2 * k + 1] = per;
 }
 
 } // namespace
@@ -726,8 +1168,10 @@ struct mrt_cache {
     float *w = nullptr, *wm = nullptr, *wv = nullptr, *wg = nullptr;
     __half *w16 = nullptr, *wt16 = nullptr;
     // grid
-    float *gp = nullptr, *gm = nullptr, *gv = nullptr, *gg = nullptr;
-    __half2* g16 = nullptr;
+    GridEntry* gs = nullptr;     // per entry: FP32 features, Adam moments, gradient
+    __half2* g16 = nullptr;      // FP16 features (what the encodings gather)
+    uint32_t* touched = nullptr; // bitmap: entries with a gradient since the last Adam step
+    __half* wimg = nullptr;      // the MLP weights in the tcgen05 kernels' shared-memory layout
     // training buffers (capacity in samples)
     uint32_t cap = 0;
     float *tq = nullptr, *tt = nullptr, *tdout = nullptr, *tdin = nullptr, *loss = nullptr;
@@ -736,7 +1180,6 @@ struct mrt_cache {
     uint32_t step = 0;
     float last_loss = 0.0f;
     float* h_loss = nullptr;
-    uint32_t* h_count = nullptr;
     uint32_t frame = 0;
     // per-frame sample buffer (training paths) and query buffers (render)
     uint32_t scap = 0;
@@ -744,14 +1187,36 @@ struct mrt_cache {
     size_t qcap = 0;
     float *qq = nullptr, *qpred = nullptr;
     float4* qpb = nullptr;
-    // inference on tcgen05 (k_cache_infer_tc, default) or mma.sync (k_cache_infer)
+    // tcgen05 training images (k_cache_fwd_tc<true> -> k_cache_bwd_tc), capacity in tiles
+    uint32_t tile_cap = 0;
+    uint4 *timg = nullptr, *tdy = nullptr;
+    // a frame's training slices (device), capacity in steps
+    uint32_t* slices = nullptr;
+    uint32_t slice_cap = 0;
+    // inference and training on tcgen05 (k_cache_fwd_tc, k_cache_bwd_tc;
+    // default) or on mma.sync (k_cache_infer, k_cache_train_fwd / _bwd)
     bool tcgen05 = true;
+    // a cache frame trains on the context's side stream while its rays are
+    // traced (joined before the cache is queried)
+    bool overlap_training = true;
     int sm_count = 0;
 };
 
 namespace {
 
 int ensure_train(mrt_ctx* ctx, mrt_cache* c, uint32_t n) {
+    const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
+    if (c->tile_cap < tiles) {
+        cudaFree(c->timg); cudaFree(c->tdy);
+        c->timg = c->tdy = nullptr;
+        c->tile_cap = 0;
+        if (cudaMalloc(&c->timg, size_t(tiles) * kImgs * kImg) != cudaSuccess ||
+            cudaMalloc(&c->tdy, size_t(tiles) * kDyImg) != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(ctx, MRT_ENOMEM, "radiance cache: training images");
+        }
+        c->tile_cap = tiles;
+    }
     if (c->cap >= n) return MRT_OK;
     cudaFree(c->tq); cudaFree(c->tt); cudaFree(c->tdout); cudaFree(c->tdin); cudaFree(c->tin); cudaFree(c->tact);
     c->cap = 0;
@@ -771,6 +1236,16 @@ int ensure_train(mrt_ctx* ctx, mrt_cache* c, uint32_t n) {
 size_t smem_infer() { return kWeights * 2 + kMlpWarps * 16 * kWidth * 2 + kMlpWarps * 16 * 3 * 4; }
 size_t smem_bwd() { return kWeights * 2 + kMlpWarps * 16 * kWidth * 4 + kMlpWarps * 16 * kWidth * 2 + kWeights * 4; }
 
+// The tcgen05 kernels' image (wimg_off) of FP16 weights [layer][out][in].
+std::vector<__half> weight_image(const std::vector<__half>& w16) {
+    std::vector<__half> img(kTcWBytes / 2, __float2half_rn(0.0f));
+    for (int L = 0; L <= kHidden; ++L)
+        for (int o = 0; o < (L < kHidden ? kWidth : kOutRows); ++o)
+            for (int i = 0; i < kWidth; ++i)
+                img[wimg_off(L, o, i) / 2] = w16[size_t(L) * kLayerW + size_t(o) * kWidth + i];
+    return img;
+}
+
 uint64_t splitmix(uint64_t& s) {
     uint64_t z = (s += 0x9E3779B97F4A7C15ull);
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -778,10 +1253,76 @@ uint64_t splitmix(uint64_t& s) {
     return z ^ (z >> 31);
 }
 
+// One training step on rows [0, n) of q / t, or on the device-side slice
+// {first row, rows <= n} of them: forward, loss, backward (on tcgen05 or
+// mma.sync), and with `apply` an Adam step.  Launches only: nothing is
+// read back.
+int train_step_launch(mrt_ctx* ctx, mrt_cache* c, const float* q, const float* t, uint32_t n, const uint32_t* slice,
+                      int apply, cudaStream_t s) {
+    int rc = ensure_train(ctx, c, n);
+    if (rc) return rc;
+    if (cudaMemsetAsync(c->loss, 0, 4, s) != cudaSuccess) return set_error(ctx, MRT_ECUDA, "train: memset");
+    if (c->tcgen05) {
+        // forward: one 128-row tile per CTA (up to 4 per SM); backward: two
+        // CTAs per SM, each accumulating the weight gradients of its tiles
+        const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
+        const TrainTc tr{t, c->timg, c->tdy, c->loss};
+        k_cache_fwd_tc<true><<<std::min<uint32_t>(tiles, uint32_t(c->sm_count) * 4u), kTcThreads, kTcSmem, s>>>(
+            c->dev, q, n, slice, nullptr, ctx->d_status, tr);
+        k_cache_bwd_tc<<<std::min<uint32_t>(tiles, uint32_t(c->sm_count) * 2u), kBwThreads, kBwSmem, s>>>(
+            c->dev, q, n, slice, c->timg, c->tdy, c->wg, c->gs, c->touched, ctx->d_status);
+        ctx->launches += 2;
+    } else {
+        const uint32_t tiles = n / 16u;
+        const uint32_t blocks = std::min<uint32_t>((tiles + kMlpWarps - 1) / kMlpWarps, 2048u);
+        k_cache_train_fwd<<<blocks, kMlpWarps * 32, smem_infer(), s>>>(c->dev, q, t, n, slice, c->tin, c->tact,
+                                                                       c->tdout, c->loss);
+        k_cache_train_bwd<<<blocks, kMlpWarps * 32, smem_bwd(), s>>>(c->dev, n, slice, c->tin, c->tact, c->tdout,
+                                                                     c->wg, c->tdin);
+        k_grid_bwd<<<(n + 127) / 128, 128, 0, s>>>(c->dev, q, c->tdin, n, slice, c->gs, c->touched);
+        ctx->launches += 3;
+    }
+    if (apply) {
+        c->step++;
+        const float b1 = 0.9f, b2 = 0.99f, eps = 1e-10f;
+        const float bc1 = 1.0f - std::pow(b1, float(c->step)), bc2 = 1.0f - std::pow(b2, float(c->step));
+        k_adam<<<(kWeights + 255) / 256, 256, 0, s>>>(c->w, c->wm, c->wv, c->wg, c->w16, c->wt16, c->wimg,
+                                                      kWeights, c->cfg.lr_mlp, b1, b2, eps, bc1, bc2, slice);
+        const uint32_t nwords = c->grid_entries / 32u;  // bitmap words, one warp each
+        k_adam_grid<<<std::min<uint32_t>((nwords + 7) / 8, uint32_t(c->sm_count) * 8u), 256, 0, s>>>(
+            c->gs, c->g16, c->touched, nwords, c->cfg.lr_grid, b1, b2, eps, bc1, bc2);
+        ctx->launches += 2;
+    }
+    if (cudaGetLastError() != cudaSuccess) return set_error(ctx, MRT_ECUDA, "train: launch failed");
+    return MRT_OK;
+}
+
+// One float2 field of every grid entry's training state to or from host
+// memory (2 floats an entry), through a staging buffer on the device.
+cudaError_t grid_field(mrt_cache* c, float* host, int field, bool to_state) {
+    const size_t bytes = size_t(c->grid_entries) * sizeof(float2);
+    float2* flat = nullptr;
+    cudaError_t e = cudaMalloc(&flat, bytes);
+    if (e != cudaSuccess) return e;
+    const uint32_t blocks = (c->grid_entries + 255u) / 256u;
+    if (to_state) {
+        e = cudaMemcpy(flat, host, bytes, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) k_grid_field<<<blocks, 256>>>(c->gs, flat, c->grid_entries, field, 1);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    } else {
+        k_grid_field<<<blocks, 256>>>(c->gs, flat, c->grid_entries, field, 0);
+        e = cudaDeviceSynchronize();
+        if (e == cudaSuccess) e = cudaMemcpy(host, flat, bytes, cudaMemcpyDeviceToHost);
+    }
+    cudaFree(flat);
+    return e;
+}
+
 } // namespace
 
 namespace mrt {
 uint32_t cache_query_vertex(const mrt_cache* c) { return c->cfg.query_vertex; }
+bool cache_overlap_training(const mrt_cache* c) { return c->overlap_training; }
 
 // Inference over device rows of 9 floats; with n_dev the row count is read
 // on the device (at most n).
@@ -791,7 +1332,7 @@ cudaError_t cache_infer(const mrt_cache* c, const float* q, uint32_t n, const ui
     if (c->tcgen05) {  // persistent: up to 4 CTAs (51 KB of shared memory, 64 TMEM columns each) per SM
         const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
         const uint32_t blocks = std::min<uint32_t>(tiles, uint32_t(c->sm_count) * 4u);
-        k_cache_infer_tc<<<blocks, kTcThreads, kTcSmem, s>>>(c->dev, q, n, n_dev, out, status);
+        k_cache_fwd_tc<false><<<blocks, kTcThreads, kTcSmem, s>>>(c->dev, q, n, n_dev, out, status, TrainTc{});
         return cudaGetLastError();
     }
     const uint32_t tiles = (n + 15u) / 16u;
@@ -822,11 +1363,16 @@ int cache_frame_buffers(mrt_ctx* ctx, mrt_cache* c, size_t n, float** q, float4*
 
 // Trains the cache on this frame: cfg.train_paths fresh paths from the
 // camera (plain estimator up to cfg.train_bounces), every vertex's suffix
-// radiance a sample, then cfg.train_steps Adam steps on equal slices.
+// radiance a sample, then cfg.train_steps Adam steps on equal slices of the
+// samples.  The slices are cut on the device from the sample count, so
+// nothing is read back and the frame stays one stream of launches (the
+// Adam step counter, and with it the bias correction, advances even for a
+// frame whose paths left no samples, whose steps then change nothing).
 int cache_train_frame(mrt_ctx* ctx, mrt_cache* c, const DevScene& sc, const FrameParams& fp, const TraceParams& tp,
                       uint32_t* status, cudaStream_t s) {
     const uint32_t paths = c->cfg.train_paths ? c->cfg.train_paths : 65536u;
     const uint32_t cap = paths * 4u;
+    const uint32_t steps = c->cfg.train_steps ? c->cfg.train_steps : 4u;
     if (c->scap < cap) {
         cudaFree(c->sq); cudaFree(c->st);
         c->sq = c->st = nullptr;
@@ -838,24 +1384,26 @@ int cache_train_frame(mrt_ctx* ctx, mrt_cache* c, const DevScene& sc, const Fram
         c->scap = cap;
     }
     if (!c->tcount) {
-        if (cudaMalloc(&c->tcount, 4) != cudaSuccess || cudaMallocHost(&c->h_count, 4) != cudaSuccess)
-            return set_error(ctx, MRT_ENOMEM, "radiance cache: counter");
+        if (cudaMalloc(&c->tcount, 4) != cudaSuccess) return set_error(ctx, MRT_ENOMEM, "radiance cache: counter");
     }
+    if (c->slice_cap < steps) {
+        cudaFree(c->slices);
+        c->slices = nullptr;
+        c->slice_cap = 0;
+        if (cudaMalloc(&c->slices, size_t(steps) * 2 * 4) != cudaSuccess)
+            return set_error(ctx, MRT_ENOMEM, "radiance cache: training slices");
+        c->slice_cap = steps;
+    }
+    const uint32_t per_max = (cap / steps) & ~15u;  // the most rows a slice can hold
+    if (per_max < 16u) return set_error(ctx, MRT_EINVAL, "cache: fewer than 16 training rows per step");
     if (cudaMemsetAsync(c->tcount, 0, 4, s) != cudaSuccess) return set_error(ctx, MRT_ECUDA, "cache: memset");
     if (launch_cache_train_paths(sc, fp, tp, c->cfg.train_bounces ? c->cfg.train_bounces : 8u, paths, c->frame++,
                                  c->sq, c->st, c->tcount, cap, status, s) != cudaSuccess)
         return set_error(ctx, MRT_ECUDA, "cache: training paths launch");
-    ctx->launches++;
-    if (cudaMemcpyAsync(c->h_count, c->tcount, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-        return set_error(ctx, MRT_ECUDA, "cache: sample count read-back");
-    const uint32_t total = std::min(*c->h_count, cap);
-    const uint32_t steps = c->cfg.train_steps ? c->cfg.train_steps : 4u;
-    const uint32_t per = (total / steps) & ~15u;
-    if (per < 16u) return MRT_OK;  // nothing hit this frame
+    k_cache_slices<<<(steps + 63) / 64, 64, 0, s>>>(c->tcount, cap, steps, c->slices);
+    ctx->launches += 2;
     for (uint32_t k = 0; k < steps; ++k) {
-        int rc = mrt_cuda_cache_train_step(ctx, c, c->sq + size_t(k) * per * 9, c->st + size_t(k) * per * 3, per, 1,
-                                           nullptr, s);
+        int rc = train_step_launch(ctx, c, c->sq, c->st, per_max, c->slices + 2 * k, 1, s);
         if (rc) return rc;
     }
     return MRT_OK;
@@ -881,10 +1429,10 @@ int mrt_cuda_cache_create(mrt_ctx* ctx, const mrt_cache_config* cfg, mrt_cache**
     bool ok = cudaMalloc(&c->w, kWeights * 4) == cudaSuccess && cudaMalloc(&c->wm, kWeights * 4) == cudaSuccess &&
               cudaMalloc(&c->wv, kWeights * 4) == cudaSuccess && cudaMalloc(&c->wg, kWeights * 4) == cudaSuccess &&
               cudaMalloc(&c->w16, kWeights * 2) == cudaSuccess && cudaMalloc(&c->wt16, kWeights * 2) == cudaSuccess &&
-              cudaMalloc(&c->gp, gn * 4) == cudaSuccess && cudaMalloc(&c->gm, gn * 4) == cudaSuccess &&
-              cudaMalloc(&c->gv, gn * 4) == cudaSuccess && cudaMalloc(&c->gg, gn * 4) == cudaSuccess &&
+              cudaMalloc(&c->gs, size_t(c->grid_entries) * sizeof(GridEntry)) == cudaSuccess &&
               cudaMalloc(&c->g16, gn * 2) == cudaSuccess && cudaMalloc(&c->loss, 4) == cudaSuccess &&
-              cudaMallocHost(&c->h_loss, 4) == cudaSuccess;
+              cudaMalloc(&c->touched, c->grid_entries / 8) == cudaSuccess &&
+              cudaMalloc(&c->wimg, kTcWBytes) == cudaSuccess && cudaMallocHost(&c->h_loss, 4) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         mrt_cuda_cache_destroy(ctx, c);
@@ -917,18 +1465,23 @@ int mrt_cuda_cache_create(mrt_ctx* ctx, const mrt_cache_config* cfg, mrt_cache**
         }
         std::vector<__half> g16(gn);
         for (size_t i = 0; i < gn; ++i) g16[i] = __float2half_rn(g[i]);
+        const std::vector<__half> img = weight_image(w16);
         ok = cudaMemcpy(c->w, w.data(), kWeights * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
              cudaMemcpy(c->w16, w16.data(), kWeights * 2, cudaMemcpyHostToDevice) == cudaSuccess &&
+             cudaMemcpy(c->wimg, img.data(), kTcWBytes, cudaMemcpyHostToDevice) == cudaSuccess &&
+             cudaMemset(c->touched, 0, c->grid_entries / 8) == cudaSuccess &&
+             cudaMemset(c->gs, 0, size_t(c->grid_entries) * sizeof(GridEntry)) == cudaSuccess &&
+             grid_field(c, g.data(), 0, true) == cudaSuccess &&
              cudaMemcpy(c->wt16, wt16.data(), kWeights * 2, cudaMemcpyHostToDevice) == cudaSuccess &&
-             cudaMemcpy(c->gp, g.data(), gn * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
              cudaMemcpy(c->g16, g16.data(), gn * 2, cudaMemcpyHostToDevice) == cudaSuccess &&
              cudaMemset(c->wm, 0, kWeights * 4) == cudaSuccess && cudaMemset(c->wv, 0, kWeights * 4) == cudaSuccess &&
-             cudaMemset(c->wg, 0, kWeights * 4) == cudaSuccess && cudaMemset(c->gm, 0, gn * 4) == cudaSuccess &&
-             cudaMemset(c->gv, 0, gn * 4) == cudaSuccess && cudaMemset(c->gg, 0, gn * 4) == cudaSuccess;
+             cudaMemset(c->wg, 0, kWeights * 4) == cudaSuccess;
     }
     if (!ok ||
         cudaFuncSetAttribute(k_cache_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_infer())) != cudaSuccess ||
-        cudaFuncSetAttribute(k_cache_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_cache_fwd_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_cache_fwd_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_cache_bwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kBwSmem) != cudaSuccess ||
         cudaFuncSetAttribute(k_cache_train_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_infer())) != cudaSuccess ||
         cudaFuncSetAttribute(k_cache_train_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bwd())) != cudaSuccess) {
         cudaGetLastError();
@@ -937,6 +1490,7 @@ int mrt_cuda_cache_create(mrt_ctx* ctx, const mrt_cache_config* cfg, mrt_cache**
     }
     c->dev.grid = c->g16;
     c->dev.W = c->w16;
+    c->dev.Wimg = c->wimg;
     c->dev.WT = c->wt16;
     c->sm_count = ctx->sm_count;
     *out = c;
@@ -949,15 +1503,21 @@ int mrt_cuda_cache_set_tcgen05(mrt_cache* c, int enable) {
     return MRT_OK;
 }
 
+int mrt_cuda_cache_set_overlap(mrt_cache* c, int enable) {
+    if (!c) return MRT_EINVAL;
+    c->overlap_training = enable != 0;
+    return MRT_OK;
+}
+
 int mrt_cuda_cache_destroy(mrt_ctx* ctx, mrt_cache* c) {
     if (!ctx || !c) return MRT_EINVAL;
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
-    void* ps[] = {c->w, c->wm, c->wv, c->wg, c->w16, c->wt16, c->gp, c->gm, c->gv, c->gg, c->g16, c->loss,
-                  c->tq, c->tt, c->tdout, c->tdin, c->tin, c->tact, c->tcount, c->sq, c->st, c->qq, c->qpred, c->qpb};
+    void* ps[] = {c->w, c->wm, c->wv, c->wg, c->w16, c->wt16, c->gs, c->g16, c->loss, c->touched, c->wimg,
+                  c->tq, c->tt, c->tdout, c->tdin, c->tin, c->tact, c->tcount, c->sq, c->st, c->qq, c->qpred, c->qpb,
+                  c->timg, c->tdy, c->slices};
     for (void* p : ps) cudaFree(p);
     if (c->h_loss) cudaFreeHost(c->h_loss);
-    if (c->h_count) cudaFreeHost(c->h_count);
     delete c;
     return MRT_OK;
 }
@@ -987,30 +1547,8 @@ int mrt_cuda_cache_train_step(mrt_ctx* ctx, mrt_cache* c, const float* queries, 
     if (n == 0) return set_error(ctx, MRT_EINVAL, "cache_train_step: fewer than 16 samples");
     cudaSetDevice(ctx->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    int rc = ensure_train(ctx, c, n);
+    int rc = train_step_launch(ctx, c, queries, targets, n, nullptr, apply_update, s);
     if (rc) return rc;
-    const uint32_t tiles = n / 16u;
-    const uint32_t blocks = std::min<uint32_t>((tiles + kMlpWarps - 1) / kMlpWarps, 2048u);
-    if (cudaMemsetAsync(c->loss, 0, 4, s) != cudaSuccess) return set_error(ctx, MRT_ECUDA, "train: memset");
-    k_cache_train_fwd<<<blocks, kMlpWarps * 32, smem_infer(), s>>>(c->dev, queries, targets, n, c->tin, c->tact,
-                                                                   c->tdout, c->loss);
-    k_cache_train_bwd<<<blocks, kMlpWarps * 32, smem_bwd(), s>>>(c->dev, n, c->tin, c->tact, c->tdout, c->wg,
-                                                                 c->tdin);
-    k_grid_bwd<<<(n + 127) / 128, 128, 0, s>>>(c->dev, queries, c->tdin, n, c->gg);
-    ctx->launches += 3;
-    if (apply_update) {
-        c->step++;
-        const float b1 = 0.9f, b2 = 0.99f, eps = 1e-10f;
-        const float bc1 = 1.0f - std::pow(b1, float(c->step)), bc2 = 1.0f - std::pow(b2, float(c->step));
-        k_adam<<<(kWeights + 255) / 256, 256, 0, s>>>(c->w, c->wm, c->wv, c->wg, c->w16, c->wt16, kWeights,
-                                                      c->cfg.lr_mlp, b1, b2, eps, bc1, bc2);
-        const uint32_t gn4 = c->grid_entries / 2u;  // 2 features per entry, 4 floats per group
-        k_adam_grid4<<<(gn4 + 255) / 256, 256, 0, s>>>(
-            reinterpret_cast<float4*>(c->gp), reinterpret_cast<float4*>(c->gm), reinterpret_cast<float4*>(c->gv),
-            reinterpret_cast<float4*>(c->gg), c->g16, gn4, c->cfg.lr_grid, b1, b2, eps, bc1, bc2);
-        ctx->launches += 2;
-    }
-    if (cudaGetLastError() != cudaSuccess) return set_error(ctx, MRT_ECUDA, "train: launch failed");
     if (loss_out) {
         if (cudaMemcpyAsync(c->h_loss, c->loss, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess)
@@ -1028,10 +1566,26 @@ int mrt_cuda_cache_params(mrt_ctx* ctx, mrt_cache* c, int which, float* host, si
     if (!ctx || !c || !host || which < 0 || which > 3) return set_error(ctx, MRT_EINVAL, "cache_params: bad arguments");
     cudaSetDevice(ctx->device);
     const size_t gn = size_t(c->grid_entries) * 2;
-    float* dptr = which == 0 ? c->w : which == 1 ? c->wg : which == 2 ? c->gp : c->gg;
     const size_t total = which < 2 ? size_t(kWeights) : gn;
     if (count != total) return set_error(ctx, MRT_EINVAL, "cache_params: count mismatch");
     cudaDeviceSynchronize();
+    if (which >= 2) {  // a field of the grid's training state: 0 features, 6 gradient
+        const int field = which == 2 ? 0 : 6;
+        if (grid_field(c, host, field, set != 0) != cudaSuccess) return set_error(ctx, MRT_ECUDA, "cache_params: copy");
+        if (!set) return MRT_OK;
+        if (which == 2) {
+            std::vector<__half> g16(gn);
+            for (size_t i = 0; i < gn; ++i) g16[i] = __float2half_rn(host[i]);
+            cudaMemcpy(c->g16, g16.data(), gn * 2, cudaMemcpyHostToDevice);
+        } else {  // gradients set by hand: mark their entries for the grid's next Adam step
+            std::vector<uint32_t> bits(c->grid_entries / 32, 0u);
+            for (size_t e = 0; e < c->grid_entries; ++e)
+                if (host[2 * e] != 0.0f || host[2 * e + 1] != 0.0f) bits[e >> 5] |= 1u << (e & 31u);
+            cudaMemcpy(c->touched, bits.data(), bits.size() * 4, cudaMemcpyHostToDevice);
+        }
+        return MRT_OK;
+    }
+    float* dptr = which == 0 ? c->w : c->wg;
     if (!set) {
         if (cudaMemcpy(host, dptr, total * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
             return set_error(ctx, MRT_ECUDA, "cache_params: copy");
@@ -1048,12 +1602,10 @@ int mrt_cuda_cache_params(mrt_ctx* ctx, mrt_cache* c, int which, float* host, si
                 for (int i = 0; i < kWidth; ++i)
                     wt16[size_t(L) * kLayerW + size_t(i) * rows + o] = w16[size_t(L) * kLayerW + size_t(o) * kWidth + i];
         }
+        const std::vector<__half> img = weight_image(w16);
         cudaMemcpy(c->w16, w16.data(), kWeights * 2, cudaMemcpyHostToDevice);
         cudaMemcpy(c->wt16, wt16.data(), kWeights * 2, cudaMemcpyHostToDevice);
-    } else if (which == 2) {
-        std::vector<__half> g16(gn);
-        for (size_t i = 0; i < gn; ++i) g16[i] = __float2half_rn(host[i]);
-        cudaMemcpy(c->g16, g16.data(), gn * 2, cudaMemcpyHostToDevice);
+        cudaMemcpy(c->wimg, img.data(), kTcWBytes, cudaMemcpyHostToDevice);
     }
     return MRT_OK;
 }

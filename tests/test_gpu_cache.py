@@ -75,12 +75,18 @@ def test_cache_inference_tcgen05_matches_mma_sync_and_oracle(ctx, n):
     assert np.mean(err) < 2e-3 * max(1.0, np.mean(np.abs(ref)))
 
 
-def test_cache_gradients_match_oracle(ctx):
+@pytest.mark.parametrize("tcgen05,n", [(True, 512), (True, 1008), (True, 16), (False, 512)])
+def test_cache_gradients_match_oracle(ctx, tcgen05, n):
+    # tcgen05 training (128-row tiles; 1008 rows = 7 full tiles + 112, 16
+    # rows = one ragged tile) and the mma.sync kernels against the FP64
+    # oracle's loss and gradients (FP16 operands as in the kernels)
     c, W, G = _cache(ctx, seed=3)
-    q = _queries(512, 4)
+    c.set_tcgen05(tcgen05)
+    q = _queries(n, 4)
     t = np.random.default_rng(5).uniform(0.1, 1.0, (len(q), 3)).astype(np.float32)
     d_q, d_t = ctx.to_device(q), ctx.to_device(t)
     loss = c.train_step(d_q, d_t, len(q), update=False, want_loss=True)
+    assert ctx.status() == 0
     gW, gG = c.params(1).astype(np.float64), c.params(3).astype(np.float64)
     rloss, rgW, rgG, _ = nrc.loss_and_grads(G.astype(np.float64), W.astype(np.float64), q.astype(np.float64),
                                             t.astype(np.float64), LOG2_T, 16.0, 512.0, fp16=True)
@@ -89,6 +95,58 @@ def test_cache_gradients_match_oracle(ctx):
         cos = a @ b / (np.linalg.norm(a) * np.linalg.norm(b))
         assert cos > 0.999, cos
         assert abs(np.linalg.norm(a) / np.linalg.norm(b) - 1.0) < 0.03
+
+
+@pytest.mark.parametrize("tcgen05", [True, False])
+def test_grid_adam_updates_only_touched_entries(ctx, tcgen05):
+    # The grid's Adam is lazy per entry: the scatter flags the entries it
+    # adds a gradient to, and the step updates those (and clears their
+    # gradients) while every other entry keeps its features bit for bit.
+    c, W, G = _cache(ctx, seed=17)
+    c.set_tcgen05(tcgen05)
+    q = _queries(300, 18)
+    t = np.random.default_rng(19).uniform(0.1, 1.0, (len(q), 3)).astype(np.float32)
+    d_q, d_t = ctx.to_device(q), ctx.to_device(t)
+    g0 = c.params(2)
+    c.train_step(d_q, d_t, len(q), update=False)
+    grad = c.params(3).reshape(-1, 2)
+    touched = np.any(grad != 0.0, axis=1)
+    assert 0 < touched.sum() < len(touched) // 4
+    c.train_step(d_q, d_t, len(q), update=True)
+    assert ctx.status() == 0
+    g1 = c.params(2).reshape(-1, 2)
+    g0 = g0.reshape(-1, 2)
+    assert np.array_equal(g1[~touched], g0[~touched])
+    moved = np.any(g1[touched] != g0[touched], axis=1)
+    assert moved.mean() > 0.99
+    assert not np.any(c.params(3))
+
+
+def test_cache_training_tcgen05_matches_mma_sync(ctx):
+    # 200,000 rows: 1,563 tiles, so each backward CTA (two per SM) sums the
+    # weight gradients of several tiles in tensor memory before adding them
+    # to the FP32 array once.  Same samples, same weights: the two paths
+    # differ only in FP32 summation order and where an FP32 sum rounds to
+    # another FP16 operand.
+    n = 200000
+    q = _queries(n, 11)
+    t = np.random.default_rng(12).uniform(0.1, 1.0, (n, 3)).astype(np.float32)
+    d_q, d_t = ctx.to_device(q), ctx.to_device(t)
+    out = {}
+    for tc in (True, False):
+        c, W, G = _cache(ctx, seed=13)
+        c.set_tcgen05(tc)
+        loss = c.train_step(d_q, d_t, n, update=False, want_loss=True)
+        out[tc] = (loss, c.params(1).astype(np.float64), c.params(3).astype(np.float64))
+        c.close()
+    assert ctx.status() == 0
+    assert abs(out[True][0] - out[False][0]) < 1e-3 * out[False][0]
+    for k in (1, 2):
+        a, b = out[True][k], out[False][k]
+        assert np.all(np.isfinite(a))
+        cos = a @ b / (np.linalg.norm(a) * np.linalg.norm(b))
+        assert cos > 0.9999, (k, cos)
+        assert abs(np.linalg.norm(a) / np.linalg.norm(b) - 1.0) < 0.01
 
 
 def test_cache_learns_a_smooth_function(ctx):
@@ -111,6 +169,40 @@ def test_cache_learns_a_smooth_function(ctx):
 
 def _rmse(a, b):
     return float(np.sqrt(np.mean((a - b) ** 2)))
+
+
+def test_cache_frame_training_overlapped_with_tracing(ctx, hf_workload, blue_noise):
+    # The same cache frames with the training on the context's second stream
+    # (overlapped with the frame's ray tracing, joined before the cache is
+    # queried) and first on the caller's stream: the same computations in
+    # the same order, so the images agree up to the training's FP32 atomic
+    # summation order.
+    from minotert_gb300.pathtracer import Pathtracer, TraceSettings, camera_consts
+    from minotert_gb300.scene import DeviceScene
+    wl, mesh, bvh = hf_workload
+    ds = DeviceScene.triangles(ctx, mesh, bvh)
+    pt = Pathtracer(ctx, ds, full_gbuffer=False)
+    ctx.blue_noise(blue_noise)
+    W, H = wl.width, wl.height
+    stream = ctx.stream()
+    imgs = {}
+    for overlap in (True, False):
+        cache = RadianceCache(ctx, default_config(train_paths=16384, train_steps=4, query_vertex=1, seed=21),
+                              bounds=(mesh.lo, mesh.hi))
+        cache.set_overlap(overlap)
+        col = ctx.alloc(12 * W * H)
+        for f in range(6):
+            pt.frame_counter = f
+            gb = pt.primaryRays((W, H), wl.camera, wl.camera, stream)
+            params = TraceSettings(1, 1, 2, 1, True, f).params(wl.sky)
+            cache.frame(ds, gb, camera_consts(wl.camera, wl.camera, f), params, col, train=True, stream=stream)
+        ctx.sync(stream)
+        imgs[overlap] = col.download(np.float32, (H, W, 3))
+        cache.close()
+    assert ctx.status() == 0
+    a, b = imgs[True], imgs[False]
+    assert np.isfinite(a).all()
+    assert _rmse(a, b) < 2e-3 * max(1e-3, float(np.mean(np.abs(b)))) + 1e-4, _rmse(a, b)
 
 
 @pytest.mark.parametrize("query_vertex", [1, 0])
