@@ -590,7 +590,7 @@ __device__ __forceinline__ void grid_grad_add(GridEntry* gs, uint32_t* touched, 
 
 // ------------------------------------------- training backward on tcgen05
 //
-// One CTA of 256 threads (two per SM) per run of 128-row tiles.  A tile
+// One CTA of 256 threads (one per SM) per run of 128-row tiles.  A tile
 // takes five phases from the output layer down; phase p works on the layer
 // whose output gradient dZ (FP16, scaled by kGradScale) sits in shared
 // memory as a K-plane image:
@@ -602,18 +602,19 @@ __device__ __forceinline__ void grid_grad_add(GridEntry* gs, uint32_t* touched, 
 //                 the forward reads K-major;
 // then the epilogue writes the next dZ = dH where the layer's input H > 0
 // (ReLU), or, below the first layer, scatters dL/d(encoded features) into
-// the hash grid's gradients.  H is the layer's input image written by the
-// forward, brought in by a bulk copy as soon as the previous phase's MMAs
-// are done with the buffer; the epilogue reads its ReLU mask from the same
-// image in global memory.  The weight gradients of all the CTA's tiles
-// accumulate in tensor memory and are added to the FP32 gradients once.
-// Tensor memory, 256 columns: [0, 64) dH; [64, 128) dW of hidden layer 3
-// (lanes 0-63) and 2 (lanes 64-127); [128, 192) dW of layers 1 and 0;
-// [192, 256) dW of the output layer (lanes 0-15).  Two layers share columns
-// by lanes: the 128 A rows of the dW product are [dZ ; zeros] for the lower
-// layer and [zeros ; dZ] for the upper one, so each adds exactly zero to
-// the other's lanes.  Shared memory holds dZ1 | 16 KB of zeros | dZ2, and
-// the phases alternate between dZ1 (lower) and dZ2 (upper).
+// the hash grid's gradients.  The five layer inputs H (the forward's
+// images) and dL/dy come by bulk copies when the tile starts — the next
+// tile's as soon as this tile's last MMAs are done — so the phases run back
+// to back, the epilogue reading its ReLU mask from the same images.  The
+// weight gradients of all the CTA's tiles accumulate in tensor memory and
+// are added to the FP32 gradients once.  Tensor memory, 256 columns:
+// [0, 64) dH; [64, 128) dW of hidden layer 3 (lanes 0-63) and 2 (lanes
+// 64-127); [128, 192) dW of layers 1 and 0; [192, 256) dW of the output
+// layer (lanes 0-15).  Two layers share columns by lanes: the 128 A rows of
+// the dW product are [dZ ; zeros] for the lower layer and [zeros ; dZ] for
+// the upper one, so each adds exactly zero to the other's lanes.  Shared
+// memory holds dZ1 | 16 KB of zeros | dZ2, and the phases alternate
+// between dZ1 (lower) and dZ2 (upper).
 constexpr int kBwThreads = 256;
 constexpr uint32_t kBwCols = 256;
 constexpr int kBwDy = 0;                      // dL/dy image; the weights follow it
@@ -621,28 +622,23 @@ constexpr int kBwW = kBwDy + kDyImg;
 constexpr int kBwD1 = kBwW + kTcWBytes;       // dZ of phases 1 and 3 (lower lanes)
 constexpr int kBwZ = kBwD1 + kImg;            // zeros
 constexpr int kBwD2 = kBwZ + kImg;            // dZ of phases 2 and 4 (upper lanes)
-constexpr int kBwH = kBwD2 + kImg;            // the phase's layer input H
-constexpr int kBwBar = kBwH + kImg;
+constexpr int kBwH = kBwD2 + kImg;            // the layer inputs: image i = input of layer i
+constexpr int kBwBar = kBwH + kImgs * kImg;
 constexpr int kBwSmem = kBwBar + 64;
 // The output layer's dW product reads 128 A rows of which the first 16 are
 // dL/dy: the other 14 row groups (2 KB apart) fall on the weights.
 static_assert(kBwDy + 16 * kTcPlaneA <= kBwD1, "the output layer's dW rows stay inside the weights");
-static_assert(2 * (kBwSmem + 1024) <= 228 * 1024, "two CTAs per SM");
+static_assert(kBwSmem <= 227 * 1024, "one CTA per SM");
 
+// dL/dy and the five layer-input images of `tile` (and, once, the weights)
+// onto mbarrier mb
 __device__ __forceinline__ void bw_load(uint32_t s0, uint32_t mb, const uint4* img, const uint4* dyimg, uint32_t tile,
-                                        int p, const __half* wimg = nullptr) {
-    const uint32_t bytes = (p == 0 ? uint32_t(kImg + kDyImg) : uint32_t(kImg)) + (wimg ? uint32_t(kTcWBytes) : 0u);
+                                        const __half* wimg) {
+    const uint32_t bytes = uint32_t(kImgs * kImg + kDyImg) + (wimg ? uint32_t(kTcWBytes) : 0u);
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
     if (wimg) bulk_load(s0 + uint32_t(kBwW), wimg, kTcWBytes, mb);
-    if (p == 0)
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                         s0 + uint32_t(kBwDy)),
-                     "l"(dyimg + size_t(tile) * (kDyImg / 16)), "r"(uint32_t(kDyImg)), "r"(mb)
-                     : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     s0 + uint32_t(kBwH)),
-                 "l"(img + (size_t(tile) * kImgs + size_t(kHidden - p)) * (kImg / 16)), "r"(uint32_t(kImg)), "r"(mb)
-                 : "memory");
+    bulk_load(s0 + uint32_t(kBwDy), dyimg + size_t(tile) * (kDyImg / 16), kDyImg, mb);
+    bulk_load(s0 + uint32_t(kBwH), img + size_t(tile) * kImgs * (kImg / 16), kImgs * kImg, mb);
 }
 
 __device__ __forceinline__ void bw_mma(uint32_t d, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
@@ -672,26 +668,24 @@ k_cache_bwd_tc(CacheDev c, const float* q, uint32_t n_max, const uint32_t* slice
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
+    const uint32_t s0 = smem_u32(bsm), mb_ld = smem_u32(bar), mb_mma = smem_u32(bar + 1);
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar + 1)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb_ld) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb_mma) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        bw_load(s0, mb_ld, img, dyimg, blockIdx.x, c.Wimg);  // the weights come with the first tile
     }
     for (int i = tid; i < kImg / 16; i += kBwThreads) reinterpret_cast<uint4*>(bsm + kBwZ)[i] = make_uint4(0, 0, 0, 0);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const uint32_t taddr = *slot, s0 = smem_u32(bsm), mb_ld = smem_u32(bar), mb_mma = smem_u32(bar + 1);
+    const uint32_t taddr = *slot;
     uint32_t ld_phase = 0u, mma_phase = 0u;
-    bool ld_pending = false, mma_pending = false, failed = false, first = true;
+    bool ld_pending = true, mma_pending = false, failed = false, first = true;
     const int quad = warp & 3, ch = warp >> 2, er = 32 * quad + lane;
     constexpr uint32_t idesc_w = mlp_idesc(kTcRows, kWidth) | (1u << 15) | (1u << 16);  // A, B MN-major
     constexpr uint32_t idesc_x = mlp_idesc(kTcRows, kWidth) | (1u << 16);               // B MN-major
-    if (tid == 0) {  // the weights come with the first tile's images
-        bw_load(s0, mb_ld, img, dyimg, blockIdx.x, 0, c.Wimg);
-        ld_pending = true;
-    }
     for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
         const uint32_t row = tile * kTcRows + uint32_t(er);
         const bool valid = row < n;
@@ -701,50 +695,52 @@ k_cache_bwd_tc(CacheDev c, const float* q, uint32_t n_max, const uint32_t* slice
             py = fminf(fmaxf(q[size_t(row) * 9 + 1], 0.0f), 1.0f);
             pz = fminf(fmaxf(q[size_t(row) * 9 + 2], 0.0f), 1.0f);
         }
-        for (int p = 0; p <= kHidden; ++p) {
-            // this thread's ReLU mask: row er, columns 32 ch .. 32 ch + 31 of H
-            uint4 hm[4];
-            if (p < kHidden) {
-                const uint4* h = img + (size_t(tile) * kImgs + size_t(kHidden - p)) * (kImg / 16);
-#pragma unroll
-                for (int pl = 0; pl < 4; ++pl) hm[pl] = h[(4 * ch + pl) * kTcRows + er];
-            }
-            bool ok = true;
-            if (tid == 0) {
-                ok = tc_wait(mb_ld, ld_phase);
-                if (ok) {
-                    ld_phase ^= 1u;
-                    ld_pending = false;
-                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    // phase p's dZ: dL/dy, then dZ1 / dZ2 alternately
-                    const bool upper = p == 2 || p == 4;
-                    const uint32_t dz = p == 0 ? s0 + kBwDy : (p & 1) ? s0 + kBwD1 : s0 + kBwD2;
-                    const uint32_t a_dw = upper ? s0 + kBwZ : dz;
-                    const uint32_t col = p == 0 ? 192u : p <= 2 ? 64u : 128u;
-                    const bool clears = first && !upper;  // the column range's first product this launch
-#pragma unroll
-                    for (int k = 0; k < kTcRows / 16; ++k)
-                        bw_mma(taddr + col, tc_sdesc(a_dw + 256u * k, 128, kTcPlaneA),
-                               tc_sdesc(s0 + kBwH + 256u * k, 128, kTcPlaneA), idesc_w,
-                               uint32_t(k > 0 || !clears));
-                    if (p == 0) {
-                        bw_mma(taddr, tc_sdesc(dz, kTcPlaneA, 128),
-                               tc_sdesc(s0 + kBwW + kHidden * kTcLayerB, 128, kOutRows * 16), idesc_x, 0u);
-                    } else {
-                        const uint32_t wl = s0 + kBwW + uint32_t(kHidden - p) * kTcLayerB;
-#pragma unroll
-                        for (int k = 0; k < kWidth / 16; ++k)
-                            bw_mma(taddr, tc_sdesc(dz + 2u * k * kTcPlaneA, kTcPlaneA, 128),
-                                   tc_sdesc(wl + 256u * k, 128, kWidth * 16), idesc_x, uint32_t(k > 0));
-                    }
-                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                                     mb_mma)
-                                 : "memory");
-                }
-            }
+        // the tile's images (every thread waits: they read the masks)
+        {
+            const bool ok = tc_wait(mb_ld, ld_phase);
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 break;
+            }
+            ld_phase ^= 1u;
+            ld_pending = false;
+        }
+        for (int p = 0; p <= kHidden; ++p) {
+            const uint32_t h = s0 + uint32_t(kBwH + (kHidden - p) * kImg);  // this phase's layer input
+            if (tid == 0) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                // phase p's dZ: dL/dy, then dZ1 / dZ2 alternately
+                const bool upper = p == 2 || p == 4;
+                const uint32_t dz = p == 0 ? s0 + kBwDy : (p & 1) ? s0 + kBwD1 : s0 + kBwD2;
+                const uint32_t a_dw = upper ? s0 + kBwZ : dz;
+                const uint32_t col = p == 0 ? 192u : p <= 2 ? 64u : 128u;
+                const bool clears = first && !upper;  // the column range's first product this launch
+#pragma unroll
+                for (int k = 0; k < kTcRows / 16; ++k)
+                    bw_mma(taddr + col, tc_sdesc(a_dw + 256u * k, 128, kTcPlaneA), tc_sdesc(h + 256u * k, 128, kTcPlaneA),
+                           idesc_w, uint32_t(k > 0 || !clears));
+                if (p == 0) {
+                    bw_mma(taddr, tc_sdesc(dz, kTcPlaneA, 128),
+                           tc_sdesc(s0 + kBwW + kHidden * kTcLayerB, 128, kOutRows * 16), idesc_x, 0u);
+                } else {
+                    const uint32_t wl = s0 + kBwW + uint32_t(kHidden - p) * kTcLayerB;
+#pragma unroll
+                    for (int k = 0; k < kWidth / 16; ++k)
+                        bw_mma(taddr, tc_sdesc(dz + 2u * k * kTcPlaneA, kTcPlaneA, 128),
+                               tc_sdesc(wl + 256u * k, 128, kWidth * 16), idesc_x, uint32_t(k > 0));
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 mb_mma)
+                             : "memory");
+            }
+            // this thread's ReLU mask while the MMAs run: row er, columns
+            // 32 ch .. 32 ch + 31 of the layer input
+            uint4 hm[4];
+            if (p < kHidden) {
+#pragma unroll
+                for (int pl = 0; pl < 4; ++pl)
+                    hm[pl] = *reinterpret_cast<const uint4*>(bsm + kBwH + (kHidden - p) * kImg + (4 * ch + pl) * kTcPlaneA +
+                                                             er * 16);
             }
             mma_pending = true;
             const bool ok2 = tc_wait(mb_mma, mma_phase);
@@ -756,15 +752,10 @@ k_cache_bwd_tc(CacheDev c, const float* q, uint32_t n_max, const uint32_t* slice
                 failed = true;
                 break;
             }
-            // the MMAs are done with H (and dL/dy): the next image comes in
-            if (tid == 0) {
-                if (p < kHidden) {
-                    bw_load(s0, mb_ld, img, dyimg, tile, p + 1);
-                    ld_pending = true;
-                } else if (tile + gridDim.x < tiles) {
-                    bw_load(s0, mb_ld, img, dyimg, tile + gridDim.x, 0);
-                    ld_pending = true;
-                }
+            // after the last phase's MMAs every buffer is free: the next tile's images come in
+            if (p == kHidden && tid == 0 && tile + gridDim.x < tiles) {
+                bw_load(s0, mb_ld, img, dyimg, tile + gridDim.x, nullptr);
+                ld_pending = true;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             if (p < kHidden) {
@@ -777,16 +768,16 @@ k_cache_bwd_tc(CacheDev c, const float* q, uint32_t n_max, const uint32_t* slice
 #pragma unroll
                 for (int pl = 0; pl < 4; ++pl) {
                     const uint32_t hw[4] = {hm[pl].x, hm[pl].y, hm[pl].z, hm[pl].w};
-                    uint32_t h[4];
+                    uint32_t hh[4];
 #pragma unroll
                     for (int e = 0; e < 4; ++e) {
                         const float h0 = __half2float(__ushort_as_half(uint16_t(hw[e] & 0xFFFFu))),
                                     h1 = __half2float(__ushort_as_half(uint16_t(hw[e] >> 16)));
-                        h[e] = pack_half2(h0 > 0.0f ? __uint_as_float(v[8 * pl + 2 * e]) : 0.0f,
-                                          h1 > 0.0f ? __uint_as_float(v[8 * pl + 2 * e + 1]) : 0.0f);
+                        hh[e] = pack_half2(h0 > 0.0f ? __uint_as_float(v[8 * pl + 2 * e]) : 0.0f,
+                                           h1 > 0.0f ? __uint_as_float(v[8 * pl + 2 * e + 1]) : 0.0f);
                     }
                     *reinterpret_cast<uint4*>(dst + (4 * ch + pl) * kTcPlaneA + er * 16) =
-                        make_uint4(h[0], h[1], h[2], h[3]);
+                        make_uint4(hh[0], hh[1], hh[2], hh[3]);
                 }
             } else {
                 // dL/d(encoded features) of row er: columns 16 ch .. 16 ch + 15,
@@ -804,8 +795,7 @@ k_cache_bwd_tc(CacheDev c, const float* q, uint32_t n_max, const uint32_t* slice
                         float w[8];
                         level_corners(c.spec, 8 * ch + j, px, py, pz, idx, w);
 #pragma unroll
-                        for (int k = 0; k < 8; ++k)
-                            grid_grad_add(gs, touched, idx[k], w[k] * d0, w[k] * d1);
+                        for (int k = 0; k < 8; ++k) grid_grad_add(gs, touched, idx[k], w[k] * d0, w[k] * d1);
                     }
                 }
             }
@@ -817,7 +807,7 @@ k_cache_bwd_tc(CacheDev c, const float* q, uint32_t n_max, const uint32_t* slice
     }
     // anything still in flight after a timeout: bounded waits before the
     // buffers and the tensor memory are released
-    if (tid == 0 && ld_pending && !tc_wait(mb_ld, ld_phase)) atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
+    if (ld_pending && !tc_wait(mb_ld, ld_phase) && tid == 0) atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
     if (mma_pending && !tc_wait(mb_mma, mma_phase) && tid == 0) atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
     if (failed) {
         if (tid == 0) atomicOr(status, MRT_STATUS_PIPE_TIMEOUT);
@@ -1263,13 +1253,13 @@ int train_step_launch(mrt_ctx* ctx, mrt_cache* c, const float* q, const float* t
     if (rc) return rc;
     if (cudaMemsetAsync(c->loss, 0, 4, s) != cudaSuccess) return set_error(ctx, MRT_ECUDA, "train: memset");
     if (c->tcgen05) {
-        // forward: one 128-row tile per CTA (up to 4 per SM); backward: two
-        // CTAs per SM, each accumulating the weight gradients of its tiles
+        // forward: one 128-row tile per CTA (up to 4 per SM); backward: one
+        // CTA per SM, each accumulating the weight gradients of its tiles
         const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
         const TrainTc tr{t, c->timg, c->tdy, c->loss};
         k_cache_fwd_tc<true><<<std::min<uint32_t>(tiles, uint32_t(c->sm_count) * 4u), kTcThreads, kTcSmem, s>>>(
             c->dev, q, n, slice, nullptr, ctx->d_status, tr);
-        k_cache_bwd_tc<<<std::min<uint32_t>(tiles, uint32_t(c->sm_count) * 2u), kBwThreads, kBwSmem, s>>>(
+        k_cache_bwd_tc<<<std::min<uint32_t>(tiles, uint32_t(c->sm_count)), kBwThreads, kBwSmem, s>>>(
             c->dev, q, n, slice, c->timg, c->tdy, c->wg, c->gs, c->touched, ctx->d_status);
         ctx->launches += 2;
     } else {
