@@ -1386,6 +1386,92 @@ def run_denoiser_train(args, world, rank, local, dist):
                       "data": "random weights, inputs and targets", "device_status": ctx.status()}))
 
 
+def run_cache_frames(args, world, rank, local, dist):
+    """Learned frames of the radiance cache at 1920 x 1080 (the radiance_cache
+    workload's scene and camera; paths end at the first bounce's hit, 65,536
+    training paths x 4 Adam steps a frame, online training from an empty
+    cache): ms per frame (primary rays + mrt_cuda_cache_frame) by CUDA
+    events over --steps frames after --warmup, with the training on the
+    context's second stream (default) and first on the caller's stream, and
+    with the tcgen05 kernels (default) and the mma.sync ones.  The cache
+    training launch list profiles this command."""
+    from minotert_gb300 import build as _build
+    _build.build()
+    from minotert_gb300 import scene, workloads
+    from minotert_gb300._lib import Context
+    from minotert_gb300.cache import RadianceCache, default_config
+    from minotert_gb300.pathtracer import Camera, Pathtracer, TraceSettings, camera_consts
+
+    base = workloads.heightfield_boxes_256()
+    W, H = 1920, 1080
+    c0 = base.camera
+    cam = Camera((W, H), c0.verticalFov, c0.nearPlane, c0.position, c0.yaw, c0.pitch)
+    mesh = base.mesh()
+    bvh = scene.build_bvh8(mesh)
+    ctx = Context(local)
+    ds = scene.DeviceScene.triangles(ctx, mesh, bvh)
+    ctx.blue_noise(_blue_noise())
+    pt = Pathtracer(ctx, ds, full_gbuffer=False)
+    stream = ctx.stream()
+    col = ctx.alloc(12 * W * H)
+    out = {}
+    for tc, overlap in ((True, True), (True, False), (False, True)):
+        cache = RadianceCache(ctx, default_config(query_vertex=1, train_paths=65536, train_steps=4),
+                              bounds=(mesh.lo, mesh.hi))
+        cache.set_tcgen05(tc)
+        cache.set_overlap(overlap)
+
+        def frames(k, f0):
+            for f in range(k):
+                pt.frame_counter = f0 + f
+                gb = pt.primaryRays((W, H), cam, cam, stream)
+                cache.frame(ds, gb, camera_consts(cam, cam, pt.frame_counter),
+                            TraceSettings(1, 1, 2, 1, True, f).params(base.sky), col, train=True, stream=stream)
+
+        frames(args.warmup, 0)
+        a, b = ctx.event(), ctx.event()
+        ctx.record(a, stream)
+        frames(args.steps, 1000)
+        ctx.record(b, stream)
+        ctx.sync(stream)
+        out[("tcgen05" if tc else "mma_sync") + ("_overlap" if overlap else "_serial")] = \
+            ctx.elapsed_ms(a, b) / args.steps
+        cache.close()
+    # one training step through the explicit API on uniform random samples
+    # (position, normal, direction; targets in [0.1, 1)): forward + backward
+    # alone (gradients accumulate) and with the Adam step, 7,680 rows (about
+    # what a frame's step gets in this scene) and 65,536
+    rng = np.random.default_rng(1)
+    steps_us = {}
+    for n in (7680, 65536):
+        q = np.zeros((n, 9), np.float32)
+        q[:, :3] = rng.uniform(0.02, 0.98, (n, 3))
+        for k in (3, 6):
+            v = rng.normal(size=(n, 3))
+            q[:, k:k + 3] = v / np.linalg.norm(v, axis=1, keepdims=True)
+        t = rng.uniform(0.1, 1.0, (n, 3)).astype(np.float32)
+        d_q, d_t = ctx.to_device(q), ctx.to_device(t)
+        for tc in (True, False):
+            cache = RadianceCache(ctx, default_config(seed=3))
+            cache.set_tcgen05(tc)
+            for upd in (False, True):
+                for _ in range(5):
+                    cache.train_step(d_q, d_t, n, update=upd, stream=stream)
+                a, b = ctx.event(), ctx.event()
+                ctx.record(a, stream)
+                for _ in range(50):
+                    cache.train_step(d_q, d_t, n, update=upd, stream=stream)
+                ctx.record(b, stream)
+                ctx.sync(stream)
+                steps_us[f"{n}_{'tcgen05' if tc else 'mma_sync'}_{'with_adam' if upd else 'fwd_bwd'}"] = \
+                    1000.0 * ctx.elapsed_ms(a, b) / 50
+            cache.close()
+    print(json.dumps({"metric": "learned radiance-cache frame ms (1920x1080, training included)", "unit": "ms",
+                      "value": out["tcgen05_overlap"], "higher_is_better": False, "variants_ms": out,
+                      "train_step_us": steps_us, "steps": args.steps, "warmup": args.warmup,
+                      "device_status": ctx.status()}))
+
+
 def run_post_kernels(args, world, rank, local, dist):
     """Per-frame cost at 1920x1080 of the passes around the path tracer:
     atmosphere + sky-view LUTs, the sky miss shader on 2,073,600
@@ -1486,7 +1572,8 @@ def main(argv=None):
     ap.add_argument("--no-sub-records", action="store_true",
                     help="headline workload only (no heightfield_boxes_256 / batched64 sub-records)")
     ap.add_argument("--workload", choices=["icospheres_1080p", "heightfield_boxes_256", "batched64",
-                                           "radiance_cache", "denoiser", "denoiser_train", "network_kernels", "post_kernels",
+                                           "radiance_cache", "radiance_cache_frames", "denoiser", "denoiser_train",
+                                           "network_kernels", "post_kernels",
                                            "reference_spheres_1080p"],
                     default="icospheres_1080p")
     args = ap.parse_args(argv)
@@ -1500,6 +1587,8 @@ def main(argv=None):
         run_batched(args, world, rank, local, dist)
     elif args.workload == "radiance_cache":
         run_cache_experiment(args, world, rank, local, dist)
+    elif args.workload == "radiance_cache_frames":
+        run_cache_frames(args, world, rank, local, dist)
     elif args.workload == "denoiser":
         run_denoise_experiment(args, world, rank, local, dist)
     elif args.workload == "network_kernels":
