@@ -483,6 +483,9 @@ struct mrt_denoiser {
     bf16* wst = nullptr;          // the 16/32-channel layers' weights for the row-stacked form
     bf16* wup = nullptr;          // per-slice weights of the phase-decomposed upsampling layers
     size_t up_off[kLayers] = {};  // their offsets in wup (upsampling layers only)
+    // tc_mode the re-laid-out weights (wtc, wst, wup) were made for; -1
+    // when the BF16 weights changed since (an Adam step, a parameter write)
+    mutable int relayout_mode = -1;
     // activation tensors (bf16) and their gradients (fp32), sized for n*h*w
     size_t cap_pix = 0, grad_pix = 0;
     bf16* act[kLayers] = {};
@@ -618,13 +621,20 @@ cudaError_t conv(const mrt_denoiser* d, int l, const bf16* a, const bf16* b, int
     return cudaGetLastError();
 }
 
-// kernels forward() launches
-int forward_launches(const mrt_denoiser* d) { return 13 + (d->tc_mode != 0 ? 1 : 0) + (d->tc_mode == 2 ? 3 : 0); }
+// whether forward() re-lays out the weights for the tensor-core kernels
+// (only after they changed: inference with fixed weights does it once)
+bool needs_relayout(const mrt_denoiser* d) { return d->tc_mode != 0 && d->relayout_mode != d->tc_mode; }
+
+// kernels the next forward() launches
+int forward_launches(const mrt_denoiser* d) {
+    return 13 + (needs_relayout(d) ? 1 + (d->tc_mode == 2 ? 3 : 0) : 0);  // 11 convolutions, 2 pools
+}
 
 // forward of the whole network over n images of h x w (h, w multiples of 4)
 cudaError_t forward(const mrt_denoiser* d, const bf16* in, int n, int h, int w, cudaStream_t s) {
     cudaError_t e;
-    if (d->tc_mode != 0) {  // the TMA convolutions read the weights per slice
+    if (needs_relayout(d)) {  // the TMA convolutions read the weights per slice
+        d->relayout_mode = d->tc_mode;
         TcLayerTable t{};
         t.count = kLayers;
         for (int l = 0; l < kLayers; ++l) {
@@ -905,10 +915,11 @@ int mrt_cuda_denoiser_infer(mrt_ctx* ctx, mrt_denoiser* d, const uint16_t* featu
     int rc = ensure_acts(ctx, d, pix, false);
     if (rc) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int fl = forward_launches(d);
     if (forward(d, reinterpret_cast<const bf16*>(features), int(batch), int(height), int(width), s) != cudaSuccess)
         return set_error(ctx, MRT_ECUDA, "denoiser_infer: launch");
     k_decode<<<grid_for(pix), 256, 0, s>>>(d->act[kLayers - 1], reinterpret_cast<const bf16*>(features), pix, out);
-    ctx->launches += forward_launches(d) + 1;  // + decode
+    ctx->launches += fl + 1;  // + decode
     return MRT_OK;
 }
 
@@ -924,6 +935,7 @@ int mrt_cuda_denoiser_train_step(mrt_ctx* ctx, mrt_denoiser* d, const uint16_t* 
     if (rc) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const bf16* in = reinterpret_cast<const bf16*>(features);
+    const int fl = forward_launches(d);
     if (forward(d, in, n, h, w, s) != cudaSuccess) return set_error(ctx, MRT_ECUDA, "denoiser_train: forward");
     cudaMemsetAsync(d->loss, 0, 4, s);
     if (d->tc_mode == 2) {
@@ -932,7 +944,7 @@ int mrt_cuda_denoiser_train_step(mrt_ctx* ctx, mrt_denoiser* d, const uint16_t* 
         int launched = 0;
         if (backward_tc(d, in, n, h, w, s, &launched) != cudaSuccess)
             return set_error(ctx, MRT_ECUDA, "denoiser_train: backward");
-        ctx->launches += forward_launches(d) + 1 + launched;  // + loss
+        ctx->launches += fl + 1 + launched;  // + loss
     } else {
         k_l1_loss<<<grid_for(pix), 256, 0, s>>>(d->act[kLayers - 1], in, targets, pix, d->grad[kLayers - 1], nullptr,
                                                d->loss);
@@ -963,6 +975,7 @@ int mrt_cuda_denoiser_train_step(mrt_ctx* ctx, mrt_denoiser* d, const uint16_t* 
         const float bc1 = 1.0f - std::pow(b1, float(d->step)), bc2 = 1.0f - std::pow(b2, float(d->step));
         k_adam_bf16<<<grid_for(d->n_w), 256, 0, s>>>(d->w, d->wm, d->wv, d->wg, d->w16, d->n_w, lr, b1, b2, eps, bc1,
                                                      bc2);
+        d->relayout_mode = -1;
         k_adam_bf16<<<grid_for(d->n_b), 256, 0, s>>>(d->w + d->n_w, d->wm + d->n_w, d->wv + d->n_w, d->wg + d->n_w,
                                                      nullptr, d->n_b, lr, b1, b2, eps, bc1, bc2);
     }
@@ -990,6 +1003,7 @@ int mrt_cuda_denoiser_params(mrt_ctx* ctx, mrt_denoiser* d, int which, float* ho
         std::vector<bf16> w16(d->n_w);
         for (size_t i = 0; i < d->n_w; ++i) w16[i] = __float2bfloat16_rn(host[i]);
         cudaMemcpy(d->w16, w16.data(), d->n_w * 2, cudaMemcpyHostToDevice);
+        d->relayout_mode = -1;
     }
     return MRT_OK;
 }
