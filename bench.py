@@ -283,8 +283,12 @@ def frame_record(args, name, steps, warmup, world, rank, local, dist, cpu=True, 
     ctx.frame_stats()
     assert ctx.status() == 0
 
+    # the timed frames run without the per-launch events of the pass
+    # breakdown (about 50 event records a frame on the stream); the
+    # breakdown takes its own frames afterwards
     ev = [(ctx.event(), ctx.event()) for _ in range(steps)]
-    ctx.set_timing(True)
+    ctx.set_timing(False)
+    ctx.frame_stats()
     if dist is not None:
         dist.barrier()
     clocks = ClockSampler(local)
@@ -299,9 +303,18 @@ def frame_record(args, name, steps, warmup, world, rank, local, dist, cpu=True, 
     clk = clocks.stop()
     ms = [ctx.elapsed_ms(a, b) for a, b in ev]
     st = ctx.frame_stats()
-    ctx.set_timing(False)
     if dist is not None:
         dist.barrier()
+    # per-pass breakdown: more frames of the same kind with events around
+    # every launch
+    n_bd = max(1, min(steps, 100))
+    ctx.set_timing(True)
+    for k in range(n_bd):
+        flush.zero(stream)
+        frame(warmup + steps + 100 + k)
+    ctx.sync(stream)
+    st_bd = ctx.frame_stats()
+    ctx.set_timing(False)
     status = ctx.status()
     total_ms = sum(ms)
     prim = int(st.primary_rays)
@@ -378,20 +391,22 @@ def frame_record(args, name, steps, warmup, world, rank, local, dist, cpu=True, 
                  "timed ones; issue_ncu: issue-slot use and SIMD efficiency of the same kernel from the "
                  "committed ncu summary (the binding resource once the data is on chip)" % n_alone})
 
-    b2 = sum(ext[1:])
-    b2_ms = sum(st.ms_extend_b[1:s.bounces])
+    ext_bd = [int(x) for x in st_bd.extension_rays]
+    b2 = sum(ext_bd[1:])
+    b2_ms = sum(st_bd.ms_extend_b[1:s.bounces])
     breakdown = {
-        "primary_mrays_s": prim / (st.ms_primary / 1e3) / 1e6 if st.ms_primary else None,
-        "bounce1_mrays_s": ext[0] / (st.ms_extend_b[0] / 1e3) / 1e6 if st.ms_extend_b[0] else None,
+        "primary_mrays_s": int(st_bd.primary_rays) / (st_bd.ms_primary / 1e3) / 1e6 if st_bd.ms_primary else None,
+        "bounce1_mrays_s": ext_bd[0] / (st_bd.ms_extend_b[0] / 1e3) / 1e6 if st_bd.ms_extend_b[0] else None,
         "bounce2plus_mrays_s": b2 / (b2_ms / 1e3) / 1e6 if b2_ms else None,
-        "shadow_mrays_s": st.shadow_rays / (st.ms_shadow / 1e3) / 1e6 if st.ms_shadow else None,
+        "shadow_mrays_s": st_bd.shadow_rays / (st_bd.ms_shadow / 1e3) / 1e6 if st_bd.ms_shadow else None,
         "all_rays_incl_shadow_mrays_s": (rays + int(st.shadow_rays)) / (total_ms / 1e3) / 1e6,
         "rays_per_frame": {"primary": prim / steps, "extension": [e / steps for e in ext[:s.bounces]],
                            "shadow": st.shadow_rays / steps},
         "frame_ms": {"median": statistics.median(ms), "min": min(ms), "max": max(ms),
                      "first_10_mean": statistics.mean(ms[:10])},
-        "ms_per_frame": {"primary": st.ms_primary / steps, "extend": st.ms_extend / steps,
-                         "shadow": st.ms_shadow / steps, "shade": st.ms_shade / steps},
+        "ms_per_frame": {"primary": st_bd.ms_primary / n_bd, "extend": st_bd.ms_extend / n_bd,
+                         "shadow": st_bd.ms_shadow / n_bd, "shade": st_bd.ms_shade / n_bd},
+        "breakdown_frames": n_bd,
         "note": "tail_bounce %d: the paths alive at that bounce finish in one persistent launch (k_tail), "
                 "timed as extension of that bounce; its shading and shadow rays are inside that time, so "
                 "shadow_mrays_s divides all shadow rays by the wavefront shadow launches' time only. "
@@ -402,26 +417,57 @@ def frame_record(args, name, steps, warmup, world, rank, local, dist, cpu=True, 
 
     # end to end through the C ABI with host buffers: camera and trace
     # parameters in, the frame's colour image out (the g-buffer stays on the
-    # device, as between the reference's passes)
-    col_h = ctx.host_alloc((H, W, 3), np.float32)
+    # device, as between the reference's passes).  Headline: frames in
+    # flight (mrt_cuda_render_frame_host_async: each frame's colour read-back
+    # overlaps the next frame's passes; host wall clock from the first call
+    # to mrt_cuda_frames_wait after the last); beside it the blocking call,
+    # which waits for each frame's read-back.  The L2 is flushed before each
+    # frame, inside the timed region, as between the device-timed frames
+    col_h = [ctx.host_alloc((H, W, 3), np.float32) for _ in range(2)]
     params = TraceSettings(s.samples, s.bounces, s.rr_start, s.rng_mode).params(wl.sky)
+    params.accumulate = 0
+
+    def e2e_frame(k, asynchronous):
+        consts = camera_consts(wl.camera, wl.camera, k)
+        flush.zero(stream)
+        if asynchronous:
+            ctx.check(lib().mrt_cuda_render_frame_host_async(ctx.handle, ds.handle, C.byref(consts), C.byref(params),
+                                                             W, H, ptr(col_h[k % 2]), C.c_void_p(stream)),
+                      "frame_async")
+        else:
+            ctx.check(lib().mrt_cuda_render_frame_host(ctx.handle, ds.handle, C.byref(consts), C.byref(params), W, H,
+                                                       None, None, ptr(col_h[0]), C.c_void_p(stream)), "frame")
+
     e2e_ms = []
     ctx.frame_stats()
     for k in range(warmup + steps):
-        consts = camera_consts(wl.camera, wl.camera, k)
         if k == warmup:
             ctx.frame_stats()
         t0 = time.perf_counter()
-        ctx.check(lib().mrt_cuda_render_frame_host(ctx.handle, ds.handle, C.byref(consts), C.byref(params), W, H,
-                                                   None, None, ptr(col_h), C.c_void_p(stream)), "frame")
+        e2e_frame(k, False)
         if k >= warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
     est = ctx.frame_stats()
     e2e_rays = int(est.primary_rays) + sum(int(x) for x in est.extension_rays)
-    e2e_val = _allsum(dist, float(e2e_rays)) / _allmax(dist, sum(e2e_ms) / 1e3) / 1e6
+    blocking_val = _allsum(dist, float(e2e_rays)) / _allmax(dist, sum(e2e_ms) / 1e3) / 1e6
+    for k in range(warmup):
+        e2e_frame(k, True)
+    ctx.check(lib().mrt_cuda_frames_wait(ctx.handle), "frames_wait")
+    ctx.frame_stats()
+    t0 = time.perf_counter()
+    for k in range(warmup, warmup + steps):
+        e2e_frame(k, True)
+    ctx.check(lib().mrt_cuda_frames_wait(ctx.handle), "frames_wait")
+    async_ms = (time.perf_counter() - t0) * 1e3
+    est = ctx.frame_stats()
+    async_rays = int(est.primary_rays) + sum(int(x) for x in est.extension_rays)
+    e2e_val = _allsum(dist, float(async_rays)) / _allmax(dist, async_ms / 1e3) / 1e6
     e2e = {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 336 + 80,
-           "d2h_bytes_per_step": W * H * 12, "ms_per_step": statistics.mean(e2e_ms),
-           "api": "mrt_cuda_render_frame_host"}
+           "d2h_bytes_per_step": W * H * 12, "ms_per_step": async_ms / steps,
+           "api": "mrt_cuda_render_frame_host_async (two frames in flight) + mrt_cuda_frames_wait",
+           "l2": "256 MiB memset before each frame, inside the timed region",
+           "blocking": {"value": blocking_val, "ms_per_step": statistics.mean(e2e_ms),
+                        "api": "mrt_cuda_render_frame_host (waits for each frame's read-back)"}}
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
            "warmup": warmup, "ms_per_step": _allmax(dist, total_ms / steps), "higher_is_better": True,

@@ -727,6 +727,24 @@ int mrt_cuda_render_frame_host(mrt_ctx* ctx, const mrt_scene* scene,
                                uint32_t* visibility, float* hit_t, float* color,
                                void* stream);
 
+/* The same frame with the read-back in flight: primary + secondary passes on
+ * `stream` into one of two library-owned colour buffers (alternating per
+ * call), then the colour copied to `color` (host, pinned for an
+ * asynchronous copy) on a stream of the context; returns without
+ * synchronising, so the next frame's passes overlap this frame's copy.
+ * `color` must not be read, and a buffer passed here not reused, before
+ * mrt_cuda_frames_wait returns.  Frames in flight do not accumulate:
+ * params->accumulate must be 0 (MRT_EINVAL otherwise).  Same image as
+ * mrt_cuda_render_frame_host. */
+int mrt_cuda_render_frame_host_async(mrt_ctx* ctx, const mrt_scene* scene,
+                                     const mrt_camera_consts* consts,
+                                     const mrt_trace_params* params,
+                                     uint32_t width, uint32_t height, float* color,
+                                     void* stream);
+/* Waits until every colour read-back of mrt_cuda_render_frame_host_async
+ * has reached the host. */
+int mrt_cuda_frames_wait(mrt_ctx* ctx);
+
 #ifdef __cplusplus
 }
 #endif

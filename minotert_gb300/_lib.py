@@ -183,6 +183,9 @@ def lib() -> C.CDLL:
             "mrt_cuda_trace_rays_counted": ([vp, vp, vp, u32, vp, vp, vp, vp], i32),
             "mrt_cuda_render_frame_host": ([vp, vp, C.POINTER(CameraConsts), C.POINTER(TraceParams), u32, u32,
                                             vp, vp, vp, vp], i32),
+            "mrt_cuda_render_frame_host_async": ([vp, vp, C.POINTER(CameraConsts), C.POINTER(TraceParams), u32,
+                                                  u32, vp, vp], i32),
+            "mrt_cuda_frames_wait": ([vp], i32),
             "mrt_cuda_primary_rays_noalloc": ([vp, u32, vp, u32, vp, u32, C.POINTER(CameraConsts),
                                                C.POINTER(GBuffer), vp, vp], i32),
             "mrt_cuda_cache_create": ([vp, C.POINTER(CacheConfig), pp], i32),

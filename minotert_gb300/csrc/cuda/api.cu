@@ -260,6 +260,12 @@ int mrt_cuda_destroy(mrt_ctx* ctx) {
     cudaFree(ctx->d_aux);
     cudaFree(ctx->d_t);
     cudaFree(ctx->d_color);
+    for (int b = 0; b < 2; ++b) {
+        cudaFree(ctx->d_color_async[b]);
+        if (ctx->ev_rendered[b]) cudaEventDestroy(ctx->ev_rendered[b]);
+        if (ctx->ev_copied[b]) cudaEventDestroy(ctx->ev_copied[b]);
+    }
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     for (auto& r : ctx->recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     for (auto e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->side) cudaStreamDestroy(ctx->side);
@@ -873,12 +879,13 @@ int mrt_cuda_trace_rays_counted(mrt_ctx* ctx, const mrt_scene* scene, const mrt_
     return MRT_OK;
 }
 
-int mrt_cuda_render_frame_host(mrt_ctx* ctx, const mrt_scene* scene, const mrt_camera_consts* consts,
-                               const mrt_trace_params* params, uint32_t width, uint32_t height, uint32_t* visibility,
-                               float* hit_t, float* color, void* stream) {
-    if (!ctx || !scene || !consts || !params || !color || width == 0 || height == 0)
-        return fail(ctx, MRT_EINVAL, "render_frame_host: bad arguments");
-    cudaSetDevice(ctx->device);
+} // extern "C"
+
+namespace {
+
+// The library-owned g-buffer of the host-buffer frame entry points, sized
+// for width x height (reallocated when the size changes).
+int frame_gbuffer(mrt_ctx* ctx, const mrt_scene* scene, uint32_t width, uint32_t height, mrt_gbuffer& g) {
     const size_t npix = size_t(width) * height;
     if (ctx->frame_pixels != npix) {
         cudaFree(ctx->d_vis); cudaFree(ctx->d_aux); cudaFree(ctx->d_t); cudaFree(ctx->d_color);
@@ -891,7 +898,6 @@ int mrt_cuda_render_frame_host(mrt_ctx* ctx, const mrt_scene* scene, const mrt_c
         MRT_CK(cudaMemset(ctx->d_color, 0, npix * 3 * sizeof(float)));
         ctx->frame_pixels = npix;
     }
-    mrt_gbuffer g;
     std::memset(&g, 0, sizeof(g));
     g.visibility = ctx->d_vis;
     g.hit_t = ctx->d_t;
@@ -901,7 +907,24 @@ int mrt_cuda_render_frame_host(mrt_ctx* ctx, const mrt_scene* scene, const mrt_c
     }
     g.width = width;
     g.height = height;
-    int rc = mrt_cuda_primary_rays(ctx, scene, consts, &g, stream);
+    return MRT_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int mrt_cuda_render_frame_host(mrt_ctx* ctx, const mrt_scene* scene, const mrt_camera_consts* consts,
+                               const mrt_trace_params* params, uint32_t width, uint32_t height, uint32_t* visibility,
+                               float* hit_t, float* color, void* stream) {
+    if (!ctx || !scene || !consts || !params || !color || width == 0 || height == 0)
+        return fail(ctx, MRT_EINVAL, "render_frame_host: bad arguments");
+    cudaSetDevice(ctx->device);
+    const size_t npix = size_t(width) * height;
+    mrt_gbuffer g;
+    int rc = frame_gbuffer(ctx, scene, width, height, g);
+    if (rc) return rc;
+    rc = mrt_cuda_primary_rays(ctx, scene, consts, &g, stream);
     if (rc) return rc;
     rc = mrt_cuda_secondary_rays(ctx, scene, &g, consts, params, ctx->d_color, stream);
     if (rc) return rc;
@@ -910,6 +933,58 @@ int mrt_cuda_render_frame_host(mrt_ctx* ctx, const mrt_scene* scene, const mrt_c
     if (hit_t) MRT_CK(cudaMemcpyAsync(hit_t, ctx->d_t, npix * 4, cudaMemcpyDeviceToHost, s));
     MRT_CK(cudaMemcpyAsync(color, ctx->d_color, npix * 12, cudaMemcpyDeviceToHost, s));
     MRT_CK(cudaStreamSynchronize(s));
+    return MRT_OK;
+}
+
+int mrt_cuda_render_frame_host_async(mrt_ctx* ctx, const mrt_scene* scene, const mrt_camera_consts* consts,
+                                     const mrt_trace_params* params, uint32_t width, uint32_t height, float* color,
+                                     void* stream) {
+    if (!ctx || !scene || !consts || !params || !color || width == 0 || height == 0)
+        return fail(ctx, MRT_EINVAL, "render_frame_host_async: bad arguments");
+    if (params->accumulate)
+        return fail(ctx, MRT_EINVAL, "render_frame_host_async: frames in flight do not accumulate");
+    cudaSetDevice(ctx->device);
+    const size_t npix = size_t(width) * height;
+    mrt_gbuffer g;
+    int rc = frame_gbuffer(ctx, scene, width, height, g);
+    if (rc) return rc;
+    if (!ctx->copy_stream) {
+        MRT_CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        for (int b = 0; b < 2; ++b) {
+            MRT_CK(cudaEventCreateWithFlags(&ctx->ev_rendered[b], cudaEventDisableTiming));
+            MRT_CK(cudaEventCreateWithFlags(&ctx->ev_copied[b], cudaEventDisableTiming));
+        }
+    }
+    if (ctx->async_pixels != npix) {
+        MRT_CK(cudaStreamSynchronize(ctx->copy_stream));
+        for (int b = 0; b < 2; ++b) {
+            cudaFree(ctx->d_color_async[b]);
+            ctx->d_color_async[b] = nullptr;
+        }
+        ctx->async_pixels = 0;
+        for (int b = 0; b < 2; ++b) MRT_CK(cudaMalloc(&ctx->d_color_async[b], npix * 3 * sizeof(float)));
+        ctx->async_pixels = npix;
+    }
+    cudaStream_t s = as_stream(stream);
+    const uint32_t b = ctx->async_next;
+    ctx->async_next ^= 1u;
+    // buffer b is free once the read-back of the frame before last is done
+    MRT_CK(cudaStreamWaitEvent(s, ctx->ev_copied[b], 0));
+    rc = mrt_cuda_primary_rays(ctx, scene, consts, &g, stream);
+    if (rc) return rc;
+    rc = mrt_cuda_secondary_rays(ctx, scene, &g, consts, params, ctx->d_color_async[b], stream);
+    if (rc) return rc;
+    MRT_CK(cudaEventRecord(ctx->ev_rendered[b], s));
+    MRT_CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_rendered[b], 0));
+    MRT_CK(cudaMemcpyAsync(color, ctx->d_color_async[b], npix * 12, cudaMemcpyDeviceToHost, ctx->copy_stream));
+    MRT_CK(cudaEventRecord(ctx->ev_copied[b], ctx->copy_stream));
+    return MRT_OK;
+}
+
+int mrt_cuda_frames_wait(mrt_ctx* ctx) {
+    if (!ctx) return MRT_EINVAL;
+    cudaSetDevice(ctx->device);
+    if (ctx->copy_stream) MRT_CK(cudaStreamSynchronize(ctx->copy_stream));
     return MRT_OK;
 }
 

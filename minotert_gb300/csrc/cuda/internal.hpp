@@ -229,6 +229,14 @@ struct mrt_ctx {
     float* d_t = nullptr;
     float* d_color = nullptr;
     size_t frame_pixels = 0;
+    // render_frame_host_async: two colour buffers in flight, read back on a
+    // copy stream; ev_rendered[b] / ev_copied[b]: buffer b's frame is
+    // rendered / read back
+    float* d_color_async[2] = {nullptr, nullptr};
+    size_t async_pixels = 0;
+    uint32_t async_next = 0;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_rendered[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
     // timing
     bool timing = false;
     bool counters = false;

@@ -13,7 +13,8 @@ import pytest
 
 import oracle
 from conftest import oracle_consts, random_rays
-from minotert_gb300._lib import (HIT_DTYPE, MRT_MISS, MRT_STATUS_BAD_NODE, MRT_STATUS_BAD_TRI, RAY_DTYPE, lib, ptr)
+from minotert_gb300._lib import (HIT_DTYPE, MRT_EINVAL, MRT_MISS, MRT_STATUS_BAD_NODE, MRT_STATUS_BAD_TRI, RAY_DTYPE,
+                                 lib, ptr)
 from minotert_gb300.pathtracer import Camera, Pathtracer, Sky, TraceSettings, camera_consts
 from minotert_gb300.scene import DeviceScene, reference_spheres
 
@@ -326,6 +327,39 @@ def test_render_frame_host_matches_passes(ctx, hf_workload, hf_scene, blue_noise
                                                wl.width, wl.height, ptr(vis), ptr(ht), ptr(col), None), "frame")
     assert np.array_equal(vis, g["visibility"])
     assert np.array_equal(col, img)
+
+
+def test_render_frame_host_async_matches_blocking(ctx, hf_workload, hf_scene, blue_noise):
+    # frames in flight (two colour buffers, read-backs on the context's copy
+    # stream) give each frame the same image as the blocking entry point
+    import ctypes as C
+    wl, mesh, bvh = hf_workload
+    params = wl.settings.params(wl.sky)
+    params.accumulate = 0
+    frames = (3, 4, 5)
+    ref = {}
+    for f in frames:
+        col = np.zeros((wl.height, wl.width, 3), np.float32)
+        consts = camera_consts(wl.camera, wl.camera, f)
+        ctx.check(lib().mrt_cuda_render_frame_host(ctx.handle, hf_scene.handle, C.byref(consts), C.byref(params),
+                                                   wl.width, wl.height, None, None, ptr(col), None), "frame")
+        ref[f] = col
+    out = {f: ctx.host_alloc((wl.height, wl.width, 3), np.float32) for f in frames}
+    stream = ctx.stream()
+    for f in frames:
+        consts = camera_consts(wl.camera, wl.camera, f)
+        ctx.check(lib().mrt_cuda_render_frame_host_async(ctx.handle, hf_scene.handle, C.byref(consts),
+                                                         C.byref(params), wl.width, wl.height, ptr(out[f]),
+                                                         C.c_void_p(stream)), "frame_async")
+    ctx.check(lib().mrt_cuda_frames_wait(ctx.handle), "frames_wait")
+    assert ctx.status() == 0
+    for f in frames:
+        assert np.array_equal(np.asarray(out[f]), ref[f]), f
+    params.accumulate = 1
+    consts = camera_consts(wl.camera, wl.camera, 6)
+    rc = lib().mrt_cuda_render_frame_host_async(ctx.handle, hf_scene.handle, C.byref(consts), C.byref(params),
+                                                wl.width, wl.height, ptr(out[3]), C.c_void_p(stream))
+    assert rc == MRT_EINVAL
 
 
 def test_corrupt_bvh_reports_status_not_hang(ctx, hf_workload, blue_noise):
