@@ -6,8 +6,9 @@ closest hit) plus a 4-bounce Lambertian path trace with Russian roulette
 after bounce 2 and a directional-light shadow ray per vertex, accumulated
 into RGB32F.  `value` counts primary + diffuse extension rays per second
 with the scene resident in HBM and the L2 flushed between timed steps;
-`e2e` is the same metric through mrt_cuda_render_frame_host with host
-buffers (results copied back every step).
+`e2e` is the same metric through mrt_cuda_render_frame_host_async with host
+buffers (each step's colour image copied back, two frames in flight; the
+blocking mrt_cuda_render_frame_host beside it).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mine|reference]
 """
