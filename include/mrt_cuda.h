@@ -286,7 +286,10 @@ typedef struct mrt_tuning {
                                      the extension rays of bounce b trace on
                                      two streams at once (a stream of the
                                      context joined before shading; same
-                                     image)                                  */
+                                     image); 2: both queues in one
+                                     persistent launch (warps refill from
+                                     the extension queue, then the shadow
+                                     queue; same image)                      */
     uint32_t tail_from_hits;      /* 1: bounce tail_bounce is traced by the
                                      wavefront kernel and the path tail
                                      starts from its hits (shading that

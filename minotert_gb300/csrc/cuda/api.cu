@@ -320,7 +320,7 @@ static uint32_t refill_min(const mrt_ctx* ctx) { return ctx->tuning.refill_min ?
 int mrt_cuda_set_tuning(mrt_ctx* ctx, const mrt_tuning* tuning) {
     if (!ctx || !tuning) return fail(ctx, MRT_EINVAL, "set_tuning: null argument");
     if (tuning->trace_blocks_per_sm > 64 || tuning->dynamic_fetch > 3 || tuning->primary_persistent > 1 ||
-        tuning->tail_bounce > MRT_MAX_BOUNCES || tuning->tri_spread > 15 || tuning->refill_min > 32 || tuning->overlap_shadow > 1 ||
+        tuning->tail_bounce > MRT_MAX_BOUNCES || tuning->tri_spread > 15 || tuning->refill_min > 32 || tuning->overlap_shadow > 2 ||
         tuning->tail_from_hits > 1 ||
         (tuning->stack_depth != 0u && tuning->stack_depth != 16u && tuning->stack_depth != 24u &&
          tuning->stack_depth != 32u))
@@ -716,14 +716,16 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
             const bool tail_from_hits = ctx->tuning.tail_from_hits != 0u;
             const bool tail_now = tail != 0u && b >= tail && !tail_from_hits;
             const bool overlap = nee && overlap_sh && !tail_now;
-            if (overlap) {
+            // overlap_shadow 2: both queues in one persistent launch instead
+            const bool merged = overlap && ctx->tuning.overlap_shadow == 2u;
+            if (overlap && !merged) {
                 MRT_CK(cudaEventRecord(ctx->ev_fork, s));
                 MRT_CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
                 MRT_LAUNCH_ON(ctx->side, 2, int(b - 1),
                               launch_trace_shadow(scene->dev, wb, tp, b - 1, tblocks, ctx->d_status, ctx->counters,
                                                   dyn_sh, refill_min(ctx), ctx->side));
                 MRT_CK(cudaEventRecord(ctx->ev_join, ctx->side));
-            } else if (nee) {
+            } else if (nee && !overlap) {
                 MRT_LAUNCH(2, int(b - 1), launch_trace_shadow(scene->dev, wb, tp, b - 1, tblocks, ctx->d_status,
                                                               ctx->counters, dyn_sh, refill_min(ctx), s));
             }
@@ -738,9 +740,13 @@ int mrt_cuda_secondary_rays(mrt_ctx* ctx, const mrt_scene* scene, const mrt_gbuf
                                                       params->sort_rays ? 0u : ctx->tuning.sort_min_rays, s));
                 ctx->launches += 2;  // histogram, scan, scatter
             }
-            MRT_LAUNCH(1, int(b), launch_trace_ext(scene->dev, wb, b, tblocks, ctx->d_status, ctx->counters, dyn,
-                                                   refill_min(ctx), s));
-            if (overlap) MRT_CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
+            if (merged)
+                MRT_LAUNCH(1, int(b), launch_trace_merged(scene->dev, wb, tp, b, tblocks, ctx->d_status,
+                                                          refill_min(ctx), s));
+            else
+                MRT_LAUNCH(1, int(b), launch_trace_ext(scene->dev, wb, b, tblocks, ctx->d_status, ctx->counters, dyn,
+                                                       refill_min(ctx), s));
+            if (overlap && !merged) MRT_CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
             if (tail != 0u && b >= tail) {  // (tail_from_hits)
                 MRT_LAUNCH(1, int(b), launch_tail(scene->dev, tp, bn, wb, W, b, true, (ctx->tuning.tri_spread & 8u) != 0u,
                                                   tblocks, ctx->d_status, s));

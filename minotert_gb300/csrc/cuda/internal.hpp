@@ -170,6 +170,8 @@ cudaError_t launch_trace_ext(const DevScene& sc, const WaveBuffers& wb, uint32_t
 cudaError_t launch_trace_shadow(const DevScene& sc, const WaveBuffers& wb, const TraceParams& tp,
                                 uint32_t vertex, int blocks, uint32_t* status, bool count, int mode,
                                 uint32_t refill_min, cudaStream_t s);
+cudaError_t launch_trace_merged(const DevScene& sc, const WaveBuffers& wb, const TraceParams& tp, uint32_t bounce,
+                                int blocks, uint32_t* status, uint32_t refill_min, cudaStream_t s);
 cudaError_t launch_shade(const DevScene& sc, const TraceParams& tp, BlueNoise bn, const WaveBuffers& wb,
                          uint32_t width, uint32_t bounce, uint32_t* status, cudaStream_t s);
 // every path of the bounce-`first` extension queue to its end (k_tail);

@@ -990,6 +990,73 @@ cudaError_t launch_trace_shadow(const DevScene& sc, const WaveBuffers& wb, const
     return cudaGetLastError();
 }
 
+// The extension rays of bounce `bounce` and the shadow rays of vertex
+// `vertex` = bounce - 1 in one persistent launch (mrt_tuning.overlap_shadow
+// 2).  The two queues are independent — only the shadow rays add radiance,
+// each pixel at most once per vertex, and the shading after this launch
+// adds the next — so a warp refills its idle lanes from the extension queue
+// and, once that is drained, from the shadow queue, and steps all its rays
+// together with the mixed spread step (closest hit or any hit per lane,
+// the triangle tests spread over the warp).  The GPU then drains one wave
+// tail instead of two launches', which two streams overlap only in part
+// (a launch's resident blocks take all of an SM's registers).  Same hits
+// and the same radiance additions as the two launches.
+__global__ void __launch_bounds__(kTraceBlock, kTraceMinBlocks)
+k_trace_merged(DevScene sc, WaveBuffers wb, TraceParams tp, uint32_t bounce, uint32_t vertex, uint32_t* status,
+               uint32_t refill_min) {
+    __shared__ uint2 stk[kStackDepth * kTraceBlock];
+    __shared__ unsigned long long slots[kTraceBlock];
+    const uint32_t n_ext = wb.counters[kCntExt + bounce], n_sh = wb.counters[kCntShadow + vertex];
+    uint2* my = stk + threadIdx.x;
+    uint32_t st = 0u;
+    Trav s{};
+    bool have = false, any_hit = false, ext_done = false, sh_done = false;
+    uint32_t ri = 0u;
+    while (true) {
+        if (!ext_done) {  // warp-uniform (warp_refill sets it from the warp's shared fetch)
+            const uint32_t idx = warp_refill(wb.counters + kCntFetchExt + bounce, n_ext, !have, ext_done, refill_min);
+            if (idx != kMiss) {
+                const PathRay* q = ext_queue(wb, bounce);
+                const float4 a = q[idx].o_pix, b = q[idx].d;
+                trav_init(s, f3{a.x, a.y, a.z}, f3{b.x, b.y, b.z}, 0.0f, INFINITY);
+                ri = idx;
+                have = true;
+                any_hit = false;
+            }
+        }
+        if (ext_done) {
+            const uint32_t idx =
+                warp_refill(wb.counters + kCntFetchShadow + vertex, n_sh, !have, sh_done, refill_min);
+            if (idx != kMiss) {
+                const float4 a = wb.sq[idx].o_pix;
+                trav_init(s, f3{a.x, a.y, a.z}, f3{tp.sun[0], tp.sun[1], tp.sun[2]}, 0.0f, INFINITY);
+                ri = idx;
+                have = true;
+                any_hit = true;
+            }
+        }
+        if (!__any_sync(0xFFFFFFFFu, have)) break;
+        const bool fin = trav_step_spread_mixed<kStackDepth>(sc, s, have, any_hit, my, kTraceBlock, st,
+                                                             slots + (threadIdx.x & ~31u));
+        if (have && fin) {
+            if (!any_hit) {
+                wb.hits[ri] = make_uint2(s.best, __float_as_uint(s.best == kMiss ? s.tmax : s.tbest));
+            } else if (s.best == kMiss) {
+                const ShadowRay sr = wb.sq[ri];
+                add_L(wb.L, __float_as_uint(sr.o_pix.w), f3{sr.contrib.x, sr.contrib.y, sr.contrib.z});
+            }
+            have = false;
+        }
+    }
+    if (st) atomicOr(status, st);
+}
+
+cudaError_t launch_trace_merged(const DevScene& sc, const WaveBuffers& wb, const TraceParams& tp, uint32_t bounce,
+                                int blocks, uint32_t* status, uint32_t refill_min, cudaStream_t s) {
+    k_trace_merged<<<blocks, kTraceBlock, 0, s>>>(sc, wb, tp, bounce, bounce - 1u, status, refill_min);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_shade(const DevScene& sc, const TraceParams& tp, BlueNoise bn, const WaveBuffers& wb,
                          uint32_t width, uint32_t bounce, uint32_t* status, cudaStream_t s) {
     k_shade<<<shade_blocks(uint32_t(wb.cap)), kShadeBlock, 0, s>>>(sc, tp, bn, wb, width, bounce, status);

@@ -84,7 +84,8 @@ def test_spread_primary_matches_oracle(ctx, hf_workload, size):
 @pytest.mark.parametrize("tail", [0, 3])
 def test_overlapped_shadow_rays_same_image(ctx, hf_workload, blue_noise, tail):
     # shadow rays of vertex b - 1 on a second stream beside the extension
-    # rays of bounce b: the same image and ray counts
+    # rays of bounce b, or both in one merged launch: the same image and ray
+    # counts
     wl, mesh, bvh = hf_workload
     ds = DeviceScene.triangles(ctx, mesh, bvh)
     settings = TraceSettings(samples=2, bounces=5, rr_start=1, rng_mode=1)
@@ -95,10 +96,14 @@ def test_overlapped_shadow_rays_same_image(ctx, hf_workload, blue_noise, tail):
         ctx.set_tuning(overlap_shadow=1)
         img, e, sh = _render(ctx, ds, wl, blue_noise, settings, 3, tail)
         assert int(ctx.tuning().overlap_shadow) == 1
+        # both queues in one persistent launch
+        ctx.set_tuning(overlap_shadow=2)
+        img2, e2, sh2 = _render(ctx, ds, wl, blue_noise, settings, 3, tail)
     finally:
         ctx.set_tuning(**{f: getattr(saved, f) for f, _ in saved._fields_})
     assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
-    assert e == ext and sh == shadow
+    assert np.array_equal(img2.view(np.uint32), ref.view(np.uint32))
+    assert e == ext and sh == shadow and e2 == ext and sh2 == shadow
     assert ctx.status() == 0
 
 
