@@ -814,7 +814,9 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a, const __grid
 // Shape of the persistent form per COUT: rows per tile (two accumulators of
 // ROWS x COUT columns within the 512 TMEM columns) and ring stages, from
 // sweeps of the 1080p inference (ms: 2 rows at COUT 64 1.008, 4 rows
-// 0.981; 8 rows below COUT 64 no change)
+// 0.981; 8 rows below COUT 64 no change).  Five stages for the 32- and
+// 64-channel layers (one CTA per SM either way) measured slower: 0.883 ->
+// 0.934 ms, e1a / e1b / d1b 51 / 58 / 58 -> 66 / 77 / 76 us
 __host__ __device__ constexpr int ws_rows(int cout) { return cout >= 128 ? 2 : 4; }
 __host__ __device__ constexpr int ws_stages(int cout) { return cout >= 128 ? 4 : 3; }
 
@@ -828,6 +830,7 @@ cudaError_t launch_conv_ws(const ConvArgs& ca, const bf16* wt, uint32_t* status,
     constexpr int kThreads = kWsThreads;
     static uint64_t configured = 0;
     static int per_sm = 0;
+    static_assert(ws_smem_bytes<COUT, kRows, kStages, STACK>() <= 227u * 1024u, "shared memory of one CTA");
     const size_t smem = ws_smem_bytes<COUT, kRows, kStages, STACK>();
     cudaError_t e = tc_configure(k_conv_ws<COUT, kRows, kStages, STACK>, smem, configured);
     if (e != cudaSuccess) return e;
