@@ -92,50 +92,63 @@ template <int COUT, int ROWS>
 __device__ __forceinline__ void tc_epilogue(const ConvArgs& a, uint32_t taddr, int n, int y0, int x0, int warp,
                                             int lane) {
     const int m = 32 * warp + lane, x = x0 + m;
+    // per 16-channel group: its biases read once for the tile, and the
+    // accumulators of up to four rows loaded before one wait
+    constexpr int kBatch = ROWS < 4 ? ROWS : 4;
+    static_assert(ROWS % kBatch == 0, "row batches");
 #pragma unroll
-    for (int r = 0; r < ROWS; ++r) {
-        const int y = y0 + r;
-        bf16* dst = a.y + ((size_t(n) * a.h + y) * a.w_ + x) * COUT;
+    for (int jj = 0; jj < COUT / 16; ++jj) {
+        float bias[16];
 #pragma unroll
-        for (int jj = 0; jj < COUT / 16; ++jj) {
-            uint32_t v[16];
-            const uint32_t ta = taddr + (uint32_t(32 * warp) << 16) + uint32_t(r * COUT + 16 * jj);
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                "[%16];\n"
-                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                  "=r"(v[15])
-                : "r"(ta));
+        for (int k = 0; k < 16; ++k) bias[k] = a.bias[16 * jj + k];
+#pragma unroll
+        for (int r0 = 0; r0 < ROWS; r0 += kBatch) {
+            uint32_t v[kBatch][16];
+#pragma unroll
+            for (int rr = 0; rr < kBatch; ++rr) {
+                const uint32_t ta = taddr + (uint32_t(32 * warp) << 16) + uint32_t((r0 + rr) * COUT + 16 * jj);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                    "[%16];\n"
+                    : "=r"(v[rr][0]), "=r"(v[rr][1]), "=r"(v[rr][2]), "=r"(v[rr][3]), "=r"(v[rr][4]), "=r"(v[rr][5]),
+                      "=r"(v[rr][6]), "=r"(v[rr][7]), "=r"(v[rr][8]), "=r"(v[rr][9]), "=r"(v[rr][10]), "=r"(v[rr][11]),
+                      "=r"(v[rr][12]), "=r"(v[rr][13]), "=r"(v[rr][14]), "=r"(v[rr][15])
+                    : "r"(ta));
+            }
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (x < a.w_ && y < a.h) {
-                uint32_t packed[8], gv[8];
-                if (a.gate) {
-                    const uint4* gp = reinterpret_cast<const uint4*>(
-                        a.gate + ((size_t(n) * a.h + y) * a.w_ + x) * COUT + 16 * jj);
-                    const uint4 g0 = gp[0], g1 = gp[1];
-                    gv[0] = g0.x; gv[1] = g0.y; gv[2] = g0.z; gv[3] = g0.w;
-                    gv[4] = g1.x; gv[5] = g1.y; gv[6] = g1.z; gv[7] = g1.w;
-                }
 #pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    float f0 = __uint_as_float(v[2 * q]) + a.bias[16 * jj + 2 * q];
-                    float f1 = __uint_as_float(v[2 * q + 1]) + a.bias[16 * jj + 2 * q + 1];
-                    if (a.relu) {
-                        f0 = fmaxf(f0, 0.0f);
-                        f1 = fmaxf(f1, 0.0f);
-                    }
+            for (int rr = 0; rr < kBatch; ++rr) {
+                const int y = y0 + r0 + rr;
+                if (x < a.w_ && y < a.h) {
+                    bf16* dst = a.y + ((size_t(n) * a.h + y) * a.w_ + x) * COUT;
+                    uint32_t packed[8], gv[8];
                     if (a.gate) {
-                        const float2 g = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&gv[q]));
-                        if (!(g.x > 0.0f)) f0 = 0.0f;
-                        if (!(g.y > 0.0f)) f1 = 0.0f;
+                        const uint4* gp = reinterpret_cast<const uint4*>(
+                            a.gate + ((size_t(n) * a.h + y) * a.w_ + x) * COUT + 16 * jj);
+                        const uint4 g0 = gp[0], g1 = gp[1];
+                        gv[0] = g0.x; gv[1] = g0.y; gv[2] = g0.z; gv[3] = g0.w;
+                        gv[4] = g1.x; gv[5] = g1.y; gv[6] = g1.z; gv[7] = g1.w;
                     }
-                    const __nv_bfloat162 hv = __floats2bfloat162_rn(f0, f1);
-                    packed[q] = *reinterpret_cast<const uint32_t*>(&hv);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        float f0 = __uint_as_float(v[rr][2 * q]) + bias[2 * q];
+                        float f1 = __uint_as_float(v[rr][2 * q + 1]) + bias[2 * q + 1];
+                        if (a.relu) {
+                            f0 = fmaxf(f0, 0.0f);
+                            f1 = fmaxf(f1, 0.0f);
+                        }
+                        if (a.gate) {
+                            const float2 g = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&gv[q]));
+                            if (!(g.x > 0.0f)) f0 = 0.0f;
+                            if (!(g.y > 0.0f)) f1 = 0.0f;
+                        }
+                        const __nv_bfloat162 hv = __floats2bfloat162_rn(f0, f1);
+                        packed[q] = *reinterpret_cast<const uint32_t*>(&hv);
+                    }
+                    uint4* o = reinterpret_cast<uint4*>(dst + 16 * jj);
+                    o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                    o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
                 }
-                uint4* o = reinterpret_cast<uint4*>(dst + 16 * jj);
-                o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-                o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
             }
         }
     }
@@ -975,39 +988,53 @@ template <int COUT, int R>
 __device__ __forceinline__ void up_epilogue(const ConvArgs& a, uint32_t taddr, int n, int Y0, int X0, int warp,
                                             int lane) {
     const int i = 32 * warp + lane;
+    // per 16-channel group: its biases read once for the tile, and the
+    // accumulators of four blocks loaded before one wait (as tc_epilogue)
+    constexpr int kBlocks = 4 * R, kBatch = 4;
+    static_assert(kBlocks % kBatch == 0, "block batches");
 #pragma unroll
-    for (int blk = 0; blk < 4 * R; ++blk) {
-        const int px = blk / (2 * R), j = blk % (2 * R);
-        const int y = 2 * Y0 + j, x = 2 * (X0 + i) + px;
-        bf16* dst = a.y + ((size_t(n) * a.h + y) * a.w_ + x) * COUT;
+    for (int jj = 0; jj < COUT / 16; ++jj) {
+        float bias[16];
 #pragma unroll
-        for (int jj = 0; jj < COUT / 16; ++jj) {
-            uint32_t v[16];
-            const uint32_t ta = taddr + (uint32_t(32 * warp) << 16) + uint32_t(blk * COUT + 16 * jj);
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                "[%16];\n"
-                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                  "=r"(v[15])
-                : "r"(ta));
+        for (int k = 0; k < 16; ++k) bias[k] = a.bias[16 * jj + k];
+#pragma unroll
+        for (int b0 = 0; b0 < kBlocks; b0 += kBatch) {
+            uint32_t v[kBatch][16];
+#pragma unroll
+            for (int bb = 0; bb < kBatch; ++bb) {
+                const uint32_t ta = taddr + (uint32_t(32 * warp) << 16) + uint32_t((b0 + bb) * COUT + 16 * jj);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                    "[%16];\n"
+                    : "=r"(v[bb][0]), "=r"(v[bb][1]), "=r"(v[bb][2]), "=r"(v[bb][3]), "=r"(v[bb][4]), "=r"(v[bb][5]),
+                      "=r"(v[bb][6]), "=r"(v[bb][7]), "=r"(v[bb][8]), "=r"(v[bb][9]), "=r"(v[bb][10]), "=r"(v[bb][11]),
+                      "=r"(v[bb][12]), "=r"(v[bb][13]), "=r"(v[bb][14]), "=r"(v[bb][15])
+                    : "r"(ta));
+            }
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (i < kUpCols && x < a.w_ && y < a.h) {
-                uint32_t packed[8];
 #pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    float f0 = __uint_as_float(v[2 * q]) + a.bias[16 * jj + 2 * q];
-                    float f1 = __uint_as_float(v[2 * q + 1]) + a.bias[16 * jj + 2 * q + 1];
-                    if (a.relu) {
-                        f0 = fmaxf(f0, 0.0f);
-                        f1 = fmaxf(f1, 0.0f);
+            for (int bb = 0; bb < kBatch; ++bb) {
+                const int blk = b0 + bb;
+                const int px = blk / (2 * R), j = blk % (2 * R);
+                const int y = 2 * Y0 + j, x = 2 * (X0 + i) + px;
+                if (i < kUpCols && x < a.w_ && y < a.h) {
+                    bf16* dst = a.y + ((size_t(n) * a.h + y) * a.w_ + x) * COUT;
+                    uint32_t packed[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        float f0 = __uint_as_float(v[bb][2 * q]) + bias[2 * q];
+                        float f1 = __uint_as_float(v[bb][2 * q + 1]) + bias[2 * q + 1];
+                        if (a.relu) {
+                            f0 = fmaxf(f0, 0.0f);
+                            f1 = fmaxf(f1, 0.0f);
+                        }
+                        const __nv_bfloat162 hv = __floats2bfloat162_rn(f0, f1);
+                        packed[q] = *reinterpret_cast<const uint32_t*>(&hv);
                     }
-                    const __nv_bfloat162 hv = __floats2bfloat162_rn(f0, f1);
-                    packed[q] = *reinterpret_cast<const uint32_t*>(&hv);
+                    uint4* o = reinterpret_cast<uint4*>(dst + 16 * jj);
+                    o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                    o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
                 }
-                uint4* o = reinterpret_cast<uint4*>(dst + 16 * jj);
-                o[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-                o[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
             }
         }
     }
