@@ -224,7 +224,10 @@ typedef struct mrt_scene mrt_scene;
 
 /* ---- context ----------------------------------------------------------- */
 /* Replaces the Vulkan service (src/sys/vulkan.ixx:426, Vulkan_impl ctor
- * :106-115): selects `device` and creates the per-context device state. */
+ * :106-115): selects `device` and creates the per-context device state.
+ * A context (with its scenes, caches and denoisers) is used by one host
+ * thread at a time: its work buffers, second stream and fork / join events
+ * are shared by the passes it runs. */
 int         mrt_cuda_create(mrt_ctx** out, int device);
 int         mrt_cuda_destroy(mrt_ctx* ctx);
 const char* mrt_cuda_last_error(const mrt_ctx* ctx);

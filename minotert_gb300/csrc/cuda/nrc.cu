@@ -1385,7 +1385,7 @@ int cache_train_frame(mrt_ctx* ctx, mrt_cache* c, const DevScene& sc, const Fram
         c->slice_cap = steps;
     }
     const uint32_t per_max = (cap / steps) & ~15u;  // the most rows a slice can hold
-    if (per_max < 16u) return set_error(ctx, MRT_EINVAL, "cache: fewer than 16 training rows per step");
+    if (per_max < 16u) return MRT_OK;  // a step could never hold a whole 16-row tile: nothing to train
     if (cudaMemsetAsync(c->tcount, 0, 4, s) != cudaSuccess) return set_error(ctx, MRT_ECUDA, "cache: memset");
     if (launch_cache_train_paths(sc, fp, tp, c->cfg.train_bounces ? c->cfg.train_bounces : 8u, paths, c->frame++,
                                  c->sq, c->st, c->tcount, cap, status, s) != cudaSuccess)
