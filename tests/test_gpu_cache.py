@@ -120,6 +120,14 @@ def test_grid_adam_updates_only_touched_entries(ctx, tcgen05):
     moved = np.any(g1[touched] != g0[touched], axis=1)
     assert moved.mean() > 0.99
     assert not np.any(c.params(3))
+    # the first Adam step (b1 0.9, b2 0.99, bias-corrected, eps 1e-10): the
+    # corrected moments are G and G^2, so a feature moves by lr * G / (|G| +
+    # eps) = lr * sign(G); G is the two passes' sum, with grad's sign
+    lr = default_config().lr_grid
+    big = np.abs(grad) > 1e-6
+    expect = g0 - lr * np.sign(grad)
+    assert big.sum() > 100
+    assert np.max(np.abs(g1[big] - expect[big])) < 1e-6
 
 
 def test_cache_training_tcgen05_matches_mma_sync(ctx):
