@@ -511,6 +511,10 @@ def run_mine(args, world, rank, local, dist):
         for rec in subs.values():
             for k in ("metric", "n_gpus", "higher_is_better", "scaling", "vs_baseline", "dtype"):
                 rec.pop(k, None)
+        # the learned parts' per-frame cost (configs 4 and 5: their time-to-
+        # RMSE experiments are the radiance_cache and denoiser workloads)
+        subs["denoiser_inference_1080p"] = network_kernels_record(local, 20, 5)
+        subs["radiance_cache_frame_1080p"] = cache_frames_record(local, 32, 8, step_timings=False)
         out["sub_records"] = subs
     cpu_inputs = out.pop("_cpu_baseline_inputs", None)
     if cpu_inputs is not None:
@@ -1346,6 +1350,11 @@ def run_network_kernels(args, world, rank, local, dist):
     events, --steps timed runs after --warmup).  The network-kernel ncu captures profile this command."""
     from minotert_gb300 import build as _build
     _build.build()
+    print(json.dumps(network_kernels_record(local, args.steps, args.warmup)))
+
+
+def network_kernels_record(local, steps, warmup):
+    """The measurement of run_network_kernels as a dict."""
     from minotert_gb300._lib import Context
     from minotert_gb300.cache import RadianceCache, default_config
     from minotert_gb300.denoiser import Denoiser, to_bf16_bits
@@ -1368,10 +1377,10 @@ def run_network_kernels(args, world, rank, local, dist):
     a, b = ctx.event(), ctx.event()
 
     def timed(fn):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             fn()
         ts = []
-        for _ in range(args.steps):
+        for _ in range(steps):
             ctx.record(a)
             fn()
             ctx.record(b)
@@ -1391,12 +1400,12 @@ def run_network_kernels(args, world, rank, local, dist):
     cache.set_tcgen05(True)
     flop = 2 * 9 * sum((ca + cb) * co * (W * H) // (4 ** sc) for ca, cb, co, ups, relu, sc in
                        __import__("minotert_gb300.denoiser", fromlist=["TOPOLOGY"]).TOPOLOGY)
-    print(json.dumps({"metric": "network inference ms at 1920x1080", "unit": "ms", "denoiser_ms": den_ms,
-                      "denoiser_tflops": flop / den_ms / 1e9, "denoiser_gflop": flop / 1e9,
-                      "denoiser_ms_other_kernels": den_modes,
-                      "cache_ms_2073600_queries": cache_ms, "cache_mqueries_s": n / cache_ms / 1e3,
-                      "cache_ms_mma_sync": cache_mma_ms, "cache_mlp_tflops": n * 29824 / cache_ms / 1e9,
-                      "steps": args.steps, "warmup": args.warmup, "data": "random weights and inputs"}))
+    return {"metric": "network inference ms at 1920x1080", "unit": "ms", "denoiser_ms": den_ms,
+            "denoiser_tflops": flop / den_ms / 1e9, "denoiser_gflop": flop / 1e9,
+            "denoiser_ms_other_kernels": den_modes,
+            "cache_ms_2073600_queries": cache_ms, "cache_mqueries_s": n / cache_ms / 1e3,
+            "cache_ms_mma_sync": cache_mma_ms, "cache_mlp_tflops": n * 29824 / cache_ms / 1e9,
+            "steps": steps, "warmup": warmup, "data": "random weights and inputs", "device_status": ctx.status()}
 
 
 def run_denoiser_train(args, world, rank, local, dist):
@@ -1457,6 +1466,12 @@ def run_cache_frames(args, world, rank, local, dist):
     training launch list profiles this command."""
     from minotert_gb300 import build as _build
     _build.build()
+    print(json.dumps(cache_frames_record(local, args.steps, args.warmup)))
+
+
+def cache_frames_record(local, steps, warmup, step_timings=True):
+    """The measurement of run_cache_frames as a dict (step_timings: with the
+    explicit-API training-step timings)."""
     from minotert_gb300 import scene, workloads
     from minotert_gb300._lib import Context
     from minotert_gb300.cache import RadianceCache, default_config
@@ -1488,14 +1503,14 @@ def run_cache_frames(args, world, rank, local, dist):
                 cache.frame(ds, gb, camera_consts(cam, cam, pt.frame_counter),
                             TraceSettings(1, 1, 2, 1, True, f).params(base.sky), col, train=True, stream=stream)
 
-        frames(args.warmup, 0)
+        frames(warmup, 0)
         a, b = ctx.event(), ctx.event()
         ctx.record(a, stream)
-        frames(args.steps, 1000)
+        frames(steps, 1000)
         ctx.record(b, stream)
         ctx.sync(stream)
         out[("tcgen05" if tc else "mma_sync") + ("_overlap" if overlap else "_serial")] = \
-            ctx.elapsed_ms(a, b) / args.steps
+            ctx.elapsed_ms(a, b) / steps
         cache.close()
     # one training step through the explicit API on uniform random samples
     # (position, normal, direction; targets in [0.1, 1)): forward + backward
@@ -1503,7 +1518,7 @@ def run_cache_frames(args, world, rank, local, dist):
     # what a frame's step gets in this scene) and 65,536
     rng = np.random.default_rng(1)
     steps_us = {}
-    for n in (7680, 65536):
+    for n in ((7680, 65536) if step_timings else ()):
         q = np.zeros((n, 9), np.float32)
         q[:, :3] = rng.uniform(0.02, 0.98, (n, 3))
         for k in (3, 6):
@@ -1526,10 +1541,9 @@ def run_cache_frames(args, world, rank, local, dist):
                 steps_us[f"{n}_{'tcgen05' if tc else 'mma_sync'}_{'with_adam' if upd else 'fwd_bwd'}"] = \
                     1000.0 * ctx.elapsed_ms(a, b) / 50
             cache.close()
-    print(json.dumps({"metric": "learned radiance-cache frame ms (1920x1080, training included)", "unit": "ms",
-                      "value": out["tcgen05_overlap"], "higher_is_better": False, "variants_ms": out,
-                      "train_step_us": steps_us, "steps": args.steps, "warmup": args.warmup,
-                      "device_status": ctx.status()}))
+    return {"metric": "learned radiance-cache frame ms (1920x1080, training included)", "unit": "ms",
+            "value": out["tcgen05_overlap"], "higher_is_better": False, "variants_ms": out,
+            "train_step_us": steps_us or None, "steps": steps, "warmup": warmup, "device_status": ctx.status()}
 
 
 def run_post_kernels(args, world, rank, local, dist):
