@@ -179,6 +179,47 @@ def _rmse(a, b):
     return float(np.sqrt(np.mean((a - b) ** 2)))
 
 
+def test_cache_experiment_reference_converges_to_fp64(ctx, blue_noise):
+    # The radiance-cache experiment's reference (bench.py --workload
+    # radiance_cache): 4096 plain frames of the heightfield scene at
+    # 1920x1080 (8 bounces, roulette after 2) against the FP64 oracle's
+    # 4096 samples per pixel on a 16 x 32 crop: both are Monte Carlo
+    # estimates of the same pixels, so they agree to within their noise
+    from minotert_gb300 import scene, workloads
+    from minotert_gb300.pathtracer import Camera, Pathtracer, TraceSettings
+    base = workloads.heightfield_boxes_256()
+    W, H = 1920, 1080
+    c0 = base.camera
+    cam = Camera((W, H), c0.verticalFov, c0.nearPlane, c0.position, c0.yaw, c0.pitch)
+    mesh = base.mesh()
+    bvh = scene.build_bvh8(mesh)
+    ds = scene.DeviceScene.triangles(ctx, mesh, bvh)
+    ctx.blue_noise(blue_noise)
+    pt = Pathtracer(ctx, ds, full_gbuffer=False)
+    stream = ctx.stream()
+    sky = base.sky
+    col = ctx.alloc(12 * W * H)
+    for f in range(4096):
+        pt.frame_counter = (1 << 20) + f
+        gb = pt.primaryRays((W, H), cam, cam, stream)
+        pt.secondaryRays(gb, cam, sky, blue_noise, TraceSettings(1, 8, 2, 1, True, f), color=col, stream=stream)
+    ref = col.download(np.float32, (H, W, 3), stream)
+    assert ctx.status() == 0
+    import oracle as orc
+    y0, y1, x0, x1 = 600, 616, 900, 932
+    consts = orc.camera_consts(cam.position, cam.yaw, cam.pitch, cam.verticalFov, cam.nearPlane, W, H)
+    p = orc.primary(consts, W, H, bvh.nodes, bvh.tris, mesh.mats, y0=y0, y1=y1)
+    sd = np.asarray(sky.sun_dir, np.float64)
+    sd = (sd / np.linalg.norm(sd)).astype(np.float32)
+    prm = orc.params_array(4096, 8, 2, 1, 1, sun=sd, sun_e=sky.sun_irradiance, sky=sky.radiance)
+    crop64, _, _ = orc.pathtrace(bvh.nodes, bvh.tris, mesh.mats, consts, W, H, p["visibility"], p["hit_t"],
+                                 blue_noise, prm, precision=64, y0=y0, y1=y1)
+    a, b = ref[y0:y1, x0:x1], crop64[y0:y1, x0:x1]
+    rel = float(np.sqrt(np.mean((a - b) ** 2)) / max(float(b.mean()), 1e-9))
+    print(f"reference crop vs FP64: relative RMSE {rel:.4f}")
+    assert rel < 0.01
+
+
 def test_cache_frame_training_overlapped_with_tracing(ctx, hf_workload, blue_noise):
     # The same cache frames with the training on the context's second stream
     # (overlapped with the frame's ray tracing, joined before the cache is
